@@ -1,0 +1,428 @@
+/* nmo.c -- ORACLE (test infrastructure only; never part of the product path).
+ *
+ * A plain-C CPU restatement of nmesh's scalarwave1 evolution right-hand side
+ * (DG volume derivative + LLF surface flux + lift) and of its classic RK4
+ * step.  It follows the reference's operation order so that, compiled with
+ * -ffp-contract=off, it reproduces the reference's FP64 results bit for bit
+ * on the same inputs.  Only tests/, __graft_entry__.smoke() and bench.py's
+ * CPU-baseline leg load it, as the checker / the timed CPU implementation.
+ *
+ * Reference functions restated here (paths within nmeshsource/nmesh):
+ *   LGL nodes/weights    src/main/basis/Legendre.c:59-98,149-213
+ *   Lagrange weights     src/main/basis/Lagrange.c:15-27
+ *   D matrix             src/main/basis/Lagrange.c:126-147
+ *   directional matmul   src/main/amr/array.c:36-45,100-120,194-304
+ *   Cartesian partials   src/main/coordinates/derivs.c:102-181
+ *   divergence           src/main/coordinates/derivs.c:756-815
+ *   fluxes / eigenvals   src/tests/scalarwave1/scalarwave1.c:39-59,62-134
+ *   volume RHS           src/tests/scalarwave1/scalarwave1.c:242-284
+ *   face fluxes          src/tests/scalarwave1/scalarwave1.c:139-209
+ *   exact plane wave     src/tests/scalarwave1/scalarwave1.c:503-524
+ *   LLF                  src/main/dg/numflux1d.c:85-112
+ *   surface flux + lift  src/main/dg/dg.c:30-151
+ *   node normals         src/main/coordinates/utilities.c:48-88
+ *   sqrtgdiag            src/main/coordinates/coordinates.c:728-800
+ *   vladdto_onfaces      src/main/main/variables.c:1044-1066
+ *   RK4                  src/main/evolve/RungeKutta.c:19-82
+ *
+ * Extensions without a reference counterpart (restated, parity unpinned):
+ *   BC kind 1: outgoing-radiation outer boundary (characteristic upwinding
+ *              of the first-order wave system: incoming characteristic
+ *              pi + c.n set to zero in the exterior state);
+ *   periodic faces are plain face connections in the neighbour table.
+ *
+ * Data layout: state arrays are [element][field][node], node = i + n*(j + n*k),
+ * fields (pi, cx, cy, cz, phi) as in the reference's vlu (scalarwave1.c:669).
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define NF 5
+
+typedef struct nmo_mesh {
+  int nelem;
+  int n;                    /* LGL nodes per direction */
+  const double *bbox;       /* [e][6] element bbox in patch coordinates */
+  const int32_t *curvi;     /* [e] 1 if the patch map is not Cartesian */
+  const double *dXdx;       /* [e][9][np] dX^a/dx^i (a-major); may be NULL if no curvi */
+  const double *xyz;        /* [e][3][np] Cartesian coordinates */
+  const int64_t *nbnode;    /* [e][6][n*n] global index e'*np+ijk' of the
+                               coincident node across the face, -1 = outer */
+  int bc;                   /* outer faces: 0 exact plane wave, 1 outgoing */
+  double k[3];              /* plane-wave vector for bc 0 */
+} nmo_mesh;
+
+/* ------------------------------------------------------------------ */
+/* basis: LGL points, weights and differentiation matrix               */
+/* ------------------------------------------------------------------ */
+static void legendre_P_dP_Q_dQ(int l, double x, double *P, double *dP,
+                               double *Q, double *dQ)
+{
+  double P0 = 1., P1 = x, dP0 = 0., dP1 = 1., Pk = 0., dPk = 0.;
+  int k;
+  if (l == 0) { *P = 1.; *dP = 0.; return; }
+  if (l == 1) { *P = x; *dP = 1.; return; }
+  for (k = 2; k <= l + 1; k++) {
+    Pk = (P1 * x * (2 * k - 1) - P0 * (k - 1)) / k;
+    dPk = P1 * (2 * k - 1) + dP0;
+    if (k >= l + 1) break;
+    P0 = P1; P1 = Pk; dP0 = dP1; dP1 = dPk;
+  }
+  *P = P1; *dP = dP1; *Q = Pk - P0; *dQ = dPk - dP0;
+}
+
+void nmo_lgl(int npoints, double *x, double *w)
+{
+  const double PI = 3.14159265358979323846264338327950;
+  int N = npoints - 1, i, j;
+  double P, dP, Q, dQ, y, dy;
+  if (N == 0) { x[0] = 0.; w[0] = 2.; return; }
+  x[0] = -1.; x[N] = 1.;
+  w[0] = 2.0 / (N * (N + 1.0)); w[N] = w[0];
+  if (N == 1) return;
+  for (j = 1; j <= N / 2; j++) {
+    if (j == N / 2.0) {
+      y = 0.;
+    } else {
+      y = -cos(PI * (j + 0.25) / N - 3 / (8 * N * PI * (j + 0.25)));
+      for (i = 0; i < 100; i++) {
+        legendre_P_dP_Q_dQ(N, y, &P, &dP, &Q, &dQ);
+        dy = -Q / dQ;
+        y += dy;
+        if (fabs(dy) < fabs(1e-15 * y)) break;
+      }
+    }
+    x[N - j] = -y;
+    x[j] = y;
+    legendre_P_dP_Q_dQ(N, y, &P, &dP, &Q, &dQ);
+    w[j] = 2.0 / ((N * (N + 1)) * P * P);
+    w[N - j] = w[j];
+  }
+}
+
+/* D[i*n + j] = d l_j / dx (x_i) */
+void nmo_diffmat(int n, const double *x, double *D)
+{
+  double wi[64];
+  int i, j, m;
+  for (i = 0; i < n; i++) {
+    double denom = 1.;
+    for (m = 0; m < n; m++) if (m != i) denom *= (x[i] - x[m]);
+    wi[i] = 1. / denom;
+  }
+  for (i = 0; i < n; i++) {
+    double Dii = 0;
+    for (j = 0; j < n; j++) {
+      if (i != j) {
+        double Dij = (wi[j] / wi[i]) / (x[i] - x[j]);
+        Dii -= Dij;
+        D[i * n + j] = Dij;
+      }
+    }
+    D[i * n + i] = Dii;
+  }
+}
+
+/* ------------------------------------------------------------------ */
+/* RHS                                                                 */
+/* ------------------------------------------------------------------ */
+static void planewave(const double k[3], const double xyz[3], double t,
+                      double u[5])
+{
+  double om = sqrt(k[0] * k[0] + k[1] * k[1] + k[2] * k[2]);
+  double arg = k[0] * xyz[0] + k[1] * xyz[1] + k[2] * xyz[2] - om * t;
+  double s = sin(arg), c = cos(arg);
+  u[4] = s;
+  u[0] = -om * c;
+  u[1] = k[0] * c;
+  u[2] = k[1] * c;
+  u[3] = k[2] * c;
+}
+
+static void flux1d(double *f, const double norm[3], const double *u)
+{
+  f[0] = -(u[1] * norm[0] + u[2] * norm[1] + u[3] * norm[2]);
+  f[1] = -u[0] * norm[0];
+  f[2] = -u[0] * norm[1];
+  f[3] = -u[0] * norm[2];
+  f[4] = 0.;
+}
+
+/* out = D_dir applied to in along direction dir (array.c MM_SET_AB order) */
+static void deriv_dir(int n, const double *D, int dir, const double *in,
+                      double *out)
+{
+  int i, j, k, l;
+  for (k = 0; k < n; k++)
+    for (j = 0; j < n; j++)
+      for (i = 0; i < n; i++) {
+        int ii = (dir == 0) ? i : (dir == 1) ? j : k;
+        double sum = 0.0;
+        for (l = 0; l < n; l++) {
+          int idx = (dir == 0) ? l + n * (j + n * k)
+                  : (dir == 1) ? i + n * (l + n * k)
+                               : i + n * (j + n * l);
+          sum += D[ii * n + l] * in[idx];
+        }
+        out[i + n * (j + n * k)] = sum;
+      }
+}
+
+/* d/dx^m of U for all m (array_cart_partials): du[m][.] */
+static void cart_partials(const nmo_mesh *m, int e, const double *D,
+                          const double *U, double *dU, double *du)
+{
+  int n = m->n, np = n * n * n, a, mm, ind;
+  const double *bb = m->bbox + 6 * e;
+  double dXbdX[3];
+  for (a = 0; a < 3; a++) dXbdX[a] = 2. / (bb[2 * a + 1] - bb[2 * a]);
+  for (a = 0; a < 3; a++) deriv_dir(n, D, a, U, dU + a * np);
+  for (ind = 0; ind < np; ind++)
+    for (a = 0; a < 3; a++) dU[a * np + ind] *= dXbdX[a];
+  if (m->curvi[e]) {
+    const double *X = m->dXdx + (size_t)e * 9 * np;
+    for (ind = 0; ind < np; ind++) {
+      double dw[3];
+      for (mm = 0; mm < 3; mm++) {
+        dw[mm] = 0.;
+        for (a = 0; a < 3; a++) dw[mm] += X[(a * 3 + mm) * np + ind] * dU[a * np + ind];
+      }
+      for (mm = 0; mm < 3; mm++) du[mm * np + ind] = dw[mm];
+    }
+  } else {
+    memcpy(du, dU, sizeof(double) * 3 * np);
+  }
+}
+
+/* divU = d_i U^i with U^i in Ux, Uy, Uz (cart_divergence, add=0) */
+static void cart_divergence(const nmo_mesh *m, int e, const double *D,
+                            const double *Ux, const double *Uy,
+                            const double *Uz, double *divU, double *tmp)
+{
+  int np = m->n * m->n * m->n, i;
+  double *dU = tmp, *du = tmp + 3 * np;
+  cart_partials(m, e, D, Ux, dU, du);
+  for (i = 0; i < np; i++) divU[i] = du[i];
+  cart_partials(m, e, D, Uy, dU, du);
+  for (i = 0; i < np; i++) divU[i] += du[np + i];
+  cart_partials(m, e, D, Uz, dU, du);
+  for (i = 0; i < np; i++) divU[i] += du[2 * np + i];
+}
+
+/* normal of face f at node ijk (node_normal_from_idXdx_at_ijk) */
+static void node_normal(const nmo_mesh *m, int e, int f, int ijk, double nrm[3])
+{
+  int np = m->n * m->n * m->n, dir = f / 2, sig = 2 * (f % 2) - 1;
+  double smag;
+  if (m->curvi[e]) {
+    const double *X = m->dXdx + (size_t)e * 9 * np;
+    nrm[0] = X[(dir * 3 + 0) * np + ijk];
+    nrm[1] = X[(dir * 3 + 1) * np + ijk];
+    nrm[2] = X[(dir * 3 + 2) * np + ijk];
+  } else {
+    nrm[0] = nrm[1] = nrm[2] = 0.;
+    nrm[dir] = 1.;
+  }
+  smag = sig * sqrt(nrm[0] * nrm[0] + nrm[1] * nrm[1] + nrm[2] * nrm[2]);
+  if (smag == 0.0) smag = sig;
+  nrm[0] /= smag; nrm[1] /= smag; nrm[2] /= smag;
+}
+
+/* sqrt(g^{dir dir}) in Xb coords at ijk for a flat 3-metric */
+static double sqrtgdiag(const nmo_mesh *m, int e, int dir, int ijk)
+{
+  int np = m->n * m->n * m->n, l;
+  const double *bb = m->bbox + 6 * e;
+  double dXbdX = 2. / (bb[2 * dir + 1] - bb[2 * dir]);
+  double g = 0.0;
+  if (m->curvi[e]) {
+    const double *X = m->dXdx + (size_t)e * 9 * np;
+    for (l = 0; l < 3; l++) g += X[(dir * 3 + l) * np + ijk] * X[(dir * 3 + l) * np + ijk];
+  } else {
+    g = 1.0;
+  }
+  return dXbdX * sqrt(g);
+}
+
+/* RHS of one element: r[e] = RHS(w) at time t.  tmp holds 18*np doubles. */
+static void rhs_elem(const nmo_mesh *m, const double *D, const double *wq,
+                     double t, const double *w, double *r, int e, double *tmp)
+{
+  int n = m->n, np = n * n * n, i, j, k, f, l;
+  const double *we = w + (size_t)e * NF * np;
+  double *re = r + (size_t)e * NF * np;
+  const double *pi = we, *cx = we + np, *cy = we + 2 * np, *cz = we + 3 * np;
+  double *fl = tmp;            /* 3 flux arrays */
+  double *divf = tmp + 3 * np; /* 4 div arrays: pi, cx, cy, cz */
+  double *work = tmp + 7 * np; /* 6 np for cart_partials */
+  double *zero = tmp + 13 * np;
+  double *fpx = fl, *fpy = fl + np, *fpz = fl + 2 * np;
+
+  /* flux arrays f_pi^i = -c_i (scalarwave1_f_divf) */
+  for (i = 0; i < np; i++) {
+    double u[5] = {pi[i], cx[i], cy[i], cz[i], we[4 * np + i]};
+    double ff[5], no[3] = {1., 0., 0.};
+    flux1d(ff, no, u); fpx[i] = ff[0];
+    no[0] = 0; no[1] = 1.;
+    flux1d(ff, no, u); fpy[i] = ff[0];
+    no[1] = 0.; no[2] = 1.;
+    flux1d(ff, no, u); fpz[i] = ff[0];
+  }
+  cart_divergence(m, e, D, fpx, fpy, fpz, divf, work);
+  /* f_{c_j}^i = -pi delta^i_j: the off-diagonal flux arrays are (signed)
+     zeros whose derivatives are zero */
+  for (j = 0; j < 3; j++) {
+    double *fc[3];
+    for (i = 0; i < 3; i++) fc[i] = zero;
+    for (i = 0; i < np; i++) fl[i] = -pi[i] * 1.0;
+    fc[j] = fl;
+    for (i = 0; i < np; i++) zero[i] = 0.;
+    cart_divergence(m, e, D, fc[0], fc[1], fc[2], divf + (1 + j) * np, work);
+  }
+
+  /* volume RHS (scalarwave1_vol_rhs_u) */
+  for (k = 0; k < n; k++)
+    for (j = 0; j < n; j++)
+      for (i = 0; i < n; i++) {
+        int ijk = i + n * (j + n * k);
+        int onface = (i == 0 || i == n - 1 || j == 0 || j == n - 1 ||
+                      k == 0 || k == n - 1);
+        double interior = !onface;
+        re[4 * np + ijk] = pi[ijk];
+        for (l = 0; l < 4; l++) re[l * np + ijk] = -divf[l * np + ijk] * interior;
+      }
+
+  /* surface fluxes (dg_add_surface_fluxes_sign_fvflag, sign=+1, sqrtgdiag) */
+  for (f = 0; f < 6; f++) {
+    int dir = f / 2, p = (f % 2) * (n - 1), a, b;
+    double oow = 1. / wq[p];
+    for (b = 0; b < n; b++)
+      for (a = 0; a < n; a++) {
+        int ii, jj, kk, ijk, JK = a + n * b;
+        double norm[3], ui[5], ua[5], fi[5], fa[5], fnum[5];
+        double gd_ow;
+        int64_t nb = m->nbnode[((size_t)e * 6 + f) * n * n + JK];
+        if (dir == 0) { ii = p; jj = a; kk = b; }
+        else if (dir == 1) { ii = a; jj = p; kk = b; }
+        else { ii = a; jj = b; kk = p; }
+        ijk = ii + n * (jj + n * kk);
+        node_normal(m, e, f, ijk, norm);
+        for (l = 0; l < NF; l++) ui[l] = we[l * np + ijk];
+        if (nb >= 0) {
+          int64_t en = nb / np, in = nb % np;
+          for (l = 0; l < NF; l++) ua[l] = w[(size_t)en * NF * np + l * np + in];
+        } else if (m->bc == 0) {
+          const double *X = m->xyz + (size_t)e * 3 * np;
+          double xyz[3] = {X[ijk], X[np + ijk], X[2 * np + ijk]};
+          planewave(m->k, xyz, t, ua);
+        } else {
+          /* outgoing radiation: exterior state with zero incoming
+             characteristic pi + c.n, copy of the outgoing characteristic
+             pi - c.n and of the tangential c */
+          double cn = ui[1] * norm[0] + ui[2] * norm[1] + ui[3] * norm[2];
+          double wout = ui[0] - cn;
+          double pie = 0.5 * wout, cne = -0.5 * wout;
+          ua[0] = pie;
+          for (l = 0; l < 3; l++) ua[1 + l] = ui[1 + l] + (cne - cn) * norm[l];
+          ua[4] = ui[4];
+        }
+        flux1d(fi, norm, ui);
+        flux1d(fa, norm, ua);
+        /* LLF with eigenvalues (1,-1,0,0,0): amax = 1 */
+        {
+          double lam[5] = {1.0, -1.0, 0.0, 0.0, 0.0};
+          double apl = 0., ami = 0., amax;
+          for (l = 0; l < NF; l++) {
+            apl = fmax(apl, lam[l]);
+            ami = fmin(ami, lam[l]);
+          }
+          apl = fabs(apl); ami = fabs(ami);
+          amax = fmax(ami, apl);
+          for (l = 0; l < NF; l++)
+            fnum[l] = 0.5 * (fa[l] + fi[l] - amax * (ua[l] - ui[l]));
+        }
+        gd_ow = sqrtgdiag(m, e, dir, ijk) * oow;
+        for (l = 0; l < 4; l++) {
+          double F = (fnum[l] - fi[l] * 1.0) * 1.0;
+          divf[l * np + ijk] += F * gd_ow;
+        }
+      }
+  }
+
+  /* vladdto_onfaces(r, -1, divf) */
+  for (k = 0; k < n; k++)
+    for (j = 0; j < n; j++)
+      for (i = 0; i < n; i++)
+        if (i == 0 || i == n - 1 || j == 0 || j == n - 1 || k == 0 || k == n - 1) {
+          int ijk = i + n * (j + n * k);
+          for (l = 0; l < 4; l++) re[l * np + ijk] += -1. * divf[l * np + ijk];
+        }
+}
+
+static void basis(int n, double *D, double *wq)
+{
+  double x[64];
+  nmo_lgl(n, x, wq);
+  nmo_diffmat(n, x, D);
+}
+
+/* r = RHS(w, t) on all elements */
+int nmo_rhs(const nmo_mesh *m, double t, const double *w, double *r)
+{
+  int n = m->n, np = n * n * n;
+  double D[64 * 64], wq[64];
+  if (n < 2 || n > 64) return 1;
+  basis(n, D, wq);
+#pragma omp parallel
+  {
+    double *tmp = (double *)malloc(sizeof(double) * 18 * np);
+    int e;
+#pragma omp for schedule(static)
+    for (e = 0; e < m->nelem; e++) rhs_elem(m, D, wq, t, w, r, e, tmp);
+    free(tmp);
+  }
+  return 0;
+}
+
+/* one classic RK4 step in place (evolve_RK4_mesh); work holds 3 states */
+int nmo_rk4_step(const nmo_mesh *m, double t, double dt, double *u,
+                 double *work)
+{
+  size_t N = (size_t)m->nelem * NF * m->n * m->n * m->n, i;
+  double *u_p = work, *w = work + N, *r = work + 2 * N;
+  const double c[4] = {dt / 6., dt / 3., dt / 3., dt / 6.};
+  const double a[3] = {dt / 2., dt / 2., dt};
+  const double ts[4] = {t, t + 0.5 * dt, t + 0.5 * dt, t + dt};
+  int s;
+  memcpy(u_p, u, N * sizeof(double));
+  memcpy(w, u, N * sizeof(double));
+  for (s = 0; s < 4; s++) {
+    if (nmo_rhs(m, ts[s], w, r)) return 1;
+#pragma omp parallel for schedule(static)
+    for (i = 0; i < N; i++) {
+      u[i] += c[s] * r[i];
+      if (s < 3) w[i] = 1. * u_p[i] + a[s] * r[i];
+    }
+  }
+  return 0;
+}
+
+/* nsteps RK4 steps; the time of each step is accumulated in long double as
+   in evolve_mesh (src/main/main/main.c:610-626) */
+int nmo_rk4(const nmo_mesh *m, double t, double dt, int nsteps, double *u)
+{
+  size_t N = (size_t)m->nelem * NF * m->n * m->n * m->n;
+  double *work = (double *)malloc(3 * N * sizeof(double));
+  long double Te = t, te = 0.;
+  int s, rc = 0;
+  if (!work) return 2;
+  for (s = 0; s < nsteps && !rc; s++) {
+    double ts = (double)(Te + te);
+    rc = nmo_rk4_step(m, ts, dt, u, work);
+    te += dt;
+  }
+  free(work);
+  return rc;
+}

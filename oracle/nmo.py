@@ -1,0 +1,166 @@
+"""ORACLE (test infrastructure only): ctypes binding of oracle/nmo.c, the
+plain-C restatement of the reference's scalarwave1 DG right-hand side and
+RK4 step, plus the coordinate-matching face connectivity it consumes.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use
+this module; the product path never imports it.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "libnmo.so")
+
+
+def build(verbose=False):
+    """Compile oracle/nmo.c into oracle/_build/libnmo.so (gcc, OpenMP,
+    -ffp-contract=off so that x86-64 and aarch64 results agree bitwise)."""
+    os.makedirs(BUILD, exist_ok=True)
+    src = os.path.join(HERE, "nmo.c")
+    if os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(src):
+        return LIB
+    cmd = ["gcc", "-O2", "-std=gnu99", "-fopenmp", "-ffp-contract=off",
+           "-fPIC", "-shared", "-o", LIB + ".tmp", src, "-lm"]
+    if verbose:
+        print(" ".join(cmd))
+    subprocess.run(cmd, check=True)
+    os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+class _Mesh(ctypes.Structure):
+    _fields_ = [("nelem", ctypes.c_int), ("n", ctypes.c_int),
+                ("bbox", ctypes.c_void_p), ("curvi", ctypes.c_void_p),
+                ("dXdx", ctypes.c_void_p), ("xyz", ctypes.c_void_p),
+                ("nbnode", ctypes.c_void_p), ("bc", ctypes.c_int),
+                ("k", ctypes.c_double * 3)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = ctypes.CDLL(build())
+        for name in ("nmo_rhs", "nmo_rk4"):
+            getattr(_lib, name).restype = ctypes.c_int
+    return _lib
+
+
+def lgl(n):
+    """LGL nodes and weights on [-1,1] (reference Legendre.c:149)."""
+    x = np.zeros(n)
+    w = np.zeros(n)
+    lib().nmo_lgl(ctypes.c_int(n), x.ctypes.data_as(ctypes.c_void_p),
+                  w.ctypes.data_as(ctypes.c_void_p))
+    return x, w
+
+
+def diffmat(n):
+    """D[i, j] = l_j'(x_i) at the LGL nodes (reference Lagrange.c:126)."""
+    x, _ = lgl(n)
+    D = np.zeros((n, n))
+    lib().nmo_diffmat(ctypes.c_int(n), x.ctypes.data_as(ctypes.c_void_p),
+                      D.ctypes.data_as(ctypes.c_void_p))
+    return D
+
+
+def face_plane_index(n, f):
+    """Volume indices (i + n*(j + n*k)) of the face-f plane, ordered by the
+    in-plane index JK = a + n*b (reference Ind_n_norm / forplaneN)."""
+    d, p = f // 2, (f % 2) * (n - 1)
+    a, b = np.meshgrid(np.arange(n), np.arange(n), indexing="xy")
+    a = a.ravel()
+    b = b.ravel()
+    if d == 0:
+        i, j, k = np.full_like(a, p), a, b
+    elif d == 1:
+        i, j, k = a, np.full_like(a, p), b
+    else:
+        i, j, k = a, b, np.full_like(a, p)
+    return i + n * (j + n * k)
+
+
+def match_faces(xyz, n, period=None, tol=1e-9):
+    """Neighbour table for the oracle by matching face-node coordinates.
+
+    xyz: [E, 3, np].  Two element faces are neighbours when they hold the
+    same set of node positions (compared modulo `period` on every axis when
+    given, which makes a box periodic).  Returns nbnode[E, 6, n*n] with
+    e'*np + ijk' of the coincident node of the neighbour, or -1 on outer
+    faces (the reference copies coincident neighbour points,
+    src/main/amr/surface.c:799-900)."""
+    E = xyz.shape[0]
+    npt = n ** 3
+    planes = [face_plane_index(n, f) for f in range(6)]
+
+    def wrap(p):
+        q = np.array(p, dtype=float)
+        if period is not None:
+            q = np.mod(q, period)
+            q = np.where(np.abs(q - period) < 1e-7, 0.0, q)
+        return q
+
+    def pkey(q):
+        return tuple(np.round(q / tol).astype(np.int64))
+
+    faces = {}
+    for e in range(E):
+        for f in range(6):
+            P = wrap(xyz[e][:, planes[f]].T)          # [n*n, 3]
+            order = np.lexsort(P.T[::-1])
+            fkey = pkey(P[order].mean(axis=0))
+            faces.setdefault(fkey, []).append((e, f, P))
+    nb = np.full((E, 6, n * n), -1, np.int64)
+    for fkey, lst in faces.items():
+        if len(lst) == 1:
+            continue
+        if len(lst) != 2:
+            raise ValueError("non-conforming face match")
+        for (e, f, P), (e2, f2, P2) in (lst, lst[::-1]):
+            where = {pkey(q): planes[f2][i] for i, q in enumerate(P2)}
+            for jk in range(n * n):
+                nb[e, f, jk] = e2 * npt + where[pkey(P[jk])]
+    return nb
+
+
+class OracleMesh:
+    """Arrays describing a mesh for the oracle, kept alive with the struct."""
+
+    def __init__(self, bbox, curvi, dXdx, xyz, nbnode, n, bc=0,
+                 k=(1.0, 1.0, 1.0)):
+        self.n = int(n)
+        self.bbox = np.ascontiguousarray(bbox, np.float64)
+        self.curvi = np.ascontiguousarray(curvi, np.int32)
+        self.dXdx = np.ascontiguousarray(dXdx, np.float64)
+        self.xyz = np.ascontiguousarray(xyz, np.float64)
+        self.nbnode = np.ascontiguousarray(nbnode, np.int64)
+        self.nelem = self.bbox.shape[0]
+        self.s = _Mesh(self.nelem, self.n, self.bbox.ctypes.data,
+                       self.curvi.ctypes.data, self.dXdx.ctypes.data,
+                       self.xyz.ctypes.data, self.nbnode.ctypes.data, int(bc),
+                       (ctypes.c_double * 3)(*k))
+
+    def rhs(self, w, t=0.0):
+        w = np.ascontiguousarray(w, np.float64)
+        r = np.zeros_like(w)
+        rc = lib().nmo_rhs(ctypes.byref(self.s), ctypes.c_double(t),
+                           w.ctypes.data_as(ctypes.c_void_p),
+                           r.ctypes.data_as(ctypes.c_void_p))
+        if rc:
+            raise RuntimeError(f"nmo_rhs failed ({rc})")
+        return r
+
+    def rk4(self, u, dt, nsteps, t=0.0):
+        u = np.array(u, np.float64, copy=True, order="C")
+        rc = lib().nmo_rk4(ctypes.byref(self.s), ctypes.c_double(t),
+                           ctypes.c_double(dt), ctypes.c_int(nsteps),
+                           u.ctypes.data_as(ctypes.c_void_p))
+        if rc:
+            raise RuntimeError(f"nmo_rk4 failed ({rc})")
+        return u

@@ -1,0 +1,159 @@
+/* nmgdump.c -- test-side add-on module that is compiled together with the
+   unmodified reference sources (see oracle/ref/Makefile).  It only uses the
+   reference's public module interface (AddFun/AddPar/Vard/formyelms) and
+   changes no reference numerics.
+
+   It writes raw FP64 dumps that pin the oracle and the CUDA path:
+     POST_INITIALDATA: optionally scales the plane-wave data by an amplitude
+                       and adds a seeded element-local perturbation, so that
+                       face values of neighbouring elements differ;
+     PRE_EVOLVE (first call): r = RHS(u, t0) through the reference's own
+                       evolve_setrhs_mesh (src/main/evolve/evolve.c:182), then
+                       dumps geometry, u and r ("<prefix>_rhs.bin");
+     FINALIZE:         dumps u after the evolution ("<prefix>_final.bin").
+
+   Record layout (little endian, all counts int32, all reals float64):
+     header: magic 'NMGD', version 1, nelem, then per element:
+       int32 pat, int32 n[3], float64 bbox[6],
+       float64 x[np], y[np], z[np]            (Cartesian coordinates)
+       float64 dXdx[9][np]                    (dX^a/dx^i, a-major)
+       float64 sqrtgdiag[3][np]
+       float64 u[5][np]  (pi, cx, cy, cz, phi)
+       float64 r[5][np]  (only in the *_rhs.bin file)
+   where np = n0*n1*n2 and arrays are i-fastest (Ind_n). */
+
+#include "nmesh.h"
+#include "evolve.h"
+
+static int nmgdump_rhs_done = 0;
+
+/* small counter-based hash -> uniform in [-1,1) */
+static double nmgdump_hash(unsigned long long a)
+{
+  a += 0x9E3779B97F4A7C15ULL;
+  a = (a ^ (a >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  a = (a ^ (a >> 27)) * 0x94D049BB133111EBULL;
+  a = a ^ (a >> 31);
+  return (double)(a >> 11) * (2.0 / 9007199254740992.0) - 1.0;
+}
+
+static void nmgdump_vl_indices(tMesh *mesh, int iu[5])
+{
+  iu[0] = Ind("scalarwave1_pi");
+  iu[1] = Ind("scalarwave1_cx");
+  iu[2] = iu[1] + 1;
+  iu[3] = iu[1] + 2;
+  iu[4] = Ind("scalarwave1_phi");
+}
+
+int nmgdump_perturb(tMesh *mesh)
+{
+  double amp = Getd(Par("nmgdump_amp"));
+  double eps = Getd(Par("nmgdump_perturb"));
+  unsigned long long seed = (unsigned long long)Geti(Par("nmgdump_seed"));
+  int iu[5];
+  int e;
+
+  nmgdump_vl_indices(mesh, iu);
+  for(e = 0; e < mesh->nmyelm; e++)
+  {
+    tElm *elm = mesh->myelm[e];
+    int f, ijk;
+    for(f = 0; f < 5; f++)
+    {
+      double *u = Vard(elm, iu[f]);
+      for(ijk = 0; ijk < elm->np; ijk++)
+      {
+        unsigned long long key = seed * 1000003ULL
+                               + ((unsigned long long)e << 24)
+                               + ((unsigned long long)f << 20)
+                               + (unsigned long long)ijk;
+        u[ijk] = amp * u[ijk] + eps * nmgdump_hash(key);
+      }
+    }
+  }
+  return 0;
+}
+
+static void nmgdump_write(tMesh *mesh, const char *suffix, int with_r)
+{
+  char fname[4096];
+  FILE *fp;
+  int iu[5], ir[5];
+  int ix = Ind("x");
+  int idXdx = Ind("dXdx");
+  int isqg = Ind("sqrtgdiagx");
+  int hdr[3] = { 0x44474D4E, 1, (int)mesh->nmyelm };
+  int e, c;
+
+  nmgdump_vl_indices(mesh, iu);
+  ir[0] = Ind("scalarwave1_pi_r");
+  ir[1] = Ind("scalarwave1_cx_r");
+  ir[2] = ir[1] + 1;
+  ir[3] = ir[1] + 2;
+  ir[4] = Ind("scalarwave1_phi_r");
+
+  snprintf(fname, sizeof(fname), "%s_%s.bin", Gets(Par("nmgdump_prefix")),
+           suffix);
+  fp = fopen(fname, "wb");
+  if(!fp) errorexits("cannot open %s", fname);
+  fwrite(hdr, sizeof(int), 3, fp);
+  for(e = 0; e < mesh->nmyelm; e++)
+  {
+    tElm *elm = mesh->myelm[e];
+    int pat = elm->pat->p;
+    int np = elm->np;
+    fwrite(&pat, sizeof(int), 1, fp);
+    fwrite(elm->n, sizeof(int), 3, fp);
+    fwrite(elm->bbox, sizeof(double), 6, fp);
+    for(c = 0; c < 3; c++) fwrite(Vard(elm, ix + c), sizeof(double), np, fp);
+    for(c = 0; c < 9; c++) fwrite(Vard(elm, idXdx + c), sizeof(double), np, fp);
+    for(c = 0; c < 3; c++) fwrite(Vard(elm, isqg + c), sizeof(double), np, fp);
+    for(c = 0; c < 5; c++) fwrite(Vard(elm, iu[c]), sizeof(double), np, fp);
+    if(with_r)
+      for(c = 0; c < 5; c++) fwrite(Vard(elm, ir[c]), sizeof(double), np, fp);
+  }
+  fclose(fp);
+  printf("nmgdump: wrote %s (%d elements)\n", fname, (int)mesh->nmyelm);
+}
+
+/* r = RHS(u, t) once, before the first step, via the reference's own
+   evolve_setrhs_mesh with w = u */
+int nmgdump_rhs(tMesh *mesh)
+{
+  tEvoSys *evosys = mesh->evosys;
+  int i;
+
+  if(nmgdump_rhs_done) return 0;
+  nmgdump_rhs_done = 1;
+
+  evolve_init_evosys(mesh);
+  forList(evosys->u, i)
+    vlcopy(NULL, ListEntry(evosys->w, i), ListEntry(evosys->u, i));
+  evolve_setrhs_mesh(mesh, evosys->rhs, evosys->w);
+  nmgdump_write(mesh, "rhs", 1);
+  return 0;
+}
+
+int nmgdump_final(tMesh *mesh)
+{
+  nmgdump_write(mesh, "final", 0);
+  return 0;
+}
+
+int nmesh_nmgdump(tMesh *mesh)
+{
+  if(!Getv(Par("physics"), "nmgdump")) return 0;
+
+  printf("Adding nmgdump\n");
+
+  AddFun(POST_INITIALDATA, nmgdump_perturb);
+  AddFun(PRE_EVOLVE, nmgdump_rhs);
+  AddFun(FINALIZE, nmgdump_final);
+
+  AddPar("nmgdump_prefix", "nmgdump", "path prefix of the dump files");
+  AddPar("nmgdump_amp", "1", "factor applied to the initial plane wave");
+  AddPar("nmgdump_perturb", "0", "amplitude of the seeded perturbation");
+  AddPar("nmgdump_seed", "1", "seed of the perturbation");
+  return 0;
+}

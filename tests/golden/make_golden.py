@@ -1,0 +1,109 @@
+"""Generate the golden fixtures in tests/golden/ by running the reference
+itself (oracle/_ref/nmesh, built from the reference sources by
+oracle/ref/Makefile) with the dump add-on module.
+
+Run in a container where the reference sources exist:
+    make -C oracle/ref -j8 && python tests/golden/make_golden.py
+
+Each case is one reference run of scalarwave1 with LLF flux and RK4:
+the dump module perturbs the plane-wave initial data with seeded noise,
+dumps u0 and r0 = RHS(u0, 0) (reference evolve_setrhs_mesh), the run takes
+`steps` RK4 steps, and the final u is dumped.  The fixture stores the
+element descriptors (patch, n, bbox), the geometry the reference computed
+(x, dXdx, sqrtgdiag), u0, r0 and u_final, plus the case parameters.
+"""
+import json
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+from oracle.refdump import read_dump  # noqa: E402
+
+PI = 3.141592653589793
+
+# name -> (mesh parameters, n, luni, k, dt, steps, perturbation, seed)
+CASES = {
+    # one Cartesian box patch [0, 2 pi]^3 (the periodic-cube workload's
+    # geometry; the reference itself has exact plane-wave outer faces)
+    "box_l1_n5": dict(mesh="box", n=5, luni=1, k=(1.0, 1.0, 1.0),
+                      dt=0.25 * (2 * PI / 2) / 16, steps=3, eps=0.01, seed=7),
+    "box_l2_n4": dict(mesh="box", n=4, luni=2, k=(1.0, -0.5, 0.25),
+                      dt=0.01, steps=2, eps=0.05, seed=11),
+    # inner cube [-1,1]^3 plus 6 cubed-sphere patches out to r = 20
+    "cs7_l0_n9": dict(mesh="cs7", n=9, luni=0, k=(0.3, -0.2, 0.1),
+                      dt=0.002, steps=2, eps=0.01, seed=3),
+    "cs7_l1_n5": dict(mesh="cs7", n=5, luni=1, k=(0.3, -0.2, 0.1),
+                      dt=0.004, steps=2, eps=0.02, seed=5),
+    "cs7_l1_n4": dict(mesh="cs7", n=4, luni=1, k=(0.25, 0.15, -0.3),
+                      dt=0.004, steps=2, eps=0.02, seed=9),
+}
+
+
+def parfile(case, prefix):
+    c = CASES[case]
+    lines = [
+        "physics = scalarwave1 nmgdump",
+        "evolve_method = RK4",
+        f"dt = {c['dt']!r}",
+        f"iterations = {c['steps']}",
+        f"amr_luni = {c['luni']}",
+        f"amr_n0 = {c['n']}", f"amr_n1 = {c['n']}", f"amr_n2 = {c['n']}",
+        "scalarwave1_k = %r %r %r" % tuple(c["k"]),
+        "scalarwave1_numflux = LLF",
+        f"nmgdump_prefix = {prefix}",
+        "nmgdump_amp = 1.0",
+        f"nmgdump_perturb = {c['eps']!r}",
+        f"nmgdump_seed = {c['seed']}",
+        "logfile_creation = no",
+        "sysmon_hours = -1",
+    ]
+    if c["mesh"] == "box":
+        lines += ["amr_mesh_type = 1 BoxMesh",
+                  f"amr_mesh_xc = {PI!r} {PI!r} {PI!r}",
+                  f"amr_BoxMesh_dout = {PI!r}"]
+    else:
+        lines += ["amr_mesh_type = 7 CubedSpheres",
+                  "amr_CubedSphere_dc = 1", "amr_CubedSphere_r0fac = 20"]
+    return "\n".join(lines) + "\n"
+
+
+def run_case(case, exe, outdir):
+    with tempfile.TemporaryDirectory() as tmp:
+        prefix = os.path.join(tmp, "d")
+        par = os.path.join(tmp, case + ".par")
+        with open(par, "w") as fp:
+            fp.write(parfile(case, prefix))
+        env = dict(os.environ, OMP_NUM_THREADS="1")
+        res = subprocess.run([exe, par], cwd=tmp, env=env,
+                             capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError(f"{case}: reference failed\n{res.stdout[-3000:]}")
+        d0 = read_dump(prefix + "_rhs.bin", True)
+        d1 = read_dump(prefix + "_final.bin", False)
+    c = CASES[case]
+    meta = dict(case=case, **{k: v for k, v in c.items()})
+    np.savez_compressed(
+        os.path.join(outdir, case + ".npz"),
+        meta=json.dumps(meta), pat=d0["pat"], n=d0["n"], bbox=d0["bbox"],
+        x=d0["x"], dXdx=d0["dXdx"], sqrtgdiag=d0["sqrtgdiag"],
+        u0=d0["u"], r0=d0["r"], u_final=d1["u"])
+    print(f"{case}: {len(d0['pat'])} elements written")
+
+
+def main():
+    exe = os.path.join(ROOT, "oracle", "_ref", "nmesh")
+    if not os.path.exists(exe):
+        raise SystemExit("build the reference first: make -C oracle/ref")
+    cases = sys.argv[1:] or list(CASES)
+    for case in cases:
+        run_case(case, exe, HERE)
+
+
+if __name__ == "__main__":
+    main()
