@@ -1,0 +1,380 @@
+"""Benchmark of the GB300-native nmesh evolution path.
+
+Workload (the cubed-sphere configuration the headline metric is quoted on):
+scalarwave1 (first-order wave, 5 FP64 fields), 7 CubedSpheres mesh (inner
+cube [-1,1]^3 + 6 cubed-sphere patches out to r = 20), uniform level 4
+(7 x 16^3 = 28672 elements), 9 LGL nodes per direction (N = 8), 104,509,440
+DOF, seeded sum of 8 Gaussian pulses, outgoing-radiation outer boundary,
+LLF flux, classic RK4.  A bench step is one RK4 step (4 fused RHS+update
+stage kernels).  Every state buffer is 836 MB, far larger than the 129 MB
+L2, so no flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line on rank 0.  --impl reference times the CPU
+implementation of the same path on the host cores (the oracle's C
+restatement of the reference, pinned bit-exact to the reference itself).
+Under torchrun every rank runs an independent replica (the path is
+replicas-only on this pool); value = all ranks' DOF-stage updates divided by
+the max over ranks of the timed region.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "FP64 DOF-updates/s per RK stage"
+UNIT = "DOF-stage/s"
+NFIELDS = 5
+
+
+def workload_config(n, luni):
+    E = 7 * 8 ** luni
+    return {
+        "workload": (f"scalarwave1 RK4, 7 CubedSpheres (cube dc=1 + 6 cubed spheres to r=20), "
+                     f"7x{2 ** luni}^3 elements, {n} LGL nodes/dir (N={n - 1}), "
+                     f"8 seeded Gaussian pulses, outgoing-radiation outer boundary, LLF"),
+        "elements": E,
+        "nodes_per_dir": n,
+        "dof": E * n ** 3 * NFIELDS,
+        "rk_stages_per_step": 4,
+        "l2": "no flush: every state buffer (%.0f MB) exceeds the 129 MB L2"
+              % (E * n ** 3 * NFIELDS * 8 / 1e6),
+    }
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def init_dist(world, backend):
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+    dist.init_process_group(backend=backend)
+    return dist
+
+
+def max_over_ranks(dist, value, device=None):
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax = float(p[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def fp64_flops_per_stage(mesh_nelem, ncurvi, n):
+    """FP64 flops one stage kernel issues (FMA = 2), counted from the
+    kernel: Cartesian nodes 6 directional derivatives (n FMA each) + 6 ops;
+    curvilinear nodes 12 derivatives + 18 chain-rule FMA; per face node 4
+    subtractions + 10 FMA; RK update 2 FMA per DOF (stage average 1.75)."""
+    np_ = n ** 3
+    ncart = mesh_nelem - ncurvi
+    vol = ncart * np_ * (6 * n * 2 + 6 * 2 - 3) + ncurvi * np_ * (12 * n * 2 + 18 * 2)
+    surf = mesh_nelem * 6 * n * n * (4 + 10 * 2)
+    rk = mesh_nelem * np_ * NFIELDS * 1.75 * 2
+    return vol + surf + rk
+
+
+def alg_bytes_per_stage(nelem, ncurvi, n):
+    """Algorithmic HBM bytes of one stage: state streams (RK4 average of
+    16 streams / 4 stages = 4 streams x 8 B per DOF) + the chain-rule metric
+    of curvilinear elements (9 doubles per node)."""
+    np_ = n ** 3
+    return nelem * np_ * NFIELDS * 4 * 8 + ncurvi * np_ * 9 * 8
+
+
+def run_ours(args, rank, world, local):
+    import torch
+    import nmesh_gb300 as ng
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from helpers import gaussian_pulses
+
+    torch.cuda.set_device(local)
+    dist = init_dist(world, "nccl")
+    n, luni = args.n, args.luni
+    cfg = workload_config(n, luni)
+    mesh = ng.Mesh.build(ng.MESH_CUBEDSPHERES7, n=n, luni=luni, cs_dc=1.0, cs_r0fac=20.0)
+    pat, _ = mesh.elements()
+    ncurvi = int((pat > 0).sum())
+    xyz = mesh.coords()
+    u0 = gaussian_pulses(xyz, seed=1234 + rank)
+    del xyz
+    ev = ng.Evolution(mesh, ng.BC_OUTGOING)
+    ev.set_state(u0)
+    dx_min = 2.0 / 2 ** luni  # inner cube element edge
+    dt = 0.25 * dx_min / (n - 1) ** 2
+    dof = cfg["dof"]
+
+    stream = torch.cuda.ExternalStream(ev.stream)
+    # warm-up (also captures the step graphs)
+    ev.rk4_steps(0.0, dt, args.warmup)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    l0 = ev.launches
+    e0.record(stream)
+    ev.rk4_steps(args.warmup * dt, dt, args.steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    launches = ev.launches - l0
+    ms = e0.elapsed_time(e1)
+    ms_max = max_over_ranks(dist, ms, torch.device("cuda", local))
+    stages = 4 * args.steps
+    value = world * dof * stages / (ms_max / 1e3)
+
+    # end to end through the public API with host buffers: every step copies
+    # u from pinned host memory to HBM, takes the RK4 step and copies u back
+    host_u = torch.empty(ev.size, dtype=torch.float64, pin_memory=True).numpy()
+    host_u[:] = ev.get_state().ravel()
+    ev.rk4_steps_host(host_u, 0.0, dt, 1, inplace=True)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for s in range(args.steps):
+        ev.rk4_steps_host(host_u, s * dt, dt, 1, inplace=True)
+    t_e2e = time.perf_counter() - t0
+    t_e2e = max_over_ranks(dist, t_e2e, torch.device("cuda", local))
+    e2e_value = world * dof * stages / t_e2e
+
+    fp64_peak = ng.fp64_peak_gflops()
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fp:
+            peaks = json.load(fp)
+    except OSError:
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    per_launch_ms = ms / stages
+    alg_bytes = alg_bytes_per_stage(mesh.nelem, ncurvi, n)
+    flops = fp64_flops_per_stage(mesh.nelem, ncurvi, n)
+    achieved_gbs = alg_bytes / (per_launch_ms / 1e3) / 1e9
+    achieved_gflops = flops / (per_launch_ms / 1e3) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "dg_stage_kernel_n9_traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as fp:
+            traffic = json.load(fp).get("bytes_per_launch_full_size")
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(args, mesh, n, luni)
+
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded Gaussian pulses on the generated mesh)",
+            "config": dict(cfg, parallelism=f"replicas x{world}"),
+            "e2e": {"value": e2e_value, "unit": UNIT,
+                    "h2d_bytes_per_step": int(ev.size * 8),
+                    "d2h_bytes_per_step": int(ev.size * 8)},
+            "gpu_launches": int(launches),
+            "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak,
+                         "unit": "GB/s", "frac": achieved_gbs / hbm_peak,
+                         "traffic": traffic,
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
+                         "alg_bytes_per_launch": alg_bytes,
+                         "kernel": f"dg_stage_kernel<{n}>",
+                         "launch_ms": per_launch_ms},
+            "roofline_fp64": {"bound": "fp64", "achieved": achieved_gflops, "peak": fp64_peak,
+                              "unit": "GFLOP/s", "frac": achieved_gflops / fp64_peak,
+                              "flops_per_launch": flops,
+                              "peak_source": "FP64 FMA probe run live (nmg_fp64_peak)"},
+            "clocks": clk,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(out))
+    ev.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def cpu_mesh(n, luni):
+    """Oracle mesh of the workload, neighbour table from the packed mesh."""
+    import nmesh_gb300 as ng
+    from oracle import nmo
+    mesh = ng.Mesh.build(ng.MESH_CUBEDSPHERES7, n=n, luni=luni, cs_dc=1.0, cs_r0fac=20.0)
+    pat, bbox = mesh.elements()
+    xyz = mesh.coords()
+    nb, code = mesh.faces()
+    npt = n ** 3
+    planes = [nmo.face_plane_index(n, f) for f in range(6)]
+    a = np.tile(np.arange(n), n)
+    b = np.repeat(np.arange(n), n)
+    nbnode = np.full((mesh.nelem, 6, n * n), -1, np.int64)
+    for o in range(8):
+        s, fa, fb = o & 1, (o >> 1) & 1, (o >> 2) & 1
+        aa, bb = (b, a) if s else (a, b)
+        aa = n - 1 - aa if fa else aa
+        bb = n - 1 - bb if fb else bb
+        for f2 in range(6):
+            sel = (nb >= 0) & ((code & 7) == f2) & ((code >> 3) == o)
+            if not sel.any():
+                continue
+            idx2 = planes[f2][aa + n * bb]
+            es, fs = np.nonzero(sel)
+            nbnode[es, fs, :] = nb[es, fs][:, None] * npt + idx2[None, :]
+    om = nmo.OracleMesh(bbox, (pat > 0).astype(np.int32), mesh.dXdx(), xyz, nbnode, n, bc=1)
+    return mesh, om
+
+
+def cpu_baseline(args, mesh_gpu, n, luni, steps=None):
+    """Time the oracle (C restatement of the reference path, OpenMP over all
+    host cores) on a bounded sample of the workload: the same mesh family,
+    order, data and boundary at level `--cpu-luni` for `--cpu-steps` RK4
+    steps."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from helpers import gaussian_pulses
+    cl = args.cpu_luni
+    mesh, om = cpu_mesh(n, cl)
+    u = gaussian_pulses(mesh.coords(), seed=1234)
+    dt = 0.25 * (2.0 / 2 ** cl) / (n - 1) ** 2
+    nsteps = steps if steps is not None else args.cpu_steps
+    om.rk4(u, dt, 1)  # warm-up (page-in, OpenMP threads)
+    t0 = time.perf_counter()
+    om.rk4(u, dt, nsteps)
+    t = time.perf_counter() - t0
+    dof = mesh.nelem * n ** 3 * NFIELDS
+    threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count()))
+    return {"value": dof * 4 * nsteps / t, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{nsteps} RK4 steps of the same workload at level {cl} "
+                      f"({mesh.nelem} elements, {dof} DOF), {t:.2f} s"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    n, luni = args.n, args.luni
+    cfg = workload_config(n, luni)
+    mesh, om = cpu_mesh(n, args.cpu_luni)
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from helpers import gaussian_pulses
+    u = gaussian_pulses(mesh.coords(), seed=1234)
+    dt = 0.25 * (2.0 / 2 ** args.cpu_luni) / (n - 1) ** 2
+    dof = mesh.nelem * n ** 3 * NFIELDS
+    for _ in range(args.warmup):
+        u = om.rk4(u, dt, 1)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        u = om.rk4(u, dt, 1)
+    t = time.perf_counter() - t0
+    value = dof * 4 * args.steps / t
+    threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count()))
+    out = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded Gaussian pulses on the generated mesh)",
+        "config": dict(cfg, parallelism="host CPU, OpenMP"),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"each step: one RK4 step of the workload at level "
+                                   f"{args.cpu_luni} ({mesh.nelem} elements, {dof} DOF)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=9)
+    ap.add_argument("--luni", type=int, default=4)
+    ap.add_argument("--cpu-luni", type=int, default=3)
+    ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

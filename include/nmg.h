@@ -1,0 +1,152 @@
+/* nmg.h -- C ABI of the GB300-native nmesh evolution path (scalarwave1 DG
+ * right-hand side, LLF face flux + lift, RK4 stage update), FP64 throughout.
+ *
+ * The reference plugs evolution in per element (EvoFuncPtr =
+ * int (*)(tElm*, tEvoVars*), src/main/main/lists.h:20) inside OpenMP loops;
+ * a GPU needs the whole mesh at once, so this boundary is taken at the mesh
+ * level: one context owns the device mirror of every element and face of a
+ * static mesh, and each call replaces one reference call over all elements.
+ *
+ * Conventions
+ *  - All functions return 0 on success and a nonzero NMG_E* code otherwise
+ *    (the reference's bin convention: 0 = fine); nmg_last_error() then
+ *    describes the failure.  Nothing here exits or aborts.
+ *  - State arrays are FP64, element-contiguous structure of arrays
+ *    [element][field][node], node = i + n*(j + n*k) (the reference's Ind_n,
+ *    src/main/amr/nmesh_amr_loops.h:279), fields in the reference's vlu order
+ *    (pi, cx, cy, cz, phi) (src/tests/scalarwave1/scalarwave1.c:669-672).
+ *  - One CUDA stream per context; a context is not re-entrant.
+ */
+#ifndef NMG_H
+#define NMG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NMG_NFIELDS 5
+
+/* error codes */
+#define NMG_OK 0
+#define NMG_EINVAL 1   /* bad argument */
+#define NMG_ECUDA 2    /* CUDA runtime error */
+#define NMG_EMESH 3    /* mesh is not conforming / cannot be packed */
+#define NMG_ENOMEM 4   /* host or device allocation failed */
+#define NMG_EUNSUP 5   /* unsupported configuration (e.g. n out of range) */
+
+/* mesh types, as the reference's amr_mesh_type (src/main/amr/mesh.c:181) */
+#define NMG_MESH_BOX 1           /* "1 BoxMesh": one Cartesian box patch */
+#define NMG_MESH_CUBEDSPHERES7 7 /* "7 CubedSpheres": box + 6 cubed spheres */
+
+/* outer-boundary treatment */
+#define NMG_BC_EXACT_PLANEWAVE 0 /* exterior state = exact plane wave
+                                    (scalarwave1.c:182-204) */
+#define NMG_BC_OUTGOING 1        /* outgoing radiation: no incoming
+                                    characteristic (no reference counterpart) */
+
+typedef struct nmg_mesh nmg_mesh; /* host-side packed mesh */
+typedef struct nmg_ctx nmg_ctx;   /* device context; owns all device memory */
+
+/* Parameters of a generated mesh, named after the reference's parameters
+ * (src/main/amr/mesh.c:181-250,350-445,447-622). */
+typedef struct nmg_mesh_params {
+  int32_t mesh_type;  /* NMG_MESH_BOX or NMG_MESH_CUBEDSPHERES7 */
+  int32_t n;          /* LGL nodes per direction (amr_n0 = amr_n1 = amr_n2) */
+  int32_t luni;       /* uniform refinement level (amr_luni) */
+  int32_t periodic;   /* box only: opposite outer faces are neighbours */
+  double xc[3];       /* amr_mesh_xc */
+  double box_dout;    /* amr_BoxMesh_dout: half edge of the box */
+  double cs_dc;       /* amr_CubedSphere_dc: half edge of the inner cube */
+  double cs_r0fac;    /* amr_CubedSphere_r0fac: outer radius / dc */
+} nmg_mesh_params;
+
+/* A mesh given element by element, e.g. packed from the reference's tMesh
+ * by an adapter (elm->bbox, elm->n, pat->dXYZ_dxyz != NULL, the x/y/z and
+ * dXdx variables of coordinates_init_node, src/main/coordinates/
+ * coordinates.c:133-224). */
+typedef struct nmg_mesh_desc {
+  int32_t nelem;
+  int32_t n;              /* LGL nodes per direction, same in all elements */
+  const int32_t *pat;     /* [nelem] patch index (informational) */
+  const double *bbox;     /* [nelem][6] element bbox in patch coordinates */
+  const int32_t *curvi;   /* [nelem] 1 if the patch map is not Cartesian */
+  const double *xyz;      /* [nelem][3][n^3] Cartesian coordinates */
+  const double *dXdx;     /* [nelem][9][n^3] dX^a/dx^i, a-major; read for
+                             curvi elements only; may be NULL if none */
+  const int64_t *nbnode;  /* [nelem][6][n*n] global index e'*n^3+ijk' of the
+                             coincident node across each face node, -1 on
+                             outer faces; NULL: matched from coordinates */
+  double period[3];       /* >0: coordinates compared modulo period when
+                             matching (periodic box); 0 otherwise */
+} nmg_mesh_desc;
+
+/* ---- host mesh ---------------------------------------------------------- */
+int nmg_mesh_build(const nmg_mesh_params *p, nmg_mesh **out);
+int nmg_mesh_from_desc(const nmg_mesh_desc *d, nmg_mesh **out);
+int64_t nmg_mesh_nelem(const nmg_mesh *m);
+int32_t nmg_mesh_n(const nmg_mesh *m);
+/* copies out [nelem] patch indices and [nelem][6] bboxes */
+int nmg_mesh_get_elements(const nmg_mesh *m, int32_t *pat, double *bbox);
+/* copies out [nelem][3][n^3] Cartesian coordinates */
+int nmg_mesh_get_coords(const nmg_mesh *m, double *xyz);
+/* copies out [nelem][9][n^3] dX^a/dx^i (identity on Cartesian elements) */
+int nmg_mesh_get_dXdx(const nmg_mesh *m, double *dXdx);
+/* copies out the face table: [nelem][6] neighbour element (-1 outer) and
+   [nelem][6] code = neighbour face | orientation << 3 */
+int nmg_mesh_get_faces(const nmg_mesh *m, int32_t *nb, int32_t *code);
+/* LGL nodes and weights on [-1,1] and D[i*n+j] = l_j'(x_i)
+   (src/main/basis/Legendre.c:149-213, Lagrange.c:126-147) */
+int nmg_basis(int32_t n, double *x, double *w, double *D);
+void nmg_mesh_free(nmg_mesh *m);
+const char *nmg_mesh_last_error(void);
+
+/* ---- device context ----------------------------------------------------- */
+/* Uploads the mesh (metric, face factors, face table) and allocates the RK4
+ * state (u, u accumulator, two stage buffers) on the current CUDA device.
+ * bc_kind: NMG_BC_*; k: plane-wave vector for NMG_BC_EXACT_PLANEWAVE. */
+int nmg_create(const nmg_mesh *m, int32_t bc_kind, const double k[3],
+               nmg_ctx **out);
+void nmg_destroy(nmg_ctx *c);
+const char *nmg_last_error(const nmg_ctx *c);
+int64_t nmg_state_size(const nmg_ctx *c); /* doubles per state */
+
+/* u <-> host ([element][field][node] FP64); a copy to/from HBM */
+int nmg_set_state(nmg_ctx *c, const double *host_u);
+int nmg_get_state(nmg_ctx *c, double *host_u);
+/* device pointer of the resident state u (for zero-copy use) */
+double *nmg_state_device_ptr(nmg_ctx *c);
+
+/* r = RHS(w, t) with w, r device pointers of nmg_state_size() doubles.
+ * Replaces evolve_setrhs_mesh (src/main/evolve/evolve.c:182-232) for the
+ * scalarwave1 VOLRHS+SURFRHS bins. */
+int nmg_rhs(nmg_ctx *c, double t, const double *w_dev, double *r_dev);
+/* same with host buffers: copies w in, computes, copies r out */
+int nmg_rhs_host(nmg_ctx *c, double t, const double *w_host, double *r_host);
+
+/* One classic RK4 step of the resident state u from t to t+dt
+ * (evolve_RK4_mesh, src/main/evolve/RungeKutta.c:19-82). */
+int nmg_rk4_step(nmg_ctx *c, double t, double dt);
+/* nsteps RK4 steps; step s starts at the time accumulated as the reference's
+ * evolve_mesh does (src/main/main/main.c:610-626).  The 4*nsteps stage
+ * launches are captured once into a CUDA graph and replayed. */
+int nmg_rk4_steps(nmg_ctx *c, double t, double dt, int32_t nsteps);
+/* host round trip: set u from host, nsteps RK4 steps, copy u back */
+int nmg_rk4_steps_host(nmg_ctx *c, double t, double dt, int32_t nsteps,
+                       double *host_u);
+
+/* ---- measurement helpers ------------------------------------------------ */
+/* kernels launched by this context so far */
+int64_t nmg_kernel_launches(const nmg_ctx *c);
+/* the CUDA stream of the context (cudaStream_t) */
+void *nmg_stream(nmg_ctx *c);
+/* measured FP64 FMA throughput of the current device in GFLOP/s (the roof
+   of this FP64 path on GB300); runs a ~10 ms probe kernel */
+int nmg_fp64_peak(double *gflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NMG_H */

@@ -1,0 +1,282 @@
+"""nmesh_gb300 -- GB300-native nmesh evolution path (scalarwave1 DG RHS,
+LLF face flux + lift, RK4), FP64, behind the C ABI of include/nmg.h.
+
+This module is a thin ctypes binding of nmesh_gb300/_build/libnmg.so.  It
+mirrors the reference's interface for the path: a mesh is made from the
+reference's amr_* parameters (src/main/amr/mesh.c:181), `rhs` replaces
+evolve_setrhs_mesh (src/main/evolve/evolve.c:182) and `rk4_step(s)` replace
+evolve_RK4_mesh (src/main/evolve/RungeKutta.c:19).  There is no CPU
+fallback: every call goes to the CUDA library and raises if it is missing
+or fails.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+NFIELDS = 5
+FIELDS = ("pi", "cx", "cy", "cz", "phi")
+MESH_BOX = 1
+MESH_CUBEDSPHERES7 = 7
+BC_EXACT_PLANEWAVE = 0
+BC_OUTGOING = 1
+
+_c_dp = ctypes.POINTER(ctypes.c_double)
+_lib = None
+
+
+class NmgError(RuntimeError):
+    pass
+
+
+class _MeshParams(ctypes.Structure):
+    _fields_ = [("mesh_type", ctypes.c_int32), ("n", ctypes.c_int32),
+                ("luni", ctypes.c_int32), ("periodic", ctypes.c_int32),
+                ("xc", ctypes.c_double * 3), ("box_dout", ctypes.c_double),
+                ("cs_dc", ctypes.c_double), ("cs_r0fac", ctypes.c_double)]
+
+
+class _MeshDesc(ctypes.Structure):
+    _fields_ = [("nelem", ctypes.c_int32), ("n", ctypes.c_int32),
+                ("pat", ctypes.c_void_p), ("bbox", ctypes.c_void_p),
+                ("curvi", ctypes.c_void_p), ("xyz", ctypes.c_void_p),
+                ("dXdx", ctypes.c_void_p), ("nbnode", ctypes.c_void_p),
+                ("period", ctypes.c_double * 3)]
+
+
+def library_path():
+    return _build.LIB
+
+
+def lib(build_if_missing=True):
+    """Load libnmg.so (building it first if it is missing or stale)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.build() if build_if_missing else _build.LIB
+    if not os.path.exists(path):
+        raise NmgError(f"native library missing: {path}")
+    L = ctypes.CDLL(path)
+    vp, i32, i64, f64 = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_double
+    sig = {
+        "nmg_mesh_build": (ctypes.c_int, [vp, vp]),
+        "nmg_mesh_from_desc": (ctypes.c_int, [vp, vp]),
+        "nmg_mesh_nelem": (i64, [vp]),
+        "nmg_mesh_n": (i32, [vp]),
+        "nmg_mesh_get_elements": (ctypes.c_int, [vp, vp, vp]),
+        "nmg_mesh_get_coords": (ctypes.c_int, [vp, vp]),
+        "nmg_mesh_get_dXdx": (ctypes.c_int, [vp, vp]),
+        "nmg_mesh_get_faces": (ctypes.c_int, [vp, vp, vp]),
+        "nmg_basis": (ctypes.c_int, [i32, vp, vp, vp]),
+        "nmg_mesh_free": (None, [vp]),
+        "nmg_mesh_last_error": (ctypes.c_char_p, []),
+        "nmg_create": (ctypes.c_int, [vp, i32, vp, vp]),
+        "nmg_destroy": (None, [vp]),
+        "nmg_last_error": (ctypes.c_char_p, [vp]),
+        "nmg_state_size": (i64, [vp]),
+        "nmg_set_state": (ctypes.c_int, [vp, vp]),
+        "nmg_get_state": (ctypes.c_int, [vp, vp]),
+        "nmg_state_device_ptr": (vp, [vp]),
+        "nmg_rhs": (ctypes.c_int, [vp, f64, vp, vp]),
+        "nmg_rhs_host": (ctypes.c_int, [vp, f64, vp, vp]),
+        "nmg_rk4_step": (ctypes.c_int, [vp, f64, f64]),
+        "nmg_rk4_steps": (ctypes.c_int, [vp, f64, f64, i32]),
+        "nmg_rk4_steps_host": (ctypes.c_int, [vp, f64, f64, i32, vp]),
+        "nmg_kernel_launches": (i64, [vp]),
+        "nmg_stream": (vp, [vp]),
+        "nmg_fp64_peak": (ctypes.c_int, [vp]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def fp64_peak_gflops():
+    """Measured FP64 FMA throughput of the current GPU (GFLOP/s)."""
+    v = ctypes.c_double(0.0)
+    if lib().nmg_fp64_peak(ctypes.byref(v)):
+        raise NmgError("nmg_fp64_peak failed")
+    return v.value
+
+
+def basis(n):
+    """LGL nodes x, weights w and D[i, j] = l_j'(x_i) (Legendre.c/Lagrange.c)."""
+    x, w, D = np.zeros(n), np.zeros(n), np.zeros((n, n))
+    if lib().nmg_basis(n, _ptr(x), _ptr(w), _ptr(D)):
+        raise NmgError(lib().nmg_mesh_last_error().decode())
+    return x, w, D
+
+
+class Mesh:
+    """Host-side packed mesh (geometry, metric, face table)."""
+
+    def __init__(self, handle):
+        self._h = ctypes.c_void_p(handle)
+        self.nelem = int(lib().nmg_mesh_nelem(self._h))
+        self.n = int(lib().nmg_mesh_n(self._h))
+        self.np = self.n ** 3
+
+    @classmethod
+    def build(cls, mesh_type=MESH_BOX, n=5, luni=0, xc=(0.0, 0.0, 0.0),
+              box_dout=1.0, cs_dc=1.0, cs_r0fac=20.0, periodic=False):
+        """Mesh from the reference's parameters: amr_mesh_type (1 BoxMesh /
+        7 CubedSpheres), amr_n0..2 = n, amr_luni, amr_mesh_xc,
+        amr_BoxMesh_dout, amr_CubedSphere_dc, amr_CubedSphere_r0fac."""
+        p = _MeshParams(int(mesh_type), int(n), int(luni), int(bool(periodic)),
+                        (ctypes.c_double * 3)(*xc), float(box_dout),
+                        float(cs_dc), float(cs_r0fac))
+        h = ctypes.c_void_p()
+        rc = lib().nmg_mesh_build(ctypes.byref(p), ctypes.byref(h))
+        if rc:
+            raise NmgError(f"nmg_mesh_build: {lib().nmg_mesh_last_error().decode()}")
+        return cls(h.value)
+
+    @classmethod
+    def from_arrays(cls, bbox, curvi, xyz, dXdx=None, nbnode=None, pat=None,
+                    period=(0.0, 0.0, 0.0)):
+        """Mesh from per-element arrays (what an nmesh adapter packs)."""
+        bbox = np.ascontiguousarray(bbox, np.float64)
+        E = bbox.shape[0]
+        xyz = np.ascontiguousarray(xyz, np.float64)
+        n = int(round(xyz.shape[-1] ** (1.0 / 3.0)))
+        keep = [bbox, np.ascontiguousarray(curvi, np.int32), xyz]
+        dX = None if dXdx is None else np.ascontiguousarray(dXdx, np.float64)
+        nb = None if nbnode is None else np.ascontiguousarray(nbnode, np.int64)
+        pt = None if pat is None else np.ascontiguousarray(pat, np.int32)
+        d = _MeshDesc(E, n, None if pt is None else pt.ctypes.data, bbox.ctypes.data,
+                      keep[1].ctypes.data, xyz.ctypes.data,
+                      None if dX is None else dX.ctypes.data,
+                      None if nb is None else nb.ctypes.data,
+                      (ctypes.c_double * 3)(*period))
+        h = ctypes.c_void_p()
+        rc = lib().nmg_mesh_from_desc(ctypes.byref(d), ctypes.byref(h))
+        if rc:
+            raise NmgError(f"nmg_mesh_from_desc: {lib().nmg_mesh_last_error().decode()}")
+        return cls(h.value)
+
+    def elements(self):
+        pat = np.zeros(self.nelem, np.int32)
+        bbox = np.zeros((self.nelem, 6))
+        lib().nmg_mesh_get_elements(self._h, _ptr(pat), _ptr(bbox))
+        return pat, bbox
+
+    def coords(self):
+        x = np.zeros((self.nelem, 3, self.np))
+        lib().nmg_mesh_get_coords(self._h, _ptr(x))
+        return x
+
+    def dXdx(self):
+        x = np.zeros((self.nelem, 9, self.np))
+        lib().nmg_mesh_get_dXdx(self._h, _ptr(x))
+        return x
+
+    def faces(self):
+        nb = np.zeros((self.nelem, 6), np.int32)
+        code = np.zeros((self.nelem, 6), np.int32)
+        lib().nmg_mesh_get_faces(self._h, _ptr(nb), _ptr(code))
+        return nb, code
+
+    def close(self):
+        if self._h:
+            lib().nmg_mesh_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Evolution:
+    """Device context: mesh data and RK4 state resident in HBM."""
+
+    def __init__(self, mesh, bc=BC_EXACT_PLANEWAVE, k=(1.0, 1.0, 1.0)):
+        self.mesh = mesh
+        kk = np.ascontiguousarray(k, np.float64)
+        h = ctypes.c_void_p()
+        rc = lib().nmg_create(mesh._h, int(bc), _ptr(kk), ctypes.byref(h))
+        self._h = h
+        if rc:
+            msg = lib().nmg_last_error(h).decode() if h.value else ""
+            self.close()
+            raise NmgError(f"nmg_create failed ({rc}): {msg}")
+        self.size = int(lib().nmg_state_size(self._h))
+        self.shape = (mesh.nelem, NFIELDS, mesh.np)
+
+    def _check(self, rc, what):
+        if rc:
+            raise NmgError(f"{what} failed ({rc}): {lib().nmg_last_error(self._h).decode()}")
+
+    def set_state(self, u):
+        u = np.ascontiguousarray(u, np.float64)
+        assert u.size == self.size
+        self._check(lib().nmg_set_state(self._h, _ptr(u)), "nmg_set_state")
+
+    def get_state(self):
+        u = np.zeros(self.shape)
+        self._check(lib().nmg_get_state(self._h, _ptr(u)), "nmg_get_state")
+        return u
+
+    def rhs(self, w, t=0.0):
+        """r = RHS(w, t) for a host array w (copied to HBM and back)."""
+        w = np.ascontiguousarray(w, np.float64)
+        assert w.size == self.size
+        r = np.zeros(self.shape)
+        self._check(lib().nmg_rhs_host(self._h, float(t), _ptr(w), _ptr(r)), "nmg_rhs_host")
+        return r
+
+    def rhs_device(self, w_ptr, r_ptr, t=0.0):
+        """r = RHS(w, t) on device pointers (ints), on the context stream."""
+        self._check(lib().nmg_rhs(self._h, float(t), ctypes.c_void_p(w_ptr),
+                                  ctypes.c_void_p(r_ptr)), "nmg_rhs")
+
+    def rk4_step(self, t, dt):
+        self._check(lib().nmg_rk4_step(self._h, float(t), float(dt)), "nmg_rk4_step")
+
+    def rk4_steps(self, t, dt, nsteps):
+        self._check(lib().nmg_rk4_steps(self._h, float(t), float(dt), int(nsteps)),
+                    "nmg_rk4_steps")
+
+    def rk4_steps_host(self, u, t, dt, nsteps, inplace=False):
+        """nsteps RK4 steps of host state u (copied to HBM and back); with
+        inplace=True u (C-contiguous float64, e.g. pinned) is updated."""
+        if not (inplace and isinstance(u, np.ndarray) and u.dtype == np.float64
+                and u.flags.c_contiguous):
+            u = np.array(u, np.float64, copy=True, order="C")
+        assert u.size == self.size
+        self._check(lib().nmg_rk4_steps_host(self._h, float(t), float(dt), int(nsteps),
+                                             _ptr(u)), "nmg_rk4_steps_host")
+        return u
+
+    @property
+    def launches(self):
+        return int(lib().nmg_kernel_launches(self._h))
+
+    @property
+    def stream(self):
+        return int(lib().nmg_stream(self._h) or 0)
+
+    @property
+    def state_ptr(self):
+        return int(lib().nmg_state_device_ptr(self._h) or 0)
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            lib().nmg_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,609 @@
+// mesh.cpp -- host-side mesh packer.
+//
+// Produces the static element/face description that the device context
+// uploads: element geometry and metric (a restatement of the reference's
+// setup-time coordinate code), and a face table (neighbour element,
+// neighbour face, dihedral orientation of the in-plane node order) found by
+// matching face-node coordinates.  Runs once per mesh; compiled with
+// -ffp-contract=off so that the geometry is bitwise the same on x86-64 and
+// aarch64 hosts.
+//
+// Reference code restated here (paths within nmeshsource/nmesh):
+//   LGL nodes/weights     src/main/basis/Legendre.c:59-98,149-213
+//   D matrix              src/main/basis/Lagrange.c:15-27,126-147
+//   box patch             src/main/coordinates/setup_Boxes.c:6-25
+//   7 CubedSpheres        src/main/amr/mesh.c:536-540 ->
+//                         src/main/coordinates/setup_CubedSpheres.c:193-218,
+//                         653-681,829-880,935-944
+//   uniform refinement    src/main/amr/connections.c:1175-1205 (bbox halving)
+//   X of Xb               src/main/coordinates/get_coords.c:384-394
+//   cubed-sphere map and  src/main/coordinates/coordtrans_CubedSphere.c:37-118,
+//   its derivatives         257-509 (outerCubedSphere, constant sigma)
+//   node coordinates      src/main/coordinates/coordinates.c:133-224
+#include "mesh.h"
+#include "../../include/nmg.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <unordered_map>
+
+namespace {
+thread_local std::string g_mesh_err;
+
+int fail(int code, const std::string &msg) {
+  g_mesh_err = msg;
+  return code;
+}
+
+void legendre_P_dP_Q_dQ(int l, double x, double *P, double *dP, double *Q,
+                        double *dQ) {
+  double P0 = 1., P1 = x, dP0 = 0., dP1 = 1., Pk = 0., dPk = 0.;
+  if (l == 0) { *P = 1.; *dP = 0.; return; }
+  if (l == 1) { *P = x; *dP = 1.; return; }
+  for (int k = 2; k <= l + 1; k++) {
+    Pk = (P1 * x * (2 * k - 1) - P0 * (k - 1)) / k;
+    dPk = P1 * (2 * k - 1) + dP0;
+    if (k >= l + 1) break;
+    P0 = P1; P1 = Pk; dP0 = dP1; dP1 = dPk;
+  }
+  *P = P1; *dP = dP1; *Q = Pk - P0; *dQ = dPk - dP0;
+}
+
+// one patch of the mesh
+struct Patch {
+  double bbox[6];
+  bool cubed = false;  // outer cubed-sphere patch (else Cartesian box)
+  int dom = 0;         // cubed-sphere domain 0..5
+  double xc[3] = {0, 0, 0};
+  double s0 = 0, s1 = 0;  // inner flat distance and outer sphere radius
+};
+
+// x and dX/dx of an outerCubedSphere patch with constant sigma1 = s1
+// (xyz_of_lamAB_CubSph / dlamAB_dxyz_CubSph), same operation order
+void cubsph_x_dXdx(const Patch &P, const double X[3], double x[3],
+                   double dXdx[3][3]) {
+  double lam = X[0], A = X[1], B = X[2];
+  int dir = P.dom / 2;
+  double pm = 2 * (P.dom % 2) - 1;
+  double xc = P.xc[0], yc = P.xc[1], zc = P.xc[2];
+  double sqrt_1_A2_B2 = sqrt(1.0 + A * A + B * B);
+  double a0 = pm * P.s0;
+  double sigma1 = P.s1;
+  double dsig1[2] = {0., 0.};
+  double dsigma_dA_osigma1 = dsig1[0] / sigma1;
+  double dsigma_dB_osigma1 = dsig1[1] / sigma1;
+  double a1 = pm * sigma1 / sqrt_1_A2_B2;
+  double da0_dx = 0.0, da0_dy = 0.0, da0_dz = 0.0;
+  double da1_dx = a1, da1_dy = a1, da1_dz = a1;
+  double dsigma_dA_osigma0 = 0.0, dsigma_dB_osigma0 = 0.0;
+  double rx, ry, rz, rx2, ry2, rz2, rc2, mx, my, mz, mx0, my0, mz0, mx1, my1,
+      mz1;
+  double *dlamdx = &dXdx[0][0], *dlamdy = &dXdx[0][1], *dlamdz = &dXdx[0][2];
+  double *dAdx = &dXdx[1][0], *dAdy = &dXdx[1][1], *dAdz = &dXdx[1][2];
+  double *dBdx = &dXdx[2][0], *dBdy = &dXdx[2][1], *dBdz = &dXdx[2][2];
+  if (dir == 0) {
+    rx = (a1 - a0) * lam + a0;
+    x[0] = xc + rx; x[1] = yc + A * rx; x[2] = zc + B * rx;
+    ry = x[1] - yc; rz = x[2] - zc;
+    rx2 = rx * rx; ry2 = ry * ry; rz2 = rz * rz;
+    rc2 = rx2 + ry2 + rz2;
+    mx = (1.0 / rx - rx / rc2); my = (-ry / rc2); mz = (-rz / rc2);
+    mx0 = -dsigma_dA_osigma0 * (ry / rx2) - dsigma_dB_osigma0 * (rz / rx2);
+    my0 = dsigma_dA_osigma0 / rx;
+    mz0 = dsigma_dB_osigma0 / rx;
+    mx1 = -dsigma_dA_osigma1 * (ry / rx2) - dsigma_dB_osigma1 * (rz / rx2);
+    my1 = dsigma_dA_osigma1 / rx;
+    mz1 = dsigma_dB_osigma1 / rx;
+    da0_dx *= (mx + mx0); da0_dy *= (my + my0); da0_dz *= (mz + mz0);
+    da1_dx *= (mx + mx1); da1_dy *= (my + my1); da1_dz *= (mz + mz1);
+    *dlamdx = (1.0 - da0_dx - (da1_dx - da0_dx) * lam) / (a1 - a0);
+    *dlamdy = (-da0_dy - (da1_dy - da0_dy) * lam) / (a1 - a0);
+    *dlamdz = (-da0_dz - (da1_dz - da0_dz) * lam) / (a1 - a0);
+    *dAdx = -ry / rx2; *dAdy = 1.0 / rx; *dAdz = 0.0;
+    *dBdx = -rz / rx2; *dBdy = 0.0; *dBdz = *dAdy;
+  } else if (dir == 1) {
+    ry = (a1 - a0) * lam + a0;
+    x[1] = yc + ry; x[0] = xc + A * ry; x[2] = zc + B * ry;
+    rx = x[0] - xc; rz = x[2] - zc;
+    rx2 = rx * rx; ry2 = ry * ry; rz2 = rz * rz;
+    rc2 = rx2 + ry2 + rz2;
+    mx = (-rx / rc2); my = (1.0 / ry - ry / rc2); mz = (-rz / rc2);
+    mx0 = dsigma_dA_osigma0 / ry;
+    my0 = -dsigma_dA_osigma0 * (rx / ry2) - dsigma_dB_osigma0 * (rz / ry2);
+    mz0 = dsigma_dB_osigma0 / ry;
+    mx1 = dsigma_dA_osigma1 / ry;
+    my1 = -dsigma_dA_osigma1 * (rx / ry2) - dsigma_dB_osigma1 * (rz / ry2);
+    mz1 = dsigma_dB_osigma1 / ry;
+    da0_dx *= (mx + mx0); da0_dy *= (my + my0); da0_dz *= (mz + mz0);
+    da1_dx *= (mx + mx1); da1_dy *= (my + my1); da1_dz *= (mz + mz1);
+    *dlamdx = (-da0_dx - (da1_dx - da0_dx) * lam) / (a1 - a0);
+    *dlamdy = (1.0 - da0_dy - (da1_dy - da0_dy) * lam) / (a1 - a0);
+    *dlamdz = (-da0_dz - (da1_dz - da0_dz) * lam) / (a1 - a0);
+    *dAdx = 1.0 / ry; *dAdy = -rx / ry2; *dAdz = 0.0;
+    *dBdx = 0.0; *dBdy = -rz / ry2; *dBdz = *dAdx;
+  } else {
+    rz = (a1 - a0) * lam + a0;
+    x[2] = zc + rz; x[1] = yc + A * rz; x[0] = xc + B * rz;
+    rx = x[0] - xc; ry = x[1] - yc;
+    rx2 = rx * rx; ry2 = ry * ry; rz2 = rz * rz;
+    rc2 = rx2 + ry2 + rz2;
+    mx = (-rx / rc2); my = (-ry / rc2); mz = (1.0 / rz - rz / rc2);
+    mx0 = dsigma_dB_osigma0 / rz;
+    my0 = dsigma_dA_osigma0 / rz;
+    mz0 = -dsigma_dA_osigma0 * (ry / rz2) - dsigma_dB_osigma0 * (rx / rz2);
+    mx1 = dsigma_dB_osigma1 / rz;
+    my1 = dsigma_dA_osigma1 / rz;
+    mz1 = -dsigma_dA_osigma1 * (ry / rz2) - dsigma_dB_osigma1 * (rx / rz2);
+    da0_dx *= (mx + mx0); da0_dy *= (my + my0); da0_dz *= (mz + mz0);
+    da1_dx *= (mx + mx1); da1_dy *= (my + my1); da1_dz *= (mz + mz1);
+    *dlamdx = (-da0_dx - (da1_dx - da0_dx) * lam) / (a1 - a0);
+    *dlamdy = (-da0_dy - (da1_dy - da0_dy) * lam) / (a1 - a0);
+    *dlamdz = (1.0 - da0_dz - (da1_dz - da0_dz) * lam) / (a1 - a0);
+    *dAdx = 0.0; *dAdy = 1.0 / rz; *dAdz = -ry / rz2;
+    *dBdx = *dAdy; *dBdy = 0.0; *dBdz = -rx / rz2;
+  }
+}
+
+// A, B ranges of cubed-sphere domain dom from the inner distances Din
+// (set_AB_min_max_from_Din)
+void ab_range(int dom, const double Din[6], double r[4]) {
+  static const int ia[6][4] = {{3, 2, 5, 4}, {2, 3, 4, 5}, {1, 0, 5, 4},
+                               {0, 1, 4, 5}, {3, 2, 1, 0}, {2, 3, 0, 1}};
+  r[0] = -Din[ia[dom][0]] / Din[dom];
+  r[1] = Din[ia[dom][1]] / Din[dom];
+  r[2] = -Din[ia[dom][2]] / Din[dom];
+  r[3] = Din[ia[dom][3]] / Din[dom];
+}
+
+// element bbox at level L and integer location (ix,iy,iz) by successive
+// halving of the patch bbox (amr_set_elm0_bbox)
+void elem_bbox(const double pb[6], int L, const int ixyz[3], double bb[6]) {
+  double LX[3];
+  for (int f = 0; f < 6; f++) bb[f] = pb[f];
+  for (int d = 0; d < 3; d++) LX[d] = bb[2 * d + 1] - bb[2 * d];
+  for (int ll = 1; ll <= L; ll++) {
+    for (int d = 0; d < 3; d++) {
+      int bit = (ixyz[d] >> (L - ll)) & 1;
+      LX[d] /= 2.;
+      if (bit) bb[2 * d] = bb[2 * d + 1] - LX[d];
+      else bb[2 * d + 1] = bb[2 * d] + LX[d];
+    }
+  }
+}
+
+// fill geometry for all elements of the given patches, uniform level L,
+// elements of a patch in Morton (Z) order
+void fill_geometry(nmg_mesh &m, const std::vector<Patch> &pats, int L) {
+  const int n = m.n, np = n * n * n;
+  const int ne1 = 1 << L;
+  const int64_t per = (int64_t)ne1 * ne1 * ne1;
+  m.nelem = per * (int64_t)pats.size();
+  m.pat.resize(m.nelem);
+  m.bbox.resize(m.nelem * 6);
+  m.curvi.resize(m.nelem);
+  m.xyz.resize(m.nelem * 3 * np);
+  m.dXdx.resize(m.nelem * 9 * np);
+  int64_t e = 0;
+  for (size_t p = 0; p < pats.size(); p++) {
+    for (int64_t mc = 0; mc < per; mc++, e++) {
+      int ixyz[3] = {0, 0, 0};
+      for (int bit = 0; bit < L; bit++)
+        for (int d = 0; d < 3; d++) ixyz[d] |= (int)((mc >> (3 * bit + d)) & 1) << bit;
+      double *bb = &m.bbox[e * 6];
+      elem_bbox(pats[p].bbox, L, ixyz, bb);
+      m.pat[e] = (int32_t)p;
+      m.curvi[e] = pats[p].cubed ? 1 : 0;
+      double *X3 = &m.xyz[e * 3 * np];
+      double *M9 = &m.dXdx[e * 9 * np];
+      for (int k = 0; k < n; k++)
+        for (int j = 0; j < n; j++)
+          for (int i = 0; i < n; i++) {
+            int ijk = i + n * (j + n * k);
+            double Xb[3] = {m.x[i], m.x[j], m.x[k]}, X[3], x[3], J[3][3];
+            for (int d = 0; d < 3; d++)
+              X[d] = 0.5 * ((bb[2 * d + 1] - bb[2 * d]) * Xb[d] + (bb[2 * d + 1] + bb[2 * d]));
+            if (pats[p].cubed) {
+              cubsph_x_dXdx(pats[p], X, x, J);
+            } else {
+              for (int d = 0; d < 3; d++) {
+                x[d] = X[d];
+                for (int c = 0; c < 3; c++) J[d][c] = (d == c) ? 1. : 0.;
+              }
+            }
+            for (int d = 0; d < 3; d++) X3[d * np + ijk] = x[d];
+            for (int a = 0; a < 3; a++)
+              for (int c = 0; c < 3; c++) M9[(a * 3 + c) * np + ijk] = J[a][c];
+          }
+    }
+  }
+}
+
+// quantised coordinates for the spatial hash of face centres
+struct Key {
+  int64_t q[3];
+  bool operator==(const Key &o) const {
+    return q[0] == o.q[0] && q[1] == o.q[1] && q[2] == o.q[2];
+  }
+};
+struct KeyHash {
+  size_t operator()(const Key &k) const {
+    uint64_t h = 1469598103934665603ULL;
+    for (int d = 0; d < 3; d++) {
+      h ^= (uint64_t)k.q[d] + 0x9e3779b97f4a7c15ULL + (h << 6) + (h >> 2);
+    }
+    return (size_t)h;
+  }
+};
+
+double wrap1(double v, double period) {
+  if (period <= 0) return v;
+  double r = std::fmod(v, period);
+  if (r < 0) r += period;
+  if (std::fabs(r - period) < 1e-9 * period) r = 0.;
+  return r;
+}
+
+}  // namespace
+
+namespace nmg {
+
+void lgl_basis(int n, double *x, double *w, double *D) {
+  const double PI = 3.14159265358979323846264338327950;
+  int N = n - 1;
+  double P, dP, Q, dQ, y, dy;
+  if (N == 0) {
+    x[0] = 0.; w[0] = 2.;
+  } else {
+    x[0] = -1.; x[N] = 1.;
+    w[0] = 2.0 / (N * (N + 1.0)); w[N] = w[0];
+    for (int j = 1; j <= N / 2; j++) {
+      if (j == N / 2.0) {
+        y = 0.;
+      } else {
+        y = -cos(PI * (j + 0.25) / N - 3 / (8 * N * PI * (j + 0.25)));
+        for (int i = 0; i < 100; i++) {
+          legendre_P_dP_Q_dQ(N, y, &P, &dP, &Q, &dQ);
+          dy = -Q / dQ;
+          y += dy;
+          if (fabs(dy) < fabs(1e-15 * y)) break;
+        }
+      }
+      x[N - j] = -y;
+      x[j] = y;
+      legendre_P_dP_Q_dQ(N, y, &P, &dP, &Q, &dQ);
+      w[j] = 2.0 / ((N * (N + 1)) * P * P);
+      w[N - j] = w[j];
+    }
+  }
+  std::vector<double> wi(n);
+  for (int i = 0; i < n; i++) {
+    double denom = 1.;
+    for (int m2 = 0; m2 < n; m2++)
+      if (m2 != i) denom *= (x[i] - x[m2]);
+    wi[i] = 1. / denom;
+  }
+  for (int i = 0; i < n; i++) {
+    double Dii = 0;
+    for (int j = 0; j < n; j++)
+      if (i != j) {
+        double Dij = (wi[j] / wi[i]) / (x[i] - x[j]);
+        Dii -= Dij;
+        D[i * n + j] = Dij;
+      }
+    D[i * n + i] = Dii;
+  }
+}
+
+std::string pack_faces(nmg_mesh &m, const int64_t *nbnode, const double period[3]) {
+  const int n = m.n, np = n * n * n, nn = n * n;
+  const int64_t E = m.nelem;
+  m.nb.assign(E * 6, -1);
+  m.code.assign(E * 6, 0);
+  double per[3] = {0, 0, 0};
+  if (period)
+    for (int d = 0; d < 3; d++) per[d] = period[d];
+  // characteristic length for the tolerance
+  double lmax = 0;
+  for (int64_t i = 0; i < E * 3 * np; i++) lmax = std::max(lmax, std::fabs(m.xyz[i]));
+  const double tol = 1e-9 * std::max(1.0, lmax);
+  const double cell = 1e3 * tol;
+
+  auto pos = [&](int64_t e, int ijk, double q[3]) {
+    for (int d = 0; d < 3; d++) q[d] = wrap1(m.xyz[(e * 3 + d) * np + ijk], per[d]);
+  };
+  auto dist2 = [&](const double *a, const double *b) {
+    double s = 0;
+    for (int d = 0; d < 3; d++) {
+      double v = std::fabs(a[d] - b[d]);
+      if (per[d] > 0) v = std::min(v, per[d] - v);
+      s += v * v;
+    }
+    return s;
+  };
+  // face centre = average of the 4 corner nodes (an element face never
+  // straddles a period, so average first and wrap the centre)
+  auto centre = [&](int64_t e, int f, double c[3]) {
+    int corner[4][2] = {{0, 0}, {n - 1, 0}, {0, n - 1}, {n - 1, n - 1}};
+    for (int d = 0; d < 3; d++) {
+      double s = 0;
+      for (int t = 0; t < 4; t++)
+        s += m.xyz[(e * 3 + d) * np + face_node(n, f, corner[t][0], corner[t][1])];
+      c[d] = wrap1(0.25 * s, per[d]);
+    }
+  };
+
+  if (nbnode) {
+    // explicit node table: derive neighbour element, face and orientation
+    for (int64_t e = 0; e < E; e++)
+      for (int f = 0; f < 6; f++) {
+        const int64_t *t = nbnode + (e * 6 + f) * nn;
+        if (t[0] < 0) {
+          for (int q = 1; q < nn; q++)
+            if (t[q] >= 0) return "face with partial neighbour table";
+          continue;
+        }
+        int64_t e2 = t[0] / np;
+        int f2 = -1;
+        for (int g = 0; g < 6 && f2 < 0; g++) {
+          int ok = 1;
+          for (int q = 0; q < nn && ok; q++) {
+            int idx = (int)(t[q] - e2 * np);
+            int ii = idx % n, jj = (idx / n) % n, kk = idx / nn;
+            int c[3] = {ii, jj, kk};
+            if (t[q] / np != e2 || c[g >> 1] != (g & 1) * (n - 1)) ok = 0;
+          }
+          if (ok) f2 = g;
+        }
+        if (f2 < 0) return "neighbour nodes do not lie on one face";
+        int found = -1;
+        for (int o = 0; o < 8 && found < 0; o++) {
+          int ok = 1;
+          for (int b = 0; b < n && ok; b++)
+            for (int a = 0; a < n && ok; a++) {
+              int a2, b2;
+              orient_map(n, o, a, b, &a2, &b2);
+              if (t[a + n * b] != e2 * np + face_node(n, f2, a2, b2)) ok = 0;
+            }
+          if (ok) found = o;
+        }
+        if (found < 0) return "face node map is not a dihedral permutation";
+        m.nb[e * 6 + f] = (int32_t)e2;
+        m.code[e * 6 + f] = f2 | (found << 3);
+      }
+    return "";
+  }
+
+  // spatial hash of face centres
+  std::unordered_map<Key, std::vector<int64_t>, KeyHash> h;
+  h.reserve((size_t)E * 6);
+  auto kcell = [&](const double c[3], const int off[3]) {
+    Key k;
+    for (int d = 0; d < 3; d++) k.q[d] = (int64_t)std::floor(c[d] / cell) + off[d];
+    return k;
+  };
+  std::vector<double> cen(E * 6 * 3);
+  for (int64_t e = 0; e < E; e++)
+    for (int f = 0; f < 6; f++) {
+      double *c = &cen[(e * 6 + f) * 3];
+      centre(e, f, c);
+      int z[3] = {0, 0, 0};
+      h[kcell(c, z)].push_back(e * 6 + f);
+    }
+  for (int64_t e = 0; e < E; e++)
+    for (int f = 0; f < 6; f++) {
+      const double *c = &cen[(e * 6 + f) * 3];
+      int64_t match = -1;
+      int nmatch = 0;
+      for (int dz = -1; dz <= 1; dz++)
+        for (int dy = -1; dy <= 1; dy++)
+          for (int dx = -1; dx <= 1; dx++) {
+            int off[3] = {dx, dy, dz};
+            Key k = kcell(c, off);
+            if (per[0] > 0 || per[1] > 0 || per[2] > 0) {
+              // cells wrap around with the period
+              for (int d = 0; d < 3; d++)
+                if (per[d] > 0) {
+                  int64_t ncell = (int64_t)std::floor(per[d] / cell) + 1;
+                  k.q[d] = ((k.q[d] % ncell) + ncell) % ncell;
+                }
+            }
+            auto it = h.find(k);
+            if (it == h.end()) continue;
+            for (int64_t g : it->second) {
+              if (g == e * 6 + f) continue;  // (a periodic element may be its own neighbour)
+              if (dist2(c, &cen[g * 3]) < tol * tol) {
+                if (g != match) nmatch++;
+                if (nmatch > 1)
+                  return "faces " + std::to_string(match) + " and " + std::to_string(g) +
+                         " both match face " + std::to_string(f) + " of element " +
+                         std::to_string(e) + " (non-conforming mesh)";
+                match = g;
+              }
+            }
+          }
+      if (nmatch == 0) continue;  // outer face
+      if (nmatch > 1)
+        return "more than one face matches face " + std::to_string(f) + " of element " +
+               std::to_string(e) + " (non-conforming mesh)";
+      int64_t e2 = match / 6;
+      int f2 = (int)(match % 6);
+      // orientation: match the in-plane node (a,b)=(1,0) and (0,1) images
+      int found = -1;
+      for (int o = 0; o < 8 && found < 0; o++) {
+        int ok = 1;
+        for (int b = 0; b < n && ok; b++)
+          for (int a = 0; a < n && ok; a++) {
+            int a2, b2;
+            orient_map(n, o, a, b, &a2, &b2);
+            double p1[3], p2[3];
+            pos(e, face_node(n, f, a, b), p1);
+            pos(e2, face_node(n, f2, a2, b2), p2);
+            if (dist2(p1, p2) > tol * tol) ok = 0;
+          }
+        if (ok) found = o;
+      }
+      if (found < 0) return "face nodes of neighbours do not coincide (non-conforming)";
+      m.nb[e * 6 + f] = (int32_t)e2;
+      m.code[e * 6 + f] = f2 | (found << 3);
+    }
+  return "";
+}
+
+}  // namespace nmg
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+const char *nmg_mesh_last_error(void) { return g_mesh_err.c_str(); }
+
+int nmg_basis(int32_t n, double *x, double *w, double *D) {
+  if (n < 2 || n > 32 || !x || !w || !D) return fail(NMG_EINVAL, "nmg_basis: bad argument");
+  nmg::lgl_basis(n, x, w, D);
+  return NMG_OK;
+}
+
+int nmg_mesh_build(const nmg_mesh_params *p, nmg_mesh **out) {
+  if (!p || !out) return fail(NMG_EINVAL, "nmg_mesh_build: null argument");
+  *out = nullptr;
+  if (p->n < 2 || p->n > 16) return fail(NMG_EUNSUP, "nmg_mesh_build: n must be in [2,16]");
+  if (p->luni < 0 || p->luni > 8) return fail(NMG_EINVAL, "nmg_mesh_build: luni must be in [0,8]");
+  nmg_mesh *m = new (std::nothrow) nmg_mesh;
+  if (!m) return fail(NMG_ENOMEM, "nmg_mesh_build: out of memory");
+  try {
+    m->n = p->n;
+    m->x.resize(p->n); m->w.resize(p->n); m->D.resize(p->n * p->n);
+    nmg::lgl_basis(p->n, m->x.data(), m->w.data(), m->D.data());
+    std::vector<Patch> pats;
+    double period[3] = {0, 0, 0};
+    if (p->mesh_type == NMG_MESH_BOX) {
+      if (!(p->box_dout > 0)) { delete m; return fail(NMG_EINVAL, "box_dout must be > 0"); }
+      Patch b;
+      for (int d = 0; d < 3; d++) {
+        b.bbox[2 * d] = p->xc[d] - p->box_dout;
+        b.bbox[2 * d + 1] = p->xc[d] + p->box_dout;
+        if (p->periodic) period[d] = 2 * p->box_dout;
+      }
+      pats.push_back(b);
+    } else if (p->mesh_type == NMG_MESH_CUBEDSPHERES7) {
+      if (!(p->cs_dc > 0) || !(p->cs_r0fac > sqrt(3.))) {
+        delete m;
+        return fail(NMG_EINVAL, "cubed spheres need cs_dc > 0 and cs_r0fac > sqrt(3)");
+      }
+      if (p->periodic) { delete m; return fail(NMG_EINVAL, "periodic only for the box"); }
+      double dc = p->cs_dc, r0 = p->cs_r0fac * dc;
+      Patch b;
+      for (int d = 0; d < 3; d++) {
+        b.bbox[2 * d] = p->xc[d] - dc;
+        b.bbox[2 * d + 1] = p->xc[d] + dc;
+      }
+      pats.push_back(b);
+      double Din[6], r[4];
+      for (int f = 0; f < 6; f++) Din[f] = dc;
+      for (int dom = 0; dom < 6; dom++) {
+        Patch c;
+        ab_range(dom, Din, r);
+        double bb[6] = {0., 1., r[0], r[1], r[2], r[3]};
+        std::memcpy(c.bbox, bb, sizeof(bb));
+        c.cubed = true;
+        c.dom = dom;
+        for (int d = 0; d < 3; d++) c.xc[d] = p->xc[d];
+        c.s0 = Din[dom];
+        c.s1 = r0;
+        pats.push_back(c);
+      }
+    } else {
+      delete m;
+      return fail(NMG_EUNSUP, "nmg_mesh_build: unknown mesh_type");
+    }
+    fill_geometry(*m, pats, p->luni);
+    std::string err = nmg::pack_faces(*m, nullptr, period);
+    if (!err.empty()) { delete m; return fail(NMG_EMESH, err); }
+  } catch (const std::bad_alloc &) {
+    delete m;
+    return fail(NMG_ENOMEM, "nmg_mesh_build: out of memory");
+  }
+  *out = m;
+  return NMG_OK;
+}
+
+int nmg_mesh_from_desc(const nmg_mesh_desc *d, nmg_mesh **out) {
+  if (!d || !out || !d->bbox || !d->curvi || !d->xyz) return fail(NMG_EINVAL, "nmg_mesh_from_desc: null argument");
+  *out = nullptr;
+  if (d->n < 2 || d->n > 16 || d->nelem <= 0) return fail(NMG_EUNSUP, "nmg_mesh_from_desc: bad n or nelem");
+  const int n = d->n, np = n * n * n;
+  const int64_t E = d->nelem;
+  for (int64_t e = 0; e < E; e++)
+    if (d->curvi[e] && !d->dXdx) return fail(NMG_EINVAL, "curvilinear element without dXdx");
+  nmg_mesh *m = new (std::nothrow) nmg_mesh;
+  if (!m) return fail(NMG_ENOMEM, "out of memory");
+  try {
+    m->n = n;
+    m->nelem = E;
+    m->x.resize(n); m->w.resize(n); m->D.resize(n * n);
+    nmg::lgl_basis(n, m->x.data(), m->w.data(), m->D.data());
+    m->pat.assign(E, 0);
+    if (d->pat) std::memcpy(m->pat.data(), d->pat, E * sizeof(int32_t));
+    m->bbox.assign(d->bbox, d->bbox + E * 6);
+    m->curvi.assign(d->curvi, d->curvi + E);
+    m->xyz.assign(d->xyz, d->xyz + E * 3 * np);
+    m->dXdx.assign(E * 9 * np, 0.);
+    for (int64_t e = 0; e < E; e++) {
+      double *M9 = &m->dXdx[e * 9 * np];
+      if (m->curvi[e]) {
+        std::memcpy(M9, d->dXdx + e * 9 * np, 9 * np * sizeof(double));
+      } else {
+        for (int a = 0; a < 3; a++)
+          for (int i = 0; i < np; i++) M9[(a * 3 + a) * np + i] = 1.;
+      }
+      for (int q = 0; q < 3; q++)
+        if (!(m->bbox[e * 6 + 2 * q + 1] > m->bbox[e * 6 + 2 * q])) {
+          delete m;
+          return fail(NMG_EINVAL, "element bbox must have positive extent");
+        }
+    }
+    std::string err = nmg::pack_faces(*m, d->nbnode, d->period);
+    if (!err.empty()) { delete m; return fail(NMG_EMESH, err); }
+  } catch (const std::bad_alloc &) {
+    delete m;
+    return fail(NMG_ENOMEM, "out of memory");
+  }
+  *out = m;
+  return NMG_OK;
+}
+
+int64_t nmg_mesh_nelem(const nmg_mesh *m) { return m ? m->nelem : -1; }
+int32_t nmg_mesh_n(const nmg_mesh *m) { return m ? m->n : -1; }
+
+int nmg_mesh_get_elements(const nmg_mesh *m, int32_t *pat, double *bbox) {
+  if (!m) return fail(NMG_EINVAL, "null mesh");
+  if (pat) std::memcpy(pat, m->pat.data(), m->nelem * sizeof(int32_t));
+  if (bbox) std::memcpy(bbox, m->bbox.data(), m->nelem * 6 * sizeof(double));
+  return NMG_OK;
+}
+
+int nmg_mesh_get_coords(const nmg_mesh *m, double *xyz) {
+  if (!m || !xyz) return fail(NMG_EINVAL, "null argument");
+  std::memcpy(xyz, m->xyz.data(), m->xyz.size() * sizeof(double));
+  return NMG_OK;
+}
+
+int nmg_mesh_get_dXdx(const nmg_mesh *m, double *dXdx) {
+  if (!m || !dXdx) return fail(NMG_EINVAL, "null argument");
+  std::memcpy(dXdx, m->dXdx.data(), m->dXdx.size() * sizeof(double));
+  return NMG_OK;
+}
+
+int nmg_mesh_get_faces(const nmg_mesh *m, int32_t *nb, int32_t *code) {
+  if (!m) return fail(NMG_EINVAL, "null mesh");
+  if (nb) std::memcpy(nb, m->nb.data(), m->nb.size() * sizeof(int32_t));
+  if (code) std::memcpy(code, m->code.data(), m->code.size() * sizeof(int32_t));
+  return NMG_OK;
+}
+
+void nmg_mesh_free(nmg_mesh *m) { delete m; }
+
+}  // extern "C"

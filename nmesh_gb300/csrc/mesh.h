@@ -1,0 +1,41 @@
+// mesh.h -- host-side packed mesh shared by the mesh packer (mesh.cpp) and
+// the device context (nmg.cu).
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+struct nmg_mesh {
+  int n = 0;        // LGL nodes per direction
+  int64_t nelem = 0;
+  std::vector<int32_t> pat;    // [E] patch index
+  std::vector<double> bbox;    // [E][6] bbox in patch coordinates
+  std::vector<int32_t> curvi;  // [E] 1 if the patch map is not Cartesian
+  std::vector<double> xyz;     // [E][3][np]
+  std::vector<double> dXdx;    // [E][9][np] dX^a/dx^i (identity if Cartesian)
+  std::vector<int32_t> nb;     // [E][6] neighbour element, -1 on outer faces
+  std::vector<int32_t> code;   // [E][6] neighbour face | orientation << 3
+  std::vector<double> x, w, D; // LGL nodes, weights, D[i*n+j]
+};
+
+namespace nmg {
+// LGL nodes/weights and differentiation matrix (Legendre.c / Lagrange.c)
+void lgl_basis(int n, double *x, double *w, double *D);
+// in-plane node (a, b) of face f -> volume index i + n*(j + n*k)
+inline int face_node(int n, int f, int a, int b) {
+  int d = f >> 1, p = (f & 1) * (n - 1);
+  if (d == 0) return p + n * (a + n * b);
+  if (d == 1) return a + n * (p + n * b);
+  return a + n * (b + n * p);
+}
+// apply a dihedral orientation code to an in-plane index pair
+inline void orient_map(int n, int o, int a, int b, int *a2, int *b2) {
+  int s = o & 1, fa = (o >> 1) & 1, fb = (o >> 2) & 1;
+  int aa = s ? b : a, bb = s ? a : b;
+  *a2 = fa ? n - 1 - aa : aa;
+  *b2 = fb ? n - 1 - bb : bb;
+}
+// build neighbour/orientation table from coordinates (or an explicit
+// node table); returns an error string or empty on success
+std::string pack_faces(nmg_mesh &m, const int64_t *nbnode, const double period[3]);
+}  // namespace nmg

@@ -154,19 +154,19 @@ static void flux1d(double *f, const double norm[3], const double *u)
 static void deriv_dir(int n, const double *D, int dir, const double *in,
                       double *out)
 {
+  /* stride of direction dir and the sum over l in ascending order */
+  const int st = (dir == 0) ? 1 : (dir == 1) ? n : n * n;
   int i, j, k, l;
   for (k = 0; k < n; k++)
     for (j = 0; j < n; j++)
       for (i = 0; i < n; i++) {
-        int ii = (dir == 0) ? i : (dir == 1) ? j : k;
+        const int ii = (dir == 0) ? i : (dir == 1) ? j : k;
+        const int ijk = i + n * (j + n * k);
+        const double *line = in + ijk - ii * st;
+        const double *Drow = D + ii * n;
         double sum = 0.0;
-        for (l = 0; l < n; l++) {
-          int idx = (dir == 0) ? l + n * (j + n * k)
-                  : (dir == 1) ? i + n * (l + n * k)
-                               : i + n * (j + n * l);
-          sum += D[ii * n + l] * in[idx];
-        }
-        out[i + n * (j + n * k)] = sum;
+        for (l = 0; l < n; l++) sum += Drow[l] * line[l * st];
+        out[ijk] = sum;
       }
 }
 

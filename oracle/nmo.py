@@ -112,9 +112,11 @@ def match_faces(xyz, n, period=None, tol=1e-9):
     faces = {}
     for e in range(E):
         for f in range(6):
-            P = wrap(xyz[e][:, planes[f]].T)          # [n*n, 3]
-            order = np.lexsort(P.T[::-1])
-            fkey = pkey(P[order].mean(axis=0))
+            raw = xyz[e][:, planes[f]].T              # [n*n, 3]
+            P = wrap(raw)
+            # a face never straddles a period: average, then wrap
+            order = np.lexsort(raw.T[::-1])
+            fkey = pkey(wrap(raw[order].mean(axis=0)))
             faces.setdefault(fkey, []).append((e, f, P))
     nb = np.full((E, 6, n * n), -1, np.int64)
     for fkey, lst in faces.items():

@@ -1,0 +1,85 @@
+"""Shared helpers of the tests: golden fixtures, element permutations,
+seeded inputs."""
+import json
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = os.path.join(HERE, "golden")
+PI = 3.141592653589793
+CASES = ["box_l1_n5", "box_l2_n4", "cs7_l0_n9", "cs7_l1_n5", "cs7_l1_n4"]
+
+# relative L2 tolerance of the CUDA path against the reference / oracle for
+# one RHS evaluation and for a few RK4 steps (FP64; FMA contraction and a
+# different summation order only)
+RTOL_RHS = 1e-12
+RTOL_RK4 = 1e-12
+
+
+def load(case):
+    d = np.load(os.path.join(GOLDEN, case + ".npz"))
+    meta = json.loads(str(d["meta"]))
+    return d, meta
+
+
+def build_mesh(meta, periodic=False):
+    import nmesh_gb300 as ng
+    if meta["mesh"] == "box":
+        return ng.Mesh.build(ng.MESH_BOX, n=meta["n"], luni=meta["luni"],
+                             xc=(PI, PI, PI), box_dout=PI, periodic=periodic)
+    return ng.Mesh.build(ng.MESH_CUBEDSPHERES7, n=meta["n"], luni=meta["luni"],
+                         cs_dc=1.0, cs_r0fac=20.0)
+
+
+def perm_to_mesh(mesh, d):
+    """Index array p such that mesh element p[i] is fixture element i."""
+    pat, bbox = mesh.elements()
+    key = {(int(a),) + tuple(b): i for i, (a, b) in enumerate(zip(pat, bbox))}
+    return np.array([key[(int(a),) + tuple(b)] for a, b in zip(d["pat"], d["bbox"])])
+
+
+def to_mesh_order(arr, perm):
+    out = np.empty_like(arr)
+    out[perm] = arr
+    return out
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm((a - b).ravel()) / max(np.linalg.norm(b.ravel()), 1e-300))
+
+
+def oracle_for(mesh, bc=0, k=(1.0, 1.0, 1.0), period=None):
+    """Oracle mesh built from the product mesh's geometry, with its own
+    coordinate-matching neighbour table."""
+    from oracle import nmo
+    pat, bbox = mesh.elements()
+    xyz = mesh.coords()
+    dXdx = mesh.dXdx()
+    curvi = np.array([0 if np.allclose(dXdx[e], np.repeat(np.eye(3).ravel()[:, None],
+                                                          mesh.np, 1)) else 1
+                      for e in range(mesh.nelem)], np.int32)
+    nb = nmo.match_faces(xyz, mesh.n, period=period)
+    return nmo.OracleMesh(bbox, curvi, dXdx, xyz, nb, mesh.n, bc=bc, k=k)
+
+
+def gaussian_pulses(xyz, seed, npulse=8, rmin=3.0, rmax=10.0, wmin=0.5, wmax=2.0,
+                    amin=0.1, amax=1.0):
+    """Seeded sum of Gaussian pulses in pi (and consistent c = grad psi of the
+    same profile), phi = psi; xyz: [E,3,np] -> u [E,5,np]."""
+    rng = np.random.default_rng(seed)
+    E, _, npt = xyz.shape
+    u = np.zeros((E, 5, npt))
+    for _ in range(npulse):
+        r = rng.uniform(rmin, rmax)
+        v = rng.normal(size=3)
+        v /= np.linalg.norm(v)
+        c = r * v
+        w = rng.uniform(wmin, wmax)
+        a = rng.uniform(amin, amax)
+        dx = xyz - c[None, :, None]
+        g = a * np.exp(-np.sum(dx * dx, axis=1) / (w * w))
+        u[:, 4] += g
+        u[:, 1:4] += -2.0 * dx / (w * w) * g[:, None, :]
+        u[:, 0] += 0.0
+    return u

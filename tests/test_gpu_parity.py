@@ -1,0 +1,119 @@
+"""Parity of the CUDA path (through the C ABI) with the reference's own
+outputs (golden fixtures) and with the oracle, FP64.  Tolerances: relative
+L2 <= 1e-12 for one RHS evaluation and for a few RK4 steps (RTOL_RHS,
+RTOL_RK4 in helpers.py); integer/index work (face tables) is exact."""
+import numpy as np
+import pytest
+
+import nmesh_gb300 as ng
+from helpers import (CASES, PI, RTOL_RHS, RTOL_RK4, build_mesh, gaussian_pulses,
+                     load, oracle_for, perm_to_mesh, rel_l2, to_mesh_order)
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(autouse=True)
+def _gpu(cuda_ok):
+    yield
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_rhs_matches_reference(case):
+    d, meta = load(case)
+    m = build_mesh(meta)
+    perm = perm_to_mesh(m, d)
+    ev = ng.Evolution(m, ng.BC_EXACT_PLANEWAVE, k=meta["k"])
+    r = ev.rhs(to_mesh_order(d["u0"], perm), 0.0)
+    assert rel_l2(r[perm], d["r0"]) <= RTOL_RHS
+    # pointwise: no node off by more than 1e-11 of the largest |r|
+    assert np.abs(r[perm] - d["r0"]).max() <= 1e-11 * np.abs(d["r0"]).max()
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_rk4_matches_reference(case):
+    d, meta = load(case)
+    m = build_mesh(meta)
+    perm = perm_to_mesh(m, d)
+    ev = ng.Evolution(m, ng.BC_EXACT_PLANEWAVE, k=meta["k"])
+    u = ev.rk4_steps_host(to_mesh_order(d["u0"], perm), 0.0, meta["dt"], meta["steps"])
+    assert rel_l2(u[perm], d["u_final"]) <= RTOL_RK4
+    # the single-step entry point gives the same state
+    ev.set_state(to_mesh_order(d["u0"], perm))
+    t = 0.0
+    for s in range(meta["steps"]):
+        ev.rk4_step(t, meta["dt"])
+        t += meta["dt"]
+    assert rel_l2(ev.get_state()[perm], d["u_final"]) <= RTOL_RK4
+
+
+@pytest.mark.parametrize("n,luni", [(2, 1), (3, 2), (6, 1), (7, 0), (8, 1), (10, 0), (11, 0), (12, 0)])
+def test_cubed_spheres_outgoing_vs_oracle(n, luni):
+    """Every compiled order: Gaussian pulses, outgoing-radiation outer
+    boundary (restated, no reference counterpart), against the oracle."""
+    m = ng.Mesh.build(ng.MESH_CUBEDSPHERES7, n=n, luni=luni, cs_dc=1.0, cs_r0fac=20.0)
+    u = gaussian_pulses(m.coords(), seed=n * 10 + luni, rmin=1.0, rmax=6.0)
+    u += 1e-3 * np.random.default_rng(n).standard_normal(u.shape)
+    o = oracle_for(m, bc=1)
+    ev = ng.Evolution(m, ng.BC_OUTGOING)
+    r = ev.rhs(u, 0.0)
+    ro = o.rhs(u, 0.0)
+    assert rel_l2(r, ro) <= RTOL_RHS
+    dt = 0.02 / n ** 2
+    uf = ev.rk4_steps_host(u, 0.0, dt, 3)
+    uo = o.rk4(u, dt, 3)
+    assert rel_l2(uf, uo) <= RTOL_RK4
+
+
+@pytest.mark.parametrize("n,luni", [(5, 1), (5, 0), (4, 2)])
+def test_periodic_box_vs_oracle(n, luni):
+    """Periodic cube [0, 2 pi]^3 (the reference has no periodic faces; the
+    oracle restates them as plain face connections).  luni=0 makes the only
+    element its own neighbour on all six faces."""
+    m = ng.Mesh.build(ng.MESH_BOX, n=n, luni=luni, xc=(PI, PI, PI), box_dout=PI,
+                      periodic=True)
+    nb, _ = m.faces()
+    assert (nb >= 0).all()
+    rng = np.random.default_rng(luni)
+    xyz = m.coords()
+    amp = rng.uniform(0.5, 1.5)
+    arg = xyz.sum(axis=1)
+    u = amp * np.stack([-np.sqrt(3) * np.cos(arg), np.cos(arg), np.cos(arg), np.cos(arg),
+                        np.sin(arg)], 1)
+    u += 0.01 * rng.standard_normal(u.shape)
+    o = oracle_for(m, period=2 * PI)
+    ev = ng.Evolution(m, ng.BC_EXACT_PLANEWAVE, k=(1.0, 1.0, 1.0))
+    assert rel_l2(ev.rhs(u), o.rhs(u)) <= RTOL_RHS
+    dt = 0.25 * (2 * PI / 2 ** luni) / (n - 1) ** 2
+    assert rel_l2(ev.rk4_steps_host(u, 0.0, dt, 4), o.rk4(u, dt, 4)) <= RTOL_RK4
+
+
+def test_rhs_device_pointers_and_determinism():
+    import torch
+    d, meta = load("cs7_l1_n5")
+    m = build_mesh(meta)
+    perm = perm_to_mesh(m, d)
+    ev = ng.Evolution(m, ng.BC_EXACT_PLANEWAVE, k=meta["k"])
+    u = to_mesh_order(d["u0"], perm)
+    w = torch.from_numpy(u).cuda()
+    r = torch.empty_like(w)
+    torch.cuda.synchronize()
+    ev.rhs_device(w.data_ptr(), r.data_ptr(), 0.0)
+    torch.cuda.synchronize()
+    r1 = ev.rhs(u)
+    ev.rhs_device(w.data_ptr(), r.data_ptr(), 0.0)
+    torch.cuda.synchronize()
+    # bitwise deterministic across calls and entry points
+    assert np.array_equal(r.cpu().numpy(), r1)
+    assert rel_l2(r1[perm], d["r0"]) <= RTOL_RHS
+
+
+def test_zero_steps_and_bad_arguments():
+    d, meta = load("box_l1_n5")
+    m = build_mesh(meta)
+    ev = ng.Evolution(m, ng.BC_EXACT_PLANEWAVE, k=meta["k"])
+    u = np.ones(ev.shape)
+    assert np.array_equal(ev.rk4_steps_host(u, 0.0, 0.01, 0), u)
+    with pytest.raises(ng.NmgError):
+        ev.rk4_steps(0.0, 0.01, -1)
+    with pytest.raises(ng.NmgError):
+        ng.Evolution(m, bc=7)

@@ -1,0 +1,104 @@
+"""Host-side mesh packer (nmesh_gb300/csrc/mesh.cpp): geometry against the
+reference's own coordinates/metric, face table against the oracle's
+independent coordinate matcher."""
+import numpy as np
+import pytest
+
+import nmesh_gb300 as ng
+from helpers import CASES, PI, build_mesh, load, perm_to_mesh
+from oracle import nmo
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_geometry_bitexact(case):
+    d, meta = load(case)
+    m = build_mesh(meta)
+    perm = perm_to_mesh(m, d)
+    assert np.array_equal(m.coords()[perm], d["x"])
+    assert np.array_equal(m.dXdx()[perm], d["dXdx"])
+
+
+def _faces_from_nbnode(nbnode, n):
+    """(neighbour element, face, orientation) implied by a node table."""
+    npt = n ** 3
+    E = nbnode.shape[0]
+    out = {}
+    for e in range(E):
+        for f in range(6):
+            t = nbnode[e, f]
+            if t[0] < 0:
+                continue
+            out[(e, f)] = tuple(int(v) for v in t)
+    return out
+
+
+@pytest.mark.parametrize("case", CASES)
+@pytest.mark.parametrize("periodic", [False, True])
+def test_face_table_matches_oracle_matcher(case, periodic):
+    d, meta = load(case)
+    if periodic and meta["mesh"] != "box":
+        pytest.skip("periodic only for the box")
+    m = build_mesh(meta, periodic=periodic)
+    n = m.n
+    nb, code = m.faces()
+    ref = nmo.match_faces(m.coords(), n, period=2 * PI if periodic else None)
+    npt = n ** 3
+    for e in range(m.nelem):
+        for f in range(6):
+            if nb[e, f] < 0:
+                assert (ref[e, f] < 0).all()
+                continue
+            f2, o = code[e, f] & 7, code[e, f] >> 3
+            for b in range(n):
+                for a in range(n):
+                    s, fa, fb = o & 1, (o >> 1) & 1, (o >> 2) & 1
+                    aa, bb = (b, a) if s else (a, b)
+                    aa = n - 1 - aa if fa else aa
+                    bb = n - 1 - bb if fb else bb
+                    idx = nmo.face_plane_index(n, f2)[aa + n * bb]
+                    assert ref[e, f, a + n * b] == nb[e, f] * npt + idx
+
+
+def test_desc_roundtrip_with_explicit_node_table():
+    d, meta = load("cs7_l1_n4")
+    m = build_mesh(meta)
+    pat, bbox = m.elements()
+    xyz = m.coords()
+    J = m.dXdx()
+    curvi = (pat > 0).astype(np.int32)
+    ref = nmo.match_faces(xyz, m.n)
+    m2 = ng.Mesh.from_arrays(bbox, curvi, xyz, J, nbnode=ref, pat=pat)
+    m3 = ng.Mesh.from_arrays(bbox, curvi, xyz, J, pat=pat)
+    for mm in (m2, m3):
+        nb2, code2 = mm.faces()
+        nb1, code1 = m.faces()
+        assert np.array_equal(nb1, nb2) and np.array_equal(code1, code2)
+
+
+def test_mesh_errors():
+    with pytest.raises(ng.NmgError):
+        ng.Mesh.build(ng.MESH_BOX, n=1)
+    with pytest.raises(ng.NmgError):
+        ng.Mesh.build(99, n=4)
+    with pytest.raises(ng.NmgError):
+        ng.Mesh.build(ng.MESH_CUBEDSPHERES7, n=4, cs_r0fac=1.0)
+    # a partial neighbour table is rejected
+    d, meta = load("box_l1_n5")
+    m = build_mesh(meta)
+    pat, bbox = m.elements()
+    xyz = m.coords()
+    ref = nmo.match_faces(xyz, m.n)
+    e, f = np.argwhere(ref[:, :, 0] >= 0)[0]
+    ref[e, f, 3] = -1
+    with pytest.raises(ng.NmgError):
+        ng.Mesh.from_arrays(bbox, np.zeros(len(pat), np.int32), xyz, nbnode=ref)
+
+
+def test_config2_mesh_counts():
+    """The cubed-sphere workload: 7 patches x 16^3 elements at n = 9."""
+    m = ng.Mesh.build(ng.MESH_CUBEDSPHERES7, n=3, luni=4, cs_dc=1.0, cs_r0fac=20.0)
+    assert m.nelem == 7 * 16 ** 3
+    nb, _ = m.faces()
+    assert (nb < 0).sum() == 6 * 16 * 16   # only the outer sphere is outer
+    r = np.linalg.norm(m.coords(), axis=1)
+    assert abs(r.max() - 20.0) < 1e-12 and abs(r.min() - 0.0) < 1e-12 or r.min() >= 0

@@ -1,0 +1,85 @@
+"""The oracle (CPU restatement, oracle/nmo.c) against the reference's own
+outputs: golden fixtures made by running the reference
+(tests/golden/make_golden.py).  The restatement follows the reference's
+operation order and must match it bit for bit."""
+import numpy as np
+import pytest
+
+from helpers import CASES, load
+from oracle import nmo
+
+
+def _oracle_mesh(d, meta):
+    n = int(d["n"][0, 0])
+    curvi = (d["pat"] > 0).astype(np.int32) if meta["mesh"] == "cs7" else \
+        np.zeros(len(d["pat"]), np.int32)
+    nb = nmo.match_faces(d["x"], n)
+    return nmo.OracleMesh(d["bbox"], curvi, d["dXdx"], d["x"], nb, n, bc=0, k=meta["k"])
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_oracle_rhs_bitexact(case):
+    d, meta = load(case)
+    m = _oracle_mesh(d, meta)
+    r = m.rhs(d["u0"], 0.0)
+    assert np.array_equal(r, d["r0"])
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_oracle_rk4_bitexact(case):
+    d, meta = load(case)
+    m = _oracle_mesh(d, meta)
+    u = m.rk4(d["u0"], meta["dt"], meta["steps"])
+    assert np.array_equal(u, d["u_final"])
+
+
+def test_lgl_basis_properties():
+    for n in range(2, 13):
+        x, w = nmo.lgl(n)
+        D = nmo.diffmat(n)
+        assert abs(w.sum() - 2.0) < 1e-13
+        assert np.all(np.diff(x) > 0)
+        # D differentiates polynomials of degree n-1 exactly
+        for p in range(n):
+            assert np.allclose(D @ x ** p, p * x ** max(p - 1, 0) * (p > 0), atol=1e-10)
+        # row sums vanish (negative-sum trick of the reference)
+        assert np.abs(D.sum(axis=1)).max() < 1e-12
+
+
+def test_outgoing_bc_absorbs_outgoing_characteristic():
+    """With the outgoing BC a state whose incoming characteristic pi + c.n
+    vanishes on the outer face gets no lift from the exterior jump in
+    pi + c.n; here: the RHS is linear and homogeneous (r(0) = 0)."""
+    d, meta = load("cs7_l0_n9")
+    n = 9
+    nb = nmo.match_faces(d["x"], n)
+    m = nmo.OracleMesh(d["bbox"], (d["pat"] > 0).astype(np.int32), d["dXdx"], d["x"],
+                       nb, n, bc=1)
+    z = np.zeros_like(d["u0"])
+    assert np.array_equal(m.rhs(z), z)
+    u = d["u0"]
+    r1 = m.rhs(u)
+    r2 = m.rhs(2.0 * u)
+    assert np.allclose(r2, 2.0 * r1, rtol=0, atol=1e-12 * np.abs(r1).max())
+
+
+def test_periodic_plane_wave_is_smooth():
+    """Periodic box: the RHS of the exact plane wave matches its time
+    derivative to truncation accuracy (no boundary at all)."""
+    import nmesh_gb300 as ng
+    from helpers import PI
+    mesh = ng.Mesh.build(ng.MESH_BOX, n=6, luni=2, xc=(PI, PI, PI), box_dout=PI,
+                         periodic=True)
+    xyz = mesh.coords()
+    k = np.array([1.0, 1.0, 1.0])
+    om = np.sqrt(3.0)
+    arg = np.einsum("i,eip->ep", k, xyz)
+    u = np.stack([-om * np.cos(arg), np.cos(arg), np.cos(arg), np.cos(arg), np.sin(arg)], 1)
+    dudt = np.stack([-om * om * np.sin(arg), om * np.sin(arg), om * np.sin(arg),
+                     om * np.sin(arg), -om * np.cos(arg)], 1)
+    nb = nmo.match_faces(xyz, 6, period=2 * PI)
+    assert (nb < 0).sum() == 0
+    _, bbox = mesh.elements()
+    m = nmo.OracleMesh(bbox, np.zeros(mesh.nelem, np.int32), mesh.dXdx(), xyz, nb, 6)
+    r = m.rhs(u)
+    assert np.abs(r - dudt).max() < 2e-3
