@@ -113,19 +113,22 @@ def match_faces(xyz, n, period=None, tol=1e-9):
     for e in range(E):
         for f in range(6):
             raw = xyz[e][:, planes[f]].T              # [n*n, 3]
-            P = wrap(raw)
             # a face never straddles a period: average, then wrap
             order = np.lexsort(raw.T[::-1])
-            fkey = pkey(wrap(raw[order].mean(axis=0)))
-            faces.setdefault(fkey, []).append((e, f, P))
+            cen = raw[order].mean(axis=0)
+            faces.setdefault(pkey(wrap(cen)), []).append((e, f, raw, cen))
     nb = np.full((E, 6, n * n), -1, np.int64)
     for fkey, lst in faces.items():
         if len(lst) == 1:
             continue
         if len(lst) != 2:
             raise ValueError("non-conforming face match")
-        for (e, f, P), (e2, f2, P2) in (lst, lst[::-1]):
-            where = {pkey(q): planes[f2][i] for i, q in enumerate(P2)}
+        for (e, f, P, c1), (e2, f2, P2, c2) in (lst, lst[::-1]):
+            # whole periods between the two faces (zero without a period)
+            shift = np.zeros(3)
+            if period is not None:
+                shift = np.round((c2 - c1) / period) * period
+            where = {pkey(q - shift): planes[f2][i] for i, q in enumerate(P2)}
             for jk in range(n * n):
                 nb[e, f, jk] = e2 * npt + where[pkey(P[jk])]
     return nb

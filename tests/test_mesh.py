@@ -102,3 +102,22 @@ def test_config2_mesh_counts():
     assert (nb < 0).sum() == 6 * 16 * 16   # only the outer sphere is outer
     r = np.linalg.norm(m.coords(), axis=1)
     assert abs(r.max() - 20.0) < 1e-12 and abs(r.min() - 0.0) < 1e-12 or r.min() >= 0
+
+
+@pytest.mark.parametrize("luni", [0, 1])
+def test_periodic_self_neighbour_face_table(luni):
+    """A periodic box with one element per direction is its own neighbour on
+    every face; the in-face node map must be the identity shifted by a
+    period, not a position collision of wrapped corners."""
+    m = ng.Mesh.build(ng.MESH_BOX, n=4, luni=luni, xc=(PI, PI, PI), box_dout=PI,
+                      periodic=True)
+    nb, code = m.faces()
+    assert (nb >= 0).all()
+    ref = nmo.match_faces(m.coords(), 4, period=2 * PI)
+    npt = 64
+    for e in range(m.nelem):
+        for f in range(6):
+            f2, o = code[e, f] & 7, code[e, f] >> 3
+            assert f2 == (f ^ 1) and o == 0
+            idx = nmo.face_plane_index(4, f2)
+            assert np.array_equal(ref[e, f], nb[e, f] * npt + idx)
