@@ -129,17 +129,31 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def fp64_flops_per_stage(mesh_nelem, ncurvi, n):
-    """FP64 flops one stage kernel issues (FMA = 2), counted from the
-    kernel: Cartesian nodes 6 directional derivatives (n FMA each) + 6 ops;
-    curvilinear nodes 12 derivatives + 18 chain-rule FMA; per face node 4
-    subtractions + 10 FMA; RK update 2 FMA per DOF (stage average 1.75)."""
-    np_ = n ** 3
-    ncart = mesh_nelem - ncurvi
-    vol = ncart * np_ * (6 * n * 2 + 6 * 2 - 3) + ncurvi * np_ * (12 * n * 2 + 18 * 2)
-    surf = mesh_nelem * 6 * n * n * (4 + 10 * 2)
-    rk = mesh_nelem * np_ * NFIELDS * 1.75 * 2
-    return vol + surf + rk
+def fp64_work_per_stage(variant, nelem, ncurvi, n, nnz_curvi=7):
+    """(flops, instructions) of FP64 work one stage kernel issues, counted
+    from the kernel source (FMA = 2 flops, 1 instruction; add/mul = 1, 1).
+    Curvilinear elements of the cubed-sphere map have nnz_curvi = 7 nonzero
+    chain-rule factors per node.  Face nodes: 4 subtractions + 10 FMA.
+    RK update: stage average 1.75 FMA per DOF."""
+    np_, nn = n ** 3, n * n
+    ncart = nelem - ncurvi
+    if variant.startswith("eo"):
+        M, odd = n // 2, n % 2
+        # per line: e/o adds, S and T sums (first term a multiply), outputs
+        ins = 2 * M + M * (M + odd) + M * M + 2 * M + odd * M
+        fl = 2 * M + M * (1 + 2 * (M + odd - 1)) + M * (1 + 2 * (M - 1)) + 2 * M \
+            + odd * (1 + 2 * (M - 1))
+        lines_cart, lines_curv = 6 * nn, (3 + nnz_curvi) * nn
+        vol_i = ncart * (lines_cart * ins + 6 * np_) + \
+            ncurvi * (lines_curv * ins + 2 * nnz_curvi * np_ + 2 * np_)
+        vol_f = ncart * (lines_cart * fl + 12 * np_) + \
+            ncurvi * (lines_curv * fl + 4 * nnz_curvi * np_ + 2 * np_)
+    else:
+        vol_i = ncart * np_ * (6 * n + 6) + ncurvi * np_ * (12 * n + 18)
+        vol_f = ncart * np_ * (12 * n + 9) + ncurvi * np_ * (24 * n + 36)
+    surf_i, surf_f = nelem * 6 * nn * 14, nelem * 6 * nn * 24
+    rk_i = nelem * np_ * NFIELDS * 1.75
+    return vol_f + surf_f + 2 * rk_i, vol_i + surf_i + rk_i
 
 
 def alg_bytes_per_stage(nelem, ncurvi, n):
@@ -224,7 +238,8 @@ def run_ours(args, rank, world, local):
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     per_launch_ms = ms / stages
     alg_bytes = alg_bytes_per_stage(mesh.nelem, ncurvi, n)
-    flops = fp64_flops_per_stage(mesh.nelem, ncurvi, n)
+    variant = ev.kernel_info().split(" | ")[0]
+    flops, fp64_ins = fp64_work_per_stage(variant, mesh.nelem, ncurvi, n)
     achieved_gbs = alg_bytes / (per_launch_ms / 1e3) / 1e9
     achieved_gflops = flops / (per_launch_ms / 1e3) / 1e9
     traffic = None
@@ -254,11 +269,14 @@ def run_ours(args, rank, world, local):
                          "traffic": traffic,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
                          "alg_bytes_per_launch": alg_bytes,
-                         "kernel": f"dg_stage_kernel<{n}>",
+                         "kernel": ev.kernel_info().split(" | ")[0],
+                         "autotune": ev.kernel_info().split(" | timings: ")[-1],
                          "launch_ms": per_launch_ms},
             "roofline_fp64": {"bound": "fp64", "achieved": achieved_gflops, "peak": fp64_peak,
                               "unit": "GFLOP/s", "frac": achieved_gflops / fp64_peak,
                               "flops_per_launch": flops,
+                              "fp64_instructions_per_launch": fp64_ins,
+                              "issue_frac": fp64_ins / (per_launch_ms / 1e3) / (fp64_peak * 1e9 / 2),
                               "peak_source": "FP64 FMA probe run live (nmg_fp64_peak)"},
             "clocks": clk,
             "cpu_baseline": cpu,

@@ -137,6 +137,17 @@ int nmg_rk4_steps(nmg_ctx *c, double t, double dt, int32_t nsteps);
 int nmg_rk4_steps_host(nmg_ctx *c, double t, double dt, int32_t nsteps,
                        double *host_u);
 
+/* ---- kernel selection (autotuner) --------------------------------------- */
+/* The first RHS/RK4 call of a context times every compiled variant of the
+ * stage kernel ("eo": even-odd line derivatives, "gather": node-parallel dot
+ * products) and tile shape (elements and threads per CTA) on the context's
+ * mesh and keeps the fastest.  spec = "auto" re-tunes; "eo", "gather" or
+ * "eo:<elements per CTA>:<threads>" forces a variant (the environment
+ * variable NMG_KERNEL does the same for new contexts). */
+int nmg_set_kernel(nmg_ctx *c, const char *spec);
+/* selected variant, candidates and tuning timings as text */
+int nmg_kernel_info(nmg_ctx *c, char *buf, int32_t len);
+
 /* ---- measurement helpers ------------------------------------------------ */
 /* kernels launched by this context so far */
 int64_t nmg_kernel_launches(const nmg_ctx *c);

@@ -87,6 +87,8 @@ def lib(build_if_missing=True):
         "nmg_kernel_launches": (i64, [vp]),
         "nmg_stream": (vp, [vp]),
         "nmg_fp64_peak": (ctypes.c_int, [vp]),
+        "nmg_set_kernel": (ctypes.c_int, [vp, ctypes.c_char_p]),
+        "nmg_kernel_info": (ctypes.c_int, [vp, vp, i32]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -257,6 +259,17 @@ class Evolution:
         self._check(lib().nmg_rk4_steps_host(self._h, float(t), float(dt), int(nsteps),
                                              _ptr(u)), "nmg_rk4_steps_host")
         return u
+
+    def set_kernel(self, spec="auto"):
+        """Force a stage-kernel variant ("eo", "gather", "eo:<epb>:<threads>")
+        or re-enable the autotuner ("auto")."""
+        self._check(lib().nmg_set_kernel(self._h, spec.encode()), "nmg_set_kernel")
+
+    def kernel_info(self):
+        buf = ctypes.create_string_buffer(4096)
+        self._check(lib().nmg_kernel_info(self._h, ctypes.cast(buf, ctypes.c_void_p), 4096),
+                    "nmg_kernel_info")
+        return buf.value.decode()
 
     @property
     def launches(self):

@@ -1,0 +1,214 @@
+// stage.cuh -- parameters and shared device code of the fused DG RHS + RK4
+// stage kernels (scalarwave1, FP64).
+//
+// Reference semantics (paths within nmeshsource/nmesh):
+//   volume terms  src/tests/scalarwave1/scalarwave1.c:62-134,242-284 with
+//                 src/main/coordinates/derivs.c:154-181,756-815
+//   face terms    src/tests/scalarwave1/scalarwave1.c:139-209,287-321 with
+//                 src/main/dg/dg.c:30-151 and src/main/dg/numflux1d.c:85-112
+//   stage update  src/main/evolve/RungeKutta.c:19-82
+//
+// r_pi = div c, r_c = grad pi (the flux of the first-order wave is
+// f_pi^i = -c_i, f_{c_j}^i = -pi delta^i_j, scalarwave1.c:39-48) plus, on
+// face nodes, the LLF lift (f* - f_in) sqrtgdiag / w_end with the wave
+// speed 1: r_pi += g (dpi + dc.n), r_c += g (dc + dpi n), where d = exterior
+// minus interior and g = sqrtgdiag / (2 w_end).  r_phi = pi.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+
+#include "../../include/nmg.h"
+
+#define NF 5
+#define NMAX 12
+
+namespace nmgk {
+
+struct StageParams {
+  int nelem;
+  const double *win;    // w read by the RHS (neighbour traces too)
+  const double *u0;     // u at the start of the step
+  double *acc;          // u accumulator
+  double *wout;         // next stage's w
+  double *rout;         // RHS output (mode 0)
+  int mode;             // 0: r only; 1..4: RK4 stage
+  double t;             // time of this RHS evaluation
+  double cacc, cw;      // stage coefficients: acc += cacc*r, wout = u0 + cw*r
+  const double *tdev;   // if non-null: step time read from tdev[*stepdev]
+  const int *stepdev;
+  double tofs_dt;       // stage time = step time + tofs_dt
+  // mesh
+  const int *nb;        // [E][6] neighbour element, -1 on outer faces
+  const int *code;      // [E][6] neighbour face | orientation << 3
+  const int *cslot;     // [E] curvilinear slot or -1 (Cartesian)
+  const int *bslot;     // [E][6] outer-face slot or -1
+  const int *cmask;     // [C] 9-bit mask of nonzero metric entries (a*3+i)
+  const double *scale;  // [E][3] dXb/dx of Cartesian elements
+  const double *gcart;  // [E][3] dXb/dx / (2 w_end): lift factor of Cartesian faces
+  const double *metric;  // [C][9][np] M[a][i] = dXb^a/dx^i (node-major)
+  const double *metricp; // [C][3 a][3 i][n q][n*n line]: pass-major layout
+  const double *fac;    // [C][6][nn][4] (g*n0, g*n1, g*n2, g)
+  const double *bxyz;   // [B][3][nn] coordinates of outer-face nodes
+  const double *bnrm;   // [B][3][nn] outward unit normals there
+  int bc;               // NMG_BC_*
+  double k0, k1, k2, om;
+  const double *D;      // [n][n] D[i*n+j] = l_j'(x_i)
+};
+
+template <int N>
+__device__ __forceinline__ int face_node_d(int f, int a, int b) {
+  const int d = f >> 1, p = (f & 1) * (N - 1);
+  return d == 0 ? p + N * (a + N * b) : d == 1 ? a + N * (p + N * b) : a + N * (b + N * p);
+}
+
+__device__ __forceinline__ double stage_time(const StageParams &P) {
+  return P.tdev ? P.tdev[*P.stepdev] + P.tofs_dt : P.t;
+}
+
+// copy pi, cx, cy, cz of w for EPB elements into sW[4][EPB][NP]
+template <int N, int EPB, int NT>
+__device__ __forceinline__ void stage_in(const StageParams &P, double *sW, int e0) {
+  constexpr int NP = N * N * N;
+  for (int q = threadIdx.x; q < EPB * 4 * NP; q += NT) {
+    const int le = q / (4 * NP), rem = q - le * 4 * NP, f = rem / NP, node = rem - f * NP;
+    const int e = e0 + le;
+    double v = 0.;
+    if (e < P.nelem) v = __ldg(P.win + ((size_t)e * NF + f) * NP + node);
+    sW[(f * EPB + le) * NP + node] = v;
+  }
+}
+
+// Face terms, one direction at a time (faces 2d and 2d+1 are disjoint node
+// sets, so no two threads of a pass touch the same node).  Accumulates
+// into sR[f][EPB][NP] for f = 0 (r_pi), 1..3 (r_c).
+template <int N, int EPB, int NT>
+__device__ __forceinline__ void face_terms(const StageParams &P, const double *sW, double *sR,
+                                           const int *sCs, const double (*sG)[3], int e0,
+                                           double t) {
+  constexpr int NP = N * N * N, NN = N * N;
+#pragma unroll 1
+  for (int d = 0; d < 3; d++) {
+    for (int q = threadIdx.x; q < EPB * 2 * NN; q += NT) {
+      const int le = q / (2 * NN), rem = q - le * 2 * NN, s = rem / NN, ab = rem - s * NN;
+      const int e = e0 + le;
+      if (e >= P.nelem) continue;
+      const int a = ab % N, b = ab / N, f = 2 * d + s;
+      const int node = face_node_d<N>(f, a, b);
+      const double ui0 = sW[(0 * EPB + le) * NP + node];
+      const double ui1 = sW[(1 * EPB + le) * NP + node];
+      const double ui2 = sW[(2 * EPB + le) * NP + node];
+      const double ui3 = sW[(3 * EPB + le) * NP + node];
+      double gn0, gn1, gn2, g;
+      const int cs = sCs[le];
+      if (cs < 0) {
+        g = sG[le][d];
+        const double sg = (f & 1) ? g : -g;
+        gn0 = d == 0 ? sg : 0.;
+        gn1 = d == 1 ? sg : 0.;
+        gn2 = d == 2 ? sg : 0.;
+      } else {
+        const double2 *F2 = reinterpret_cast<const double2 *>(P.fac) +
+                            (((size_t)cs * 6 + f) * NN + ab) * 2;
+        const double2 fa = __ldg(F2), fb = __ldg(F2 + 1);
+        gn0 = fa.x; gn1 = fa.y; gn2 = fb.x; g = fb.y;
+      }
+      double ua0, ua1, ua2, ua3;
+      const int nbe = __ldg(P.nb + e * 6 + f);
+      if (nbe >= 0) {
+        const int cd = __ldg(P.code + e * 6 + f), f2 = cd & 7, o = cd >> 3;
+        const int sw = o & 1, fa = (o >> 1) & 1, fb = (o >> 2) & 1;
+        int aa = sw ? b : a, bb = sw ? a : b;
+        aa = fa ? N - 1 - aa : aa;
+        bb = fb ? N - 1 - bb : bb;
+        const double *W2 = P.win + (size_t)nbe * NF * NP + face_node_d<N>(f2, aa, bb);
+        ua0 = __ldg(W2);
+        ua1 = __ldg(W2 + NP);
+        ua2 = __ldg(W2 + 2 * NP);
+        ua3 = __ldg(W2 + 3 * NP);
+      } else {
+        const int bs = __ldg(P.bslot + e * 6 + f);
+        if (P.bc == NMG_BC_EXACT_PLANEWAVE) {
+          const double *X = P.bxyz + (size_t)bs * 3 * NN + ab;
+          const double arg = P.k0 * X[0] + P.k1 * X[NN] + P.k2 * X[2 * NN] - P.om * t;
+          double sn, cn;
+          sincos(arg, &sn, &cn);
+          ua0 = -P.om * cn;
+          ua1 = P.k0 * cn;
+          ua2 = P.k1 * cn;
+          ua3 = P.k2 * cn;
+        } else {
+          // outgoing radiation: zero incoming characteristic pi + c.n
+          const double *Nr = P.bnrm + (size_t)bs * 3 * NN + ab;
+          const double n0 = Nr[0], n1 = Nr[NN], n2 = Nr[2 * NN];
+          const double cnv = ui1 * n0 + ui2 * n1 + ui3 * n2;
+          const double wo = ui0 - cnv;
+          const double dcn = -0.5 * wo - cnv;  // exterior c.n minus interior c.n
+          ua0 = 0.5 * wo;
+          ua1 = fma(dcn, n0, ui1);
+          ua2 = fma(dcn, n1, ui2);
+          ua3 = fma(dcn, n2, ui3);
+        }
+      }
+      const double dpi = ua0 - ui0, dcx = ua1 - ui1, dcy = ua2 - ui2, dcz = ua3 - ui3;
+      double *r0 = sR + (0 * EPB + le) * NP + node;
+      double *r1 = sR + (1 * EPB + le) * NP + node;
+      double *r2 = sR + (2 * EPB + le) * NP + node;
+      double *r3 = sR + (3 * EPB + le) * NP + node;
+      *r0 = fma(dcx, gn0, fma(dcy, gn1, fma(dcz, gn2, fma(g, dpi, *r0))));
+      *r1 = fma(dpi, gn0, fma(g, dcx, *r1));
+      *r2 = fma(dpi, gn1, fma(g, dcy, *r2));
+      *r3 = fma(dpi, gn2, fma(g, dcz, *r3));
+    }
+    __syncthreads();
+  }
+}
+
+// r out (mode 0) or RK4 stage update.  r_pi = sR[0] (+ sR[4] + sR[5] for
+// elements whose divergence is split over three partial sums).
+template <int N, int EPB, int NT, bool SPLIT>
+__device__ __forceinline__ void epilogue(const StageParams &P, const double *sW, const double *sR,
+                                         const int *sCs, int e0) {
+  constexpr int NP = N * N * N;
+  for (int q = threadIdx.x; q < EPB * NF * NP; q += NT) {
+    const int le = q / (NF * NP), rem = q - le * NF * NP, f = rem / NP, node = rem - f * NP;
+    const int e = e0 + le;
+    if (e >= P.nelem) continue;
+    const size_t idx = ((size_t)e * NF + f) * NP + node;
+    double r;
+    if (f < 4) {
+      r = sR[(f * EPB + le) * NP + node];
+      if (SPLIT && f == 0 && sCs[le] >= 0)
+        r += sR[(4 * EPB + le) * NP + node] + sR[(5 * EPB + le) * NP + node];
+    } else {
+      r = sW[(0 * EPB + le) * NP + node];  // r_phi = pi
+    }
+    if (P.mode == 0) {
+      P.rout[idx] = r;
+    } else if (P.mode == 1) {
+      const double u = __ldg(P.u0 + idx);
+      P.acc[idx] = fma(P.cacc, r, u);
+      P.wout[idx] = fma(P.cw, r, u);
+    } else if (P.mode == 4) {
+      P.acc[idx] = fma(P.cacc, r, P.acc[idx]);
+    } else {
+      P.acc[idx] = fma(P.cacc, r, P.acc[idx]);
+      P.wout[idx] = fma(P.cw, r, __ldg(P.u0 + idx));
+    }
+  }
+}
+
+// host-side launch entry points of the kernel variants
+typedef cudaError_t (*LaunchFn)(const StageParams &, cudaStream_t);
+struct Variant {
+  const char *name;  // "gather" or "eo"
+  int epb, nt;       // elements per CTA, threads per CTA
+  LaunchFn launch;   // nelem == 0: set the smem limit only
+};
+// all compiled variants for n (returns count, fills out[])
+int gather_variants(int n, Variant *out, int cap);
+int eo_variants(int n, Variant *out, int cap);
+// even-odd coefficients of D for n into constant memory
+cudaError_t eo_upload(int n, const double *D);
+
+}  // namespace nmgk

@@ -17,24 +17,31 @@ def _gpu(cuda_ok):
     yield
 
 
+VARIANTS = ["eo", "gather"]
+
+
+@pytest.mark.parametrize("variant", VARIANTS)
 @pytest.mark.parametrize("case", CASES)
-def test_rhs_matches_reference(case):
+def test_rhs_matches_reference(case, variant):
     d, meta = load(case)
     m = build_mesh(meta)
     perm = perm_to_mesh(m, d)
     ev = ng.Evolution(m, ng.BC_EXACT_PLANEWAVE, k=meta["k"])
+    ev.set_kernel(variant)
     r = ev.rhs(to_mesh_order(d["u0"], perm), 0.0)
     assert rel_l2(r[perm], d["r0"]) <= RTOL_RHS
     # pointwise: no node off by more than 1e-11 of the largest |r|
     assert np.abs(r[perm] - d["r0"]).max() <= 1e-11 * np.abs(d["r0"]).max()
 
 
+@pytest.mark.parametrize("variant", VARIANTS + ["auto"])
 @pytest.mark.parametrize("case", CASES)
-def test_rk4_matches_reference(case):
+def test_rk4_matches_reference(case, variant):
     d, meta = load(case)
     m = build_mesh(meta)
     perm = perm_to_mesh(m, d)
     ev = ng.Evolution(m, ng.BC_EXACT_PLANEWAVE, k=meta["k"])
+    ev.set_kernel(variant)
     u = ev.rk4_steps_host(to_mesh_order(d["u0"], perm), 0.0, meta["dt"], meta["steps"])
     assert rel_l2(u[perm], d["u_final"]) <= RTOL_RK4
     # the single-step entry point gives the same state
@@ -47,7 +54,8 @@ def test_rk4_matches_reference(case):
 
 
 @pytest.mark.parametrize("n,luni", [(2, 1), (3, 2), (6, 1), (7, 0), (8, 1), (10, 0), (11, 0), (12, 0)])
-def test_cubed_spheres_outgoing_vs_oracle(n, luni):
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_cubed_spheres_outgoing_vs_oracle(n, luni, variant):
     """Every compiled order: Gaussian pulses, outgoing-radiation outer
     boundary (restated, no reference counterpart), against the oracle."""
     m = ng.Mesh.build(ng.MESH_CUBEDSPHERES7, n=n, luni=luni, cs_dc=1.0, cs_r0fac=20.0)
@@ -55,6 +63,7 @@ def test_cubed_spheres_outgoing_vs_oracle(n, luni):
     u += 1e-3 * np.random.default_rng(n).standard_normal(u.shape)
     o = oracle_for(m, bc=1)
     ev = ng.Evolution(m, ng.BC_OUTGOING)
+    ev.set_kernel(variant)
     r = ev.rhs(u, 0.0)
     ro = o.rhs(u, 0.0)
     assert rel_l2(r, ro) <= RTOL_RHS
@@ -65,7 +74,8 @@ def test_cubed_spheres_outgoing_vs_oracle(n, luni):
 
 
 @pytest.mark.parametrize("n,luni", [(5, 1), (5, 0), (4, 2)])
-def test_periodic_box_vs_oracle(n, luni):
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_periodic_box_vs_oracle(n, luni, variant):
     """Periodic cube [0, 2 pi]^3 (the reference has no periodic faces; the
     oracle restates them as plain face connections).  luni=0 makes the only
     element its own neighbour on all six faces."""
@@ -82,6 +92,7 @@ def test_periodic_box_vs_oracle(n, luni):
     u += 0.01 * rng.standard_normal(u.shape)
     o = oracle_for(m, period=2 * PI)
     ev = ng.Evolution(m, ng.BC_EXACT_PLANEWAVE, k=(1.0, 1.0, 1.0))
+    ev.set_kernel(variant)
     assert rel_l2(ev.rhs(u), o.rhs(u)) <= RTOL_RHS
     dt = 0.25 * (2 * PI / 2 ** luni) / (n - 1) ** 2
     assert rel_l2(ev.rk4_steps_host(u, 0.0, dt, 4), o.rk4(u, dt, 4)) <= RTOL_RK4
@@ -117,3 +128,23 @@ def test_zero_steps_and_bad_arguments():
         ev.rk4_steps(0.0, 0.01, -1)
     with pytest.raises(ng.NmgError):
         ng.Evolution(m, bc=7)
+
+
+def test_autotuner_and_every_tile_shape():
+    """The autotuner times every compiled variant/tile shape; each one of
+    them must give the reference's RHS."""
+    d, meta = load("cs7_l1_n5")
+    m = build_mesh(meta)
+    perm = perm_to_mesh(m, d)
+    ev = ng.Evolution(m, ng.BC_EXACT_PLANEWAVE, k=meta["k"])
+    u = to_mesh_order(d["u0"], perm)
+    ev.rhs(u)
+    info = ev.kernel_info()
+    assert "timings" in info
+    cands = info.split("candidates:")[1].split("|")[0].split()
+    assert any(c.startswith("eo") for c in cands) and any(c.startswith("gather") for c in cands)
+    for c in cands:
+        ev.set_kernel(c)
+        assert rel_l2(ev.rhs(u)[perm], d["r0"]) <= RTOL_RHS, c
+    with pytest.raises(ng.NmgError):
+        ev.set_kernel("nonsense")
