@@ -137,6 +137,22 @@ int nmg_rk4_steps(nmg_ctx *c, double t, double dt, int32_t nsteps);
 int nmg_rk4_steps_host(nmg_ctx *c, double t, double dt, int32_t nsteps,
                        double *host_u);
 
+/* ---- allocation-free step ----------------------------------------------- */
+/* No counterpart in the reference.  For callers that cannot call cudaMalloc
+ * while they step (device memory owned by their own pool or a framework
+ * allocator, regions where the memory footprint must not grow): one RK4
+ * step from u_in_dev to u_out_dev (distinct device buffers of
+ * nmg_state_size() doubles) that allocates nothing.  Its two stage buffers
+ * live in one static device array of 2 x NMG_NOALLOC_MAX_STATE doubles
+ * (32 MiB) that every GPU loading this library holds until exit; larger
+ * states are rejected with NMG_EINVAL.  The first call on a device looks up
+ * that array (cudaGetSymbolAddress) and should come before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU race.
+ * Nothing in it needs to start at zero.  Waits for the step to finish. */
+#define NMG_NOALLOC_MAX_STATE 2097152
+int nmg_rk4_step_noalloc(nmg_ctx *c, double t, double dt, const double *u_in_dev,
+                         double *u_out_dev);
+
 /* ---- kernel selection (autotuner) --------------------------------------- */
 /* The first RHS/RK4 call of a context times every compiled variant of the
  * stage kernel ("eo": even-odd line derivatives, "gather": node-parallel dot

@@ -88,6 +88,7 @@ def lib(build_if_missing=True):
         "nmg_stream": (vp, [vp]),
         "nmg_fp64_peak": (ctypes.c_int, [vp]),
         "nmg_set_kernel": (ctypes.c_int, [vp, ctypes.c_char_p]),
+        "nmg_rk4_step_noalloc": (ctypes.c_int, [vp, f64, f64, vp, vp]),
         "nmg_kernel_info": (ctypes.c_int, [vp, vp, i32]),
     }
     for name, (res, args) in sig.items():

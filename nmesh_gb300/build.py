@@ -11,8 +11,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libnmg.so")
-SOURCES = ["nmg.cu", "stage_eo.cu", "stage_gather.cu", "mesh.cpp"]
-HEADERS = ["mesh.h", "stage.cuh", os.path.join("..", "..", "include", "nmg.h")]
+SOURCES = ["nmg.cu", "stage_eo.cu", "stage_gather.cu", "noalloc.cu", "mesh.cpp"]
+HEADERS = ["mesh.h", "stage.cuh", "ctx.h",os.path.join("..", "..", "include", "nmg.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
                      "-Xcompiler", "-fPIC,-ffp-contract=off", "-Xptxas", "-v"]

@@ -25,6 +25,7 @@
 #include <vector>
 
 #include "../../include/nmg.h"
+#include "ctx.h"
 #include "mesh.h"
 #include "stage.cuh"
 
@@ -60,6 +61,7 @@ constexpr int kMaxVariants = 16;
 // ---------------------------------------------------------------------------
 struct nmg_ctx {
   std::string err;
+  const char *err_static = nullptr;  // set instead of err by allocation-free paths
   int n = 0, np = 0, nn = 0;
   int64_t nelem = 0, ncurvi = 0, nbface = 0;
   size_t state_len = 0;
@@ -88,8 +90,47 @@ struct nmg_ctx {
 };
 
 static int set_err(nmg_ctx *c, int code, const std::string &msg) {
-  if (c) c->err = msg;
+  if (c) {
+    c->err = msg;
+    c->err_static = nullptr;
+  }
   return code;
+}
+
+static StageParams base_params(nmg_ctx *c);
+
+size_t nmg_ctx_state_len(const nmg_ctx *c) { return c->state_len; }
+
+int nmg_ctx_fail_static(nmg_ctx *c, int code, const char *msg) {
+  c->err_static = msg;
+  return code;
+}
+
+int nmg_ctx_rk4_step_buffers(nmg_ctx *c, double t, double dt, const double *u_in,
+                             double *u_out, double *s1, double *s2) {
+  const Variant &V = c->variants[c->sel >= 0 ? c->sel : 0];
+  const double cacc[4] = {dt / 6., dt / 3., dt / 3., dt / 6.};
+  const double cw[4] = {dt / 2., dt / 2., dt, 0.};
+  const double ts[4] = {t, t + 0.5 * dt, t + 0.5 * dt, t + dt};
+  const double *win[4] = {u_in, s1, s2, s1};
+  double *wout[4] = {s1, s2, s1, nullptr};
+  for (int s = 0; s < 4; s++) {
+    StageParams P = base_params(c);
+    P.win = win[s];
+    P.u0 = u_in;
+    P.acc = u_out;
+    P.wout = wout[s];
+    P.mode = s + 1;
+    P.cacc = cacc[s];
+    P.cw = cw[s];
+    P.t = ts[s];
+    cudaError_t e = V.launch(P, c->stream);
+    if (e != cudaSuccess) return nmg_ctx_fail_static(c, NMG_ECUDA, cudaGetErrorString(e));
+    c->launches++;
+  }
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return nmg_ctx_fail_static(c, NMG_ECUDA, cudaGetErrorString(e));
+  return NMG_OK;
 }
 
 #define CK(call)                                                                        \
@@ -384,7 +425,10 @@ void nmg_destroy(nmg_ctx *c) {
   delete c;
 }
 
-const char *nmg_last_error(const nmg_ctx *c) { return c ? c->err.c_str() : "null context"; }
+const char *nmg_last_error(const nmg_ctx *c) {
+  if (!c) return "null context";
+  return c->err_static ? c->err_static : c->err.c_str();
+}
 int64_t nmg_state_size(const nmg_ctx *c) { return c ? (int64_t)c->state_len : -1; }
 int64_t nmg_kernel_launches(const nmg_ctx *c) { return c ? c->launches : -1; }
 void *nmg_stream(nmg_ctx *c) { return c ? (void *)c->stream : nullptr; }
