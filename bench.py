@@ -228,6 +228,43 @@ def run_ours(args, rank, world, local):
     t_e2e = max_over_ranks(dist, t_e2e, torch.device("cuda", local))
     e2e_value = world * dof * stages / t_e2e
 
+    # adjoint cost on the same mesh and data: one transposed RK4 step, and
+    # the checkpointed gradient of J = sum_s dt sum W phi^2 over a short
+    # horizon (forward sweep + recompute + adjoint sweep)
+    adjoint = None
+    if not args.no_adjoint:
+        ev.set_state(u0)
+        lam = torch.from_numpy(u0.ravel().copy()).cuda()
+        torch.cuda.synchronize()
+        ev.rk4_step_vjp_device(lam.data_ptr(), 0.0, dt)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        nv = 5
+        for s in range(nv):
+            ev.rk4_step_vjp_device(lam.data_ptr(), 0.0, dt)
+        torch.cuda.synchronize()
+        vjp_ms = 1e3 * (time.perf_counter() - t0) / nv
+        xyz = mesh.coords()
+        r = np.linalg.norm(xyz, axis=1)
+        del xyz
+        Wt = torch.from_numpy(np.where((r >= 17.0) & (r <= 19.0), 1.0, 0.0)).cuda()
+        del r
+        g = torch.empty_like(lam)
+        nsteps_adj, ckpt = 20, 5
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        Jv = ev.adjoint_gradient_device(Wt.data_ptr(), g.data_ptr(), 0.0, dt, nsteps_adj, ckpt)
+        torch.cuda.synchronize()
+        grad_ms = 1e3 * (time.perf_counter() - t0)
+        fwd_ms = ms_max / args.steps
+        adjoint = {"vjp_step_ms": vjp_ms, "forward_step_ms": fwd_ms,
+                   "vjp_step_over_forward_step": vjp_ms / fwd_ms,
+                   "gradient": f"J = sum_s dt sum W phi^2 on the shell 17<=r<=19, "
+                               f"{nsteps_adj} RK4 steps, checkpoints every {ckpt}",
+                   "gradient_ms": grad_ms, "J": Jv,
+                   "gradient_cost_per_step_over_forward_step": grad_ms / (nsteps_adj * fwd_ms)}
+        del lam, g, Wt
+
     fp64_peak = ng.fp64_peak_gflops()
     peaks = {}
     try:
@@ -280,6 +317,7 @@ def run_ours(args, rank, world, local):
                               "peak_source": "FP64 FMA probe run live (nmg_fp64_peak)"},
             "clocks": clk,
             "cpu_baseline": cpu,
+            "adjoint": adjoint,
         }
         print(json.dumps(out))
     ev.close()
@@ -384,6 +422,7 @@ def main():
     ap.add_argument("--cpu-luni", type=int, default=3)
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

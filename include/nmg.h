@@ -137,6 +137,29 @@ int nmg_rk4_steps(nmg_ctx *c, double t, double dt, int32_t nsteps);
 int nmg_rk4_steps_host(nmg_ctx *c, double t, double dt, int32_t nsteps,
                        double *host_u);
 
+/* ---- adjoint (vector-Jacobian products) --------------------------------- */
+/* The reference has no adjoint; these are the hand-written transposes of
+ * the RHS and of the RK4 step above.  The scalar-wave RHS is linear in w, so
+ * wbar = (dRHS/dw)^T rbar does not depend on w (w_dev may be NULL) and the
+ * exterior plane-wave data (constant in w) drops out.
+ *   nmg_rhs_vjp:       wbar_dev = J^T rbar_dev (device buffers, distinct)
+ *   nmg_rk4_step_vjp:  ubar_dev <- (du_{n+1}/du_n)^T ubar_dev, in place; the
+ *                      step Jacobian is the RK4 polynomial of dt L, so this is
+ *                      an RK4 step of the transposed operator (u_n unused).
+ *   nmg_adjoint_gradient: for u0 = the context's current state,
+ *                      J = sum_{s=1..nsteps} dt sum_nodes W phi(t_s)^2
+ *                      (weight_dev: [nelem][n^3] doubles) and grad_dev =
+ *                      dJ/du0 (nmg_state_size() doubles), by the discrete
+ *                      adjoint of the trajectory with u checkpointed every
+ *                      ckpt_every steps and recomputed segment by segment in
+ *                      the reverse sweep (device memory for nsteps/ckpt_every
+ *                      + max(ckpt_every,2) + 2 states is allocated per call). */
+int nmg_rhs_vjp(nmg_ctx *c, double t, const double *w_dev, const double *rbar_dev,
+                double *wbar_dev);
+int nmg_rk4_step_vjp(nmg_ctx *c, double t, double dt, const double *u_n_dev, double *ubar_dev);
+int nmg_adjoint_gradient(nmg_ctx *c, double t0, double dt, int32_t nsteps, int32_t ckpt_every,
+                         const double *weight_dev, double *J, double *grad_dev);
+
 /* ---- allocation-free step ----------------------------------------------- */
 /* No counterpart in the reference.  For callers that cannot call cudaMalloc
  * while they step (device memory owned by their own pool or a framework

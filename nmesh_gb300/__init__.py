@@ -89,6 +89,9 @@ def lib(build_if_missing=True):
         "nmg_fp64_peak": (ctypes.c_int, [vp]),
         "nmg_set_kernel": (ctypes.c_int, [vp, ctypes.c_char_p]),
         "nmg_rk4_step_noalloc": (ctypes.c_int, [vp, f64, f64, vp, vp]),
+        "nmg_rhs_vjp": (ctypes.c_int, [vp, f64, vp, vp, vp]),
+        "nmg_rk4_step_vjp": (ctypes.c_int, [vp, f64, f64, vp, vp]),
+        "nmg_adjoint_gradient": (ctypes.c_int, [vp, f64, f64, i32, i32, vp, vp, vp]),
         "nmg_kernel_info": (ctypes.c_int, [vp, vp, i32]),
     }
     for name, (res, args) in sig.items():
@@ -260,6 +263,26 @@ class Evolution:
         self._check(lib().nmg_rk4_steps_host(self._h, float(t), float(dt), int(nsteps),
                                              _ptr(u)), "nmg_rk4_steps_host")
         return u
+
+    # ---- adjoint ----
+    def rhs_vjp_device(self, rbar_ptr, wbar_ptr, t=0.0):
+        """wbar = (dRHS/dw)^T rbar on device pointers (ints)."""
+        self._check(lib().nmg_rhs_vjp(self._h, float(t), None, ctypes.c_void_p(rbar_ptr),
+                                      ctypes.c_void_p(wbar_ptr)), "nmg_rhs_vjp")
+
+    def rk4_step_vjp_device(self, ubar_ptr, t, dt):
+        """ubar <- (du_{n+1}/du_n)^T ubar in place on a device pointer."""
+        self._check(lib().nmg_rk4_step_vjp(self._h, float(t), float(dt), None,
+                                           ctypes.c_void_p(ubar_ptr)), "nmg_rk4_step_vjp")
+
+    def adjoint_gradient_device(self, weight_ptr, grad_ptr, t0, dt, nsteps, ckpt_every):
+        """J and dJ/du0 for u0 = the current state (see include/nmg.h)."""
+        J = ctypes.c_double(0.0)
+        self._check(lib().nmg_adjoint_gradient(self._h, float(t0), float(dt), int(nsteps),
+                                               int(ckpt_every), ctypes.c_void_p(weight_ptr),
+                                               ctypes.byref(J), ctypes.c_void_p(grad_ptr)),
+                    "nmg_adjoint_gradient")
+        return J.value
 
     def set_kernel(self, spec="auto"):
         """Force a stage-kernel variant ("eo", "gather", "eo:<epb>:<threads>")

@@ -54,6 +54,49 @@ __global__ void __launch_bounds__(256) fp64_peak_kernel(double *out, int iters, 
 
 constexpr int kMaxVariants = 16;
 
+// Objective J = dt sum_nodes W phi^2 of one state, in two deterministic
+// passes: per-block partial sums (fixed-order tree), then one thread adds
+// the partials in order and accumulates dt * sum into *out.
+constexpr int kObjThreads = 256;
+__global__ void __launch_bounds__(kObjThreads)
+    obj_partial_kernel(const double *u, const double *W, int nelem, int np, double *partial) {
+  __shared__ double sh[kObjThreads];
+  double s = 0.;
+  const int64_t nn = (int64_t)nelem * np;
+  const int64_t per = (nn + gridDim.x - 1) / gridDim.x;
+  const int64_t b0 = per * blockIdx.x, b1 = min(nn, b0 + per);
+  for (int64_t q = b0 + threadIdx.x; q < b1; q += kObjThreads) {
+    const int64_t e = q / np, node = q - e * np;
+    const double phi = u[(e * NF + 4) * np + node];
+    s = fma(W[q] * phi, phi, s);
+  }
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = kObjThreads / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
+}
+
+__global__ void obj_final_kernel(const double *partial, int nblk, double dt, double *out) {
+  double s = 0.;
+  for (int b = 0; b < nblk; b++) s += partial[b];
+  *out += dt * s;
+}
+
+// adjoint source of J at one step: lambda_phi += coef W phi
+__global__ void adj_source_kernel(double *lambda, const double *u, const double *W, int nelem,
+                                  int np, double coef) {
+  const int64_t nn = (int64_t)nelem * np;
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < nn;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e = q / np, node = q - e * np;
+    const int64_t idx = (e * NF + 4) * np + node;
+    lambda[idx] = fma(coef * W[q], u[idx], lambda[idx]);
+  }
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -69,6 +112,7 @@ struct nmg_ctx {
   double k[3] = {0, 0, 0};
   cudaStream_t stream = nullptr;
   Variant variants[kMaxVariants];
+  Variant vjp;  // transposed stage kernel
   int nvariants = 0;
   int sel = -1;      // selected variant, -1: autotune on first use
   bool tuned = false;
@@ -106,9 +150,10 @@ int nmg_ctx_fail_static(nmg_ctx *c, int code, const char *msg) {
   return code;
 }
 
-int nmg_ctx_rk4_step_buffers(nmg_ctx *c, double t, double dt, const double *u_in,
-                             double *u_out, double *s1, double *s2) {
-  const Variant &V = c->variants[c->sel >= 0 ? c->sel : 0];
+// one RK4 step u_in -> u_out with explicit stage buffers s1, s2 and kernel
+// variant V (forward or transposed), enqueued on the context stream
+static int step_buffers(nmg_ctx *c, const Variant &V, double t, double dt, const double *u_in,
+                        double *u_out, double *s1, double *s2) {
   const double cacc[4] = {dt / 6., dt / 3., dt / 3., dt / 6.};
   const double cw[4] = {dt / 2., dt / 2., dt, 0.};
   const double ts[4] = {t, t + 0.5 * dt, t + 0.5 * dt, t + dt};
@@ -128,6 +173,13 @@ int nmg_ctx_rk4_step_buffers(nmg_ctx *c, double t, double dt, const double *u_in
     if (e != cudaSuccess) return nmg_ctx_fail_static(c, NMG_ECUDA, cudaGetErrorString(e));
     c->launches++;
   }
+  return NMG_OK;
+}
+
+int nmg_ctx_rk4_step_buffers(nmg_ctx *c, double t, double dt, const double *u_in,
+                             double *u_out, double *s1, double *s2) {
+  int rc = step_buffers(c, c->variants[c->sel >= 0 ? c->sel : 0], t, dt, u_in, u_out, s1, s2);
+  if (rc) return rc;
   cudaError_t e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return nmg_ctx_fail_static(c, NMG_ECUDA, cudaGetErrorString(e));
   return NMG_OK;
@@ -277,6 +329,8 @@ int nmg_create(const nmg_mesh *m, int32_t bc_kind, const double k[3], nmg_ctx **
   c->nvariants += nmgk::gather_variants(m->n, c->variants + c->nvariants,
                                         kMaxVariants - c->nvariants);
   if (c->nvariants == 0) return set_err(c, NMG_EUNSUP, "nmg_create: n must be in [2,12]");
+  if (nmgk::vjp_variants(m->n, &c->vjp, 1) != 1)
+    return set_err(c, NMG_EUNSUP, "nmg_create: no transposed kernel for this n");
   int dev = 0;
   CK(cudaGetDevice(&dev));
   const int n = m->n, np = n * n * n, nn = n * n;
@@ -407,6 +461,11 @@ int nmg_create(const nmg_mesh *m, int32_t bc_kind, const double k[3], nmg_ctx **
     StageParams P0;
     std::memset(&P0, 0, sizeof(P0));
     CK(c->variants[v].launch(P0, c->stream));  // nelem == 0: only sets the smem limit
+  }
+  {
+    StageParams P0;
+    std::memset(&P0, 0, sizeof(P0));
+    CK(c->vjp.launch(P0, c->stream));
   }
   CK(cudaDeviceSynchronize());
   return NMG_OK;
@@ -594,6 +653,138 @@ int nmg_rk4_steps_host(nmg_ctx *c, double t, double dt, int32_t nsteps, double *
   if (rc) return rc;
   CK(cudaMemcpyAsync(host_u, c->d_buf[c->cur], bytes, cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
+  return NMG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// adjoint (vector-Jacobian) entry points
+// ---------------------------------------------------------------------------
+int nmg_rhs_vjp(nmg_ctx *c, double t, const double *w_dev, const double *rbar_dev,
+                double *wbar_dev) {
+  (void)t;
+  (void)w_dev;  // the RHS is linear in w: its Jacobian does not depend on w
+  if (!c || !rbar_dev || !wbar_dev || rbar_dev == wbar_dev)
+    return set_err(c, NMG_EINVAL, "nmg_rhs_vjp: need distinct rbar and wbar device buffers");
+  StageParams P = base_params(c);
+  P.win = rbar_dev;
+  P.rout = wbar_dev;
+  P.mode = 0;
+  CK(c->vjp.launch(P, c->stream));
+  c->launches++;
+  CK(cudaStreamSynchronize(c->stream));
+  return NMG_OK;
+}
+
+int nmg_rk4_step_vjp(nmg_ctx *c, double t, double dt, const double *u_n_dev, double *ubar_dev) {
+  (void)u_n_dev;  // linear RHS: the step's Jacobian is P(dt L), independent of u_n
+  if (!c || !ubar_dev) return set_err(c, NMG_EINVAL, "nmg_rk4_step_vjp: null argument");
+  double *acc = c->d_buf[1 - c->cur];  // free between steps
+  int rc = step_buffers(c, c->vjp, t, dt, ubar_dev, acc, c->d_buf[2], c->d_buf[3]);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(ubar_dev, acc, c->state_len * sizeof(double), cudaMemcpyDeviceToDevice,
+                     c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return NMG_OK;
+}
+
+// J(u0) = sum_{s=1..nsteps} dt sum_nodes W phi(t_s)^2 and dJ/du0 by the
+// discrete adjoint of the RK4 trajectory, with u checkpointed every
+// ckpt_every steps and the states of each segment recomputed in reverse.
+int nmg_adjoint_gradient(nmg_ctx *c, double t0, double dt, int32_t nsteps, int32_t ckpt_every,
+                         const double *weight_dev, double *J, double *grad_dev) {
+  if (!c || !weight_dev || !J || !grad_dev || nsteps <= 0 || ckpt_every <= 0)
+    return set_err(c, NMG_EINVAL, "nmg_adjoint_gradient: bad argument");
+  int rc = autotune(c);
+  if (rc) return rc;
+  const Variant &F = c->variants[c->sel];
+  const size_t L = c->state_len, bytes = L * sizeof(double);
+  const int K = ckpt_every, nck = (nsteps + K - 1) / K;
+  const int np = c->np, E = (int)c->nelem;
+  const int nseg = std::max(K, 2);  // the forward sweep ping-pongs through them
+  std::vector<double *> ck(nck, nullptr), seg(nseg, nullptr);
+  double *lam[2] = {nullptr, nullptr}, *jdev = nullptr, *partial = nullptr;
+  const int nblk = 4 * 152;
+  // step times as evolve_mesh accumulates them (main.c:610-626)
+  std::vector<double> ts(nsteps + 1);
+  {
+    long double Te = t0, te = 0.;
+    for (int s = 0; s <= nsteps; s++) {
+      ts[s] = (double)(Te + te);
+      te += dt;
+    }
+  }
+  auto cleanup = [&]() {
+    for (auto p : ck) cudaFree(p);
+    for (auto p : seg) cudaFree(p);
+    cudaFree(lam[0]);
+    cudaFree(lam[1]);
+    cudaFree(jdev);
+    cudaFree(partial);
+  };
+  auto fail = [&](cudaError_t e, const char *what) {
+    cleanup();
+    return set_err(c, NMG_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+  };
+  cudaError_t e;
+  for (int i = 0; i < nck; i++)
+    if ((e = cudaMalloc((void **)&ck[i], bytes)) != cudaSuccess) return fail(e, "checkpoint");
+  for (int i = 0; i < nseg; i++)
+    if ((e = cudaMalloc((void **)&seg[i], bytes)) != cudaSuccess) return fail(e, "segment");
+  for (int i = 0; i < 2; i++)
+    if ((e = cudaMalloc((void **)&lam[i], bytes)) != cudaSuccess) return fail(e, "adjoint");
+  if ((e = cudaMalloc((void **)&jdev, sizeof(double))) != cudaSuccess) return fail(e, "J");
+  if ((e = cudaMalloc((void **)&partial, nblk * sizeof(double))) != cudaSuccess)
+    return fail(e, "partials");
+  cudaStream_t st = c->stream;
+  double *WA = c->d_buf[2], *WB = c->d_buf[3];
+  // forward sweep: J and the checkpoints
+  cudaMemsetAsync(jdev, 0, sizeof(double), st);
+  cudaMemcpyAsync(ck[0], c->d_buf[c->cur], bytes, cudaMemcpyDeviceToDevice, st);
+  {
+    const double *u = ck[0];
+    for (int s = 1; s <= nsteps; s++) {
+      double *out = seg[(s - 1) % nseg];
+      if ((rc = step_buffers(c, F, ts[s - 1], dt, u, out, WA, WB))) { cleanup(); return rc; }
+      obj_partial_kernel<<<nblk, kObjThreads, 0, st>>>(out, weight_dev, E, np, partial);
+      obj_final_kernel<<<1, 1, 0, st>>>(partial, nblk, dt, jdev);
+      c->launches += 2;
+      if (s % K == 0 && s / K < nck)
+        cudaMemcpyAsync(ck[s / K], out, bytes, cudaMemcpyDeviceToDevice, st);
+      u = out;
+    }
+  }
+  // reverse sweep
+  cudaMemsetAsync(lam[0], 0, bytes, st);
+  int li = 0;
+  for (int cidx = nck - 1; cidx >= 0; cidx--) {
+    const int s0 = cidx * K, s1 = std::min(nsteps, s0 + K);
+    const double *u = ck[cidx];
+    for (int s = s0 + 1; s <= s1; s++) {  // recompute u_{s0+1..s1}
+      if ((rc = step_buffers(c, F, ts[s - 1], dt, u, seg[s - s0 - 1], WA, WB))) {
+        cleanup();
+        return rc;
+      }
+      u = seg[s - s0 - 1];
+    }
+    for (int s = s1; s > s0; s--) {
+      adj_source_kernel<<<nblk, 256, 0, st>>>(lam[li], seg[s - s0 - 1], weight_dev, E, np,
+                                              2.0 * dt);
+      if ((rc = step_buffers(c, c->vjp, ts[s - 1], dt, lam[li], lam[1 - li], WA, WB))) {
+        cleanup();
+        return rc;
+      }
+      c->launches++;
+      li = 1 - li;
+    }
+  }
+  cudaMemcpyAsync(grad_dev, lam[li], bytes, cudaMemcpyDeviceToDevice, st);
+  double Jh = 0.;
+  cudaMemcpyAsync(&Jh, jdev, sizeof(double), cudaMemcpyDeviceToHost, st);
+  e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return fail(e, "nmg_adjoint_gradient");
+  if ((e = cudaGetLastError()) != cudaSuccess) return fail(e, "nmg_adjoint_gradient launch");
+  *J = Jh;
+  cleanup();
   return NMG_OK;
 }
 

@@ -208,6 +208,8 @@ struct Variant {
 // all compiled variants for n (returns count, fills out[])
 int gather_variants(int n, Variant *out, int cap);
 int eo_variants(int n, Variant *out, int cap);
+// transposed (vector-Jacobian) stage kernel for n
+int vjp_variants(int n, Variant *out, int cap);
 // even-odd coefficients of D for n into constant memory
 cudaError_t eo_upload(int n, const double *D);
 

@@ -22,11 +22,12 @@ namespace nmgk {
 namespace {
 
 constexpr int MMAX = NMAX / 2;
-__constant__ double cEA[NMAX + 1][MMAX][MMAX + 1];  // A_ij, j < m; A_im = D_ic (odd n)
-__constant__ double cEB[NMAX + 1][MMAX][MMAX];      // B_ij
-__constant__ double cEC[NMAX + 1][MMAX];            // middle row (odd n): B_cj
+// [0]: coefficients of D, [1]: of its transpose (also centro-antisymmetric)
+__constant__ double cEA[2][NMAX + 1][MMAX][MMAX + 1];  // A_ij, j < m; A_im = D_ic (odd n)
+__constant__ double cEB[2][NMAX + 1][MMAX][MMAX];      // B_ij
+__constant__ double cEC[2][NMAX + 1][MMAX];            // middle row (odd n): B_cj
 
-template <int N>
+template <int N, int TR>
 __device__ __forceinline__ void line_deriv(const double *__restrict__ s, int st, double *out) {
   constexpr int M = N / 2;
   constexpr bool ODD = (N & 1) != 0;
@@ -40,19 +41,19 @@ __device__ __forceinline__ void line_deriv(const double *__restrict__ s, int st,
   const double uc = ODD ? s[M * st] : 0.;
 #pragma unroll
   for (int i = 0; i < M; i++) {
-    double S = ODD ? cEA[N][i][M] * uc : cEA[N][i][0] * e[0];
-    double T = cEB[N][i][0] * o[0];
+    double S = ODD ? cEA[TR][N][i][M] * uc : cEA[TR][N][i][0] * e[0];
+    double T = cEB[TR][N][i][0] * o[0];
 #pragma unroll
-    for (int j = ODD ? 0 : 1; j < M; j++) S = fma(cEA[N][i][j], e[j], S);
+    for (int j = ODD ? 0 : 1; j < M; j++) S = fma(cEA[TR][N][i][j], e[j], S);
 #pragma unroll
-    for (int j = 1; j < M; j++) T = fma(cEB[N][i][j], o[j], T);
+    for (int j = 1; j < M; j++) T = fma(cEB[TR][N][i][j], o[j], T);
     out[i] = S + T;
     out[N - 1 - i] = T - S;
   }
   if (ODD) {
-    double c = cEC[N][0] * o[0];
+    double c = cEC[TR][N][0] * o[0];
 #pragma unroll
-    for (int j = 1; j < M; j++) c = fma(cEC[N][j], o[j], c);
+    for (int j = 1; j < M; j++) c = fma(cEC[TR][N][j], o[j], c);
     out[M] = c;
   }
 }
@@ -109,7 +110,7 @@ __global__ void __launch_bounds__(NT) eo_kernel(StageParams P) {
       const int l0 = L % N, l1 = L / N;
       const int base = a == 0 ? N * (l0 + N * l1) : (a == 1 ? l0 + NN * l1 : l0 + N * l1);
       double out[N];
-      line_deriv<N>(sW + (fld * EPB + le) * NP + base, st, out);
+      line_deriv<N, 0>(sW + (fld * EPB + le) * NP + base, st, out);
       const int cs = sCs[le];
       const int row = (sMask[le] >> (3 * a)) & 7;
       if (fld == 0) {
@@ -164,6 +165,244 @@ cudaError_t launch_eo(const StageParams &P, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// Transposed stage kernel (vector-Jacobian product).  The scalar-wave RHS is
+// linear in w, r = L w (+ exterior plane-wave data that does not depend on
+// w), so its VJP is wbar = L^T rbar, evaluated here from `win` = rbar:
+//   volume  pibar  = sum_a D_a^T (sum_i M[a][i] rbar_c_i),
+//           cbar_i = sum_a D_a^T (M[a][i] rbar_pi),   pibar += rbar_phi;
+//   faces   for face node x of element e with neighbour node y of e':
+//           pibar_x -= g_x rbar_pi(x) + gn_x . rbar_c(x)
+//           cbar_x  -= gn_x rbar_pi(x) + g_x rbar_c(x)
+//           pibar_x += g_y rbar_pi(y) + gn_y . rbar_c(y)     (y's lift
+//           cbar_x  += gn_y rbar_pi(y) + g_y rbar_c(y)        depends on x)
+//   outgoing outer faces (r += -g s (1, n), s = pi + c.n):
+//           pibar_x -= g sb, cbar_x -= g sb n, sb = rbar_pi + n . rbar_c.
+// Every contribution is gathered by the node that receives it, so there
+// are no atomics and the result is deterministic.  D^T is centro-
+// antisymmetric too, so the even-odd line transform applies unchanged.
+template <int N, int EPB, int NT>
+__global__ void __launch_bounds__(NT) vjp_kernel(StageParams P) {
+  constexpr int NP = N * N * N, NN = N * N;
+  extern __shared__ double smem[];
+  double *sW = smem;                 // [4][EPB][NP]: rbar pi, c (from win)
+  double *sR = smem + 4 * EPB * NP;  // [4][EPB][NP]: wbar pi, c
+  __shared__ int sCs[EPB];
+  __shared__ int sMask[EPB];
+  __shared__ double sScale[EPB][3];
+  __shared__ double sG[EPB][3];
+  __shared__ unsigned char sPair[3][4 * EPB];
+  __shared__ int sNPair[3];
+
+  const int e0 = blockIdx.x * EPB;
+  const int tid = threadIdx.x;
+  for (int q = tid; q < EPB; q += NT) {
+    const int e = e0 + q;
+    const int cs = (e < P.nelem) ? P.cslot[e] : -1;
+    sCs[q] = cs;
+    sMask[q] = (e >= P.nelem) ? 0 : (cs >= 0 ? P.cmask[cs] : (1 | (1 << 4) | (1 << 8)));
+    for (int d = 0; d < 3; d++) sScale[q][d] = (e < P.nelem) ? P.scale[e * 3 + d] : 0.;
+    for (int d = 0; d < 3; d++) sG[q][d] = (e < P.nelem) ? P.gcart[e * 3 + d] : 0.;
+  }
+  for (int q = tid; q < 4 * EPB * NP; q += NT) sR[q] = 0.;
+  stage_in<N, EPB, NT>(P, sW, e0);
+  __syncthreads();
+  if (tid < 3) {
+    const int a = tid;
+    int np = 0;
+    for (int le = 0; le < EPB; le++) {
+      const int row = (sMask[le] >> (3 * a)) & 7;
+      if (!row) continue;
+      sPair[a][np++] = (unsigned char)(le * 4 + 0);
+      for (int i = 0; i < 3; i++)
+        if (row & (1 << i)) sPair[a][np++] = (unsigned char)(le * 4 + 1 + i);
+    }
+    sNPair[a] = np;
+  }
+  __syncthreads();
+
+  // ---- transposed volume terms, one direction per pass ----
+#pragma unroll 1
+  for (int a = 0; a < 3; a++) {
+    const int ntask = sNPair[a] * NN;
+    const int st = a == 0 ? 1 : (a == 1 ? N : NN);
+    for (int q = tid; q < ntask; q += NT) {
+      const int p = q / NN, L = q - p * NN;
+      const int pr = sPair[a][p], le = pr >> 2, fld = pr & 3;
+      const int l0 = L % N, l1 = L / N;
+      const int base = a == 0 ? N * (l0 + N * l1) : (a == 1 ? l0 + NN * l1 : l0 + N * l1);
+      const int cs = sCs[le];
+      const int row = (sMask[le] >> (3 * a)) & 7;
+      double y[N], out[N];
+      if (fld == 0) {
+        // y = sum_i M[a][i] rbar_c_i along the line
+#pragma unroll
+        for (int qq = 0; qq < N; qq++) y[qq] = 0.;
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+          if (!(row & (1 << i))) continue;
+          const double *rc = sW + ((1 + i) * EPB + le) * NP + base;
+          if (cs < 0) {
+            const double s = sScale[le][a];
+#pragma unroll
+            for (int qq = 0; qq < N; qq++) y[qq] = fma(s, rc[qq * st], y[qq]);
+          } else {
+            const double *Mp = P.metricp + (((size_t)cs * 3 + a) * 3 + i) * N * NN + L;
+#pragma unroll
+            for (int qq = 0; qq < N; qq++) y[qq] = fma(__ldg(Mp + qq * NN), rc[qq * st], y[qq]);
+          }
+        }
+      } else {
+        const int i = fld - 1;
+        const double *rp = sW + (0 * EPB + le) * NP + base;
+        if (cs < 0) {
+          const double s = sScale[le][a];
+#pragma unroll
+          for (int qq = 0; qq < N; qq++) y[qq] = s * rp[qq * st];
+        } else {
+          const double *Mp = P.metricp + (((size_t)cs * 3 + a) * 3 + i) * N * NN + L;
+#pragma unroll
+          for (int qq = 0; qq < N; qq++) y[qq] = __ldg(Mp + qq * NN) * rp[qq * st];
+        }
+      }
+      line_deriv<N, 1>(y, 1, out);
+      double *r = sR + (fld * EPB + le) * NP + base;
+#pragma unroll
+      for (int qq = 0; qq < N; qq++) r[qq * st] += out[qq];
+    }
+    __syncthreads();
+  }
+
+  // ---- transposed face terms, one direction at a time ----
+#pragma unroll 1
+  for (int d = 0; d < 3; d++) {
+    for (int q = tid; q < EPB * 2 * NN; q += NT) {
+      const int le = q / (2 * NN), rem = q - le * 2 * NN, s = rem / NN, ab = rem - s * NN;
+      const int e = e0 + le;
+      if (e >= P.nelem) continue;
+      const int a = ab % N, b = ab / N, f = 2 * d + s;
+      const int node = face_node_d<N>(f, a, b);
+      const double rp = sW[(0 * EPB + le) * NP + node];
+      const double rc0 = sW[(1 * EPB + le) * NP + node];
+      const double rc1 = sW[(2 * EPB + le) * NP + node];
+      const double rc2 = sW[(3 * EPB + le) * NP + node];
+      double gn0, gn1, gn2, g;
+      const int cs = sCs[le];
+      if (cs < 0) {
+        g = sG[le][d];
+        const double sg = (f & 1) ? g : -g;
+        gn0 = d == 0 ? sg : 0.;
+        gn1 = d == 1 ? sg : 0.;
+        gn2 = d == 2 ? sg : 0.;
+      } else {
+        const double2 *F2 = reinterpret_cast<const double2 *>(P.fac) +
+                            (((size_t)cs * 6 + f) * NN + ab) * 2;
+        const double2 fa = __ldg(F2), fb = __ldg(F2 + 1);
+        gn0 = fa.x; gn1 = fa.y; gn2 = fb.x; g = fb.y;
+      }
+      double dp, dc0, dc1, dc2;
+      const int nbe = __ldg(P.nb + e * 6 + f);
+      if (nbe >= 0 || P.bc == NMG_BC_EXACT_PLANEWAVE) {
+        dp = -fma(g, rp, fma(gn0, rc0, fma(gn1, rc1, gn2 * rc2)));
+        dc0 = -fma(gn0, rp, g * rc0);
+        dc1 = -fma(gn1, rp, g * rc1);
+        dc2 = -fma(gn2, rp, g * rc2);
+        if (nbe >= 0) {
+          const int cd = __ldg(P.code + e * 6 + f), f2 = cd & 7, o = cd >> 3;
+          const int sw = o & 1, fa = (o >> 1) & 1, fb = (o >> 2) & 1;
+          int aa = sw ? b : a, bb = sw ? a : b;
+          aa = fa ? N - 1 - aa : aa;
+          bb = fb ? N - 1 - bb : bb;
+          const double *W2 = P.win + (size_t)nbe * NF * NP + face_node_d<N>(f2, aa, bb);
+          const double yp = __ldg(W2), yc0 = __ldg(W2 + NP), yc1 = __ldg(W2 + 2 * NP),
+                       yc2 = __ldg(W2 + 3 * NP);
+          double hn0, hn1, hn2, h;
+          const int cs2 = __ldg(P.cslot + nbe);
+          if (cs2 < 0) {
+            const int d2 = f2 >> 1;
+            h = __ldg(P.gcart + nbe * 3 + d2);
+            const double sg = (f2 & 1) ? h : -h;
+            hn0 = d2 == 0 ? sg : 0.;
+            hn1 = d2 == 1 ? sg : 0.;
+            hn2 = d2 == 2 ? sg : 0.;
+          } else {
+            const double2 *F2 = reinterpret_cast<const double2 *>(P.fac) +
+                                (((size_t)cs2 * 6 + f2) * NN + aa + N * bb) * 2;
+            const double2 fa2 = __ldg(F2), fb2 = __ldg(F2 + 1);
+            hn0 = fa2.x; hn1 = fa2.y; hn2 = fb2.x; h = fb2.y;
+          }
+          dp += fma(h, yp, fma(hn0, yc0, fma(hn1, yc1, hn2 * yc2)));
+          dc0 += fma(hn0, yp, h * yc0);
+          dc1 += fma(hn1, yp, h * yc1);
+          dc2 += fma(hn2, yp, h * yc2);
+        }
+      } else {
+        // outgoing radiation
+        const int bs = __ldg(P.bslot + e * 6 + f);
+        const double *Nr = P.bnrm + (size_t)bs * 3 * NN + ab;
+        const double n0 = Nr[0], n1 = Nr[NN], n2 = Nr[2 * NN];
+        const double gsb = g * fma(n0, rc0, fma(n1, rc1, fma(n2, rc2, rp)));
+        dp = -gsb;
+        dc0 = -gsb * n0;
+        dc1 = -gsb * n1;
+        dc2 = -gsb * n2;
+      }
+      sR[(0 * EPB + le) * NP + node] += dp;
+      sR[(1 * EPB + le) * NP + node] += dc0;
+      sR[(2 * EPB + le) * NP + node] += dc1;
+      sR[(3 * EPB + le) * NP + node] += dc2;
+    }
+    __syncthreads();
+  }
+
+  // ---- epilogue: wbar = (pibar + rbar_phi, cbar, 0) ----
+  for (int q = tid; q < EPB * NF * NP; q += NT) {
+    const int le = q / (NF * NP), rem = q - le * NF * NP, f = rem / NP, node = rem - f * NP;
+    const int e = e0 + le;
+    if (e >= P.nelem) continue;
+    const size_t idx = ((size_t)e * NF + f) * NP + node;
+    double r;
+    if (f == 0)
+      r = sR[le * NP + node] + __ldg(P.win + ((size_t)e * NF + 4) * NP + node);
+    else if (f < 4)
+      r = sR[(f * EPB + le) * NP + node];
+    else
+      r = 0.;
+    if (P.mode == 0) {
+      P.rout[idx] = r;
+    } else if (P.mode == 1) {
+      const double u = __ldg(P.u0 + idx);
+      P.acc[idx] = fma(P.cacc, r, u);
+      P.wout[idx] = fma(P.cw, r, u);
+    } else if (P.mode == 4) {
+      P.acc[idx] = fma(P.cacc, r, P.acc[idx]);
+    } else {
+      P.acc[idx] = fma(P.cacc, r, P.acc[idx]);
+      P.wout[idx] = fma(P.cw, r, __ldg(P.u0 + idx));
+    }
+  }
+}
+
+template <int N, int EPB, int NT>
+cudaError_t launch_vjp(const StageParams &P, cudaStream_t st) {
+  constexpr int NP = N * N * N;
+  const size_t shmem = sizeof(double) * 8 * EPB * NP;
+  if (P.nelem <= 0)
+    return cudaFuncSetAttribute(vjp_kernel<N, EPB, NT>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shmem);
+  vjp_kernel<N, EPB, NT><<<(P.nelem + EPB - 1) / EPB, NT, shmem, st>>>(P);
+  return cudaGetLastError();
+}
+
+template <int N>
+int add_vjp(Variant *out, int cap) {
+  constexpr int NN = N * N;
+  constexpr int E1 = (128 / (2 * NN)) > 1 ? (128 / (2 * NN)) : 1;
+  if (cap < 1) return 0;
+  out[0] = Variant{"vjp", E1, 256, launch_vjp<N, E1, 256>};
+  return 1;
+}
+
 constexpr size_t kSmemMax = 220 * 1024;
 
 template <int N, int EPB, int NT>
@@ -204,23 +443,48 @@ int eo_variants(int n, Variant *out, int cap) {
   }
 }
 
+int vjp_variants(int n, Variant *out, int cap) {
+  switch (n) {
+    case 2: return add_vjp<2>(out, cap);
+    case 3: return add_vjp<3>(out, cap);
+    case 4: return add_vjp<4>(out, cap);
+    case 5: return add_vjp<5>(out, cap);
+    case 6: return add_vjp<6>(out, cap);
+    case 7: return add_vjp<7>(out, cap);
+    case 8: return add_vjp<8>(out, cap);
+    case 9: return add_vjp<9>(out, cap);
+    case 10: return add_vjp<10>(out, cap);
+    case 11: return add_vjp<11>(out, cap);
+    case 12: return add_vjp<12>(out, cap);
+    default: return 0;
+  }
+}
+
 cudaError_t eo_upload(int n, const double *D) {
   if (n < 2 || n > NMAX) return cudaErrorInvalidValue;
   const int m = n / 2, odd = n & 1, c = n / 2;
-  double A[MMAX][MMAX + 1] = {}, B[MMAX][MMAX] = {}, C[MMAX] = {};
-  for (int i = 0; i < m; i++) {
-    for (int j = 0; j < m; j++) {
-      A[i][j] = 0.5 * (D[i * n + j] + D[i * n + (n - 1 - j)]);
-      B[i][j] = 0.5 * (D[i * n + j] - D[i * n + (n - 1 - j)]);
+  double Dt[NMAX * NMAX];
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++) Dt[i * n + j] = D[j * n + i];
+  for (int tr = 0; tr < 2; tr++) {
+    const double *X = tr ? Dt : D;
+    double A[MMAX][MMAX + 1] = {}, B[MMAX][MMAX] = {}, C[MMAX] = {};
+    for (int i = 0; i < m; i++) {
+      for (int j = 0; j < m; j++) {
+        A[i][j] = 0.5 * (X[i * n + j] + X[i * n + (n - 1 - j)]);
+        B[i][j] = 0.5 * (X[i * n + j] - X[i * n + (n - 1 - j)]);
+      }
+      if (odd) A[i][m] = X[i * n + c];
     }
-    if (odd) A[i][m] = D[i * n + c];
+    if (odd)
+      for (int j = 0; j < m; j++) C[j] = 0.5 * (X[c * n + j] - X[c * n + (n - 1 - j)]);
+    const size_t slot = (size_t)tr * (NMAX + 1) + n;
+    cudaError_t e;
+    if ((e = cudaMemcpyToSymbol(cEA, A, sizeof(A), sizeof(A) * slot)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyToSymbol(cEB, B, sizeof(B), sizeof(B) * slot)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyToSymbol(cEC, C, sizeof(C), sizeof(C) * slot)) != cudaSuccess) return e;
   }
-  if (odd)
-    for (int j = 0; j < m; j++) C[j] = 0.5 * (D[c * n + j] - D[c * n + (n - 1 - j)]);
-  cudaError_t e;
-  if ((e = cudaMemcpyToSymbol(cEA, A, sizeof(A), sizeof(A) * n)) != cudaSuccess) return e;
-  if ((e = cudaMemcpyToSymbol(cEB, B, sizeof(B), sizeof(B) * n)) != cudaSuccess) return e;
-  return cudaMemcpyToSymbol(cEC, C, sizeof(C), sizeof(C) * n);
+  return cudaSuccess;
 }
 
 }  // namespace nmgk
