@@ -265,6 +265,13 @@ def run_ours(args, rank, world, local):
                    "gradient_cost_per_step_over_forward_step": grad_ms / (nsteps_adj * fwd_ms)}
         del lam, g, Wt
 
+    kinfo = ev.kernel_info()
+    state_bytes = int(ev.size * 8)
+    batched = None
+    if not args.no_batched and rank == 0:
+        ev.close()  # free the workload's buffers for the batch of problems
+        batched = batched_bench(args)
+
     fp64_peak = ng.fp64_peak_gflops()
     peaks = {}
     try:
@@ -275,7 +282,7 @@ def run_ours(args, rank, world, local):
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     per_launch_ms = ms / stages
     alg_bytes = alg_bytes_per_stage(mesh.nelem, ncurvi, n)
-    variant = ev.kernel_info().split(" | ")[0]
+    variant = kinfo.split(" | ")[0]
     flops, fp64_ins = fp64_work_per_stage(variant, mesh.nelem, ncurvi, n)
     achieved_gbs = alg_bytes / (per_launch_ms / 1e3) / 1e9
     achieved_gflops = flops / (per_launch_ms / 1e3) / 1e9
@@ -298,16 +305,16 @@ def run_ours(args, rank, world, local):
             "data": "synthetic (seeded Gaussian pulses on the generated mesh)",
             "config": dict(cfg, parallelism=f"replicas x{world}"),
             "e2e": {"value": e2e_value, "unit": UNIT,
-                    "h2d_bytes_per_step": int(ev.size * 8),
-                    "d2h_bytes_per_step": int(ev.size * 8)},
+                    "h2d_bytes_per_step": state_bytes,
+                    "d2h_bytes_per_step": state_bytes},
             "gpu_launches": int(launches),
             "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak,
                          "unit": "GB/s", "frac": achieved_gbs / hbm_peak,
                          "traffic": traffic,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
                          "alg_bytes_per_launch": alg_bytes,
-                         "kernel": ev.kernel_info().split(" | ")[0],
-                         "autotune": ev.kernel_info().split(" | timings: ")[-1],
+                         "kernel": kinfo.split(" | ")[0],
+                         "autotune": kinfo.split(" | timings: ")[-1],
                          "launch_ms": per_launch_ms},
             "roofline_fp64": {"bound": "fp64", "achieved": achieved_gflops, "peak": fp64_peak,
                               "unit": "GFLOP/s", "frac": achieved_gflops / fp64_peak,
@@ -318,11 +325,100 @@ def run_ours(args, rank, world, local):
             "clocks": clk,
             "cpu_baseline": cpu,
             "adjoint": adjoint,
+            "batched": batched,
         }
         print(json.dumps(out))
     ev.close()
     if dist:
         dist.destroy_process_group()
+
+
+def batch_problem_specs(count, seed=4242):
+    """Seeded set of independent problems: element counts log-uniform in
+    [64, 32768] (realised by the nearest box (8^L) or 7-cubed-sphere (7*8^L)
+    mesh), orders N uniform in {3..9} (n = N+1 nodes)."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    opts = [("box", L, 8 ** L) for L in range(2, 6)] + \
+        [("cs7", L, 7 * 8 ** L) for L in range(1, 5)]
+    for _ in range(count):
+        target = np.exp(rng.uniform(np.log(64), np.log(32768)))
+        kind, L, E = min(opts, key=lambda o: abs(np.log(o[2]) - np.log(target)))
+        n = int(rng.integers(3, 10)) + 1
+        specs.append((kind, L, n, E))
+    return specs
+
+
+def batched_bench(args):
+    """Batched persistent execution of many independent problems (one launch
+    per RK4 stage for all of them, graph-captured) against the same problems
+    stepped one after the other through their own contexts (4 launches per
+    problem and step)."""
+    import torch
+    import nmesh_gb300 as ng
+    specs = batch_problem_specs(args.batch_problems)
+    meshes = []
+    for kind, L, n, E in specs:
+        if kind == "box":
+            meshes.append(ng.Mesh.build(ng.MESH_BOX, n=n, luni=L, xc=(PI, PI, PI),
+                                        box_dout=PI, periodic=True))
+        else:
+            meshes.append(ng.Mesh.build(ng.MESH_CUBEDSPHERES7, n=n, luni=L, cs_dc=1.0,
+                                        cs_r0fac=20.0))
+    rng = np.random.default_rng(7)
+    states = [1e-3 * rng.standard_normal((m.nelem, NFIELDS, m.np)) for m in meshes]
+    dof = sum(m.nelem * m.np * NFIELDS for m in meshes)
+    dt, K = 1e-4, args.batch_steps
+    b = ng.Batch(meshes, ng.BC_OUTGOING)
+    for p, u in enumerate(states):
+        b.set_state(p, u)
+    b.rk4_steps(0.0, dt, 2)  # autotune + graph capture + warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b.rk4_steps(2 * dt, dt, K)
+    torch.cuda.synchronize()
+    t_batch = time.perf_counter() - t0
+    info = b.info()
+    b.close()
+    evs = []
+    for m, u in zip(meshes, states):
+        ev = ng.Evolution(m, ng.BC_OUTGOING)
+        ev.set_state(u)
+        ev.rk4_step(0.0, dt)  # autotune + warm-up
+        evs.append(ev)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for s in range(K):
+        for ev in evs:
+            ev.rk4_step((2 + s) * dt, dt)
+    torch.cuda.synchronize()
+    t_plain = time.perf_counter() - t0
+    for ev in evs:
+        ev.rk4_steps(0.0, dt, 1)  # per-problem graphs captured
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for ev in evs:
+        ev.rk4_steps(0.0, dt, K)
+    torch.cuda.synchronize()
+    t_graphs = time.perf_counter() - t0
+    for ev in evs:
+        ev.close()
+    nelem = [m.nelem for m in meshes]
+    return {"problems": len(meshes), "elements": int(sum(nelem)), "dof": int(dof),
+            "orders_n": sorted(set(int(m.n) for m in meshes)),
+            "element_counts_min_max": [int(min(nelem)), int(max(nelem))],
+            "steps": K,
+            "batched_dof_stage_per_s": dof * 4 * K / t_batch,
+            "plain_dof_stage_per_s": dof * 4 * K / t_plain,
+            "per_problem_graphs_dof_stage_per_s": dof * 4 * K / t_graphs,
+            "speedup_vs_plain_launches": t_plain / t_batch,
+            "speedup_vs_per_problem_graphs": t_graphs / t_batch,
+            "batch_info": info,
+            "note": "orders are per problem (faces between elements of different n or "
+                    "level are not conforming); all problems share dt"}
+
+
+PI = 3.141592653589793
 
 
 def cpu_mesh(n, luni):
@@ -423,6 +519,9 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--batch-problems", type=int, default=64)
+    ap.add_argument("--batch-steps", type=int, default=5)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

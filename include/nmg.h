@@ -137,6 +137,32 @@ int nmg_rk4_steps(nmg_ctx *c, double t, double dt, int32_t nsteps);
 int nmg_rk4_steps_host(nmg_ctx *c, double t, double dt, int32_t nsteps,
                        double *host_u);
 
+/* ---- batched execution of many independent problems --------------------- */
+/* The reference runs one mesh per process; these run many independent
+ * problems (each its own mesh and order n in [2,10]) together.  Problems of
+ * the same order are merged into one mesh (nmg_mesh_concat); one persistent
+ * kernel launch per RK4 stage walks the element tiles of all orders
+ * (runtime dispatch to the order's kernel body, highest order first), and
+ * one RK4 step (4 launches + a step counter) is captured in a CUDA graph.
+ * The persistent grid size is chosen by timing (autotuner).  All problems
+ * share t, dt and the boundary kind. */
+typedef struct nmg_batch nmg_batch;
+int nmg_mesh_concat(const nmg_mesh *const *meshes, int32_t count, nmg_mesh **out);
+int nmg_batch_create(const nmg_mesh *const *meshes, int32_t count, int32_t bc_kind,
+                     const double k[3], nmg_batch **out);
+void nmg_batch_destroy(nmg_batch *b);
+const char *nmg_batch_last_error(const nmg_batch *b);
+int64_t nmg_batch_problem_size(const nmg_batch *b, int32_t p); /* doubles of problem p */
+int nmg_batch_set_state(nmg_batch *b, int32_t p, const double *host_u);
+int nmg_batch_get_state(nmg_batch *b, int32_t p, double *host_u);
+/* nsteps RK4 steps of every problem (== evolve_RK4_mesh on each mesh) */
+int nmg_rk4_steps_batched(nmg_batch *b, double t, double dt, int32_t nsteps);
+int nmg_batch_info(nmg_batch *b, char *buf, int32_t len);
+/* 0: the autotuner chooses (default); 1: persistent single launch only;
+   2: one launch per order (each with its order's tuned kernel variant) */
+int nmg_batch_set_mode(nmg_batch *b, int32_t mode);
+void *nmg_batch_stream(nmg_batch *b);
+
 /* ---- adjoint (vector-Jacobian products) --------------------------------- */
 /* The reference has no adjoint; these are the hand-written transposes of
  * the RHS and of the RK4 step above.  The scalar-wave RHS is linear in w, so

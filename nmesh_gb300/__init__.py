@@ -89,6 +89,17 @@ def lib(build_if_missing=True):
         "nmg_fp64_peak": (ctypes.c_int, [vp]),
         "nmg_set_kernel": (ctypes.c_int, [vp, ctypes.c_char_p]),
         "nmg_rk4_step_noalloc": (ctypes.c_int, [vp, f64, f64, vp, vp]),
+        "nmg_mesh_concat": (ctypes.c_int, [vp, i32, vp]),
+        "nmg_batch_create": (ctypes.c_int, [vp, i32, i32, vp, vp]),
+        "nmg_batch_destroy": (None, [vp]),
+        "nmg_batch_last_error": (ctypes.c_char_p, [vp]),
+        "nmg_batch_problem_size": (i64, [vp, i32]),
+        "nmg_batch_set_state": (ctypes.c_int, [vp, i32, vp]),
+        "nmg_batch_get_state": (ctypes.c_int, [vp, i32, vp]),
+        "nmg_rk4_steps_batched": (ctypes.c_int, [vp, f64, f64, i32]),
+        "nmg_batch_info": (ctypes.c_int, [vp, vp, i32]),
+        "nmg_batch_stream": (vp, [vp]),
+        "nmg_batch_set_mode": (ctypes.c_int, [vp, i32]),
         "nmg_rhs_vjp": (ctypes.c_int, [vp, f64, vp, vp, vp]),
         "nmg_rk4_step_vjp": (ctypes.c_int, [vp, f64, f64, vp, vp]),
         "nmg_adjoint_gradient": (ctypes.c_int, [vp, f64, f64, i32, i32, vp, vp, vp]),
@@ -310,6 +321,68 @@ class Evolution:
     def close(self):
         if getattr(self, "_h", None) and self._h.value:
             lib().nmg_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Many independent problems stepped together (nmg_batch_*)."""
+
+    def __init__(self, meshes, bc=BC_OUTGOING, k=(1.0, 1.0, 1.0)):
+        self.meshes = list(meshes)
+        arr = (ctypes.c_void_p * len(self.meshes))(*[m._h.value for m in self.meshes])
+        kk = np.ascontiguousarray(k, np.float64)
+        h = ctypes.c_void_p()
+        rc = lib().nmg_batch_create(arr, len(self.meshes), int(bc), _ptr(kk), ctypes.byref(h))
+        self._h = h
+        if rc:
+            msg = lib().nmg_batch_last_error(h).decode() if h.value else ""
+            self.close()
+            raise NmgError(f"nmg_batch_create failed ({rc}): {msg}")
+
+    def _check(self, rc, what):
+        if rc:
+            raise NmgError(f"{what} failed ({rc}): {lib().nmg_batch_last_error(self._h).decode()}")
+
+    def shape(self, p):
+        m = self.meshes[p]
+        return (m.nelem, NFIELDS, m.np)
+
+    def set_state(self, p, u):
+        u = np.ascontiguousarray(u, np.float64)
+        assert u.size == lib().nmg_batch_problem_size(self._h, p)
+        self._check(lib().nmg_batch_set_state(self._h, p, _ptr(u)), "nmg_batch_set_state")
+
+    def get_state(self, p):
+        u = np.zeros(self.shape(p))
+        self._check(lib().nmg_batch_get_state(self._h, p, _ptr(u)), "nmg_batch_get_state")
+        return u
+
+    def rk4_steps(self, t, dt, nsteps):
+        self._check(lib().nmg_rk4_steps_batched(self._h, float(t), float(dt), int(nsteps)),
+                    "nmg_rk4_steps_batched")
+
+    def set_mode(self, mode):
+        """0 autotune, 1 persistent single launch, 2 one launch per order."""
+        self._check(lib().nmg_batch_set_mode(self._h, int(mode)), "nmg_batch_set_mode")
+
+    def info(self):
+        buf = ctypes.create_string_buffer(8192)
+        lib().nmg_batch_info(self._h, ctypes.cast(buf, ctypes.c_void_p), 8192)
+        return buf.value.decode()
+
+    @property
+    def stream(self):
+        return int(lib().nmg_batch_stream(self._h) or 0)
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            lib().nmg_batch_destroy(self._h)
             self._h = ctypes.c_void_p()
 
     def __del__(self):

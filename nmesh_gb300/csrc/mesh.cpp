@@ -606,4 +606,40 @@ int nmg_mesh_get_faces(const nmg_mesh *m, int32_t *nb, int32_t *code) {
 
 void nmg_mesh_free(nmg_mesh *m) { delete m; }
 
+int nmg_mesh_concat(const nmg_mesh *const *ms, int32_t count, nmg_mesh **out) {
+  if (!ms || count <= 0 || !out) return fail(NMG_EINVAL, "nmg_mesh_concat: bad argument");
+  *out = nullptr;
+  const int n = ms[0] ? ms[0]->n : 0;
+  for (int i = 0; i < count; i++)
+    if (!ms[i] || ms[i]->n != n)
+      return fail(NMG_EINVAL, "nmg_mesh_concat: meshes must exist and share n");
+  nmg_mesh *m = new (std::nothrow) nmg_mesh;
+  if (!m) return fail(NMG_ENOMEM, "nmg_mesh_concat: out of memory");
+  try {
+    m->n = n;
+    m->x = ms[0]->x;
+    m->w = ms[0]->w;
+    m->D = ms[0]->D;
+    int64_t off = 0;
+    for (int i = 0; i < count; i++) {
+      const nmg_mesh &a = *ms[i];
+      for (int64_t e = 0; e < a.nelem; e++) m->pat.push_back(a.pat[e]);
+      m->bbox.insert(m->bbox.end(), a.bbox.begin(), a.bbox.end());
+      m->curvi.insert(m->curvi.end(), a.curvi.begin(), a.curvi.end());
+      m->xyz.insert(m->xyz.end(), a.xyz.begin(), a.xyz.end());
+      m->dXdx.insert(m->dXdx.end(), a.dXdx.begin(), a.dXdx.end());
+      for (size_t q = 0; q < a.nb.size(); q++)
+        m->nb.push_back(a.nb[q] < 0 ? -1 : (int32_t)(a.nb[q] + off));
+      m->code.insert(m->code.end(), a.code.begin(), a.code.end());
+      off += a.nelem;
+    }
+    m->nelem = off;
+  } catch (const std::bad_alloc &) {
+    delete m;
+    return fail(NMG_ENOMEM, "nmg_mesh_concat: out of memory");
+  }
+  *out = m;
+  return NMG_OK;
+}
+
 }  // extern "C"

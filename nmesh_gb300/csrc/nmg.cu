@@ -820,3 +820,378 @@ int nmg_fp64_peak(double *gflops) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// batched execution of many independent problems
+// ---------------------------------------------------------------------------
+struct nmg_batch {
+  std::string err;
+  int nprob = 0;
+  std::vector<nmg_mesh *> gmesh;  // merged mesh of each order (owned)
+  std::vector<nmg_ctx *> gctx;    // one context per order
+  std::vector<int> gn, gblk0;     // per group, highest order first
+  int ntile = 0;
+  std::vector<int> pgroup;
+  std::vector<int64_t> pelem0, pnelem;
+  size_t smem = 0;
+  int grid = 0;  // persistent CTAs, chosen by timing
+  int grouped = 0;  // 1: one launch per order with that order's tuned variant
+  int force_mode = 0;  // 0 autotune, 1 persistent only, 2 per-order launches only
+  std::vector<StageParams> hparams;  // host copy of d_params
+  std::string tune_log;
+  cudaStream_t stream = nullptr;
+  StageParams *d_params = nullptr;  // [parity][stage][group]
+  int *d_gn = nullptr, *d_gblk0 = nullptr;
+  double *d_times = nullptr;
+  int *d_step = nullptr;
+  int times_cap = 0;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  double graph_dt = 0;
+  int cur = 0;
+  int64_t launches = 0;
+};
+
+static int batch_err(nmg_batch *b, int code, const std::string &msg) {
+  if (b) b->err = msg;
+  return code;
+}
+
+#define BK(call)                                                                          \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess)                                                                \
+      return batch_err(b, NMG_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+// per-group stage parameters of one RK4 step with u in buffer `parity`,
+// stage times read from the batch's device time array
+static void batch_params(nmg_batch *b, int parity, std::vector<StageParams> &out) {
+  const int G = (int)b->gctx.size();
+  out.assign(2 * 4 * G, StageParams());
+  for (int par = 0; par < 2; par++)
+    for (int s = 0; s < 4; s++)
+      for (int g = 0; g < G; g++) {
+        nmg_ctx *c = b->gctx[g];
+        double *U = c->d_buf[par], *ACC = c->d_buf[1 - par], *WA = c->d_buf[2],
+               *WB = c->d_buf[3];
+        const double *win[4] = {U, WA, WB, WA};
+        double *wout[4] = {WA, WB, WA, nullptr};
+        StageParams P = base_params(c);
+        P.win = win[s];
+        P.u0 = U;
+        P.acc = ACC;
+        P.wout = wout[s];
+        P.mode = s + 1;
+        P.tdev = b->d_times;
+        P.stepdev = b->d_step;
+        out[(par * 4 + s) * G + g] = P;
+      }
+  (void)parity;
+}
+
+// stage coefficients depend on dt: fill them and upload all parameters
+static int batch_upload_params(nmg_batch *b, double dt) {
+  std::vector<StageParams> ps;
+  batch_params(b, 0, ps);
+  const int G = (int)b->gctx.size();
+  const double cacc[4] = {dt / 6., dt / 3., dt / 3., dt / 6.};
+  const double cw[4] = {dt / 2., dt / 2., dt, 0.};
+  const double tofs[4] = {0., 0.5 * dt, 0.5 * dt, dt};
+  for (int par = 0; par < 2; par++)
+    for (int s = 0; s < 4; s++)
+      for (int g = 0; g < G; g++) {
+        StageParams &P = ps[(par * 4 + s) * G + g];
+        P.cacc = cacc[s];
+        P.cw = cw[s];
+        P.tofs_dt = tofs[s];
+      }
+  BK(cudaMemcpy(b->d_params, ps.data(), ps.size() * sizeof(StageParams),
+                cudaMemcpyHostToDevice));
+  b->hparams = ps;
+  return NMG_OK;
+}
+
+static int batch_enqueue_stage(nmg_batch *b, int par, int s) {
+  const int G = (int)b->gctx.size();
+  if (b->grouped) {
+    for (int g = 0; g < G; g++) {
+      nmg_ctx *c = b->gctx[g];
+      BK(c->variants[c->sel].launch(b->hparams[(par * 4 + s) * G + g], b->stream));
+      b->launches++;
+    }
+  } else {
+    BK(nmgk::batch_launch(b->d_params + (par * 4 + s) * G, b->d_gn, b->d_gblk0, G, b->ntile,
+                          b->grid, b->smem, b->stream));
+    b->launches++;
+  }
+  return NMG_OK;
+}
+
+static int batch_enqueue_step(nmg_batch *b, int par) {
+  for (int s = 0; s < 4; s++) {
+    int rc = batch_enqueue_stage(b, par, s);
+    if (rc) return rc;
+  }
+  return NMG_OK;
+}
+
+static void batch_drop_graphs(nmg_batch *b) {
+  for (int g = 0; g < 2; g++)
+    if (b->graph[g]) {
+      cudaGraphExecDestroy(b->graph[g]);
+      b->graph[g] = nullptr;
+    }
+}
+
+// autotuner of the batched launch: persistent grid size by timing stage 1
+// (which reads u and writes only the accumulator and a stage buffer)
+static int batch_autotune(nmg_batch *b, double dt) {
+  if (b->grid > 0) return NMG_OK;
+  int dev = 0, sms = 0;
+  BK(cudaGetDevice(&dev));
+  BK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  int rc = batch_upload_params(b, dt);
+  if (rc) return rc;
+  double t0 = 0.;
+  BK(cudaMemcpyAsync(b->d_times, &t0, sizeof(double), cudaMemcpyHostToDevice, b->stream));
+  BK(cudaMemsetAsync(b->d_step, 0, sizeof(int), b->stream));
+  // each order's own variant first (the grouped mode launches those)
+  for (auto c : b->gctx) {
+    rc = autotune(c);
+    if (rc) return batch_err(b, rc, std::string("batch autotune: ") + nmg_last_error(c));
+  }
+  // candidates: grid > 0 = one persistent launch with that many CTAs,
+  // grid = 0 = one launch per order
+  std::vector<int> cands;
+  if (b->force_mode != 2) {
+    cands.push_back(b->ntile);
+    for (int k = 1; k <= 4; k++)
+      if (sms * k < b->ntile) cands.push_back(sms * k);
+  }
+  if (b->force_mode != 1) cands.push_back(0);
+  cudaEvent_t e0, e1;
+  BK(cudaEventCreate(&e0));
+  BK(cudaEventCreate(&e1));
+  float best = 1e30f;
+  int bestg = b->ntile;
+  b->tune_log.clear();
+  for (int grid : cands) {
+    b->grouped = grid == 0;
+    b->grid = grid == 0 ? b->ntile : grid;
+    if ((rc = batch_enqueue_stage(b, 0, 0))) return rc;
+    BK(cudaEventRecord(e0, b->stream));
+    for (int r = 0; r < 3; r++)
+      if ((rc = batch_enqueue_stage(b, 0, 0))) return rc;
+    BK(cudaEventRecord(e1, b->stream));
+    BK(cudaEventSynchronize(e1));
+    float ms = 0;
+    BK(cudaEventElapsedTime(&ms, e0, e1));
+    ms /= 3;
+    char buf[64];
+    if (grid) snprintf(buf, sizeof buf, "persistent-grid%d=%.4fms ", grid, ms);
+    else snprintf(buf, sizeof buf, "per-order-launches=%.4fms ", ms);
+    b->tune_log += buf;
+    if (ms < best) { best = ms; bestg = grid; }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  b->grouped = bestg == 0;
+  b->grid = bestg == 0 ? b->ntile : bestg;
+  return NMG_OK;
+}
+
+extern "C" {
+
+int nmg_batch_create(const nmg_mesh *const *meshes, int32_t count, int32_t bc_kind,
+                     const double k[3], nmg_batch **out) {
+  if (!out) return NMG_EINVAL;
+  *out = nullptr;
+  nmg_batch *b = new (std::nothrow) nmg_batch;
+  if (!b) return NMG_ENOMEM;
+  *out = b;
+  if (!meshes || count <= 0) return batch_err(b, NMG_EINVAL, "nmg_batch_create: no meshes");
+  b->nprob = count;
+  std::vector<int> orders;
+  for (int p = 0; p < count; p++) {
+    if (!meshes[p]) return batch_err(b, NMG_EINVAL, "nmg_batch_create: null mesh");
+    const int n = meshes[p]->n;
+    if (nmgk::batch_epb(n) <= 0)
+      return batch_err(b, NMG_EUNSUP, "nmg_batch_create: orders n in [2,10] only");
+    if (std::find(orders.begin(), orders.end(), n) == orders.end()) orders.push_back(n);
+  }
+  std::sort(orders.begin(), orders.end(), [](int a, int c) { return a > c; });
+  b->pgroup.assign(count, -1);
+  b->pelem0.assign(count, 0);
+  b->pnelem.assign(count, 0);
+  int tile = 0;
+  for (size_t g = 0; g < orders.size(); g++) {
+    const int n = orders[g];
+    std::vector<const nmg_mesh *> list;
+    int64_t off = 0;
+    for (int p = 0; p < count; p++)
+      if (meshes[p]->n == n) {
+        list.push_back(meshes[p]);
+        b->pgroup[p] = (int)g;
+        b->pelem0[p] = off;
+        b->pnelem[p] = meshes[p]->nelem;
+        off += meshes[p]->nelem;
+      }
+    nmg_mesh *mm = nullptr;
+    if (nmg_mesh_concat(list.data(), (int)list.size(), &mm))
+      return batch_err(b, NMG_EMESH, std::string("nmg_batch_create: ") + nmg_mesh_last_error());
+    b->gmesh.push_back(mm);
+    nmg_ctx *c = nullptr;
+    int rc = nmg_create(mm, bc_kind, k, &c);
+    b->gctx.push_back(c);
+    if (rc) return batch_err(b, rc, std::string("nmg_batch_create: ") + nmg_last_error(c));
+    b->gn.push_back(n);
+    b->gblk0.push_back(tile);
+    tile += (int)((mm->nelem + nmgk::batch_epb(n) - 1) / nmgk::batch_epb(n));
+    b->smem = std::max(b->smem, nmgk::batch_smem(n));
+  }
+  b->ntile = tile;
+  BK(nmgk::batch_prepare(b->smem));
+  BK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+  const int G = (int)b->gctx.size();
+  BK(cudaMalloc((void **)&b->d_params, sizeof(StageParams) * 8 * G));
+  BK(cudaMalloc((void **)&b->d_gn, sizeof(int) * G));
+  BK(cudaMalloc((void **)&b->d_gblk0, sizeof(int) * G));
+  BK(cudaMemcpy(b->d_gn, b->gn.data(), sizeof(int) * G, cudaMemcpyHostToDevice));
+  BK(cudaMemcpy(b->d_gblk0, b->gblk0.data(), sizeof(int) * G, cudaMemcpyHostToDevice));
+  BK(cudaMalloc((void **)&b->d_step, sizeof(int)));
+  BK(cudaMalloc((void **)&b->d_times, sizeof(double)));
+  b->times_cap = 1;
+  return NMG_OK;
+}
+
+void nmg_batch_destroy(nmg_batch *b) {
+  if (!b) return;
+  batch_drop_graphs(b);
+  for (auto c : b->gctx) nmg_destroy(c);
+  for (auto m : b->gmesh) nmg_mesh_free(m);
+  cudaFree(b->d_params);
+  cudaFree(b->d_gn);
+  cudaFree(b->d_gblk0);
+  cudaFree(b->d_times);
+  cudaFree(b->d_step);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+}
+
+const char *nmg_batch_last_error(const nmg_batch *b) {
+  return b ? b->err.c_str() : "null batch";
+}
+
+int64_t nmg_batch_problem_size(const nmg_batch *b, int32_t p) {
+  if (!b || p < 0 || p >= b->nprob) return -1;
+  const int n = b->gn[b->pgroup[p]];
+  return b->pnelem[p] * NF * (int64_t)n * n * n;
+}
+
+static double *batch_problem_ptr(nmg_batch *b, int p) {
+  const int g = b->pgroup[p];
+  const int np = b->gctx[g]->np;
+  return b->gctx[g]->d_buf[b->cur] + b->pelem0[p] * NF * (int64_t)np;
+}
+
+int nmg_batch_set_state(nmg_batch *b, int32_t p, const double *host_u) {
+  if (!b || !host_u || p < 0 || p >= b->nprob)
+    return batch_err(b, NMG_EINVAL, "nmg_batch_set_state: bad argument");
+  BK(cudaMemcpy(batch_problem_ptr(b, p), host_u,
+                nmg_batch_problem_size(b, p) * sizeof(double), cudaMemcpyHostToDevice));
+  return NMG_OK;
+}
+
+int nmg_batch_get_state(nmg_batch *b, int32_t p, double *host_u) {
+  if (!b || !host_u || p < 0 || p >= b->nprob)
+    return batch_err(b, NMG_EINVAL, "nmg_batch_get_state: bad argument");
+  BK(cudaMemcpy(host_u, batch_problem_ptr(b, p), nmg_batch_problem_size(b, p) * sizeof(double),
+                cudaMemcpyDeviceToHost));
+  return NMG_OK;
+}
+
+int nmg_rk4_steps_batched(nmg_batch *b, double t, double dt, int32_t nsteps) {
+  if (!b || nsteps < 0) return batch_err(b, NMG_EINVAL, "nmg_rk4_steps_batched: bad argument");
+  if (nsteps == 0) return NMG_OK;
+  for (auto c : b->gctx) BK(cudaStreamSynchronize(c->stream));  // state copies are done
+  std::vector<double> times(nsteps);
+  long double Te = t, te = 0.;
+  for (int s = 0; s < nsteps; s++) {
+    times[s] = (double)(Te + te);
+    te += dt;
+  }
+  if (nsteps > b->times_cap) {
+    cudaFree(b->d_times);
+    b->d_times = nullptr;
+    BK(cudaMalloc((void **)&b->d_times, sizeof(double) * nsteps));
+    b->times_cap = nsteps;
+    batch_drop_graphs(b);
+  }
+  if (dt != b->graph_dt) {
+    batch_drop_graphs(b);
+    b->graph_dt = dt;
+  }
+  int rc = batch_autotune(b, dt);
+  if (rc) return rc;
+  if (!b->graph[0] || !b->graph[1]) {
+    rc = batch_upload_params(b, dt);
+    if (rc) return rc;
+    for (int par = 0; par < 2; par++) {
+      cudaGraph_t g;
+      BK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+      int64_t l0 = b->launches;
+      rc = batch_enqueue_step(b, par);
+      advance_step_kernel<<<1, 1, 0, b->stream>>>(b->d_step);
+      cudaError_t e1 = cudaGetLastError();
+      cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
+      b->launches = l0;
+      if (rc) return rc;
+      BK(e1);
+      BK(e2);
+      cudaError_t e3 = cudaGraphInstantiate(&b->graph[par], g, 0);
+      cudaGraphDestroy(g);
+      BK(e3);
+    }
+  }
+  BK(cudaMemcpyAsync(b->d_times, times.data(), sizeof(double) * nsteps, cudaMemcpyHostToDevice,
+                     b->stream));
+  BK(cudaMemsetAsync(b->d_step, 0, sizeof(int), b->stream));
+  for (int s = 0; s < nsteps; s++) {
+    BK(cudaGraphLaunch(b->graph[b->cur], b->stream));
+    b->launches += 5;
+    b->cur = 1 - b->cur;
+  }
+  BK(cudaStreamSynchronize(b->stream));
+  return NMG_OK;
+}
+
+int nmg_batch_info(nmg_batch *b, char *buf, int32_t len) {
+  if (!b || !buf || len <= 0) return NMG_EINVAL;
+  std::string s = "groups:";
+  for (size_t g = 0; g < b->gn.size(); g++) {
+    char t[96];
+    snprintf(t, sizeof t, " n%d:%lld elems/%d per tile", b->gn[g],
+             (long long)b->gctx[g]->nelem, nmgk::batch_epb(b->gn[g]));
+    s += t;
+  }
+  char t[128];
+  snprintf(t, sizeof t, " | mode %s | tiles %d | grid %d | launches %lld",
+           b->grouped ? "per-order-launches" : "persistent", b->ntile, b->grid,
+           (long long)b->launches);
+  s += t;
+  if (!b->tune_log.empty()) s += " | timings: " + b->tune_log;
+  snprintf(buf, (size_t)len, "%s", s.c_str());
+  return NMG_OK;
+}
+
+void *nmg_batch_stream(nmg_batch *b) { return b ? (void *)b->stream : nullptr; }
+
+int nmg_batch_set_mode(nmg_batch *b, int32_t mode) {
+  if (!b || mode < 0 || mode > 2) return batch_err(b, NMG_EINVAL, "nmg_batch_set_mode: 0, 1 or 2");
+  b->force_mode = mode;
+  b->grid = 0;  // re-tune on the next step
+  batch_drop_graphs(b);
+  return NMG_OK;
+}
+
+}  // extern "C"

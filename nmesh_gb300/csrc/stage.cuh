@@ -210,6 +210,13 @@ int gather_variants(int n, Variant *out, int cap);
 int eo_variants(int n, Variant *out, int cap);
 // transposed (vector-Jacobian) stage kernel for n
 int vjp_variants(int n, Variant *out, int cap);
+// batched persistent kernel over element groups of different n (2..10)
+constexpr int kBatchMaxN = 10;
+int batch_epb(int n);        // elements per tile for n (0: unsupported n)
+size_t batch_smem(int n);    // dynamic shared memory of an n tile
+cudaError_t batch_prepare(size_t smem);
+cudaError_t batch_launch(const StageParams *d_params, const int *d_gn, const int *d_gblk0,
+                         int ngroup, int ntile, int grid, size_t smem, cudaStream_t st);
 // even-odd coefficients of D for n into constant memory
 cudaError_t eo_upload(int n, const double *D);
 

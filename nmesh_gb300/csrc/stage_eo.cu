@@ -58,8 +58,9 @@ __device__ __forceinline__ void line_deriv(const double *__restrict__ s, int st,
   }
 }
 
+// one CTA's work: elements [blk*EPB, blk*EPB+EPB) of P
 template <int N, int EPB, int NT>
-__global__ void __launch_bounds__(NT) eo_kernel(StageParams P) {
+__device__ __forceinline__ void eo_body(const StageParams &P, int blk) {
   constexpr int NP = N * N * N, NN = N * N;
   extern __shared__ double smem[];
   double *sW = smem;                 // [4][EPB][NP]: pi, cx, cy, cz of w
@@ -71,7 +72,7 @@ __global__ void __launch_bounds__(NT) eo_kernel(StageParams P) {
   __shared__ unsigned char sPair[3][4 * EPB];  // per pass: le*4 + field
   __shared__ int sNPair[3];
 
-  const int e0 = blockIdx.x * EPB;
+  const int e0 = blk * EPB;
   const int tid = threadIdx.x;
   for (int q = tid; q < EPB; q += NT) {
     const int e = e0 + q;
@@ -155,6 +156,11 @@ __global__ void __launch_bounds__(NT) eo_kernel(StageParams P) {
 }
 
 template <int N, int EPB, int NT>
+__global__ void __launch_bounds__(NT) eo_kernel(StageParams P) {
+  eo_body<N, EPB, NT>(P, blockIdx.x);
+}
+
+template <int N, int EPB, int NT>
 cudaError_t launch_eo(const StageParams &P, cudaStream_t st) {
   constexpr int NP = N * N * N;
   const size_t shmem = sizeof(double) * 10 * EPB * NP;
@@ -163,6 +169,45 @@ cudaError_t launch_eo(const StageParams &P, cudaStream_t st) {
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shmem);
   eo_kernel<N, EPB, NT><<<(P.nelem + EPB - 1) / EPB, NT, shmem, st>>>(P);
   return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Batched persistent kernel: several element groups, each with its own
+// order n and its own StageParams (one group = all problems of one order,
+// merged into one mesh), walked by persistent CTAs in one launch.  Tile
+// t -> (group g, block t - gblk0[g]); tiles of the highest order come first
+// so that the long tiles start early.  Tile shape per n: EPB = bEPB(n),
+// 256 threads (the eo:<bEPB>:256 variant, bitwise the same arithmetic).
+constexpr int kBatchNT = 256;
+constexpr int bEPB(int n) { return (128 / (2 * n * n)) > 1 ? (128 / (2 * n * n)) : 1; }
+
+template <int N>
+__device__ __forceinline__ void batch_tile(const StageParams *params, int g, int blk) {
+  const StageParams P = params[g];
+  eo_body<N, bEPB(N), kBatchNT>(P, blk);
+}
+
+__global__ void __launch_bounds__(kBatchNT, 2)
+    batch_kernel(const StageParams *params, const int *gn, const int *gblk0, int ngroup,
+                 int ntile) {
+  for (int b = blockIdx.x; b < ntile; b += gridDim.x) {
+    int g = 0;
+    while (g + 1 < ngroup && b >= gblk0[g + 1]) g++;
+    const int blk = b - gblk0[g];
+    __syncthreads();  // the previous tile's epilogue has read its shared memory
+    switch (gn[g]) {
+      case 2: batch_tile<2>(params, g, blk); break;
+      case 3: batch_tile<3>(params, g, blk); break;
+      case 4: batch_tile<4>(params, g, blk); break;
+      case 5: batch_tile<5>(params, g, blk); break;
+      case 6: batch_tile<6>(params, g, blk); break;
+      case 7: batch_tile<7>(params, g, blk); break;
+      case 8: batch_tile<8>(params, g, blk); break;
+      case 9: batch_tile<9>(params, g, blk); break;
+      case 10: batch_tile<10>(params, g, blk); break;
+      default: break;
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -441,6 +486,23 @@ int eo_variants(int n, Variant *out, int cap) {
     case 12: return add_eo<12>(out, cap);
     default: return 0;
   }
+}
+
+int batch_epb(int n) { return (n >= 2 && n <= kBatchMaxN) ? bEPB(n) : 0; }
+
+size_t batch_smem(int n) {
+  return (n >= 2 && n <= kBatchMaxN) ? sizeof(double) * 10 * bEPB(n) * n * n * n : 0;
+}
+
+cudaError_t batch_prepare(size_t smem) {
+  return cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)smem);
+}
+
+cudaError_t batch_launch(const StageParams *d_params, const int *d_gn, const int *d_gblk0,
+                         int ngroup, int ntile, int grid, size_t smem, cudaStream_t st) {
+  batch_kernel<<<grid, kBatchNT, smem, st>>>(d_params, d_gn, d_gblk0, ngroup, ntile);
+  return cudaGetLastError();
 }
 
 int vjp_variants(int n, Variant *out, int cap) {
