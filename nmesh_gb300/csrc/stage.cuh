@@ -164,6 +164,91 @@ __device__ __forceinline__ void face_terms(const StageParams &P, const double *s
   }
 }
 
+// Face data of one face node, split so that the global loads can be issued
+// early and the arithmetic done later: the lift factors (g n, g) and either
+// the neighbour's interior values, the exact exterior state, or (outgoing
+// boundary) the unit normal.
+struct FaceData {
+  double gn0, gn1, gn2, g;
+  double v0, v1, v2, v3;  // neighbour / exterior state, or normal (kind 2)
+  int kind;               // 0: neighbour or exact exterior state, 2: outgoing
+};
+
+template <int N>
+__device__ __forceinline__ void face_fetch(const StageParams &P, int e, int f, int ab, int cs,
+                                           double gcart_d, double t, FaceData &F) {
+  constexpr int NP = N * N * N, NN = N * N;
+  const int d = f >> 1, a = ab % N, b = ab / N;
+  if (cs < 0) {
+    const double sg = (f & 1) ? gcart_d : -gcart_d;
+    F.g = gcart_d;
+    F.gn0 = d == 0 ? sg : 0.;
+    F.gn1 = d == 1 ? sg : 0.;
+    F.gn2 = d == 2 ? sg : 0.;
+  } else {
+    const double2 *F2 = reinterpret_cast<const double2 *>(P.fac) + (((size_t)cs * 6 + f) * NN + ab) * 2;
+    const double2 fa = __ldg(F2), fb = __ldg(F2 + 1);
+    F.gn0 = fa.x; F.gn1 = fa.y; F.gn2 = fb.x; F.g = fb.y;
+  }
+  const int nbe = __ldg(P.nb + e * 6 + f);
+  F.kind = 0;
+  if (nbe >= 0) {
+    const int cd = __ldg(P.code + e * 6 + f), f2 = cd & 7, o = cd >> 3;
+    const int sw = o & 1, fa = (o >> 1) & 1, fb = (o >> 2) & 1;
+    int aa = sw ? b : a, bb = sw ? a : b;
+    aa = fa ? N - 1 - aa : aa;
+    bb = fb ? N - 1 - bb : bb;
+    const double *W2 = P.win + (size_t)nbe * NF * NP + face_node_d<N>(f2, aa, bb);
+    F.v0 = __ldg(W2);
+    F.v1 = __ldg(W2 + NP);
+    F.v2 = __ldg(W2 + 2 * NP);
+    F.v3 = __ldg(W2 + 3 * NP);
+  } else {
+    const int bs = __ldg(P.bslot + e * 6 + f);
+    if (P.bc == NMG_BC_EXACT_PLANEWAVE) {
+      const double *X = P.bxyz + (size_t)bs * 3 * NN + ab;
+      const double arg = P.k0 * X[0] + P.k1 * X[NN] + P.k2 * X[2 * NN] - P.om * t;
+      double sn, cn;
+      sincos(arg, &sn, &cn);
+      F.v0 = -P.om * cn;
+      F.v1 = P.k0 * cn;
+      F.v2 = P.k1 * cn;
+      F.v3 = P.k2 * cn;
+    } else {
+      const double *Nr = P.bnrm + (size_t)bs * 3 * NN + ab;
+      F.v0 = __ldg(Nr);
+      F.v1 = __ldg(Nr + NN);
+      F.v2 = __ldg(Nr + 2 * NN);
+      F.kind = 2;
+    }
+  }
+}
+
+// LLF lift of one face node given the interior state ui: adds to r[0..3]
+__device__ __forceinline__ void face_apply(const FaceData &F, double ui0, double ui1, double ui2,
+                                           double ui3, double &r0, double &r1, double &r2,
+                                           double &r3) {
+  double ua0, ua1, ua2, ua3;
+  if (F.kind == 0) {
+    ua0 = F.v0; ua1 = F.v1; ua2 = F.v2; ua3 = F.v3;
+  } else {
+    // outgoing radiation: zero incoming characteristic pi + c.n
+    const double n0 = F.v0, n1 = F.v1, n2 = F.v2;
+    const double cnv = ui1 * n0 + ui2 * n1 + ui3 * n2;
+    const double wo = ui0 - cnv;
+    const double dcn = -0.5 * wo - cnv;
+    ua0 = 0.5 * wo;
+    ua1 = fma(dcn, n0, ui1);
+    ua2 = fma(dcn, n1, ui2);
+    ua3 = fma(dcn, n2, ui3);
+  }
+  const double dpi = ua0 - ui0, dcx = ua1 - ui1, dcy = ua2 - ui2, dcz = ua3 - ui3;
+  r0 = fma(dcx, F.gn0, fma(dcy, F.gn1, fma(dcz, F.gn2, fma(F.g, dpi, r0))));
+  r1 = fma(dpi, F.gn0, fma(F.g, dcx, r1));
+  r2 = fma(dpi, F.gn1, fma(F.g, dcy, r2));
+  r3 = fma(dpi, F.gn2, fma(F.g, dcz, r3));
+}
+
 // r out (mode 0) or RK4 stage update.  r_pi = sR[0] (+ sR[4] + sR[5] for
 // elements whose divergence is split over three partial sums).
 template <int N, int EPB, int NT, bool SPLIT>

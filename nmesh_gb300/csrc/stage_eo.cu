@@ -172,6 +172,173 @@ cudaError_t launch_eo(const StageParams &P, cudaStream_t st) {
 }
 
 // ---------------------------------------------------------------------------
+// "eof": the eo kernel with the face terms folded into the volume passes.
+// The a-line through a face node of faces 2a / 2a+1 ends on that face, so
+// the pi task of each a-line also applies the LLF lift at its two end nodes
+// (neighbour values and lift factors are fetched before the line transform
+// so that their latency overlaps the arithmetic).  In pass a that task is
+// the only writer of r_c at its nodes; its r_pi face part goes to a
+// seventh accumulator.  This removes the three separate face passes.
+template <int N, int EPB, int NT>
+__device__ __forceinline__ void eof_body(const StageParams &P, int blk) {
+  constexpr int NP = N * N * N, NN = N * N;
+  extern __shared__ double smem[];
+  double *sW = smem;                 // [4][EPB][NP]: pi, cx, cy, cz of w
+  double *sR = smem + 4 * EPB * NP;  // [7][EPB][NP]: r_pi^0, r_c(3), r_pi^1, r_pi^2, r_pi^face
+  __shared__ int sCs[EPB];
+  __shared__ int sMask[EPB];
+  __shared__ double sScale[EPB][3];
+  __shared__ double sG[EPB][3];
+  __shared__ unsigned char sPair[3][4 * EPB];
+  __shared__ int sNPair[3];
+
+  const int e0 = blk * EPB;
+  const int tid = threadIdx.x;
+  for (int q = tid; q < EPB; q += NT) {
+    const int e = e0 + q;
+    const int cs = (e < P.nelem) ? P.cslot[e] : -1;
+    sCs[q] = cs;
+    sMask[q] = (e >= P.nelem) ? -1 : (cs >= 0 ? P.cmask[cs] : (1 | (1 << 4) | (1 << 8)));
+    for (int d = 0; d < 3; d++) sScale[q][d] = (e < P.nelem) ? P.scale[e * 3 + d] : 0.;
+    for (int d = 0; d < 3; d++) sG[q][d] = (e < P.nelem) ? P.gcart[e * 3 + d] : 0.;
+  }
+  for (int q = tid; q < 7 * EPB * NP; q += NT) sR[q] = 0.;
+  const double t = stage_time(P);
+  stage_in<N, EPB, NT>(P, sW, e0);
+  __syncthreads();
+  if (tid < 3) {
+    const int a = tid;
+    int np = 0;
+    for (int le = 0; le < EPB; le++) {
+      if (sMask[le] < 0) continue;  // past the last element
+      const int row = (sMask[le] >> (3 * a)) & 7;
+      sPair[a][np++] = (unsigned char)(le * 4 + 0);  // always: it carries the faces
+      for (int i = 0; i < 3; i++)
+        if (row & (1 << i)) sPair[a][np++] = (unsigned char)(le * 4 + 1 + i);
+    }
+    sNPair[a] = np;
+  }
+  __syncthreads();
+
+#pragma unroll 1
+  for (int a = 0; a < 3; a++) {
+    const int ntask = sNPair[a] * NN;
+    const int st = a == 0 ? 1 : (a == 1 ? N : NN);
+    for (int q = tid; q < ntask; q += NT) {
+      const int p = q / NN, L = q - p * NN;
+      const int pr = sPair[a][p], le = pr >> 2, fld = pr & 3;
+      const int l0 = L % N, l1 = L / N;
+      const int base = a == 0 ? N * (l0 + N * l1) : (a == 1 ? l0 + NN * l1 : l0 + N * l1);
+      const int cs = sCs[le];
+      const int row = (sMask[le] >> (3 * a)) & 7;
+      if (fld == 0) {
+        FaceData FL, FR;
+        face_fetch<N>(P, e0 + le, 2 * a, L, cs, sG[le][a], t, FL);
+        face_fetch<N>(P, e0 + le, 2 * a + 1, L, cs, sG[le][a], t, FR);
+        double out[N];
+        line_deriv<N, 0>(sW + (0 * EPB + le) * NP + base, st, out);
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+          if (!(row & (1 << i))) continue;
+          double *r = sR + ((1 + i) * EPB + le) * NP + base;
+          if (cs < 0) {
+            const double s = sScale[le][a];
+#pragma unroll
+            for (int qq = 0; qq < N; qq++) r[qq * st] = fma(s, out[qq], r[qq * st]);
+          } else {
+            const double *Mp = P.metricp + (((size_t)cs * 3 + a) * 3 + i) * N * NN + L;
+#pragma unroll
+            for (int qq = 0; qq < N; qq++)
+              r[qq * st] = fma(__ldg(Mp + qq * NN), out[qq], r[qq * st]);
+          }
+        }
+        // face terms at the two ends of the line
+#pragma unroll
+        for (int side = 0; side < 2; side++) {
+          const int node = base + (side ? (N - 1) * st : 0);
+          const double *w = sW + le * NP + node;
+          double *r = sR + le * NP + node;
+          double r0 = r[6 * EPB * NP], r1 = r[1 * EPB * NP], r2 = r[2 * EPB * NP],
+                 r3 = r[3 * EPB * NP];
+          face_apply(side ? FR : FL, w[0], w[EPB * NP], w[2 * EPB * NP], w[3 * EPB * NP], r0,
+                     r1, r2, r3);
+          r[6 * EPB * NP] = r0;
+          r[1 * EPB * NP] = r1;
+          r[2 * EPB * NP] = r2;
+          r[3 * EPB * NP] = r3;
+        }
+      } else {
+        double out[N];
+        line_deriv<N, 0>(sW + (fld * EPB + le) * NP + base, st, out);
+        const int i = fld - 1;
+        if (cs < 0) {
+          double *r = sR + (0 * EPB + le) * NP + base;
+          const double s = sScale[le][a];
+#pragma unroll
+          for (int qq = 0; qq < N; qq++) r[qq * st] = fma(s, out[qq], r[qq * st]);
+        } else {
+          const int slot = i == 0 ? 0 : 3 + i;
+          double *r = sR + (slot * EPB + le) * NP + base;
+          const double *Mp = P.metricp + (((size_t)cs * 3 + a) * 3 + i) * N * NN + L;
+#pragma unroll
+          for (int qq = 0; qq < N; qq++)
+            r[qq * st] = fma(__ldg(Mp + qq * NN), out[qq], r[qq * st]);
+        }
+      }
+    }
+    __syncthreads();
+  }
+
+  // epilogue: r_pi = r_pi^0 (+ r_pi^1 + r_pi^2) + r_pi^face, r_phi = pi
+  for (int q = tid; q < EPB * NF * NP; q += NT) {
+    const int le = q / (NF * NP), rem = q - le * NF * NP, f = rem / NP, node = rem - f * NP;
+    const int e = e0 + le;
+    if (e >= P.nelem) continue;
+    const size_t idx = ((size_t)e * NF + f) * NP + node;
+    double r;
+    if (f == 0) {
+      r = sR[le * NP + node];
+      if (sCs[le] >= 0) r += sR[(4 * EPB + le) * NP + node] + sR[(5 * EPB + le) * NP + node];
+      r += sR[(6 * EPB + le) * NP + node];
+    } else if (f < 4) {
+      r = sR[(f * EPB + le) * NP + node];
+    } else {
+      r = sW[le * NP + node];
+    }
+    if (P.mode == 0) {
+      P.rout[idx] = r;
+    } else if (P.mode == 1) {
+      const double u = __ldg(P.u0 + idx);
+      P.acc[idx] = fma(P.cacc, r, u);
+      P.wout[idx] = fma(P.cw, r, u);
+    } else if (P.mode == 4) {
+      P.acc[idx] = fma(P.cacc, r, P.acc[idx]);
+    } else {
+      P.acc[idx] = fma(P.cacc, r, P.acc[idx]);
+      P.wout[idx] = fma(P.cw, r, __ldg(P.u0 + idx));
+    }
+  }
+}
+
+// MINB: minimum resident CTAs per SM asked of the register allocator
+// (1: no register cap)
+template <int N, int EPB, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) eof_kernel(StageParams P) {
+  eof_body<N, EPB, NT>(P, blockIdx.x);
+}
+
+template <int N, int EPB, int NT, int MINB>
+cudaError_t launch_eof(const StageParams &P, cudaStream_t st) {
+  constexpr int NP = N * N * N;
+  const size_t shmem = sizeof(double) * 11 * EPB * NP;
+  if (P.nelem <= 0)
+    return cudaFuncSetAttribute(eof_kernel<N, EPB, NT, MINB>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shmem);
+  eof_kernel<N, EPB, NT, MINB><<<(P.nelem + EPB - 1) / EPB, NT, shmem, st>>>(P);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // Batched persistent kernel: several element groups, each with its own
 // order n and its own StageParams (one group = all problems of one order,
 // merged into one mesh), walked by persistent CTAs in one launch.  Tile
@@ -457,6 +624,14 @@ void add_one(Variant *out, int cap, int &k) {
   }
 }
 
+template <int N, int EPB, int NT, int MINB>
+void add_one_f(Variant *out, int cap, int &k) {
+  if constexpr (sizeof(double) * 11 * EPB * N * N * N + 4096 <= kSmemMax && EPB <= 64) {
+    if (k < cap)
+      out[k++] = Variant{MINB > 1 ? "eof" : "eofu", EPB, NT, launch_eof<N, EPB, NT, MINB>};
+  }
+}
+
 template <int N>
 int add_eo(Variant *out, int cap) {
   constexpr int NN = N * N;
@@ -466,6 +641,10 @@ int add_eo(Variant *out, int cap) {
   add_one<N, E1, 256>(out, cap, k);
   add_one<N, 2 * E1, 128>(out, cap, k);
   add_one<N, 2 * E1, 256>(out, cap, k);
+  add_one_f<N, E1, 128, 6>(out, cap, k);
+  add_one_f<N, E1, 256, 3>(out, cap, k);
+  add_one_f<N, E1, 128, 1>(out, cap, k);
+  add_one_f<N, E1, 256, 1>(out, cap, k);
   return k;
 }
 

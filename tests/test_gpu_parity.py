@@ -17,7 +17,7 @@ def _gpu(cuda_ok):
     yield
 
 
-VARIANTS = ["eo", "gather"]
+VARIANTS = ["eo", "eof", "eofu", "gather"]
 
 
 @pytest.mark.parametrize("variant", VARIANTS)
