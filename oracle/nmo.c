@@ -25,6 +25,20 @@
  *   vladdto_onfaces      src/main/main/variables.c:1044-1066
  *   RK4                  src/main/evolve/RungeKutta.c:19-82
  *
+ * Finite-volume elements (fv_divf with use_only_right_flux, LLF at the
+ * midpoints, WENO reconstruction; coordinates_midpoint_data = no):
+ *   uniform points       src/main/basis/Legendre.c:626-660,701-719
+ *   midpoints, dists     src/main/coordinates/get_coords.c:509-518,1702-1865
+ *   det(dXb/dx)          src/main/coordinates/coordinates.c:174-223,
+ *                        src/main/coordinates/utilities.c:199-211
+ *   fv_divf              src/main/dg/fv.c:115-624
+ *   WENO3 / WENOm3_2     src/main/dg/rec1d.c:16-27,121-227,880-1030
+ *   WENO5 / WENOm5_2     src/main/dg/rec1d.c:1186-1368
+ *   dnfn extrapolation   src/main/dg/rec1d.c:542-628
+ *   midpoint states      src/tests/scalarwave1/scalarwave1.c:761-802
+ *   fin.-vol. surface    src/main/dg/dg.c:58-70,81-90 (oow = 1/|distXb|,
+ *                        F = f*)
+ *
  * Extensions without a reference counterpart (restated, parity unpinned):
  *   BC kind 1: outgoing-radiation outer boundary (characteristic upwinding
  *              of the first-order wave system: incoming characteristic
@@ -52,7 +66,14 @@ typedef struct nmo_mesh {
                                coincident node across the face, -1 = outer */
   int bc;                   /* outer faces: 0 exact plane wave, 1 outgoing */
   double k[3];              /* plane-wave vector for bc 0 */
+  /* finite-volume elements (fv.c); fv == NULL: all elements are DG */
+  const int32_t *fv;        /* [e] 1: fin.-vol. element on uniform points */
+  int fv_rec;               /* NMO_REC_* reconstruction (par fv_rec) */
+  int fv_extrap;            /* 0: fv_divf_extrap = no, 1: dnfn_extrap1 */
+  double fv_w3ratio;        /* par fv_WENOm3_opt_weightratio (default 2) */
 } nmo_mesh;
+
+enum { NMO_REC_1 = 0, NMO_REC_WENOM3_2 = 1, NMO_REC_WENOM5_2 = 2 };
 
 /* ------------------------------------------------------------------ */
 /* basis: LGL points, weights and differentiation matrix               */
@@ -148,6 +169,24 @@ static void flux1d(double *f, const double norm[3], const double *u)
   f[2] = -u[0] * norm[1];
   f[3] = -u[0] * norm[2];
   f[4] = 0.;
+}
+
+/* numflux1d_LLF with the scalar-wave eigenvalues (1,-1,0,0,0) on both
+   sides: amax = 1 */
+static void llf(const double *ui, const double *ua, const double *fi,
+                const double *fa, double *fnum)
+{
+  const double lam[5] = {1.0, -1.0, 0.0, 0.0, 0.0};
+  double apl = 0., ami = 0., amax;
+  int l;
+  for (l = 0; l < NF; l++) {
+    apl = fmax(apl, lam[l]);
+    ami = fmin(ami, lam[l]);
+  }
+  apl = fabs(apl); ami = fabs(ami);
+  amax = fmax(ami, apl);
+  for (l = 0; l < NF; l++)
+    fnum[l] = 0.5 * (fa[l] + fi[l] - amax * (ua[l] - ui[l]));
 }
 
 /* out = D_dir applied to in along direction dir (array.c MM_SET_AB order) */
@@ -246,6 +285,51 @@ static double sqrtgdiag(const nmo_mesh *m, int e, int dir, int ijk)
   return dXbdX * sqrt(g);
 }
 
+/* volume index of in-plane point (a, b) on face f (forplaneN order) */
+static int face_node(int n, int f, int a, int b)
+{
+  int dir = f / 2, p = (f % 2) * (n - 1);
+  if (dir == 0) return p + n * (a + n * b);
+  if (dir == 1) return a + n * (p + n * b);
+  return a + n * (b + n * p);
+}
+
+/* LLF flux f* through face f at face node ijk (in-plane index JK) of element
+   e: inner state from w, outer state from the coincident neighbour node or
+   the boundary condition (scalarwave1_fluxes_pt + numflux1d_LLF).  Returns
+   the inner flux fi and f*. */
+static void face_fnum(const nmo_mesh *m, int e, int f, int ijk, int JK,
+                      double t, const double *w, double fi[5], double fnum[5])
+{
+  int n = m->n, np = n * n * n, l;
+  const double *we = w + (size_t)e * NF * np;
+  double norm[3], ui[5], ua[5], fa[5];
+  int64_t nb = m->nbnode[((size_t)e * 6 + f) * n * n + JK];
+  node_normal(m, e, f, ijk, norm);
+  for (l = 0; l < NF; l++) ui[l] = we[l * np + ijk];
+  if (nb >= 0) {
+    int64_t en = nb / np, in = nb % np;
+    for (l = 0; l < NF; l++) ua[l] = w[(size_t)en * NF * np + l * np + in];
+  } else if (m->bc == 0) {
+    const double *X = m->xyz + (size_t)e * 3 * np;
+    double xyz[3] = {X[ijk], X[np + ijk], X[2 * np + ijk]};
+    planewave(m->k, xyz, t, ua);
+  } else {
+    /* outgoing radiation: exterior state with zero incoming
+       characteristic pi + c.n, copy of the outgoing characteristic
+       pi - c.n and of the tangential c */
+    double cn = ui[1] * norm[0] + ui[2] * norm[1] + ui[3] * norm[2];
+    double wout = ui[0] - cn;
+    double pie = 0.5 * wout, cne = -0.5 * wout;
+    ua[0] = pie;
+    for (l = 0; l < 3; l++) ua[1 + l] = ui[1 + l] + (cne - cn) * norm[l];
+    ua[4] = ui[4];
+  }
+  flux1d(fi, norm, ui);
+  flux1d(fa, norm, ua);
+  llf(ui, ua, fi, fa, fnum);
+}
+
 /* RHS of one element: r[e] = RHS(w) at time t.  tmp holds 18*np doubles. */
 static void rhs_elem(const nmo_mesh *m, const double *D, const double *wq,
                      double t, const double *w, double *r, int e, double *tmp)
@@ -300,49 +384,9 @@ static void rhs_elem(const nmo_mesh *m, const double *D, const double *wq,
     double oow = 1. / wq[p];
     for (b = 0; b < n; b++)
       for (a = 0; a < n; a++) {
-        int ii, jj, kk, ijk, JK = a + n * b;
-        double norm[3], ui[5], ua[5], fi[5], fa[5], fnum[5];
-        double gd_ow;
-        int64_t nb = m->nbnode[((size_t)e * 6 + f) * n * n + JK];
-        if (dir == 0) { ii = p; jj = a; kk = b; }
-        else if (dir == 1) { ii = a; jj = p; kk = b; }
-        else { ii = a; jj = b; kk = p; }
-        ijk = ii + n * (jj + n * kk);
-        node_normal(m, e, f, ijk, norm);
-        for (l = 0; l < NF; l++) ui[l] = we[l * np + ijk];
-        if (nb >= 0) {
-          int64_t en = nb / np, in = nb % np;
-          for (l = 0; l < NF; l++) ua[l] = w[(size_t)en * NF * np + l * np + in];
-        } else if (m->bc == 0) {
-          const double *X = m->xyz + (size_t)e * 3 * np;
-          double xyz[3] = {X[ijk], X[np + ijk], X[2 * np + ijk]};
-          planewave(m->k, xyz, t, ua);
-        } else {
-          /* outgoing radiation: exterior state with zero incoming
-             characteristic pi + c.n, copy of the outgoing characteristic
-             pi - c.n and of the tangential c */
-          double cn = ui[1] * norm[0] + ui[2] * norm[1] + ui[3] * norm[2];
-          double wout = ui[0] - cn;
-          double pie = 0.5 * wout, cne = -0.5 * wout;
-          ua[0] = pie;
-          for (l = 0; l < 3; l++) ua[1 + l] = ui[1 + l] + (cne - cn) * norm[l];
-          ua[4] = ui[4];
-        }
-        flux1d(fi, norm, ui);
-        flux1d(fa, norm, ua);
-        /* LLF with eigenvalues (1,-1,0,0,0): amax = 1 */
-        {
-          double lam[5] = {1.0, -1.0, 0.0, 0.0, 0.0};
-          double apl = 0., ami = 0., amax;
-          for (l = 0; l < NF; l++) {
-            apl = fmax(apl, lam[l]);
-            ami = fmin(ami, lam[l]);
-          }
-          apl = fabs(apl); ami = fabs(ami);
-          amax = fmax(ami, apl);
-          for (l = 0; l < NF; l++)
-            fnum[l] = 0.5 * (fa[l] + fi[l] - amax * (ua[l] - ui[l]));
-        }
+        int ijk = face_node(n, f, a, b), JK = a + n * b;
+        double fi[5], fnum[5], gd_ow;
+        face_fnum(m, e, f, ijk, JK, t, w, fi, fnum);
         gd_ow = sqrtgdiag(m, e, dir, ijk) * oow;
         for (l = 0; l < 4; l++) {
           double F = (fnum[l] - fi[l] * 1.0) * 1.0;
@@ -350,6 +394,280 @@ static void rhs_elem(const nmo_mesh *m, const double *D, const double *wq,
         }
       }
   }
+
+  /* vladdto_onfaces(r, -1, divf) */
+  for (k = 0; k < n; k++)
+    for (j = 0; j < n; j++)
+      for (i = 0; i < n; i++)
+        if (i == 0 || i == n - 1 || j == 0 || j == n - 1 || k == 0 || k == n - 1) {
+          int ijk = i + n * (j + n * k);
+          for (l = 0; l < 4; l++) re[l * np + ijk] += -1. * divf[l * np + ijk];
+        }
+}
+
+/* ------------------------------------------------------------------ */
+/* finite-volume elements                                              */
+/* ------------------------------------------------------------------ */
+/* equally spaced points on [-1, 1] (uniform_x) */
+void nmo_uniform(int npoints, double *x)
+{
+  int N = npoints - 1, j;
+  double y, h;
+  if (N == 0) { x[0] = 0.; return; }
+  x[0] = -1.; x[N] = 1.;
+  if (N == 1) return;
+  h = 2. / N;
+  for (j = 1; j <= N / 2; j++) {
+    if (j == N / 2.0) y = 0.;
+    else y = -1. + j * h;
+    x[N - j] = -y;
+    x[j] = +y;
+  }
+}
+
+/* WENO3 towards midpoint im from the left (rec1d_p_WENO3, u_scale = 1) */
+static double weno3_p(const double *u, int im, double o0, double o1,
+                      double l00, double l01, double l10, double l11)
+{
+  double u_im1 = u[im - 1], u_i = u[im], u_ip1 = u[im + 1];
+  double d1 = u_i - u_im1, d2 = u_ip1 - u_i;
+  double b1 = d1 * d1 + 1e-6 * 1.0, b2 = d2 * d2 + 1e-6 * 1.0;
+  double ob1 = o0 / (b1 * b1), ob2 = o1 / (b2 * b2);
+  double sum = ob1 + ob2;
+  double w1 = ob1 / sum, w2 = ob2 / sum;
+  double u1 = l00 * u_im1 + l01 * u_i, u2 = l10 * u_i + l11 * u_ip1;
+  return w1 * u1 + w2 * u2;
+}
+
+/* WENO3 towards midpoint im from the right (rec1d_m_WENO3) */
+static double weno3_m(const double *u, int im, double o0, double o1,
+                      double l00, double l01, double l10, double l11)
+{
+  double u_i = u[im], u_ip1 = u[im + 1], u_ip2 = u[im + 2];
+  double d1 = u_ip1 - u_i, d2 = u_ip2 - u_ip1;
+  double b1 = d1 * d1 + 1e-6 * 1.0, b2 = d2 * d2 + 1e-6 * 1.0;
+  double ob1 = o0 / (b1 * b1), ob2 = o1 / (b2 * b2);
+  double sum = ob1 + ob2;
+  double w1 = ob1 / sum, w2 = ob2 / sum;
+  double u1 = l00 * u_i + l01 * u_ip1, u2 = l10 * u_ip1 + l11 * u_ip2;
+  return w1 * u1 + w2 * u2;
+}
+
+#define C1312 (1.083333333333333333333333)
+/* WENO5 with uniform weights (rec1d_p_WENO5_uniform) */
+static double weno5_p(const double *u, int im)
+{
+  const double oo6 = 1 / 6.;
+  double u_im2 = u[im - 2], u_im1 = u[im - 1], u_i = u[im];
+  double u_ip1 = u[im + 1], u_ip2 = u[im + 2];
+  double b01 = u_im2 - 2. * u_im1 + u_i, b02 = u_im2 - 4. * u_im1 + 3. * u_i;
+  double b11 = u_im1 - 2. * u_i + u_ip1, b12 = u_im1 - u_ip1;
+  double b21 = u_i - 2. * u_ip1 + u_ip2, b22 = 3. * u_i - 4. * u_ip1 + u_ip2;
+  double b0 = C1312 * b01 * b01 + 0.25 * b02 * b02;
+  double b1 = C1312 * b11 * b11 + 0.25 * b12 * b12;
+  double b2 = C1312 * b21 * b21 + 0.25 * b22 * b22;
+  double e0 = b0 + 1e-40 * 1.0, e1 = b1 + 1e-40 * 1.0, e2 = b2 + 1e-40 * 1.0;
+  double o0 = 1. / (e0 * e0), o1 = 6. / (e1 * e1), o2 = 3. / (e2 * e2);
+  double oos = 1. / (o0 + o1 + o2);
+  double w0 = o0 * oos, w1 = o1 * oos, w2 = o2 * oos;
+  double q0 = (2. * oo6) * u_im2 + (-7. * oo6) * u_im1 + (11. * oo6) * u_i;
+  double q1 = (-oo6) * u_im1 + (5. * oo6) * u_i + (2. * oo6) * u_ip1;
+  double q2 = (2. * oo6) * u_i + (5. * oo6) * u_ip1 + (-oo6) * u_ip2;
+  return w0 * q0 + w1 * q1 + w2 * q2;
+}
+
+/* rec1d_m_WENO5_uniform */
+static double weno5_m(const double *u, int im)
+{
+  const double oo6 = 1 / 6.;
+  double u_im1 = u[im - 1], u_i = u[im], u_ip1 = u[im + 1];
+  double u_ip2 = u[im + 2], u_ip3 = u[im + 3];
+  double b21 = u_ip1 - 2. * u_ip2 + u_ip3, b22 = 3. * u_ip1 - 4. * u_ip2 + u_ip3;
+  double b11 = u_i - 2. * u_ip1 + u_ip2, b12 = u_i - u_ip2;
+  double b01 = u_im1 - 2. * u_i + u_ip1, b02 = u_im1 - 4. * u_i + 3. * u_ip1;
+  double b2 = C1312 * b21 * b21 + 0.25 * b22 * b22;
+  double b1 = C1312 * b11 * b11 + 0.25 * b12 * b12;
+  double b0 = C1312 * b01 * b01 + 0.25 * b02 * b02;
+  double e2 = b2 + 1e-40 * 1.0, e1 = b1 + 1e-40 * 1.0, e0 = b0 + 1e-40 * 1.0;
+  double o2 = 1. / (e2 * e2), o1 = 6. / (e1 * e1), o0 = 3. / (e0 * e0);
+  double oos = 1. / (o0 + o1 + o2);
+  double w2 = o2 * oos, w1 = o1 * oos, w0 = o0 * oos;
+  double q2 = (11. * oo6) * u_ip1 + (-7. * oo6) * u_ip2 + (2. * oo6) * u_ip3;
+  double q1 = (2. * oo6) * u_i + (5. * oo6) * u_ip1 + (-oo6) * u_ip2;
+  double q0 = (-oo6) * u_im1 + (5. * oo6) * u_i + (2. * oo6) * u_ip1;
+  return w0 * q0 + w1 * q1 + w2 * q2;
+}
+
+/* left state at midpoint im (0..n-2) of a pencil of n values */
+static double rec_p(int mode, int n, const double *u, int im, double r3)
+{
+  if (mode == NMO_REC_1) return u[im];
+  if (mode == NMO_REC_WENOM5_2 && im >= 2 && im <= n - 3) return weno5_p(u, im);
+  /* rec1d_p_WENOm3_2 */
+  if (im >= 1 && im <= n - 2) return weno3_p(u, im, 1., r3, -0.5, 1.5, 0.5, 0.5);
+  if (n < 3) return u[im];
+  return 0.5 * u[0] + 0.5 * u[1];            /* im == 0 */
+}
+
+/* right state at midpoint im */
+static double rec_m(int mode, int n, const double *u, int im, double r3)
+{
+  if (mode == NMO_REC_1) return u[im + 1];
+  if (mode == NMO_REC_WENOM5_2 && im >= 1 && im <= n - 4) return weno5_m(u, im);
+  /* rec1d_m_WENOm3_2 */
+  if (im >= 0 && im <= n - 3) return weno3_m(u, im, r3, 1., 0.5, 0.5, 1.5, -0.5);
+  if (n < 3) return u[im + 1];
+  return 0.5 * u[n - 2] + 0.5 * u[n - 1];    /* im == n-2 */
+}
+
+/* det(dXb/dx) at node ijk (coordinates_init_node) */
+static double det_dXbdx(const nmo_mesh *m, int e, int ijk)
+{
+  int np = m->n * m->n * m->n, a, b;
+  const double *bb = m->bbox + 6 * e;
+  double d0 = 2. / (bb[1] - bb[0]), d1 = 2. / (bb[3] - bb[2]);
+  double d2 = 2. / (bb[5] - bb[4]);
+  double det = d0 * d1 * d2, M[3][3];
+  if (!m->curvi[e]) return det;
+  for (a = 0; a < 3; a++)
+    for (b = 0; b < 3; b++) M[a][b] = m->dXdx[((size_t)e * 9 + a * 3 + b) * np + ijk];
+  return det * (M[0][0] * M[1][1] * M[2][2] - M[0][2] * M[1][1] * M[2][0] +
+                M[0][1] * M[1][2] * M[2][0] + M[0][2] * M[1][0] * M[2][1] -
+                M[0][0] * M[1][2] * M[2][1] - M[0][1] * M[1][0] * M[2][2]);
+}
+
+/* RHS of one fin.-vol. element (scalarwave1_vol_rhs_u / _surf_rhs_u with
+   use_fv: fv_divf, then the surface terms).  tmp holds 8*np doubles. */
+static void rhs_elem_fv(const nmo_mesh *m, double t, const double *w,
+                        double *r, int e, double *tmp)
+{
+  int n = m->n, np = n * n * n, i, j, k, f, l, dir, a, b, i0;
+  const double *we = w + (size_t)e * NF * np;
+  double *re = r + (size_t)e * NF * np;
+  const double *bb = m->bbox + 6 * e;
+  double *divf = tmp, *ooJ = tmp + 4 * np, *sg = tmp + 5 * np;
+  double Xb[64], Xbm[64], dXb[64], distXb[6];
+  double fnumR[4] = {0., 0., 0., 0.}, fnumL[4] = {0., 0., 0., 0.};
+  const int addsurf = (m->fv_extrap == 1);     /* dnfn_extrap1 */
+  const double r3 = m->fv_w3ratio;
+
+  /* points, midpoints and the n distances dXb (set_nm_nodemidpoint_distsXb_dir) */
+  nmo_uniform(n, Xb);
+  for (i = 0; i < n - 1; i++) Xbm[i] = 0.5 * (Xb[i] + Xb[i + 1]);
+  for (f = 0; f < 6; f++) {
+    int d = f / 2, right = f % 2, id = (n - 2) * right;
+    double Xbf = (2. * bb[f] - (bb[2 * d + 1] + bb[2 * d])) / (bb[2 * d + 1] - bb[2 * d]);
+    distXb[f] = fabs(Xbm[id] - Xbf);
+  }
+  for (i = 0; i < np; i++) {
+    ooJ[i] = det_dXbdx(m, e, i);
+    for (dir = 0; dir < 3; dir++) sg[dir * np + i] = sqrtgdiag(m, e, dir, i);
+  }
+  for (i = 0; i < 4 * np; i++) divf[i] = 0.;
+
+  for (dir = 0; dir < 3; dir++) {
+    const int st = (dir == 0) ? 1 : (dir == 1) ? n : n * n;
+    const double *sgd = sg + dir * np;
+    dXb[0] = distXb[2 * dir];
+    dXb[n - 1] = distXb[2 * dir + 1];
+    for (i = 1; i < n - 1; i++) dXb[i] = Xbm[i] - Xbm[i - 1];
+    for (b = 0; b < n; b++)
+      for (a = 0; a < n; a++) {
+        const int base = face_node(n, 2 * dir, a, b);   /* i0 = 0 of this pencil */
+        double qc[NF][64], df[4][64];
+        for (i0 = 0; i0 < n; i0++)
+          for (l = 0; l < NF; l++) qc[l][i0] = we[l * np + base + i0 * st];
+        for (i0 = 0; i0 < n; i0++) {
+          const int ccc = base + i0 * st;
+          const int g0 = (i0 > 0), lN = (i0 < n - 1);
+          const int cccL = base + (g0 ? i0 - 1 : i0) * st;
+          const int cccR = base + (lN ? i0 : i0 - 1) * st;
+          const double wc = dXb[i0];
+          double JR, JL;
+          if (g0 && lN) {
+            JR = sgd[cccR] / (ooJ[cccR] * wc);
+            JL = sgd[cccL] / (ooJ[cccL] * wc);
+          } else if (!g0 && lN) {
+            JR = sgd[cccR] / (ooJ[cccR] * wc);
+            JL = sgd[ccc] / (ooJ[ccc] * wc);
+          } else if (g0 && !lN) {
+            JR = sgd[ccc] / (ooJ[ccc] * wc);
+            JL = sgd[cccL] / (ooJ[cccL] * wc);
+          } else {
+            JR = JL = sgd[ccc] / (ooJ[ccc] * wc);
+          }
+          if (!addsurf) { JR = lN * JR; JL = g0 * JL; }
+          if (g0) {
+            for (l = 0; l < 4; l++) fnumL[l] = -fnumR[l];
+          } else if (addsurf) {
+            double fi[5], fn[5];
+            face_fnum(m, e, 2 * dir, ccc, a + n * b, t, w, fi, fn);
+            for (l = 0; l < 4; l++) fnumL[l] = fn[l];
+          }
+          if (lN) {
+            double ui[5], ua[5], fi[5], fa[5], fn[5], norm[3];
+            node_normal(m, e, 2 * dir + 1, ccc, norm);
+            for (l = 0; l < NF; l++) {
+              ui[l] = rec_p(m->fv_rec, n, qc[l], i0, r3);
+              ua[l] = rec_m(m->fv_rec, n, qc[l], i0, r3);
+            }
+            flux1d(fi, norm, ui);
+            flux1d(fa, norm, ua);
+            llf(ui, ua, fi, fa, fn);
+            for (l = 0; l < 4; l++) fnumR[l] = fn[l];
+          } else if (addsurf) {
+            double fi[5], fn[5];
+            face_fnum(m, e, 2 * dir + 1, ccc, a + n * b, t, w, fi, fn);
+            for (l = 0; l < 4; l++) fnumR[l] = fn[l];
+          }
+          for (l = 0; l < 4; l++) {
+            double fR = fnumR[l] - 0., fL = fnumL[l] - 0.;
+            df[l][i0] = JR * fR + JL * fL;
+          }
+        }
+        if (addsurf && n > 2) {    /* FV_DNFN_EXTRAP1, s1 = 0, s2 = DBL_MAX */
+          const double w0 = 1. / 0.75, w1 = 1. - w0;
+          for (l = 0; l < 4; l++) {
+            df[l][0] = w0 * df[l][0] + w1 * df[l][1];
+            df[l][n - 1] = w0 * df[l][n - 1] + w1 * df[l][n - 2];
+          }
+        }
+        for (i0 = 0; i0 < n; i0++) {
+          const int ccc = base + i0 * st;
+          for (l = 0; l < 4; l++) divf[l * np + ccc] += df[l][i0] * ooJ[ccc];
+        }
+      }
+  }
+
+  /* volume RHS */
+  for (k = 0; k < n; k++)
+    for (j = 0; j < n; j++)
+      for (i = 0; i < n; i++) {
+        int ijk = i + n * (j + n * k);
+        int onface = (i == 0 || i == n - 1 || j == 0 || j == n - 1 ||
+                      k == 0 || k == n - 1);
+        double interior = !onface;
+        re[4 * np + ijk] = we[ijk];
+        for (l = 0; l < 4; l++) re[l * np + ijk] = -divf[l * np + ijk] * interior;
+      }
+
+  /* surface terms on fin.-vol. faces: only when fv_divf did not add them */
+  if (!addsurf)
+    for (f = 0; f < 6; f++) {
+      int d = f / 2;
+      double oow = 1. / (0. + distXb[f] * 1.);
+      for (b = 0; b < n; b++)
+        for (a = 0; a < n; a++) {
+          int ijk = face_node(n, f, a, b);
+          double fi[5], fn[5], gd_ow;
+          face_fnum(m, e, f, ijk, a + n * b, t, w, fi, fn);
+          gd_ow = sg[d * np + ijk] * oow;
+          for (l = 0; l < 4; l++) {
+            double F = (fn[l] - fi[l] * 0.) * 1.0;
+            divf[l * np + ijk] += F * gd_ow;
+          }
+        }
+    }
 
   /* vladdto_onfaces(r, -1, divf) */
   for (k = 0; k < n; k++)
@@ -380,7 +698,10 @@ int nmo_rhs(const nmo_mesh *m, double t, const double *w, double *r)
     double *tmp = (double *)malloc(sizeof(double) * 18 * np);
     int e;
 #pragma omp for schedule(static)
-    for (e = 0; e < m->nelem; e++) rhs_elem(m, D, wq, t, w, r, e, tmp);
+    for (e = 0; e < m->nelem; e++) {
+      if (m->fv && m->fv[e]) rhs_elem_fv(m, t, w, r, e, tmp);
+      else rhs_elem(m, D, wq, t, w, r, e, tmp);
+    }
     free(tmp);
   }
   return 0;

@@ -37,7 +37,14 @@ class _Mesh(ctypes.Structure):
                 ("bbox", ctypes.c_void_p), ("curvi", ctypes.c_void_p),
                 ("dXdx", ctypes.c_void_p), ("xyz", ctypes.c_void_p),
                 ("nbnode", ctypes.c_void_p), ("bc", ctypes.c_int),
-                ("k", ctypes.c_double * 3)]
+                ("k", ctypes.c_double * 3), ("fv", ctypes.c_void_p),
+                ("fv_rec", ctypes.c_int), ("fv_extrap", ctypes.c_int),
+                ("fv_w3ratio", ctypes.c_double)]
+
+# reconstruction modes (reference par fv_rec) and div(f) extrapolation
+# modes (par fv_divf_extrap) understood by the oracle
+FV_REC = {"1": 0, "WENOm3_2": 1, "WENOm5_2": 2}
+FV_EXTRAP = {"no": 0, "dnfn_extrap1": 1}
 
 
 _lib = None
@@ -50,6 +57,13 @@ def lib():
         for name in ("nmo_rhs", "nmo_rk4"):
             getattr(_lib, name).restype = ctypes.c_int
     return _lib
+
+
+def uniform(n):
+    """Equally spaced points on [-1,1] (reference Legendre.c:626)."""
+    x = np.zeros(n)
+    lib().nmo_uniform(ctypes.c_int(n), x.ctypes.data_as(ctypes.c_void_p))
+    return x
 
 
 def lgl(n):
@@ -138,7 +152,10 @@ class OracleMesh:
     """Arrays describing a mesh for the oracle, kept alive with the struct."""
 
     def __init__(self, bbox, curvi, dXdx, xyz, nbnode, n, bc=0,
-                 k=(1.0, 1.0, 1.0)):
+                 k=(1.0, 1.0, 1.0), fv=None, fv_rec="WENOm5_2",
+                 fv_extrap="dnfn_extrap1", fv_w3ratio=2.0):
+        """fv: per-element finite-volume flags (None: all DG); fv_rec and
+        fv_extrap name the reference's fv_rec / fv_divf_extrap modes."""
         self.n = int(n)
         self.bbox = np.ascontiguousarray(bbox, np.float64)
         self.curvi = np.ascontiguousarray(curvi, np.int32)
@@ -146,10 +163,13 @@ class OracleMesh:
         self.xyz = np.ascontiguousarray(xyz, np.float64)
         self.nbnode = np.ascontiguousarray(nbnode, np.int64)
         self.nelem = self.bbox.shape[0]
+        self.fv = None if fv is None else np.ascontiguousarray(fv, np.int32)
         self.s = _Mesh(self.nelem, self.n, self.bbox.ctypes.data,
                        self.curvi.ctypes.data, self.dXdx.ctypes.data,
                        self.xyz.ctypes.data, self.nbnode.ctypes.data, int(bc),
-                       (ctypes.c_double * 3)(*k))
+                       (ctypes.c_double * 3)(*k),
+                       None if self.fv is None else self.fv.ctypes.data,
+                       FV_REC[fv_rec], FV_EXTRAP[fv_extrap], float(fv_w3ratio))
 
     def rhs(self, w, t=0.0):
         w = np.ascontiguousarray(w, np.float64)

@@ -13,11 +13,12 @@
      FINALIZE:         dumps u after the evolution ("<prefix>_final.bin").
 
    Record layout (little endian, all counts int32, all reals float64):
-     header: magic 'NMGD', version 1, nelem, then per element:
-       int32 pat, int32 n[3], float64 bbox[6],
+     header: magic 'NMGD', version 2, nelem, then per element:
+       int32 pat, int32 n[3], int32 use_fv, float64 bbox[6],
        float64 x[np], y[np], z[np]            (Cartesian coordinates)
        float64 dXdx[9][np]                    (dX^a/dx^i, a-major)
        float64 sqrtgdiag[3][np]
+       float64 det_dXbdx[np]
        float64 u[5][np]  (pi, cx, cy, cz, phi)
        float64 r[5][np]  (only in the *_rhs.bin file)
    where np = n0*n1*n2 and arrays are i-fastest (Ind_n). */
@@ -83,7 +84,8 @@ static void nmgdump_write(tMesh *mesh, const char *suffix, int with_r)
   int ix = Ind("x");
   int idXdx = Ind("dXdx");
   int isqg = Ind("sqrtgdiagx");
-  int hdr[3] = { 0x44474D4E, 1, (int)mesh->nmyelm };
+  int idet = Ind("det_dXbdx");
+  int hdr[3] = { 0x44474D4E, 2, (int)mesh->nmyelm };
   int e, c;
 
   nmgdump_vl_indices(mesh, iu);
@@ -103,12 +105,15 @@ static void nmgdump_write(tMesh *mesh, const char *suffix, int with_r)
     tElm *elm = mesh->myelm[e];
     int pat = elm->pat->p;
     int np = elm->np;
+    int use_fv = elm->dat->info->use_fv;
     fwrite(&pat, sizeof(int), 1, fp);
     fwrite(elm->n, sizeof(int), 3, fp);
+    fwrite(&use_fv, sizeof(int), 1, fp);
     fwrite(elm->bbox, sizeof(double), 6, fp);
     for(c = 0; c < 3; c++) fwrite(Vard(elm, ix + c), sizeof(double), np, fp);
     for(c = 0; c < 9; c++) fwrite(Vard(elm, idXdx + c), sizeof(double), np, fp);
     for(c = 0; c < 3; c++) fwrite(Vard(elm, isqg + c), sizeof(double), np, fp);
+    fwrite(Vard(elm, idet), sizeof(double), np, fp);
     for(c = 0; c < 5; c++) fwrite(Vard(elm, iu[c]), sizeof(double), np, fp);
     if(with_r)
       for(c = 0; c < 5; c++) fwrite(Vard(elm, ir[c]), sizeof(double), np, fp);

@@ -42,6 +42,26 @@ CASES = {
                       dt=0.004, steps=2, eps=0.02, seed=5),
     "cs7_l1_n4": dict(mesh="cs7", n=4, luni=1, k=(0.25, 0.15, -0.3),
                       dt=0.004, steps=2, eps=0.02, seed=9),
+    # finite-volume elements everywhere: uniform points (amr_uniform_p),
+    # fin. vol. mode (amr_fv_p), WENO reconstruction at the midpoints
+    "fvbox_l1_n7_w5no": dict(mesh="box", n=7, luni=1, k=(1.0, 1.0, 1.0),
+                             dt=0.005, steps=2, eps=0.05, seed=21,
+                             fv=dict(rec="WENOm5_2", extrap="no")),
+    "fvbox_l1_n7_w5dnfn": dict(mesh="box", n=7, luni=1, k=(1.0, -0.5, 0.25),
+                               dt=0.005, steps=2, eps=0.05, seed=22,
+                               fv=dict(rec="WENOm5_2", extrap="dnfn_extrap1")),
+    "fvbox_l2_n5_w3dnfn": dict(mesh="box", n=5, luni=2, k=(0.5, 1.0, -1.0),
+                               dt=0.004, steps=2, eps=0.1, seed=23,
+                               fv=dict(rec="WENOm3_2", extrap="dnfn_extrap1")),
+    "fvbox_l0_n13_w5dnfn": dict(mesh="box", n=13, luni=0, k=(1.0, 0.5, 0.25),
+                                dt=0.004, steps=2, eps=0.3, seed=24,
+                                fv=dict(rec="WENOm5_2", extrap="dnfn_extrap1")),
+    "fvcs7_l0_n7_w5dnfn": dict(mesh="cs7", n=7, luni=0, k=(0.3, -0.2, 0.1),
+                               dt=0.002, steps=2, eps=0.02, seed=25,
+                               fv=dict(rec="WENOm5_2", extrap="dnfn_extrap1")),
+    "fvcs7_l0_n6_w5no": dict(mesh="cs7", n=6, luni=0, k=(0.25, 0.15, -0.3),
+                             dt=0.002, steps=2, eps=0.02, seed=26,
+                             fv=dict(rec="WENOm5_2", extrap="no")),
 }
 
 
@@ -67,9 +87,15 @@ def parfile(case, prefix):
         lines += ["amr_mesh_type = 1 BoxMesh",
                   f"amr_mesh_xc = {PI!r} {PI!r} {PI!r}",
                   f"amr_BoxMesh_dout = {PI!r}"]
+        pats = "0"
     else:
         lines += ["amr_mesh_type = 7 CubedSpheres",
                   "amr_CubedSphere_dc = 1", "amr_CubedSphere_r0fac = 20"]
+        pats = "0 1 2 3 4 5 6"
+    if "fv" in c:
+        lines += [f"amr_uniform_p = {pats}", f"amr_fv_p = {pats}",
+                  f"fv_rec = {c['fv']['rec']}",
+                  f"fv_divf_extrap = {c['fv']['extrap']}"]
     return "\n".join(lines) + "\n"
 
 
@@ -88,11 +114,14 @@ def run_case(case, exe, outdir):
         d1 = read_dump(prefix + "_final.bin", False)
     c = CASES[case]
     meta = dict(case=case, **{k: v for k, v in c.items()})
+    extra = {}
+    if "fv" in c:   # fin.-vol. cases also keep the flag and det(dXb/dx)
+        extra = dict(use_fv=d0["use_fv"], det_dXbdx=d0["det_dXbdx"])
     np.savez_compressed(
         os.path.join(outdir, case + ".npz"),
         meta=json.dumps(meta), pat=d0["pat"], n=d0["n"], bbox=d0["bbox"],
         x=d0["x"], dXdx=d0["dXdx"], sqrtgdiag=d0["sqrtgdiag"],
-        u0=d0["u"], r0=d0["r"], u_final=d1["u"])
+        u0=d0["u"], r0=d0["r"], u_final=d1["u"], **extra)
     print(f"{case}: {len(d0['pat'])} elements written")
 
 

@@ -5,7 +5,7 @@ operation order and must match it bit for bit."""
 import numpy as np
 import pytest
 
-from helpers import CASES, load
+from helpers import CASES, FV_CASES, load
 from oracle import nmo
 
 
@@ -14,10 +14,15 @@ def _oracle_mesh(d, meta):
     curvi = (d["pat"] > 0).astype(np.int32) if meta["mesh"] == "cs7" else \
         np.zeros(len(d["pat"]), np.int32)
     nb = nmo.match_faces(d["x"], n)
-    return nmo.OracleMesh(d["bbox"], curvi, d["dXdx"], d["x"], nb, n, bc=0, k=meta["k"])
+    fv = {}
+    if "fv" in meta:
+        fv = dict(fv=d["use_fv"], fv_rec=meta["fv"]["rec"],
+                  fv_extrap=meta["fv"]["extrap"])
+    return nmo.OracleMesh(d["bbox"], curvi, d["dXdx"], d["x"], nb, n, bc=0,
+                          k=meta["k"], **fv)
 
 
-@pytest.mark.parametrize("case", CASES)
+@pytest.mark.parametrize("case", CASES + FV_CASES)
 def test_oracle_rhs_bitexact(case):
     d, meta = load(case)
     m = _oracle_mesh(d, meta)
@@ -25,7 +30,7 @@ def test_oracle_rhs_bitexact(case):
     assert np.array_equal(r, d["r0"])
 
 
-@pytest.mark.parametrize("case", CASES)
+@pytest.mark.parametrize("case", CASES + FV_CASES)
 def test_oracle_rk4_bitexact(case):
     d, meta = load(case)
     m = _oracle_mesh(d, meta)
