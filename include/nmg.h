@@ -47,6 +47,16 @@ extern "C" {
 #define NMG_BC_OUTGOING 1        /* outgoing radiation: no incoming
                                     characteristic (no reference counterpart) */
 
+/* finite-volume reconstruction at the midpoints, the reference's par fv_rec
+ * (src/main/dg/dg.c:286-330, rec1d.c) */
+#define NMG_FV_REC_1 0        /* "1": first order (rec1d_p_1 / rec1d_m_1) */
+#define NMG_FV_REC_WENOM3_2 1 /* "WENOm3_2" (reference default) */
+#define NMG_FV_REC_WENOM5_2 2 /* "WENOm5_2": WENO5 inside, WENOm3_2 near ends */
+/* how div(f) is completed on face points, the reference's par fv_divf_extrap
+ * (src/main/dg/dg.c:341-361) */
+#define NMG_FV_EXTRAP_NO 0    /* "no": face fluxes weighted by 1/|distXb| */
+#define NMG_FV_EXTRAP_DNFN1 1 /* "dnfn_extrap1" (reference default) */
+
 typedef struct nmg_mesh nmg_mesh; /* host-side packed mesh */
 typedef struct nmg_ctx nmg_ctx;   /* device context; owns all device memory */
 
@@ -61,6 +71,9 @@ typedef struct nmg_mesh_params {
   double box_dout;    /* amr_BoxMesh_dout: half edge of the box */
   double cs_dc;       /* amr_CubedSphere_dc: half edge of the inner cube */
   double cs_r0fac;    /* amr_CubedSphere_r0fac: outer radius / dc */
+  int32_t fv;         /* 1: every element is a finite-volume element on
+                         equally spaced points (amr_uniform_p and amr_fv_p
+                         list every patch, src/main/amr/mesh.c:35-83) */
 } nmg_mesh_params;
 
 /* A mesh given element by element, e.g. packed from the reference's tMesh
@@ -81,6 +94,9 @@ typedef struct nmg_mesh_desc {
                              outer faces; NULL: matched from coordinates */
   double period[3];       /* >0: coordinates compared modulo period when
                              matching (periodic box); 0 otherwise */
+  const int32_t *fv;      /* [nelem] node->dat->info->use_fv (elements on
+                             equally spaced points), or NULL: all DG.  Mixed
+                             meshes are rejected with NMG_EUNSUP. */
 } nmg_mesh_desc;
 
 /* ---- host mesh ---------------------------------------------------------- */
@@ -97,9 +113,13 @@ int nmg_mesh_get_dXdx(const nmg_mesh *m, double *dXdx);
 /* copies out the face table: [nelem][6] neighbour element (-1 outer) and
    [nelem][6] code = neighbour face | orientation << 3 */
 int nmg_mesh_get_faces(const nmg_mesh *m, int32_t *nb, int32_t *code);
+/* copies out [nelem] finite-volume flags (1: element on uniform points) */
+int nmg_mesh_get_fv(const nmg_mesh *m, int32_t *fv);
 /* LGL nodes and weights on [-1,1] and D[i*n+j] = l_j'(x_i)
    (src/main/basis/Legendre.c:149-213, Lagrange.c:126-147) */
 int nmg_basis(int32_t n, double *x, double *w, double *D);
+/* equally spaced points on [-1,1] (uniform_x, src/main/basis/Legendre.c:626) */
+int nmg_uniform_points(int32_t n, double *x);
 void nmg_mesh_free(nmg_mesh *m);
 const char *nmg_mesh_last_error(void);
 
@@ -118,6 +138,12 @@ int nmg_set_state(nmg_ctx *c, const double *host_u);
 int nmg_get_state(nmg_ctx *c, double *host_u);
 /* device pointer of the resident state u (for zero-copy use) */
 double *nmg_state_device_ptr(nmg_ctx *c);
+
+/* Finite-volume options of a context whose mesh is finite-volume: the
+ * reference's DG globals fv_rec, fv_divf_extrap and
+ * fv_WENOm3_opt_weightratio (src/main/dg/dg.c:286-400; defaults WENOm3_2,
+ * dnfn_extrap1, 2).  NMG_EUNSUP on a DG context. */
+int nmg_set_fv(nmg_ctx *c, int32_t rec, int32_t extrap, double w3ratio);
 
 /* r = RHS(w, t) with w, r device pointers of nmg_state_size() doubles.
  * Replaces evolve_setrhs_mesh (src/main/evolve/evolve.c:182-232) for the

@@ -22,6 +22,10 @@ MESH_BOX = 1
 MESH_CUBEDSPHERES7 = 7
 BC_EXACT_PLANEWAVE = 0
 BC_OUTGOING = 1
+# finite-volume reconstruction (reference par fv_rec) and div(f) completion
+# on face points (par fv_divf_extrap)
+FV_REC = {"1": 0, "WENOm3_2": 1, "WENOm5_2": 2}
+FV_EXTRAP = {"no": 0, "dnfn_extrap1": 1}
 
 _c_dp = ctypes.POINTER(ctypes.c_double)
 _lib = None
@@ -35,7 +39,8 @@ class _MeshParams(ctypes.Structure):
     _fields_ = [("mesh_type", ctypes.c_int32), ("n", ctypes.c_int32),
                 ("luni", ctypes.c_int32), ("periodic", ctypes.c_int32),
                 ("xc", ctypes.c_double * 3), ("box_dout", ctypes.c_double),
-                ("cs_dc", ctypes.c_double), ("cs_r0fac", ctypes.c_double)]
+                ("cs_dc", ctypes.c_double), ("cs_r0fac", ctypes.c_double),
+                ("fv", ctypes.c_int32)]
 
 
 class _MeshDesc(ctypes.Structure):
@@ -43,7 +48,7 @@ class _MeshDesc(ctypes.Structure):
                 ("pat", ctypes.c_void_p), ("bbox", ctypes.c_void_p),
                 ("curvi", ctypes.c_void_p), ("xyz", ctypes.c_void_p),
                 ("dXdx", ctypes.c_void_p), ("nbnode", ctypes.c_void_p),
-                ("period", ctypes.c_double * 3)]
+                ("period", ctypes.c_double * 3), ("fv", ctypes.c_void_p)]
 
 
 def library_path():
@@ -104,6 +109,9 @@ def lib(build_if_missing=True):
         "nmg_rk4_step_vjp": (ctypes.c_int, [vp, f64, f64, vp, vp]),
         "nmg_adjoint_gradient": (ctypes.c_int, [vp, f64, f64, i32, i32, vp, vp, vp]),
         "nmg_kernel_info": (ctypes.c_int, [vp, vp, i32]),
+        "nmg_mesh_get_fv": (ctypes.c_int, [vp, vp]),
+        "nmg_uniform_points": (ctypes.c_int, [i32, vp]),
+        "nmg_set_fv": (ctypes.c_int, [vp, i32, i32, f64]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -144,13 +152,14 @@ class Mesh:
 
     @classmethod
     def build(cls, mesh_type=MESH_BOX, n=5, luni=0, xc=(0.0, 0.0, 0.0),
-              box_dout=1.0, cs_dc=1.0, cs_r0fac=20.0, periodic=False):
+              box_dout=1.0, cs_dc=1.0, cs_r0fac=20.0, periodic=False, fv=False):
         """Mesh from the reference's parameters: amr_mesh_type (1 BoxMesh /
         7 CubedSpheres), amr_n0..2 = n, amr_luni, amr_mesh_xc,
-        amr_BoxMesh_dout, amr_CubedSphere_dc, amr_CubedSphere_r0fac."""
+        amr_BoxMesh_dout, amr_CubedSphere_dc, amr_CubedSphere_r0fac;
+        fv=True puts every patch in amr_uniform_p and amr_fv_p."""
         p = _MeshParams(int(mesh_type), int(n), int(luni), int(bool(periodic)),
                         (ctypes.c_double * 3)(*xc), float(box_dout),
-                        float(cs_dc), float(cs_r0fac))
+                        float(cs_dc), float(cs_r0fac), int(bool(fv)))
         h = ctypes.c_void_p()
         rc = lib().nmg_mesh_build(ctypes.byref(p), ctypes.byref(h))
         if rc:
@@ -159,7 +168,7 @@ class Mesh:
 
     @classmethod
     def from_arrays(cls, bbox, curvi, xyz, dXdx=None, nbnode=None, pat=None,
-                    period=(0.0, 0.0, 0.0)):
+                    period=(0.0, 0.0, 0.0), fv=None):
         """Mesh from per-element arrays (what an nmesh adapter packs)."""
         bbox = np.ascontiguousarray(bbox, np.float64)
         E = bbox.shape[0]
@@ -169,11 +178,13 @@ class Mesh:
         dX = None if dXdx is None else np.ascontiguousarray(dXdx, np.float64)
         nb = None if nbnode is None else np.ascontiguousarray(nbnode, np.int64)
         pt = None if pat is None else np.ascontiguousarray(pat, np.int32)
+        fva = None if fv is None else np.ascontiguousarray(fv, np.int32)
         d = _MeshDesc(E, n, None if pt is None else pt.ctypes.data, bbox.ctypes.data,
                       keep[1].ctypes.data, xyz.ctypes.data,
                       None if dX is None else dX.ctypes.data,
                       None if nb is None else nb.ctypes.data,
-                      (ctypes.c_double * 3)(*period))
+                      (ctypes.c_double * 3)(*period),
+                      None if fva is None else fva.ctypes.data)
         h = ctypes.c_void_p()
         rc = lib().nmg_mesh_from_desc(ctypes.byref(d), ctypes.byref(h))
         if rc:
@@ -195,6 +206,12 @@ class Mesh:
         x = np.zeros((self.nelem, 9, self.np))
         lib().nmg_mesh_get_dXdx(self._h, _ptr(x))
         return x
+
+    def fv(self):
+        """Per-element finite-volume flags."""
+        f = np.zeros(self.nelem, np.int32)
+        lib().nmg_mesh_get_fv(self._h, _ptr(f))
+        return f
 
     def faces(self):
         nb = np.zeros((self.nelem, 6), np.int32)
@@ -294,6 +311,14 @@ class Evolution:
                                                ctypes.byref(J), ctypes.c_void_p(grad_ptr)),
                     "nmg_adjoint_gradient")
         return J.value
+
+    def set_fv(self, rec="WENOm3_2", extrap="dnfn_extrap1", w3ratio=2.0):
+        """Finite-volume options (reference pars fv_rec, fv_divf_extrap,
+        fv_WENOm3_opt_weightratio)."""
+        if rec not in FV_REC or extrap not in FV_EXTRAP:
+            raise NmgError(f"nmg_set_fv: unknown fv_rec {rec!r} or fv_divf_extrap {extrap!r}")
+        self._check(lib().nmg_set_fv(self._h, FV_REC[rec], FV_EXTRAP[extrap],
+                                     float(w3ratio)), "nmg_set_fv")
 
     def set_kernel(self, spec="auto"):
         """Force a stage-kernel variant ("eo", "gather", "eo:<epb>:<threads>")

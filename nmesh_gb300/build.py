@@ -11,7 +11,10 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libnmg.so")
-SOURCES = ["nmg.cu", "stage_eo.cu", "stage_gather.cu", "noalloc.cu", "mesh.cpp"]
+SOURCES = ["nmg.cu", "stage_eo.cu", "stage_gather.cu", "stage_fv.cu", "noalloc.cu", "mesh.cpp"]
+# per-file extra flags: the finite-volume kernel rounds every product and sum
+# separately, in the reference's order (no FMA contraction)
+EXTRA_FLAGS = {"stage_fv.cu": ["-fmad=false"]}
 HEADERS = ["mesh.h", "stage.cuh", "ctx.h",os.path.join("..", "..", "include", "nmg.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
@@ -45,7 +48,8 @@ def build(force=False, verbose=False):
 
     def compile_one(src):
         obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
-        cmd = [nvcc] + NVCC_FLAGS + ["-c", os.path.join(CSRC, src), "-o", obj]
+        cmd = [nvcc] + NVCC_FLAGS + EXTRA_FLAGS.get(src, []) + \
+            ["-c", os.path.join(CSRC, src), "-o", obj]
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
             raise RuntimeError(f"nvcc failed for {src}:\n{res.stderr}")

@@ -249,6 +249,28 @@ double wrap1(double v, double period) {
 
 namespace nmg {
 
+// D[i*n+j] = l_j'(x_i) of the Lagrange polynomials through x (Lagrange_DT,
+// src/main/basis/Lagrange.c:126-147, with the weights of Lagrange.c:15-27)
+static void lagrange_D(int n, const double *x, double *D) {
+  std::vector<double> wi(n);
+  for (int i = 0; i < n; i++) {
+    double denom = 1.;
+    for (int m2 = 0; m2 < n; m2++)
+      if (m2 != i) denom *= (x[i] - x[m2]);
+    wi[i] = 1. / denom;
+  }
+  for (int i = 0; i < n; i++) {
+    double Dii = 0;
+    for (int j = 0; j < n; j++)
+      if (i != j) {
+        double Dij = (wi[j] / wi[i]) / (x[i] - x[j]);
+        Dii -= Dij;
+        D[i * n + j] = Dij;
+      }
+    D[i * n + i] = Dii;
+  }
+}
+
 void lgl_basis(int n, double *x, double *w, double *D) {
   const double PI = 3.14159265358979323846264338327950;
   int N = n - 1;
@@ -277,23 +299,25 @@ void lgl_basis(int n, double *x, double *w, double *D) {
       w[N - j] = w[j];
     }
   }
-  std::vector<double> wi(n);
-  for (int i = 0; i < n; i++) {
-    double denom = 1.;
-    for (int m2 = 0; m2 < n; m2++)
-      if (m2 != i) denom *= (x[i] - x[m2]);
-    wi[i] = 1. / denom;
+  lagrange_D(n, x, D);
+}
+
+void uniform_basis(int n, double *x, double *w, double *D) {
+  const int N = n - 1;
+  if (N == 0) {
+    x[0] = 0.; w[0] = 2.;
+  } else {
+    x[0] = -1.; x[N] = 1.;
+    const double h = 2. / N;
+    for (int j = 1; j <= N / 2; j++) {
+      const double y = (j == N / 2.0) ? 0. : -1. + j * h;
+      x[N - j] = -y;
+      x[j] = +y;
+    }
+    w[N] = w[0] = 1. / N;
+    for (int j = 1; j < N; j++) w[j] = 2. / N;
   }
-  for (int i = 0; i < n; i++) {
-    double Dii = 0;
-    for (int j = 0; j < n; j++)
-      if (i != j) {
-        double Dij = (wi[j] / wi[i]) / (x[i] - x[j]);
-        Dii -= Dij;
-        D[i * n + j] = Dij;
-      }
-    D[i * n + i] = Dii;
-  }
+  lagrange_D(n, x, D);
 }
 
 std::string pack_faces(nmg_mesh &m, const int64_t *nbnode, const double period[3]) {
@@ -476,7 +500,12 @@ int nmg_mesh_build(const nmg_mesh_params *p, nmg_mesh **out) {
   try {
     m->n = p->n;
     m->x.resize(p->n); m->w.resize(p->n); m->D.resize(p->n * p->n);
-    nmg::lgl_basis(p->n, m->x.data(), m->w.data(), m->D.data());
+    if (p->fv) {
+      m->uniform = true;
+      nmg::uniform_basis(p->n, m->x.data(), m->w.data(), m->D.data());
+    } else {
+      nmg::lgl_basis(p->n, m->x.data(), m->w.data(), m->D.data());
+    }
     std::vector<Patch> pats;
     double period[3] = {0, 0, 0};
     if (p->mesh_type == NMG_MESH_BOX) {
@@ -520,6 +549,7 @@ int nmg_mesh_build(const nmg_mesh_params *p, nmg_mesh **out) {
       return fail(NMG_EUNSUP, "nmg_mesh_build: unknown mesh_type");
     }
     fill_geometry(*m, pats, p->luni);
+    if (p->fv) m->fv.assign(m->nelem, 1);
     std::string err = nmg::pack_faces(*m, nullptr, period);
     if (!err.empty()) { delete m; return fail(NMG_EMESH, err); }
   } catch (const std::bad_alloc &) {
@@ -544,7 +574,20 @@ int nmg_mesh_from_desc(const nmg_mesh_desc *d, nmg_mesh **out) {
     m->n = n;
     m->nelem = E;
     m->x.resize(n); m->w.resize(n); m->D.resize(n * n);
-    nmg::lgl_basis(n, m->x.data(), m->w.data(), m->D.data());
+    int64_t nfv = 0;
+    if (d->fv)
+      for (int64_t e = 0; e < E; e++) nfv += d->fv[e] ? 1 : 0;
+    if (nfv > 0 && nfv < E) {
+      delete m;
+      return fail(NMG_EUNSUP, "nmg_mesh_from_desc: mixed DG / finite-volume meshes are not supported");
+    }
+    if (nfv > 0) {
+      m->uniform = true;
+      m->fv.assign(E, 1);
+      nmg::uniform_basis(n, m->x.data(), m->w.data(), m->D.data());
+    } else {
+      nmg::lgl_basis(n, m->x.data(), m->w.data(), m->D.data());
+    }
     m->pat.assign(E, 0);
     if (d->pat) std::memcpy(m->pat.data(), d->pat, E * sizeof(int32_t));
     m->bbox.assign(d->bbox, d->bbox + E * 6);
@@ -604,6 +647,19 @@ int nmg_mesh_get_faces(const nmg_mesh *m, int32_t *nb, int32_t *code) {
   return NMG_OK;
 }
 
+int nmg_mesh_get_fv(const nmg_mesh *m, int32_t *fv) {
+  if (!m || !fv) return fail(NMG_EINVAL, "null argument");
+  for (int64_t e = 0; e < m->nelem; e++) fv[e] = m->fv.empty() ? 0 : m->fv[e];
+  return NMG_OK;
+}
+
+int nmg_uniform_points(int32_t n, double *x) {
+  if (n < 1 || n > 64 || !x) return fail(NMG_EINVAL, "nmg_uniform_points: bad argument");
+  std::vector<double> w(n), D((size_t)n * n);
+  nmg::uniform_basis(n, x, w.data(), D.data());
+  return NMG_OK;
+}
+
 void nmg_mesh_free(nmg_mesh *m) { delete m; }
 
 int nmg_mesh_concat(const nmg_mesh *const *ms, int32_t count, nmg_mesh **out) {
@@ -613,6 +669,9 @@ int nmg_mesh_concat(const nmg_mesh *const *ms, int32_t count, nmg_mesh **out) {
   for (int i = 0; i < count; i++)
     if (!ms[i] || ms[i]->n != n)
       return fail(NMG_EINVAL, "nmg_mesh_concat: meshes must exist and share n");
+  for (int i = 0; i < count; i++)
+    if (ms[i]->uniform != ms[0]->uniform || ms[i]->fv.empty() != ms[0]->fv.empty())
+      return fail(NMG_EUNSUP, "nmg_mesh_concat: meshes must share the point type");
   nmg_mesh *m = new (std::nothrow) nmg_mesh;
   if (!m) return fail(NMG_ENOMEM, "nmg_mesh_concat: out of memory");
   try {
@@ -620,6 +679,7 @@ int nmg_mesh_concat(const nmg_mesh *const *ms, int32_t count, nmg_mesh **out) {
     m->x = ms[0]->x;
     m->w = ms[0]->w;
     m->D = ms[0]->D;
+    m->uniform = ms[0]->uniform;
     int64_t off = 0;
     for (int i = 0; i < count; i++) {
       const nmg_mesh &a = *ms[i];
@@ -631,6 +691,7 @@ int nmg_mesh_concat(const nmg_mesh *const *ms, int32_t count, nmg_mesh **out) {
       for (size_t q = 0; q < a.nb.size(); q++)
         m->nb.push_back(a.nb[q] < 0 ? -1 : (int32_t)(a.nb[q] + off));
       m->code.insert(m->code.end(), a.code.begin(), a.code.end());
+      m->fv.insert(m->fv.end(), a.fv.begin(), a.fv.end());
       off += a.nelem;
     }
     m->nelem = off;

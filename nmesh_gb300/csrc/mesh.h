@@ -15,12 +15,18 @@ struct nmg_mesh {
   std::vector<double> dXdx;    // [E][9][np] dX^a/dx^i (identity if Cartesian)
   std::vector<int32_t> nb;     // [E][6] neighbour element, -1 on outer faces
   std::vector<int32_t> code;   // [E][6] neighbour face | orientation << 3
-  std::vector<double> x, w, D; // LGL nodes, weights, D[i*n+j]
+  std::vector<double> x, w, D; // points, quadrature weights, D[i*n+j]
+  std::vector<int32_t> fv;     // [E] 1: finite-volume element on uniform
+                               // points; empty: all elements DG on LGL points
+  bool uniform = false;        // x are equally spaced (finite-volume mesh)
 };
 
 namespace nmg {
 // LGL nodes/weights and differentiation matrix (Legendre.c / Lagrange.c)
 void lgl_basis(int n, double *x, double *w, double *D);
+// equally spaced points with trapezoid weights (uniform_x_wTrapez,
+// Legendre.c:626-719) and the Lagrange D matrix on them
+void uniform_basis(int n, double *x, double *w, double *D);
 // in-plane node (a, b) of face f -> volume index i + n*(j + n*k)
 inline int face_node(int n, int f, int a, int b) {
   int d = f >> 1, p = (f & 1) * (n - 1);

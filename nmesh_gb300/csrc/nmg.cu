@@ -127,6 +127,11 @@ struct nmg_ctx {
   double *d_times = nullptr;
   int *d_step = nullptr;
   int times_cap = 0;
+  // finite-volume mesh: options and geometry (stage_fv.cu)
+  bool fv = false;
+  int fv_rec = NMG_FV_REC_WENOM3_2, fv_extrap = NMG_FV_EXTRAP_DNFN1;
+  double fv_w3ratio = 2.;
+  double *d_fvgeo = nullptr, *d_fvdist = nullptr, *d_fvdxb = nullptr;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // one RK4 step, u in d_buf[0] / d_buf[1]
   double graph_dt = 0;
   int graph_sel = -1;
@@ -209,6 +214,13 @@ static StageParams base_params(nmg_ctx *c) {
   P.bxyz = c->d_bxyz;
   P.bnrm = c->d_bnrm;
   P.D = c->d_D;
+  P.n = c->n;
+  P.fv_rec = c->fv_rec;
+  P.fv_extrap = c->fv_extrap;
+  P.fv_w3ratio = c->fv_w3ratio;
+  P.fvgeo = c->d_fvgeo;
+  P.fvdist = c->d_fvdist;
+  P.fvdxb = c->d_fvdxb;
   P.bc = c->bc;
   P.k0 = c->k[0];
   P.k1 = c->k[1];
@@ -306,6 +318,47 @@ static int enqueue_step(nmg_ctx *c, int cur, double t, double dt, bool devtime) 
   return NMG_OK;
 }
 
+// Finite-volume geometry of element e (coordinates_midpoint_data = no: the
+// midpoint factors are those of the grid points): distance of each face to
+// its nearest midpoint (set_nodemidpoints_to_face_distXb,
+// src/main/coordinates/get_coords.c:1807-1836) and, on curvilinear elements,
+// per node 1/J = det(dXb/dx) (coordinates.c:174-223, utilities.c:199-211),
+// sqrtgdiag (coordinates.c:728-800) and the unit normals of the faces 2d+1
+// (utilities.c:48-88), in the reference's operation order.
+static void fv_pack_element(const nmg_mesh &m, int64_t e, int cs, std::vector<double> *geo,
+                            std::vector<double> *dist) {
+  const int n = m.n, np = n * n * n;
+  const double *bb = &m.bbox[e * 6];
+  for (int f = 0; f < 6; f++) {
+    const int d = f / 2, right = f % 2, id = (n - 2) * right;
+    const double Xbm = 0.5 * (m.x[id] + m.x[id + 1]);
+    const double Xbf = (2. * bb[f] - (bb[2 * d + 1] + bb[2 * d])) / (bb[2 * d + 1] - bb[2 * d]);
+    (*dist)[e * 6 + f] = std::fabs(Xbm - Xbf);
+  }
+  if (cs < 0) return;
+  const double *X9 = &m.dXdx[(size_t)e * 9 * np];
+  double *G = &(*geo)[(size_t)cs * 13 * np];
+  const double d0 = 2. / (bb[1] - bb[0]), d1 = 2. / (bb[3] - bb[2]), d2 = 2. / (bb[5] - bb[4]);
+  const double dXbdX[3] = {d0, d1, d2};
+  for (int q = 0; q < np; q++) {
+    double M[3][3];
+    for (int a = 0; a < 3; a++)
+      for (int b = 0; b < 3; b++) M[a][b] = X9[(a * 3 + b) * np + q];
+    const double det = M[0][0] * M[1][1] * M[2][2] - M[0][2] * M[1][1] * M[2][0] +
+                       M[0][1] * M[1][2] * M[2][0] + M[0][2] * M[1][0] * M[2][1] -
+                       M[0][0] * M[1][2] * M[2][1] - M[0][1] * M[1][0] * M[2][2];
+    G[q] = d0 * d1 * d2 * det;
+    for (int d = 0; d < 3; d++) {
+      double g = 0.0;
+      for (int l = 0; l < 3; l++) g += M[d][l] * M[d][l];
+      G[(1 + d) * np + q] = dXbdX[d] * sqrt(g);
+      double smag = sqrt(M[d][0] * M[d][0] + M[d][1] * M[d][1] + M[d][2] * M[d][2]);
+      if (smag == 0.0) smag = 1.;
+      for (int l = 0; l < 3; l++) G[(4 + 3 * d + l) * np + q] = M[d][l] / smag;
+    }
+  }
+}
+
 static void drop_graphs(nmg_ctx *c) {
   for (int g = 0; g < 2; g++)
     if (c->graph[g]) {
@@ -325,12 +378,22 @@ int nmg_create(const nmg_mesh *m, int32_t bc_kind, const double k[3], nmg_ctx **
   if (!m) return set_err(c, NMG_EINVAL, "nmg_create: null mesh");
   if (bc_kind != NMG_BC_EXACT_PLANEWAVE && bc_kind != NMG_BC_OUTGOING)
     return set_err(c, NMG_EINVAL, "nmg_create: unknown bc kind");
-  c->nvariants = nmgk::eo_variants(m->n, c->variants, kMaxVariants);
-  c->nvariants += nmgk::gather_variants(m->n, c->variants + c->nvariants,
-                                        kMaxVariants - c->nvariants);
-  if (c->nvariants == 0) return set_err(c, NMG_EUNSUP, "nmg_create: n must be in [2,12]");
-  if (nmgk::vjp_variants(m->n, &c->vjp, 1) != 1)
-    return set_err(c, NMG_EUNSUP, "nmg_create: no transposed kernel for this n");
+  int64_t nfv = 0;
+  for (size_t e = 0; e < m->fv.size(); e++) nfv += m->fv[e] ? 1 : 0;
+  if (nfv > 0 && nfv < m->nelem)
+    return set_err(c, NMG_EUNSUP, "nmg_create: mixed DG / finite-volume meshes are not supported");
+  c->fv = nfv > 0;
+  if (c->fv) {
+    c->nvariants = nmgk::fv_variants(m->n, c->variants, kMaxVariants);
+    if (c->nvariants == 0) return set_err(c, NMG_EUNSUP, "nmg_create: finite-volume n must be in [2,13]");
+  } else {
+    c->nvariants = nmgk::eo_variants(m->n, c->variants, kMaxVariants);
+    c->nvariants += nmgk::gather_variants(m->n, c->variants + c->nvariants,
+                                          kMaxVariants - c->nvariants);
+    if (c->nvariants == 0) return set_err(c, NMG_EUNSUP, "nmg_create: n must be in [2,12]");
+    if (nmgk::vjp_variants(m->n, &c->vjp, 1) != 1)
+      return set_err(c, NMG_EUNSUP, "nmg_create: no transposed kernel for this n");
+  }
   int dev = 0;
   CK(cudaGetDevice(&dev));
   const int n = m->n, np = n * n * n, nn = n * n;
@@ -355,12 +418,17 @@ int nmg_create(const nmg_mesh *m, int32_t bc_kind, const double k[3], nmg_ctx **
   }
   c->ncurvi = C;
   c->nbface = B;
-  std::vector<double> metric, metricp, fac, bxyz, bnrm;
+  std::vector<double> metric, metricp, fac, bxyz, bnrm, fvgeo, fvdist, fvdxb;
   std::vector<int> cmask((size_t)std::max<int64_t>(C, 1), 0);
+  const int64_t Cdg = c->fv ? 0 : C;  // DG metric arrays, FV geometry
+  const int64_t Cfv = c->fv ? C : 0;
   try {
-    metric.assign((size_t)std::max<int64_t>(C, 1) * 9 * np, 0.);
-    metricp.assign((size_t)std::max<int64_t>(C, 1) * 9 * np, 0.);
-    fac.assign((size_t)std::max<int64_t>(C, 1) * 6 * nn * 4, 0.);
+    metric.assign((size_t)std::max<int64_t>(Cdg, 1) * 9 * np, 0.);
+    metricp.assign((size_t)std::max<int64_t>(Cdg, 1) * 9 * np, 0.);
+    fac.assign((size_t)std::max<int64_t>(Cdg, 1) * 6 * nn * 4, 0.);
+    fvgeo.assign((size_t)std::max<int64_t>(Cfv, 1) * 13 * np, 0.);
+    fvdist.assign((size_t)(c->fv ? E : 1) * 6, 0.);
+    fvdxb.assign((size_t)n, 0.);
     bxyz.assign((size_t)std::max<int64_t>(B, 1) * 3 * nn, 0.);
     bnrm.assign((size_t)std::max<int64_t>(B, 1) * 3 * nn, 0.);
   } catch (const std::bad_alloc &) {
@@ -370,7 +438,8 @@ int nmg_create(const nmg_mesh *m, int32_t bc_kind, const double k[3], nmg_ctx **
     const double *X9 = &m->dXdx[(size_t)e * 9 * np];
     const double *sc = &scale[e * 3];
     const int cs = cslot[e];
-    if (cs >= 0) {
+    if (c->fv) fv_pack_element(*m, e, cs, &fvgeo, &fvdist);
+    if (cs >= 0 && !c->fv) {
       double *Mt = &metric[(size_t)cs * 9 * np];
       double *Mp = &metricp[(size_t)cs * 9 * np];
       int mask = 0;
@@ -430,6 +499,13 @@ int nmg_create(const nmg_mesh *m, int32_t bc_kind, const double k[3], nmg_ctx **
         }
     }
   }
+  if (c->fv) {
+    // midpoint spacings of the uniform points (set_nm_nodemidpoint_distsXb_dir)
+    std::vector<double> Xb(n), Xbm(std::max(n - 1, 1));
+    for (int i = 0; i < n; i++) Xb[i] = m->x[i];
+    for (int i = 0; i < n - 1; i++) Xbm[i] = 0.5 * (Xb[i] + Xb[i + 1]);
+    for (int i = 1; i < n - 1; i++) fvdxb[i] = Xbm[i] - Xbm[i - 1];
+  }
   std::vector<int> code(m->code.begin(), m->code.end());
   CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
   auto up = [&](auto **dst, const auto &vec) -> cudaError_t {
@@ -451,7 +527,13 @@ int nmg_create(const nmg_mesh *m, int32_t bc_kind, const double k[3], nmg_ctx **
   CK(up(&c->d_bxyz, bxyz));
   CK(up(&c->d_bnrm, bnrm));
   CK(up(&c->d_D, m->D));
-  CK(nmgk::eo_upload(n, m->D.data()));
+  if (c->fv) {
+    CK(up(&c->d_fvgeo, fvgeo));
+    CK(up(&c->d_fvdist, fvdist));
+    CK(up(&c->d_fvdxb, fvdxb));
+  } else {
+    CK(nmgk::eo_upload(n, m->D.data()));
+  }
   for (int b = 0; b < 4; b++) {
     CK(cudaMalloc((void **)&c->d_buf[b], c->state_len * sizeof(double)));
     CK(cudaMemset(c->d_buf[b], 0, c->state_len * sizeof(double)));
@@ -462,12 +544,34 @@ int nmg_create(const nmg_mesh *m, int32_t bc_kind, const double k[3], nmg_ctx **
     std::memset(&P0, 0, sizeof(P0));
     CK(c->variants[v].launch(P0, c->stream));  // nelem == 0: only sets the smem limit
   }
-  {
+  if (!c->fv) {
     StageParams P0;
     std::memset(&P0, 0, sizeof(P0));
     CK(c->vjp.launch(P0, c->stream));
+  } else {
+    for (int v = 0; v < c->nvariants; v++) {
+      StageParams P0;
+      std::memset(&P0, 0, sizeof(P0));
+      P0.n = n;
+      CK(c->variants[v].launch(P0, c->stream));  // smem limit of this n
+    }
   }
   CK(cudaDeviceSynchronize());
+  return NMG_OK;
+}
+
+int nmg_set_fv(nmg_ctx *c, int32_t rec, int32_t extrap, double w3ratio) {
+  if (!c) return NMG_EINVAL;
+  if (!c->fv) return set_err(c, NMG_EUNSUP, "nmg_set_fv: the mesh has no finite-volume elements");
+  if (rec < NMG_FV_REC_1 || rec > NMG_FV_REC_WENOM5_2)
+    return set_err(c, NMG_EINVAL, "nmg_set_fv: unknown reconstruction");
+  if (extrap != NMG_FV_EXTRAP_NO && extrap != NMG_FV_EXTRAP_DNFN1)
+    return set_err(c, NMG_EINVAL, "nmg_set_fv: unknown div(f) extrapolation");
+  if (!(w3ratio > 0.)) return set_err(c, NMG_EINVAL, "nmg_set_fv: w3ratio must be > 0");
+  c->fv_rec = rec;
+  c->fv_extrap = extrap;
+  c->fv_w3ratio = w3ratio;
+  drop_graphs(c);
   return NMG_OK;
 }
 
@@ -478,6 +582,7 @@ void nmg_destroy(nmg_ctx *c) {
   cudaFree(c->d_cmask); cudaFree(c->d_scale); cudaFree(c->d_gcart); cudaFree(c->d_metric);
   cudaFree(c->d_metricp); cudaFree(c->d_fac); cudaFree(c->d_bxyz); cudaFree(c->d_bnrm);
   cudaFree(c->d_D);
+  cudaFree(c->d_fvgeo); cudaFree(c->d_fvdist); cudaFree(c->d_fvdxb);
   for (int b = 0; b < 4; b++) cudaFree(c->d_buf[b]);
   cudaFree(c->d_times); cudaFree(c->d_step);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -665,6 +770,7 @@ int nmg_rhs_vjp(nmg_ctx *c, double t, const double *w_dev, const double *rbar_de
   (void)w_dev;  // the RHS is linear in w: its Jacobian does not depend on w
   if (!c || !rbar_dev || !wbar_dev || rbar_dev == wbar_dev)
     return set_err(c, NMG_EINVAL, "nmg_rhs_vjp: need distinct rbar and wbar device buffers");
+  if (c->fv) return set_err(c, NMG_EUNSUP, "nmg_rhs_vjp: finite-volume RHS is nonlinear");
   StageParams P = base_params(c);
   P.win = rbar_dev;
   P.rout = wbar_dev;
@@ -678,6 +784,7 @@ int nmg_rhs_vjp(nmg_ctx *c, double t, const double *w_dev, const double *rbar_de
 int nmg_rk4_step_vjp(nmg_ctx *c, double t, double dt, const double *u_n_dev, double *ubar_dev) {
   (void)u_n_dev;  // linear RHS: the step's Jacobian is P(dt L), independent of u_n
   if (!c || !ubar_dev) return set_err(c, NMG_EINVAL, "nmg_rk4_step_vjp: null argument");
+  if (c->fv) return set_err(c, NMG_EUNSUP, "nmg_rk4_step_vjp: finite-volume RHS is nonlinear");
   double *acc = c->d_buf[1 - c->cur];  // free between steps
   int rc = step_buffers(c, c->vjp, t, dt, ubar_dev, acc, c->d_buf[2], c->d_buf[3]);
   if (rc) return rc;
@@ -692,6 +799,7 @@ int nmg_rk4_step_vjp(nmg_ctx *c, double t, double dt, const double *u_n_dev, dou
 // ckpt_every steps and the states of each segment recomputed in reverse.
 int nmg_adjoint_gradient(nmg_ctx *c, double t0, double dt, int32_t nsteps, int32_t ckpt_every,
                          const double *weight_dev, double *J, double *grad_dev) {
+  if (c && c->fv) return set_err(c, NMG_EUNSUP, "nmg_adjoint_gradient: finite-volume RHS is nonlinear");
   if (!c || !weight_dev || !J || !grad_dev || nsteps <= 0 || ckpt_every <= 0)
     return set_err(c, NMG_EINVAL, "nmg_adjoint_gradient: bad argument");
   int rc = autotune(c);
@@ -1014,6 +1122,8 @@ int nmg_batch_create(const nmg_mesh *const *meshes, int32_t count, int32_t bc_ki
   std::vector<int> orders;
   for (int p = 0; p < count; p++) {
     if (!meshes[p]) return batch_err(b, NMG_EINVAL, "nmg_batch_create: null mesh");
+    if (!meshes[p]->fv.empty())
+      return batch_err(b, NMG_EUNSUP, "nmg_batch_create: finite-volume meshes are not batched");
     const int n = meshes[p]->n;
     if (nmgk::batch_epb(n) <= 0)
       return batch_err(b, NMG_EUNSUP, "nmg_batch_create: orders n in [2,10] only");

@@ -54,6 +54,14 @@ struct StageParams {
   int bc;               // NMG_BC_*
   double k0, k1, k2, om;
   const double *D;      // [n][n] D[i*n+j] = l_j'(x_i)
+  // finite-volume elements (stage_fv.cu)
+  int n;                // points per direction
+  int fv_rec;           // NMG_FV_REC_*
+  int fv_extrap;        // NMG_FV_EXTRAP_*
+  double fv_w3ratio;    // WENOm3 optimal-weight ratio
+  const double *fvgeo;  // [C][13][np]: 1/J, sqrtgdiag[3], unit normals n_d[3] (d-major)
+  const double *fvdist; // [E][6] distance (element coords) of each face to its nearest midpoint
+  const double *fvdxb;  // [n] midpoint spacings dXb[i] = Xbm[i] - Xbm[i-1], 1 <= i <= n-2
 };
 
 template <int N>
@@ -304,5 +312,9 @@ cudaError_t batch_launch(const StageParams *d_params, const int *d_gn, const int
                          int ngroup, int ntile, int grid, size_t smem, cudaStream_t st);
 // even-odd coefficients of D for n into constant memory
 cudaError_t eo_upload(int n, const double *D);
+// finite-volume stage kernels (all n up to kFvMaxN)
+constexpr int kFvMaxN = 13;
+size_t fv_smem(int n);
+int fv_variants(int n, Variant *out, int cap);
 
 }  // namespace nmgk

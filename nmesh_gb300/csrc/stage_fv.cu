@@ -1,0 +1,402 @@
+// stage_fv.cu -- fused finite-volume RHS + RK4 stage kernel for elements in
+// the reference's finite-volume mode (scalarwave1, FP64).
+//
+// Reference semantics (paths within nmeshsource/nmesh):
+//   fv_divf            src/main/dg/fv.c:115-624 (use_only_right_flux,
+//                      coordinates_midpoint_data = no, fv_flux = fnum)
+//   midpoint states    src/tests/scalarwave1/scalarwave1.c:761-802
+//   WENO3 / WENOm3_2   src/main/dg/rec1d.c:16-27,121-227,880-1030
+//   WENO5 / WENOm5_2   src/main/dg/rec1d.c:1186-1368
+//   dnfn extrapolation src/main/dg/rec1d.c:542-628 (s1 = 0, s2 = DBL_MAX)
+//   face fluxes        src/tests/scalarwave1/scalarwave1.c:139-209,
+//                      src/main/dg/numflux1d.c:85-112
+//   surface terms      src/main/dg/dg.c:30-151 (fin.-vol. weight 1/|distXb|)
+//   stage update       src/main/evolve/RungeKutta.c:19-82
+//
+// This file is compiled with -fmad=false: every FP64 product and sum is
+// rounded separately in the reference's order, and IEEE division and
+// square root are used, so on meshes without exact-data outer faces
+// (whose sin/cos come from a different math library) the result equals the
+// reference's bit for bit.
+//
+// Work split inside one CTA (one element): the element's pi, c state is
+// staged in shared memory; per direction, one thread per midpoint
+// reconstructs the left/right states of the four fluxed fields and forms
+// the LLF flux (stored in shared memory), then one thread per node forms
+// the conservative difference with the J sqrtgdiag / dXb factors and
+// accumulates div f; the face terms and the RK4 update follow.
+#include <cuda_runtime.h>
+
+#include "stage.cuh"
+
+namespace nmgk {
+namespace {
+
+constexpr int kGeo = 13;  // per-node FV geometry of curvilinear elements
+
+__device__ __forceinline__ double weno3_p(const double *q, double o0, double o1, double l00,
+                                          double l01, double l10, double l11) {
+  // q[0..2] = u[im-1], u[im], u[im+1]  (rec1d_p_WENO3, u_scale = 1)
+  const double d1 = q[1] - q[0], d2 = q[2] - q[1];
+  const double b1 = d1 * d1 + 1e-6 * 1.0, b2 = d2 * d2 + 1e-6 * 1.0;
+  const double ob1 = o0 / (b1 * b1), ob2 = o1 / (b2 * b2);
+  const double sum = ob1 + ob2;
+  const double w1 = ob1 / sum, w2 = ob2 / sum;
+  const double u1 = l00 * q[0] + l01 * q[1], u2 = l10 * q[1] + l11 * q[2];
+  return w1 * u1 + w2 * u2;
+}
+
+__device__ __forceinline__ double weno3_m(const double *q, double o0, double o1, double l00,
+                                          double l01, double l10, double l11) {
+  // q[0..2] = u[im], u[im+1], u[im+2]  (rec1d_m_WENO3)
+  const double d1 = q[1] - q[0], d2 = q[2] - q[1];
+  const double b1 = d1 * d1 + 1e-6 * 1.0, b2 = d2 * d2 + 1e-6 * 1.0;
+  const double ob1 = o0 / (b1 * b1), ob2 = o1 / (b2 * b2);
+  const double sum = ob1 + ob2;
+  const double w1 = ob1 / sum, w2 = ob2 / sum;
+  const double u1 = l00 * q[0] + l01 * q[1], u2 = l10 * q[1] + l11 * q[2];
+  return w1 * u1 + w2 * u2;
+}
+
+#define NMG_C1312 (1.083333333333333333333333)
+
+// q[0..4] = u[im-2..im+2]  (rec1d_p_WENO5_uniform)
+__device__ __forceinline__ double weno5_p(const double *q) {
+  const double oo6 = 1 / 6.;
+  const double b01 = q[0] - 2. * q[1] + q[2], b02 = q[0] - 4. * q[1] + 3. * q[2];
+  const double b11 = q[1] - 2. * q[2] + q[3], b12 = q[1] - q[3];
+  const double b21 = q[2] - 2. * q[3] + q[4], b22 = 3. * q[2] - 4. * q[3] + q[4];
+  const double b0 = NMG_C1312 * b01 * b01 + 0.25 * b02 * b02;
+  const double b1 = NMG_C1312 * b11 * b11 + 0.25 * b12 * b12;
+  const double b2 = NMG_C1312 * b21 * b21 + 0.25 * b22 * b22;
+  const double e0 = b0 + 1e-40 * 1.0, e1 = b1 + 1e-40 * 1.0, e2 = b2 + 1e-40 * 1.0;
+  const double o0 = 1. / (e0 * e0), o1 = 6. / (e1 * e1), o2 = 3. / (e2 * e2);
+  const double oos = 1. / (o0 + o1 + o2);
+  const double w0 = o0 * oos, w1 = o1 * oos, w2 = o2 * oos;
+  const double u0 = (2. * oo6) * q[0] + (-7. * oo6) * q[1] + (11. * oo6) * q[2];
+  const double u1 = (-oo6) * q[1] + (5. * oo6) * q[2] + (2. * oo6) * q[3];
+  const double u2 = (2. * oo6) * q[2] + (5. * oo6) * q[3] + (-oo6) * q[4];
+  return w0 * u0 + w1 * u1 + w2 * u2;
+}
+
+// q[0..4] = u[im-1..im+3]  (rec1d_m_WENO5_uniform)
+__device__ __forceinline__ double weno5_m(const double *q) {
+  const double oo6 = 1 / 6.;
+  const double b21 = q[2] - 2. * q[3] + q[4], b22 = 3. * q[2] - 4. * q[3] + q[4];
+  const double b11 = q[1] - 2. * q[2] + q[3], b12 = q[1] - q[3];
+  const double b01 = q[0] - 2. * q[1] + q[2], b02 = q[0] - 4. * q[1] + 3. * q[2];
+  const double b2 = NMG_C1312 * b21 * b21 + 0.25 * b22 * b22;
+  const double b1 = NMG_C1312 * b11 * b11 + 0.25 * b12 * b12;
+  const double b0 = NMG_C1312 * b01 * b01 + 0.25 * b02 * b02;
+  const double e2 = b2 + 1e-40 * 1.0, e1 = b1 + 1e-40 * 1.0, e0 = b0 + 1e-40 * 1.0;
+  const double o2 = 1. / (e2 * e2), o1 = 6. / (e1 * e1), o0 = 3. / (e0 * e0);
+  const double oos = 1. / (o0 + o1 + o2);
+  const double w2 = o2 * oos, w1 = o1 * oos, w0 = o0 * oos;
+  const double u2 = (11. * oo6) * q[2] + (-7. * oo6) * q[3] + (2. * oo6) * q[4];
+  const double u1 = (2. * oo6) * q[1] + (5. * oo6) * q[2] + (-oo6) * q[3];
+  const double u0 = (-oo6) * q[0] + (5. * oo6) * q[1] + (2. * oo6) * q[2];
+  return w0 * u0 + w1 * u1 + w2 * u2;
+}
+
+// Left (p) and right (m) states at midpoint im of a pencil of n values;
+// v[j] = u[im - 2 + j] for the indices inside the pencil.
+__device__ __forceinline__ double rec_p(int mode, int n, const double *v, int im, double r3) {
+  if (mode == NMG_FV_REC_1) return v[2];
+  if (mode == NMG_FV_REC_WENOM5_2 && im >= 2 && im <= n - 3) return weno5_p(v);
+  if (im >= 1 && im <= n - 2) return weno3_p(v + 1, 1., r3, -0.5, 1.5, 0.5, 0.5);
+  if (n < 3) return v[2];
+  return 0.5 * v[2] + 0.5 * v[3];  // im == 0
+}
+
+__device__ __forceinline__ double rec_m(int mode, int n, const double *v, int im, double r3) {
+  if (mode == NMG_FV_REC_1) return v[3];
+  if (mode == NMG_FV_REC_WENOM5_2 && im >= 1 && im <= n - 4) return weno5_m(v + 1);
+  if (im >= 0 && im <= n - 3) return weno3_m(v + 2, r3, 1., 0.5, 0.5, 1.5, -0.5);
+  if (n < 3) return v[3];
+  return 0.5 * v[2] + 0.5 * v[3];  // im == n-2
+}
+
+__device__ __forceinline__ int fnode(int n, int f, int a, int b) {
+  const int d = f >> 1, p = (f & 1) * (n - 1);
+  return d == 0 ? p + n * (a + n * b) : d == 1 ? a + n * (p + n * b) : a + n * (b + n * p);
+}
+
+// pencil P (in-plane index a + n b of the face-2d plane) -> its i0 = 0 node
+__device__ __forceinline__ int pencil_base(int n, int d, int P) {
+  return fnode(n, 2 * d, P % n, P / n);
+}
+
+// unit normal at node for face 2d+1 (node_normal_at_ijk); the face-2d normal
+// is its negation (x / -m == -(x / m) exactly)
+__device__ __forceinline__ void normal_at(const StageParams &P, const double *G, int np, int d,
+                                          int node, double nr[3]) {
+  if (G) {
+    nr[0] = __ldg(G + (4 + 3 * d + 0) * np + node);
+    nr[1] = __ldg(G + (4 + 3 * d + 1) * np + node);
+    nr[2] = __ldg(G + (4 + 3 * d + 2) * np + node);
+  } else {
+    nr[0] = d == 0 ? 1. : 0.;
+    nr[1] = d == 1 ? 1. : 0.;
+    nr[2] = d == 2 ? 1. : 0.;
+  }
+}
+
+// sqrtgdiag_d and 1/J at node
+__device__ __forceinline__ double sg_at(const double *G, int np, const double *sc, int d,
+                                        int node) {
+  return G ? __ldg(G + (1 + d) * np + node) : sc[d];
+}
+__device__ __forceinline__ double ooj_at(const double *G, int np, double oojc, int node) {
+  return G ? __ldg(G + node) : oojc;
+}
+
+// LLF flux (amax = 1) of the four fluxed fields for normal nr
+__device__ __forceinline__ void llf4(const double *ui, const double *ua, const double nr[3],
+                                     double *fn) {
+  const double fi0 = -(ui[1] * nr[0] + ui[2] * nr[1] + ui[3] * nr[2]);
+  const double fa0 = -(ua[1] * nr[0] + ua[2] * nr[1] + ua[3] * nr[2]);
+  fn[0] = 0.5 * (fa0 + fi0 - (ua[0] - ui[0]));
+#pragma unroll
+  for (int l = 1; l < 4; l++) {
+    const double fil = -ui[0] * nr[l - 1], fal = -ua[0] * nr[l - 1];
+    fn[l] = 0.5 * (fal + fil - (ua[l] - ui[l]));
+  }
+}
+
+// LLF flux f* through face f at face node (a, b) of element e with interior
+// state ui (scalarwave1_fluxes_pt: neighbour trace, exact plane wave or the
+// outgoing-radiation exterior state)
+__device__ void face_fnum(const StageParams &P, int e, int f, int a, int b, const double *ui,
+                          const double nrp[3], double t, double *fn) {
+  const int n = P.n, np = n * n * n, nn = n * n;
+  const double sg = (f & 1) ? 1. : -1.;
+  double nr[3];
+  for (int q = 0; q < 3; q++) nr[q] = sg > 0. ? nrp[q] : -nrp[q];
+  double ua[4];
+  const int nbe = __ldg(P.nb + e * 6 + f);
+  if (nbe >= 0) {
+    const int cd = __ldg(P.code + e * 6 + f), f2 = cd & 7, o = cd >> 3;
+    const int sw = o & 1, fa = (o >> 1) & 1, fb = (o >> 2) & 1;
+    int aa = sw ? b : a, bb = sw ? a : b;
+    aa = fa ? n - 1 - aa : aa;
+    bb = fb ? n - 1 - bb : bb;
+    const double *W2 = P.win + (size_t)nbe * NF * np + fnode(n, f2, aa, bb);
+    for (int l = 0; l < 4; l++) ua[l] = __ldg(W2 + l * np);
+  } else {
+    const int bs = __ldg(P.bslot + e * 6 + f), ab = a + n * b;
+    if (P.bc == NMG_BC_EXACT_PLANEWAVE) {
+      const double *X = P.bxyz + (size_t)bs * 3 * nn + ab;
+      const double arg = P.k0 * X[0] + P.k1 * X[nn] + P.k2 * X[2 * nn] - P.om * t;
+      double sn, cn;
+      sincos(arg, &sn, &cn);
+      ua[0] = -P.om * cn;
+      ua[1] = P.k0 * cn;
+      ua[2] = P.k1 * cn;
+      ua[3] = P.k2 * cn;
+    } else {
+      const double cnv = ui[1] * nr[0] + ui[2] * nr[1] + ui[3] * nr[2];
+      const double wo = ui[0] - cnv;
+      const double pie = 0.5 * wo, cne = -0.5 * wo;
+      ua[0] = pie;
+      for (int l = 0; l < 3; l++) ua[1 + l] = ui[1 + l] + (cne - cnv) * nr[l];
+    }
+  }
+  llf4(ui, ua, nr, fn);
+}
+
+// J sqrtgdiag / dXb factors of node i0 of a pencil (fv.c:384-411)
+__device__ __forceinline__ void jgdow(const double *G, int np, const double *sc, double oojc,
+                                      int d, int n, int base, int st, int i0, double wc,
+                                      bool addsurf, double &JR, double &JL) {
+  const int g0 = i0 > 0, lN = i0 < n - 1;
+  const int ccc = base + i0 * st;
+  const int cccL = base + (g0 ? i0 - 1 : i0) * st, cccR = base + (lN ? i0 : i0 - 1) * st;
+  if (g0 && lN) {
+    JR = sg_at(G, np, sc, d, cccR) / (ooj_at(G, np, oojc, cccR) * wc);
+    JL = sg_at(G, np, sc, d, cccL) / (ooj_at(G, np, oojc, cccL) * wc);
+  } else if (!g0 && lN) {
+    JR = sg_at(G, np, sc, d, cccR) / (ooj_at(G, np, oojc, cccR) * wc);
+    JL = sg_at(G, np, sc, d, ccc) / (ooj_at(G, np, oojc, ccc) * wc);
+  } else if (g0 && !lN) {
+    JR = sg_at(G, np, sc, d, ccc) / (ooj_at(G, np, oojc, ccc) * wc);
+    JL = sg_at(G, np, sc, d, cccL) / (ooj_at(G, np, oojc, cccL) * wc);
+  } else {
+    JR = JL = sg_at(G, np, sc, d, ccc) / (ooj_at(G, np, oojc, ccc) * wc);
+  }
+  if (!addsurf) {
+    JR = (double)lN * JR;
+    JL = (double)g0 * JL;
+  }
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NT) fv_kernel(const StageParams P) {
+  extern __shared__ double smem[];
+  const int n = P.n, np = n * n * n, nn = n * n, nm = n - 1;
+  const int e = blockIdx.x;
+  if (e >= P.nelem) return;
+  double *sW = smem;             // [4][np]  pi, cx, cy, cz of w
+  double *sD = sW + 4 * np;      // [4][np]  div f accumulators
+  double *sF = sD + 4 * np;      // [4][nm][nn] midpoint fluxes of one direction
+  __shared__ double sSc[3], sDist[6], sOoJc;
+  __shared__ int sCs;
+  const double t = stage_time(P);
+  const bool addsurf = P.fv_extrap == NMG_FV_EXTRAP_DNFN1;
+  const double r3 = P.fv_w3ratio;
+
+  if (threadIdx.x == 0) {
+    sCs = __ldg(P.cslot + e);
+    for (int d = 0; d < 3; d++) sSc[d] = __ldg(P.scale + e * 3 + d);
+    sOoJc = sSc[0] * sSc[1] * sSc[2];
+    for (int f = 0; f < 6; f++) sDist[f] = __ldg(P.fvdist + e * 6 + f);
+  }
+  for (int q = threadIdx.x; q < 4 * np; q += NT) {
+    sW[q] = __ldg(P.win + (size_t)e * NF * np + q);
+    sD[q] = 0.;
+  }
+  __syncthreads();
+  const double *G = sCs >= 0 ? P.fvgeo + (size_t)sCs * kGeo * np : nullptr;
+  const double oojc = sOoJc;
+
+#pragma unroll 1
+  for (int d = 0; d < 3; d++) {
+    const int st = d == 0 ? 1 : d == 1 ? n : nn;
+    // midpoint fluxes fnumR of midpoint im (normal at its left node)
+    for (int q = threadIdx.x; q < nm * nn; q += NT) {
+      const int im = q / nn, Pn = q - im * nn;
+      const int base = pencil_base(n, d, Pn);
+      double ui[4], ua[4];
+#pragma unroll
+      for (int l = 0; l < 4; l++) {
+        const double *u = sW + l * np + base;
+        double v[6];
+#pragma unroll
+        for (int j = 0; j < 6; j++) {
+          const int i = im - 2 + j;
+          v[j] = (i >= 0 && i < n) ? u[i * st] : 0.;
+        }
+        ui[l] = rec_p(P.fv_rec, n, v, im, r3);
+        ua[l] = rec_m(P.fv_rec, n, v, im, r3);
+      }
+      double nr[3], fn[4];
+      normal_at(P, G, np, d, base + im * st, nr);
+      llf4(ui, ua, nr, fn);
+#pragma unroll
+      for (int l = 0; l < 4; l++) sF[(l * nm + im) * nn + Pn] = fn[l];
+    }
+    __syncthreads();
+    // conservative difference at every node of the direction's pencils
+    for (int q = threadIdx.x; q < np; q += NT) {
+      const int i0 = q / nn, Pn = q - i0 * nn;
+      const int base = pencil_base(n, d, Pn);
+      const int node = base + i0 * st;
+      const double wc = i0 == 0 ? sDist[2 * d] : i0 == n - 1 ? sDist[2 * d + 1] : __ldg(P.fvdxb + i0);
+      double JR, JL;
+      jgdow(G, np, sSc, oojc, d, n, base, st, i0, wc, addsurf, JR, JL);
+      double fR[4], fL[4];
+      if (i0 < n - 1) {
+        for (int l = 0; l < 4; l++) fR[l] = sF[(l * nm + i0) * nn + Pn];
+      } else if (addsurf) {
+        double ui[4], nr[3];
+        for (int l = 0; l < 4; l++) ui[l] = sW[l * np + node];
+        normal_at(P, G, np, d, node, nr);
+        face_fnum(P, e, 2 * d + 1, Pn % n, Pn / n, ui, nr, t, fR);
+      } else {
+        for (int l = 0; l < 4; l++) fR[l] = 0.;
+      }
+      if (i0 > 0) {
+        for (int l = 0; l < 4; l++) fL[l] = -sF[(l * nm + i0 - 1) * nn + Pn];
+      } else if (addsurf) {
+        double ui[4], nr[3];
+        for (int l = 0; l < 4; l++) ui[l] = sW[l * np + node];
+        normal_at(P, G, np, d, node, nr);
+        face_fnum(P, e, 2 * d, Pn % n, Pn / n, ui, nr, t, fL);
+      } else {
+        for (int l = 0; l < 4; l++) fL[l] = 0.;
+      }
+      double df[4];
+      for (int l = 0; l < 4; l++) df[l] = JR * fR[l] + JL * fL[l];
+      if (addsurf && n > 2 && (i0 == 0 || i0 == n - 1)) {
+        // dnfn extrapolation: df_face = w0 df_face + w1 df_next
+        const int i1 = i0 == 0 ? 1 : n - 2;
+        const double wc1 = (i1 == 0 || i1 == n - 1) ? sDist[2 * d + (i1 != 0)] : __ldg(P.fvdxb + i1);
+        double JR1, JL1;
+        jgdow(G, np, sSc, oojc, d, n, base, st, i1, wc1, addsurf, JR1, JL1);
+        const double w0 = 1. / 0.75, w1 = 1. - w0;
+        for (int l = 0; l < 4; l++) {
+          const double fR1 = sF[(l * nm + i1) * nn + Pn], fL1 = -sF[(l * nm + i1 - 1) * nn + Pn];
+          const double df1 = JR1 * fR1 + JL1 * fL1;
+          df[l] = w0 * df[l] + w1 * df1;
+        }
+      }
+      const double oj = ooj_at(G, np, oojc, node);
+      for (int l = 0; l < 4; l++) sD[l * np + node] += df[l] * oj;
+    }
+    __syncthreads();
+  }
+
+  // surface terms of fin.-vol. faces when fv_divf did not add them
+  if (!addsurf) {
+#pragma unroll 1
+    for (int d = 0; d < 3; d++) {
+      for (int q = threadIdx.x; q < 2 * nn; q += NT) {
+        const int s = q / nn, ab = q - s * nn, f = 2 * d + s;
+        const int a = ab % n, b = ab / n, node = fnode(n, f, a, b);
+        double ui[4], nr[3], fn[4];
+        for (int l = 0; l < 4; l++) ui[l] = sW[l * np + node];
+        normal_at(P, G, np, d, node, nr);
+        face_fnum(P, e, f, a, b, ui, nr, t, fn);
+        const double oow = 1. / sDist[f];
+        const double gd_ow = sg_at(G, np, sSc, d, node) * oow;
+        for (int l = 0; l < 4; l++) sD[l * np + node] += fn[l] * gd_ow;
+      }
+      __syncthreads();
+    }
+  }
+
+  // r = -div f (r_phi = pi) and the RK4 stage update
+  for (int q = threadIdx.x; q < NF * np; q += NT) {
+    const int f = q / np, node = q - f * np;
+    const size_t idx = (size_t)e * NF * np + q;
+    const double r = f < 4 ? -sD[f * np + node] : sW[node];
+    if (P.mode == 0) {
+      P.rout[idx] = r;
+    } else if (P.mode == 1) {
+      const double u = __ldg(P.u0 + idx);
+      P.acc[idx] = u + P.cacc * r;
+      P.wout[idx] = u + P.cw * r;
+    } else if (P.mode == 4) {
+      P.acc[idx] = P.acc[idx] + P.cacc * r;
+    } else {
+      P.acc[idx] = P.acc[idx] + P.cacc * r;
+      P.wout[idx] = __ldg(P.u0 + idx) + P.cw * r;
+    }
+  }
+}
+
+template <int NT>
+cudaError_t launch_fv(const StageParams &P, cudaStream_t st) {
+  const size_t smem = fv_smem(P.n);
+  if (P.nelem == 0)
+    return cudaFuncSetAttribute(fv_kernel<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem);
+  fv_kernel<NT><<<P.nelem, NT, smem, st>>>(P);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+size_t fv_smem(int n) {
+  const size_t np = (size_t)n * n * n, nn = (size_t)n * n;
+  return (8 * np + 4 * (n - 1) * nn) * sizeof(double);
+}
+
+int fv_variants(int n, Variant *out, int cap) {
+  if (n < 2 || n > kFvMaxN || cap < 3) return 0;
+  out[0] = {"fvx", 1, 128, launch_fv<128>};
+  out[1] = {"fvx", 1, 256, launch_fv<256>};
+  out[2] = {"fvx", 1, 512, launch_fv<512>};
+  return 3;
+}
+
+}  // namespace nmgk

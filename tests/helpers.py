@@ -28,11 +28,12 @@ def load(case):
 
 def build_mesh(meta, periodic=False):
     import nmesh_gb300 as ng
+    fv = "fv" in meta
     if meta["mesh"] == "box":
         return ng.Mesh.build(ng.MESH_BOX, n=meta["n"], luni=meta["luni"],
-                             xc=(PI, PI, PI), box_dout=PI, periodic=periodic)
+                             xc=(PI, PI, PI), box_dout=PI, periodic=periodic, fv=fv)
     return ng.Mesh.build(ng.MESH_CUBEDSPHERES7, n=meta["n"], luni=meta["luni"],
-                         cs_dc=1.0, cs_r0fac=20.0)
+                         cs_dc=1.0, cs_r0fac=20.0, fv=fv)
 
 
 def perm_to_mesh(mesh, d):
@@ -52,9 +53,11 @@ def rel_l2(a, b):
     return float(np.linalg.norm((a - b).ravel()) / max(np.linalg.norm(b.ravel()), 1e-300))
 
 
-def oracle_for(mesh, bc=0, k=(1.0, 1.0, 1.0), period=None):
+def oracle_for(mesh, bc=0, k=(1.0, 1.0, 1.0), period=None, fv_rec="WENOm3_2",
+               fv_extrap="dnfn_extrap1", fv_w3ratio=2.0):
     """Oracle mesh built from the product mesh's geometry, with its own
-    coordinate-matching neighbour table."""
+    coordinate-matching neighbour table (and the mesh's finite-volume flags
+    with the given fin.-vol. options)."""
     from oracle import nmo
     pat, bbox = mesh.elements()
     xyz = mesh.coords()
@@ -63,7 +66,10 @@ def oracle_for(mesh, bc=0, k=(1.0, 1.0, 1.0), period=None):
                                                           mesh.np, 1)) else 1
                       for e in range(mesh.nelem)], np.int32)
     nb = nmo.match_faces(xyz, mesh.n, period=period)
-    return nmo.OracleMesh(bbox, curvi, dXdx, xyz, nb, mesh.n, bc=bc, k=k)
+    fv = mesh.fv()
+    return nmo.OracleMesh(bbox, curvi, dXdx, xyz, nb, mesh.n, bc=bc, k=k,
+                          fv=fv if fv.any() else None, fv_rec=fv_rec,
+                          fv_extrap=fv_extrap, fv_w3ratio=fv_w3ratio)
 
 
 def gaussian_pulses(xyz, seed, npulse=8, rmin=3.0, rmax=10.0, wmin=0.5, wmax=2.0,

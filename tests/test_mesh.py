@@ -5,17 +5,44 @@ import numpy as np
 import pytest
 
 import nmesh_gb300 as ng
-from helpers import CASES, PI, build_mesh, load, perm_to_mesh
+from helpers import CASES, FV_CASES, PI, build_mesh, load, perm_to_mesh
 from oracle import nmo
 
 
-@pytest.mark.parametrize("case", CASES)
+@pytest.mark.parametrize("case", CASES + FV_CASES)
 def test_geometry_bitexact(case):
+    """Coordinates and metric on LGL points (DG) and on equally spaced
+    points (finite-volume meshes) equal the reference's."""
     d, meta = load(case)
     m = build_mesh(meta)
     perm = perm_to_mesh(m, d)
     assert np.array_equal(m.coords()[perm], d["x"])
     assert np.array_equal(m.dXdx()[perm], d["dXdx"])
+    if "fv" in meta:
+        assert np.array_equal(m.fv()[perm], d["use_fv"])
+
+
+def test_uniform_points_match_oracle():
+    import ctypes
+    for n in range(1, 20):
+        x = np.zeros(n)
+        assert ng.lib().nmg_uniform_points(n, x.ctypes.data_as(ctypes.c_void_p)) == 0
+        assert np.array_equal(x, nmo.uniform(n))
+
+
+def test_mixed_fv_desc_rejected():
+    m = ng.Mesh.build(ng.MESH_BOX, n=4, luni=1, xc=(0, 0, 0), box_dout=1.0, fv=True)
+    pat, bbox = m.elements()
+    fv = np.zeros(m.nelem, np.int32)
+    fv[0] = 1
+    with pytest.raises(ng.NmgError):
+        ng.Mesh.from_arrays(bbox, np.zeros(m.nelem, np.int32), m.coords(), fv=fv)
+    m2 = ng.Mesh.from_arrays(bbox, np.zeros(m.nelem, np.int32), m.coords(),
+                             fv=np.ones(m.nelem, np.int32))
+    assert m2.fv().all()
+    nb1, code1 = m.faces()
+    nb2, code2 = m2.faces()
+    assert np.array_equal(nb1, nb2) and np.array_equal(code1, code2)
 
 
 def _faces_from_nbnode(nbnode, n):
