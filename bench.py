@@ -268,9 +268,13 @@ def run_ours(args, rank, world, local):
     kinfo = ev.kernel_info()
     state_bytes = int(ev.size * 8)
     batched = None
-    if not args.no_batched and rank == 0:
-        ev.close()  # free the workload's buffers for the batch of problems
-        batched = batched_bench(args)
+    fvres = None
+    if rank == 0 and (not args.no_batched or not args.no_fv):
+        ev.close()  # free the workload's buffers for the sub-benchmarks
+        if not args.no_batched:
+            batched = batched_bench(args)
+        if not args.no_fv:
+            fvres = fv_bench(args)
 
     fp64_peak = ng.fp64_peak_gflops()
     peaks = {}
@@ -326,6 +330,7 @@ def run_ours(args, rank, world, local):
             "cpu_baseline": cpu,
             "adjoint": adjoint,
             "batched": batched,
+            "fv": fvres,
         }
         print(json.dumps(out))
     ev.close()
@@ -421,11 +426,72 @@ def batched_bench(args):
 PI = 3.141592653589793
 
 
-def cpu_mesh(n, luni):
+def fv_bench(args):
+    """All-finite-volume workload: the 7-patch cubed-sphere mesh with every
+    element a finite-volume element on n^3 equally spaced points, WENOm5_2
+    midpoint states, dnfn_extrap1, outgoing boundary, graph-captured RK4
+    steps; the oracle timed on a bounded sample of the same workload."""
+    import torch
+    import nmesh_gb300 as ng
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from helpers import gaussian_pulses
+    n, L = args.fv_n, args.fv_luni
+    rec, ex = "WENOm5_2", "dnfn_extrap1"
+    mesh = ng.Mesh.build(ng.MESH_CUBEDSPHERES7, n=n, luni=L, cs_dc=1.0, cs_r0fac=20.0, fv=True)
+    u0 = gaussian_pulses(mesh.coords(), seed=99)
+    ev = ng.Evolution(mesh, ng.BC_OUTGOING)
+    ev.set_fv(rec, ex)
+    ev.set_state(u0)
+    dt = 0.1 * (2.0 / 2 ** L) / (n - 1)
+    dof = mesh.nelem * mesh.np * NFIELDS
+    stream = torch.cuda.ExternalStream(ev.stream)
+    ev.rk4_steps(0.0, dt, 3)  # autotune, graph capture, warm-up
+    torch.cuda.synchronize()
+    K = args.fv_steps
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    l0 = ev.launches
+    e0.record(stream)
+    ev.rk4_steps(3 * dt, dt, K)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    launches = ev.launches - l0
+    kinfo = ev.kernel_info()
+    state_mb = ev.size * 8 / 1e6
+    ev.close()
+    out = {"workload": f"cubedspheres7 luni={L}, all {mesh.nelem} elements finite-volume "
+                       f"on {n}^3 uniform points, fv_rec={rec}, fv_divf_extrap={ex}, "
+                       f"outgoing boundary", "elements": int(mesh.nelem), "dof": int(dof),
+           "state_mb": state_mb, "steps": K, "ms_per_step": ms / K,
+           "value": dof * 4 * K / (ms / 1e3), "unit": UNIT,
+           "kernel": kinfo.split(" | ")[0], "autotune": kinfo.split(" | timings: ")[-1],
+           "gpu_launches": int(launches)}
+    if not args.no_cpu_baseline:
+        cl = args.fv_cpu_luni
+        cm, om = cpu_mesh(n, cl, fv=True, fv_rec=rec, fv_extrap=ex)
+        u = gaussian_pulses(cm.coords(), seed=99)
+        cdt = 0.1 * (2.0 / 2 ** cl) / (n - 1)
+        om.rk4(u, cdt, 1)
+        t0 = time.perf_counter()
+        om.rk4(u, cdt, args.fv_cpu_steps)
+        t = time.perf_counter() - t0
+        cdof = cm.nelem * cm.np * NFIELDS
+        threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count()))
+        out["cpu_baseline"] = {
+            "value": cdof * 4 * args.fv_cpu_steps / t, "unit": UNIT, "cores": threads,
+            "kind": "port",
+            "sample": f"{args.fv_cpu_steps} RK4 steps of the same workload at level {cl} "
+                      f"({cm.nelem} elements, {cdof} DOF), {t:.2f} s"}
+    return out
+
+
+def cpu_mesh(n, luni, fv=False, fv_rec="WENOm5_2", fv_extrap="dnfn_extrap1"):
     """Oracle mesh of the workload, neighbour table from the packed mesh."""
     import nmesh_gb300 as ng
     from oracle import nmo
-    mesh = ng.Mesh.build(ng.MESH_CUBEDSPHERES7, n=n, luni=luni, cs_dc=1.0, cs_r0fac=20.0)
+    mesh = ng.Mesh.build(ng.MESH_CUBEDSPHERES7, n=n, luni=luni, cs_dc=1.0, cs_r0fac=20.0,
+                         fv=fv)
     pat, bbox = mesh.elements()
     xyz = mesh.coords()
     nb, code = mesh.faces()
@@ -446,7 +512,9 @@ def cpu_mesh(n, luni):
             idx2 = planes[f2][aa + n * bb]
             es, fs = np.nonzero(sel)
             nbnode[es, fs, :] = nb[es, fs][:, None] * npt + idx2[None, :]
-    om = nmo.OracleMesh(bbox, (pat > 0).astype(np.int32), mesh.dXdx(), xyz, nbnode, n, bc=1)
+    fvk = dict(fv=mesh.fv(), fv_rec=fv_rec, fv_extrap=fv_extrap) if fv else {}
+    om = nmo.OracleMesh(bbox, (pat > 0).astype(np.int32), mesh.dXdx(), xyz, nbnode, n, bc=1,
+                        **fvk)
     return mesh, om
 
 
@@ -522,6 +590,12 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batch-problems", type=int, default=64)
     ap.add_argument("--batch-steps", type=int, default=5)
+    ap.add_argument("--no-fv", action="store_true")
+    ap.add_argument("--fv-n", type=int, default=13)
+    ap.add_argument("--fv-luni", type=int, default=3)
+    ap.add_argument("--fv-steps", type=int, default=5)
+    ap.add_argument("--fv-cpu-luni", type=int, default=2)
+    ap.add_argument("--fv-cpu-steps", type=int, default=2)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
