@@ -11,7 +11,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libnmg.so")
-SOURCES = ["nmg.cu", "stage_eo.cu", "stage_gather.cu", "stage_fv.cu", "noalloc.cu", "mesh.cpp"]
+SOURCES = ["nmg.cu", "stage_eo.cu", "stage_gather.cu", "stage_fv.cu", "stage_fv_fast.cu",
+           "noalloc.cu", "mesh.cpp"]
 # per-file extra flags: the finite-volume kernel rounds every product and sum
 # separately, in the reference's order (no FMA contraction)
 EXTRA_FLAGS = {"stage_fv.cu": ["-fmad=false"]}

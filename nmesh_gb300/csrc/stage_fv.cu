@@ -13,11 +13,17 @@
 //   surface terms      src/main/dg/dg.c:30-151 (fin.-vol. weight 1/|distXb|)
 //   stage update       src/main/evolve/RungeKutta.c:19-82
 //
-// This file is compiled with -fmad=false: every FP64 product and sum is
-// rounded separately in the reference's order, and IEEE division and
-// square root are used, so on meshes without exact-data outer faces
-// (whose sin/cos come from a different math library) the result equals the
-// reference's bit for bit.
+// Two variants are built from this file:
+//   "fvx" (this translation unit, compiled with -fmad=false): every FP64
+//         product and sum is rounded separately in the reference's order,
+//         with IEEE division, so on meshes without exact-data outer faces
+//         (whose sin/cos come from a different math library) the result
+//         equals the reference's bit for bit;
+//   "fv"  (stage_fv_fast.cu defines NMG_FV_FAST and includes this file):
+//         FMA contraction allowed and the nonlinear weights normalised with
+//         one division per reconstruction, w_k = g_k prod_{j!=k} e_j^2 /
+//         sum_k g_k prod_{j!=k} e_j^2 (the same weights as g_k/e_k^2 over
+//         their sum, in exact arithmetic); within FP64 rounding of "fvx".
 //
 // Work split inside one CTA (one element): the element's pi, c state is
 // staged in shared memory; per direction, one thread per midpoint
@@ -29,7 +35,16 @@
 
 #include "stage.cuh"
 
+#ifdef NMG_FV_FAST
+#define NMG_FVNS fv_fast
+#define NMG_FV_NAME "fv"
+#else
+#define NMG_FVNS fv_exact
+#define NMG_FV_NAME "fvx"
+#endif
+
 namespace nmgk {
+namespace NMG_FVNS {
 namespace {
 
 constexpr int kGeo = 13;  // per-node FV geometry of curvilinear elements
@@ -39,11 +54,16 @@ __device__ __forceinline__ double weno3_p(const double *q, double o0, double o1,
   // q[0..2] = u[im-1], u[im], u[im+1]  (rec1d_p_WENO3, u_scale = 1)
   const double d1 = q[1] - q[0], d2 = q[2] - q[1];
   const double b1 = d1 * d1 + 1e-6 * 1.0, b2 = d2 * d2 + 1e-6 * 1.0;
+  const double u1 = l00 * q[0] + l01 * q[1], u2 = l10 * q[1] + l11 * q[2];
+#ifdef NMG_FV_FAST
+  const double w1 = o0 * (b2 * b2), w2 = o1 * (b1 * b1);
+  return (w1 * u1 + w2 * u2) / (w1 + w2);
+#else
   const double ob1 = o0 / (b1 * b1), ob2 = o1 / (b2 * b2);
   const double sum = ob1 + ob2;
   const double w1 = ob1 / sum, w2 = ob2 / sum;
-  const double u1 = l00 * q[0] + l01 * q[1], u2 = l10 * q[1] + l11 * q[2];
   return w1 * u1 + w2 * u2;
+#endif
 }
 
 __device__ __forceinline__ double weno3_m(const double *q, double o0, double o1, double l00,
@@ -51,11 +71,16 @@ __device__ __forceinline__ double weno3_m(const double *q, double o0, double o1,
   // q[0..2] = u[im], u[im+1], u[im+2]  (rec1d_m_WENO3)
   const double d1 = q[1] - q[0], d2 = q[2] - q[1];
   const double b1 = d1 * d1 + 1e-6 * 1.0, b2 = d2 * d2 + 1e-6 * 1.0;
+  const double u1 = l00 * q[0] + l01 * q[1], u2 = l10 * q[1] + l11 * q[2];
+#ifdef NMG_FV_FAST
+  const double w1 = o0 * (b2 * b2), w2 = o1 * (b1 * b1);
+  return (w1 * u1 + w2 * u2) / (w1 + w2);
+#else
   const double ob1 = o0 / (b1 * b1), ob2 = o1 / (b2 * b2);
   const double sum = ob1 + ob2;
   const double w1 = ob1 / sum, w2 = ob2 / sum;
-  const double u1 = l00 * q[0] + l01 * q[1], u2 = l10 * q[1] + l11 * q[2];
   return w1 * u1 + w2 * u2;
+#endif
 }
 
 #define NMG_C1312 (1.083333333333333333333333)
@@ -70,13 +95,19 @@ __device__ __forceinline__ double weno5_p(const double *q) {
   const double b1 = NMG_C1312 * b11 * b11 + 0.25 * b12 * b12;
   const double b2 = NMG_C1312 * b21 * b21 + 0.25 * b22 * b22;
   const double e0 = b0 + 1e-40 * 1.0, e1 = b1 + 1e-40 * 1.0, e2 = b2 + 1e-40 * 1.0;
-  const double o0 = 1. / (e0 * e0), o1 = 6. / (e1 * e1), o2 = 3. / (e2 * e2);
-  const double oos = 1. / (o0 + o1 + o2);
-  const double w0 = o0 * oos, w1 = o1 * oos, w2 = o2 * oos;
   const double u0 = (2. * oo6) * q[0] + (-7. * oo6) * q[1] + (11. * oo6) * q[2];
   const double u1 = (-oo6) * q[1] + (5. * oo6) * q[2] + (2. * oo6) * q[3];
   const double u2 = (2. * oo6) * q[2] + (5. * oo6) * q[3] + (-oo6) * q[4];
+#ifdef NMG_FV_FAST
+  const double a0 = e0 * e0, a1 = e1 * e1, a2 = e2 * e2;
+  const double w0 = 1. * (a1 * a2), w1 = 6. * (a0 * a2), w2 = 3. * (a0 * a1);
+  return (w0 * u0 + w1 * u1 + w2 * u2) / (w0 + w1 + w2);
+#else
+  const double o0 = 1. / (e0 * e0), o1 = 6. / (e1 * e1), o2 = 3. / (e2 * e2);
+  const double oos = 1. / (o0 + o1 + o2);
+  const double w0 = o0 * oos, w1 = o1 * oos, w2 = o2 * oos;
   return w0 * u0 + w1 * u1 + w2 * u2;
+#endif
 }
 
 // q[0..4] = u[im-1..im+3]  (rec1d_m_WENO5_uniform)
@@ -89,13 +120,19 @@ __device__ __forceinline__ double weno5_m(const double *q) {
   const double b1 = NMG_C1312 * b11 * b11 + 0.25 * b12 * b12;
   const double b0 = NMG_C1312 * b01 * b01 + 0.25 * b02 * b02;
   const double e2 = b2 + 1e-40 * 1.0, e1 = b1 + 1e-40 * 1.0, e0 = b0 + 1e-40 * 1.0;
-  const double o2 = 1. / (e2 * e2), o1 = 6. / (e1 * e1), o0 = 3. / (e0 * e0);
-  const double oos = 1. / (o0 + o1 + o2);
-  const double w2 = o2 * oos, w1 = o1 * oos, w0 = o0 * oos;
   const double u2 = (11. * oo6) * q[2] + (-7. * oo6) * q[3] + (2. * oo6) * q[4];
   const double u1 = (2. * oo6) * q[1] + (5. * oo6) * q[2] + (-oo6) * q[3];
   const double u0 = (-oo6) * q[0] + (5. * oo6) * q[1] + (2. * oo6) * q[2];
+#ifdef NMG_FV_FAST
+  const double a0 = e0 * e0, a1 = e1 * e1, a2 = e2 * e2;
+  const double w2 = 1. * (a0 * a1), w1 = 6. * (a0 * a2), w0 = 3. * (a1 * a2);
+  return (w0 * u0 + w1 * u1 + w2 * u2) / (w0 + w1 + w2);
+#else
+  const double o2 = 1. / (e2 * e2), o1 = 6. / (e1 * e1), o0 = 3. / (e0 * e0);
+  const double oos = 1. / (o0 + o1 + o2);
+  const double w2 = o2 * oos, w1 = o1 * oos, w0 = o0 * oos;
   return w0 * u0 + w1 * u1 + w2 * u2;
+#endif
 }
 
 // Left (p) and right (m) states at midpoint im of a pencil of n values;
@@ -386,17 +423,31 @@ cudaError_t launch_fv(const StageParams &P, cudaStream_t st) {
 
 }  // namespace
 
+int variants(int n, Variant *out, int cap) {
+  if (n < 2 || n > kFvMaxN || cap < 3) return 0;
+  out[0] = {NMG_FV_NAME, 1, 128, launch_fv<128>};
+  out[1] = {NMG_FV_NAME, 1, 256, launch_fv<256>};
+  out[2] = {NMG_FV_NAME, 1, 512, launch_fv<512>};
+  return 3;
+}
+
+}  // namespace NMG_FVNS
+
+#ifndef NMG_FV_FAST
+namespace fv_fast {
+int variants(int n, Variant *out, int cap);
+}
+
 size_t fv_smem(int n) {
   const size_t np = (size_t)n * n * n, nn = (size_t)n * n;
   return (8 * np + 4 * (n - 1) * nn) * sizeof(double);
 }
 
+// the fast variants first, then the exact ones
 int fv_variants(int n, Variant *out, int cap) {
-  if (n < 2 || n > kFvMaxN || cap < 3) return 0;
-  out[0] = {"fvx", 1, 128, launch_fv<128>};
-  out[1] = {"fvx", 1, 256, launch_fv<256>};
-  out[2] = {"fvx", 1, 512, launch_fv<512>};
-  return 3;
+  int k = fv_fast::variants(n, out, cap);
+  return k + fv_exact::variants(n, out + k, cap - k);
 }
+#endif
 
 }  // namespace nmgk

@@ -16,7 +16,11 @@ from helpers import (FV_CASES, PI, RTOL_RHS, RTOL_RK4, build_mesh, gaussian_puls
 
 pytestmark = pytest.mark.gpu
 
-FV_VARIANTS = ["fvx:1:128", "fvx:1:256", "fvx:1:512"]
+# "fvx": reference operation order, no FMA; "fv": FMA and one division per
+# WENO reconstruction (within FP64 rounding)
+FV_EXACT = ["fvx:1:128", "fvx:1:256", "fvx:1:512"]
+FV_FAST = ["fv:1:128", "fv:1:256", "fv:1:512"]
+FV_VARIANTS = FV_EXACT + FV_FAST
 
 
 @pytest.fixture(autouse=True)
@@ -43,12 +47,14 @@ def test_fv_rhs_matches_reference(case, variant):
     assert np.abs(r[perm] - d["r0"]).max() <= 1e-11 * np.abs(d["r0"]).max()
 
 
+@pytest.mark.parametrize("variant", ["fvx", "fv", "auto"])
 @pytest.mark.parametrize("case", FV_CASES)
-def test_fv_rk4_matches_reference(case):
+def test_fv_rk4_matches_reference(case, variant):
     d, meta = load(case)
     m = build_mesh(meta)
     perm = perm_to_mesh(m, d)
     ev = _ev(m, meta)
+    ev.set_kernel(variant)
     u = ev.rk4_steps_host(to_mesh_order(d["u0"], perm), 0.0, meta["dt"], meta["steps"])
     assert rel_l2(u[perm], d["u_final"]) <= RTOL_RK4
 
@@ -61,6 +67,7 @@ def test_fv_rhs_vs_oracle_with_reference_data(case):
     m = build_mesh(meta)
     perm = perm_to_mesh(m, d)
     ev = _ev(m, meta)
+    ev.set_kernel("fvx")
     u = to_mesh_order(d["u0"], perm)
     r = ev.rhs(u, 0.0)
     o = oracle_for(m, bc=0, k=meta["k"], fv_rec=meta["fv"]["rec"],
@@ -88,10 +95,16 @@ def test_fv_periodic_box_bitexact_vs_oracle(n, luni, rec, extrap):
     u += 0.2 * rng.standard_normal(u.shape)
     ev = ng.Evolution(m, ng.BC_OUTGOING)
     ev.set_fv(rec, extrap)
+    ev.set_kernel("fvx")
     o = oracle_for(m, bc=1, period=2 * PI, fv_rec=rec, fv_extrap=extrap)
-    assert np.array_equal(ev.rhs(u, 0.0), o.rhs(u, 0.0))
+    ro = o.rhs(u, 0.0)
+    assert np.array_equal(ev.rhs(u, 0.0), ro)
     dt = 0.05 * (2 * PI / 2 ** luni) / n
-    assert np.array_equal(ev.rk4_steps_host(u, 0.0, dt, 3), o.rk4(u, dt, 3))
+    uo = o.rk4(u, dt, 3)
+    assert np.array_equal(ev.rk4_steps_host(u, 0.0, dt, 3), uo)
+    ev.set_kernel("fv")
+    assert rel_l2(ev.rhs(u, 0.0), ro) <= RTOL_RHS
+    assert rel_l2(ev.rk4_steps_host(u, 0.0, dt, 3), uo) <= RTOL_RK4
 
 
 @pytest.mark.parametrize("rec,extrap", [("WENOm5_2", "dnfn_extrap1"), ("WENOm3_2", "no")])
@@ -102,10 +115,16 @@ def test_fv_cubed_spheres_outgoing_bitexact_vs_oracle(n, luni, rec, extrap):
     u += 1e-2 * np.random.default_rng(n).standard_normal(u.shape)
     ev = ng.Evolution(m, ng.BC_OUTGOING)
     ev.set_fv(rec, extrap)
+    ev.set_kernel("fvx")
     o = oracle_for(m, bc=1, fv_rec=rec, fv_extrap=extrap)
-    assert np.array_equal(ev.rhs(u, 0.0), o.rhs(u, 0.0))
+    ro = o.rhs(u, 0.0)
+    assert np.array_equal(ev.rhs(u, 0.0), ro)
     dt = 0.02 / n
-    assert np.array_equal(ev.rk4_steps_host(u, 0.0, dt, 2), o.rk4(u, dt, 2))
+    uo = o.rk4(u, dt, 2)
+    assert np.array_equal(ev.rk4_steps_host(u, 0.0, dt, 2), uo)
+    ev.set_kernel("fv")
+    assert rel_l2(ev.rhs(u, 0.0), ro) <= RTOL_RHS
+    assert rel_l2(ev.rk4_steps_host(u, 0.0, dt, 2), uo) <= RTOL_RK4
 
 
 def test_fv_variants_bitwise_identical_and_graph_steps():
@@ -117,8 +136,13 @@ def test_fv_variants_bitwise_identical_and_graph_steps():
     for v in FV_VARIANTS:
         ev.set_kernel(v)
         outs.append(ev.rk4_steps_host(u, 0.0, 0.002, 4))
-    for o in outs[1:]:
+    # the thread count does not change any thread's arithmetic
+    for o in outs[1:3]:
         assert np.array_equal(o, outs[0])
+    for o in outs[4:]:
+        assert np.array_equal(o, outs[3])
+    assert rel_l2(outs[3], outs[0]) <= RTOL_RK4
+    ev.set_kernel("fvx:1:256")
     # the single-step path equals the graph-captured multi-step path
     ev.set_state(u)
     t = 0.0
@@ -127,7 +151,8 @@ def test_fv_variants_bitwise_identical_and_graph_steps():
         t += 0.002
     assert np.array_equal(ev.get_state(), outs[0])
     ev.set_kernel("auto")
-    assert "fvx" in ev.kernel_info()
+    ev.rhs(u)
+    assert "fvx" in ev.kernel_info() and "fv:1:256" in ev.kernel_info()
 
 
 def test_fv_rejections():
