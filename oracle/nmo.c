@@ -38,6 +38,11 @@
  *   midpoint states      src/tests/scalarwave1/scalarwave1.c:761-802
  *   fin.-vol. surface    src/main/dg/dg.c:58-70,81-90 (oow = 1/|distXb|,
  *                        F = f*)
+ *   DG / FV interfaces   src/main/amr/surface.c:1080-1250 (neighbour trace
+ *                        interpolated onto the face points: Lagrange from a
+ *                        DG neighbour, piecewise linear from a fin.-vol.
+ *                        one), src/main/basis/interpolate.c:53-100,296-360,
+ *                        src/main/basis/Lagrange.c:15-27,151-159
  *
  * Extensions without a reference counterpart (restated, parity unpinned):
  *   BC kind 1: outgoing-radiation outer boundary (characteristic upwinding
@@ -63,7 +68,8 @@ typedef struct nmo_mesh {
   const double *dXdx;       /* [e][9][np] dX^a/dx^i (a-major); may be NULL if no curvi */
   const double *xyz;        /* [e][3][np] Cartesian coordinates */
   const int64_t *nbnode;    /* [e][6][n*n] global index e'*np+ijk' of the
-                               coincident node across the face, -1 = outer */
+                               coincident node across the face, -1 = outer,
+                               -2 = neighbour with the other point type */
   int bc;                   /* outer faces: 0 exact plane wave, 1 outgoing */
   double k[3];              /* plane-wave vector for bc 0 */
   /* finite-volume elements (fv.c); fv == NULL: all elements are DG */
@@ -71,7 +77,15 @@ typedef struct nmo_mesh {
   int fv_rec;               /* NMO_REC_* reconstruction (par fv_rec) */
   int fv_extrap;            /* 0: fv_divf_extrap = no, 1: dnfn_extrap1 */
   double fv_w3ratio;        /* par fv_WENOm3_opt_weightratio (default 2) */
+  const int32_t *mixface;   /* [e][6][3] (e', f', orientation) of the faces
+                               marked -2 in nbnode; NULL if none */
 } nmo_mesh;
+
+/* points of both point types: LGL (DG) with their Lagrange weights, and
+   equally spaced (finite volume) */
+typedef struct nmo_pts {
+  double xl[64], wl[64], xu[64];
+} nmo_pts;
 
 enum { NMO_REC_1 = 0, NMO_REC_WENOM3_2 = 1, NMO_REC_WENOM5_2 = 2 };
 
@@ -298,7 +312,67 @@ static int face_node(int n, int f, int a, int b)
    e: inner state from w, outer state from the coincident neighbour node or
    the boundary condition (scalarwave1_fluxes_pt + numflux1d_LLF).  Returns
    the inner flux fi and f*. */
-static void face_fnum(const nmo_mesh *m, int e, int f, int ijk, int JK,
+/* piecewise linear basis function k at x (basis_pw_linear) */
+static double pw_linear(int k, double x, int np, const double *xp)
+{
+  if (np <= 1) return 1.;
+  if (x < xp[1]) {
+    if (k == 0) return (x - xp[1]) / (xp[0] - xp[1]);
+    if (k == 1) return (x - xp[0]) / (xp[1] - xp[0]);
+    return 0.;
+  }
+  if (x >= xp[np - 2]) {
+    int n0 = np - 2, n1 = np - 1, l = k - n0;
+    if (l == 0) return (x - xp[n1]) / (xp[n0] - xp[n1]);
+    if (l == 1) return (x - xp[n0]) / (xp[n1] - xp[n0]);
+    return 0.;
+  }
+  if (k < np - 1 && x >= xp[k] && x < xp[k + 1]) return (x - xp[k + 1]) / (xp[k] - xp[k + 1]);
+  if (k > 0 && x >= xp[k - 1] && x < xp[k]) return (x - xp[k - 1]) / (xp[k] - xp[k - 1]);
+  return 0.;
+}
+
+/* Lagrange basis function k at x (Lagrange_of_x) */
+static double lagrange_of_x(int k, double x, int np, const double *xp, const double *wl)
+{
+  double prod = 1.;
+  int q;
+  for (q = 0; q < np; q++) if (q != k) prod *= (x - xp[q]);
+  return prod * wl[k];
+}
+
+/* Exterior state at face node (a, b) of face f of element e whose neighbour
+   (e2, f2, orientation o) has the other point type: the neighbour's face
+   plane interpolated to this node (basis_array_interp2d). */
+static void mixed_trace(const nmo_mesh *m, const nmo_pts *P, int e, int f, int a, int b,
+                        const double *w, double ua[5])
+{
+  int n = m->n, np = n * n * n, l, j, k;
+  const int32_t *mf = m->mixface + ((size_t)e * 6 + f) * 3;
+  int e2 = mf[0], f2 = mf[1], o = mf[2];
+  int sw = o & 1, fa = (o >> 1) & 1, fb = (o >> 2) & 1;
+  int aa = sw ? b : a, bb = sw ? a : b;
+  const double *xme = m->fv[e] ? P->xu : P->xl;
+  int nbfv = m->fv[e2] != 0;
+  double c1, c2, B1[64], B2[64];
+  aa = fa ? n - 1 - aa : aa;
+  bb = fb ? n - 1 - bb : bb;
+  c1 = xme[aa];
+  c2 = xme[bb];
+  for (k = 0; k < n; k++) {
+    B1[k] = nbfv ? pw_linear(k, c1, n, P->xu) : lagrange_of_x(k, c1, n, P->xl, P->wl);
+    B2[k] = nbfv ? pw_linear(k, c2, n, P->xu) : lagrange_of_x(k, c2, n, P->xl, P->wl);
+  }
+  for (l = 0; l < NF; l++) {
+    const double *v = w + ((size_t)e2 * NF + l) * np;
+    double sum = 0.;
+    for (k = 0; k < n; k++)
+      for (j = 0; j < n; j++) sum += v[face_node(n, f2, j, k)] * B1[j] * B2[k];
+    ua[l] = sum;
+  }
+}
+
+static void face_fnum(const nmo_mesh *m, const nmo_pts *P, int e, int f, int ijk, int JK,
                       double t, const double *w, double fi[5], double fnum[5])
 {
   int n = m->n, np = n * n * n, l;
@@ -310,6 +384,8 @@ static void face_fnum(const nmo_mesh *m, int e, int f, int ijk, int JK,
   if (nb >= 0) {
     int64_t en = nb / np, in = nb % np;
     for (l = 0; l < NF; l++) ua[l] = w[(size_t)en * NF * np + l * np + in];
+  } else if (nb == -2) {
+    mixed_trace(m, P, e, f, JK % n, JK / n, w, ua);
   } else if (m->bc == 0) {
     const double *X = m->xyz + (size_t)e * 3 * np;
     double xyz[3] = {X[ijk], X[np + ijk], X[2 * np + ijk]};
@@ -331,8 +407,9 @@ static void face_fnum(const nmo_mesh *m, int e, int f, int ijk, int JK,
 }
 
 /* RHS of one element: r[e] = RHS(w) at time t.  tmp holds 18*np doubles. */
-static void rhs_elem(const nmo_mesh *m, const double *D, const double *wq,
-                     double t, const double *w, double *r, int e, double *tmp)
+static void rhs_elem(const nmo_mesh *m, const nmo_pts *P, const double *D,
+                     const double *wq, double t, const double *w, double *r, int e,
+                     double *tmp)
 {
   int n = m->n, np = n * n * n, i, j, k, f, l;
   const double *we = w + (size_t)e * NF * np;
@@ -386,7 +463,7 @@ static void rhs_elem(const nmo_mesh *m, const double *D, const double *wq,
       for (a = 0; a < n; a++) {
         int ijk = face_node(n, f, a, b), JK = a + n * b;
         double fi[5], fnum[5], gd_ow;
-        face_fnum(m, e, f, ijk, JK, t, w, fi, fnum);
+        face_fnum(m, P, e, f, ijk, JK, t, w, fi, fnum);
         gd_ow = sqrtgdiag(m, e, dir, ijk) * oow;
         for (l = 0; l < 4; l++) {
           double F = (fnum[l] - fi[l] * 1.0) * 1.0;
@@ -538,8 +615,8 @@ static double det_dXbdx(const nmo_mesh *m, int e, int ijk)
 
 /* RHS of one fin.-vol. element (scalarwave1_vol_rhs_u / _surf_rhs_u with
    use_fv: fv_divf, then the surface terms).  tmp holds 8*np doubles. */
-static void rhs_elem_fv(const nmo_mesh *m, double t, const double *w,
-                        double *r, int e, double *tmp)
+static void rhs_elem_fv(const nmo_mesh *m, const nmo_pts *P, double t,
+                        const double *w, double *r, int e, double *tmp)
 {
   int n = m->n, np = n * n * n, i, j, k, f, l, dir, a, b, i0;
   const double *we = w + (size_t)e * NF * np;
@@ -601,7 +678,7 @@ static void rhs_elem_fv(const nmo_mesh *m, double t, const double *w,
             for (l = 0; l < 4; l++) fnumL[l] = -fnumR[l];
           } else if (addsurf) {
             double fi[5], fn[5];
-            face_fnum(m, e, 2 * dir, ccc, a + n * b, t, w, fi, fn);
+            face_fnum(m, P, e, 2 * dir, ccc, a + n * b, t, w, fi, fn);
             for (l = 0; l < 4; l++) fnumL[l] = fn[l];
           }
           if (lN) {
@@ -617,7 +694,7 @@ static void rhs_elem_fv(const nmo_mesh *m, double t, const double *w,
             for (l = 0; l < 4; l++) fnumR[l] = fn[l];
           } else if (addsurf) {
             double fi[5], fn[5];
-            face_fnum(m, e, 2 * dir + 1, ccc, a + n * b, t, w, fi, fn);
+            face_fnum(m, P, e, 2 * dir + 1, ccc, a + n * b, t, w, fi, fn);
             for (l = 0; l < 4; l++) fnumR[l] = fn[l];
           }
           for (l = 0; l < 4; l++) {
@@ -660,7 +737,7 @@ static void rhs_elem_fv(const nmo_mesh *m, double t, const double *w,
         for (a = 0; a < n; a++) {
           int ijk = face_node(n, f, a, b);
           double fi[5], fn[5], gd_ow;
-          face_fnum(m, e, f, ijk, a + n * b, t, w, fi, fn);
+          face_fnum(m, P, e, f, ijk, a + n * b, t, w, fi, fn);
           gd_ow = sg[d * np + ijk] * oow;
           for (l = 0; l < 4; l++) {
             double F = (fn[l] - fi[l] * 0.) * 1.0;
@@ -689,18 +766,26 @@ static void basis(int n, double *D, double *wq)
 /* r = RHS(w, t) on all elements */
 int nmo_rhs(const nmo_mesh *m, double t, const double *w, double *r)
 {
-  int n = m->n, np = n * n * n;
+  int n = m->n, np = n * n * n, i, j;
   double D[64 * 64], wq[64];
+  nmo_pts P;
   if (n < 2 || n > 64) return 1;
   basis(n, D, wq);
+  nmo_lgl(n, P.xl, wq);
+  nmo_uniform(n, P.xu);
+  for (i = 0; i < n; i++) {          /* Lagrange_winterp */
+    double denom = 1.;
+    for (j = 0; j < n; j++) if (j != i) denom *= (P.xl[i] - P.xl[j]);
+    P.wl[i] = 1. / denom;
+  }
 #pragma omp parallel
   {
     double *tmp = (double *)malloc(sizeof(double) * 18 * np);
     int e;
 #pragma omp for schedule(static)
     for (e = 0; e < m->nelem; e++) {
-      if (m->fv && m->fv[e]) rhs_elem_fv(m, t, w, r, e, tmp);
-      else rhs_elem(m, D, wq, t, w, r, e, tmp);
+      if (m->fv && m->fv[e]) rhs_elem_fv(m, &P, t, w, r, e, tmp);
+      else rhs_elem(m, &P, D, wq, t, w, r, e, tmp);
     }
     free(tmp);
   }

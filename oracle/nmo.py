@@ -39,7 +39,7 @@ class _Mesh(ctypes.Structure):
                 ("nbnode", ctypes.c_void_p), ("bc", ctypes.c_int),
                 ("k", ctypes.c_double * 3), ("fv", ctypes.c_void_p),
                 ("fv_rec", ctypes.c_int), ("fv_extrap", ctypes.c_int),
-                ("fv_w3ratio", ctypes.c_double)]
+                ("fv_w3ratio", ctypes.c_double), ("mixface", ctypes.c_void_p)]
 
 # reconstruction modes (reference par fv_rec) and div(f) extrapolation
 # modes (par fv_divf_extrap) understood by the oracle
@@ -100,18 +100,24 @@ def face_plane_index(n, f):
     return i + n * (j + n * k)
 
 
-def match_faces(xyz, n, period=None, tol=1e-9):
+def match_faces(xyz, n, period=None, tol=1e-9, fv=None):
     """Neighbour table for the oracle by matching face-node coordinates.
 
-    xyz: [E, 3, np].  Two element faces are neighbours when they hold the
-    same set of node positions (compared modulo `period` on every axis when
-    given, which makes a box periodic).  Returns nbnode[E, 6, n*n] with
+    xyz: [E, 3, np].  Two element faces are neighbours when their four
+    corners coincide (compared modulo `period` on every axis when given,
+    which makes a box periodic).  Returns nbnode[E, 6, n*n] with
     e'*np + ijk' of the coincident node of the neighbour, or -1 on outer
     faces (the reference copies coincident neighbour points,
-    src/main/amr/surface.c:799-900)."""
+    src/main/amr/surface.c:799-900).  With per-element point types `fv`
+    (1: equally spaced points), a face whose neighbour has the other point
+    type is marked -2 and (nbnode, mixface) is returned, mixface[E, 6, 3] =
+    (neighbour element, neighbour face, orientation o) where in-plane node
+    (a, b) lies at the neighbour's in-plane position (a', b') = (s ? b : a,
+    s ? a : b), reversed per axis by bits 1 and 2 of o (s = bit 0)."""
     E = xyz.shape[0]
     npt = n ** 3
     planes = [face_plane_index(n, f) for f in range(6)]
+    corners = [0, n - 1, n * (n - 1), n * n - 1]   # (a, b) = (0,0),(n-1,0),(0,n-1),(n-1,n-1)
 
     def wrap(p):
         q = np.array(p, dtype=float)
@@ -123,15 +129,20 @@ def match_faces(xyz, n, period=None, tol=1e-9):
     def pkey(q):
         return tuple(np.round(q / tol).astype(np.int64))
 
+    def orient(o, a, b):
+        aa, bb = (b, a) if o & 1 else (a, b)
+        return (n - 1 - aa if o & 2 else aa), (n - 1 - bb if o & 4 else bb)
+
     faces = {}
     for e in range(E):
         for f in range(6):
             raw = xyz[e][:, planes[f]].T              # [n*n, 3]
-            # a face never straddles a period: average, then wrap
-            order = np.lexsort(raw.T[::-1])
-            cen = raw[order].mean(axis=0)
+            # a face never straddles a period: average the corners, then wrap
+            cen = raw[corners].mean(axis=0)
             faces.setdefault(pkey(wrap(cen)), []).append((e, f, raw, cen))
     nb = np.full((E, 6, n * n), -1, np.int64)
+    mixface = np.zeros((E, 6, 3), np.int32)
+    mixed = False
     for fkey, lst in faces.items():
         if len(lst) == 1:
             continue
@@ -142,9 +153,28 @@ def match_faces(xyz, n, period=None, tol=1e-9):
             shift = np.zeros(3)
             if period is not None:
                 shift = np.round((c2 - c1) / period) * period
+            if fv is not None and bool(fv[e]) != bool(fv[e2]):
+                found = None
+                for o in range(8):
+                    ok = True
+                    for a, b in ((0, 0), (n - 1, 0), (0, n - 1), (n - 1, n - 1)):
+                        aa, bb = orient(o, a, b)
+                        if pkey(P[a + n * b]) != pkey(P2[aa + n * bb] - shift):
+                            ok = False
+                    if ok:
+                        found = o
+                        break
+                if found is None:
+                    raise ValueError("mixed face: corners do not match")
+                nb[e, f, :] = -2
+                mixface[e, f] = (e2, f2, found)
+                mixed = True
+                continue
             where = {pkey(q - shift): planes[f2][i] for i, q in enumerate(P2)}
             for jk in range(n * n):
                 nb[e, f, jk] = e2 * npt + where[pkey(P[jk])]
+    if fv is not None:
+        return nb, (mixface if mixed else None)
     return nb
 
 
@@ -153,9 +183,10 @@ class OracleMesh:
 
     def __init__(self, bbox, curvi, dXdx, xyz, nbnode, n, bc=0,
                  k=(1.0, 1.0, 1.0), fv=None, fv_rec="WENOm5_2",
-                 fv_extrap="dnfn_extrap1", fv_w3ratio=2.0):
+                 fv_extrap="dnfn_extrap1", fv_w3ratio=2.0, mixface=None):
         """fv: per-element finite-volume flags (None: all DG); fv_rec and
-        fv_extrap name the reference's fv_rec / fv_divf_extrap modes."""
+        fv_extrap name the reference's fv_rec / fv_divf_extrap modes;
+        mixface: faces between the two point types (see match_faces)."""
         self.n = int(n)
         self.bbox = np.ascontiguousarray(bbox, np.float64)
         self.curvi = np.ascontiguousarray(curvi, np.int32)
@@ -164,12 +195,14 @@ class OracleMesh:
         self.nbnode = np.ascontiguousarray(nbnode, np.int64)
         self.nelem = self.bbox.shape[0]
         self.fv = None if fv is None else np.ascontiguousarray(fv, np.int32)
+        self.mixface = None if mixface is None else np.ascontiguousarray(mixface, np.int32)
         self.s = _Mesh(self.nelem, self.n, self.bbox.ctypes.data,
                        self.curvi.ctypes.data, self.dXdx.ctypes.data,
                        self.xyz.ctypes.data, self.nbnode.ctypes.data, int(bc),
                        (ctypes.c_double * 3)(*k),
                        None if self.fv is None else self.fv.ctypes.data,
-                       FV_REC[fv_rec], FV_EXTRAP[fv_extrap], float(fv_w3ratio))
+                       FV_REC[fv_rec], FV_EXTRAP[fv_extrap], float(fv_w3ratio),
+                       None if self.mixface is None else self.mixface.ctypes.data)
 
     def rhs(self, w, t=0.0):
         w = np.ascontiguousarray(w, np.float64)

@@ -62,6 +62,16 @@ CASES = {
     "fvcs7_l0_n6_w5no": dict(mesh="cs7", n=6, luni=0, k=(0.25, 0.15, -0.3),
                              dt=0.002, steps=2, eps=0.02, seed=26,
                              fv=dict(rec="WENOm5_2", extrap="no")),
+    # mixed meshes: the inner cube (patch 0) finite-volume, the six
+    # cubed-sphere patches DG; face traces across the DG / FV interface are
+    # interpolated (Lagrange from DG, piecewise linear from FV)
+    "mixcs7_l0_n7_w5dnfn": dict(mesh="cs7", n=7, luni=0, k=(0.3, -0.2, 0.1),
+                                dt=0.002, steps=2, eps=0.02, seed=27,
+                                fv=dict(rec="WENOm5_2", extrap="dnfn_extrap1",
+                                        patches="0")),
+    "mixcs7_l1_n5_w3no": dict(mesh="cs7", n=5, luni=1, k=(0.25, 0.15, -0.3),
+                              dt=0.002, steps=2, eps=0.02, seed=28,
+                              fv=dict(rec="WENOm3_2", extrap="no", patches="0")),
 }
 
 
@@ -93,6 +103,7 @@ def parfile(case, prefix):
                   "amr_CubedSphere_dc = 1", "amr_CubedSphere_r0fac = 20"]
         pats = "0 1 2 3 4 5 6"
     if "fv" in c:
+        pats = c["fv"].get("patches", pats)
         lines += [f"amr_uniform_p = {pats}", f"amr_fv_p = {pats}",
                   f"fv_rec = {c['fv']['rec']}",
                   f"fv_divf_extrap = {c['fv']['extrap']}"]

@@ -12,6 +12,8 @@ CASES = ["box_l1_n5", "box_l2_n4", "cs7_l0_n9", "cs7_l1_n5", "cs7_l1_n4"]
 # all-finite-volume fixtures (uniform points, WENO at the midpoints)
 FV_CASES = ["fvbox_l1_n7_w5no", "fvbox_l1_n7_w5dnfn", "fvbox_l2_n5_w3dnfn",
             "fvbox_l0_n13_w5dnfn", "fvcs7_l0_n7_w5dnfn", "fvcs7_l0_n6_w5no"]
+# mixed fixtures: inner cube finite-volume, cubed-sphere shells DG
+MIX_CASES = ["mixcs7_l0_n7_w5dnfn", "mixcs7_l1_n5_w3no"]
 
 # relative L2 tolerance of the CUDA path against the reference / oracle for
 # one RHS evaluation and for a few RK4 steps (FP64; FMA contraction and a

@@ -5,7 +5,7 @@ operation order and must match it bit for bit."""
 import numpy as np
 import pytest
 
-from helpers import CASES, FV_CASES, load
+from helpers import CASES, FV_CASES, MIX_CASES, load
 from oracle import nmo
 
 
@@ -13,11 +13,13 @@ def _oracle_mesh(d, meta):
     n = int(d["n"][0, 0])
     curvi = (d["pat"] > 0).astype(np.int32) if meta["mesh"] == "cs7" else \
         np.zeros(len(d["pat"]), np.int32)
-    nb = nmo.match_faces(d["x"], n)
     fv = {}
     if "fv" in meta:
+        nb, mix = nmo.match_faces(d["x"], n, fv=d["use_fv"])
         fv = dict(fv=d["use_fv"], fv_rec=meta["fv"]["rec"],
-                  fv_extrap=meta["fv"]["extrap"])
+                  fv_extrap=meta["fv"]["extrap"], mixface=mix)
+    else:
+        nb = nmo.match_faces(d["x"], n)
     return nmo.OracleMesh(d["bbox"], curvi, d["dXdx"], d["x"], nb, n, bc=0,
                           k=meta["k"], **fv)
 
@@ -36,6 +38,17 @@ def test_oracle_rk4_bitexact(case):
     m = _oracle_mesh(d, meta)
     u = m.rk4(d["u0"], meta["dt"], meta["steps"])
     assert np.array_equal(u, d["u_final"])
+
+
+@pytest.mark.parametrize("case", MIX_CASES)
+def test_oracle_mixed_dg_fv_bitexact(case):
+    """Mixed DG / finite-volume meshes (inner cube FV, shells DG): the
+    interface traces are interpolated at the face points (Lagrange from the
+    DG side, piecewise linear from the FV side) as the reference does."""
+    d, meta = load(case)
+    m = _oracle_mesh(d, meta)
+    assert np.array_equal(m.rhs(d["u0"], 0.0), d["r0"])
+    assert np.array_equal(m.rk4(d["u0"], meta["dt"], meta["steps"]), d["u_final"])
 
 
 def test_lgl_basis_properties():
