@@ -71,9 +71,10 @@ typedef struct nmg_mesh_params {
   double box_dout;    /* amr_BoxMesh_dout: half edge of the box */
   double cs_dc;       /* amr_CubedSphere_dc: half edge of the inner cube */
   double cs_r0fac;    /* amr_CubedSphere_r0fac: outer radius / dc */
-  int32_t fv;         /* 1: every element is a finite-volume element on
-                         equally spaced points (amr_uniform_p and amr_fv_p
-                         list every patch, src/main/amr/mesh.c:35-83) */
+  int32_t fv;         /* bit p set: the elements of patch p are
+                         finite-volume elements on equally spaced points
+                         (amr_uniform_p and amr_fv_p list patch p,
+                         src/main/amr/mesh.c:35-83); -1: every patch; 0: DG */
 } nmg_mesh_params;
 
 /* A mesh given element by element, e.g. packed from the reference's tMesh
@@ -95,8 +96,10 @@ typedef struct nmg_mesh_desc {
   double period[3];       /* >0: coordinates compared modulo period when
                              matching (periodic box); 0 otherwise */
   const int32_t *fv;      /* [nelem] node->dat->info->use_fv (elements on
-                             equally spaced points), or NULL: all DG.  Mixed
-                             meshes are rejected with NMG_EUNSUP. */
+                             equally spaced points), or NULL: all DG.  Faces
+                             between a DG and a finite-volume element are
+                             found from coordinates (nbnode must be NULL
+                             then) and get interpolated traces. */
 } nmg_mesh_desc;
 
 /* ---- host mesh ---------------------------------------------------------- */

@@ -156,10 +156,19 @@ class Mesh:
         """Mesh from the reference's parameters: amr_mesh_type (1 BoxMesh /
         7 CubedSpheres), amr_n0..2 = n, amr_luni, amr_mesh_xc,
         amr_BoxMesh_dout, amr_CubedSphere_dc, amr_CubedSphere_r0fac;
-        fv=True puts every patch in amr_uniform_p and amr_fv_p."""
+        fv=True puts every patch in amr_uniform_p and amr_fv_p, a list of
+        patch indices puts those patches there."""
+        if fv is True:
+            mask = -1
+        elif not fv:
+            mask = 0
+        else:
+            mask = 0
+            for p_ in fv:
+                mask |= 1 << int(p_)
         p = _MeshParams(int(mesh_type), int(n), int(luni), int(bool(periodic)),
                         (ctypes.c_double * 3)(*xc), float(box_dout),
-                        float(cs_dc), float(cs_r0fac), int(bool(fv)))
+                        float(cs_dc), float(cs_r0fac), int(mask))
         h = ctypes.c_void_p()
         rc = lib().nmg_mesh_build(ctypes.byref(p), ctypes.byref(h))
         if rc:

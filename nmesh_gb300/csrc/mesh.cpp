@@ -175,7 +175,7 @@ void elem_bbox(const double pb[6], int L, const int ixyz[3], double bb[6]) {
 
 // fill geometry for all elements of the given patches, uniform level L,
 // elements of a patch in Morton (Z) order
-void fill_geometry(nmg_mesh &m, const std::vector<Patch> &pats, int L) {
+void fill_geometry(nmg_mesh &m, const std::vector<Patch> &pats, int L, int32_t fvmask) {
   const int n = m.n, np = n * n * n;
   const int ne1 = 1 << L;
   const int64_t per = (int64_t)ne1 * ne1 * ne1;
@@ -185,6 +185,7 @@ void fill_geometry(nmg_mesh &m, const std::vector<Patch> &pats, int L) {
   m.curvi.resize(m.nelem);
   m.xyz.resize(m.nelem * 3 * np);
   m.dXdx.resize(m.nelem * 9 * np);
+  m.fv.assign(m.nelem, 0);
   int64_t e = 0;
   for (size_t p = 0; p < pats.size(); p++) {
     for (int64_t mc = 0; mc < per; mc++, e++) {
@@ -195,13 +196,16 @@ void fill_geometry(nmg_mesh &m, const std::vector<Patch> &pats, int L) {
       elem_bbox(pats[p].bbox, L, ixyz, bb);
       m.pat[e] = (int32_t)p;
       m.curvi[e] = pats[p].cubed ? 1 : 0;
+      const bool isfv = (fvmask >> p) & 1;
+      if (isfv) m.fv[e] = 1;
+      const double *px = isfv ? m.xu.data() : m.x.data();
       double *X3 = &m.xyz[e * 3 * np];
       double *M9 = &m.dXdx[e * 9 * np];
       for (int k = 0; k < n; k++)
         for (int j = 0; j < n; j++)
           for (int i = 0; i < n; i++) {
             int ijk = i + n * (j + n * k);
-            double Xb[3] = {m.x[i], m.x[j], m.x[k]}, X[3], x[3], J[3][3];
+            double Xb[3] = {px[i], px[j], px[k]}, X[3], x[3], J[3][3];
             for (int d = 0; d < 3; d++)
               X[d] = 0.5 * ((bb[2 * d + 1] - bb[2 * d]) * Xb[d] + (bb[2 * d + 1] + bb[2 * d]));
             if (pats[p].cubed) {
@@ -453,12 +457,16 @@ std::string pack_faces(nmg_mesh &m, const int64_t *nbnode, const double period[3
                std::to_string(e) + " (non-conforming mesh)";
       int64_t e2 = match / 6;
       int f2 = (int)(match % 6);
-      // orientation: match the in-plane node (a,b)=(1,0) and (0,1) images
+      // orientation: every face node must coincide with the oriented image;
+      // between a DG and a finite-volume element (different points) only
+      // the corners do
+      const bool mixed = !m.fv.empty() && (m.fv[e] != 0) != (m.fv[e2] != 0);
       int found = -1;
       for (int o = 0; o < 8 && found < 0; o++) {
         int ok = 1;
         for (int b = 0; b < n && ok; b++)
           for (int a = 0; a < n && ok; a++) {
+            if (mixed && !((a == 0 || a == n - 1) && (b == 0 || b == n - 1))) continue;
             int a2, b2;
             orient_map(n, o, a, b, &a2, &b2);
             double p1[3], p2[3];
@@ -470,7 +478,7 @@ std::string pack_faces(nmg_mesh &m, const int64_t *nbnode, const double period[3
       }
       if (found < 0) return "face nodes of neighbours do not coincide (non-conforming)";
       m.nb[e * 6 + f] = (int32_t)e2;
-      m.code[e * 6 + f] = f2 | (found << 3);
+      m.code[e * 6 + f] = f2 | (found << 3) | (mixed ? NMG_CODE_MIXED : 0);
     }
   return "";
 }
@@ -500,11 +508,11 @@ int nmg_mesh_build(const nmg_mesh_params *p, nmg_mesh **out) {
   try {
     m->n = p->n;
     m->x.resize(p->n); m->w.resize(p->n); m->D.resize(p->n * p->n);
-    if (p->fv) {
-      m->uniform = true;
-      nmg::uniform_basis(p->n, m->x.data(), m->w.data(), m->D.data());
-    } else {
-      nmg::lgl_basis(p->n, m->x.data(), m->w.data(), m->D.data());
+    nmg::lgl_basis(p->n, m->x.data(), m->w.data(), m->D.data());
+    {
+      std::vector<double> wu(p->n), Du((size_t)p->n * p->n);
+      m->xu.resize(p->n);
+      nmg::uniform_basis(p->n, m->xu.data(), wu.data(), Du.data());
     }
     std::vector<Patch> pats;
     double period[3] = {0, 0, 0};
@@ -548,8 +556,10 @@ int nmg_mesh_build(const nmg_mesh_params *p, nmg_mesh **out) {
       delete m;
       return fail(NMG_EUNSUP, "nmg_mesh_build: unknown mesh_type");
     }
-    fill_geometry(*m, pats, p->luni);
-    if (p->fv) m->fv.assign(m->nelem, 1);
+    fill_geometry(*m, pats, p->luni, p->fv);
+    bool anyfv = false;
+    for (int64_t e = 0; e < m->nelem; e++) anyfv = anyfv || m->fv[e];
+    if (!anyfv) m->fv.clear();
     std::string err = nmg::pack_faces(*m, nullptr, period);
     if (!err.empty()) { delete m; return fail(NMG_EMESH, err); }
   } catch (const std::bad_alloc &) {
@@ -574,19 +584,18 @@ int nmg_mesh_from_desc(const nmg_mesh_desc *d, nmg_mesh **out) {
     m->n = n;
     m->nelem = E;
     m->x.resize(n); m->w.resize(n); m->D.resize(n * n);
+    nmg::lgl_basis(n, m->x.data(), m->w.data(), m->D.data());
+    {
+      std::vector<double> wu(n), Du((size_t)n * n);
+      m->xu.resize(n);
+      nmg::uniform_basis(n, m->xu.data(), wu.data(), Du.data());
+    }
     int64_t nfv = 0;
     if (d->fv)
       for (int64_t e = 0; e < E; e++) nfv += d->fv[e] ? 1 : 0;
-    if (nfv > 0 && nfv < E) {
-      delete m;
-      return fail(NMG_EUNSUP, "nmg_mesh_from_desc: mixed DG / finite-volume meshes are not supported");
-    }
     if (nfv > 0) {
-      m->uniform = true;
-      m->fv.assign(E, 1);
-      nmg::uniform_basis(n, m->x.data(), m->w.data(), m->D.data());
-    } else {
-      nmg::lgl_basis(n, m->x.data(), m->w.data(), m->D.data());
+      m->fv.assign(E, 0);
+      for (int64_t e = 0; e < E; e++) m->fv[e] = d->fv[e] ? 1 : 0;
     }
     m->pat.assign(E, 0);
     if (d->pat) std::memcpy(m->pat.data(), d->pat, E * sizeof(int32_t));
@@ -670,8 +679,8 @@ int nmg_mesh_concat(const nmg_mesh *const *ms, int32_t count, nmg_mesh **out) {
     if (!ms[i] || ms[i]->n != n)
       return fail(NMG_EINVAL, "nmg_mesh_concat: meshes must exist and share n");
   for (int i = 0; i < count; i++)
-    if (ms[i]->uniform != ms[0]->uniform || ms[i]->fv.empty() != ms[0]->fv.empty())
-      return fail(NMG_EUNSUP, "nmg_mesh_concat: meshes must share the point type");
+    if (!ms[i]->fv.empty())
+      return fail(NMG_EUNSUP, "nmg_mesh_concat: finite-volume meshes are not concatenated");
   nmg_mesh *m = new (std::nothrow) nmg_mesh;
   if (!m) return fail(NMG_ENOMEM, "nmg_mesh_concat: out of memory");
   try {
@@ -679,7 +688,7 @@ int nmg_mesh_concat(const nmg_mesh *const *ms, int32_t count, nmg_mesh **out) {
     m->x = ms[0]->x;
     m->w = ms[0]->w;
     m->D = ms[0]->D;
-    m->uniform = ms[0]->uniform;
+    m->xu = ms[0]->xu;
     int64_t off = 0;
     for (int i = 0; i < count; i++) {
       const nmg_mesh &a = *ms[i];
@@ -691,7 +700,6 @@ int nmg_mesh_concat(const nmg_mesh *const *ms, int32_t count, nmg_mesh **out) {
       for (size_t q = 0; q < a.nb.size(); q++)
         m->nb.push_back(a.nb[q] < 0 ? -1 : (int32_t)(a.nb[q] + off));
       m->code.insert(m->code.end(), a.code.begin(), a.code.end());
-      m->fv.insert(m->fv.end(), a.fv.begin(), a.fv.end());
       off += a.nelem;
     }
     m->nelem = off;

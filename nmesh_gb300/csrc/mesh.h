@@ -15,11 +15,15 @@ struct nmg_mesh {
   std::vector<double> dXdx;    // [E][9][np] dX^a/dx^i (identity if Cartesian)
   std::vector<int32_t> nb;     // [E][6] neighbour element, -1 on outer faces
   std::vector<int32_t> code;   // [E][6] neighbour face | orientation << 3
-  std::vector<double> x, w, D; // points, quadrature weights, D[i*n+j]
-  std::vector<int32_t> fv;     // [E] 1: finite-volume element on uniform
-                               // points; empty: all elements DG on LGL points
-  bool uniform = false;        // x are equally spaced (finite-volume mesh)
+  std::vector<double> x, w, D; // LGL points, quadrature weights, D[i*n+j]
+  std::vector<double> xu;      // equally spaced points (finite-volume elements)
+  std::vector<int32_t> fv;     // [E] 1: finite-volume element on equally
+                               // spaced points; empty: all DG on LGL points
 };
+
+// face-table code bit: the neighbour has the other point type (DG / FV), its
+// trace is interpolated onto this face's points
+constexpr int NMG_CODE_MIXED = 64;
 
 namespace nmg {
 // LGL nodes/weights and differentiation matrix (Legendre.c / Lagrange.c)

@@ -128,13 +128,21 @@ struct nmg_ctx {
   int *d_step = nullptr;
   int times_cap = 0;
   // finite-volume mesh: options and geometry (stage_fv.cu)
-  bool fv = false;
+  bool fv = false;     // some elements are finite-volume
+  bool mixed = false;  // ... and some DG: variants[0, ndg) DG, [ndg, n) FV
+  int ndg = 0, fsel = -1;
+  bool ftuned = false;
+  int nfvel = 0, nghost = 0;
+  int *d_fvlist = nullptr, *d_gtab = nullptr;
+  unsigned char *d_isfv = nullptr;
+  double *d_ghost = nullptr, *d_gM = nullptr;
   int fv_rec = NMG_FV_REC_WENOM3_2, fv_extrap = NMG_FV_EXTRAP_DNFN1;
   double fv_w3ratio = 2.;
   double *d_fvgeo = nullptr, *d_fvdist = nullptr, *d_fvdxb = nullptr;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // one RK4 step, u in d_buf[0] / d_buf[1]
   double graph_dt = 0;
   int graph_sel = -1;
+  int64_t graph_launches = 5;
   int64_t launches = 0;
 };
 
@@ -155,9 +163,35 @@ int nmg_ctx_fail_static(nmg_ctx *c, int code, const char *msg) {
   return code;
 }
 
-// one RK4 step u_in -> u_out with explicit stage buffers s1, s2 and kernel
-// variant V (forward or transposed), enqueued on the context stream
-static int step_buffers(nmg_ctx *c, const Variant &V, double t, double dt, const double *u_in,
+// One stage with variant v.  On a mixed DG / finite-volume mesh a stage is
+// three launches: the interpolated interface traces of the stage input, the
+// DG kernel over all elements (writing only the DG ones) and the
+// finite-volume kernel over the finite-volume elements.
+static cudaError_t run_stage(nmg_ctx *c, int v, StageParams P) {
+  cudaError_t e;
+  if (c->mixed) {
+    e = nmgk::ghost_launch(c->nghost, c->n, c->d_gtab, c->d_isfv, c->d_gM, P.win, c->d_ghost,
+                           c->stream);
+    if (e != cudaSuccess) return e;
+    c->launches++;
+    P.skip = c->d_isfv;
+    if ((e = c->variants[v].launch(P, c->stream)) != cudaSuccess) return e;
+    c->launches++;
+    P.skip = nullptr;
+    P.fvlist = c->d_fvlist;
+    P.nfvel = c->nfvel;
+    if ((e = c->variants[c->fsel].launch(P, c->stream)) != cudaSuccess) return e;
+    c->launches++;
+    return cudaSuccess;
+  }
+  e = c->variants[v].launch(P, c->stream);
+  if (e == cudaSuccess) c->launches++;
+  return e;
+}
+
+// one RK4 step u_in -> u_out with explicit stage buffers s1, s2, forward
+// (the selected variants) or transposed (vjp), enqueued on the context stream
+static int step_buffers(nmg_ctx *c, bool vjp, double t, double dt, const double *u_in,
                         double *u_out, double *s1, double *s2) {
   const double cacc[4] = {dt / 6., dt / 3., dt / 3., dt / 6.};
   const double cw[4] = {dt / 2., dt / 2., dt, 0.};
@@ -174,16 +208,22 @@ static int step_buffers(nmg_ctx *c, const Variant &V, double t, double dt, const
     P.cacc = cacc[s];
     P.cw = cw[s];
     P.t = ts[s];
-    cudaError_t e = V.launch(P, c->stream);
+    cudaError_t e;
+    if (vjp) {
+      e = c->vjp.launch(P, c->stream);
+      if (e == cudaSuccess) c->launches++;
+    } else {
+      e = run_stage(c, c->sel >= 0 ? c->sel : 0, P);
+    }
     if (e != cudaSuccess) return nmg_ctx_fail_static(c, NMG_ECUDA, cudaGetErrorString(e));
-    c->launches++;
   }
   return NMG_OK;
 }
 
 int nmg_ctx_rk4_step_buffers(nmg_ctx *c, double t, double dt, const double *u_in,
                              double *u_out, double *s1, double *s2) {
-  int rc = step_buffers(c, c->variants[c->sel >= 0 ? c->sel : 0], t, dt, u_in, u_out, s1, s2);
+  if (c->mixed && c->fsel < 0) c->fsel = c->ndg;
+  int rc = step_buffers(c, false, t, dt, u_in, u_out, s1, s2);
   if (rc) return rc;
   cudaError_t e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return nmg_ctx_fail_static(c, NMG_ECUDA, cudaGetErrorString(e));
@@ -221,6 +261,7 @@ static StageParams base_params(nmg_ctx *c) {
   P.fvgeo = c->d_fvgeo;
   P.fvdist = c->d_fvdist;
   P.fvdxb = c->d_fvdxb;
+  P.ghost = c->d_ghost;
   P.bc = c->bc;
   P.k0 = c->k[0];
   P.k1 = c->k[1];
@@ -229,34 +270,28 @@ static StageParams base_params(nmg_ctx *c) {
   return P;
 }
 
-// Autotuner: time every compiled variant on an RHS of the current state and
-// keep the fastest.  Runs once per context, before any graph capture.
-static int autotune(nmg_ctx *c) {
-  if (c->tuned) return NMG_OK;
-  const char *force = getenv("NMG_KERNEL");  // e.g. "eo", "gather", "eo:1:128"
-  c->tune_log.clear();
-  if (c->sel < 0 && force && *force) {
-    for (int v = 0; v < c->nvariants; v++) {
-      char buf[64];
-      snprintf(buf, sizeof buf, "%s:%d:%d", c->variants[v].name, c->variants[v].epb,
-               c->variants[v].nt);
-      if (!strcmp(force, c->variants[v].name) || !strcmp(force, buf)) { c->sel = v; break; }
-    }
-  }
-  if (c->sel >= 0) {
-    c->tuned = true;
-    return NMG_OK;
-  }
+// Autotuner: time the compiled variants on an RHS of the current state and
+// keep the fastest (on a mixed mesh the DG and the finite-volume variants
+// separately).  Runs once per context, before any graph capture.
+static int tune_range(nmg_ctx *c, int v0, int v1, bool fvpart, int *best_out) {
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
   float best = 1e30f;
-  int bestv = 0;
-  for (int v = 0; v < c->nvariants; v++) {
+  int bestv = v0;
+  for (int v = v0; v < v1; v++) {
     StageParams P = base_params(c);
     P.win = c->d_buf[c->cur];
     P.rout = c->d_buf[3];
     P.mode = 0;
+    if (c->mixed) {
+      if (fvpart) {
+        P.fvlist = c->d_fvlist;
+        P.nfvel = c->nfvel;
+      } else {
+        P.skip = c->d_isfv;
+      }
+    }
     CK(c->variants[v].launch(P, c->stream));  // warm-up
     float tot = 0;
     const int reps = 3;
@@ -274,16 +309,46 @@ static int autotune(nmg_ctx *c) {
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  c->sel = bestv;
-  c->tuned = true;
+  *best_out = bestv;
+  return NMG_OK;
+}
+
+static int autotune(nmg_ctx *c) {
+  if (c->tuned && (!c->mixed || c->ftuned)) return NMG_OK;
+  const char *force = getenv("NMG_KERNEL");  // e.g. "eo", "gather", "eo:1:128"
+  const int ndg = c->mixed ? c->ndg : c->nvariants;
+  if (force && *force) {
+    for (int v = 0; v < c->nvariants; v++) {
+      char buf[64];
+      snprintf(buf, sizeof buf, "%s:%d:%d", c->variants[v].name, c->variants[v].epb,
+               c->variants[v].nt);
+      if (!strcmp(force, c->variants[v].name) || !strcmp(force, buf)) {
+        if (v < ndg && c->sel < 0) c->sel = v;
+        if (v >= ndg && c->mixed && c->fsel < 0) c->fsel = v;
+        break;
+      }
+    }
+  }
+  if (c->sel >= 0) c->tuned = true;
+  if (c->fsel >= 0) c->ftuned = true;
+  if (!c->tuned || (c->mixed && !c->ftuned)) c->tune_log.clear();
+  if (!c->tuned) {
+    int rc = tune_range(c, 0, ndg, false, &c->sel);
+    if (rc) return rc;
+    c->tuned = true;
+  }
+  if (c->mixed && !c->ftuned) {
+    int rc = tune_range(c, c->ndg, c->nvariants, true, &c->fsel);
+    if (rc) return rc;
+    c->ftuned = true;
+  }
   return NMG_OK;
 }
 
 static int launch_stage(nmg_ctx *c, const StageParams &P) {
   int rc = autotune(c);
   if (rc) return rc;
-  CK(c->variants[c->sel].launch(P, c->stream));
-  c->launches++;
+  CK(run_stage(c, c->sel, P));
   return NMG_OK;
 }
 
@@ -331,7 +396,7 @@ static void fv_pack_element(const nmg_mesh &m, int64_t e, int cs, std::vector<do
   const double *bb = &m.bbox[e * 6];
   for (int f = 0; f < 6; f++) {
     const int d = f / 2, right = f % 2, id = (n - 2) * right;
-    const double Xbm = 0.5 * (m.x[id] + m.x[id + 1]);
+    const double Xbm = 0.5 * (m.xu[id] + m.xu[id + 1]);
     const double Xbf = (2. * bb[f] - (bb[2 * d + 1] + bb[2 * d])) / (bb[2 * d + 1] - bb[2 * d]);
     (*dist)[e * 6 + f] = std::fabs(Xbm - Xbf);
   }
@@ -380,10 +445,16 @@ int nmg_create(const nmg_mesh *m, int32_t bc_kind, const double k[3], nmg_ctx **
     return set_err(c, NMG_EINVAL, "nmg_create: unknown bc kind");
   int64_t nfv = 0;
   for (size_t e = 0; e < m->fv.size(); e++) nfv += m->fv[e] ? 1 : 0;
-  if (nfv > 0 && nfv < m->nelem)
-    return set_err(c, NMG_EUNSUP, "nmg_create: mixed DG / finite-volume meshes are not supported");
   c->fv = nfv > 0;
-  if (c->fv) {
+  c->mixed = nfv > 0 && nfv < m->nelem;
+  if (c->mixed) {
+    c->ndg = nmgk::eo_variants(m->n, c->variants, kMaxVariants);
+    c->ndg += nmgk::gather_variants(m->n, c->variants + c->ndg, kMaxVariants - c->ndg);
+    const int nf = nmgk::fv_variants(m->n, c->variants + c->ndg, kMaxVariants - c->ndg);
+    if (c->ndg == 0 || nf == 0)
+      return set_err(c, NMG_EUNSUP, "nmg_create: mixed DG / finite-volume n must be in [2,12]");
+    c->nvariants = c->ndg + nf;
+  } else if (c->fv) {
     c->nvariants = nmgk::fv_variants(m->n, c->variants, kMaxVariants);
     if (c->nvariants == 0) return set_err(c, NMG_EUNSUP, "nmg_create: finite-volume n must be in [2,13]");
   } else {
@@ -408,10 +479,22 @@ int nmg_create(const nmg_mesh *m, int32_t bc_kind, const double k[3], nmg_ctx **
   std::vector<int> cslot(E, -1), bslot(E * 6, -1);
   std::vector<double> scale(E * 3, 0.), gcart(E * 3, 0.);
   int64_t C = 0, B = 0;
+  std::vector<int> gtab, fvlist;
+  std::vector<unsigned char> isfv(E, 0);
   for (int64_t e = 0; e < E; e++) {
     if (m->curvi[e]) cslot[e] = (int)C++;
     for (int f = 0; f < 6; f++)
       if (m->nb[e * 6 + f] < 0) bslot[e * 6 + f] = (int)B++;
+    if (c->fv && m->fv[e]) {
+      isfv[e] = 1;
+      fvlist.push_back((int)e);
+    }
+    // faces to a neighbour of the other point type: slots of interpolated traces
+    for (int f = 0; f < 6; f++)
+      if (m->nb[e * 6 + f] >= 0 && (m->code[e * 6 + f] & NMG_CODE_MIXED)) {
+        bslot[e * 6 + f] = (int)(gtab.size() / 4);
+        gtab.insert(gtab.end(), {(int)e, f, m->nb[e * 6 + f], m->code[e * 6 + f]});
+      }
     for (int d = 0; d < 3; d++)
       scale[e * 3 + d] = 2. / (m->bbox[e * 6 + 2 * d + 1] - m->bbox[e * 6 + 2 * d]);
     for (int d = 0; d < 3; d++) gcart[e * 3 + d] = 0.5 * scale[e * 3 + d] / m->w[0];
@@ -420,7 +503,7 @@ int nmg_create(const nmg_mesh *m, int32_t bc_kind, const double k[3], nmg_ctx **
   c->nbface = B;
   std::vector<double> metric, metricp, fac, bxyz, bnrm, fvgeo, fvdist, fvdxb;
   std::vector<int> cmask((size_t)std::max<int64_t>(C, 1), 0);
-  const int64_t Cdg = c->fv ? 0 : C;  // DG metric arrays, FV geometry
+  const int64_t Cdg = (c->fv && !c->mixed) ? 0 : C;  // DG metric arrays, FV geometry
   const int64_t Cfv = c->fv ? C : 0;
   try {
     metric.assign((size_t)std::max<int64_t>(Cdg, 1) * 9 * np, 0.);
@@ -439,7 +522,7 @@ int nmg_create(const nmg_mesh *m, int32_t bc_kind, const double k[3], nmg_ctx **
     const double *sc = &scale[e * 3];
     const int cs = cslot[e];
     if (c->fv) fv_pack_element(*m, e, cs, &fvgeo, &fvdist);
-    if (cs >= 0 && !c->fv) {
+    if (cs >= 0 && Cdg > 0) {
       double *Mt = &metric[(size_t)cs * 9 * np];
       double *Mp = &metricp[(size_t)cs * 9 * np];
       int mask = 0;
@@ -481,8 +564,10 @@ int nmg_create(const nmg_mesh *m, int32_t bc_kind, const double k[3], nmg_ctx **
       }
     }
     for (int f = 0; f < 6; f++) {
+      // outer faces only (bslot of a face with a neighbour is an
+      // interface-trace slot)
       const int bs = bslot[e * 6 + f];
-      if (bs < 0) continue;
+      if (bs < 0 || m->nb[e * 6 + f] >= 0) continue;
       const int d = f >> 1;
       const double sig = (f & 1) ? 1. : -1.;
       for (int b = 0; b < n; b++)
@@ -499,10 +584,53 @@ int nmg_create(const nmg_mesh *m, int32_t bc_kind, const double k[3], nmg_ctx **
         }
     }
   }
+  std::vector<double> gM(2 * (size_t)nn, 0.);
+  if (c->mixed) {
+    // M[0][p][j]: Lagrange weight of LGL point j at the equally spaced point
+    // p (Lagrange_of_x with the weights of Lagrange_winterp); M[1][p][j]:
+    // piecewise-linear weight of equally spaced point j at LGL point p
+    // (basis_pw_linear), src/main/basis/Lagrange.c:15-27,151-159 and
+    // src/main/basis/interpolate.c:53-100
+    const double *xl = m->x.data(), *xu = m->xu.data();
+    std::vector<double> wl(n);
+    for (int i = 0; i < n; i++) {
+      double denom = 1.;
+      for (int j = 0; j < n; j++)
+        if (j != i) denom *= (xl[i] - xl[j]);
+      wl[i] = 1. / denom;
+    }
+    auto pwlin = [&](int k, double x) -> double {
+      if (n <= 1) return 1.;
+      if (x < xu[1]) {
+        if (k == 0) return (x - xu[1]) / (xu[0] - xu[1]);
+        if (k == 1) return (x - xu[0]) / (xu[1] - xu[0]);
+        return 0.;
+      }
+      if (x >= xu[n - 2]) {
+        const int n0 = n - 2, n1 = n - 1, l = k - n0;
+        if (l == 0) return (x - xu[n1]) / (xu[n0] - xu[n1]);
+        if (l == 1) return (x - xu[n0]) / (xu[n1] - xu[n0]);
+        return 0.;
+      }
+      if (k < n - 1 && x >= xu[k] && x < xu[k + 1]) return (x - xu[k + 1]) / (xu[k] - xu[k + 1]);
+      if (k > 0 && x >= xu[k - 1] && x < xu[k]) return (x - xu[k - 1]) / (xu[k] - xu[k - 1]);
+      return 0.;
+    };
+    for (int p = 0; p < n; p++)
+      for (int j = 0; j < n; j++) {
+        double prod = 1.;
+        for (int q = 0; q < n; q++)
+          if (q != j) prod *= (xu[p] - xl[q]);
+        gM[p * n + j] = prod * wl[j];
+        gM[nn + p * n + j] = pwlin(j, xl[p]);
+      }
+  }
+  c->nfvel = (int)fvlist.size();
+  c->nghost = (int)(gtab.size() / 4);
   if (c->fv) {
     // midpoint spacings of the uniform points (set_nm_nodemidpoint_distsXb_dir)
     std::vector<double> Xb(n), Xbm(std::max(n - 1, 1));
-    for (int i = 0; i < n; i++) Xb[i] = m->x[i];
+    for (int i = 0; i < n; i++) Xb[i] = m->xu[i];
     for (int i = 0; i < n - 1; i++) Xbm[i] = 0.5 * (Xb[i] + Xb[i + 1]);
     for (int i = 1; i < n - 1; i++) fvdxb[i] = Xbm[i] - Xbm[i - 1];
   }
@@ -531,15 +659,23 @@ int nmg_create(const nmg_mesh *m, int32_t bc_kind, const double k[3], nmg_ctx **
     CK(up(&c->d_fvgeo, fvgeo));
     CK(up(&c->d_fvdist, fvdist));
     CK(up(&c->d_fvdxb, fvdxb));
-  } else {
-    CK(nmgk::eo_upload(n, m->D.data()));
+  }
+  if (!c->fv || c->mixed) CK(nmgk::eo_upload(n, m->D.data()));
+  if (c->mixed) {
+    CK(up(&c->d_isfv, isfv));
+    CK(up(&c->d_fvlist, fvlist));
+    CK(up(&c->d_gtab, gtab));
+    CK(up(&c->d_gM, gM));
+    CK(cudaMalloc((void **)&c->d_ghost, sizeof(double) * 4 * nn * std::max(c->nghost, 1)));
+    CK(cudaMemset(c->d_ghost, 0, sizeof(double) * 4 * nn * std::max(c->nghost, 1)));
   }
   for (int b = 0; b < 4; b++) {
     CK(cudaMalloc((void **)&c->d_buf[b], c->state_len * sizeof(double)));
     CK(cudaMemset(c->d_buf[b], 0, c->state_len * sizeof(double)));
   }
   CK(cudaMalloc((void **)&c->d_step, sizeof(int)));
-  for (int v = 0; v < c->nvariants; v++) {
+  const int ndgv = c->mixed ? c->ndg : (c->fv ? 0 : c->nvariants);
+  for (int v = 0; v < ndgv; v++) {
     StageParams P0;
     std::memset(&P0, 0, sizeof(P0));
     CK(c->variants[v].launch(P0, c->stream));  // nelem == 0: only sets the smem limit
@@ -549,7 +685,7 @@ int nmg_create(const nmg_mesh *m, int32_t bc_kind, const double k[3], nmg_ctx **
     std::memset(&P0, 0, sizeof(P0));
     CK(c->vjp.launch(P0, c->stream));
   } else {
-    for (int v = 0; v < c->nvariants; v++) {
+    for (int v = c->mixed ? c->ndg : 0; v < c->nvariants; v++) {
       StageParams P0;
       std::memset(&P0, 0, sizeof(P0));
       P0.n = n;
@@ -583,6 +719,8 @@ void nmg_destroy(nmg_ctx *c) {
   cudaFree(c->d_metricp); cudaFree(c->d_fac); cudaFree(c->d_bxyz); cudaFree(c->d_bnrm);
   cudaFree(c->d_D);
   cudaFree(c->d_fvgeo); cudaFree(c->d_fvdist); cudaFree(c->d_fvdxb);
+  cudaFree(c->d_fvlist); cudaFree(c->d_gtab); cudaFree(c->d_isfv); cudaFree(c->d_ghost);
+  cudaFree(c->d_gM);
   for (int b = 0; b < 4; b++) cudaFree(c->d_buf[b]);
   cudaFree(c->d_times); cudaFree(c->d_step);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -603,6 +741,8 @@ int nmg_set_kernel(nmg_ctx *c, const char *spec) {
   if (!spec || !*spec || !strcmp(spec, "auto")) {
     c->sel = -1;
     c->tuned = false;
+    c->fsel = -1;
+    c->ftuned = false;
     drop_graphs(c);
     return NMG_OK;
   }
@@ -611,8 +751,13 @@ int nmg_set_kernel(nmg_ctx *c, const char *spec) {
     snprintf(buf, sizeof buf, "%s:%d:%d", c->variants[v].name, c->variants[v].epb,
              c->variants[v].nt);
     if (!strcmp(spec, c->variants[v].name) || !strcmp(spec, buf)) {
-      c->sel = v;
-      c->tuned = true;
+      if (c->mixed && v >= c->ndg) {  // the finite-volume part of a mixed mesh
+        c->fsel = v;
+        c->ftuned = true;
+      } else {
+        c->sel = v;
+        c->tuned = true;
+      }
       drop_graphs(c);
       return NMG_OK;
     }
@@ -630,6 +775,15 @@ int nmg_kernel_info(nmg_ctx *c, char *buf, int32_t len) {
     s = b;
   } else {
     s = "untuned";
+  }
+  if (c->mixed) {
+    char b[64];
+    if (c->fsel >= 0)
+      snprintf(b, sizeof b, " + %s:%d:%d", c->variants[c->fsel].name, c->variants[c->fsel].epb,
+               c->variants[c->fsel].nt);
+    else
+      snprintf(b, sizeof b, " + untuned");
+    s += b;
   }
   s += " | candidates:";
   for (int v = 0; v < c->nvariants; v++) {
@@ -700,6 +854,7 @@ static int capture_step_graph(nmg_ctx *c, int cur, double dt) {
   advance_step_kernel<<<1, 1, 0, c->stream>>>(c->d_step);
   cudaError_t e1 = cudaGetLastError();
   cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
+  c->graph_launches = c->launches - l0 + 1;  // stage launches + step counter
   c->launches = l0;  // captured, not launched
   if (rc) return rc;
   CK(e1);
@@ -728,7 +883,7 @@ int nmg_rk4_steps(nmg_ctx *c, double t, double dt, int32_t nsteps) {
     c->times_cap = nsteps;
     drop_graphs(c);
   }
-  if (dt != c->graph_dt || c->graph_sel != c->sel) {
+  if (dt != c->graph_dt || c->graph_sel != c->sel * 64 + c->fsel) {
     drop_graphs(c);
     c->graph_dt = dt;
   }
@@ -737,13 +892,13 @@ int nmg_rk4_steps(nmg_ctx *c, double t, double dt, int32_t nsteps) {
       int rc = capture_step_graph(c, g, dt);
       if (rc) return rc;
     }
-  c->graph_sel = c->sel;
+  c->graph_sel = c->sel * 64 + c->fsel;
   CK(cudaMemcpyAsync(c->d_times, times.data(), sizeof(double) * nsteps, cudaMemcpyHostToDevice,
                      c->stream));
   CK(cudaMemsetAsync(c->d_step, 0, sizeof(int), c->stream));
   for (int s = 0; s < nsteps; s++) {
     CK(cudaGraphLaunch(c->graph[c->cur], c->stream));
-    c->launches += 5;
+    c->launches += c->graph_launches;
     c->cur = 1 - c->cur;
   }
   CK(cudaStreamSynchronize(c->stream));
@@ -786,7 +941,7 @@ int nmg_rk4_step_vjp(nmg_ctx *c, double t, double dt, const double *u_n_dev, dou
   if (!c || !ubar_dev) return set_err(c, NMG_EINVAL, "nmg_rk4_step_vjp: null argument");
   if (c->fv) return set_err(c, NMG_EUNSUP, "nmg_rk4_step_vjp: finite-volume RHS is nonlinear");
   double *acc = c->d_buf[1 - c->cur];  // free between steps
-  int rc = step_buffers(c, c->vjp, t, dt, ubar_dev, acc, c->d_buf[2], c->d_buf[3]);
+  int rc = step_buffers(c, true, t, dt, ubar_dev, acc, c->d_buf[2], c->d_buf[3]);
   if (rc) return rc;
   CK(cudaMemcpyAsync(ubar_dev, acc, c->state_len * sizeof(double), cudaMemcpyDeviceToDevice,
                      c->stream));
@@ -804,7 +959,6 @@ int nmg_adjoint_gradient(nmg_ctx *c, double t0, double dt, int32_t nsteps, int32
     return set_err(c, NMG_EINVAL, "nmg_adjoint_gradient: bad argument");
   int rc = autotune(c);
   if (rc) return rc;
-  const Variant &F = c->variants[c->sel];
   const size_t L = c->state_len, bytes = L * sizeof(double);
   const int K = ckpt_every, nck = (nsteps + K - 1) / K;
   const int np = c->np, E = (int)c->nelem;
@@ -852,7 +1006,7 @@ int nmg_adjoint_gradient(nmg_ctx *c, double t0, double dt, int32_t nsteps, int32
     const double *u = ck[0];
     for (int s = 1; s <= nsteps; s++) {
       double *out = seg[(s - 1) % nseg];
-      if ((rc = step_buffers(c, F, ts[s - 1], dt, u, out, WA, WB))) { cleanup(); return rc; }
+      if ((rc = step_buffers(c, false, ts[s - 1], dt, u, out, WA, WB))) { cleanup(); return rc; }
       obj_partial_kernel<<<nblk, kObjThreads, 0, st>>>(out, weight_dev, E, np, partial);
       obj_final_kernel<<<1, 1, 0, st>>>(partial, nblk, dt, jdev);
       c->launches += 2;
@@ -868,7 +1022,7 @@ int nmg_adjoint_gradient(nmg_ctx *c, double t0, double dt, int32_t nsteps, int32
     const int s0 = cidx * K, s1 = std::min(nsteps, s0 + K);
     const double *u = ck[cidx];
     for (int s = s0 + 1; s <= s1; s++) {  // recompute u_{s0+1..s1}
-      if ((rc = step_buffers(c, F, ts[s - 1], dt, u, seg[s - s0 - 1], WA, WB))) {
+      if ((rc = step_buffers(c, false, ts[s - 1], dt, u, seg[s - s0 - 1], WA, WB))) {
         cleanup();
         return rc;
       }
@@ -877,7 +1031,7 @@ int nmg_adjoint_gradient(nmg_ctx *c, double t0, double dt, int32_t nsteps, int32
     for (int s = s1; s > s0; s--) {
       adj_source_kernel<<<nblk, 256, 0, st>>>(lam[li], seg[s - s0 - 1], weight_dev, E, np,
                                               2.0 * dt);
-      if ((rc = step_buffers(c, c->vjp, ts[s - 1], dt, lam[li], lam[1 - li], WA, WB))) {
+      if ((rc = step_buffers(c, true, ts[s - 1], dt, lam[li], lam[1 - li], WA, WB))) {
         cleanup();
         return rc;
       }

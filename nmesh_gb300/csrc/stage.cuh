@@ -62,7 +62,15 @@ struct StageParams {
   const double *fvgeo;  // [C][13][np]: 1/J, sqrtgdiag[3], unit normals n_d[3] (d-major)
   const double *fvdist; // [E][6] distance (element coords) of each face to its nearest midpoint
   const double *fvdxb;  // [n] midpoint spacings dXb[i] = Xbm[i] - Xbm[i-1], 1 <= i <= n-2
+  // mixed DG / finite-volume meshes
+  const unsigned char *skip;  // [E] 1: finite-volume element (DG kernels write nothing)
+  const int *fvlist;    // [nfvel] finite-volume elements (FV kernel grid), or null: all
+  int nfvel;
+  const double *ghost;  // [G][4][nn] interpolated traces of faces with code & 64;
+                        // slot G = bslot[e*6+f]
 };
+
+constexpr int kCodeMixed = 64;  // face-table bit: neighbour of the other point type
 
 template <int N>
 __device__ __forceinline__ int face_node_d(int f, int a, int b) {
@@ -125,15 +133,23 @@ __device__ __forceinline__ void face_terms(const StageParams &P, const double *s
       const int nbe = __ldg(P.nb + e * 6 + f);
       if (nbe >= 0) {
         const int cd = __ldg(P.code + e * 6 + f), f2 = cd & 7, o = cd >> 3;
-        const int sw = o & 1, fa = (o >> 1) & 1, fb = (o >> 2) & 1;
-        int aa = sw ? b : a, bb = sw ? a : b;
-        aa = fa ? N - 1 - aa : aa;
-        bb = fb ? N - 1 - bb : bb;
-        const double *W2 = P.win + (size_t)nbe * NF * NP + face_node_d<N>(f2, aa, bb);
-        ua0 = __ldg(W2);
-        ua1 = __ldg(W2 + NP);
-        ua2 = __ldg(W2 + 2 * NP);
-        ua3 = __ldg(W2 + 3 * NP);
+        if (cd & kCodeMixed) {
+          const double *G = P.ghost + (size_t)__ldg(P.bslot + e * 6 + f) * 4 * NN + ab;
+          ua0 = G[0];
+          ua1 = G[NN];
+          ua2 = G[2 * NN];
+          ua3 = G[3 * NN];
+        } else {
+          const int sw = o & 1, fa = (o >> 1) & 1, fb = (o >> 2) & 1;
+          int aa = sw ? b : a, bb = sw ? a : b;
+          aa = fa ? N - 1 - aa : aa;
+          bb = fb ? N - 1 - bb : bb;
+          const double *W2 = P.win + (size_t)nbe * NF * NP + face_node_d<N>(f2, aa, bb);
+          ua0 = __ldg(W2);
+          ua1 = __ldg(W2 + NP);
+          ua2 = __ldg(W2 + 2 * NP);
+          ua3 = __ldg(W2 + 3 * NP);
+        }
       } else {
         const int bs = __ldg(P.bslot + e * 6 + f);
         if (P.bc == NMG_BC_EXACT_PLANEWAVE) {
@@ -202,15 +218,23 @@ __device__ __forceinline__ void face_fetch(const StageParams &P, int e, int f, i
   F.kind = 0;
   if (nbe >= 0) {
     const int cd = __ldg(P.code + e * 6 + f), f2 = cd & 7, o = cd >> 3;
-    const int sw = o & 1, fa = (o >> 1) & 1, fb = (o >> 2) & 1;
-    int aa = sw ? b : a, bb = sw ? a : b;
-    aa = fa ? N - 1 - aa : aa;
-    bb = fb ? N - 1 - bb : bb;
-    const double *W2 = P.win + (size_t)nbe * NF * NP + face_node_d<N>(f2, aa, bb);
-    F.v0 = __ldg(W2);
-    F.v1 = __ldg(W2 + NP);
-    F.v2 = __ldg(W2 + 2 * NP);
-    F.v3 = __ldg(W2 + 3 * NP);
+    if (cd & kCodeMixed) {
+      const double *G = P.ghost + (size_t)__ldg(P.bslot + e * 6 + f) * 4 * NN + ab;
+      F.v0 = G[0];
+      F.v1 = G[NN];
+      F.v2 = G[2 * NN];
+      F.v3 = G[3 * NN];
+    } else {
+      const int sw = o & 1, fa = (o >> 1) & 1, fb = (o >> 2) & 1;
+      int aa = sw ? b : a, bb = sw ? a : b;
+      aa = fa ? N - 1 - aa : aa;
+      bb = fb ? N - 1 - bb : bb;
+      const double *W2 = P.win + (size_t)nbe * NF * NP + face_node_d<N>(f2, aa, bb);
+      F.v0 = __ldg(W2);
+      F.v1 = __ldg(W2 + NP);
+      F.v2 = __ldg(W2 + 2 * NP);
+      F.v3 = __ldg(W2 + 3 * NP);
+    }
   } else {
     const int bs = __ldg(P.bslot + e * 6 + f);
     if (P.bc == NMG_BC_EXACT_PLANEWAVE) {
@@ -266,7 +290,7 @@ __device__ __forceinline__ void epilogue(const StageParams &P, const double *sW,
   for (int q = threadIdx.x; q < EPB * NF * NP; q += NT) {
     const int le = q / (NF * NP), rem = q - le * NF * NP, f = rem / NP, node = rem - f * NP;
     const int e = e0 + le;
-    if (e >= P.nelem) continue;
+    if (e >= P.nelem || (P.skip && P.skip[e])) continue;
     const size_t idx = ((size_t)e * NF + f) * NP + node;
     double r;
     if (f < 4) {
@@ -316,5 +340,11 @@ cudaError_t eo_upload(int n, const double *D);
 constexpr int kFvMaxN = 13;
 size_t fv_smem(int n);
 int fv_variants(int n, Variant *out, int cap);
+// interpolated traces of the faces between DG and finite-volume elements:
+// gtab[g] = (e, f, e2, code), M = [2][n][n] (Lagrange weights of the LGL
+// points at the equally spaced positions; piecewise-linear weights of the
+// equally spaced points at the LGL positions)
+cudaError_t ghost_launch(int nghost, int n, const int *gtab, const unsigned char *isfv,
+                         const double *M, const double *win, double *ghost, cudaStream_t st);
 
 }  // namespace nmgk

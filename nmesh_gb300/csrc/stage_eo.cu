@@ -293,7 +293,7 @@ __device__ __forceinline__ void eof_body(const StageParams &P, int blk) {
   for (int q = tid; q < EPB * NF * NP; q += NT) {
     const int le = q / (NF * NP), rem = q - le * NF * NP, f = rem / NP, node = rem - f * NP;
     const int e = e0 + le;
-    if (e >= P.nelem) continue;
+    if (e >= P.nelem || (P.skip && P.skip[e])) continue;
     const size_t idx = ((size_t)e * NF + f) * NP + node;
     double r;
     if (f == 0) {

@@ -33,6 +33,9 @@
 // accumulates div f; the face terms and the RK4 update follow.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cstdint>
+
 #include "stage.cuh"
 
 #ifdef NMG_FV_FAST
@@ -213,12 +216,17 @@ __device__ void face_fnum(const StageParams &P, int e, int f, int a, int b, cons
   const int nbe = __ldg(P.nb + e * 6 + f);
   if (nbe >= 0) {
     const int cd = __ldg(P.code + e * 6 + f), f2 = cd & 7, o = cd >> 3;
-    const int sw = o & 1, fa = (o >> 1) & 1, fb = (o >> 2) & 1;
-    int aa = sw ? b : a, bb = sw ? a : b;
-    aa = fa ? n - 1 - aa : aa;
-    bb = fb ? n - 1 - bb : bb;
-    const double *W2 = P.win + (size_t)nbe * NF * np + fnode(n, f2, aa, bb);
-    for (int l = 0; l < 4; l++) ua[l] = __ldg(W2 + l * np);
+    if (cd & kCodeMixed) {
+      const double *G = P.ghost + (size_t)__ldg(P.bslot + e * 6 + f) * 4 * nn + a + n * b;
+      for (int l = 0; l < 4; l++) ua[l] = G[l * nn];
+    } else {
+      const int sw = o & 1, fa = (o >> 1) & 1, fb = (o >> 2) & 1;
+      int aa = sw ? b : a, bb = sw ? a : b;
+      aa = fa ? n - 1 - aa : aa;
+      bb = fb ? n - 1 - bb : bb;
+      const double *W2 = P.win + (size_t)nbe * NF * np + fnode(n, f2, aa, bb);
+      for (int l = 0; l < 4; l++) ua[l] = __ldg(W2 + l * np);
+    }
   } else {
     const int bs = __ldg(P.bslot + e * 6 + f), ab = a + n * b;
     if (P.bc == NMG_BC_EXACT_PLANEWAVE) {
@@ -270,7 +278,7 @@ template <int NT>
 __global__ void __launch_bounds__(NT) fv_kernel(const StageParams P) {
   extern __shared__ double smem[];
   const int n = P.n, np = n * n * n, nn = n * n, nm = n - 1;
-  const int e = blockIdx.x;
+  const int e = P.fvlist ? __ldg(P.fvlist + blockIdx.x) : (int)blockIdx.x;
   if (e >= P.nelem) return;
   double *sW = smem;             // [4][np]  pi, cx, cy, cz of w
   double *sD = sW + 4 * np;      // [4][np]  div f accumulators
@@ -417,7 +425,9 @@ cudaError_t launch_fv(const StageParams &P, cudaStream_t st) {
   if (P.nelem == 0)
     return cudaFuncSetAttribute(fv_kernel<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)smem);
-  fv_kernel<NT><<<P.nelem, NT, smem, st>>>(P);
+  const int grid = P.fvlist ? P.nfvel : P.nelem;
+  if (grid == 0) return cudaSuccess;
+  fv_kernel<NT><<<grid, NT, smem, st>>>(P);
   return cudaGetLastError();
 }
 
@@ -447,6 +457,49 @@ size_t fv_smem(int n) {
 int fv_variants(int n, Variant *out, int cap) {
   int k = fv_fast::variants(n, out, cap);
   return k + fv_exact::variants(n, out + k, cap - k);
+}
+
+namespace {
+// One thread per (slot, field, face node): the neighbour's face plane
+// interpolated to this face's node, sum_b sum_a v(a,b) B1[a] B2[b] with the
+// neighbour's basis (basis_array_interp2d, src/main/basis/interpolate.c:296),
+// rounded in that order (this file has no FMA contraction).
+__global__ void __launch_bounds__(256) ghost_kernel(int nghost, int n, const int *gtab,
+                                                   const unsigned char *isfv, const double *M,
+                                                   const double *win, double *ghost) {
+  const int nn = n * n, np = nn * n;
+  const int64_t total = (int64_t)nghost * 4 * nn;
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    const int g = (int)(q / (4 * nn)), rem = (int)(q - (int64_t)g * 4 * nn);
+    const int l = rem / nn, ab = rem - l * nn, a = ab % n, b = ab / n;
+    const int e2 = __ldg(gtab + 4 * g + 2), cd = __ldg(gtab + 4 * g + 3);
+    const int f2 = cd & 7, o = (cd >> 3) & 7;
+    const int sw = o & 1, fa = (o >> 1) & 1, fb = (o >> 2) & 1;
+    int aa = sw ? b : a, bb = sw ? a : b;
+    aa = fa ? n - 1 - aa : aa;
+    bb = fb ? n - 1 - bb : bb;
+    // basis of the neighbour's points at this face's point positions
+    const double *Mk = M + (isfv[e2] ? 1 : 0) * nn;
+    const double *v = win + ((size_t)e2 * NF + l) * np;
+    double sum = 0.;
+    for (int k = 0; k < n; k++) {
+      const double B2 = __ldg(Mk + bb * n + k);
+      for (int j = 0; j < n; j++)
+        sum += __ldg(v + fv_exact::fnode(n, f2, j, k)) * __ldg(Mk + aa * n + j) * B2;
+    }
+    ghost[(size_t)g * 4 * nn + l * nn + ab] = sum;
+  }
+}
+}  // namespace
+
+cudaError_t ghost_launch(int nghost, int n, const int *gtab, const unsigned char *isfv,
+                         const double *M, const double *win, double *ghost, cudaStream_t st) {
+  if (nghost <= 0) return cudaSuccess;
+  const int64_t total = (int64_t)nghost * 4 * n * n;
+  const int grid = (int)std::min<int64_t>((total + 255) / 256, 152 * 16);
+  ghost_kernel<<<grid, 256, 0, st>>>(nghost, n, gtab, isfv, M, win, ghost);
+  return cudaGetLastError();
 }
 #endif
 

@@ -31,6 +31,8 @@ def load(case):
 def build_mesh(meta, periodic=False):
     import nmesh_gb300 as ng
     fv = "fv" in meta
+    if fv and "patches" in meta["fv"]:
+        fv = [int(p) for p in meta["fv"]["patches"].split()]
     if meta["mesh"] == "box":
         return ng.Mesh.build(ng.MESH_BOX, n=meta["n"], luni=meta["luni"],
                              xc=(PI, PI, PI), box_dout=PI, periodic=periodic, fv=fv)
@@ -67,11 +69,15 @@ def oracle_for(mesh, bc=0, k=(1.0, 1.0, 1.0), period=None, fv_rec="WENOm3_2",
     curvi = np.array([0 if np.allclose(dXdx[e], np.repeat(np.eye(3).ravel()[:, None],
                                                           mesh.np, 1)) else 1
                       for e in range(mesh.nelem)], np.int32)
-    nb = nmo.match_faces(xyz, mesh.n, period=period)
     fv = mesh.fv()
+    mix = None
+    if fv.any():
+        nb, mix = nmo.match_faces(xyz, mesh.n, period=period, fv=fv)
+    else:
+        nb = nmo.match_faces(xyz, mesh.n, period=period)
     return nmo.OracleMesh(bbox, curvi, dXdx, xyz, nb, mesh.n, bc=bc, k=k,
                           fv=fv if fv.any() else None, fv_rec=fv_rec,
-                          fv_extrap=fv_extrap, fv_w3ratio=fv_w3ratio)
+                          fv_extrap=fv_extrap, fv_w3ratio=fv_w3ratio, mixface=mix)
 
 
 def gaussian_pulses(xyz, seed, npulse=8, rmin=3.0, rmax=10.0, wmin=0.5, wmax=2.0,

@@ -5,11 +5,11 @@ import numpy as np
 import pytest
 
 import nmesh_gb300 as ng
-from helpers import CASES, FV_CASES, PI, build_mesh, load, perm_to_mesh
+from helpers import CASES, FV_CASES, MIX_CASES, PI, build_mesh, load, perm_to_mesh
 from oracle import nmo
 
 
-@pytest.mark.parametrize("case", CASES + FV_CASES)
+@pytest.mark.parametrize("case", CASES + FV_CASES + MIX_CASES)
 def test_geometry_bitexact(case):
     """Coordinates and metric on LGL points (DG) and on equally spaced
     points (finite-volume meshes) equal the reference's."""
@@ -30,19 +30,34 @@ def test_uniform_points_match_oracle():
         assert np.array_equal(x, nmo.uniform(n))
 
 
-def test_mixed_fv_desc_rejected():
-    m = ng.Mesh.build(ng.MESH_BOX, n=4, luni=1, xc=(0, 0, 0), box_dout=1.0, fv=True)
+def test_mixed_dg_fv_face_table():
+    """Inner cube finite-volume, shells DG: exactly the faces between the two
+    point types carry the mixed bit (64), with the orientation found from the
+    corners; the element-by-element description reproduces the table."""
+    m = ng.Mesh.build(ng.MESH_CUBEDSPHERES7, n=5, luni=1, cs_dc=1.0, cs_r0fac=20.0, fv=[0])
     pat, bbox = m.elements()
-    fv = np.zeros(m.nelem, np.int32)
-    fv[0] = 1
-    with pytest.raises(ng.NmgError):
-        ng.Mesh.from_arrays(bbox, np.zeros(m.nelem, np.int32), m.coords(), fv=fv)
-    m2 = ng.Mesh.from_arrays(bbox, np.zeros(m.nelem, np.int32), m.coords(),
-                             fv=np.ones(m.nelem, np.int32))
-    assert m2.fv().all()
-    nb1, code1 = m.faces()
+    fv = m.fv()
+    assert np.array_equal(fv, (pat == 0).astype(np.int32))
+    nb, code = m.faces()
+    for e in range(m.nelem):
+        for f in range(6):
+            if nb[e, f] < 0:
+                assert code[e, f] == 0
+                continue
+            assert bool(code[e, f] & 64) == (fv[e] != fv[nb[e, f]])
+    assert (code & 64).any()
+    m2 = ng.Mesh.from_arrays(bbox, (pat > 0).astype(np.int32), m.coords(), dXdx=m.dXdx(),
+                             pat=pat, fv=fv)
+    assert np.array_equal(m2.fv(), fv)
     nb2, code2 = m2.faces()
-    assert np.array_equal(nb1, nb2) and np.array_equal(code1, code2)
+    assert np.array_equal(nb, nb2) and np.array_equal(code, code2)
+    # the oracle's own matcher finds the same mixed faces and orientations
+    nbo, mix = nmo.match_faces(m.coords(), 5, fv=fv)
+    for e in range(m.nelem):
+        for f in range(6):
+            if code[e, f] & 64:
+                assert (nbo[e, f] == -2).all()
+                assert tuple(mix[e, f]) == (nb[e, f], code[e, f] & 7, (code[e, f] >> 3) & 7)
 
 
 def _faces_from_nbnode(nbnode, n):
