@@ -142,6 +142,46 @@ int nmg_get_state(nmg_ctx *c, double *host_u);
 /* device pointer of the resident state u (for zero-copy use) */
 double *nmg_state_device_ptr(nmg_ctx *c);
 
+/* A context whose elements can switch between DG (LGL points) and finite
+ * volume (equally spaced points) while it runs: both geometries of every
+ * element are kept, and every RK4 stage runs the interface-trace, DG and
+ * finite-volume kernels.  The mesh must be generated (nmg_mesh_build) or
+ * have Cartesian elements only. */
+int nmg_create_switchable(const nmg_mesh *m, int32_t bc_kind, const double k[3],
+                          nmg_ctx **out);
+/* switch element types (fv[e] = 1: finite volume) and convert the resident
+ * state of the switched elements: LGL -> equally spaced points by Lagrange
+ * interpolation, back by its inverse (the reference's p-refinement between
+ * P_LGL and P_UNIFORM, src/main/basis/gridpoints.c:158-317) */
+int nmg_set_element_types(nmg_ctx *c, const int32_t *fv);
+int nmg_get_element_types(nmg_ctx *c, int32_t *fv);
+
+/* Trouble detection for the scalar wave: an element is troubled when a
+ * field leaves the relaxed discrete maximum principle bounds of the previous
+ * state over the element and its face neighbours (evolve_RDMP_trouble,
+ * src/main/evolve/trouble.c:438-503) or, on a DG element, when Persson's
+ * modal indicator of a field exceeds persson_max
+ * (evolve_Persson_array_indicator, trouble.c:505-564). */
+typedef struct nmg_trouble_params {
+  double rdmp_deltafac, rdmp_delta0, rdmp_epsilon;  /* evolve_RDMP_trouble args */
+  double persson_max;      /* log10 indicator threshold (large: off) */
+  double persson_uscale;   /* u_scale of the indicator (< 0: keep c_0) */
+  int32_t notroubles;      /* quiet steps before switching back to DG
+                              (NOTROUBLES = 11, src/main/evolve/evolve.h:60) */
+} nmg_trouble_params;
+/* flags[e]: DG troubled 1, DG fine 0, FV troubled 0, FV fine -1 (the
+ * reference's TROUBLE return convention, trouble.c:17-26) for state u_dev
+ * against u_p_dev; persson[E][5] (may be NULL): the indicators (0 on FV) */
+int nmg_trouble_check(nmg_ctx *c, const double *u_dev, const double *u_p_dev,
+                      const nmg_trouble_params *tp, int32_t *flags, double *persson);
+/* One RK4 step of the resident state with trouble detection and element
+ * switching (evolve_mesh with evolve_redo_troubled = step,
+ * src/main/evolve/evolve.c:74-140); switched[0] = elements switched to FV
+ * (the step was then redone), switched[1] = elements switched back to DG */
+int nmg_rk4_step_trouble(nmg_ctx *c, double t, double dt, const nmg_trouble_params *tp,
+                         int32_t *switched);
+int nmg_get_trouble_scores(nmg_ctx *c, int32_t *scores);
+
 /* Finite-volume options of a context whose mesh is finite-volume: the
  * reference's DG globals fv_rec, fv_divf_extrap and
  * fv_WENOm3_opt_weightratio (src/main/dg/dg.c:286-400; defaults WENOm3_2,

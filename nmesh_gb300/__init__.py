@@ -43,6 +43,18 @@ class _MeshParams(ctypes.Structure):
                 ("fv", ctypes.c_int32)]
 
 
+class TroubleParams(ctypes.Structure):
+    """Trouble detection parameters (include/nmg.h nmg_trouble_params)."""
+    _fields_ = [("rdmp_deltafac", ctypes.c_double), ("rdmp_delta0", ctypes.c_double),
+                ("rdmp_epsilon", ctypes.c_double), ("persson_max", ctypes.c_double),
+                ("persson_uscale", ctypes.c_double), ("notroubles", ctypes.c_int32)]
+
+    def __init__(self, rdmp_deltafac=1.0, rdmp_delta0=1e-4, rdmp_epsilon=1e-3,
+                 persson_max=1e300, persson_uscale=-1.0, notroubles=11):
+        super().__init__(rdmp_deltafac, rdmp_delta0, rdmp_epsilon, persson_max,
+                         persson_uscale, notroubles)
+
+
 class _MeshDesc(ctypes.Structure):
     _fields_ = [("nelem", ctypes.c_int32), ("n", ctypes.c_int32),
                 ("pat", ctypes.c_void_p), ("bbox", ctypes.c_void_p),
@@ -112,6 +124,12 @@ def lib(build_if_missing=True):
         "nmg_mesh_get_fv": (ctypes.c_int, [vp, vp]),
         "nmg_uniform_points": (ctypes.c_int, [i32, vp]),
         "nmg_set_fv": (ctypes.c_int, [vp, i32, i32, f64]),
+        "nmg_create_switchable": (ctypes.c_int, [vp, i32, vp, vp]),
+        "nmg_set_element_types": (ctypes.c_int, [vp, vp]),
+        "nmg_get_element_types": (ctypes.c_int, [vp, vp]),
+        "nmg_trouble_check": (ctypes.c_int, [vp, vp, vp, vp, vp, vp]),
+        "nmg_rk4_step_trouble": (ctypes.c_int, [vp, f64, f64, vp, vp]),
+        "nmg_get_trouble_scores": (ctypes.c_int, [vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -243,11 +261,14 @@ class Mesh:
 class Evolution:
     """Device context: mesh data and RK4 state resident in HBM."""
 
-    def __init__(self, mesh, bc=BC_EXACT_PLANEWAVE, k=(1.0, 1.0, 1.0)):
+    def __init__(self, mesh, bc=BC_EXACT_PLANEWAVE, k=(1.0, 1.0, 1.0), switchable=False):
+        """switchable=True: elements can change between DG and finite volume
+        (nmg_create_switchable)."""
         self.mesh = mesh
         kk = np.ascontiguousarray(k, np.float64)
         h = ctypes.c_void_p()
-        rc = lib().nmg_create(mesh._h, int(bc), _ptr(kk), ctypes.byref(h))
+        create = lib().nmg_create_switchable if switchable else lib().nmg_create
+        rc = create(mesh._h, int(bc), _ptr(kk), ctypes.byref(h))
         self._h = h
         if rc:
             msg = lib().nmg_last_error(h).decode() if h.value else ""
@@ -328,6 +349,42 @@ class Evolution:
             raise NmgError(f"nmg_set_fv: unknown fv_rec {rec!r} or fv_divf_extrap {extrap!r}")
         self._check(lib().nmg_set_fv(self._h, FV_REC[rec], FV_EXTRAP[extrap],
                                      float(w3ratio)), "nmg_set_fv")
+
+    # ---- DG <-> finite-volume switching ----
+    def set_element_types(self, fv):
+        """Switch element types (1: finite volume) converting the state."""
+        f = np.ascontiguousarray(fv, np.int32)
+        self._check(lib().nmg_set_element_types(self._h, _ptr(f)), "nmg_set_element_types")
+
+    def element_types(self):
+        f = np.zeros(self.mesh.nelem, np.int32)
+        self._check(lib().nmg_get_element_types(self._h, _ptr(f)), "nmg_get_element_types")
+        return f
+
+    def trouble_check_device(self, u_ptr, u_p_ptr, params=None):
+        """Trouble flags and Persson indicators of device state u_ptr against
+        u_p_ptr (ints)."""
+        tp = params or TroubleParams()
+        fl = np.zeros(self.mesh.nelem, np.int32)
+        pe = np.zeros((self.mesh.nelem, NFIELDS))
+        self._check(lib().nmg_trouble_check(self._h, ctypes.c_void_p(u_ptr),
+                                            ctypes.c_void_p(u_p_ptr), ctypes.byref(tp),
+                                            _ptr(fl), _ptr(pe)), "nmg_trouble_check")
+        return fl, pe
+
+    def rk4_step_trouble(self, t, dt, params=None):
+        """One RK4 step with trouble detection and element switching; returns
+        (elements switched to FV, elements switched back to DG)."""
+        tp = params or TroubleParams()
+        sw = np.zeros(2, np.int32)
+        self._check(lib().nmg_rk4_step_trouble(self._h, float(t), float(dt), ctypes.byref(tp),
+                                               _ptr(sw)), "nmg_rk4_step_trouble")
+        return int(sw[0]), int(sw[1])
+
+    def trouble_scores(self):
+        s_ = np.zeros(self.mesh.nelem, np.int32)
+        self._check(lib().nmg_get_trouble_scores(self._h, _ptr(s_)), "nmg_get_trouble_scores")
+        return s_
 
     def set_kernel(self, spec="auto"):
         """Force a stage-kernel variant ("eo", "gather", "eo:<epb>:<threads>")

@@ -52,13 +52,7 @@ void legendre_P_dP_Q_dQ(int l, double x, double *P, double *dP, double *Q,
 }
 
 // one patch of the mesh
-struct Patch {
-  double bbox[6];
-  bool cubed = false;  // outer cubed-sphere patch (else Cartesian box)
-  int dom = 0;         // cubed-sphere domain 0..5
-  double xc[3] = {0, 0, 0};
-  double s0 = 0, s1 = 0;  // inner flat distance and outer sphere radius
-};
+using nmg::Patch;
 
 // x and dX/dx of an outerCubedSphere patch with constant sigma1 = s1
 // (xyz_of_lamAB_CubSph / dlamAB_dxyz_CubSph), same operation order
@@ -174,12 +168,14 @@ void elem_bbox(const double pb[6], int L, const int ixyz[3], double bb[6]) {
 }
 
 // fill geometry for all elements of the given patches, uniform level L,
-// elements of a patch in Morton (Z) order
+// elements of a patch in Morton (Z) order; patches in fvmask get equally
+// spaced points
 void fill_geometry(nmg_mesh &m, const std::vector<Patch> &pats, int L, int32_t fvmask) {
   const int n = m.n, np = n * n * n;
   const int ne1 = 1 << L;
   const int64_t per = (int64_t)ne1 * ne1 * ne1;
   m.nelem = per * (int64_t)pats.size();
+  m.patches = pats;
   m.pat.resize(m.nelem);
   m.bbox.resize(m.nelem * 6);
   m.curvi.resize(m.nelem);
@@ -192,34 +188,12 @@ void fill_geometry(nmg_mesh &m, const std::vector<Patch> &pats, int L, int32_t f
       int ixyz[3] = {0, 0, 0};
       for (int bit = 0; bit < L; bit++)
         for (int d = 0; d < 3; d++) ixyz[d] |= (int)((mc >> (3 * bit + d)) & 1) << bit;
-      double *bb = &m.bbox[e * 6];
-      elem_bbox(pats[p].bbox, L, ixyz, bb);
+      elem_bbox(pats[p].bbox, L, ixyz, &m.bbox[e * 6]);
       m.pat[e] = (int32_t)p;
       m.curvi[e] = pats[p].cubed ? 1 : 0;
       const bool isfv = (fvmask >> p) & 1;
       if (isfv) m.fv[e] = 1;
-      const double *px = isfv ? m.xu.data() : m.x.data();
-      double *X3 = &m.xyz[e * 3 * np];
-      double *M9 = &m.dXdx[e * 9 * np];
-      for (int k = 0; k < n; k++)
-        for (int j = 0; j < n; j++)
-          for (int i = 0; i < n; i++) {
-            int ijk = i + n * (j + n * k);
-            double Xb[3] = {px[i], px[j], px[k]}, X[3], x[3], J[3][3];
-            for (int d = 0; d < 3; d++)
-              X[d] = 0.5 * ((bb[2 * d + 1] - bb[2 * d]) * Xb[d] + (bb[2 * d + 1] + bb[2 * d]));
-            if (pats[p].cubed) {
-              cubsph_x_dXdx(pats[p], X, x, J);
-            } else {
-              for (int d = 0; d < 3; d++) {
-                x[d] = X[d];
-                for (int c = 0; c < 3; c++) J[d][c] = (d == c) ? 1. : 0.;
-              }
-            }
-            for (int d = 0; d < 3; d++) X3[d * np + ijk] = x[d];
-            for (int a = 0; a < 3; a++)
-              for (int c = 0; c < 3; c++) M9[(a * 3 + c) * np + ijk] = J[a][c];
-          }
+      nmg::element_geometry(m, e, isfv, &m.xyz[e * 3 * np], &m.dXdx[e * 9 * np]);
     }
   }
 }
@@ -322,6 +296,35 @@ void uniform_basis(int n, double *x, double *w, double *D) {
     for (int j = 1; j < N; j++) w[j] = 2. / N;
   }
   lagrange_D(n, x, D);
+}
+
+bool element_geometry(const nmg_mesh &m, int64_t e, bool uniform, double *xyz, double *dXdx) {
+  const int n = m.n, np = n * n * n;
+  const double *bb = &m.bbox[e * 6];
+  const double *px = uniform ? m.xu.data() : m.x.data();
+  const Patch *pat = nullptr;
+  if (!m.patches.empty()) pat = &m.patches[m.pat[e]];
+  else if (m.curvi[e]) return false;  // map of a described curvilinear element unknown
+  for (int k = 0; k < n; k++)
+    for (int j = 0; j < n; j++)
+      for (int i = 0; i < n; i++) {
+        const int ijk = i + n * (j + n * k);
+        double Xb[3] = {px[i], px[j], px[k]}, X[3], x[3], J[3][3];
+        for (int d = 0; d < 3; d++)
+          X[d] = 0.5 * ((bb[2 * d + 1] - bb[2 * d]) * Xb[d] + (bb[2 * d + 1] + bb[2 * d]));
+        if (pat && pat->cubed) {
+          cubsph_x_dXdx(*pat, X, x, J);
+        } else {
+          for (int d = 0; d < 3; d++) {
+            x[d] = X[d];
+            for (int c = 0; c < 3; c++) J[d][c] = (d == c) ? 1. : 0.;
+          }
+        }
+        for (int d = 0; d < 3; d++) xyz[d * np + ijk] = x[d];
+        for (int a = 0; a < 3; a++)
+          for (int c = 0; c < 3; c++) dXdx[(a * 3 + c) * np + ijk] = J[a][c];
+      }
+  return true;
 }
 
 std::string pack_faces(nmg_mesh &m, const int64_t *nbnode, const double period[3]) {

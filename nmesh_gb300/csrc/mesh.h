@@ -5,6 +5,18 @@
 #include <string>
 #include <vector>
 
+namespace nmg {
+// a patch of a generated mesh: a Cartesian box or an outer cubed-sphere
+// patch (coordtrans_CubedSphere.c with constant sigma)
+struct Patch {
+  double bbox[6];
+  bool cubed = false;  // outer cubed-sphere patch (else Cartesian box)
+  int dom = 0;         // cubed-sphere domain 0..5
+  double xc[3] = {0, 0, 0};
+  double s0 = 0, s1 = 0;  // inner flat distance and outer sphere radius
+};
+}  // namespace nmg
+
 struct nmg_mesh {
   int n = 0;        // LGL nodes per direction
   int64_t nelem = 0;
@@ -19,6 +31,8 @@ struct nmg_mesh {
   std::vector<double> xu;      // equally spaced points (finite-volume elements)
   std::vector<int32_t> fv;     // [E] 1: finite-volume element on equally
                                // spaced points; empty: all DG on LGL points
+  std::vector<nmg::Patch> patches;  // patch maps of a generated mesh (empty
+                                    // for a described one)
 };
 
 // face-table code bit: the neighbour has the other point type (DG / FV), its
@@ -38,6 +52,10 @@ inline int face_node(int n, int f, int a, int b) {
   if (d == 1) return a + n * (p + n * b);
   return a + n * (b + n * p);
 }
+// coordinates [3][np] and dX^a/dx^i [9][np] of element e on LGL points
+// (uniform = false) or equally spaced points; false if the element's patch
+// map is not known (a described curvilinear element)
+bool element_geometry(const nmg_mesh &m, int64_t e, bool uniform, double *xyz, double *dXdx);
 // apply a dihedral orientation code to an in-plane index pair
 inline void orient_map(int n, int o, int a, int b, int *a2, int *b2) {
   int s = o & 1, fa = (o >> 1) & 1, fb = (o >> 2) & 1;

@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -136,6 +137,21 @@ struct nmg_ctx {
   int *d_fvlist = nullptr, *d_gtab = nullptr;
   unsigned char *d_isfv = nullptr;
   double *d_ghost = nullptr, *d_gM = nullptr;
+  double *d_fvbxyz = nullptr, *d_fvbnrm = nullptr;  // outer faces on equally spaced points
+  int ghost_cap = 0;
+  // switchable contexts: element types can change (nmg_set_element_types)
+  bool switchable = false;
+  std::vector<int32_t> h_nb, h_code0, h_bslot0, h_fv;  // face table without the mixed bit,
+                                                       // outer-face slots, current types
+  double *d_PR = nullptr;      // [3][n][n] LGL -> uniform (P), uniform -> LGL (R), and
+                               // the modal analysis matrix of the LGL points (A)
+  std::vector<int32_t> h_score;  // trouble score of each element
+  int *d_conv = nullptr;       // [E] element list of a conversion
+  double *d_mm = nullptr;      // [E][5][2] min/max of u_p per element and field
+  int *d_trb = nullptr;        // [E] trouble flag of the last check
+  int *d_score = nullptr;      // [E] trouble score (node->dat->info->trbl_score)
+  double *d_up = nullptr;      // u_p: state at the start of a checked step
+  double *d_pers = nullptr;    // [E][5] Persson indicators of the last check
   int fv_rec = NMG_FV_REC_WENOM3_2, fv_extrap = NMG_FV_EXTRAP_DNFN1;
   double fv_w3ratio = 2.;
   double *d_fvgeo = nullptr, *d_fvdist = nullptr, *d_fvdxb = nullptr;
@@ -262,6 +278,8 @@ static StageParams base_params(nmg_ctx *c) {
   P.fvdist = c->d_fvdist;
   P.fvdxb = c->d_fvdxb;
   P.ghost = c->d_ghost;
+  P.fvbxyz = c->d_fvbxyz;
+  P.fvbnrm = c->d_fvbnrm;
   P.bc = c->bc;
   P.k0 = c->k[0];
   P.k1 = c->k[1];
@@ -314,7 +332,7 @@ static int tune_range(nmg_ctx *c, int v0, int v1, bool fvpart, int *best_out) {
 }
 
 static int autotune(nmg_ctx *c) {
-  if (c->tuned && (!c->mixed || c->ftuned)) return NMG_OK;
+  if (c->tuned && (!c->mixed || c->ftuned || (c->nfvel == 0 && c->fsel >= 0))) return NMG_OK;
   const char *force = getenv("NMG_KERNEL");  // e.g. "eo", "gather", "eo:1:128"
   const int ndg = c->mixed ? c->ndg : c->nvariants;
   if (force && *force) {
@@ -338,9 +356,13 @@ static int autotune(nmg_ctx *c) {
     c->tuned = true;
   }
   if (c->mixed && !c->ftuned) {
-    int rc = tune_range(c, c->ndg, c->nvariants, true, &c->fsel);
-    if (rc) return rc;
-    c->ftuned = true;
+    if (c->nfvel == 0) {  // nothing to time yet (a switchable context without FV elements)
+      if (c->fsel < 0) c->fsel = c->ndg;
+    } else {
+      int rc = tune_range(c, c->ndg, c->nvariants, true, &c->fsel);
+      if (rc) return rc;
+      c->ftuned = true;
+    }
   }
   return NMG_OK;
 }
@@ -390,8 +412,8 @@ static int enqueue_step(nmg_ctx *c, int cur, double t, double dt, bool devtime) 
 // per node 1/J = det(dXb/dx) (coordinates.c:174-223, utilities.c:199-211),
 // sqrtgdiag (coordinates.c:728-800) and the unit normals of the faces 2d+1
 // (utilities.c:48-88), in the reference's operation order.
-static void fv_pack_element(const nmg_mesh &m, int64_t e, int cs, std::vector<double> *geo,
-                            std::vector<double> *dist) {
+static void fv_pack_element(const nmg_mesh &m, int64_t e, int cs, const double *X9,
+                            std::vector<double> *geo, std::vector<double> *dist) {
   const int n = m.n, np = n * n * n;
   const double *bb = &m.bbox[e * 6];
   for (int f = 0; f < 6; f++) {
@@ -401,7 +423,6 @@ static void fv_pack_element(const nmg_mesh &m, int64_t e, int cs, std::vector<do
     (*dist)[e * 6 + f] = std::fabs(Xbm - Xbf);
   }
   if (cs < 0) return;
-  const double *X9 = &m.dXdx[(size_t)e * 9 * np];
   double *G = &(*geo)[(size_t)cs * 13 * np];
   const double d0 = 2. / (bb[1] - bb[0]), d1 = 2. / (bb[3] - bb[2]), d2 = 2. / (bb[5] - bb[4]);
   const double dXbdX[3] = {d0, d1, d2};
@@ -434,7 +455,54 @@ static void drop_graphs(nmg_ctx *c) {
 
 extern "C" {
 
-int nmg_create(const nmg_mesh *m, int32_t bc_kind, const double k[3], nmg_ctx **out) {
+// Type-dependent tables of a context with finite-volume elements: element
+// flags and list, face codes with the mixed bit, interface-trace slots.
+// Rebuilt and uploaded whenever element types change.
+static int upload_type_tables(nmg_ctx *c) {
+  const int64_t E = c->nelem;
+  const int nn = c->nn;
+  std::vector<unsigned char> isfv(E, 0);
+  std::vector<int> fvlist, gtab;
+  std::vector<int32_t> code(c->h_code0), bslot(c->h_bslot0);
+  for (int64_t e = 0; e < E; e++) {
+    if (c->h_fv[e]) {
+      isfv[e] = 1;
+      fvlist.push_back((int)e);
+    }
+    for (int f = 0; f < 6; f++) {
+      const int nbe = c->h_nb[e * 6 + f];
+      if (nbe >= 0 && (c->h_fv[e] != 0) != (c->h_fv[nbe] != 0)) {
+        code[e * 6 + f] |= NMG_CODE_MIXED;
+        bslot[e * 6 + f] = (int)(gtab.size() / 4);
+        gtab.insert(gtab.end(), {(int)e, f, nbe, code[e * 6 + f]});
+      }
+    }
+  }
+  c->nfvel = (int)fvlist.size();
+  c->nghost = (int)(gtab.size() / 4);
+  if (c->nghost > c->ghost_cap) {
+    cudaFree(c->d_ghost);
+    c->d_ghost = nullptr;
+    CK(cudaMalloc((void **)&c->d_ghost, sizeof(double) * 4 * nn * c->nghost));
+    CK(cudaMemset(c->d_ghost, 0, sizeof(double) * 4 * nn * c->nghost));
+    c->ghost_cap = c->nghost;
+  }
+  CK(cudaMemcpy(c->d_code, code.data(), sizeof(int32_t) * E * 6, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(c->d_bslot, bslot.data(), sizeof(int32_t) * E * 6, cudaMemcpyHostToDevice));
+  if (c->mixed) {
+    CK(cudaMemcpy(c->d_isfv, isfv.data(), E, cudaMemcpyHostToDevice));
+    if (!fvlist.empty())
+      CK(cudaMemcpy(c->d_fvlist, fvlist.data(), sizeof(int) * fvlist.size(),
+                    cudaMemcpyHostToDevice));
+    if (!gtab.empty())
+      CK(cudaMemcpy(c->d_gtab, gtab.data(), sizeof(int) * gtab.size(), cudaMemcpyHostToDevice));
+  }
+  drop_graphs(c);
+  return NMG_OK;
+}
+
+static int create_impl(const nmg_mesh *m, int32_t bc_kind, const double k[3], bool switchable,
+                       nmg_ctx **out) {
   if (!out) return NMG_EINVAL;
   *out = nullptr;
   nmg_ctx *c = new (std::nothrow) nmg_ctx;
@@ -445,8 +513,9 @@ int nmg_create(const nmg_mesh *m, int32_t bc_kind, const double k[3], nmg_ctx **
     return set_err(c, NMG_EINVAL, "nmg_create: unknown bc kind");
   int64_t nfv = 0;
   for (size_t e = 0; e < m->fv.size(); e++) nfv += m->fv[e] ? 1 : 0;
-  c->fv = nfv > 0;
-  c->mixed = nfv > 0 && nfv < m->nelem;
+  c->switchable = switchable;
+  c->fv = nfv > 0 || switchable;
+  c->mixed = (nfv > 0 && nfv < m->nelem) || switchable;
   if (c->mixed) {
     c->ndg = nmgk::eo_variants(m->n, c->variants, kMaxVariants);
     c->ndg += nmgk::gather_variants(m->n, c->variants + c->ndg, kMaxVariants - c->ndg);
@@ -475,35 +544,35 @@ int nmg_create(const nmg_mesh *m, int32_t bc_kind, const double k[3], nmg_ctx **
   if (k) for (int d = 0; d < 3; d++) c->k[d] = k[d];
   c->state_len = (size_t)E * NF * np;
 
+  // element types and the type-independent face table
+  c->h_fv.assign(E, 0);
+  for (int64_t e = 0; e < E && !m->fv.empty(); e++) c->h_fv[e] = m->fv[e] ? 1 : 0;
+  c->h_nb.assign(m->nb.begin(), m->nb.end());
+  c->h_code0.resize(E * 6);
+  for (int64_t q = 0; q < E * 6; q++) c->h_code0[q] = m->code[q] & ~NMG_CODE_MIXED;
+
   // host-side packing of per-element data
-  std::vector<int> cslot(E, -1), bslot(E * 6, -1);
+  std::vector<int> cslot(E, -1);
+  c->h_bslot0.assign(E * 6, -1);
   std::vector<double> scale(E * 3, 0.), gcart(E * 3, 0.);
   int64_t C = 0, B = 0;
-  std::vector<int> gtab, fvlist;
-  std::vector<unsigned char> isfv(E, 0);
   for (int64_t e = 0; e < E; e++) {
     if (m->curvi[e]) cslot[e] = (int)C++;
     for (int f = 0; f < 6; f++)
-      if (m->nb[e * 6 + f] < 0) bslot[e * 6 + f] = (int)B++;
-    if (c->fv && m->fv[e]) {
-      isfv[e] = 1;
-      fvlist.push_back((int)e);
-    }
-    // faces to a neighbour of the other point type: slots of interpolated traces
-    for (int f = 0; f < 6; f++)
-      if (m->nb[e * 6 + f] >= 0 && (m->code[e * 6 + f] & NMG_CODE_MIXED)) {
-        bslot[e * 6 + f] = (int)(gtab.size() / 4);
-        gtab.insert(gtab.end(), {(int)e, f, m->nb[e * 6 + f], m->code[e * 6 + f]});
-      }
+      if (m->nb[e * 6 + f] < 0) c->h_bslot0[e * 6 + f] = (int)B++;
     for (int d = 0; d < 3; d++)
       scale[e * 3 + d] = 2. / (m->bbox[e * 6 + 2 * d + 1] - m->bbox[e * 6 + 2 * d]);
     for (int d = 0; d < 3; d++) gcart[e * 3 + d] = 0.5 * scale[e * 3 + d] / m->w[0];
   }
   c->ncurvi = C;
   c->nbface = B;
-  std::vector<double> metric, metricp, fac, bxyz, bnrm, fvgeo, fvdist, fvdxb;
+  // which geometries are needed: DG (LGL points) for DG elements, FV
+  // (equally spaced points) for FV elements, both for every element of a
+  // switchable context
+  const bool anydg = nfv < E || switchable;
+  std::vector<double> metric, metricp, fac, bxyz, bnrm, fvbxyz, fvbnrm, fvgeo, fvdist, fvdxb;
   std::vector<int> cmask((size_t)std::max<int64_t>(C, 1), 0);
-  const int64_t Cdg = (c->fv && !c->mixed) ? 0 : C;  // DG metric arrays, FV geometry
+  const int64_t Cdg = anydg ? C : 0;
   const int64_t Cfv = c->fv ? C : 0;
   try {
     metric.assign((size_t)std::max<int64_t>(Cdg, 1) * 9 * np, 0.);
@@ -514,77 +583,95 @@ int nmg_create(const nmg_mesh *m, int32_t bc_kind, const double k[3], nmg_ctx **
     fvdxb.assign((size_t)n, 0.);
     bxyz.assign((size_t)std::max<int64_t>(B, 1) * 3 * nn, 0.);
     bnrm.assign((size_t)std::max<int64_t>(B, 1) * 3 * nn, 0.);
+    fvbxyz.assign((size_t)(c->fv ? std::max<int64_t>(B, 1) : 1) * 3 * nn, 0.);
+    fvbnrm.assign((size_t)(c->fv ? std::max<int64_t>(B, 1) : 1) * 3 * nn, 0.);
   } catch (const std::bad_alloc &) {
     return set_err(c, NMG_ENOMEM, "nmg_create: host out of memory");
   }
+  std::vector<double> gx(3 * np), gX(9 * np);  // geometry of the other point type
   for (int64_t e = 0; e < E; e++) {
-    const double *X9 = &m->dXdx[(size_t)e * 9 * np];
     const double *sc = &scale[e * 3];
     const int cs = cslot[e];
-    if (c->fv) fv_pack_element(*m, e, cs, &fvgeo, &fvdist);
-    if (cs >= 0 && Cdg > 0) {
-      double *Mt = &metric[(size_t)cs * 9 * np];
-      double *Mp = &metricp[(size_t)cs * 9 * np];
-      int mask = 0;
-      for (int a = 0; a < 3; a++)
-        for (int i = 0; i < 3; i++) {
-          for (int q = 0; q < np; q++) {
-            const double v = sc[a] * X9[(a * 3 + i) * np + q];
-            Mt[(a * 3 + i) * np + q] = v;
-            if (v != 0.) mask |= 1 << (a * 3 + i);
-          }
-          // pass-major: [a][i][position q along the a-line][line L]
-          for (int L = 0; L < nn; L++) {
-            const int l0 = L % n, l1 = L / n;
-            for (int q = 0; q < n; q++) {
-              const int node = a == 0 ? q + n * (l0 + n * l1)
-                             : a == 1 ? l0 + n * (q + n * l1)
-                                      : l0 + n * (l1 + n * q);
-              Mp[(a * 3 + i) * np + q * nn + L] = sc[a] * X9[(a * 3 + i) * np + node];
+    const bool efv = c->h_fv[e] != 0;
+    for (int pass = 0; pass < 2; pass++) {
+      const bool uni = pass == 1;   // pass 0: DG geometry, pass 1: FV geometry
+      if (uni ? !(efv || switchable) : !(!efv || switchable)) continue;
+      const double *X3 = &m->xyz[(size_t)e * 3 * np];
+      const double *X9 = &m->dXdx[(size_t)e * 9 * np];
+      if (uni != efv) {
+        if (!nmg::element_geometry(*m, e, uni, gx.data(), gX.data()))
+          return set_err(c, NMG_EUNSUP,
+                         "nmg_create: switchable context needs the patch map of every "
+                         "curvilinear element (a generated mesh)");
+        X3 = gx.data();
+        X9 = gX.data();
+      }
+      if (uni) {
+        fv_pack_element(*m, e, cs, X9, &fvgeo, &fvdist);
+      } else if (cs >= 0) {
+        double *Mt = &metric[(size_t)cs * 9 * np];
+        double *Mp = &metricp[(size_t)cs * 9 * np];
+        int mask = 0;
+        for (int a = 0; a < 3; a++)
+          for (int i = 0; i < 3; i++) {
+            for (int q = 0; q < np; q++) {
+              const double v = sc[a] * X9[(a * 3 + i) * np + q];
+              Mt[(a * 3 + i) * np + q] = v;
+              if (v != 0.) mask |= 1 << (a * 3 + i);
+            }
+            // pass-major: [a][i][position q along the a-line][line L]
+            for (int L = 0; L < nn; L++) {
+              const int l0 = L % n, l1 = L / n;
+              for (int q = 0; q < n; q++) {
+                const int node = a == 0 ? q + n * (l0 + n * l1)
+                               : a == 1 ? l0 + n * (q + n * l1)
+                                        : l0 + n * (l1 + n * q);
+                Mp[(a * 3 + i) * np + q * nn + L] = sc[a] * X9[(a * 3 + i) * np + node];
+              }
             }
           }
+        cmask[cs] = mask;
+        for (int f = 0; f < 6; f++) {
+          const int d = f >> 1, p = (f & 1) * (n - 1);
+          const double sig = (f & 1) ? 1. : -1.;
+          for (int b = 0; b < n; b++)
+            for (int a = 0; a < n; a++) {
+              const int node = nmg::face_node(n, f, a, b);
+              const double v0 = X9[(d * 3 + 0) * np + node], v1 = X9[(d * 3 + 1) * np + node],
+                           v2 = X9[(d * 3 + 2) * np + node];
+              const double mag = sqrt(v0 * v0 + v1 * v1 + v2 * v2);
+              const double g = 0.5 * sc[d] * mag / m->w[p];  // sqrtgdiag / (2 w_end)
+              double *F4 = &fac[(((size_t)cs * 6 + f) * nn + a + n * b) * 4];
+              F4[0] = g * sig * v0 / mag;
+              F4[1] = g * sig * v1 / mag;
+              F4[2] = g * sig * v2 / mag;
+              F4[3] = g;
+            }
         }
-      cmask[cs] = mask;
+      }
+      // outer faces: coordinates and unit normals on this point type
+      std::vector<double> &BX = uni ? fvbxyz : bxyz, &BN = uni ? fvbnrm : bnrm;
       for (int f = 0; f < 6; f++) {
-        const int d = f >> 1, p = (f & 1) * (n - 1);
+        const int bs = c->h_bslot0[e * 6 + f];
+        if (bs < 0) continue;
+        const int d = f >> 1;
         const double sig = (f & 1) ? 1. : -1.;
         for (int b = 0; b < n; b++)
           for (int a = 0; a < n; a++) {
-            const int node = nmg::face_node(n, f, a, b);
+            const int node = nmg::face_node(n, f, a, b), ab = a + n * b;
+            for (int q = 0; q < 3; q++) BX[((size_t)bs * 3 + q) * nn + ab] = X3[q * np + node];
             const double v0 = X9[(d * 3 + 0) * np + node], v1 = X9[(d * 3 + 1) * np + node],
                          v2 = X9[(d * 3 + 2) * np + node];
             const double mag = sqrt(v0 * v0 + v1 * v1 + v2 * v2);
-            const double g = 0.5 * sc[d] * mag / m->w[p];  // sqrtgdiag / (2 w_end)
-            double *F4 = &fac[(((size_t)cs * 6 + f) * nn + a + n * b) * 4];
-            F4[0] = g * sig * v0 / mag;
-            F4[1] = g * sig * v1 / mag;
-            F4[2] = g * sig * v2 / mag;
-            F4[3] = g;
+            BN[((size_t)bs * 3 + 0) * nn + ab] = sig * v0 / mag;
+            BN[((size_t)bs * 3 + 1) * nn + ab] = sig * v1 / mag;
+            BN[((size_t)bs * 3 + 2) * nn + ab] = sig * v2 / mag;
           }
       }
     }
-    for (int f = 0; f < 6; f++) {
-      // outer faces only (bslot of a face with a neighbour is an
-      // interface-trace slot)
-      const int bs = bslot[e * 6 + f];
-      if (bs < 0 || m->nb[e * 6 + f] >= 0) continue;
-      const int d = f >> 1;
-      const double sig = (f & 1) ? 1. : -1.;
-      for (int b = 0; b < n; b++)
-        for (int a = 0; a < n; a++) {
-          const int node = nmg::face_node(n, f, a, b), ab = a + n * b;
-          for (int q = 0; q < 3; q++)
-            bxyz[((size_t)bs * 3 + q) * nn + ab] = m->xyz[((size_t)e * 3 + q) * np + node];
-          const double v0 = X9[(d * 3 + 0) * np + node], v1 = X9[(d * 3 + 1) * np + node],
-                       v2 = X9[(d * 3 + 2) * np + node];
-          const double mag = sqrt(v0 * v0 + v1 * v1 + v2 * v2);
-          bnrm[((size_t)bs * 3 + 0) * nn + ab] = sig * v0 / mag;
-          bnrm[((size_t)bs * 3 + 1) * nn + ab] = sig * v1 / mag;
-          bnrm[((size_t)bs * 3 + 2) * nn + ab] = sig * v2 / mag;
-        }
-    }
   }
-  std::vector<double> gM(2 * (size_t)nn, 0.);
+  // 1D transfer matrices between the two point sets
+  std::vector<double> gM(2 * (size_t)nn, 0.), PR(3 * (size_t)nn, 0.);
   if (c->mixed) {
     // M[0][p][j]: Lagrange weight of LGL point j at the equally spaced point
     // p (Lagrange_of_x with the weights of Lagrange_winterp); M[1][p][j]:
@@ -624,9 +711,66 @@ int nmg_create(const nmg_mesh *m, int32_t bc_kind, const double k[3], nmg_ctx **
         gM[p * n + j] = prod * wl[j];
         gM[nn + p * n + j] = pwlin(j, xl[p]);
       }
+    // element switches: P = the same Lagrange matrix (LGL -> equally spaced,
+    // gridpoints.c:158-178) and R = P^{-1} (uniform -> LGL; the reference's
+    // default PseudoInv (P^T P)^{-1} P^T is the inverse of the square P),
+    // inverted by Gauss-Jordan elimination with partial pivoting
+    std::vector<long double> A(nn), I(nn, 0.L);
+    for (int q = 0; q < nn; q++) A[q] = gM[q];
+    for (int i = 0; i < n; i++) I[i * n + i] = 1.L;
+    for (int col = 0; col < n; col++) {
+      int piv = col;
+      for (int r = col + 1; r < n; r++)
+        if (fabsl(A[r * n + col]) > fabsl(A[piv * n + col])) piv = r;
+      for (int q = 0; q < n; q++) {
+        std::swap(A[col * n + q], A[piv * n + q]);
+        std::swap(I[col * n + q], I[piv * n + q]);
+      }
+      const long double d = A[col * n + col];
+      for (int q = 0; q < n; q++) {
+        A[col * n + q] /= d;
+        I[col * n + q] /= d;
+      }
+      for (int r = 0; r < n; r++)
+        if (r != col) {
+          const long double fct = A[r * n + col];
+          for (int q = 0; q < n; q++) {
+            A[r * n + q] -= fct * A[col * n + q];
+            I[r * n + q] -= fct * I[col * n + q];
+          }
+        }
+    }
+    for (int q = 0; q < nn; q++) {
+      PR[q] = gM[q];
+      PR[nn + q] = (double)I[q];
+    }
+    // modal analysis matrix of the LGL points with normalised Legendre
+    // polynomials (LGL_AT_ST_matrices, src/main/basis/Legendre.c:14-38,277-310):
+    // A[i][j] = w_j P_i(x_j) / sqrt(c_i), 1/c_i = (2i+1)/2 (i/2 for i = N)
+    const int N = n - 1;
+    for (int i = 0; i < n; i++) {
+      double ooci = 0.5 * (2 * i + 1);
+      if (i == N && N != 0) ooci = 0.5 * i;
+      const double oosci = sqrt(ooci);
+      for (int j = 0; j < n; j++) {
+        const double x = xl[j];
+        double Pk = 0., P0 = 1., P1 = x, Pi;
+        if (i == 0) {
+          Pi = P0;
+        } else if (i == 1) {
+          Pi = P1;
+        } else {
+          for (int kk = 2; kk <= i; kk++) {
+            Pk = (x * (2 * kk - 1) * P1 - (kk - 1) * P0) / kk;
+            P0 = P1;
+            P1 = Pk;
+          }
+          Pi = Pk;
+        }
+        PR[2 * nn + i * n + j] = m->w[j] * (Pi * oosci);
+      }
+    }
   }
-  c->nfvel = (int)fvlist.size();
-  c->nghost = (int)(gtab.size() / 4);
   if (c->fv) {
     // midpoint spacings of the uniform points (set_nm_nodemidpoint_distsXb_dir)
     std::vector<double> Xb(n), Xbm(std::max(n - 1, 1));
@@ -634,18 +778,17 @@ int nmg_create(const nmg_mesh *m, int32_t bc_kind, const double k[3], nmg_ctx **
     for (int i = 0; i < n - 1; i++) Xbm[i] = 0.5 * (Xb[i] + Xb[i + 1]);
     for (int i = 1; i < n - 1; i++) fvdxb[i] = Xbm[i] - Xbm[i - 1];
   }
-  std::vector<int> code(m->code.begin(), m->code.end());
   CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
   auto up = [&](auto **dst, const auto &vec) -> cudaError_t {
     size_t bytes = vec.size() * sizeof(vec[0]);
-    cudaError_t e2 = cudaMalloc((void **)dst, bytes);
-    if (e2 != cudaSuccess) return e2;
+    cudaError_t e2 = cudaMalloc((void **)dst, std::max<size_t>(bytes, 16));
+    if (e2 != cudaSuccess || bytes == 0) return e2;
     return cudaMemcpy(*dst, vec.data(), bytes, cudaMemcpyHostToDevice);
   };
   CK(up(&c->d_nb, m->nb));
-  CK(up(&c->d_code, code));
+  CK(up(&c->d_code, c->h_code0));
   CK(up(&c->d_cslot, cslot));
-  CK(up(&c->d_bslot, bslot));
+  CK(up(&c->d_bslot, c->h_bslot0));
   CK(up(&c->d_cmask, cmask));
   CK(up(&c->d_scale, scale));
   CK(up(&c->d_gcart, gcart));
@@ -659,15 +802,20 @@ int nmg_create(const nmg_mesh *m, int32_t bc_kind, const double k[3], nmg_ctx **
     CK(up(&c->d_fvgeo, fvgeo));
     CK(up(&c->d_fvdist, fvdist));
     CK(up(&c->d_fvdxb, fvdxb));
+    CK(up(&c->d_fvbxyz, fvbxyz));
+    CK(up(&c->d_fvbnrm, fvbnrm));
   }
-  if (!c->fv || c->mixed) CK(nmgk::eo_upload(n, m->D.data()));
+  if (anydg) CK(nmgk::eo_upload(n, m->D.data()));
   if (c->mixed) {
-    CK(up(&c->d_isfv, isfv));
-    CK(up(&c->d_fvlist, fvlist));
-    CK(up(&c->d_gtab, gtab));
+    CK(cudaMalloc((void **)&c->d_isfv, E));
+    CK(cudaMalloc((void **)&c->d_fvlist, sizeof(int) * E));
+    CK(cudaMalloc((void **)&c->d_gtab, sizeof(int) * E * 6 * 4));
     CK(up(&c->d_gM, gM));
-    CK(cudaMalloc((void **)&c->d_ghost, sizeof(double) * 4 * nn * std::max(c->nghost, 1)));
-    CK(cudaMemset(c->d_ghost, 0, sizeof(double) * 4 * nn * std::max(c->nghost, 1)));
+    CK(up(&c->d_PR, PR));
+  }
+  if (c->fv) {
+    int rc = upload_type_tables(c);
+    if (rc) return rc;
   }
   for (int b = 0; b < 4; b++) {
     CK(cudaMalloc((void **)&c->d_buf[b], c->state_len * sizeof(double)));
@@ -696,6 +844,159 @@ int nmg_create(const nmg_mesh *m, int32_t bc_kind, const double k[3], nmg_ctx **
   return NMG_OK;
 }
 
+int nmg_create(const nmg_mesh *m, int32_t bc_kind, const double k[3], nmg_ctx **out) {
+  return create_impl(m, bc_kind, k, false, out);
+}
+
+int nmg_create_switchable(const nmg_mesh *m, int32_t bc_kind, const double k[3], nmg_ctx **out) {
+  return create_impl(m, bc_kind, k, true, out);
+}
+
+// ---------------------------------------------------------------------------
+// element switches between DG and finite volume, trouble indicators
+// ---------------------------------------------------------------------------
+// switch element types to fv[], converting the resident state of every
+// element whose type changes (LGL -> uniform with P, uniform -> LGL with R)
+static int switch_types(nmg_ctx *c, const int32_t *fv, int *nto_fv, int *nto_dg) {
+  const int64_t E = c->nelem;
+  std::vector<int> lst;
+  int a = 0, b = 0;
+  for (int64_t e = 0; e < E; e++)
+    if (fv[e] && !c->h_fv[e]) { lst.push_back((int)e); a++; }
+  for (int64_t e = 0; e < E; e++)
+    if (!fv[e] && c->h_fv[e]) { lst.push_back((int)e); b++; }
+  if (nto_fv) *nto_fv = a;
+  if (nto_dg) *nto_dg = b;
+  if (lst.empty()) return NMG_OK;
+  if (!c->d_conv) CK(cudaMalloc((void **)&c->d_conv, sizeof(int) * E));
+  CK(cudaMemcpyAsync(c->d_conv, lst.data(), sizeof(int) * lst.size(), cudaMemcpyHostToDevice,
+                     c->stream));
+  const int nn = c->nn;
+  CK(nmgk::convert_launch(c->n, c->d_conv, a, c->d_PR, c->d_buf[c->cur], c->stream));
+  CK(nmgk::convert_launch(c->n, c->d_conv + a, b, c->d_PR + nn, c->d_buf[c->cur], c->stream));
+  c->launches += (a > 0) + (b > 0);
+  CK(cudaStreamSynchronize(c->stream));
+  for (int64_t e = 0; e < E; e++) c->h_fv[e] = fv[e] ? 1 : 0;
+  return upload_type_tables(c);
+}
+
+static int ensure_trouble_buffers(nmg_ctx *c) {
+  const int64_t E = c->nelem;
+  if (!c->d_mm) CK(cudaMalloc((void **)&c->d_mm, sizeof(double) * E * NF * 2));
+  if (!c->d_trb) CK(cudaMalloc((void **)&c->d_trb, sizeof(int) * E));
+  if (!c->d_pers) CK(cudaMalloc((void **)&c->d_pers, sizeof(double) * E * NF));
+  if (!c->d_up) CK(cudaMalloc((void **)&c->d_up, sizeof(double) * c->state_len));
+  if ((int64_t)c->h_score.size() != E) c->h_score.assign(E, 0);
+  return NMG_OK;
+}
+
+static int trouble_flags(nmg_ctx *c, const double *u, const double *u_p,
+                         const nmg_trouble_params *tp, std::vector<int32_t> *flags) {
+  CK(nmgk::trouble_launch(c->n, (int)c->nelem, u, u_p, c->d_mm, c->d_nb, c->d_isfv,
+                          c->d_PR + 2 * c->nn, tp->rdmp_deltafac, tp->rdmp_delta0,
+                          tp->rdmp_epsilon, tp->persson_max, tp->persson_uscale, c->d_trb,
+                          c->d_pers, c->stream));
+  c->launches += 2;
+  flags->resize(c->nelem);
+  CK(cudaMemcpyAsync(flags->data(), c->d_trb, sizeof(int32_t) * c->nelem,
+                     cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return NMG_OK;
+}
+
+int nmg_set_element_types(nmg_ctx *c, const int32_t *fv) {
+  if (!c || !fv) return set_err(c, NMG_EINVAL, "nmg_set_element_types: null argument");
+  if (!c->switchable)
+    return set_err(c, NMG_EUNSUP, "nmg_set_element_types: context is not switchable");
+  return switch_types(c, fv, nullptr, nullptr);
+}
+
+int nmg_get_element_types(nmg_ctx *c, int32_t *fv) {
+  if (!c || !fv) return set_err(c, NMG_EINVAL, "nmg_get_element_types: null argument");
+  for (int64_t e = 0; e < c->nelem; e++) fv[e] = c->h_fv.empty() ? 0 : c->h_fv[e];
+  return NMG_OK;
+}
+
+int nmg_trouble_check(nmg_ctx *c, const double *u_dev, const double *u_p_dev,
+                      const nmg_trouble_params *tp, int32_t *flags, double *persson) {
+  if (!c || !u_dev || !u_p_dev || !tp || !flags)
+    return set_err(c, NMG_EINVAL, "nmg_trouble_check: null argument");
+  if (!c->switchable)
+    return set_err(c, NMG_EUNSUP, "nmg_trouble_check: context is not switchable");
+  int rc = ensure_trouble_buffers(c);
+  if (rc) return rc;
+  std::vector<int32_t> fl;
+  if ((rc = trouble_flags(c, u_dev, u_p_dev, tp, &fl))) return rc;
+  std::memcpy(flags, fl.data(), sizeof(int32_t) * c->nelem);
+  if (persson)
+    CK(cudaMemcpy(persson, c->d_pers, sizeof(double) * c->nelem * NF, cudaMemcpyDeviceToHost));
+  return NMG_OK;
+}
+
+int nmg_get_trouble_scores(nmg_ctx *c, int32_t *scores) {
+  if (!c || !scores) return set_err(c, NMG_EINVAL, "nmg_get_trouble_scores: null argument");
+  for (int64_t e = 0; e < c->nelem; e++)
+    scores[e] = (int64_t)c->h_score.size() == c->nelem ? c->h_score[e] : 0;
+  return NMG_OK;
+}
+
+// One RK4 step with trouble detection, as evolve_mesh does with
+// evolve_redo_troubled = step (src/main/evolve/evolve.c:74-140): step,
+// score every element (evolve_set_trouble_score, trouble.c:27-110), and if
+// the global score is positive go back to u_p, switch the troubled DG
+// elements to finite volume (trouble.c:187-260) and redo the step; finally
+// switch finite-volume elements whose score reached -notroubles back to DG
+// (trouble.c:288-373).
+int nmg_rk4_step_trouble(nmg_ctx *c, double t, double dt, const nmg_trouble_params *tp,
+                         int32_t *switched) {
+  if (!c || !tp) return set_err(c, NMG_EINVAL, "nmg_rk4_step_trouble: null argument");
+  if (!c->switchable)
+    return set_err(c, NMG_EUNSUP, "nmg_rk4_step_trouble: context is not switchable");
+  int rc = ensure_trouble_buffers(c);
+  if (rc) return rc;
+  const int64_t E = c->nelem;
+  const size_t bytes = c->state_len * sizeof(double);
+  CK(cudaMemcpyAsync(c->d_up, c->d_buf[c->cur], bytes, cudaMemcpyDeviceToDevice, c->stream));
+  if ((rc = nmg_rk4_step(c, t, dt))) return rc;
+  std::vector<int32_t> fl;
+  if ((rc = trouble_flags(c, c->d_buf[c->cur], c->d_up, tp, &fl))) return rc;
+  const int maxt = 1073741824;
+  int smax = INT32_MIN, smin = INT32_MAX;
+  for (int64_t e = 0; e < E; e++) {
+    int32_t &sc = c->h_score[e];
+    if (fl[e] > 0) sc = sc <= 0 ? 1 : sc + 1;
+    else if (fl[e] == 0) sc = 0;
+    else sc = sc >= 0 ? -1 : sc - 1;
+    if (sc < -maxt) sc = -maxt;
+    if (sc > maxt) sc = maxt;
+    smax = std::max(smax, sc);
+    smin = std::min(smin, sc);
+  }
+  const int global = smax > 0 ? smax : smin;
+  int nfv = 0, ndg = 0;
+  if (global > 0) {
+    // go back to u_p, switch the troubled elements, redo the step
+    CK(cudaMemcpyAsync(c->d_buf[c->cur], c->d_up, bytes, cudaMemcpyDeviceToDevice, c->stream));
+    std::vector<int32_t> types(c->h_fv);
+    for (int64_t e = 0; e < E; e++)
+      if (c->h_score[e] > 0) types[e] = 1;
+    if ((rc = switch_types(c, types.data(), &nfv, nullptr))) return rc;
+    if ((rc = nmg_rk4_step(c, t, dt))) return rc;
+  }
+  if (global > 0 || global <= -tp->notroubles) {
+    std::vector<int32_t> types(c->h_fv);
+    for (int64_t e = 0; e < E; e++)
+      if (c->h_fv[e] && c->h_score[e] <= -tp->notroubles) types[e] = 0;
+    if ((rc = switch_types(c, types.data(), nullptr, &ndg))) return rc;
+  }
+  if (switched) {
+    switched[0] = nfv;
+    switched[1] = ndg;
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  return NMG_OK;
+}
+
 int nmg_set_fv(nmg_ctx *c, int32_t rec, int32_t extrap, double w3ratio) {
   if (!c) return NMG_EINVAL;
   if (!c->fv) return set_err(c, NMG_EUNSUP, "nmg_set_fv: the mesh has no finite-volume elements");
@@ -720,7 +1021,9 @@ void nmg_destroy(nmg_ctx *c) {
   cudaFree(c->d_D);
   cudaFree(c->d_fvgeo); cudaFree(c->d_fvdist); cudaFree(c->d_fvdxb);
   cudaFree(c->d_fvlist); cudaFree(c->d_gtab); cudaFree(c->d_isfv); cudaFree(c->d_ghost);
-  cudaFree(c->d_gM);
+  cudaFree(c->d_gM); cudaFree(c->d_fvbxyz); cudaFree(c->d_fvbnrm); cudaFree(c->d_PR);
+  cudaFree(c->d_conv); cudaFree(c->d_mm); cudaFree(c->d_trb); cudaFree(c->d_score);
+  cudaFree(c->d_up); cudaFree(c->d_pers);
   for (int b = 0; b < 4; b++) cudaFree(c->d_buf[b]);
   cudaFree(c->d_times); cudaFree(c->d_step);
   if (c->stream) cudaStreamDestroy(c->stream);

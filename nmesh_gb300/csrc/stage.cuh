@@ -68,6 +68,8 @@ struct StageParams {
   int nfvel;
   const double *ghost;  // [G][4][nn] interpolated traces of faces with code & 64;
                         // slot G = bslot[e*6+f]
+  const double *fvbxyz; // [B][3][nn] outer-face coordinates on equally spaced points
+  const double *fvbnrm; // [B][3][nn] outer-face unit normals there
 };
 
 constexpr int kCodeMixed = 64;  // face-table bit: neighbour of the other point type
@@ -346,5 +348,15 @@ int fv_variants(int n, Variant *out, int cap);
 // equally spaced points at the LGL positions)
 cudaError_t ghost_launch(int nghost, int n, const int *gtab, const unsigned char *isfv,
                          const double *M, const double *win, double *ghost, cudaStream_t st);
+// u of the listed elements <- (M x M x M) u (all fields), in place
+cudaError_t convert_launch(int n, const int *list, int count, const double *M, double *u,
+                           cudaStream_t st);
+// per-element min/max of u_p, then the trouble flag of every element (RDMP
+// on all elements, Persson's indicator with the modal analysis matrix A on
+// DG elements); pers[E][5] receives the indicators (may be null)
+cudaError_t trouble_launch(int n, int nelem, const double *u, const double *u_p, double *mm,
+                           const int *nb, const unsigned char *isfv, const double *A,
+                           double deltafac, double delta0, double epsilon, double persson_max,
+                           double uscale, int *flag, double *pers, cudaStream_t st);
 
 }  // namespace nmgk

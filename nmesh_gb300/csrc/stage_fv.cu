@@ -230,7 +230,7 @@ __device__ void face_fnum(const StageParams &P, int e, int f, int a, int b, cons
   } else {
     const int bs = __ldg(P.bslot + e * 6 + f), ab = a + n * b;
     if (P.bc == NMG_BC_EXACT_PLANEWAVE) {
-      const double *X = P.bxyz + (size_t)bs * 3 * nn + ab;
+      const double *X = P.fvbxyz + (size_t)bs * 3 * nn + ab;
       const double arg = P.k0 * X[0] + P.k1 * X[nn] + P.k2 * X[2 * nn] - P.om * t;
       double sn, cn;
       sincos(arg, &sn, &cn);
@@ -492,6 +492,179 @@ __global__ void __launch_bounds__(256) ghost_kernel(int nghost, int n, const int
   }
 }
 }  // namespace
+
+// ---------------------------------------------------------------------------
+// element switches and trouble indicators
+// ---------------------------------------------------------------------------
+namespace {
+// out = M along direction d of in (one field of one element, n^3 values)
+__device__ void apply_dir(int n, const double *M, int d, const double *in, double *out) {
+  const int np = n * n * n, st = d == 0 ? 1 : d == 1 ? n : n * n;
+  for (int q = threadIdx.x; q < np; q += blockDim.x) {
+    const int i = d == 0 ? q % n : d == 1 ? (q / n) % n : q / (n * n);
+    const double *line = in + q - i * st;
+    double s = 0.;
+    for (int j = 0; j < n; j++) s += M[i * n + j] * line[j * st];
+    out[q] = s;
+  }
+  __syncthreads();
+}
+
+// u of the listed elements <- (M x M x M) u, all five fields, in place
+__global__ void __launch_bounds__(256) convert_kernel(int n, const int *list, const double *M,
+                                                     double *u) {
+  extern __shared__ double sm[];
+  const int np = n * n * n;
+  double *a = sm, *b = sm + np, *sM = sm + 2 * np;
+  for (int q = threadIdx.x; q < n * n; q += blockDim.x) sM[q] = M[q];
+  const int e = __ldg(list + blockIdx.x);
+  for (int l = 0; l < NF; l++) {
+    double *v = u + ((size_t)e * NF + l) * np;
+    __syncthreads();
+    for (int q = threadIdx.x; q < np; q += blockDim.x) a[q] = v[q];
+    __syncthreads();
+    apply_dir(n, sM, 0, a, b);
+    apply_dir(n, sM, 1, b, a);
+    apply_dir(n, sM, 2, a, b);
+    for (int q = threadIdx.x; q < np; q += blockDim.x) v[q] = b[q];
+  }
+}
+
+// min and max of each field over each element (limdata_MRS)
+__global__ void __launch_bounds__(256) minmax_kernel(int n, int nelem, const double *u,
+                                                    double *mm) {
+  __shared__ double smin[256], smax[256];
+  const int np = n * n * n;
+  const int e = blockIdx.x;
+  if (e >= nelem) return;
+  for (int l = 0; l < NF; l++) {
+    const double *v = u + ((size_t)e * NF + l) * np;
+    double lo = v[threadIdx.x < np ? threadIdx.x : 0], hi = lo;
+    for (int q = threadIdx.x; q < np; q += blockDim.x) {
+      lo = fmin(lo, v[q]);
+      hi = fmax(hi, v[q]);
+    }
+    smin[threadIdx.x] = lo;
+    smax[threadIdx.x] = hi;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+      if (threadIdx.x < w) {
+        smin[threadIdx.x] = fmin(smin[threadIdx.x], smin[threadIdx.x + w]);
+        smax[threadIdx.x] = fmax(smax[threadIdx.x], smax[threadIdx.x + w]);
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      mm[((size_t)e * NF + l) * 2] = smin[0];
+      mm[((size_t)e * NF + l) * 2 + 1] = smax[0];
+    }
+    __syncthreads();
+  }
+}
+
+// Trouble flag of each element: the relaxed discrete maximum principle
+// (evolve_RDMP_trouble, src/main/evolve/trouble.c:438-503: u must stay
+// within [min - delta, max + delta] of u_p over the element and its face
+// neighbours, delta = deltafac max(delta0, epsilon (max - min))) and, on DG
+// elements, Persson's modal indicator (evolve_Persson_array_indicator,
+// trouble.c:505-564) above persson_max.  Flag: DG troubled 1, DG fine 0,
+// finite-volume troubled 0, finite-volume fine -1.
+__global__ void __launch_bounds__(256) trouble_kernel(int n, int nelem, const double *u,
+                                                     const double *mm, const int *nb,
+                                                     const unsigned char *isfv, const double *A,
+                                                     double deltafac, double delta0,
+                                                     double epsilon, double persson_max,
+                                                     double uscale, int *flag, double *pers) {
+  extern __shared__ double sm[];
+  const int np = n * n * n, nn = n * n;
+  double *a = sm, *b = sm + np, *sA = sm + 2 * np;
+  __shared__ double red[2][256];
+  __shared__ int bad;
+  const int e = blockIdx.x;
+  if (e >= nelem) return;
+  for (int q = threadIdx.x; q < nn; q += blockDim.x) sA[q] = A[q];
+  if (threadIdx.x == 0) bad = 0;
+  const bool efv = isfv && isfv[e];
+  __syncthreads();
+  for (int l = 0; l < NF; l++) {
+    double lo = mm[((size_t)e * NF + l) * 2], hi = mm[((size_t)e * NF + l) * 2 + 1];
+    for (int f = 0; f < 6; f++) {
+      const int e2 = __ldg(nb + e * 6 + f);
+      if (e2 < 0) continue;
+      const double lo2 = mm[((size_t)e2 * NF + l) * 2], hi2 = mm[((size_t)e2 * NF + l) * 2 + 1];
+      if (lo2 < lo) lo = lo2;
+      if (hi2 > hi) hi = hi2;
+    }
+    const double delta = deltafac * fmax(delta0, epsilon * (hi - lo));
+    const double lower = lo - delta, upper = hi + delta;
+    const double *v = u + ((size_t)e * NF + l) * np;
+    for (int q = threadIdx.x; q < np; q += blockDim.x)
+      if (v[q] < lower || v[q] > upper) bad = 1;
+    if (!efv) {  // Persson's indicator of this field
+      __syncthreads();
+      for (int q = threadIdx.x; q < np; q += blockDim.x) a[q] = v[q];
+      __syncthreads();
+      apply_dir(n, sA, 0, a, b);
+      apply_dir(n, sA, 1, b, a);
+      apply_dir(n, sA, 2, a, b);
+      if (threadIdx.x == 0 && uscale >= 0.) b[0] = uscale * 2. * sqrt(2.);
+      __syncthreads();
+      double s2 = 0., sh = 0.;
+      for (int q = threadIdx.x; q < np; q += blockDim.x) {
+        const int i = q % n, j = (q / n) % n, k = q / nn;
+        const double co = b[q];
+        s2 += co * co;
+        if ((i == n - 1 && n > 1) || (j == n - 1 && n > 1) || (k == n - 1 && n > 1)) sh += co * co;
+      }
+      red[0][threadIdx.x] = s2;
+      red[1][threadIdx.x] = sh;
+      __syncthreads();
+      for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+          red[0][threadIdx.x] += red[0][threadIdx.x + w];
+          red[1][threadIdx.x] += red[1][threadIdx.x + w];
+        }
+        __syncthreads();
+      }
+      if (threadIdx.x == 0) {
+        const double se = log10(red[1][0] / (red[0][0] + 2.2250738585072014e-308) + 1e-50);
+        if (pers) pers[(size_t)e * NF + l] = se;
+        if (se > persson_max) bad = 1;
+      }
+    } else if (threadIdx.x == 0 && pers) {
+      pers[(size_t)e * NF + l] = 0.;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) flag[e] = efv ? (bad ? 0 : -1) : (bad ? 1 : 0);
+}
+}  // namespace
+
+cudaError_t convert_launch(int n, const int *list, int count, const double *M, double *u,
+                           cudaStream_t st) {
+  if (count <= 0) return cudaSuccess;
+  const size_t smem = sizeof(double) * (2 * (size_t)n * n * n + (size_t)n * n);
+  cudaError_t e = cudaFuncSetAttribute(convert_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return e;
+  convert_kernel<<<count, 256, smem, st>>>(n, list, M, u);
+  return cudaGetLastError();
+}
+
+cudaError_t trouble_launch(int n, int nelem, const double *u, const double *u_p, double *mm,
+                           const int *nb, const unsigned char *isfv, const double *A,
+                           double deltafac, double delta0, double epsilon, double persson_max,
+                           double uscale, int *flag, double *pers, cudaStream_t st) {
+  minmax_kernel<<<nelem, 256, 0, st>>>(n, nelem, u_p, mm);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  const size_t smem = sizeof(double) * (2 * (size_t)n * n * n + (size_t)n * n);
+  e = cudaFuncSetAttribute(trouble_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  trouble_kernel<<<nelem, 256, smem, st>>>(n, nelem, u, mm, nb, isfv, A, deltafac, delta0,
+                                           epsilon, persson_max, uscale, flag, pers);
+  return cudaGetLastError();
+}
 
 cudaError_t ghost_launch(int nghost, int n, const int *gtab, const unsigned char *isfv,
                          const double *M, const double *win, double *ghost, cudaStream_t st) {

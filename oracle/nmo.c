@@ -38,6 +38,9 @@
  *   midpoint states      src/tests/scalarwave1/scalarwave1.c:761-802
  *   fin.-vol. surface    src/main/dg/dg.c:58-70,81-90 (oow = 1/|distXb|,
  *                        F = f*)
+ *   trouble indicators   src/main/evolve/trouble.c:438-564 (RDMP, Persson),
+ *                        src/main/basis/Legendre.c:14-38,277-310 (modal
+ *                        analysis matrix)
  *   DG / FV interfaces   src/main/amr/surface.c:1080-1250 (neighbour trace
  *                        interpolated onto the face points: Lagrange from a
  *                        DG neighbour, piecewise linear from a fin.-vol.
@@ -754,6 +757,138 @@ static void rhs_elem_fv(const nmo_mesh *m, const nmo_pts *P, double t,
           int ijk = i + n * (j + n * k);
           for (l = 0; l < 4; l++) re[l * np + ijk] += -1. * divf[l * np + ijk];
         }
+}
+
+/* ------------------------------------------------------------------ */
+/* trouble indicators                                                  */
+/* ------------------------------------------------------------------ */
+static double legendre_p(int l, double x)       /* basis_LegendreP */
+{
+  double Pk = 0., P0 = 1.0, P1 = x;
+  int k;
+  if (l == 0) return P0;
+  if (l == 1) return P1;
+  for (k = 2; k <= l; k++) {
+    Pk = (x * (2 * k - 1) * P1 - (k - 1) * P0) / k;
+    P0 = P1;
+    P1 = Pk;
+  }
+  return Pk;
+}
+
+/* Persson's indicator of one field on LGL points, all n^3 coefficients
+   (evolve_Persson_array_indicator with the analysis matrices of
+   LGL_AT_ST_matrices) */
+double nmo_persson(int n, const double *u, double u_scale)
+{
+  double x[64], w[64], A[64 * 64];
+  int np = n * n * n, N = n - 1, i, j, k, l, d;
+  double *c = (double *)malloc(sizeof(double) * 2 * np), *t = c + np;
+  double c2_sum = 0., c2_hi = 0., se;
+  nmo_lgl(n, x, w);
+  for (i = 0; i < n; i++) {
+    double ooci = 0.5 * (2 * i + 1), oosci;
+    if (i == N && N != 0) ooci = 0.5 * i;
+    oosci = sqrt(ooci);
+    for (j = 0; j < n; j++) A[i * n + j] = w[j] * (legendre_p(i, x[j]) * oosci);
+  }
+  memcpy(t, u, sizeof(double) * np);
+  for (d = 0; d < 3; d++) {
+    const int st = (d == 0) ? 1 : (d == 1) ? n : n * n;
+    for (k = 0; k < np; k++) {
+      const int ii = (d == 0) ? k % n : (d == 1) ? (k / n) % n : k / (n * n);
+      const double *line = t + k - ii * st;
+      double sum = 0.0;
+      for (l = 0; l < n; l++) sum += A[ii * n + l] * line[l * st];
+      c[k] = sum;
+    }
+    memcpy(t, c, sizeof(double) * np);
+  }
+  if (u_scale >= 0.) c[0] = u_scale * 2. * sqrt(2.);
+  for (k = 0; k < n; k++)
+    for (j = 0; j < n; j++)
+      for (i = 0; i < n; i++) {
+        double co = c[i + n * (j + n * k)];
+        c2_sum += co * co;
+      }
+  for (k = 0; k < n; k++)
+    for (j = 0; j < n; j++)
+      for (i = 0; i < n; i++)
+        if ((i == n - 1 && n > 1) || (j == n - 1 && n > 1) || (k == n - 1 && n > 1)) {
+          double co = c[i + n * (j + n * k)];
+          c2_hi += co * co;
+        }
+  se = log10(c2_hi / (c2_sum + 2.2250738585072014e-308) + 1e-50);
+  free(c);
+  return se;
+}
+
+/* neighbour element across face f of element e, -1 on outer faces */
+static int64_t face_neighbour(const nmo_mesh *m, int e, int f)
+{
+  int n = m->n, np = n * n * n;
+  int64_t nb = m->nbnode[((size_t)e * 6 + f) * n * n];
+  if (nb >= 0) return nb / np;
+  if (nb == -2) return m->mixface[((size_t)e * 6 + f) * 3];
+  return -1;
+}
+
+/* Trouble flags of all elements for state u against u_p: relaxed discrete
+   maximum principle over the element and its face neighbours
+   (evolve_RDMP_trouble) on every element, Persson's indicator above
+   persson_max on DG elements.  Flags: DG troubled 1, DG fine 0, FV troubled
+   0, FV fine -1.  pers[E][5] gets the indicators (0 on FV elements). */
+int nmo_trouble(const nmo_mesh *m, const double *u, const double *u_p, double deltafac,
+                double delta0, double epsilon, double persson_max, double uscale,
+                int32_t *flags, double *pers)
+{
+  int n = m->n, np = n * n * n, e;
+  double *mm = (double *)malloc(sizeof(double) * (size_t)m->nelem * NF * 2);
+  if (!mm) return 2;
+  for (e = 0; e < m->nelem; e++) {
+    int l, q;
+    for (l = 0; l < NF; l++) {
+      const double *v = u_p + ((size_t)e * NF + l) * np;
+      double lo = v[0], hi = v[0];
+      for (q = 1; q < np; q++) {
+        if (v[q] < lo) lo = v[q];
+        if (v[q] > hi) hi = v[q];
+      }
+      mm[((size_t)e * NF + l) * 2] = lo;
+      mm[((size_t)e * NF + l) * 2 + 1] = hi;
+    }
+  }
+#pragma omp parallel for schedule(static)
+  for (e = 0; e < m->nelem; e++) {
+    int l, q, f, bad = 0;
+    int efv = m->fv && m->fv[e];
+    for (l = 0; l < NF; l++) {
+      double lo = mm[((size_t)e * NF + l) * 2], hi = mm[((size_t)e * NF + l) * 2 + 1];
+      double delta, lower, upper;
+      const double *v = u + ((size_t)e * NF + l) * np;
+      for (f = 0; f < 6; f++) {
+        int64_t e2 = face_neighbour(m, e, f);
+        if (e2 < 0) continue;
+        if (mm[((size_t)e2 * NF + l) * 2] < lo) lo = mm[((size_t)e2 * NF + l) * 2];
+        if (mm[((size_t)e2 * NF + l) * 2 + 1] > hi) hi = mm[((size_t)e2 * NF + l) * 2 + 1];
+      }
+      delta = deltafac * fmax(delta0, epsilon * (hi - lo));
+      lower = lo - delta;
+      upper = hi + delta;
+      for (q = 0; q < np; q++)
+        if (v[q] < lower || v[q] > upper) bad = 1;
+      if (!efv) {
+        double se = nmo_persson(n, v, uscale);
+        if (pers) pers[(size_t)e * NF + l] = se;
+        if (se > persson_max) bad = 1;
+      } else if (pers) {
+        pers[(size_t)e * NF + l] = 0.;
+      }
+    }
+    flags[e] = efv ? (bad ? 0 : -1) : (bad ? 1 : 0);
+  }
+  free(mm);
+  return 0;
 }
 
 static void basis(int n, double *D, double *wq)

@@ -59,6 +59,15 @@ def lib():
     return _lib
 
 
+def persson(n, u, u_scale=-1.0):
+    """Persson's modal indicator of one field u[n^3] on LGL points
+    (reference evolve_Persson_array_indicator, trouble.c:505)."""
+    f = lib().nmo_persson
+    f.restype = ctypes.c_double
+    u = np.ascontiguousarray(u, np.float64)
+    return f(ctypes.c_int(n), u.ctypes.data_as(ctypes.c_void_p), ctypes.c_double(u_scale))
+
+
 def uniform(n):
     """Equally spaced points on [-1,1] (reference Legendre.c:626)."""
     x = np.zeros(n)
@@ -213,6 +222,24 @@ class OracleMesh:
         if rc:
             raise RuntimeError(f"nmo_rhs failed ({rc})")
         return r
+
+    def trouble(self, u, u_p, deltafac=1.0, delta0=1e-4, epsilon=1e-3, persson_max=1e300,
+                uscale=-1.0):
+        """Trouble flags [E] (DG troubled 1 / fine 0, FV troubled 0 / fine -1)
+        and Persson indicators [E, 5] of state u against the previous u_p."""
+        u = np.ascontiguousarray(u, np.float64)
+        u_p = np.ascontiguousarray(u_p, np.float64)
+        fl = np.zeros(self.nelem, np.int32)
+        pe = np.zeros((self.nelem, 5))
+        rc = lib().nmo_trouble(ctypes.byref(self.s), u.ctypes.data_as(ctypes.c_void_p),
+                               u_p.ctypes.data_as(ctypes.c_void_p), ctypes.c_double(deltafac),
+                               ctypes.c_double(delta0), ctypes.c_double(epsilon),
+                               ctypes.c_double(persson_max), ctypes.c_double(uscale),
+                               fl.ctypes.data_as(ctypes.c_void_p),
+                               pe.ctypes.data_as(ctypes.c_void_p))
+        if rc:
+            raise RuntimeError(f"nmo_trouble failed ({rc})")
+        return fl, pe
 
     def rk4(self, u, dt, nsteps, t=0.0):
         u = np.array(u, np.float64, copy=True, order="C")

@@ -26,6 +26,10 @@
 #include "nmesh.h"
 #include "evolve.h"
 
+/* defined in src/main/evolve/trouble.c, not declared in a header */
+double evolve_Persson_array_indicator(tArray *u, double u_scale,
+                                      int pt_typ[3], int ncoeffs[3]);
+
 static int nmgdump_rhs_done = 0;
 
 /* small counter-based hash -> uniform in [-1,1) */
@@ -124,6 +128,34 @@ static void nmgdump_write(tMesh *mesh, const char *suffix, int with_r)
 
 /* r = RHS(u, t) once, before the first step, via the reference's own
    evolve_setrhs_mesh with w = u */
+/* Persson's modal indicator of each field of each element (the reference's
+   evolve_Persson_array_indicator, u_scale < 0, all coefficients):
+   "<prefix>_persson.bin" = int32 nelem, then float64 [nelem][5] */
+static void nmgdump_persson(tMesh *mesh)
+{
+  char fname[4096];
+  FILE *fp;
+  int iu[5];
+  int ne = (int)mesh->nmyelm, e, c;
+
+  nmgdump_vl_indices(mesh, iu);
+  snprintf(fname, sizeof(fname), "%s_persson.bin", Gets(Par("nmgdump_prefix")));
+  fp = fopen(fname, "wb");
+  if(!fp) errorexits("cannot open %s", fname);
+  fwrite(&ne, sizeof(int), 1, fp);
+  for(e = 0; e < ne; e++)
+  {
+    tElm *elm = mesh->myelm[e];
+    for(c = 0; c < 5; c++)
+    {
+      double se = evolve_Persson_array_indicator(VarA(elm, iu[c]), -1.,
+                                                 elm->pt_typ, elm->n);
+      fwrite(&se, sizeof(double), 1, fp);
+    }
+  }
+  fclose(fp);
+}
+
 int nmgdump_rhs(tMesh *mesh)
 {
   tEvoSys *evosys = mesh->evosys;
@@ -137,6 +169,7 @@ int nmgdump_rhs(tMesh *mesh)
     vlcopy(NULL, ListEntry(evosys->w, i), ListEntry(evosys->u, i));
   evolve_setrhs_mesh(mesh, evosys->rhs, evosys->w);
   nmgdump_write(mesh, "rhs", 1);
+  if(Getb(Par("nmgdump_persson"))) nmgdump_persson(mesh);
   return 0;
 }
 
@@ -160,5 +193,6 @@ int nmesh_nmgdump(tMesh *mesh)
   AddPar("nmgdump_amp", "1", "factor applied to the initial plane wave");
   AddPar("nmgdump_perturb", "0", "amplitude of the seeded perturbation");
   AddPar("nmgdump_seed", "1", "seed of the perturbation");
+  AddPar("nmgdump_persson", "no", "also dump Persson's indicator of u0 [no,yes]");
   return 0;
 }

@@ -72,6 +72,9 @@ CASES = {
     "mixcs7_l1_n5_w3no": dict(mesh="cs7", n=5, luni=1, k=(0.25, 0.15, -0.3),
                               dt=0.002, steps=2, eps=0.02, seed=28,
                               fv=dict(rec="WENOm3_2", extrap="no", patches="0")),
+    # DG data with Persson's modal indicator of u0 (every element, field)
+    "trbl_cs7_l1_n6": dict(mesh="cs7", n=6, luni=1, k=(0.9, -0.7, 0.5),
+                           dt=0.002, steps=1, eps=0.05, seed=29, persson=True),
 }
 
 
@@ -90,6 +93,7 @@ def parfile(case, prefix):
         "nmgdump_amp = 1.0",
         f"nmgdump_perturb = {c['eps']!r}",
         f"nmgdump_seed = {c['seed']}",
+        f"nmgdump_persson = {'yes' if c.get('persson') else 'no'}",
         "logfile_creation = no",
         "sysmon_hours = -1",
     ]
@@ -123,11 +127,18 @@ def run_case(case, exe, outdir):
             raise RuntimeError(f"{case}: reference failed\n{res.stdout[-3000:]}")
         d0 = read_dump(prefix + "_rhs.bin", True)
         d1 = read_dump(prefix + "_final.bin", False)
+        pers = None
+        if CASES[case].get("persson"):
+            raw = np.fromfile(prefix + "_persson.bin", dtype="<i4", count=1)
+            pers = np.fromfile(prefix + "_persson.bin", dtype="<f8", offset=4)
+            pers = pers.reshape(int(raw[0]), 5)
     c = CASES[case]
     meta = dict(case=case, **{k: v for k, v in c.items()})
     extra = {}
     if "fv" in c:   # fin.-vol. cases also keep the flag and det(dXb/dx)
         extra = dict(use_fv=d0["use_fv"], det_dXbdx=d0["det_dXbdx"])
+    if pers is not None:
+        extra["persson"] = pers
     np.savez_compressed(
         os.path.join(outdir, case + ".npz"),
         meta=json.dumps(meta), pat=d0["pat"], n=d0["n"], bbox=d0["bbox"],

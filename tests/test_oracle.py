@@ -101,3 +101,19 @@ def test_periodic_plane_wave_is_smooth():
     m = nmo.OracleMesh(bbox, np.zeros(mesh.nelem, np.int32), mesh.dXdx(), xyz, nb, 6)
     r = m.rhs(u)
     assert np.abs(r - dudt).max() < 2e-3
+
+
+def test_oracle_persson_matches_reference():
+    """Persson's indicator of every field of every element of u0 against the
+    reference's evolve_Persson_array_indicator (dumped by the reference run)."""
+    d, meta = load("trbl_cs7_l1_n6")
+    n = meta["n"]
+    got = np.array([[nmo.persson(n, d["u0"][e, l]) for l in range(5)]
+                    for e in range(len(d["pat"]))])
+    assert np.array_equal(got, d["persson"])
+    m = _oracle_mesh(d, meta)
+    fl, pe = m.trouble(d["u0"], d["u0"])
+    assert np.array_equal(pe, d["persson"])
+    assert (fl == 0).all()                      # u == u_p: inside its own bounds
+    fl, _ = m.trouble(d["u0"], d["u0"], persson_max=-2.0)
+    assert np.array_equal(fl, (d["persson"] > -2.0).any(axis=1).astype(np.int32))
