@@ -182,6 +182,27 @@ int nmg_rk4_step_trouble(nmg_ctx *c, double t, double dt, const nmg_trouble_para
                          int32_t *switched);
 int nmg_get_trouble_scores(nmg_ctx *c, int32_t *scores);
 
+/* ---- GRHD: pointwise conservative <-> primitive conversion ---------------
+ * Ideal gas on a conformally flat 3-metric gamma_ij = psi^4 delta_ij; no
+ * counterpart in the reference (its GRHD is external), except the root
+ * finder newton1d_brak (src/utility/numerics/newton1d_brak.c:20-121).
+ * Arrays are device SoA [5][npts]: conserved (D, S_1, S_2, S_3, tau)
+ * densitized by psi^6, primitives (rho, v^1, v^2, v^3, p); psi may be NULL
+ * (flat).  con2prim uses prim[4] as the starting pressure, writes status
+ * (iterations >= 0, or < 0 where the atmosphere was set and the conserved
+ * variables reset), and runs on `stream` (a cudaStream_t, NULL: default). */
+typedef struct nmg_grhd_params {
+  double gamma;    /* adiabatic index of p = (gamma - 1) rho eps */
+  double rho_atm;  /* atmosphere density (floor of D / psi^6) */
+  double p_atm;    /* atmosphere pressure */
+  double tol;      /* relative pressure accuracy of the root finder */
+  int32_t maxits;  /* iteration limit of the root finder */
+} nmg_grhd_params;
+int nmg_grhd_prim2con(const nmg_grhd_params *g, int64_t npts, const double *psi_dev,
+                      const double *prim_dev, double *cons_dev, void *stream);
+int nmg_grhd_con2prim(const nmg_grhd_params *g, int64_t npts, const double *psi_dev,
+                      double *cons_dev, double *prim_dev, int32_t *status_dev, void *stream);
+
 /* Finite-volume options of a context whose mesh is finite-volume: the
  * reference's DG globals fv_rec, fv_divf_extrap and
  * fv_WENOm3_opt_weightratio (src/main/dg/dg.c:286-400; defaults WENOm3_2,

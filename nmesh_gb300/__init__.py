@@ -55,6 +55,37 @@ class TroubleParams(ctypes.Structure):
                          persson_uscale, notroubles)
 
 
+class GrhdParams(ctypes.Structure):
+    """Ideal-gas GRHD conversion parameters (include/nmg.h nmg_grhd_params)."""
+    _fields_ = [("gamma", ctypes.c_double), ("rho_atm", ctypes.c_double),
+                ("p_atm", ctypes.c_double), ("tol", ctypes.c_double),
+                ("maxits", ctypes.c_int32)]
+
+    def __init__(self, gamma=2.0, rho_atm=1e-12, p_atm=1e-14, tol=1e-15, maxits=100):
+        super().__init__(gamma, rho_atm, p_atm, tol, maxits)
+
+
+def grhd_prim2con_device(params, npts, psi_ptr, prim_ptr, cons_ptr, stream=0):
+    """Conserved (D, S_i, tau) from primitives (rho, v^i, p) on device SoA
+    arrays [5][npts] (ints are device pointers; psi_ptr 0: flat)."""
+    rc = lib().nmg_grhd_prim2con(ctypes.byref(params), int(npts),
+                                 ctypes.c_void_p(psi_ptr or None), ctypes.c_void_p(prim_ptr),
+                                 ctypes.c_void_p(cons_ptr), ctypes.c_void_p(stream or None))
+    if rc:
+        raise NmgError(f"nmg_grhd_prim2con failed ({rc})")
+
+
+def grhd_con2prim_device(params, npts, psi_ptr, cons_ptr, prim_ptr, status_ptr, stream=0):
+    """Primitives from conserved variables (atmosphere where needed); see
+    include/nmg.h nmg_grhd_con2prim."""
+    rc = lib().nmg_grhd_con2prim(ctypes.byref(params), int(npts),
+                                 ctypes.c_void_p(psi_ptr or None), ctypes.c_void_p(cons_ptr),
+                                 ctypes.c_void_p(prim_ptr), ctypes.c_void_p(status_ptr),
+                                 ctypes.c_void_p(stream or None))
+    if rc:
+        raise NmgError(f"nmg_grhd_con2prim failed ({rc})")
+
+
 class _MeshDesc(ctypes.Structure):
     _fields_ = [("nelem", ctypes.c_int32), ("n", ctypes.c_int32),
                 ("pat", ctypes.c_void_p), ("bbox", ctypes.c_void_p),
@@ -130,6 +161,8 @@ def lib(build_if_missing=True):
         "nmg_trouble_check": (ctypes.c_int, [vp, vp, vp, vp, vp, vp]),
         "nmg_rk4_step_trouble": (ctypes.c_int, [vp, f64, f64, vp, vp]),
         "nmg_get_trouble_scores": (ctypes.c_int, [vp, vp]),
+        "nmg_grhd_prim2con": (ctypes.c_int, [vp, i64, vp, vp, vp, vp]),
+        "nmg_grhd_con2prim": (ctypes.c_int, [vp, i64, vp, vp, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

@@ -12,10 +12,10 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libnmg.so")
 SOURCES = ["nmg.cu", "stage_eo.cu", "stage_gather.cu", "stage_fv.cu", "stage_fv_fast.cu",
-           "noalloc.cu", "mesh.cpp"]
+           "grhd.cu", "noalloc.cu", "mesh.cpp"]
 # per-file extra flags: the finite-volume kernel rounds every product and sum
 # separately, in the reference's order (no FMA contraction)
-EXTRA_FLAGS = {"stage_fv.cu": ["-fmad=false"]}
+EXTRA_FLAGS = {"stage_fv.cu": ["-fmad=false"], "grhd.cu": ["-fmad=false"]}
 HEADERS = ["mesh.h", "stage.cuh", "ctx.h",os.path.join("..", "..", "include", "nmg.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",

@@ -38,6 +38,9 @@
  *   midpoint states      src/tests/scalarwave1/scalarwave1.c:761-802
  *   fin.-vol. surface    src/main/dg/dg.c:58-70,81-90 (oow = 1/|distXb|,
  *                        F = f*)
+ *   root finder          src/utility/numerics/newton1d_brak.c:20-121 (GRHD
+ *                        con2prim; the GRHD physics itself has no
+ *                        reference counterpart: parity unpinned)
  *   trouble indicators   src/main/evolve/trouble.c:438-564 (RDMP, Persson),
  *                        src/main/basis/Legendre.c:14-38,277-310 (modal
  *                        analysis matrix)
@@ -966,4 +969,175 @@ int nmo_rk4(const nmo_mesh *m, double t, double dt, int nsteps, double *u)
   }
   free(work);
   return rc;
+}
+
+/* ------------------------------------------------------------------ */
+/* GRHD conservative-to-primitive recovery (config 3's physics)        */
+/* ------------------------------------------------------------------ */
+/* Newton-Raphson with bracketing and bisection fallback in [x1, x2]
+   (newton1d_brak, src/utility/numerics/newton1d_brak.c:20-121); returns the
+   number of iterations (>= 0) or a negative error code, the root in *x0. */
+int nmo_newton1d_brak(double *x0, void (*fdf)(double, void *, double *, double *),
+                      double x1, double x2, void *par, int maxits, double xacc)
+{
+  int j, bisect;
+  double f, fh, fl, df, xh, xl, xrt, dx, dxold, tmp;
+  if (!isfinite(x1) || !isfinite(x2)) return -2 * maxits - 2;
+  if ((x1 <= *x0 && *x0 <= x2) || (x2 <= *x0 && *x0 <= x1)) xrt = *x0;
+  else xrt = 0.5 * (x1 + x2);
+  fdf(x1, par, &fl, &df);
+  fdf(x2, par, &fh, &df);
+  j = 0;
+  if (fl <= 0.0 && fh >= 0.0) j = 1;
+  if (fl >= 0.0 && fh <= 0.0) j = 1;
+  if (!j) return -2 * maxits - 3;
+  if (fl == 0.0) { *x0 = x1; return 0; }
+  if (fh == 0.0) { *x0 = x2; return 0; }
+  if (fl < 0.0) { xl = x1; xh = x2; }
+  else { xh = x1; xl = x2; }
+  dxold = fabs(x2 - x1);
+  dx = dxold;
+  for (j = 1; j <= maxits; j++) {
+    fdf(xrt, par, &f, &df);
+    if (!isfinite(f)) return -j;
+    if (f == 0.0) { *x0 = xrt; return j; }
+    if (f < 0.0) xl = xrt;
+    else xh = xrt;
+    if (!isfinite(df)) bisect = 1;
+    else bisect = (fabs(2.0 * f) > fabs(dxold * df));
+    if (bisect == 0) {
+      dxold = dx;
+      dx = f / df;
+      tmp = xrt;
+      xrt -= dx;
+      if (((xrt - xh) * (xrt - xl) > 0.0) || (tmp == xrt)) {
+        bisect = 1; xrt = tmp; dx = dxold;
+      }
+    }
+    if (bisect) {
+      dxold = dx;
+      dx = 0.5 * (xh - xl);
+      xrt = xl + dx;
+      if (xl == xrt) { *x0 = xrt; return j; }
+    }
+    if (fabs(dx) < xacc) { *x0 = xrt; return j; }
+  }
+  *x0 = xrt;
+  return j;
+}
+
+/* Ideal-gas GRHD on a conformally flat 3-metric gamma_ij = psi^4 delta_ij
+   (restated; the reference has no GRHD, so this is parity unpinned):
+   conserved (D, S_i, tau) densitized by sqrt(gamma) = psi^6,
+   D = psi^6 rho W, S_i = psi^6 rho h W^2 v_i, tau = psi^6 (rho h W^2 - p) - D,
+   v_i = psi^4 v^i, W = 1/sqrt(1 - v_i v^i), h = 1 + eps + p/rho,
+   p = (gamma - 1) rho eps.  Primitives (rho, v^1, v^2, v^3, p). */
+typedef struct nmo_grhd {
+  double gamma, rho_atm, p_atm, tol;
+  int maxits;
+} nmo_grhd;
+
+typedef struct nmo_c2p_par {
+  double D, tau, S2, gm1, gam;
+} nmo_c2p_par;
+
+/* f(p) = (gamma-1) rho(p) eps(p) - p and the approximation
+   f'(p) = v^2 c_s^2 - 1 */
+static void c2p_fdf(double p, void *vp, double *f, double *df)
+{
+  const nmo_c2p_par *q = (const nmo_c2p_par *)vp;
+  double E = q->tau + q->D + p;
+  double v2 = q->S2 / (E * E);
+  double W = 1. / sqrt(1. - v2);
+  double rho = q->D / W;
+  double eps = (q->tau + q->D * (1. - W) + p * (1. - W * W)) / (q->D * W);
+  double cs2 = q->gam * q->gm1 * eps / (1. + q->gam * eps);
+  *f = q->gm1 * rho * eps - p;
+  *df = v2 * cs2 - 1.;
+}
+
+void nmo_grhd_prim2con(const nmo_grhd *g, int64_t npts, const double *psi, const double *prim,
+                       double *cons)
+{
+  int64_t i;
+  for (i = 0; i < npts; i++) {
+    double ps = psi ? psi[i] : 1.;
+    double ps4 = ps * ps * ps * ps, ps6 = ps4 * ps * ps;
+    double rho = prim[i], vx = prim[npts + i], vy = prim[2 * npts + i];
+    double vz = prim[3 * npts + i], p = prim[4 * npts + i];
+    double v2 = ps4 * (vx * vx + vy * vy + vz * vz);
+    double W = 1. / sqrt(1. - v2);
+    double eps = p / ((g->gamma - 1.) * rho);
+    double h = 1. + eps + p / rho;
+    double rhW2 = rho * h * W * W;
+    cons[i] = ps6 * rho * W;
+    cons[npts + i] = ps6 * rhW2 * ps4 * vx;
+    cons[2 * npts + i] = ps6 * rhW2 * ps4 * vy;
+    cons[3 * npts + i] = ps6 * rhW2 * ps4 * vz;
+    cons[4 * npts + i] = ps6 * (rhW2 - p) - cons[i];
+  }
+}
+
+/* con2prim with pressure as the unknown (newton1d_brak on f above; the
+   previous prim[4] is the starting guess).  Points that are below the
+   atmosphere density or where the root finder fails are set to the
+   atmosphere (rho_atm, v = 0, p_atm) and their conserved variables are
+   reset to match.  status[i] = iterations (>= 0) or < 0 (atmosphere). */
+void nmo_grhd_con2prim(const nmo_grhd *g, int64_t npts, const double *psi, double *cons,
+                       double *prim, int32_t *status)
+{
+  int64_t i;
+  for (i = 0; i < npts; i++) {
+    double ps = psi ? psi[i] : 1.;
+    double ps4 = ps * ps * ps * ps, ps6 = ps4 * ps * ps;
+    double D = cons[i] / ps6, Sx = cons[npts + i] / ps6, Sy = cons[2 * npts + i] / ps6;
+    double Sz = cons[3 * npts + i] / ps6, tau = cons[4 * npts + i] / ps6;
+    double S2 = (Sx * Sx + Sy * Sy + Sz * Sz) / ps4;
+    nmo_c2p_par q;
+    double plo, phi, p, f, df, xacc;
+    int rc = -1, k;
+    q.D = D; q.tau = tau; q.S2 = S2; q.gm1 = g->gamma - 1.; q.gam = g->gamma;
+    if (D >= g->rho_atm && isfinite(D) && isfinite(tau) && isfinite(S2)) {
+      double S = sqrt(S2);
+      plo = S - tau - D;
+      plo = plo > 0. ? plo * (1. + 1e-14) : 0.;
+      phi = q.gm1 * (tau + D);
+      if (phi < plo) phi = 2. * plo;
+      if (phi <= 0.) phi = 1e-300;
+      for (k = 0; k < 200; k++) {      /* widen upwards until f(phi) < 0 */
+        c2p_fdf(phi, &q, &f, &df);
+        if (f < 0.) break;
+        phi *= 2.;
+      }
+      p = prim[4 * npts + i];
+      xacc = g->tol * phi;
+      rc = nmo_newton1d_brak(&p, c2p_fdf, plo, phi, &q, g->maxits, xacc);
+      if (rc >= 0) {
+        double E = tau + D + p, W, rho;
+        double v2 = S2 / (E * E);
+        W = 1. / sqrt(1. - v2);
+        rho = D / W;
+        if (!(rho >= g->rho_atm) || !(p > 0.) || !isfinite(W)) rc = -1;
+        else {
+          double fac = 1. / (E * ps4);          /* v^i = S^i / (E psi^4) */
+          prim[i] = rho;
+          prim[npts + i] = Sx * fac;
+          prim[2 * npts + i] = Sy * fac;
+          prim[3 * npts + i] = Sz * fac;
+          prim[4 * npts + i] = p;
+        }
+      }
+    }
+    if (rc < 0) {                            /* atmosphere, conserved reset */
+      double eps_atm = g->p_atm / ((g->gamma - 1.) * g->rho_atm);
+      double h = 1. + eps_atm + g->p_atm / g->rho_atm;
+      prim[i] = g->rho_atm;
+      prim[npts + i] = prim[2 * npts + i] = prim[3 * npts + i] = 0.;
+      prim[4 * npts + i] = g->p_atm;
+      cons[i] = ps6 * g->rho_atm;
+      cons[npts + i] = cons[2 * npts + i] = cons[3 * npts + i] = 0.;
+      cons[4 * npts + i] = ps6 * (g->rho_atm * h - g->p_atm) - cons[i];
+    }
+    status[i] = rc;
+  }
 }

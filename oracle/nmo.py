@@ -249,3 +249,60 @@ class OracleMesh:
         if rc:
             raise RuntimeError(f"nmo_rk4 failed ({rc})")
         return u
+
+
+# ---- GRHD (restated; the root finder follows the reference's newton1d_brak)
+class _Grhd(ctypes.Structure):
+    _fields_ = [("gamma", ctypes.c_double), ("rho_atm", ctypes.c_double),
+                ("p_atm", ctypes.c_double), ("tol", ctypes.c_double), ("maxits", ctypes.c_int)]
+
+
+FDF = ctypes.CFUNCTYPE(None, ctypes.c_double, ctypes.c_void_p,
+                       ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double))
+
+
+def newton1d_brak(fdf, x0, x1, x2, maxits=100, xacc=1e-14, lib_=None):
+    """Restated newton1d_brak (or, with lib_, the same-signature function of
+    another library such as the reference's own): returns (rc, root)."""
+    L = lib_ or lib()
+    fn = L.nmo_newton1d_brak if lib_ is None else L.newton1d_brak
+    fn.restype = ctypes.c_int
+    x = ctypes.c_double(x0)
+    cb = FDF(lambda xx, par, f, df: fdf(xx, f, df))
+    if lib_ is None:
+        rc = fn(ctypes.byref(x), cb, ctypes.c_double(x1), ctypes.c_double(x2), None,
+                ctypes.c_int(maxits), ctypes.c_double(xacc))
+    else:   # the reference's signature has a trailing print flag
+        rc = fn(ctypes.byref(x), cb, ctypes.c_double(x1), ctypes.c_double(x2), None,
+                ctypes.c_int(maxits), ctypes.c_double(xacc), ctypes.c_int(0))
+    return rc, x.value
+
+
+def grhd_prim2con(prim, psi=None, gamma=2.0, rho_atm=1e-12, p_atm=1e-14, tol=1e-15, maxits=100):
+    prim = np.ascontiguousarray(prim, np.float64)
+    npts = prim.shape[1]
+    cons = np.zeros_like(prim)
+    g = _Grhd(gamma, rho_atm, p_atm, tol, maxits)
+    ps = None if psi is None else np.ascontiguousarray(psi, np.float64)
+    lib().nmo_grhd_prim2con(ctypes.byref(g), ctypes.c_int64(npts),
+                            None if ps is None else ps.ctypes.data_as(ctypes.c_void_p),
+                            prim.ctypes.data_as(ctypes.c_void_p),
+                            cons.ctypes.data_as(ctypes.c_void_p))
+    return cons
+
+
+def grhd_con2prim(cons, prim_guess, psi=None, gamma=2.0, rho_atm=1e-12, p_atm=1e-14,
+                  tol=1e-15, maxits=100):
+    """Returns (prim, cons after atmosphere resets, status)."""
+    cons = np.array(cons, np.float64, copy=True, order="C")
+    prim = np.array(prim_guess, np.float64, copy=True, order="C")
+    npts = cons.shape[1]
+    st = np.zeros(npts, np.int32)
+    g = _Grhd(gamma, rho_atm, p_atm, tol, maxits)
+    ps = None if psi is None else np.ascontiguousarray(psi, np.float64)
+    lib().nmo_grhd_con2prim(ctypes.byref(g), ctypes.c_int64(npts),
+                            None if ps is None else ps.ctypes.data_as(ctypes.c_void_p),
+                            cons.ctypes.data_as(ctypes.c_void_p),
+                            prim.ctypes.data_as(ctypes.c_void_p),
+                            st.ctypes.data_as(ctypes.c_void_p))
+    return prim, cons, st
