@@ -182,6 +182,14 @@ int nmg_rk4_step_trouble(nmg_ctx *c, double t, double dt, const nmg_trouble_para
                          int32_t *switched);
 int nmg_get_trouble_scores(nmg_ctx *c, int32_t *scores);
 
+/* 0d norms of a state on the device (the ingredients of output0d_mesh_vl,
+ * src/utility/output/output0d.c:44-176, with the volume integrals of
+ * MeshVolumeIntegral / NodeVolumeIntegral, src/main/main/norms.c:10-28,
+ * src/main/coordinates/integrals.c:12-60): out[0] = volume, then per field
+ * (pi, cx, cy, cz, phi) VolInt, mean, rms, min, max, maxAbs (31 doubles).
+ * u_dev NULL: the resident state.  Only the 31 numbers leave the GPU. */
+int nmg_norms(nmg_ctx *c, const double *u_dev, double *out);
+
 /* ---- GRHD: pointwise conservative <-> primitive conversion ---------------
  * Ideal gas on a conformally flat 3-metric gamma_ij = psi^4 delta_ij; no
  * counterpart in the reference (its GRHD is external), except the root

@@ -161,6 +161,7 @@ def lib(build_if_missing=True):
         "nmg_trouble_check": (ctypes.c_int, [vp, vp, vp, vp, vp, vp]),
         "nmg_rk4_step_trouble": (ctypes.c_int, [vp, f64, f64, vp, vp]),
         "nmg_get_trouble_scores": (ctypes.c_int, [vp, vp]),
+        "nmg_norms": (ctypes.c_int, [vp, vp, vp]),
         "nmg_grhd_prim2con": (ctypes.c_int, [vp, i64, vp, vp, vp, vp]),
         "nmg_grhd_con2prim": (ctypes.c_int, [vp, i64, vp, vp, vp, vp, vp]),
     }
@@ -382,6 +383,19 @@ class Evolution:
             raise NmgError(f"nmg_set_fv: unknown fv_rec {rec!r} or fv_divf_extrap {extrap!r}")
         self._check(lib().nmg_set_fv(self._h, FV_REC[rec], FV_EXTRAP[extrap],
                                      float(w3ratio)), "nmg_set_fv")
+
+    def norms(self, u_ptr=0):
+        """0d norms of the resident state (or of device state u_ptr): dict
+        with 'volume' and per field name (VolInt, mean, rms, min, max,
+        maxAbs) (the reference's output0d quantities)."""
+        out = np.zeros(1 + 6 * NFIELDS)
+        self._check(lib().nmg_norms(self._h, ctypes.c_void_p(u_ptr or None), _ptr(out)),
+                    "nmg_norms")
+        res = {"volume": out[0]}
+        for l, name in enumerate(FIELDS):
+            res[name] = dict(zip(("VolInt", "mean", "rms", "min", "max", "maxAbs"),
+                                 out[1 + 6 * l: 7 + 6 * l]))
+        return res
 
     # ---- DG <-> finite-volume switching ----
     def set_element_types(self, fv):

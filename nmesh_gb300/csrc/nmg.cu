@@ -86,6 +86,83 @@ __global__ void obj_final_kernel(const double *partial, int nblk, double dt, dou
   *out += dt * s;
 }
 
+// 0d norms: per element and field the quadrature sums of v and v^2 with the
+// weights w_i w_j w_k / |det(dXb/dx)| (NodeVolumeIntegral,
+// src/main/coordinates/integrals.c:12-60), min and max; then one thread per
+// field adds the element partials in element order
+constexpr int kNormThreads = 128;
+__global__ void __launch_bounds__(kNormThreads)
+    norms_elem_kernel(int n, int nelem, const double *u, const int *cslot, const double *scale,
+                      const double *metric, const double *fvgeo, int allfv,
+                      const unsigned char *isfv, const double *wl, const double *wu,
+                      double *part) {
+  __shared__ double sh[4][kNormThreads];
+  const int np = n * n * n, e = blockIdx.x;
+  if (e >= nelem) return;
+  const bool efv = allfv || (isfv && isfv[e]);
+  const double *w = efv ? wu : wl;
+  const int cs = cslot[e];
+  const double s0 = scale[e * 3], s1 = scale[e * 3 + 1], s2 = scale[e * 3 + 2];
+  for (int l = -1; l < NF; l++) {   // l = -1: the volume (v = 1)
+    double a1 = 0., a2 = 0., lo = 1e300, hi = -1e300;
+    for (int q = threadIdx.x; q < np; q += kNormThreads) {
+      const int i = q % n, j = (q / n) % n, k = q / (n * n);
+      double det;
+      if (cs < 0) {
+        det = s0 * s1 * s2;
+      } else if (efv) {
+        det = fvgeo[(size_t)cs * 13 * np + q];
+      } else {
+        const double *M = metric + (size_t)cs * 9 * np + q;
+        const double m00 = M[0], m01 = M[np], m02 = M[2 * np], m10 = M[3 * np], m11 = M[4 * np],
+                     m12 = M[5 * np], m20 = M[6 * np], m21 = M[7 * np], m22 = M[8 * np];
+        det = m00 * (m11 * m22 - m12 * m21) - m01 * (m10 * m22 - m12 * m20) +
+              m02 * (m10 * m21 - m11 * m20);
+      }
+      const double qw = det != 0. ? w[i] * w[j] * w[k] / fabs(det) : 0.;
+      const double v = l < 0 ? 1. : u[((size_t)e * NF + l) * np + q];
+      a1 += qw * v;
+      a2 += qw * v * v;
+      lo = fmin(lo, v);
+      hi = fmax(hi, v);
+    }
+    sh[0][threadIdx.x] = a1;
+    sh[1][threadIdx.x] = a2;
+    sh[2][threadIdx.x] = lo;
+    sh[3][threadIdx.x] = hi;
+    __syncthreads();
+    for (int s = kNormThreads / 2; s > 0; s >>= 1) {
+      if (threadIdx.x < s) {
+        sh[0][threadIdx.x] += sh[0][threadIdx.x + s];
+        sh[1][threadIdx.x] += sh[1][threadIdx.x + s];
+        sh[2][threadIdx.x] = fmin(sh[2][threadIdx.x], sh[2][threadIdx.x + s]);
+        sh[3][threadIdx.x] = fmax(sh[3][threadIdx.x], sh[3][threadIdx.x + s]);
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0)
+      for (int c = 0; c < 4; c++) part[((size_t)e * (NF + 1) + (l + 1)) * 4 + c] = sh[c][0];
+    __syncthreads();
+  }
+}
+
+__global__ void norms_final_kernel(int nelem, const double *part, double *out) {
+  const int l = threadIdx.x;  // 0: volume, 1..5: fields
+  if (l > NF) return;
+  double a1 = 0., a2 = 0., lo = 1e300, hi = -1e300;
+  for (int e = 0; e < nelem; e++) {
+    const double *p = part + ((size_t)e * (NF + 1) + l) * 4;
+    a1 += p[0];
+    a2 += p[1];
+    lo = fmin(lo, p[2]);
+    hi = fmax(hi, p[3]);
+  }
+  out[l * 4] = a1;
+  out[l * 4 + 1] = a2;
+  out[l * 4 + 2] = lo;
+  out[l * 4 + 3] = hi;
+}
+
 // adjoint source of J at one step: lambda_phi += coef W phi
 __global__ void adj_source_kernel(double *lambda, const double *u, const double *W, int nelem,
                                   int np, double coef) {
@@ -152,6 +229,8 @@ struct nmg_ctx {
   int *d_score = nullptr;      // [E] trouble score (node->dat->info->trbl_score)
   double *d_up = nullptr;      // u_p: state at the start of a checked step
   double *d_pers = nullptr;    // [E][5] Persson indicators of the last check
+  double *d_wq = nullptr;      // [2][n] LGL and trapezoid (equally spaced) weights
+  double *d_npart = nullptr;   // [E][6][4] partial norms
   int fv_rec = NMG_FV_REC_WENOM3_2, fv_extrap = NMG_FV_EXTRAP_DNFN1;
   double fv_w3ratio = 2.;
   double *d_fvgeo = nullptr, *d_fvdist = nullptr, *d_fvdxb = nullptr;
@@ -798,6 +877,13 @@ static int create_impl(const nmg_mesh *m, int32_t bc_kind, const double k[3], bo
   CK(up(&c->d_bxyz, bxyz));
   CK(up(&c->d_bnrm, bnrm));
   CK(up(&c->d_D, m->D));
+  {
+    std::vector<double> wq(2 * (size_t)n);
+    for (int i = 0; i < n; i++) wq[i] = m->w[i];
+    for (int i = 0; i < n; i++)  // uniform_x_wTrapez (Legendre.c:701-719)
+      wq[n + i] = (n == 1) ? 2. : (i == 0 || i == n - 1) ? 1. / (n - 1) : 2. / (n - 1);
+    CK(up(&c->d_wq, wq));
+  }
   if (c->fv) {
     CK(up(&c->d_fvgeo, fvgeo));
     CK(up(&c->d_fvdist, fvdist));
@@ -997,6 +1083,39 @@ int nmg_rk4_step_trouble(nmg_ctx *c, double t, double dt, const nmg_trouble_para
   return NMG_OK;
 }
 
+int nmg_norms(nmg_ctx *c, const double *u_dev, double *out) {
+  if (!c || !out) return set_err(c, NMG_EINVAL, "nmg_norms: null argument");
+  const int64_t E = c->nelem;
+  if (!c->d_npart) CK(cudaMalloc((void **)&c->d_npart, sizeof(double) * E * (NF + 1) * 4 + 256));
+  const double *u = u_dev ? u_dev : c->d_buf[c->cur];
+  norms_elem_kernel<<<(unsigned)E, kNormThreads, 0, c->stream>>>(
+      c->n, (int)E, u, c->d_cslot, c->d_scale, c->d_metric, c->d_fvgeo,
+      (c->fv && !c->mixed) ? 1 : 0, c->mixed ? c->d_isfv : nullptr, c->d_wq, c->d_wq + c->n,
+      c->d_npart);
+  CK(cudaGetLastError());
+  double *fin = c->d_npart + E * (NF + 1) * 4;  // the 256 spare bytes: 24 doubles
+  norms_final_kernel<<<1, 32, 0, c->stream>>>((int)E, c->d_npart, fin);
+  CK(cudaGetLastError());
+  c->launches += 2;
+  double h[(NF + 1) * 4];
+  CK(cudaMemcpyAsync(h, fin, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  // out: Vol, then per field VolInt, mean, rms, min, max, maxAbs
+  const double vol = h[0];
+  out[0] = vol;
+  for (int l = 0; l < NF; l++) {
+    const double *q = h + (l + 1) * 4;
+    double *o = out + 1 + l * 6;
+    o[0] = q[0];
+    o[1] = q[0] / vol;
+    o[2] = sqrt(fabs(q[1] / vol));
+    o[3] = q[2];
+    o[4] = q[3];
+    o[5] = fabs(q[3]) > fabs(q[2]) ? fabs(q[3]) : fabs(q[2]);
+  }
+  return NMG_OK;
+}
+
 int nmg_set_fv(nmg_ctx *c, int32_t rec, int32_t extrap, double w3ratio) {
   if (!c) return NMG_EINVAL;
   if (!c->fv) return set_err(c, NMG_EUNSUP, "nmg_set_fv: the mesh has no finite-volume elements");
@@ -1023,7 +1142,7 @@ void nmg_destroy(nmg_ctx *c) {
   cudaFree(c->d_fvlist); cudaFree(c->d_gtab); cudaFree(c->d_isfv); cudaFree(c->d_ghost);
   cudaFree(c->d_gM); cudaFree(c->d_fvbxyz); cudaFree(c->d_fvbnrm); cudaFree(c->d_PR);
   cudaFree(c->d_conv); cudaFree(c->d_mm); cudaFree(c->d_trb); cudaFree(c->d_score);
-  cudaFree(c->d_up); cudaFree(c->d_pers);
+  cudaFree(c->d_up); cudaFree(c->d_pers); cudaFree(c->d_wq); cudaFree(c->d_npart);
   for (int b = 0; b < 4; b++) cudaFree(c->d_buf[b]);
   cudaFree(c->d_times); cudaFree(c->d_step);
   if (c->stream) cudaStreamDestroy(c->stream);

@@ -156,6 +156,36 @@ static void nmgdump_persson(tMesh *mesh)
   fclose(fp);
 }
 
+/* the reference's 0d norms of each field of u0 (output0d_mesh_vl's
+   ingredients): "<prefix>_norms.bin" = float64 Vol, then per field
+   VolInt, Int(v^2), min, max */
+static void nmgdump_norms(tMesh *mesh)
+{
+  char fname[4096], nodeloc[105];
+  FILE *fp;
+  int iu[5], c, p, ijk;
+  double X[3], x[3], v;
+
+  nmgdump_vl_indices(mesh, iu);
+  snprintf(fname, sizeof(fname), "%s_norms.bin", Gets(Par("nmgdump_prefix")));
+  fp = fopen(fname, "wb");
+  if(!fp) errorexits("cannot open %s", fname);
+  v = MeshVolumeIntegral(mesh, NULL, Ind("X"), 0.0, 0);
+  fwrite(&v, sizeof(double), 1, fp);
+  for(c = 0; c < 5; c++)
+  {
+    v = MeshVolumeIntegral(mesh, NULL, iu[c], 1., 0);
+    fwrite(&v, sizeof(double), 1, fp);
+    v = MeshVolumeIntegral(mesh, NULL, iu[c], 2., 0);
+    fwrite(&v, sizeof(double), 1, fp);
+    v = MeshExtremumLoc(mesh, NULL, iu[c], 0, &p, nodeloc, &ijk, X, x);
+    fwrite(&v, sizeof(double), 1, fp);
+    v = MeshExtremumLoc(mesh, NULL, iu[c], 1, &p, nodeloc, &ijk, X, x);
+    fwrite(&v, sizeof(double), 1, fp);
+  }
+  fclose(fp);
+}
+
 int nmgdump_rhs(tMesh *mesh)
 {
   tEvoSys *evosys = mesh->evosys;
@@ -170,6 +200,7 @@ int nmgdump_rhs(tMesh *mesh)
   evolve_setrhs_mesh(mesh, evosys->rhs, evosys->w);
   nmgdump_write(mesh, "rhs", 1);
   if(Getb(Par("nmgdump_persson"))) nmgdump_persson(mesh);
+  if(Getb(Par("nmgdump_norms"))) nmgdump_norms(mesh);
   return 0;
 }
 
@@ -194,5 +225,6 @@ int nmesh_nmgdump(tMesh *mesh)
   AddPar("nmgdump_perturb", "0", "amplitude of the seeded perturbation");
   AddPar("nmgdump_seed", "1", "seed of the perturbation");
   AddPar("nmgdump_persson", "no", "also dump Persson's indicator of u0 [no,yes]");
+  AddPar("nmgdump_norms", "no", "also dump the 0d norms of u0 [no,yes]");
   return 0;
 }

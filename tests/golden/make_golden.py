@@ -75,6 +75,13 @@ CASES = {
     # DG data with Persson's modal indicator of u0 (every element, field)
     "trbl_cs7_l1_n6": dict(mesh="cs7", n=6, luni=1, k=(0.9, -0.7, 0.5),
                            dt=0.002, steps=1, eps=0.05, seed=29, persson=True),
+    # 0d norms (volume integrals, extrema) of u0 on DG and on mixed meshes
+    "norms_cs7_l1_n5": dict(mesh="cs7", n=5, luni=1, k=(0.3, -0.2, 0.1),
+                            dt=0.002, steps=1, eps=0.05, seed=30, norms=True),
+    "norms_mixcs7_l0_n6": dict(mesh="cs7", n=6, luni=0, k=(0.3, 0.2, -0.1),
+                               dt=0.002, steps=1, eps=0.05, seed=31, norms=True,
+                               fv=dict(rec="WENOm3_2", extrap="dnfn_extrap1",
+                                       patches="0")),
 }
 
 
@@ -94,6 +101,7 @@ def parfile(case, prefix):
         f"nmgdump_perturb = {c['eps']!r}",
         f"nmgdump_seed = {c['seed']}",
         f"nmgdump_persson = {'yes' if c.get('persson') else 'no'}",
+        f"nmgdump_norms = {'yes' if c.get('norms') else 'no'}",
         "logfile_creation = no",
         "sysmon_hours = -1",
     ]
@@ -132,6 +140,9 @@ def run_case(case, exe, outdir):
             raw = np.fromfile(prefix + "_persson.bin", dtype="<i4", count=1)
             pers = np.fromfile(prefix + "_persson.bin", dtype="<f8", offset=4)
             pers = pers.reshape(int(raw[0]), 5)
+        norms = None
+        if CASES[case].get("norms"):
+            norms = np.fromfile(prefix + "_norms.bin", dtype="<f8")
     c = CASES[case]
     meta = dict(case=case, **{k: v for k, v in c.items()})
     extra = {}
@@ -139,6 +150,8 @@ def run_case(case, exe, outdir):
         extra = dict(use_fv=d0["use_fv"], det_dXbdx=d0["det_dXbdx"])
     if pers is not None:
         extra["persson"] = pers
+    if norms is not None:      # Vol, then per field VolInt, Int v^2, min, max
+        extra["norms"] = norms
     np.savez_compressed(
         os.path.join(outdir, case + ".npz"),
         meta=json.dumps(meta), pat=d0["pat"], n=d0["n"], bbox=d0["bbox"],
