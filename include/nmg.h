@@ -47,6 +47,11 @@ extern "C" {
 #define NMG_BC_OUTGOING 1        /* outgoing radiation: no incoming
                                     characteristic (no reference counterpart) */
 
+/* numerical flux, the reference's par scalarwave1_numflux
+ * (src/tests/scalarwave1/scalarwave1.c:701-704; its default is upwind) */
+#define NMG_NUMFLUX_LLF 0    /* "LLF": numflux1d_LLF (src/main/dg/numflux1d.c:85) */
+#define NMG_NUMFLUX_UPWIND 1 /* scalarwave1_numflux1d_upwind (scalarwave1.c:323) */
+
 /* finite-volume reconstruction at the midpoints, the reference's par fv_rec
  * (src/main/dg/dg.c:286-330, rec1d.c) */
 #define NMG_FV_REC_1 0        /* "1": first order (rec1d_p_1 / rec1d_m_1) */
@@ -210,6 +215,10 @@ int nmg_grhd_prim2con(const nmg_grhd_params *g, int64_t npts, const double *psi_
                       const double *prim_dev, double *cons_dev, void *stream);
 int nmg_grhd_con2prim(const nmg_grhd_params *g, int64_t npts, const double *psi_dev,
                       double *cons_dev, double *prim_dev, int32_t *status_dev, void *stream);
+
+/* numerical flux of a context (default NMG_NUMFLUX_LLF, what the workloads
+ * use); the adjoint entry points support LLF only */
+int nmg_set_numflux(nmg_ctx *c, int32_t kind);
 
 /* Finite-volume options of a context whose mesh is finite-volume: the
  * reference's DG globals fv_rec, fv_divf_extrap and

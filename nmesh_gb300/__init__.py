@@ -162,6 +162,7 @@ def lib(build_if_missing=True):
         "nmg_rk4_step_trouble": (ctypes.c_int, [vp, f64, f64, vp, vp]),
         "nmg_get_trouble_scores": (ctypes.c_int, [vp, vp]),
         "nmg_norms": (ctypes.c_int, [vp, vp, vp]),
+        "nmg_set_numflux": (ctypes.c_int, [vp, i32]),
         "nmg_grhd_prim2con": (ctypes.c_int, [vp, i64, vp, vp, vp, vp]),
         "nmg_grhd_con2prim": (ctypes.c_int, [vp, i64, vp, vp, vp, vp, vp]),
     }
@@ -375,6 +376,13 @@ class Evolution:
                                                ctypes.byref(J), ctypes.c_void_p(grad_ptr)),
                     "nmg_adjoint_gradient")
         return J.value
+
+    def set_numflux(self, kind="LLF"):
+        """Numerical flux: "LLF" or "upwind" (reference par scalarwave1_numflux)."""
+        k = {"LLF": 0, "upwind": 1}.get(kind)
+        if k is None:
+            raise NmgError(f"nmg_set_numflux: unknown numerical flux {kind!r}")
+        self._check(lib().nmg_set_numflux(self._h, k), "nmg_set_numflux")
 
     def set_fv(self, rec="WENOm3_2", extrap="dnfn_extrap1", w3ratio=2.0):
         """Finite-volume options (reference pars fv_rec, fv_divf_extrap,

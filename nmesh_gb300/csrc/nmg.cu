@@ -206,6 +206,7 @@ struct nmg_ctx {
   int *d_step = nullptr;
   int times_cap = 0;
   // finite-volume mesh: options and geometry (stage_fv.cu)
+  int numflux = NMG_NUMFLUX_LLF;
   bool fv = false;     // some elements are finite-volume
   bool mixed = false;  // ... and some DG: variants[0, ndg) DG, [ndg, n) FV
   int ndg = 0, fsel = -1;
@@ -357,6 +358,7 @@ static StageParams base_params(nmg_ctx *c) {
   P.fvdist = c->d_fvdist;
   P.fvdxb = c->d_fvdxb;
   P.ghost = c->d_ghost;
+  P.numflux = c->numflux;
   P.fvbxyz = c->d_fvbxyz;
   P.fvbnrm = c->d_fvbnrm;
   P.bc = c->bc;
@@ -1116,6 +1118,15 @@ int nmg_norms(nmg_ctx *c, const double *u_dev, double *out) {
   return NMG_OK;
 }
 
+int nmg_set_numflux(nmg_ctx *c, int32_t kind) {
+  if (!c) return NMG_EINVAL;
+  if (kind != NMG_NUMFLUX_LLF && kind != NMG_NUMFLUX_UPWIND)
+    return set_err(c, NMG_EINVAL, "nmg_set_numflux: unknown numerical flux");
+  c->numflux = kind;
+  drop_graphs(c);
+  return NMG_OK;
+}
+
 int nmg_set_fv(nmg_ctx *c, int32_t rec, int32_t extrap, double w3ratio) {
   if (!c) return NMG_EINVAL;
   if (!c->fv) return set_err(c, NMG_EUNSUP, "nmg_set_fv: the mesh has no finite-volume elements");
@@ -1348,6 +1359,8 @@ int nmg_rhs_vjp(nmg_ctx *c, double t, const double *w_dev, const double *rbar_de
   if (!c || !rbar_dev || !wbar_dev || rbar_dev == wbar_dev)
     return set_err(c, NMG_EINVAL, "nmg_rhs_vjp: need distinct rbar and wbar device buffers");
   if (c->fv) return set_err(c, NMG_EUNSUP, "nmg_rhs_vjp: finite-volume RHS is nonlinear");
+  if (c->numflux != NMG_NUMFLUX_LLF)
+    return set_err(c, NMG_EUNSUP, "nmg_rhs_vjp: the transposed kernel implements LLF only");
   StageParams P = base_params(c);
   P.win = rbar_dev;
   P.rout = wbar_dev;
@@ -1362,6 +1375,8 @@ int nmg_rk4_step_vjp(nmg_ctx *c, double t, double dt, const double *u_n_dev, dou
   (void)u_n_dev;  // linear RHS: the step's Jacobian is P(dt L), independent of u_n
   if (!c || !ubar_dev) return set_err(c, NMG_EINVAL, "nmg_rk4_step_vjp: null argument");
   if (c->fv) return set_err(c, NMG_EUNSUP, "nmg_rk4_step_vjp: finite-volume RHS is nonlinear");
+  if (c->numflux != NMG_NUMFLUX_LLF)
+    return set_err(c, NMG_EUNSUP, "nmg_rk4_step_vjp: the transposed kernel implements LLF only");
   double *acc = c->d_buf[1 - c->cur];  // free between steps
   int rc = step_buffers(c, true, t, dt, ubar_dev, acc, c->d_buf[2], c->d_buf[3]);
   if (rc) return rc;
@@ -1377,6 +1392,8 @@ int nmg_rk4_step_vjp(nmg_ctx *c, double t, double dt, const double *u_n_dev, dou
 int nmg_adjoint_gradient(nmg_ctx *c, double t0, double dt, int32_t nsteps, int32_t ckpt_every,
                          const double *weight_dev, double *J, double *grad_dev) {
   if (c && c->fv) return set_err(c, NMG_EUNSUP, "nmg_adjoint_gradient: finite-volume RHS is nonlinear");
+  if (c && c->numflux != NMG_NUMFLUX_LLF)
+    return set_err(c, NMG_EUNSUP, "nmg_adjoint_gradient: the transposed kernel implements LLF only");
   if (!c || !weight_dev || !J || !grad_dev || nsteps <= 0 || ckpt_every <= 0)
     return set_err(c, NMG_EINVAL, "nmg_adjoint_gradient: bad argument");
   int rc = autotune(c);

@@ -68,6 +68,7 @@ struct StageParams {
   int nfvel;
   const double *ghost;  // [G][4][nn] interpolated traces of faces with code & 64;
                         // slot G = bslot[e*6+f]
+  int numflux;          // NMG_NUMFLUX_LLF or NMG_NUMFLUX_UPWIND
   const double *fvbxyz; // [B][3][nn] outer-face coordinates on equally spaced points
   const double *fvbnrm; // [B][3][nn] outer-face unit normals there
 };
@@ -182,9 +183,17 @@ __device__ __forceinline__ void face_terms(const StageParams &P, const double *s
       double *r2 = sR + (2 * EPB + le) * NP + node;
       double *r3 = sR + (3 * EPB + le) * NP + node;
       *r0 = fma(dcx, gn0, fma(dcy, gn1, fma(dcz, gn2, fma(g, dpi, *r0))));
-      *r1 = fma(dpi, gn0, fma(g, dcx, *r1));
-      *r2 = fma(dpi, gn1, fma(g, dcy, *r2));
-      *r3 = fma(dpi, gn2, fma(g, dcz, *r3));
+      if (P.numflux == NMG_NUMFLUX_UPWIND) {
+        // upwind: only the normal part of the c jump is lifted
+        const double q = dpi + fma(gn0, dcx, fma(gn1, dcy, gn2 * dcz)) / g;
+        *r1 = fma(q, gn0, *r1);
+        *r2 = fma(q, gn1, *r2);
+        *r3 = fma(q, gn2, *r3);
+      } else {
+        *r1 = fma(dpi, gn0, fma(g, dcx, *r1));
+        *r2 = fma(dpi, gn1, fma(g, dcy, *r2));
+        *r3 = fma(dpi, gn2, fma(g, dcz, *r3));
+      }
     }
     __syncthreads();
   }
@@ -258,10 +267,10 @@ __device__ __forceinline__ void face_fetch(const StageParams &P, int e, int f, i
   }
 }
 
-// LLF lift of one face node given the interior state ui: adds to r[0..3]
+// LLF (or upwind) lift of one face node given the interior state ui: adds to r[0..3]
 __device__ __forceinline__ void face_apply(const FaceData &F, double ui0, double ui1, double ui2,
                                            double ui3, double &r0, double &r1, double &r2,
-                                           double &r3) {
+                                           double &r3, int numflux = NMG_NUMFLUX_LLF) {
   double ua0, ua1, ua2, ua3;
   if (F.kind == 0) {
     ua0 = F.v0; ua1 = F.v1; ua2 = F.v2; ua3 = F.v3;
@@ -278,9 +287,16 @@ __device__ __forceinline__ void face_apply(const FaceData &F, double ui0, double
   }
   const double dpi = ua0 - ui0, dcx = ua1 - ui1, dcy = ua2 - ui2, dcz = ua3 - ui3;
   r0 = fma(dcx, F.gn0, fma(dcy, F.gn1, fma(dcz, F.gn2, fma(F.g, dpi, r0))));
-  r1 = fma(dpi, F.gn0, fma(F.g, dcx, r1));
-  r2 = fma(dpi, F.gn1, fma(F.g, dcy, r2));
-  r3 = fma(dpi, F.gn2, fma(F.g, dcz, r3));
+  if (numflux == NMG_NUMFLUX_UPWIND) {
+    const double q = dpi + fma(F.gn0, dcx, fma(F.gn1, dcy, F.gn2 * dcz)) / F.g;
+    r1 = fma(q, F.gn0, r1);
+    r2 = fma(q, F.gn1, r2);
+    r3 = fma(q, F.gn2, r3);
+  } else {
+    r1 = fma(dpi, F.gn0, fma(F.g, dcx, r1));
+    r2 = fma(dpi, F.gn1, fma(F.g, dcy, r2));
+    r3 = fma(dpi, F.gn2, fma(F.g, dcz, r3));
+  }
 }
 
 // r out (mode 0) or RK4 stage update.  r_pi = sR[0] (+ sR[4] + sR[5] for

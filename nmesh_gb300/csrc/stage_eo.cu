@@ -261,7 +261,7 @@ __device__ __forceinline__ void eof_body(const StageParams &P, int blk) {
           double r0 = r[6 * EPB * NP], r1 = r[1 * EPB * NP], r2 = r[2 * EPB * NP],
                  r3 = r[3 * EPB * NP];
           face_apply(side ? FR : FL, w[0], w[EPB * NP], w[2 * EPB * NP], w[3 * EPB * NP], r0,
-                     r1, r2, r3);
+                     r1, r2, r3, P.numflux);
           r[6 * EPB * NP] = r0;
           r[1 * EPB * NP] = r1;
           r[2 * EPB * NP] = r2;

@@ -203,6 +203,67 @@ __device__ __forceinline__ void llf4(const double *ui, const double *ua, const d
   }
 }
 
+// upwind flux (scalarwave1_numflux1d_upwind): R diag(lam+) R^-1 u_in +
+// R diag(lam-) R^-1 u_adj with the characteristic matrices of the normal,
+// evaluated as the matrix products in that order (so that "fvx" stays
+// bit-exact), eigenvalues (1, -1, 0, 0)
+__device__ void upwind4(const double *ui, const double *ua, const double nr[3], double *fn) {
+  const double lam[4] = {1.0, -1.0, 0.0, 0.0};
+  const double nx = nr[0], ny = nr[1], nz = nr[2];
+  double lp[4][4], ln[4][4], ip[4][4], in_[4][4], sp[4][4], sn[4][4], fi[4], fa[4];
+  double R[4][4], Ri[4][4];
+  for (int l = 0; l < 4; l++) {
+    for (int m = 0; m < 4; m++) lp[l][m] = ln[l][m] = ip[l][m] = in_[l][m] = sp[l][m] = sn[l][m] = 0.;
+    fi[l] = fa[l] = 0.;
+  }
+  for (int l = 0; l < 4; l++) {
+    if (lam[l] > 0.) lp[l][l] = lam[l];
+    else ln[l][l] = lam[l];
+  }
+  R[0][0] = 1.0; R[0][1] = 1.0; R[0][2] = 0.0; R[0][3] = 0.0;
+  R[1][0] = -nx; R[1][1] = nx; R[2][0] = -ny; R[2][1] = ny; R[3][0] = -nz; R[3][1] = nz;
+  Ri[0][0] = 1.0 / 2.0; Ri[0][1] = -nx / 2.0; Ri[0][2] = -ny / 2.0; Ri[0][3] = -nz / 2.0;
+  Ri[1][0] = 1.0 / 2.0; Ri[1][1] = nx / 2.0; Ri[1][2] = ny / 2.0; Ri[1][3] = nz / 2.0;
+  Ri[2][0] = 0.0; Ri[3][0] = 0.0;
+  if (nz != 0) {
+    R[1][2] = 0.0; R[1][3] = nz; R[2][2] = nz; R[2][3] = 0.0; R[3][2] = -ny; R[3][3] = -nx;
+    Ri[2][1] = -(nx * ny) / nz; Ri[2][2] = (nx * nx + nz * nz) / nz; Ri[2][3] = -ny;
+    Ri[3][1] = (ny * ny + nz * nz) / nz; Ri[3][2] = -(nx * ny) / nz; Ri[3][3] = -nx;
+  } else if (nx != 0) {
+    R[1][2] = -nz; R[1][3] = -ny; R[2][2] = 0.0; R[2][3] = nx; R[3][2] = nx; R[3][3] = 0.0;
+    Ri[2][1] = -nz; Ri[2][2] = -(ny * nz) / nx; Ri[2][3] = (nx * nx + ny * ny) / nx;
+    Ri[3][1] = -ny; Ri[3][2] = (nx * nx + nz * nz) / nx; Ri[3][3] = -(ny * nz) / nx;
+  } else {
+    R[1][2] = 0.0; R[1][3] = ny; R[2][2] = -nz; R[2][3] = -nx; R[3][2] = ny; R[3][3] = 0.0;
+    Ri[2][1] = -(nx * nz) / ny; Ri[2][2] = -nz; Ri[2][3] = (nx * nx + ny * ny) / ny;
+    Ri[3][1] = (ny * ny + nz * nz) / ny; Ri[3][2] = -nx; Ri[3][3] = -(nx * nz) / ny;
+  }
+  for (int l = 0; l < 4; l++)
+    for (int m = 0; m < 4; m++)
+      for (int q = 0; q < 4; q++) {
+        ip[l][m] += lp[l][q] * Ri[q][m];
+        in_[l][m] += ln[l][q] * Ri[q][m];
+      }
+  for (int l = 0; l < 4; l++)
+    for (int m = 0; m < 4; m++)
+      for (int q = 0; q < 4; q++) {
+        sp[l][m] += R[l][q] * ip[q][m];
+        sn[l][m] += R[l][q] * in_[q][m];
+      }
+  for (int l = 0; l < 4; l++)
+    for (int m = 0; m < 4; m++) {
+      fi[l] += sp[l][m] * ui[m];
+      fa[l] += sn[l][m] * ua[m];
+    }
+  for (int l = 0; l < 4; l++) fn[l] = fi[l] + fa[l];
+}
+
+__device__ __forceinline__ void numflux4(int kind, const double *ui, const double *ua,
+                                         const double nr[3], double *fn) {
+  if (kind == NMG_NUMFLUX_UPWIND) upwind4(ui, ua, nr, fn);
+  else llf4(ui, ua, nr, fn);
+}
+
 // LLF flux f* through face f at face node (a, b) of element e with interior
 // state ui (scalarwave1_fluxes_pt: neighbour trace, exact plane wave or the
 // outgoing-radiation exterior state)
@@ -246,7 +307,7 @@ __device__ void face_fnum(const StageParams &P, int e, int f, int a, int b, cons
       for (int l = 0; l < 3; l++) ua[1 + l] = ui[1 + l] + (cne - cnv) * nr[l];
     }
   }
-  llf4(ui, ua, nr, fn);
+  numflux4(P.numflux, ui, ua, nr, fn);
 }
 
 // J sqrtgdiag / dXb factors of node i0 of a pencil (fv.c:384-411)
@@ -325,7 +386,7 @@ __global__ void __launch_bounds__(NT) fv_kernel(const StageParams P) {
       }
       double nr[3], fn[4];
       normal_at(P, G, np, d, base + im * st, nr);
-      llf4(ui, ua, nr, fn);
+      numflux4(P.numflux, ui, ua, nr, fn);
 #pragma unroll
       for (int l = 0; l < 4; l++) sF[(l * nm + im) * nn + Pn] = fn[l];
     }

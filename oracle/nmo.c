@@ -19,6 +19,7 @@
  *   face fluxes          src/tests/scalarwave1/scalarwave1.c:139-209
  *   exact plane wave     src/tests/scalarwave1/scalarwave1.c:503-524
  *   LLF                  src/main/dg/numflux1d.c:85-112
+ *   upwind flux          src/tests/scalarwave1/scalarwave1.c:323-499
  *   surface flux + lift  src/main/dg/dg.c:30-151
  *   node normals         src/main/coordinates/utilities.c:48-88
  *   sqrtgdiag            src/main/coordinates/coordinates.c:728-800
@@ -85,6 +86,7 @@ typedef struct nmo_mesh {
   double fv_w3ratio;        /* par fv_WENOm3_opt_weightratio (default 2) */
   const int32_t *mixface;   /* [e][6][3] (e', f', orientation) of the faces
                                marked -2 in nbnode; NULL if none */
+  int numflux;              /* 0: LLF, 1: upwind (par scalarwave1_numflux) */
 } nmo_mesh;
 
 /* points of both point types: LGL (DG) with their Lagrange weights, and
@@ -207,6 +209,75 @@ static void llf(const double *ui, const double *ua, const double *fi,
   amax = fmax(ami, apl);
   for (l = 0; l < NF; l++)
     fnum[l] = 0.5 * (fa[l] + fi[l] - amax * (ua[l] - ui[l]));
+}
+
+/* Upwind flux of the first-order wave (scalarwave1_numflux1d_upwind):
+   f* = R diag(lam+) R^-1 u_in + R diag(lam-) R^-1 u_adj over (pi, c) with
+   the characteristic matrices R, R^-1 of the face normal (three forms,
+   chosen by which normal component is nonzero), evaluated as matrix
+   products in that order; f*_phi = 0.  Eigenvalues (1, -1, 0, 0). */
+static void upwind(const double *ui, const double *ua, const double nrm[3], double *fnum)
+{
+  const double lam[4] = {1.0, -1.0, 0.0, 0.0};
+  const double nx = nrm[0], ny = nrm[1], nz = nrm[2];
+  double lp[4][4], ln[4][4], ip[4][4], in_[4][4], sp[4][4], sn[4][4], fi[4], fa[4];
+  double R[4][4], Ri[4][4];
+  int l, m, q;
+  for (l = 0; l < 4; l++) {
+    for (m = 0; m < 4; m++) lp[l][m] = ln[l][m] = ip[l][m] = in_[l][m] = sp[l][m] = sn[l][m] = 0.;
+    fi[l] = fa[l] = 0.;
+  }
+  for (l = 0; l < 4; l++) {
+    if (lam[l] > 0.) lp[l][l] = lam[l];
+    else ln[l][l] = lam[l];
+  }
+  if (nz != 0) {
+    double A[4][4] = {{1.0, 1.0, 0.0, 0.0}, {-nx, nx, 0.0, nz}, {-ny, ny, nz, 0.0},
+                      {-nz, nz, -ny, -nx}};
+    double B[4][4] = {{1.0 / 2.0, -nx / 2.0, -ny / 2.0, -nz / 2.0},
+                      {1.0 / 2.0, nx / 2.0, ny / 2.0, nz / 2.0},
+                      {0.0, -(nx * ny) / nz, (nx * nx + nz * nz) / nz, -ny},
+                      {0.0, (ny * ny + nz * nz) / nz, -(nx * ny) / nz, -nx}};
+    memcpy(R, A, sizeof R);
+    memcpy(Ri, B, sizeof Ri);
+  } else if (nx != 0) {
+    double A[4][4] = {{1.0, 1.0, 0.0, 0.0}, {-nx, nx, -nz, -ny}, {-ny, ny, 0.0, nx},
+                      {-nz, nz, nx, 0.0}};
+    double B[4][4] = {{1.0 / 2.0, -nx / 2.0, -ny / 2.0, -nz / 2.0},
+                      {1.0 / 2.0, nx / 2.0, ny / 2.0, nz / 2.0},
+                      {0.0, -nz, -(ny * nz) / nx, (nx * nx + ny * ny) / nx},
+                      {0.0, -ny, (nx * nx + nz * nz) / nx, -(ny * nz) / nx}};
+    memcpy(R, A, sizeof R);
+    memcpy(Ri, B, sizeof Ri);
+  } else {
+    double A[4][4] = {{1.0, 1.0, 0.0, 0.0}, {-nx, nx, 0.0, ny}, {-ny, ny, -nz, -nx},
+                      {-nz, nz, ny, 0.0}};
+    double B[4][4] = {{1.0 / 2.0, -nx / 2.0, -ny / 2.0, -nz / 2.0},
+                      {1.0 / 2.0, nx / 2.0, ny / 2.0, nz / 2.0},
+                      {0.0, -(nx * nz) / ny, -nz, (nx * nx + ny * ny) / ny},
+                      {0.0, (ny * ny + nz * nz) / ny, -nx, -(nx * nz) / ny}};
+    memcpy(R, A, sizeof R);
+    memcpy(Ri, B, sizeof Ri);
+  }
+  for (l = 0; l < 4; l++)
+    for (m = 0; m < 4; m++)
+      for (q = 0; q < 4; q++) {
+        ip[l][m] += lp[l][q] * Ri[q][m];
+        in_[l][m] += ln[l][q] * Ri[q][m];
+      }
+  for (l = 0; l < 4; l++)
+    for (m = 0; m < 4; m++)
+      for (q = 0; q < 4; q++) {
+        sp[l][m] += R[l][q] * ip[q][m];
+        sn[l][m] += R[l][q] * in_[q][m];
+      }
+  for (l = 0; l < 4; l++)
+    for (m = 0; m < 4; m++) {
+      fi[l] += sp[l][m] * ui[m];
+      fa[l] += sn[l][m] * ua[m];
+    }
+  for (l = 0; l < 4; l++) fnum[l] = fi[l] + fa[l];
+  fnum[4] = 0.;
 }
 
 /* out = D_dir applied to in along direction dir (array.c MM_SET_AB order) */
@@ -409,7 +480,8 @@ static void face_fnum(const nmo_mesh *m, const nmo_pts *P, int e, int f, int ijk
   }
   flux1d(fi, norm, ui);
   flux1d(fa, norm, ua);
-  llf(ui, ua, fi, fa, fnum);
+  if (m->numflux == 1) upwind(ui, ua, norm, fnum);
+  else llf(ui, ua, fi, fa, fnum);
 }
 
 /* RHS of one element: r[e] = RHS(w) at time t.  tmp holds 18*np doubles. */
@@ -696,7 +768,8 @@ static void rhs_elem_fv(const nmo_mesh *m, const nmo_pts *P, double t,
             }
             flux1d(fi, norm, ui);
             flux1d(fa, norm, ua);
-            llf(ui, ua, fi, fa, fn);
+            if (m->numflux == 1) upwind(ui, ua, norm, fn);
+            else llf(ui, ua, fi, fa, fn);
             for (l = 0; l < 4; l++) fnumR[l] = fn[l];
           } else if (addsurf) {
             double fi[5], fn[5];

@@ -39,7 +39,8 @@ class _Mesh(ctypes.Structure):
                 ("nbnode", ctypes.c_void_p), ("bc", ctypes.c_int),
                 ("k", ctypes.c_double * 3), ("fv", ctypes.c_void_p),
                 ("fv_rec", ctypes.c_int), ("fv_extrap", ctypes.c_int),
-                ("fv_w3ratio", ctypes.c_double), ("mixface", ctypes.c_void_p)]
+                ("fv_w3ratio", ctypes.c_double), ("mixface", ctypes.c_void_p),
+                ("numflux", ctypes.c_int)]
 
 # reconstruction modes (reference par fv_rec) and div(f) extrapolation
 # modes (par fv_divf_extrap) understood by the oracle
@@ -192,10 +193,11 @@ class OracleMesh:
 
     def __init__(self, bbox, curvi, dXdx, xyz, nbnode, n, bc=0,
                  k=(1.0, 1.0, 1.0), fv=None, fv_rec="WENOm5_2",
-                 fv_extrap="dnfn_extrap1", fv_w3ratio=2.0, mixface=None):
+                 fv_extrap="dnfn_extrap1", fv_w3ratio=2.0, mixface=None, numflux="LLF"):
         """fv: per-element finite-volume flags (None: all DG); fv_rec and
         fv_extrap name the reference's fv_rec / fv_divf_extrap modes;
-        mixface: faces between the two point types (see match_faces)."""
+        mixface: faces between the two point types (see match_faces);
+        numflux: "LLF" or "upwind" (the reference's scalarwave1_numflux)."""
         self.n = int(n)
         self.bbox = np.ascontiguousarray(bbox, np.float64)
         self.curvi = np.ascontiguousarray(curvi, np.int32)
@@ -211,7 +213,8 @@ class OracleMesh:
                        (ctypes.c_double * 3)(*k),
                        None if self.fv is None else self.fv.ctypes.data,
                        FV_REC[fv_rec], FV_EXTRAP[fv_extrap], float(fv_w3ratio),
-                       None if self.mixface is None else self.mixface.ctypes.data)
+                       None if self.mixface is None else self.mixface.ctypes.data,
+                       1 if numflux == "upwind" else 0)
 
     def rhs(self, w, t=0.0):
         w = np.ascontiguousarray(w, np.float64)

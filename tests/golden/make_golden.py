@@ -82,6 +82,18 @@ CASES = {
                                dt=0.002, steps=1, eps=0.05, seed=31, norms=True,
                                fv=dict(rec="WENOm3_2", extrap="dnfn_extrap1",
                                        patches="0")),
+    # the reference's default numerical flux (scalarwave1_numflux = upwind)
+    "upw_cs7_l1_n5": dict(mesh="cs7", n=5, luni=1, k=(0.3, -0.2, 0.1),
+                          dt=0.004, steps=2, eps=0.02, seed=32, numflux="upwind"),
+    "upw_box_l1_n6": dict(mesh="box", n=6, luni=1, k=(1.0, -0.5, 0.25),
+                          dt=0.01, steps=2, eps=0.05, seed=33, numflux="upwind"),
+    "upw_mixcs7_l0_n7_w5dnfn": dict(mesh="cs7", n=7, luni=0, k=(0.3, -0.2, 0.1),
+                                    dt=0.002, steps=2, eps=0.02, seed=34, numflux="upwind",
+                                    fv=dict(rec="WENOm5_2", extrap="dnfn_extrap1",
+                                            patches="0")),
+    "upw_fvbox_l1_n7_w5no": dict(mesh="box", n=7, luni=1, k=(1.0, 1.0, 1.0),
+                                 dt=0.005, steps=2, eps=0.05, seed=35, numflux="upwind",
+                                 fv=dict(rec="WENOm5_2", extrap="no")),
 }
 
 
@@ -95,7 +107,7 @@ def parfile(case, prefix):
         f"amr_luni = {c['luni']}",
         f"amr_n0 = {c['n']}", f"amr_n1 = {c['n']}", f"amr_n2 = {c['n']}",
         "scalarwave1_k = %r %r %r" % tuple(c["k"]),
-        "scalarwave1_numflux = LLF",
+        f"scalarwave1_numflux = {c.get('numflux', 'LLF')}",
         f"nmgdump_prefix = {prefix}",
         "nmgdump_amp = 1.0",
         f"nmgdump_perturb = {c['eps']!r}",

@@ -14,6 +14,8 @@ FV_CASES = ["fvbox_l1_n7_w5no", "fvbox_l1_n7_w5dnfn", "fvbox_l2_n5_w3dnfn",
             "fvbox_l0_n13_w5dnfn", "fvcs7_l0_n7_w5dnfn", "fvcs7_l0_n6_w5no"]
 # mixed fixtures: inner cube finite-volume, cubed-sphere shells DG
 MIX_CASES = ["mixcs7_l0_n7_w5dnfn", "mixcs7_l1_n5_w3no"]
+# the reference's default upwind flux (DG, mixed, finite volume)
+UPW_CASES = ["upw_cs7_l1_n5", "upw_box_l1_n6", "upw_mixcs7_l0_n7_w5dnfn", "upw_fvbox_l1_n7_w5no"]
 
 # relative L2 tolerance of the CUDA path against the reference / oracle for
 # one RHS evaluation and for a few RK4 steps (FP64; FMA contraction and a
@@ -58,7 +60,7 @@ def rel_l2(a, b):
 
 
 def oracle_for(mesh, bc=0, k=(1.0, 1.0, 1.0), period=None, fv_rec="WENOm3_2",
-               fv_extrap="dnfn_extrap1", fv_w3ratio=2.0):
+               fv_extrap="dnfn_extrap1", fv_w3ratio=2.0, numflux="LLF"):
     """Oracle mesh built from the product mesh's geometry, with its own
     coordinate-matching neighbour table (and the mesh's finite-volume flags
     with the given fin.-vol. options)."""
@@ -77,7 +79,8 @@ def oracle_for(mesh, bc=0, k=(1.0, 1.0, 1.0), period=None, fv_rec="WENOm3_2",
         nb = nmo.match_faces(xyz, mesh.n, period=period)
     return nmo.OracleMesh(bbox, curvi, dXdx, xyz, nb, mesh.n, bc=bc, k=k,
                           fv=fv if fv.any() else None, fv_rec=fv_rec,
-                          fv_extrap=fv_extrap, fv_w3ratio=fv_w3ratio, mixface=mix)
+                          fv_extrap=fv_extrap, fv_w3ratio=fv_w3ratio, mixface=mix,
+                          numflux=numflux)
 
 
 def gaussian_pulses(xyz, seed, npulse=8, rmin=3.0, rmax=10.0, wmin=0.5, wmax=2.0,

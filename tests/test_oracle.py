@@ -5,7 +5,7 @@ operation order and must match it bit for bit."""
 import numpy as np
 import pytest
 
-from helpers import CASES, FV_CASES, MIX_CASES, load
+from helpers import CASES, FV_CASES, MIX_CASES, UPW_CASES, load
 from oracle import nmo
 
 
@@ -21,7 +21,7 @@ def _oracle_mesh(d, meta):
     else:
         nb = nmo.match_faces(d["x"], n)
     return nmo.OracleMesh(d["bbox"], curvi, d["dXdx"], d["x"], nb, n, bc=0,
-                          k=meta["k"], **fv)
+                          k=meta["k"], numflux=meta.get("numflux", "LLF"), **fv)
 
 
 @pytest.mark.parametrize("case", CASES + FV_CASES)
@@ -40,7 +40,7 @@ def test_oracle_rk4_bitexact(case):
     assert np.array_equal(u, d["u_final"])
 
 
-@pytest.mark.parametrize("case", MIX_CASES)
+@pytest.mark.parametrize("case", MIX_CASES + UPW_CASES)
 def test_oracle_mixed_dg_fv_bitexact(case):
     """Mixed DG / finite-volume meshes (inner cube FV, shells DG): the
     interface traces are interpolated at the face points (Lagrange from the
