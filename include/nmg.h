@@ -215,6 +215,18 @@ int nmg_grhd_prim2con(const nmg_grhd_params *g, int64_t npts, const double *psi_
                       const double *prim_dev, double *cons_dev, void *stream);
 int nmg_grhd_con2prim(const nmg_grhd_params *g, int64_t npts, const double *psi_dev,
                       double *cons_dev, double *prim_dev, int32_t *status_dev, void *stream);
+/* Valencia fluxes along direction dir of the densitized conserved variables
+ * (flux [5][npts]) and the characteristic speeds (lam [2][npts]: lambda_-,
+ * lambda_+) on the static background ds^2 = -alpha^2 dt^2 + psi^4 dx^2
+ * (alpha, psi may be NULL: 1) */
+int nmg_grhd_fluxes(const nmg_grhd_params *g, int64_t npts, int32_t dir, const double *alpha_dev,
+                    const double *psi_dev, const double *prim_dev, double *flux_dev,
+                    double *lam_dev, void *stream);
+/* Cowling source terms [5][npts] (0 for D) from alpha, psi and their
+ * gradients dalpha, dpsi [3][npts] */
+int nmg_grhd_sources(const nmg_grhd_params *g, int64_t npts, const double *alpha_dev,
+                     const double *psi_dev, const double *dalpha_dev, const double *dpsi_dev,
+                     const double *prim_dev, double *src_dev, void *stream);
 
 /* numerical flux of a context (default NMG_NUMFLUX_LLF, what the workloads
  * use); the adjoint entry points support LLF only */

@@ -86,6 +86,28 @@ def grhd_con2prim_device(params, npts, psi_ptr, cons_ptr, prim_ptr, status_ptr, 
         raise NmgError(f"nmg_grhd_con2prim failed ({rc})")
 
 
+def grhd_fluxes_device(params, npts, d, alpha_ptr, psi_ptr, prim_ptr, flux_ptr, lam_ptr,
+                       stream=0):
+    """Valencia fluxes along d and characteristic speeds (include/nmg.h)."""
+    rc = lib().nmg_grhd_fluxes(ctypes.byref(params), int(npts), int(d),
+                               ctypes.c_void_p(alpha_ptr or None), ctypes.c_void_p(psi_ptr or None),
+                               ctypes.c_void_p(prim_ptr), ctypes.c_void_p(flux_ptr),
+                               ctypes.c_void_p(lam_ptr), ctypes.c_void_p(stream or None))
+    if rc:
+        raise NmgError(f"nmg_grhd_fluxes failed ({rc})")
+
+
+def grhd_sources_device(params, npts, alpha_ptr, psi_ptr, dalpha_ptr, dpsi_ptr, prim_ptr,
+                        src_ptr, stream=0):
+    """Cowling source terms (include/nmg.h)."""
+    rc = lib().nmg_grhd_sources(ctypes.byref(params), int(npts), ctypes.c_void_p(alpha_ptr),
+                                ctypes.c_void_p(psi_ptr), ctypes.c_void_p(dalpha_ptr),
+                                ctypes.c_void_p(dpsi_ptr), ctypes.c_void_p(prim_ptr),
+                                ctypes.c_void_p(src_ptr), ctypes.c_void_p(stream or None))
+    if rc:
+        raise NmgError(f"nmg_grhd_sources failed ({rc})")
+
+
 class _MeshDesc(ctypes.Structure):
     _fields_ = [("nelem", ctypes.c_int32), ("n", ctypes.c_int32),
                 ("pat", ctypes.c_void_p), ("bbox", ctypes.c_void_p),
@@ -165,6 +187,8 @@ def lib(build_if_missing=True):
         "nmg_set_numflux": (ctypes.c_int, [vp, i32]),
         "nmg_grhd_prim2con": (ctypes.c_int, [vp, i64, vp, vp, vp, vp]),
         "nmg_grhd_con2prim": (ctypes.c_int, [vp, i64, vp, vp, vp, vp, vp]),
+        "nmg_grhd_fluxes": (ctypes.c_int, [vp, i64, i32, vp, vp, vp, vp, vp, vp]),
+        "nmg_grhd_sources": (ctypes.c_int, [vp, i64, vp, vp, vp, vp, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

@@ -13,8 +13,10 @@
 // (f'(p) ~ v^2 c_s^2 - 1), with the previous pressure as the starting guess,
 // and sets the atmosphere (rho_atm, v = 0, p_atm; conserved variables reset)
 // where D/psi^6 < rho_atm or the root finder fails.  Every iteration loop
-// is bounded (maxits, 200 bracket doublings).  This file is compiled with
-// -fmad=false so that it rounds like the host restatement.
+// is bounded (maxits, 200 bracket doublings).  With a lapse alpha (static
+// background, zero shift) it also gives the Valencia fluxes, the
+// characteristic speeds and the Cowling source terms.  This file is
+// compiled with -fmad=false so that it rounds like the host restatement.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -170,6 +172,66 @@ __global__ void con2prim_kernel(nmg_grhd_params g, int64_t npts, const double *p
   }
 }
 
+// Valencia fluxes along direction d and the characteristic speeds there
+// (static conformally flat background, zero shift)
+__global__ void fluxes_kernel(nmg_grhd_params g, int64_t npts, int d, const double *alpha,
+                              const double *psi, const double *prim, double *flux, double *lam) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < npts;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double al = alpha ? alpha[i] : 1., ps = psi ? psi[i] : 1.;
+    const double ps4 = ps * ps * ps * ps, ps6 = ps4 * ps * ps;
+    const double rho = prim[i];
+    const double v[3] = {prim[npts + i], prim[2 * npts + i], prim[3 * npts + i]};
+    const double p = prim[4 * npts + i];
+    const double v2 = ps4 * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    const double W = 1. / sqrt(1. - v2);
+    const double eps = p / ((g.gamma - 1.) * rho);
+    const double h = 1. + eps + p / rho;
+    const double rhW2 = rho * h * W * W;
+    const double D = ps6 * rho * W, tau = ps6 * (rhW2 - p) - D, avd = al * v[d];
+    const double cs2 = g.gamma * p / (rho * h);
+    double disc = (1. - v2) * (1. / ps4 * (1. - v2 * cs2) - v[d] * v[d] * (1. - cs2));
+    const double fac = al / (1. - v2 * cs2);
+    flux[i] = avd * D;
+    for (int j = 0; j < 3; j++) {
+      const double Sj = ps6 * rhW2 * ps4 * v[j];
+      flux[(1 + j) * npts + i] = avd * Sj + (j == d ? al * ps6 * p : 0.);
+    }
+    flux[4 * npts + i] = avd * tau + al * ps6 * p * v[d];
+    if (disc < 0.) disc = 0.;
+    lam[i] = fac * (v[d] * (1. - cs2) - sqrt(cs2) * sqrt(disc));
+    lam[npts + i] = fac * (v[d] * (1. - cs2) + sqrt(cs2) * sqrt(disc));
+  }
+}
+
+// Cowling source terms of S_j and tau (D has none)
+__global__ void sources_kernel(nmg_grhd_params g, int64_t npts, const double *alpha,
+                               const double *psi, const double *dalpha, const double *dpsi,
+                               const double *prim, double *src) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < npts;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double al = alpha[i], ps = psi[i];
+    const double ps4 = ps * ps * ps * ps, ps6 = ps4 * ps * ps;
+    const double rho = prim[i];
+    const double v[3] = {prim[npts + i], prim[2 * npts + i], prim[3 * npts + i]};
+    const double p = prim[4 * npts + i];
+    const double v2 = ps4 * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    const double W = 1. / sqrt(1. - v2);
+    const double eps = p / ((g.gamma - 1.) * rho);
+    const double h = 1. + eps + p / rho;
+    const double rhW2 = rho * h * W * W;
+    const double E = rhW2 - p;
+    double vda = 0.;
+    src[i] = 0.;
+    for (int j = 0; j < 3; j++) {
+      const double da = dalpha[j * npts + i], dp = dpsi[j * npts + i];
+      src[(1 + j) * npts + i] = ps6 * (2. * al * (dp / ps) * (rhW2 * v2 + 3. * p) - E * da);
+      vda += v[j] * da;
+    }
+    src[4 * npts + i] = -ps6 * rhW2 * vda;
+  }
+}
+
 bool bad_params(const nmg_grhd_params *g) {
   return !g || !(g->gamma > 1.) || !(g->rho_atm > 0.) || !(g->p_atm > 0.) || !(g->tol > 0.) ||
          g->maxits <= 0 || g->maxits > 100000;
@@ -196,6 +258,32 @@ int nmg_grhd_con2prim(const nmg_grhd_params *g, int64_t npts, const double *psi_
   const int grid = (int)std::min<int64_t>((npts + 127) / 128, 152 * 32);
   con2prim_kernel<<<grid, 128, 0, (cudaStream_t)stream>>>(*g, npts, psi_dev, cons_dev, prim_dev,
                                                           status_dev);
+  return cudaGetLastError() == cudaSuccess ? NMG_OK : NMG_ECUDA;
+}
+
+int nmg_grhd_fluxes(const nmg_grhd_params *g, int64_t npts, int32_t dir, const double *alpha_dev,
+                    const double *psi_dev, const double *prim_dev, double *flux_dev,
+                    double *lam_dev, void *stream) {
+  if (bad_params(g) || npts < 0 || dir < 0 || dir > 2 ||
+      (npts > 0 && (!prim_dev || !flux_dev || !lam_dev)))
+    return NMG_EINVAL;
+  if (npts == 0) return NMG_OK;
+  const int grid = (int)std::min<int64_t>((npts + 255) / 256, 152 * 32);
+  fluxes_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(*g, npts, dir, alpha_dev, psi_dev,
+                                                        prim_dev, flux_dev, lam_dev);
+  return cudaGetLastError() == cudaSuccess ? NMG_OK : NMG_ECUDA;
+}
+
+int nmg_grhd_sources(const nmg_grhd_params *g, int64_t npts, const double *alpha_dev,
+                     const double *psi_dev, const double *dalpha_dev, const double *dpsi_dev,
+                     const double *prim_dev, double *src_dev, void *stream) {
+  if (bad_params(g) || npts < 0 ||
+      (npts > 0 && (!alpha_dev || !psi_dev || !dalpha_dev || !dpsi_dev || !prim_dev || !src_dev)))
+    return NMG_EINVAL;
+  if (npts == 0) return NMG_OK;
+  const int grid = (int)std::min<int64_t>((npts + 255) / 256, 152 * 32);
+  sources_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(*g, npts, alpha_dev, psi_dev,
+                                                         dalpha_dev, dpsi_dev, prim_dev, src_dev);
   return cudaGetLastError() == cudaSuccess ? NMG_OK : NMG_ECUDA;
 }
 

@@ -1214,3 +1214,70 @@ void nmo_grhd_con2prim(const nmo_grhd *g, int64_t npts, const double *psi, doubl
     status[i] = rc;
   }
 }
+
+/* Valencia fluxes, characteristic speeds and Cowling sources on a static
+   conformally flat background ds^2 = -alpha^2 dt^2 + psi^4 dx^2 (zero
+   shift), from primitives (rho, v^i, p):
+     F^d(D) = alpha v^d D, F^d(S_j) = alpha v^d S_j + alpha psi^6 p delta^d_j,
+     F^d(tau) = alpha v^d tau + alpha psi^6 p v^d  (densitized D, S_j, tau);
+     S(S_j) = psi^6 [2 alpha (d_j psi / psi)(rho h W^2 v^2 + 3 p) - E d_j alpha],
+     S(tau) = -psi^6 rho h W^2 v^j d_j alpha,  E = rho h W^2 - p;
+   speeds along d: lambda_pm = alpha/(1 - v^2 c_s^2) [v^d (1 - c_s^2) pm
+     c_s sqrt((1 - v^2)(psi^-4 (1 - v^2 c_s^2) - v^d v^d (1 - c_s^2)))].
+   (restated; the reference has no GRHD) */
+void nmo_grhd_fluxes(const nmo_grhd *g, int64_t npts, int d, const double *alpha,
+                     const double *psi, const double *prim, double *flux, double *lam)
+{
+  int64_t i;
+  for (i = 0; i < npts; i++) {
+    double al = alpha ? alpha[i] : 1., ps = psi ? psi[i] : 1.;
+    double ps4 = ps * ps * ps * ps, ps6 = ps4 * ps * ps;
+    double rho = prim[i], v[3] = {prim[npts + i], prim[2 * npts + i], prim[3 * npts + i]};
+    double p = prim[4 * npts + i];
+    double v2 = ps4 * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    double W = 1. / sqrt(1. - v2);
+    double eps = p / ((g->gamma - 1.) * rho);
+    double h = 1. + eps + p / rho;
+    double rhW2 = rho * h * W * W;
+    double D = ps6 * rho * W, tau = ps6 * (rhW2 - p) - D, avd = al * v[d];
+    double cs2 = g->gamma * p / (rho * h);
+    double disc = (1. - v2) * (1. / ps4 * (1. - v2 * cs2) - v[d] * v[d] * (1. - cs2));
+    double fac = al / (1. - v2 * cs2);
+    int j;
+    flux[i] = avd * D;
+    for (j = 0; j < 3; j++) {
+      double Sj = ps6 * rhW2 * ps4 * v[j];
+      flux[(1 + j) * npts + i] = avd * Sj + (j == d ? al * ps6 * p : 0.);
+    }
+    flux[4 * npts + i] = avd * tau + al * ps6 * p * v[d];
+    if (disc < 0.) disc = 0.;
+    lam[i] = fac * (v[d] * (1. - cs2) - sqrt(cs2) * sqrt(disc));
+    lam[npts + i] = fac * (v[d] * (1. - cs2) + sqrt(cs2) * sqrt(disc));
+  }
+}
+
+void nmo_grhd_sources(const nmo_grhd *g, int64_t npts, const double *alpha, const double *psi,
+                      const double *dalpha, const double *dpsi, const double *prim, double *src)
+{
+  int64_t i;
+  for (i = 0; i < npts; i++) {
+    double al = alpha[i], ps = psi[i];
+    double ps4 = ps * ps * ps * ps, ps6 = ps4 * ps * ps;
+    double rho = prim[i], v[3] = {prim[npts + i], prim[2 * npts + i], prim[3 * npts + i]};
+    double p = prim[4 * npts + i];
+    double v2 = ps4 * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    double W = 1. / sqrt(1. - v2);
+    double eps = p / ((g->gamma - 1.) * rho);
+    double h = 1. + eps + p / rho;
+    double rhW2 = rho * h * W * W;
+    double E = rhW2 - p, vda = 0.;
+    int j;
+    src[i] = 0.;
+    for (j = 0; j < 3; j++) {
+      double da = dalpha[j * npts + i], dp = dpsi[j * npts + i];
+      src[(1 + j) * npts + i] = ps6 * (2. * al * (dp / ps) * (rhW2 * v2 + 3. * p) - E * da);
+      vda += v[j] * da;
+    }
+    src[4 * npts + i] = -ps6 * rhW2 * vda;
+  }
+}

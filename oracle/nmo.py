@@ -309,3 +309,33 @@ def grhd_con2prim(cons, prim_guess, psi=None, gamma=2.0, rho_atm=1e-12, p_atm=1e
                             prim.ctypes.data_as(ctypes.c_void_p),
                             st.ctypes.data_as(ctypes.c_void_p))
     return prim, cons, st
+
+
+def grhd_fluxes(prim, d, alpha=None, psi=None, gamma=2.0):
+    prim = np.ascontiguousarray(prim, np.float64)
+    npts = prim.shape[1]
+    flux = np.zeros_like(prim)
+    lam = np.zeros((2, npts))
+    g = _Grhd(gamma, 1e-12, 1e-14, 1e-15, 100)
+    a = None if alpha is None else np.ascontiguousarray(alpha, np.float64)
+    ps = None if psi is None else np.ascontiguousarray(psi, np.float64)
+    lib().nmo_grhd_fluxes(ctypes.byref(g), ctypes.c_int64(npts), ctypes.c_int(d),
+                          None if a is None else a.ctypes.data_as(ctypes.c_void_p),
+                          None if ps is None else ps.ctypes.data_as(ctypes.c_void_p),
+                          prim.ctypes.data_as(ctypes.c_void_p),
+                          flux.ctypes.data_as(ctypes.c_void_p),
+                          lam.ctypes.data_as(ctypes.c_void_p))
+    return flux, lam
+
+
+def grhd_sources(prim, alpha, psi, dalpha, dpsi, gamma=2.0):
+    prim = np.ascontiguousarray(prim, np.float64)
+    npts = prim.shape[1]
+    src = np.zeros_like(prim)
+    g = _Grhd(gamma, 1e-12, 1e-14, 1e-15, 100)
+    arrs = [np.ascontiguousarray(x, np.float64) for x in (alpha, psi, dalpha, dpsi)]
+    lib().nmo_grhd_sources(ctypes.byref(g), ctypes.c_int64(npts),
+                           *[x.ctypes.data_as(ctypes.c_void_p) for x in arrs],
+                           prim.ctypes.data_as(ctypes.c_void_p),
+                           src.ctypes.data_as(ctypes.c_void_p))
+    return src

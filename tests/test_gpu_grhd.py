@@ -68,3 +68,31 @@ def test_gpu_grhd_rejects_bad_params():
     with pytest.raises(ng.NmgError):
         ng.grhd_con2prim_device(ng.GrhdParams(maxits=0), 2, 0, d.data_ptr(), d.data_ptr(),
                                 d.data_ptr())
+
+
+def test_gpu_grhd_fluxes_sources_bitexact_vs_oracle():
+    n = 5000
+    rng = np.random.default_rng(21)
+    prim = random_prims(n, seed=22)
+    psi = rng.uniform(1.0, 1.4, n)
+    prim[1:4] /= psi ** 2
+    alpha = rng.uniform(0.4, 1.0, n)
+    da = rng.normal(size=(3, n))
+    dp = rng.normal(size=(3, n))
+    g = ng.GrhdParams()
+    dprim, dpsi_, dal = _dev(prim), _dev(psi), _dev(alpha)
+    dflux = torch.zeros_like(dprim)
+    dlam = torch.zeros(2 * n, dtype=torch.float64, device="cuda")
+    for d in range(3):
+        ng.grhd_fluxes_device(g, n, d, dal.data_ptr(), dpsi_.data_ptr(), dprim.data_ptr(),
+                              dflux.data_ptr(), dlam.data_ptr())
+        torch.cuda.synchronize()
+        fo, lo = nmo.grhd_fluxes(prim, d, alpha, psi)
+        assert np.array_equal(dflux.cpu().numpy(), fo)
+        assert np.array_equal(dlam.cpu().numpy().reshape(2, n), lo)
+    dsrc = torch.zeros_like(dprim)
+    dda, ddp = _dev(da), _dev(dp)      # kept alive until the kernel has run
+    ng.grhd_sources_device(g, n, dal.data_ptr(), dpsi_.data_ptr(), dda.data_ptr(),
+                           ddp.data_ptr(), dprim.data_ptr(), dsrc.data_ptr())
+    torch.cuda.synchronize()
+    assert np.array_equal(dsrc.cpu().numpy(), nmo.grhd_sources(prim, alpha, psi, da, dp))

@@ -89,3 +89,45 @@ def test_oracle_grhd_atmosphere():
         assert got[0, i] == 1e-12 and got[4, i] == 1e-14 and not got[1:4, i].any()
         assert cons2[0, i] == 1e-12 and not cons2[1:4, i].any()
     assert (st[4:] >= 0).all()
+
+
+def test_oracle_grhd_fluxes_and_speeds():
+    n = 2000
+    prim = random_prims(n, seed=8)
+    for d in range(3):
+        flux, lam = nmo.grhd_fluxes(prim, d)
+        cons = nmo.grhd_prim2con(prim)
+        # F^d = v^d U (+ pressure terms) in flat space with alpha = 1
+        assert np.allclose(flux[0], prim[1 + d] * cons[0], rtol=1e-14, atol=0)
+        assert np.allclose(flux[4], prim[1 + d] * cons[4] + prim[4] * prim[1 + d],
+                           rtol=1e-13, atol=1e-300)
+        # subluminal, ordered, around the flow velocity
+        assert (np.abs(lam) < 1).all() and (lam[0] <= prim[1 + d]).all()
+        assert (lam[1] >= prim[1 + d]).all()
+    # fluid at rest: lambda = -+ c_s
+    rest = prim.copy()
+    rest[1:4] = 0.0
+    _, lam = nmo.grhd_fluxes(rest, 0)
+    eps = rest[4] / rest[0]          # gamma = 2: p = rho eps
+    cs = np.sqrt(2.0 * rest[4] / (rest[0] * (1.0 + eps + rest[4] / rest[0])))
+    assert np.allclose(lam[1], cs, rtol=1e-13) and np.allclose(lam[0], -cs, rtol=1e-13)
+
+
+def test_oracle_grhd_sources_static_fluid():
+    """A static fluid (v = 0) feels only the gravity of the lapse:
+    S(S_j) = psi^6 (6 alpha p d_j psi / psi - E d_j alpha), S(tau) = 0."""
+    n = 500
+    rng = np.random.default_rng(9)
+    prim = random_prims(n, seed=10)
+    prim[1:4] = 0.0
+    alpha = rng.uniform(0.5, 1.0, n)
+    psi = rng.uniform(1.0, 1.5, n)
+    da = rng.normal(size=(3, n))
+    dp = rng.normal(size=(3, n))
+    src = nmo.grhd_sources(prim, alpha, psi, da, dp)
+    rho, p = prim[0], prim[4]
+    E = rho * (1.0 + p / rho + p / rho) - p
+    for j in range(3):
+        ref = psi ** 6 * (6.0 * alpha * dp[j] / psi * p - E * da[j])
+        assert np.allclose(src[1 + j], ref, rtol=1e-12, atol=1e-300)
+    assert not src[0].any() and not src[4].any()
