@@ -236,6 +236,11 @@ struct nmg_ctx {
   double fv_w3ratio = 2.;
   double *d_fvgeo = nullptr, *d_fvdist = nullptr, *d_fvdxb = nullptr;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // one RK4 step, u in d_buf[0] / d_buf[1]
+  // host round trips: the last stage runs in element chunks whose results are
+  // copied back on a second stream while later chunks compute
+  static constexpr int kChunks = 8;
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t chunk_ev[kChunks] = {};
   double graph_dt = 0;
   int graph_sel = -1;
   int64_t graph_launches = 5;
@@ -1156,6 +1161,9 @@ void nmg_destroy(nmg_ctx *c) {
   cudaFree(c->d_up); cudaFree(c->d_pers); cudaFree(c->d_wq); cudaFree(c->d_npart);
   for (int b = 0; b < 4; b++) cudaFree(c->d_buf[b]);
   cudaFree(c->d_times); cudaFree(c->d_step);
+  for (int k = 0; k < nmg_ctx::kChunks; k++)
+    if (c->chunk_ev[k]) cudaEventDestroy(c->chunk_ev[k]);
+  if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -1338,15 +1346,80 @@ int nmg_rk4_steps(nmg_ctx *c, double t, double dt, int32_t nsteps) {
   return NMG_OK;
 }
 
+// One RK4 step of u = d_buf[cur] at time t whose final stage runs in element
+// chunks; each chunk's new u is copied to host_u on the copy stream as soon
+// as the chunk is done (the chunks start at multiples of the variant's
+// elements per CTA, so every element is computed by the same tile as in an
+// unchunked launch and the result is bitwise the same).
+static int last_step_streamed(nmg_ctx *c, double t, double dt, double *host_u) {
+  int rc = autotune(c);
+  if (rc) return rc;
+  if (!c->copy_stream) {
+    CK(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+    for (int k = 0; k < nmg_ctx::kChunks; k++)
+      CK(cudaEventCreateWithFlags(&c->chunk_ev[k], cudaEventDisableTiming));
+  }
+  const int cur = c->cur;
+  double *U = c->d_buf[cur], *ACC = c->d_buf[1 - cur], *WA = c->d_buf[2], *WB = c->d_buf[3];
+  const double cacc[4] = {dt / 6., dt / 3., dt / 3., dt / 6.};
+  const double cw[4] = {dt / 2., dt / 2., dt, 0.};
+  const double *win[4] = {U, WA, WB, WA};
+  double *wout[4] = {WA, WB, WA, nullptr};
+  for (int s = 0; s < 4; s++) {
+    StageParams P = base_params(c);
+    P.win = win[s];
+    P.u0 = U;
+    P.acc = ACC;
+    P.wout = wout[s];
+    P.mode = s + 1;
+    P.cacc = cacc[s];
+    P.cw = cw[s];
+    P.t = (s == 0) ? t : (s == 3) ? t + dt : t + 0.5 * dt;
+    if (s < 3) {
+      CK(run_stage(c, c->sel, P));
+      continue;
+    }
+    const int64_t E = c->nelem, epb = std::max(1, c->variants[c->sel].epb);
+    int64_t chunk = (E + nmg_ctx::kChunks - 1) / nmg_ctx::kChunks;
+    chunk = (chunk + epb - 1) / epb * epb;
+    const size_t per = (size_t)NF * c->np;
+    int k = 0;
+    for (int64_t ea = 0; ea < E; ea += chunk, k++) {
+      const int64_t eb = std::min(E, ea + chunk);
+      P.ebase = (int)ea;
+      P.ecount = (int)(eb - ea);
+      CK(run_stage(c, c->sel, P));
+      CK(cudaEventRecord(c->chunk_ev[k], c->stream));
+      CK(cudaStreamWaitEvent(c->copy_stream, c->chunk_ev[k], 0));
+      CK(cudaMemcpyAsync(host_u + ea * per, ACC + ea * per, (size_t)(eb - ea) * per * sizeof(double),
+                         cudaMemcpyDeviceToHost, c->copy_stream));
+    }
+  }
+  CK(cudaStreamSynchronize(c->copy_stream));
+  CK(cudaStreamSynchronize(c->stream));
+  c->cur = 1 - cur;
+  return NMG_OK;
+}
+
 int nmg_rk4_steps_host(nmg_ctx *c, double t, double dt, int32_t nsteps, double *host_u) {
   if (!c || !host_u) return set_err(c, NMG_EINVAL, "nmg_rk4_steps_host: null argument");
+  if (nsteps < 0) return set_err(c, NMG_EINVAL, "nmg_rk4_steps_host: bad argument");
   const size_t bytes = c->state_len * sizeof(double);
   CK(cudaMemcpyAsync(c->d_buf[c->cur], host_u, bytes, cudaMemcpyHostToDevice, c->stream));
-  int rc = nmg_rk4_steps(c, t, dt, nsteps);
-  if (rc) return rc;
-  CK(cudaMemcpyAsync(host_u, c->d_buf[c->cur], bytes, cudaMemcpyDeviceToHost, c->stream));
-  CK(cudaStreamSynchronize(c->stream));
-  return NMG_OK;
+  int rc;
+  if (c->mixed || nsteps == 0) {
+    rc = nmg_rk4_steps(c, t, dt, nsteps);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(host_u, c->d_buf[c->cur], bytes, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return NMG_OK;
+  }
+  // all steps but the last through the step graphs, the last one streamed
+  // back; step times accumulated as evolve_mesh does (main.c:610-626)
+  if (nsteps > 1 && (rc = nmg_rk4_steps(c, t, dt, nsteps - 1))) return rc;
+  long double Te = t, te = 0.;
+  for (int s = 0; s < nsteps - 1; s++) te += dt;
+  return last_step_streamed(c, (double)(Te + te), dt, host_u);
 }
 
 // ---------------------------------------------------------------------------

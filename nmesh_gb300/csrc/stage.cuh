@@ -27,6 +27,7 @@ namespace nmgk {
 
 struct StageParams {
   int nelem;
+  int ebase, ecount;    // element range of this launch (ecount 0: all nelem)
   const double *win;    // w read by the RHS (neighbour traces too)
   const double *u0;     // u at the start of the step
   double *acc;          // u accumulator

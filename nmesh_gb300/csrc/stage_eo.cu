@@ -72,7 +72,7 @@ __device__ __forceinline__ void eo_body(const StageParams &P, int blk) {
   __shared__ unsigned char sPair[3][4 * EPB];  // per pass: le*4 + field
   __shared__ int sNPair[3];
 
-  const int e0 = blk * EPB;
+  const int e0 = P.ebase + blk * EPB;
   const int tid = threadIdx.x;
   for (int q = tid; q < EPB; q += NT) {
     const int e = e0 + q;
@@ -167,7 +167,8 @@ cudaError_t launch_eo(const StageParams &P, cudaStream_t st) {
   if (P.nelem <= 0)
     return cudaFuncSetAttribute(eo_kernel<N, EPB, NT>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shmem);
-  eo_kernel<N, EPB, NT><<<(P.nelem + EPB - 1) / EPB, NT, shmem, st>>>(P);
+  const int ne = P.ecount > 0 ? P.ecount : P.nelem;
+  eo_kernel<N, EPB, NT><<<(ne + EPB - 1) / EPB, NT, shmem, st>>>(P);
   return cudaGetLastError();
 }
 
@@ -192,7 +193,7 @@ __device__ __forceinline__ void eof_body(const StageParams &P, int blk) {
   __shared__ unsigned char sPair[3][4 * EPB];
   __shared__ int sNPair[3];
 
-  const int e0 = blk * EPB;
+  const int e0 = P.ebase + blk * EPB;
   const int tid = threadIdx.x;
   for (int q = tid; q < EPB; q += NT) {
     const int e = e0 + q;
@@ -334,7 +335,8 @@ cudaError_t launch_eof(const StageParams &P, cudaStream_t st) {
   if (P.nelem <= 0)
     return cudaFuncSetAttribute(eof_kernel<N, EPB, NT, MINB>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shmem);
-  eof_kernel<N, EPB, NT, MINB><<<(P.nelem + EPB - 1) / EPB, NT, shmem, st>>>(P);
+  const int ne = P.ecount > 0 ? P.ecount : P.nelem;
+  eof_kernel<N, EPB, NT, MINB><<<(ne + EPB - 1) / EPB, NT, shmem, st>>>(P);
   return cudaGetLastError();
 }
 

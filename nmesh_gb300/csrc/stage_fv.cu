@@ -339,7 +339,7 @@ template <int NT>
 __global__ void __launch_bounds__(NT) fv_kernel(const StageParams P) {
   extern __shared__ double smem[];
   const int n = P.n, np = n * n * n, nn = n * n, nm = n - 1;
-  const int e = P.fvlist ? __ldg(P.fvlist + blockIdx.x) : (int)blockIdx.x;
+  const int e = P.fvlist ? __ldg(P.fvlist + blockIdx.x) : P.ebase + (int)blockIdx.x;
   if (e >= P.nelem) return;
   double *sW = smem;             // [4][np]  pi, cx, cy, cz of w
   double *sD = sW + 4 * np;      // [4][np]  div f accumulators
@@ -486,7 +486,7 @@ cudaError_t launch_fv(const StageParams &P, cudaStream_t st) {
   if (P.nelem == 0)
     return cudaFuncSetAttribute(fv_kernel<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)smem);
-  const int grid = P.fvlist ? P.nfvel : P.nelem;
+  const int grid = P.fvlist ? P.nfvel : (P.ecount > 0 ? P.ecount : P.nelem);
   if (grid == 0) return cudaSuccess;
   fv_kernel<NT><<<grid, NT, smem, st>>>(P);
   return cudaGetLastError();

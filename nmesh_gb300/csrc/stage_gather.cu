@@ -19,7 +19,7 @@ __global__ void __launch_bounds__(NT) gather_kernel(StageParams P) {
   __shared__ double sScale[EPB][3];
   __shared__ double sG[EPB][3];
 
-  const int e0 = blockIdx.x * EPB;
+  const int e0 = P.ebase + blockIdx.x * EPB;
   const int tid = threadIdx.x;
   for (int q = tid; q < N * N; q += NT) sD[q] = P.D[q];
   for (int q = tid; q < EPB; q += NT) {
@@ -113,7 +113,8 @@ cudaError_t launch_gather(const StageParams &P, cudaStream_t st) {
   if (P.nelem <= 0)
     return cudaFuncSetAttribute(gather_kernel<N, EPB, NT>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shmem);
-  gather_kernel<N, EPB, NT><<<(P.nelem + EPB - 1) / EPB, NT, shmem, st>>>(P);
+  const int ne = P.ecount > 0 ? P.ecount : P.nelem;
+  gather_kernel<N, EPB, NT><<<(ne + EPB - 1) / EPB, NT, shmem, st>>>(P);
   return cudaGetLastError();
 }
 

@@ -148,3 +148,19 @@ def test_autotuner_and_every_tile_shape():
         assert rel_l2(ev.rhs(u)[perm], d["r0"]) <= RTOL_RHS, c
     with pytest.raises(ng.NmgError):
         ev.set_kernel("nonsense")
+
+
+@pytest.mark.parametrize("variant", ["eo:2:128", "eo:4:256", "gather", "eof"])
+@pytest.mark.parametrize("nsteps", [1, 3])
+def test_host_round_trip_streams_last_stage_bitwise(variant, nsteps):
+    """nmg_rk4_steps_host runs its last stage in element chunks and copies
+    each chunk back while the next computes; the state equals the resident
+    multi-step path bit for bit."""
+    m = ng.Mesh.build(ng.MESH_CUBEDSPHERES7, n=5, luni=2, cs_dc=1.0, cs_r0fac=20.0)
+    u = gaussian_pulses(m.coords(), seed=4, rmin=1.0, rmax=6.0)
+    ev = ng.Evolution(m, ng.BC_OUTGOING)
+    ev.set_kernel(variant)
+    got = ev.rk4_steps_host(u, 0.0, 0.01, nsteps)
+    ev.set_state(u)
+    ev.rk4_steps(0.0, 0.01, nsteps)
+    assert np.array_equal(got, ev.get_state())
