@@ -240,7 +240,12 @@ struct nmg_ctx {
   // copied back on a second stream while later chunks compute
   static constexpr int kChunks = 8;
   cudaStream_t copy_stream = nullptr;
-  cudaEvent_t chunk_ev[kChunks] = {};
+  cudaEvent_t chunk_ev[kChunks] = {}, h2d_ev[kChunks] = {};
+  // first-stage element groups of a chunked host->device copy: group k holds
+  // the elements whose face neighbourhood lies in the copy chunks 0..k
+  int *d_elist = nullptr;
+  std::vector<int> h2d_off;   // [kChunks + 1] group offsets into d_elist
+  int64_t h2d_chunk = 0;      // elements per copy chunk
   double graph_dt = 0;
   int graph_sel = -1;
   int64_t graph_launches = 5;
@@ -1161,8 +1166,11 @@ void nmg_destroy(nmg_ctx *c) {
   cudaFree(c->d_up); cudaFree(c->d_pers); cudaFree(c->d_wq); cudaFree(c->d_npart);
   for (int b = 0; b < 4; b++) cudaFree(c->d_buf[b]);
   cudaFree(c->d_times); cudaFree(c->d_step);
-  for (int k = 0; k < nmg_ctx::kChunks; k++)
+  for (int k = 0; k < nmg_ctx::kChunks; k++) {
     if (c->chunk_ev[k]) cudaEventDestroy(c->chunk_ev[k]);
+    if (c->h2d_ev[k]) cudaEventDestroy(c->h2d_ev[k]);
+  }
+  cudaFree(c->d_elist);
   if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
@@ -1351,14 +1359,44 @@ int nmg_rk4_steps(nmg_ctx *c, double t, double dt, int32_t nsteps) {
 // as the chunk is done (the chunks start at multiples of the variant's
 // elements per CTA, so every element is computed by the same tile as in an
 // unchunked launch and the result is bitwise the same).
-static int last_step_streamed(nmg_ctx *c, double t, double dt, double *host_u) {
+static int prepare_h2d_groups(nmg_ctx *c) {
+  if (c->d_elist) return NMG_OK;
+  const int64_t E = c->nelem;
+  const int K = nmg_ctx::kChunks;
+  const int64_t chunk = (E + K - 1) / K;
+  std::vector<std::vector<int>> grp(K);
+  for (int64_t e = 0; e < E; e++) {
+    int64_t r = e / chunk;
+    for (int f = 0; f < 6; f++) {
+      const int nb = c->h_nb[e * 6 + f];
+      if (nb >= 0) r = std::max<int64_t>(r, nb / chunk);
+    }
+    grp[r].push_back((int)e);
+  }
+  std::vector<int> lst;
+  c->h2d_off.assign(K + 1, 0);
+  for (int k = 0; k < K; k++) {
+    lst.insert(lst.end(), grp[k].begin(), grp[k].end());
+    c->h2d_off[k + 1] = (int)lst.size();
+  }
+  c->h2d_chunk = chunk;
+  CK(cudaMalloc((void **)&c->d_elist, sizeof(int) * std::max<size_t>(lst.size(), 1)));
+  CK(cudaMemcpy(c->d_elist, lst.data(), sizeof(int) * lst.size(), cudaMemcpyHostToDevice));
+  return NMG_OK;
+}
+
+static int last_step_streamed(nmg_ctx *c, double t, double dt, double *host_u,
+                              const double *host_in) {
   int rc = autotune(c);
   if (rc) return rc;
   if (!c->copy_stream) {
     CK(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
-    for (int k = 0; k < nmg_ctx::kChunks; k++)
+    for (int k = 0; k < nmg_ctx::kChunks; k++) {
       CK(cudaEventCreateWithFlags(&c->chunk_ev[k], cudaEventDisableTiming));
+      CK(cudaEventCreateWithFlags(&c->h2d_ev[k], cudaEventDisableTiming));
+    }
   }
+  if (host_in && (rc = prepare_h2d_groups(c))) return rc;
   const int cur = c->cur;
   double *U = c->d_buf[cur], *ACC = c->d_buf[1 - cur], *WA = c->d_buf[2], *WB = c->d_buf[3];
   const double cacc[4] = {dt / 6., dt / 3., dt / 3., dt / 6.};
@@ -1375,6 +1413,29 @@ static int last_step_streamed(nmg_ctx *c, double t, double dt, double *host_u) {
     P.cacc = cacc[s];
     P.cw = cw[s];
     P.t = (s == 0) ? t : (s == 3) ? t + dt : t + 0.5 * dt;
+    if (s == 0 && host_in) {
+      // copy u in chunks; each element group runs as soon as its face
+      // neighbourhood has arrived (per element the same arithmetic)
+      const size_t per = (size_t)NF * c->np;
+      for (int k = 0; k < nmg_ctx::kChunks; k++) {
+        const int64_t ea = k * c->h2d_chunk, eb = std::min<int64_t>(c->nelem, ea + c->h2d_chunk);
+        if (eb > ea)
+          CK(cudaMemcpyAsync(U + ea * per, host_in + ea * per, (size_t)(eb - ea) * per * sizeof(double),
+                             cudaMemcpyHostToDevice, c->copy_stream));
+        CK(cudaEventRecord(c->h2d_ev[k], c->copy_stream));
+      }
+      for (int k = 0; k < nmg_ctx::kChunks; k++) {
+        CK(cudaStreamWaitEvent(c->stream, c->h2d_ev[k], 0));
+        const int n0 = c->h2d_off[k], n1 = c->h2d_off[k + 1];
+        if (n1 == n0) continue;
+        StageParams Q = P;
+        Q.elist = c->d_elist;
+        Q.ebase = n0;
+        Q.ecount = n1 - n0;
+        CK(run_stage(c, c->sel, Q));
+      }
+      continue;
+    }
     if (s < 3) {
       CK(run_stage(c, c->sel, P));
       continue;
@@ -1405,8 +1466,10 @@ int nmg_rk4_steps_host(nmg_ctx *c, double t, double dt, int32_t nsteps, double *
   if (!c || !host_u) return set_err(c, NMG_EINVAL, "nmg_rk4_steps_host: null argument");
   if (nsteps < 0) return set_err(c, NMG_EINVAL, "nmg_rk4_steps_host: bad argument");
   const size_t bytes = c->state_len * sizeof(double);
-  CK(cudaMemcpyAsync(c->d_buf[c->cur], host_u, bytes, cudaMemcpyHostToDevice, c->stream));
   int rc;
+  if (!c->fv && nsteps == 1)  // copy in, step and copy out overlapped
+    return last_step_streamed(c, t, dt, host_u, host_u);
+  CK(cudaMemcpyAsync(c->d_buf[c->cur], host_u, bytes, cudaMemcpyHostToDevice, c->stream));
   if (c->mixed || nsteps == 0) {
     rc = nmg_rk4_steps(c, t, dt, nsteps);
     if (rc) return rc;
@@ -1419,7 +1482,7 @@ int nmg_rk4_steps_host(nmg_ctx *c, double t, double dt, int32_t nsteps, double *
   if (nsteps > 1 && (rc = nmg_rk4_steps(c, t, dt, nsteps - 1))) return rc;
   long double Te = t, te = 0.;
   for (int s = 0; s < nsteps - 1; s++) te += dt;
-  return last_step_streamed(c, (double)(Te + te), dt, host_u);
+  return last_step_streamed(c, (double)(Te + te), dt, host_u, nullptr);
 }
 
 // ---------------------------------------------------------------------------

@@ -28,6 +28,7 @@ namespace nmgk {
 struct StageParams {
   int nelem;
   int ebase, ecount;    // element range of this launch (ecount 0: all nelem)
+  const int *elist;     // if set: the launch's elements are elist[ebase .. ebase+ecount)
   const double *win;    // w read by the RHS (neighbour traces too)
   const double *u0;     // u at the start of the step
   double *acc;          // u accumulator
@@ -82,6 +83,13 @@ __device__ __forceinline__ int face_node_d(int f, int a, int b) {
   return d == 0 ? p + N * (a + N * b) : d == 1 ? a + N * (p + N * b) : a + N * (b + N * p);
 }
 
+// element of tile slot i (i = ebase + tile * EPB + le): i itself, or the
+// i-th entry of the launch's element list (nelem past its end: no element)
+__device__ __forceinline__ int elem_at(const StageParams &P, int i) {
+  if (!P.elist) return i;
+  return i < P.ebase + P.ecount ? __ldg(P.elist + i) : P.nelem;
+}
+
 __device__ __forceinline__ double stage_time(const StageParams &P) {
   return P.tdev ? P.tdev[*P.stepdev] + P.tofs_dt : P.t;
 }
@@ -92,7 +100,7 @@ __device__ __forceinline__ void stage_in(const StageParams &P, double *sW, int e
   constexpr int NP = N * N * N;
   for (int q = threadIdx.x; q < EPB * 4 * NP; q += NT) {
     const int le = q / (4 * NP), rem = q - le * 4 * NP, f = rem / NP, node = rem - f * NP;
-    const int e = e0 + le;
+    const int e = elem_at(P, e0 + le);
     double v = 0.;
     if (e < P.nelem) v = __ldg(P.win + ((size_t)e * NF + f) * NP + node);
     sW[(f * EPB + le) * NP + node] = v;
@@ -111,7 +119,7 @@ __device__ __forceinline__ void face_terms(const StageParams &P, const double *s
   for (int d = 0; d < 3; d++) {
     for (int q = threadIdx.x; q < EPB * 2 * NN; q += NT) {
       const int le = q / (2 * NN), rem = q - le * 2 * NN, s = rem / NN, ab = rem - s * NN;
-      const int e = e0 + le;
+      const int e = elem_at(P, e0 + le);
       if (e >= P.nelem) continue;
       const int a = ab % N, b = ab / N, f = 2 * d + s;
       const int node = face_node_d<N>(f, a, b);
@@ -308,7 +316,7 @@ __device__ __forceinline__ void epilogue(const StageParams &P, const double *sW,
   constexpr int NP = N * N * N;
   for (int q = threadIdx.x; q < EPB * NF * NP; q += NT) {
     const int le = q / (NF * NP), rem = q - le * NF * NP, f = rem / NP, node = rem - f * NP;
-    const int e = e0 + le;
+    const int e = elem_at(P, e0 + le);
     if (e >= P.nelem || (P.skip && P.skip[e])) continue;
     const size_t idx = ((size_t)e * NF + f) * NP + node;
     double r;

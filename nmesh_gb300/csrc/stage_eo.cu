@@ -75,7 +75,7 @@ __device__ __forceinline__ void eo_body(const StageParams &P, int blk) {
   const int e0 = P.ebase + blk * EPB;
   const int tid = threadIdx.x;
   for (int q = tid; q < EPB; q += NT) {
-    const int e = e0 + q;
+    const int e = elem_at(P, e0 + q);
     const int cs = (e < P.nelem) ? P.cslot[e] : -1;
     sCs[q] = cs;
     sMask[q] = (e >= P.nelem) ? 0 : (cs >= 0 ? P.cmask[cs] : (1 | (1 << 4) | (1 << 8)));
@@ -196,7 +196,7 @@ __device__ __forceinline__ void eof_body(const StageParams &P, int blk) {
   const int e0 = P.ebase + blk * EPB;
   const int tid = threadIdx.x;
   for (int q = tid; q < EPB; q += NT) {
-    const int e = e0 + q;
+    const int e = elem_at(P, e0 + q);
     const int cs = (e < P.nelem) ? P.cslot[e] : -1;
     sCs[q] = cs;
     sMask[q] = (e >= P.nelem) ? -1 : (cs >= 0 ? P.cmask[cs] : (1 | (1 << 4) | (1 << 8)));
@@ -234,8 +234,8 @@ __device__ __forceinline__ void eof_body(const StageParams &P, int blk) {
       const int row = (sMask[le] >> (3 * a)) & 7;
       if (fld == 0) {
         FaceData FL, FR;
-        face_fetch<N>(P, e0 + le, 2 * a, L, cs, sG[le][a], t, FL);
-        face_fetch<N>(P, e0 + le, 2 * a + 1, L, cs, sG[le][a], t, FR);
+        face_fetch<N>(P, elem_at(P, e0 + le), 2 * a, L, cs, sG[le][a], t, FL);
+        face_fetch<N>(P, elem_at(P, e0 + le), 2 * a + 1, L, cs, sG[le][a], t, FR);
         double out[N];
         line_deriv<N, 0>(sW + (0 * EPB + le) * NP + base, st, out);
 #pragma unroll
@@ -293,7 +293,7 @@ __device__ __forceinline__ void eof_body(const StageParams &P, int blk) {
   // epilogue: r_pi = r_pi^0 (+ r_pi^1 + r_pi^2) + r_pi^face, r_phi = pi
   for (int q = tid; q < EPB * NF * NP; q += NT) {
     const int le = q / (NF * NP), rem = q - le * NF * NP, f = rem / NP, node = rem - f * NP;
-    const int e = e0 + le;
+    const int e = elem_at(P, e0 + le);
     if (e >= P.nelem || (P.skip && P.skip[e])) continue;
     const size_t idx = ((size_t)e * NF + f) * NP + node;
     double r;

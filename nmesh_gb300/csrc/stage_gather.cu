@@ -23,7 +23,7 @@ __global__ void __launch_bounds__(NT) gather_kernel(StageParams P) {
   const int tid = threadIdx.x;
   for (int q = tid; q < N * N; q += NT) sD[q] = P.D[q];
   for (int q = tid; q < EPB; q += NT) {
-    const int e = e0 + q;
+    const int e = elem_at(P, e0 + q);
     sCs[q] = (e < P.nelem) ? P.cslot[e] : -1;
     for (int d = 0; d < 3; d++) sScale[q][d] = (e < P.nelem) ? P.scale[e * 3 + d] : 0.;
     for (int d = 0; d < 3; d++) sG[q][d] = (e < P.nelem) ? P.gcart[e * 3 + d] : 0.;
