@@ -238,7 +238,8 @@ struct nmg_ctx {
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // one RK4 step, u in d_buf[0] / d_buf[1]
   // host round trips: the last stage runs in element chunks whose results are
   // copied back on a second stream while later chunks compute
-  static constexpr int kChunks = 8;
+  static constexpr int kChunks = 32;   // capacity; nchunks are used
+  int nchunks = 8;                     // NMG_COPY_CHUNKS overrides (1..32)
   cudaStream_t copy_stream = nullptr;
   cudaEvent_t chunk_ev[kChunks] = {}, h2d_ev[kChunks] = {};
   // first-stage element groups of a chunked host->device copy: group k holds
@@ -605,6 +606,10 @@ static int create_impl(const nmg_mesh *m, int32_t bc_kind, const double k[3], bo
   int64_t nfv = 0;
   for (size_t e = 0; e < m->fv.size(); e++) nfv += m->fv[e] ? 1 : 0;
   c->switchable = switchable;
+  if (const char *nc = getenv("NMG_COPY_CHUNKS")) {
+    const int v = atoi(nc);
+    if (v >= 1 && v <= nmg_ctx::kChunks) c->nchunks = v;
+  }
   c->fv = nfv > 0 || switchable;
   c->mixed = (nfv > 0 && nfv < m->nelem) || switchable;
   if (c->mixed) {
@@ -1362,7 +1367,7 @@ int nmg_rk4_steps(nmg_ctx *c, double t, double dt, int32_t nsteps) {
 static int prepare_h2d_groups(nmg_ctx *c) {
   if (c->d_elist) return NMG_OK;
   const int64_t E = c->nelem;
-  const int K = nmg_ctx::kChunks;
+  const int K = c->nchunks;
   const int64_t chunk = (E + K - 1) / K;
   std::vector<std::vector<int>> grp(K);
   for (int64_t e = 0; e < E; e++) {
@@ -1374,7 +1379,7 @@ static int prepare_h2d_groups(nmg_ctx *c) {
     grp[r].push_back((int)e);
   }
   std::vector<int> lst;
-  c->h2d_off.assign(K + 1, 0);
+  c->h2d_off.assign(nmg_ctx::kChunks + 1, (int)0);
   for (int k = 0; k < K; k++) {
     lst.insert(lst.end(), grp[k].begin(), grp[k].end());
     c->h2d_off[k + 1] = (int)lst.size();
@@ -1417,14 +1422,14 @@ static int last_step_streamed(nmg_ctx *c, double t, double dt, double *host_u,
       // copy u in chunks; each element group runs as soon as its face
       // neighbourhood has arrived (per element the same arithmetic)
       const size_t per = (size_t)NF * c->np;
-      for (int k = 0; k < nmg_ctx::kChunks; k++) {
+      for (int k = 0; k < c->nchunks; k++) {
         const int64_t ea = k * c->h2d_chunk, eb = std::min<int64_t>(c->nelem, ea + c->h2d_chunk);
         if (eb > ea)
           CK(cudaMemcpyAsync(U + ea * per, host_in + ea * per, (size_t)(eb - ea) * per * sizeof(double),
                              cudaMemcpyHostToDevice, c->copy_stream));
         CK(cudaEventRecord(c->h2d_ev[k], c->copy_stream));
       }
-      for (int k = 0; k < nmg_ctx::kChunks; k++) {
+      for (int k = 0; k < c->nchunks; k++) {
         CK(cudaStreamWaitEvent(c->stream, c->h2d_ev[k], 0));
         const int n0 = c->h2d_off[k], n1 = c->h2d_off[k + 1];
         if (n1 == n0) continue;
@@ -1441,7 +1446,7 @@ static int last_step_streamed(nmg_ctx *c, double t, double dt, double *host_u,
       continue;
     }
     const int64_t E = c->nelem, epb = std::max(1, c->variants[c->sel].epb);
-    int64_t chunk = (E + nmg_ctx::kChunks - 1) / nmg_ctx::kChunks;
+    int64_t chunk = (E + c->nchunks - 1) / c->nchunks;
     chunk = (chunk + epb - 1) / epb * epb;
     const size_t per = (size_t)NF * c->np;
     int k = 0;
