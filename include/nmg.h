@@ -195,6 +195,29 @@ int nmg_get_trouble_scores(nmg_ctx *c, int32_t *scores);
  * u_dev NULL: the resident state.  Only the 31 numbers leave the GPU. */
 int nmg_norms(nmg_ctx *c, const double *u_dev, double *out);
 
+/* ---- checkpoints in the reference's variable file format ---------------
+ * The state as the reference's checkpoint "variables.bin"
+ * (checkpoint_save_EvoVars / checkpoint_load_Vars,
+ * src/main/checkpoint/checkpoint_save.c:335-470, checkpoint_load.c:397),
+ * matched by element name ("<patch>_<octree digits>", known for generated
+ * meshes; names[e] given otherwise, NULL for a generated mesh) and variable
+ * name (scalarwave1_pi, _cx, _cy, _cz, _phi).  A GPU run restarts from a
+ * reference checkpoint with nmg_checkpoint_read, and the reference restarts
+ * from a checkpoint directory whose variables.bin nmg_checkpoint_write
+ * produced (its CRC.txt vars entry then no longer matches: a warning). */
+int nmg_checkpoint_write(nmg_ctx *c, const nmg_mesh *m, const char *path,
+                         const char *const *names);
+int nmg_checkpoint_read(nmg_ctx *c, const nmg_mesh *m, const char *path,
+                        const char *const *names);
+/* the same with a host state [element][field][node] */
+int nmg_checkpoint_write_host(const nmg_mesh *m, const double *u, const char *path,
+                              const char *const *names);
+int nmg_checkpoint_read_host(const nmg_mesh *m, const char *path, double *u,
+                             const char *const *names);
+const char *nmg_checkpoint_last_error(void);
+/* the reference's name of mesh element e (NULL for a described mesh) */
+const char *nmg_mesh_element_name(const nmg_mesh *m, int64_t e);
+
 /* ---- GRHD: pointwise conservative <-> primitive conversion ---------------
  * Ideal gas on a conformally flat 3-metric gamma_ij = psi^4 delta_ij; no
  * counterpart in the reference (its GRHD is external), except the root

@@ -185,6 +185,12 @@ def lib(build_if_missing=True):
         "nmg_get_trouble_scores": (ctypes.c_int, [vp, vp]),
         "nmg_norms": (ctypes.c_int, [vp, vp, vp]),
         "nmg_set_numflux": (ctypes.c_int, [vp, i32]),
+        "nmg_checkpoint_write": (ctypes.c_int, [vp, vp, ctypes.c_char_p, vp]),
+        "nmg_checkpoint_read": (ctypes.c_int, [vp, vp, ctypes.c_char_p, vp]),
+        "nmg_checkpoint_write_host": (ctypes.c_int, [vp, vp, ctypes.c_char_p, vp]),
+        "nmg_checkpoint_read_host": (ctypes.c_int, [vp, ctypes.c_char_p, vp, vp]),
+        "nmg_checkpoint_last_error": (ctypes.c_char_p, []),
+        "nmg_mesh_element_name": (ctypes.c_char_p, [vp, i64]),
         "nmg_grhd_prim2con": (ctypes.c_int, [vp, i64, vp, vp, vp, vp]),
         "nmg_grhd_con2prim": (ctypes.c_int, [vp, i64, vp, vp, vp, vp, vp]),
         "nmg_grhd_fluxes": (ctypes.c_int, [vp, i64, i32, vp, vp, vp, vp, vp, vp]),
@@ -299,6 +305,12 @@ class Mesh:
         lib().nmg_mesh_get_fv(self._h, _ptr(f))
         return f
 
+    def names(self):
+        """The reference's element names "<patch>_<octree digits>" (None for
+        a mesh built from arrays)."""
+        out = [lib().nmg_mesh_element_name(self._h, e) for e in range(self.nelem)]
+        return None if any(x is None for x in out) else [x.decode() for x in out]
+
     def faces(self):
         nb = np.zeros((self.nelem, 6), np.int32)
         code = np.zeros((self.nelem, 6), np.int32)
@@ -315,6 +327,30 @@ class Mesh:
             self.close()
         except Exception:
             pass
+
+
+def _names_arg(names):
+    if names is None:
+        return None, None
+    arr = (ctypes.c_char_p * len(names))(*[str(x).encode() for x in names])
+    return ctypes.cast(arr, ctypes.c_void_p), arr
+
+
+def checkpoint_write_host(mesh, u, path, names=None):
+    """Write host state u [E,5,np] as the reference's checkpoint variables.bin."""
+    u = np.ascontiguousarray(u, np.float64)
+    p, keep = _names_arg(names)
+    if lib().nmg_checkpoint_write_host(mesh._h, _ptr(u), str(path).encode(), p):
+        raise NmgError(lib().nmg_checkpoint_last_error().decode())
+
+
+def checkpoint_read_host(mesh, path, names=None):
+    """Read the reference's checkpoint variables.bin into a host state."""
+    u = np.zeros((mesh.nelem, NFIELDS, mesh.np))
+    p, keep = _names_arg(names)
+    if lib().nmg_checkpoint_read_host(mesh._h, str(path).encode(), _ptr(u), p):
+        raise NmgError(lib().nmg_checkpoint_last_error().decode())
+    return u
 
 
 class Evolution:
@@ -428,6 +464,18 @@ class Evolution:
             res[name] = dict(zip(("VolInt", "mean", "rms", "min", "max", "maxAbs"),
                                  out[1 + 6 * l: 7 + 6 * l]))
         return res
+
+    def checkpoint_write(self, path, names=None):
+        """Resident state -> the reference's checkpoint variables.bin."""
+        p, keep = _names_arg(names)
+        if lib().nmg_checkpoint_write(self._h, self.mesh._h, str(path).encode(), p):
+            raise NmgError(lib().nmg_checkpoint_last_error().decode())
+
+    def checkpoint_read(self, path, names=None):
+        """Resident state <- the reference's checkpoint variables.bin."""
+        p, keep = _names_arg(names)
+        if lib().nmg_checkpoint_read(self._h, self.mesh._h, str(path).encode(), p):
+            raise NmgError(lib().nmg_checkpoint_last_error().decode())
 
     # ---- DG <-> finite-volume switching ----
     def set_element_types(self, fv):

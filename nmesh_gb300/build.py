@@ -12,7 +12,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libnmg.so")
 SOURCES = ["nmg.cu", "stage_eo.cu", "stage_gather.cu", "stage_fv.cu", "stage_fv_fast.cu",
-           "grhd.cu", "noalloc.cu", "mesh.cpp"]
+           "grhd.cu", "noalloc.cu", "mesh.cpp", "ckpt.cpp"]
 # per-file extra flags: the finite-volume kernel rounds every product and sum
 # separately, in the reference's order (no FMA contraction)
 EXTRA_FLAGS = {"stage_fv.cu": ["-fmad=false"], "grhd.cu": ["-fmad=false"]}

@@ -182,6 +182,7 @@ void fill_geometry(nmg_mesh &m, const std::vector<Patch> &pats, int L, int32_t f
   m.xyz.resize(m.nelem * 3 * np);
   m.dXdx.resize(m.nelem * 9 * np);
   m.fv.assign(m.nelem, 0);
+  m.names.assign(m.nelem, std::string());
   int64_t e = 0;
   for (size_t p = 0; p < pats.size(); p++) {
     for (int64_t mc = 0; mc < per; mc++, e++) {
@@ -189,6 +190,15 @@ void fill_geometry(nmg_mesh &m, const std::vector<Patch> &pats, int L, int32_t f
       for (int bit = 0; bit < L; bit++)
         for (int d = 0; d < 3; d++) ixyz[d] |= (int)((mc >> (3 * bit + d)) & 1) << bit;
       elem_bbox(pats[p].bbox, L, ixyz, &m.bbox[e * 6]);
+      // elmname: patch, then one octree child digit per level, bit d set
+      // for the upper half in direction d (connections.c:819-866,1186-1200)
+      std::string nm = std::to_string(p) + "_";
+      for (int ll = 1; ll <= L; ll++) {
+        int dig = 0;
+        for (int d = 0; d < 3; d++) dig |= ((ixyz[d] >> (L - ll)) & 1) << d;
+        nm += (char)('0' + dig);
+      }
+      m.names[e] = nm;
       m.pat[e] = (int32_t)p;
       m.curvi[e] = pats[p].cubed ? 1 : 0;
       const bool isfv = (fvmask >> p) & 1;

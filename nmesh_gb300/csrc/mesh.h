@@ -33,6 +33,8 @@ struct nmg_mesh {
                                // spaced points; empty: all DG on LGL points
   std::vector<nmg::Patch> patches;  // patch maps of a generated mesh (empty
                                     // for a described one)
+  std::vector<std::string> names;   // [E] the reference's element names
+                                    // "<patch>_<octree digits>" (generated meshes)
 };
 
 // face-table code bit: the neighbour has the other point type (DG / FV), its

@@ -94,6 +94,11 @@ CASES = {
     "upw_fvbox_l1_n7_w5no": dict(mesh="box", n=7, luni=1, k=(1.0, 1.0, 1.0),
                                  dt=0.005, steps=2, eps=0.05, seed=35, numflux="upwind",
                                  fv=dict(rec="WENOm5_2", extrap="no")),
+    # the reference's own checkpoint of the final state (variables.bin)
+    "ckpt_box_l1_n4": dict(mesh="box", n=4, luni=1, k=(1.0, -0.5, 0.25),
+                           dt=0.01, steps=1, eps=0.01, seed=36, checkpoint=True),
+    "ckpt_cs7_l1_n3": dict(mesh="cs7", n=3, luni=1, k=(0.3, -0.2, 0.1),
+                           dt=0.002, steps=1, eps=0.01, seed=37, checkpoint=True),
 }
 
 
@@ -126,6 +131,8 @@ def parfile(case, prefix):
         lines += ["amr_mesh_type = 7 CubedSpheres",
                   "amr_CubedSphere_dc = 1", "amr_CubedSphere_r0fac = 20"]
         pats = "0 1 2 3 4 5 6"
+    if c.get("checkpoint"):
+        lines += ["checkpoint = yes"]
     if "fv" in c:
         pats = c["fv"].get("patches", pats)
         lines += [f"amr_uniform_p = {pats}", f"amr_fv_p = {pats}",
@@ -155,6 +162,10 @@ def run_case(case, exe, outdir):
         norms = None
         if CASES[case].get("norms"):
             norms = np.fromfile(prefix + "_norms.bin", dtype="<f8")
+        if CASES[case].get("checkpoint"):
+            import shutil
+            src = os.path.join(tmp, case, "checkpoint", "variables.bin")
+            shutil.copyfile(src, os.path.join(outdir, case + "_variables.bin"))
     c = CASES[case]
     meta = dict(case=case, **{k: v for k, v in c.items()})
     extra = {}

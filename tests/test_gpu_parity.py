@@ -164,3 +164,27 @@ def test_host_round_trip_streams_last_stage_bitwise(variant, nsteps):
     ev.set_state(u)
     ev.rk4_steps(0.0, 0.01, nsteps)
     assert np.array_equal(got, ev.get_state())
+
+
+def test_periodic_cube_plane_wave_workload():
+    """The periodic-cube workload: [0, 2 pi]^3, 8^3 elements, n = 5, plane
+    wave psi = A sin(x + y + z) with a seeded amplitude, LLF, RK4 with
+    dt = 0.25 (2 pi / 8) / 16, 10 steps: the oracle within 1e-12 and the exact
+    solution within the scheme's truncation error."""
+    m = ng.Mesh.build(ng.MESH_BOX, n=5, luni=3, xc=(PI, PI, PI), box_dout=PI, periodic=True)
+    A = np.random.default_rng(2024).uniform(0.5, 1.5)
+    xyz = m.coords()
+    om = np.sqrt(3.0)
+
+    def exact(t):
+        arg = xyz[:, 0] + xyz[:, 1] + xyz[:, 2] - om * t
+        c, s = np.cos(arg), np.sin(arg)
+        return A * np.stack([-om * c, c, c, c, s], 1)
+
+    dt = 0.25 * (2 * PI / 8) / 16
+    u0 = exact(0.0)
+    ev = ng.Evolution(m, ng.BC_OUTGOING)
+    u = ev.rk4_steps_host(u0, 0.0, dt, 10)
+    o = oracle_for(m, bc=1, period=2 * PI)
+    assert rel_l2(u, o.rk4(u0, dt, 10)) <= RTOL_RK4
+    assert rel_l2(u, exact(10 * dt)) <= 1e-3
