@@ -80,6 +80,9 @@ typedef struct nmg_mesh_params {
                          finite-volume elements on equally spaced points
                          (amr_uniform_p and amr_fv_p list patch p,
                          src/main/amr/mesh.c:35-83); -1: every patch; 0: DG */
+  int32_t hrefine;    /* bit p set: patch p is refined one level further
+                         (amr_hrefine_p, src/main/amr/mesh.c:269-284); its
+                         faces against other patches are non-conforming */
 } nmg_mesh_params;
 
 /* A mesh given element by element, e.g. packed from the reference's tMesh
@@ -127,6 +130,15 @@ int nmg_mesh_get_fv(const nmg_mesh *m, int32_t *fv);
    (src/main/basis/Legendre.c:149-213, Lagrange.c:126-147) */
 int nmg_basis(int32_t n, double *x, double *w, double *D);
 /* equally spaced points on [-1,1] (uniform_x, src/main/basis/Legendre.c:626) */
+/* Non-conforming faces of the mesh (patches at different levels): counts,
+ * and if the arrays are given, per face (element, face) [nface][2], per face
+ * node the offsets of its contributions [nface*n*n + 1], per contribution
+ * the source (element, face) [ncontrib][2] and the node's position on the
+ * source face in its in-plane coordinates [ncontrib][2].  A face node's
+ * trace is the average of its contributions (set_ajsurf_vl,
+ * src/main/amr/surface.c:799-1360). */
+int nmg_mesh_get_hanging(const nmg_mesh *m, int64_t *nface, int64_t *ncontrib, int32_t *hface,
+                         int32_t *hoff, int32_t *hsrc, double *hpos);
 int nmg_uniform_points(int32_t n, double *x);
 void nmg_mesh_free(nmg_mesh *m);
 const char *nmg_mesh_last_error(void);

@@ -40,7 +40,7 @@ class _MeshParams(ctypes.Structure):
                 ("luni", ctypes.c_int32), ("periodic", ctypes.c_int32),
                 ("xc", ctypes.c_double * 3), ("box_dout", ctypes.c_double),
                 ("cs_dc", ctypes.c_double), ("cs_r0fac", ctypes.c_double),
-                ("fv", ctypes.c_int32)]
+                ("fv", ctypes.c_int32), ("hrefine", ctypes.c_int32)]
 
 
 class TroubleParams(ctypes.Structure):
@@ -191,6 +191,7 @@ def lib(build_if_missing=True):
         "nmg_checkpoint_read_host": (ctypes.c_int, [vp, ctypes.c_char_p, vp, vp]),
         "nmg_checkpoint_last_error": (ctypes.c_char_p, []),
         "nmg_mesh_element_name": (ctypes.c_char_p, [vp, i64]),
+        "nmg_mesh_get_hanging": (ctypes.c_int, [vp, vp, vp, vp, vp, vp, vp]),
         "nmg_grhd_prim2con": (ctypes.c_int, [vp, i64, vp, vp, vp, vp]),
         "nmg_grhd_con2prim": (ctypes.c_int, [vp, i64, vp, vp, vp, vp, vp]),
         "nmg_grhd_fluxes": (ctypes.c_int, [vp, i64, i32, vp, vp, vp, vp, vp, vp]),
@@ -235,12 +236,17 @@ class Mesh:
 
     @classmethod
     def build(cls, mesh_type=MESH_BOX, n=5, luni=0, xc=(0.0, 0.0, 0.0),
-              box_dout=1.0, cs_dc=1.0, cs_r0fac=20.0, periodic=False, fv=False):
+              box_dout=1.0, cs_dc=1.0, cs_r0fac=20.0, periodic=False, fv=False,
+              hrefine=()):
         """Mesh from the reference's parameters: amr_mesh_type (1 BoxMesh /
         7 CubedSpheres), amr_n0..2 = n, amr_luni, amr_mesh_xc,
         amr_BoxMesh_dout, amr_CubedSphere_dc, amr_CubedSphere_r0fac;
         fv=True puts every patch in amr_uniform_p and amr_fv_p, a list of
-        patch indices puts those patches there."""
+        patch indices puts those patches there; hrefine lists the patches
+        of amr_hrefine_p (refined one level further)."""
+        hmask = 0
+        for p_ in hrefine:
+            hmask |= 1 << int(p_)
         if fv is True:
             mask = -1
         elif not fv:
@@ -251,7 +257,7 @@ class Mesh:
                 mask |= 1 << int(p_)
         p = _MeshParams(int(mesh_type), int(n), int(luni), int(bool(periodic)),
                         (ctypes.c_double * 3)(*xc), float(box_dout),
-                        float(cs_dc), float(cs_r0fac), int(mask))
+                        float(cs_dc), float(cs_r0fac), int(mask), hmask)
         h = ctypes.c_void_p()
         rc = lib().nmg_mesh_build(ctypes.byref(p), ctypes.byref(h))
         if rc:
@@ -310,6 +316,30 @@ class Mesh:
         a mesh built from arrays)."""
         out = [lib().nmg_mesh_element_name(self._h, e) for e in range(self.nelem)]
         return None if any(x is None for x in out) else [x.decode() for x in out]
+
+    @classmethod
+    def concat(cls, meshes):
+        """One mesh of several of the same n, elements renumbered in order
+        (nmg_mesh_concat)."""
+        arr = (ctypes.c_void_p * len(meshes))(*[m_._h for m_ in meshes])
+        h = ctypes.c_void_p()
+        if lib().nmg_mesh_concat(arr, len(meshes), ctypes.byref(h)):
+            raise NmgError(f"nmg_mesh_concat: {lib().nmg_mesh_last_error().decode()}")
+        return cls(h.value)
+
+    def hanging(self):
+        """Non-conforming faces: (hface [H,2], hoff [H*n*n+1], hsrc [C,2],
+        hpos [C,2]) — per face node the contributions averaged into its trace."""
+        H, C = ctypes.c_int64(), ctypes.c_int64()
+        lib().nmg_mesh_get_hanging(self._h, ctypes.byref(H), ctypes.byref(C), None, None, None,
+                                   None)
+        hface = np.zeros((H.value, 2), np.int32)
+        hoff = np.zeros(H.value * self.n * self.n + 1 if H.value else 0, np.int32)
+        hsrc = np.zeros((C.value, 2), np.int32)
+        hpos = np.zeros((C.value, 2))
+        lib().nmg_mesh_get_hanging(self._h, ctypes.byref(H), ctypes.byref(C), _ptr(hface),
+                                   _ptr(hoff), _ptr(hsrc), _ptr(hpos))
+        return hface, hoff, hsrc, hpos
 
     def faces(self):
         nb = np.zeros((self.nelem, 6), np.int32)

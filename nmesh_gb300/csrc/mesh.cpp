@@ -167,14 +167,14 @@ void elem_bbox(const double pb[6], int L, const int ixyz[3], double bb[6]) {
   }
 }
 
-// fill geometry for all elements of the given patches, uniform level L,
-// elements of a patch in Morton (Z) order; patches in fvmask get equally
-// spaced points
-void fill_geometry(nmg_mesh &m, const std::vector<Patch> &pats, int L, int32_t fvmask) {
+// fill geometry for all elements of the given patches, patch p at uniform
+// level L[p], elements of a patch in Morton (Z) order; patches in fvmask get
+// equally spaced points
+void fill_geometry(nmg_mesh &m, const std::vector<Patch> &pats, const std::vector<int> &L,
+                   int32_t fvmask) {
   const int n = m.n, np = n * n * n;
-  const int ne1 = 1 << L;
-  const int64_t per = (int64_t)ne1 * ne1 * ne1;
-  m.nelem = per * (int64_t)pats.size();
+  m.nelem = 0;
+  for (size_t p = 0; p < pats.size(); p++) m.nelem += (int64_t)1 << (3 * L[p]);
   m.patches = pats;
   m.pat.resize(m.nelem);
   m.bbox.resize(m.nelem * 6);
@@ -183,22 +183,28 @@ void fill_geometry(nmg_mesh &m, const std::vector<Patch> &pats, int L, int32_t f
   m.dXdx.resize(m.nelem * 9 * np);
   m.fv.assign(m.nelem, 0);
   m.names.assign(m.nelem, std::string());
+  m.level.assign(m.nelem, 0);
+  m.ixyz.assign(m.nelem * 3, 0);
   int64_t e = 0;
   for (size_t p = 0; p < pats.size(); p++) {
+    const int Lp = L[p];
+    const int64_t per = (int64_t)1 << (3 * Lp);
     for (int64_t mc = 0; mc < per; mc++, e++) {
       int ixyz[3] = {0, 0, 0};
-      for (int bit = 0; bit < L; bit++)
+      for (int bit = 0; bit < Lp; bit++)
         for (int d = 0; d < 3; d++) ixyz[d] |= (int)((mc >> (3 * bit + d)) & 1) << bit;
-      elem_bbox(pats[p].bbox, L, ixyz, &m.bbox[e * 6]);
+      elem_bbox(pats[p].bbox, Lp, ixyz, &m.bbox[e * 6]);
       // elmname: patch, then one octree child digit per level, bit d set
       // for the upper half in direction d (connections.c:819-866,1186-1200)
       std::string nm = std::to_string(p) + "_";
-      for (int ll = 1; ll <= L; ll++) {
+      for (int ll = 1; ll <= Lp; ll++) {
         int dig = 0;
-        for (int d = 0; d < 3; d++) dig |= ((ixyz[d] >> (L - ll)) & 1) << d;
+        for (int d = 0; d < 3; d++) dig |= ((ixyz[d] >> (Lp - ll)) & 1) << d;
         nm += (char)('0' + dig);
       }
       m.names[e] = nm;
+      m.level[e] = Lp;
+      for (int d = 0; d < 3; d++) m.ixyz[e * 3 + d] = ixyz[d];
       m.pat[e] = (int32_t)p;
       m.curvi[e] = pats[p].cubed ? 1 : 0;
       const bool isfv = (fvmask >> p) & 1;
@@ -493,6 +499,141 @@ std::string pack_faces(nmg_mesh &m, const int64_t *nbnode, const double period[3
       m.nb[e * 6 + f] = (int32_t)e2;
       m.code[e * 6 + f] = f2 | (found << 3) | (mixed ? NMG_CODE_MIXED : 0);
     }
+  if (m.level.empty()) return "";
+
+  // Non-conforming faces of a generated mesh (patches at different levels):
+  // a face without a conforming neighbour that lies on its parent's face is
+  // matched against the coarser elements' faces by the parent face's
+  // corners, which the four siblings on that face carry.  The neighbour
+  // relation set_ajsurf_vl (src/main/amr/surface.c:799-1360) works with:
+  // each face node takes the average of the neighbour faces that contain it,
+  // each interpolated at the node's position (basis_interp2d_toIpoints).
+  std::vector<int64_t> pstart;
+  for (int64_t e = 0; e < E; e++)
+    if (pstart.empty() || m.pat[e] != m.pat[pstart.back()]) pstart.push_back(e);
+  auto elem_of = [&](int p, const int q[3], int L) {
+    int64_t mc = 0;
+    for (int bit = 0; bit < L; bit++)
+      for (int d = 0; d < 3; d++) mc |= (int64_t)((q[d] >> bit) & 1) << (3 * bit + d);
+    return pstart[p] + mc;
+  };
+  struct HPair { int64_t fe; int ff; int64_t ce; int cf; int A, B, o; };
+  std::vector<HPair> pairs;
+  for (int64_t e = 0; e < E; e++)
+    for (int f = 0; f < 6; f++) {
+      const int L = m.level[e];
+      if (m.nb[e * 6 + f] >= 0 || L < 1) continue;
+      const int d = f >> 1, s = f & 1, d1 = d == 0 ? 1 : 0, d2 = d == 2 ? 1 : 2;
+      const int *q = &m.ixyz[e * 3];
+      if ((q[d] & 1) != s) continue;  // not on the parent's face f
+      int64_t sib[4];
+      double corner[4][3], pc[3];
+      for (int t = 0; t < 4; t++) {
+        int qs[3] = {q[0], q[1], q[2]};
+        qs[d1] = (qs[d1] & ~1) | (t & 1);
+        qs[d2] = (qs[d2] & ~1) | (t >> 1);
+        sib[t] = elem_of(m.pat[e], qs, L);
+        pos(sib[t], face_node(n, f, (t & 1) * (n - 1), (t >> 1) * (n - 1)), corner[t]);
+      }
+      for (int dd = 0; dd < 3; dd++) {
+        double sum = 0;
+        for (int t = 0; t < 4; t++)
+          sum += m.xyz[(sib[t] * 3 + dd) * np +
+                       face_node(n, f, (t & 1) * (n - 1), (t >> 1) * (n - 1))];
+        pc[dd] = wrap1(0.25 * sum, per[dd]);
+      }
+      int64_t match = -1;
+      for (int dz = -1; dz <= 1 && match < 0; dz++)
+        for (int dy = -1; dy <= 1 && match < 0; dy++)
+          for (int dx = -1; dx <= 1 && match < 0; dx++) {
+            int off[3] = {dx, dy, dz};
+            auto it = h.find(kcell(pc, off));
+            if (it == h.end()) continue;
+            for (int64_t g : it->second)
+              if (m.nb[g] < 0 && m.level[g / 6] == L - 1 && dist2(pc, &cen[g * 3]) < tol * tol) {
+                match = g;
+                break;
+              }
+          }
+      if (match < 0) continue;  // outer face
+      const int64_t e2 = match / 6;
+      const int f2 = (int)(match % 6);
+      int found = -1;
+      for (int o = 0; o < 8 && found < 0; o++) {
+        int ok = 1;
+        for (int t = 0; t < 4 && ok; t++) {
+          int a2, b2;
+          orient_map(n, o, (t & 1) * (n - 1), (t >> 1) * (n - 1), &a2, &b2);
+          double p2[3];
+          pos(e2, face_node(n, f2, a2, b2), p2);
+          if (dist2(corner[t], p2) > tol * tol) ok = 0;
+        }
+        if (ok) found = o;
+      }
+      if (found < 0) return "non-conforming face corners do not coincide";
+      pairs.push_back({e, f, e2, f2, q[d1] & 1, q[d2] & 1, found});
+    }
+  if (pairs.empty()) return "";
+
+  const double tq = 1e-10;  // a node on the line between two fine faces belongs to both
+  const std::vector<double> &x = m.x;
+  auto add_face = [&](int64_t e, int f) {
+    m.hface.push_back((int32_t)e);
+    m.hface.push_back(f);
+  };
+  auto add_src = [&](int64_t e, int f, double u, double v) {
+    m.hsrc.push_back((int32_t)e);
+    m.hsrc.push_back(f);
+    m.hpos.push_back(u);
+    m.hpos.push_back(v);
+  };
+  m.hoff.assign(1, 0);
+  // fine faces: one contribution per node, the coarse face at the node's
+  // position in the parent face mapped by the orientation
+  for (const HPair &P : pairs) {
+    add_face(P.fe, P.ff);
+    const int sw = P.o & 1, fa = (P.o >> 1) & 1, fb = (P.o >> 2) & 1;
+    for (int b = 0; b < n; b++)
+      for (int a = 0; a < n; a++) {
+        const double pa = (x[a] + (2 * P.A - 1)) * 0.5, pb = (x[b] + (2 * P.B - 1)) * 0.5;
+        double u = sw ? pb : pa, v = sw ? pa : pb;
+        if (fa) u = -u;
+        if (fb) v = -v;
+        add_src(P.ce, P.cf, u, v);
+        m.hoff.push_back((int32_t)(m.hsrc.size() / 2));
+      }
+    m.nb[P.fe * 6 + P.ff] = (int32_t)P.ce;
+    m.code[P.fe * 6 + P.ff] = P.cf | (P.o << 3) | NMG_CODE_HANG;
+  }
+  // coarse faces: each node averages the fine faces that contain it
+  std::vector<size_t> order(pairs.size());
+  for (size_t i = 0; i < order.size(); i++) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](size_t i, size_t j) {
+    if (pairs[i].ce != pairs[j].ce) return pairs[i].ce < pairs[j].ce;
+    if (pairs[i].cf != pairs[j].cf) return pairs[i].cf < pairs[j].cf;
+    return pairs[i].A + 2 * pairs[i].B < pairs[j].A + 2 * pairs[j].B;
+  });
+  for (size_t i = 0; i < order.size(); i += 4) {
+    const HPair &P0 = pairs[order[i]];
+    if (i + 3 >= order.size() || pairs[order[i + 3]].ce != P0.ce || pairs[order[i + 3]].cf != P0.cf)
+      return "coarse face of element " + std::to_string(P0.ce) +
+             " does not have four finer neighbours";
+    add_face(P0.ce, P0.cf);
+    const int sw = P0.o & 1, fa = (P0.o >> 1) & 1, fb = (P0.o >> 2) & 1;
+    for (int b2 = 0; b2 < n; b2++)
+      for (int a2 = 0; a2 < n; a2++) {
+        const double u = fa ? -x[a2] : x[a2], v = fb ? -x[b2] : x[b2];
+        const double pa = sw ? v : u, pb = sw ? u : v;
+        for (int t = 0; t < 4; t++) {
+          const HPair &P = pairs[order[i + t]];
+          const bool ina = P.A ? pa >= -tq : pa <= tq, inb = P.B ? pb >= -tq : pb <= tq;
+          if (ina && inb) add_src(P.fe, P.ff, 2 * pa - (2 * P.A - 1), 2 * pb - (2 * P.B - 1));
+        }
+        m.hoff.push_back((int32_t)(m.hsrc.size() / 2));
+      }
+    m.nb[P0.ce * 6 + P0.cf] = (int32_t)P0.fe;
+    m.code[P0.ce * 6 + P0.cf] = P0.ff | NMG_CODE_HANG;
+  }
   return "";
 }
 
@@ -569,7 +710,10 @@ int nmg_mesh_build(const nmg_mesh_params *p, nmg_mesh **out) {
       delete m;
       return fail(NMG_EUNSUP, "nmg_mesh_build: unknown mesh_type");
     }
-    fill_geometry(*m, pats, p->luni, p->fv);
+    std::vector<int> L(pats.size(), p->luni);
+    for (size_t q = 0; q < pats.size(); q++)
+      if ((p->hrefine >> q) & 1) L[q]++;
+    fill_geometry(*m, pats, L, p->fv);
     bool anyfv = false;
     for (int64_t e = 0; e < m->nelem; e++) anyfv = anyfv || m->fv[e];
     if (!anyfv) m->fv.clear();
@@ -675,6 +819,18 @@ int nmg_mesh_get_fv(const nmg_mesh *m, int32_t *fv) {
   return NMG_OK;
 }
 
+int nmg_mesh_get_hanging(const nmg_mesh *m, int64_t *nface, int64_t *ncontrib, int32_t *hface,
+                         int32_t *hoff, int32_t *hsrc, double *hpos) {
+  if (!m || !nface || !ncontrib) return fail(NMG_EINVAL, "nmg_mesh_get_hanging: null argument");
+  *nface = (int64_t)m->hface.size() / 2;
+  *ncontrib = (int64_t)m->hsrc.size() / 2;
+  if (hface) std::copy(m->hface.begin(), m->hface.end(), hface);
+  if (hoff) std::copy(m->hoff.begin(), m->hoff.end(), hoff);
+  if (hsrc) std::copy(m->hsrc.begin(), m->hsrc.end(), hsrc);
+  if (hpos) std::copy(m->hpos.begin(), m->hpos.end(), hpos);
+  return NMG_OK;
+}
+
 int nmg_uniform_points(int32_t n, double *x) {
   if (n < 1 || n > 64 || !x) return fail(NMG_EINVAL, "nmg_uniform_points: bad argument");
   std::vector<double> w(n), D((size_t)n * n);
@@ -703,6 +859,7 @@ int nmg_mesh_concat(const nmg_mesh *const *ms, int32_t count, nmg_mesh **out) {
     m->D = ms[0]->D;
     m->xu = ms[0]->xu;
     int64_t off = 0;
+    m->hoff.assign(1, 0);
     for (int i = 0; i < count; i++) {
       const nmg_mesh &a = *ms[i];
       for (int64_t e = 0; e < a.nelem; e++) m->pat.push_back(a.pat[e]);
@@ -713,9 +870,22 @@ int nmg_mesh_concat(const nmg_mesh *const *ms, int32_t count, nmg_mesh **out) {
       for (size_t q = 0; q < a.nb.size(); q++)
         m->nb.push_back(a.nb[q] < 0 ? -1 : (int32_t)(a.nb[q] + off));
       m->code.insert(m->code.end(), a.code.begin(), a.code.end());
+      // non-conforming faces keep their interpolation lists, renumbered
+      for (size_t q = 0; q < a.hface.size(); q += 2) {
+        m->hface.push_back((int32_t)(a.hface[q] + off));
+        m->hface.push_back(a.hface[q + 1]);
+      }
+      const int32_t c0 = m->hoff.back();
+      for (size_t q = 1; q < a.hoff.size(); q++) m->hoff.push_back(c0 + a.hoff[q]);
+      for (size_t q = 0; q < a.hsrc.size(); q += 2) {
+        m->hsrc.push_back((int32_t)(a.hsrc[q] + off));
+        m->hsrc.push_back(a.hsrc[q + 1]);
+      }
+      m->hpos.insert(m->hpos.end(), a.hpos.begin(), a.hpos.end());
       off += a.nelem;
     }
     m->nelem = off;
+    if (m->hface.empty()) m->hoff.clear();
   } catch (const std::bad_alloc &) {
     delete m;
     return fail(NMG_ENOMEM, "nmg_mesh_concat: out of memory");

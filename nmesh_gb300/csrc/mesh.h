@@ -35,11 +35,25 @@ struct nmg_mesh {
                                     // for a described one)
   std::vector<std::string> names;   // [E] the reference's element names
                                     // "<patch>_<octree digits>" (generated meshes)
+  std::vector<int32_t> level;       // [E] refinement level (generated meshes)
+  std::vector<int32_t> ixyz;        // [E][3] integer position at that level
+  // Non-conforming faces (a level jump between neighbours): per such face
+  // (element, face) and, per face node, the list of contributions (source
+  // element, source face, the node's position in the source face's
+  // in-plane coordinates in [-1,1]); the trace is the average of the
+  // contributions' interpolated values.
+  std::vector<int32_t> hface;       // [H][2]
+  std::vector<int32_t> hoff;        // [H*n*n + 1]
+  std::vector<int32_t> hsrc;        // [C][2]
+  std::vector<double> hpos;         // [C][2]
 };
 
 // face-table code bit: the neighbour has the other point type (DG / FV), its
 // trace is interpolated onto this face's points
 constexpr int NMG_CODE_MIXED = 64;
+// face-table bit: the face is non-conforming (neighbours of another level),
+// its trace is interpolated from the listed neighbour faces
+constexpr int NMG_CODE_HANG = 128;
 
 namespace nmg {
 // LGL nodes/weights and differentiation matrix (Legendre.c / Lagrange.c)

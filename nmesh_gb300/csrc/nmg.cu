@@ -217,6 +217,12 @@ struct nmg_ctx {
   double *d_ghost = nullptr, *d_gM = nullptr;
   double *d_fvbxyz = nullptr, *d_fvbnrm = nullptr;  // outer faces on equally spaced points
   int ghost_cap = 0;
+  // non-conforming faces: their traces (slots of d_ghost) are interpolated
+  // from the neighbour faces each stage (stage_fv.cu: hang_kernel)
+  int nhang = 0;
+  int *d_hoff = nullptr;    // [H*nn + 1] contribution offsets per face node
+  int *d_hsrc = nullptr;    // [C][2] source element, source face
+  double *d_hw = nullptr;   // [C][2][n] Lagrange weights at the node's position
   // switchable contexts: element types can change (nmg_set_element_types)
   bool switchable = false;
   std::vector<int32_t> h_nb, h_code0, h_bslot0, h_fv;  // face table without the mixed bit,
@@ -274,8 +280,14 @@ int nmg_ctx_fail_static(nmg_ctx *c, int code, const char *msg) {
 // three launches: the interpolated interface traces of the stage input, the
 // DG kernel over all elements (writing only the DG ones) and the
 // finite-volume kernel over the finite-volume elements.
-static cudaError_t run_stage(nmg_ctx *c, int v, StageParams P) {
+static cudaError_t run_stage(nmg_ctx *c, int v, StageParams P, bool traces = true) {
   cudaError_t e;
+  if (c->nhang > 0 && traces) {
+    e = nmgk::hang_launch(c->nhang, c->n, c->d_hoff, c->d_hsrc, c->d_hw, P.win, c->d_ghost,
+                          c->stream);
+    if (e != cudaSuccess) return e;
+    c->launches++;
+  }
   if (c->mixed) {
     e = nmgk::ghost_launch(c->nghost, c->n, c->d_gtab, c->d_isfv, c->d_gM, P.win, c->d_ghost,
                            c->stream);
@@ -606,6 +618,10 @@ static int create_impl(const nmg_mesh *m, int32_t bc_kind, const double k[3], bo
   int64_t nfv = 0;
   for (size_t e = 0; e < m->fv.size(); e++) nfv += m->fv[e] ? 1 : 0;
   c->switchable = switchable;
+  const int64_t H = (int64_t)m->hface.size() / 2;
+  if (H > 0 && (nfv > 0 || switchable))
+    return set_err(c, NMG_EUNSUP,
+                   "nmg_create: non-conforming faces are supported on DG meshes only");
   if (const char *nc = getenv("NMG_COPY_CHUNKS")) {
     const int v = atoi(nc);
     if (v >= 1 && v <= nmg_ctx::kChunks) c->nchunks = v;
@@ -749,7 +765,7 @@ static int create_impl(const nmg_mesh *m, int32_t bc_kind, const double k[3], bo
       std::vector<double> &BX = uni ? fvbxyz : bxyz, &BN = uni ? fvbnrm : bnrm;
       for (int f = 0; f < 6; f++) {
         const int bs = c->h_bslot0[e * 6 + f];
-        if (bs < 0) continue;
+        if (bs < 0 || m->nb[e * 6 + f] >= 0) continue;
         const int d = f >> 1;
         const double sig = (f & 1) ? 1. : -1.;
         for (int b = 0; b < n; b++)
@@ -881,6 +897,15 @@ static int create_impl(const nmg_mesh *m, int32_t bc_kind, const double k[3], bo
     if (e2 != cudaSuccess || bytes == 0) return e2;
     return cudaMemcpy(*dst, vec.data(), bytes, cudaMemcpyHostToDevice);
   };
+  // non-conforming faces take their trace from slot h of the interface-trace
+  // buffer (the kernels' ghost-trace path); their bslot is that slot, not an
+  // outer-face slot
+  for (int64_t h = 0; h < H; h++) {
+    const int64_t q = (int64_t)m->hface[2 * h] * 6 + m->hface[2 * h + 1];
+    if (m->nb[q] < 0) return set_err(c, NMG_EMESH, "nmg_create: non-conforming face without neighbour");
+    c->h_code0[q] |= NMG_CODE_MIXED;
+    c->h_bslot0[q] = (int)h;
+  }
   CK(up(&c->d_nb, m->nb));
   CK(up(&c->d_code, c->h_code0));
   CK(up(&c->d_cslot, cslot));
@@ -919,6 +944,36 @@ static int create_impl(const nmg_mesh *m, int32_t bc_kind, const double k[3], bo
   if (c->fv) {
     int rc = upload_type_tables(c);
     if (rc) return rc;
+  }
+  if (H > 0) {
+    // per contribution the Lagrange weights of the source face's points at
+    // the node's position in both in-plane directions (Lagrange_of_x,
+    // src/main/basis/Lagrange.c:151-159, with the weights of :15-27)
+    const double *xl = m->x.data();
+    std::vector<double> wl(n);
+    for (int i = 0; i < n; i++) {
+      double denom = 1.;
+      for (int j = 0; j < n; j++)
+        if (j != i) denom *= (xl[i] - xl[j]);
+      wl[i] = 1. / denom;
+    }
+    const size_t Cn = m->hsrc.size() / 2;
+    std::vector<double> hw(Cn * 2 * n);
+    for (size_t q = 0; q < Cn; q++)
+      for (int dd = 0; dd < 2; dd++)
+        for (int k2 = 0; k2 < n; k2++) {
+          double prod = 1.;
+          for (int j = 0; j < n; j++)
+            if (j != k2) prod *= (m->hpos[2 * q + dd] - xl[j]);
+          hw[(q * 2 + dd) * n + k2] = prod * wl[k2];
+        }
+    CK(up(&c->d_hoff, m->hoff));
+    CK(up(&c->d_hsrc, m->hsrc));
+    CK(up(&c->d_hw, hw));
+    CK(cudaMalloc((void **)&c->d_ghost, sizeof(double) * 4 * nn * H));
+    CK(cudaMemset(c->d_ghost, 0, sizeof(double) * 4 * nn * H));
+    c->ghost_cap = (int)H;
+    c->nhang = (int)H;
   }
   for (int b = 0; b < 4; b++) {
     CK(cudaMalloc((void **)&c->d_buf[b], c->state_len * sizeof(double)));
@@ -1166,6 +1221,7 @@ void nmg_destroy(nmg_ctx *c) {
   cudaFree(c->d_D);
   cudaFree(c->d_fvgeo); cudaFree(c->d_fvdist); cudaFree(c->d_fvdxb);
   cudaFree(c->d_fvlist); cudaFree(c->d_gtab); cudaFree(c->d_isfv); cudaFree(c->d_ghost);
+  cudaFree(c->d_hoff); cudaFree(c->d_hsrc); cudaFree(c->d_hw);
   cudaFree(c->d_gM); cudaFree(c->d_fvbxyz); cudaFree(c->d_fvbnrm); cudaFree(c->d_PR);
   cudaFree(c->d_conv); cudaFree(c->d_mm); cudaFree(c->d_trb); cudaFree(c->d_score);
   cudaFree(c->d_up); cudaFree(c->d_pers); cudaFree(c->d_wq); cudaFree(c->d_npart);
@@ -1454,7 +1510,7 @@ static int last_step_streamed(nmg_ctx *c, double t, double dt, double *host_u,
       const int64_t eb = std::min(E, ea + chunk);
       P.ebase = (int)ea;
       P.ecount = (int)(eb - ea);
-      CK(run_stage(c, c->sel, P));
+      CK(run_stage(c, c->sel, P, ea == 0));  // traces once per stage
       CK(cudaEventRecord(c->chunk_ev[k], c->stream));
       CK(cudaStreamWaitEvent(c->copy_stream, c->chunk_ev[k], 0));
       CK(cudaMemcpyAsync(host_u + ea * per, ACC + ea * per, (size_t)(eb - ea) * per * sizeof(double),
@@ -1472,7 +1528,7 @@ int nmg_rk4_steps_host(nmg_ctx *c, double t, double dt, int32_t nsteps, double *
   if (nsteps < 0) return set_err(c, NMG_EINVAL, "nmg_rk4_steps_host: bad argument");
   const size_t bytes = c->state_len * sizeof(double);
   int rc;
-  if (!c->fv && nsteps == 1)  // copy in, step and copy out overlapped
+  if (!c->fv && !c->nhang && nsteps == 1)  // copy in, step and copy out overlapped
     return last_step_streamed(c, t, dt, host_u, host_u);
   CK(cudaMemcpyAsync(c->d_buf[c->cur], host_u, bytes, cudaMemcpyHostToDevice, c->stream));
   if (c->mixed || nsteps == 0) {
@@ -1500,6 +1556,7 @@ int nmg_rhs_vjp(nmg_ctx *c, double t, const double *w_dev, const double *rbar_de
   if (!c || !rbar_dev || !wbar_dev || rbar_dev == wbar_dev)
     return set_err(c, NMG_EINVAL, "nmg_rhs_vjp: need distinct rbar and wbar device buffers");
   if (c->fv) return set_err(c, NMG_EUNSUP, "nmg_rhs_vjp: finite-volume RHS is nonlinear");
+  if (c->nhang) return set_err(c, NMG_EUNSUP, "nmg_rhs_vjp: no transposed non-conforming faces");
   if (c->numflux != NMG_NUMFLUX_LLF)
     return set_err(c, NMG_EUNSUP, "nmg_rhs_vjp: the transposed kernel implements LLF only");
   StageParams P = base_params(c);
@@ -1516,6 +1573,7 @@ int nmg_rk4_step_vjp(nmg_ctx *c, double t, double dt, const double *u_n_dev, dou
   (void)u_n_dev;  // linear RHS: the step's Jacobian is P(dt L), independent of u_n
   if (!c || !ubar_dev) return set_err(c, NMG_EINVAL, "nmg_rk4_step_vjp: null argument");
   if (c->fv) return set_err(c, NMG_EUNSUP, "nmg_rk4_step_vjp: finite-volume RHS is nonlinear");
+  if (c->nhang) return set_err(c, NMG_EUNSUP, "nmg_rk4_step_vjp: no transposed non-conforming faces");
   if (c->numflux != NMG_NUMFLUX_LLF)
     return set_err(c, NMG_EUNSUP, "nmg_rk4_step_vjp: the transposed kernel implements LLF only");
   double *acc = c->d_buf[1 - c->cur];  // free between steps
@@ -1533,6 +1591,8 @@ int nmg_rk4_step_vjp(nmg_ctx *c, double t, double dt, const double *u_n_dev, dou
 int nmg_adjoint_gradient(nmg_ctx *c, double t0, double dt, int32_t nsteps, int32_t ckpt_every,
                          const double *weight_dev, double *J, double *grad_dev) {
   if (c && c->fv) return set_err(c, NMG_EUNSUP, "nmg_adjoint_gradient: finite-volume RHS is nonlinear");
+  if (c && c->nhang)
+    return set_err(c, NMG_EUNSUP, "nmg_adjoint_gradient: no transposed non-conforming faces");
   if (c && c->numflux != NMG_NUMFLUX_LLF)
     return set_err(c, NMG_EUNSUP, "nmg_adjoint_gradient: the transposed kernel implements LLF only");
   if (!c || !weight_dev || !J || !grad_dev || nsteps <= 0 || ckpt_every <= 0)
@@ -1755,6 +1815,13 @@ static int batch_upload_params(nmg_batch *b, double dt) {
 
 static int batch_enqueue_stage(nmg_batch *b, int par, int s) {
   const int G = (int)b->gctx.size();
+  for (int g = 0; g < G; g++) {  // traces of non-conforming faces first
+    nmg_ctx *c = b->gctx[g];
+    if (c->nhang <= 0) continue;
+    BK(nmgk::hang_launch(c->nhang, c->n, c->d_hoff, c->d_hsrc, c->d_hw,
+                         b->hparams[(par * 4 + s) * G + g].win, c->d_ghost, b->stream));
+    b->launches++;
+  }
   if (b->grouped) {
     for (int g = 0; g < G; g++) {
       nmg_ctx *c = b->gctx[g];

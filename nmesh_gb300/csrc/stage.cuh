@@ -371,6 +371,10 @@ int fv_variants(int n, Variant *out, int cap);
 // gtab[g] = (e, f, e2, code), M = [2][n][n] (Lagrange weights of the LGL
 // points at the equally spaced positions; piecewise-linear weights of the
 // equally spaced points at the LGL positions)
+// traces of non-conforming faces: per slot, field and face node the average
+// over its contributions of the source face interpolated at the node
+cudaError_t hang_launch(int nhang, int n, const int *hoff, const int *hsrc, const double *hw,
+                        const double *win, double *ghost, cudaStream_t st);
 cudaError_t ghost_launch(int nghost, int n, const int *gtab, const unsigned char *isfv,
                          const double *M, const double *win, double *ghost, cudaStream_t st);
 // u of the listed elements <- (M x M x M) u (all fields), in place

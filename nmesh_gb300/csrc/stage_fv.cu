@@ -554,6 +554,50 @@ __global__ void __launch_bounds__(256) ghost_kernel(int nghost, int n, const int
 }
 }  // namespace
 
+namespace {
+// One thread per (slot, field, face node) of a non-conforming face: each
+// contribution is the source face's plane interpolated at the node,
+// sum_b sum_a v(a,b) B1[a] B2[b] (basis_interp2d_toIpoints), and the node
+// takes their average (set_ajsurf_vl, src/main/amr/surface.c:1320-1337),
+// rounded in that order (this file has no FMA contraction).
+__global__ void __launch_bounds__(256) hang_kernel(int nhang, int n, const int *hoff,
+                                                  const int *hsrc, const double *hw,
+                                                  const double *win, double *ghost) {
+  const int nn = n * n, np = nn * n;
+  const int64_t total = (int64_t)nhang * 4 * nn;
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    const int h = (int)(q / (4 * nn)), rem = (int)(q - (int64_t)h * 4 * nn);
+    const int l = rem / nn, ab = rem - l * nn;
+    const int c0 = __ldg(hoff + (size_t)h * nn + ab), c1 = __ldg(hoff + (size_t)h * nn + ab + 1);
+    double acc = 0.;
+    for (int c = c0; c < c1; c++) {
+      const int e2 = __ldg(hsrc + 2 * c), f2 = __ldg(hsrc + 2 * c + 1);
+      const double *B1 = hw + (size_t)c * 2 * n, *B2 = B1 + n;
+      const double *v = win + ((size_t)e2 * NF + l) * np;
+      double sum = 0.;
+      for (int k = 0; k < n; k++) {
+        const double b2 = __ldg(B2 + k);
+        for (int j = 0; j < n; j++)
+          sum += __ldg(v + fv_exact::fnode(n, f2, j, k)) * __ldg(B1 + j) * b2;
+      }
+      acc += sum;
+    }
+    if (c1 - c0 > 1) acc /= (c1 - c0);
+    ghost[(size_t)h * 4 * nn + l * nn + ab] = acc;
+  }
+}
+}  // namespace
+
+cudaError_t hang_launch(int nhang, int n, const int *hoff, const int *hsrc, const double *hw,
+                        const double *win, double *ghost, cudaStream_t st) {
+  if (nhang <= 0) return cudaSuccess;
+  const int64_t total = (int64_t)nhang * 4 * n * n;
+  const int grid = (int)std::min<int64_t>((total + 255) / 256, 152 * 16);
+  hang_kernel<<<grid, 256, 0, st>>>(nhang, n, hoff, hsrc, hw, win, ghost);
+  return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------------------
 // element switches and trouble indicators
 // ---------------------------------------------------------------------------

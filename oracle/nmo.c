@@ -87,6 +87,13 @@ typedef struct nmo_mesh {
   const int32_t *mixface;   /* [e][6][3] (e', f', orientation) of the faces
                                marked -2 in nbnode; NULL if none */
   int numflux;              /* 0: LLF, 1: upwind (par scalarwave1_numflux) */
+  /* non-conforming faces (nbnode -3): per face node (e, f, JK) the
+     contributions hang_off[q] .. hang_off[q+1]-1, q = (e*6+f)*n*n + JK,
+     each a neighbour face (hang_src: e', f') and the node's position on it
+     (hang_pos: in-plane coordinates in [-1,1]); NULL if none */
+  const int32_t *hang_off;  /* [e*6*n*n + 1] */
+  const int32_t *hang_src;  /* [c][2] */
+  const double *hang_pos;   /* [c][2] */
 } nmo_mesh;
 
 /* points of both point types: LGL (DG) with their Lagrange weights, and
@@ -449,6 +456,36 @@ static void mixed_trace(const nmo_mesh *m, const nmo_pts *P, int e, int f, int a
   }
 }
 
+/* Exterior state at face node JK of a non-conforming face: each neighbour
+   face that contains the node interpolated there (basis_interp2d_toIpoints
+   with Lagrange_of_x), then the average over those neighbours
+   (set_ajsurf_vl, src/main/amr/surface.c:1160-1340). */
+static void hang_trace(const nmo_mesh *m, const nmo_pts *P, int e, int f, int JK,
+                       const double *w, double ua[5])
+{
+  int n = m->n, np = n * n * n, l, j, k, c;
+  size_t q = ((size_t)e * 6 + f) * n * n + JK;
+  int c0 = m->hang_off[q], c1 = m->hang_off[q + 1], cnt = c1 - c0;
+  for (l = 0; l < NF; l++) ua[l] = 0.;
+  for (c = c0; c < c1; c++) {
+    int e2 = m->hang_src[2 * c], f2 = m->hang_src[2 * c + 1];
+    double B1[64], B2[64];
+    for (k = 0; k < n; k++) {
+      B1[k] = lagrange_of_x(k, m->hang_pos[2 * c], n, P->xl, P->wl);
+      B2[k] = lagrange_of_x(k, m->hang_pos[2 * c + 1], n, P->xl, P->wl);
+    }
+    for (l = 0; l < NF; l++) {
+      const double *v = w + ((size_t)e2 * NF + l) * np;
+      double sum = 0.;
+      for (k = 0; k < n; k++)
+        for (j = 0; j < n; j++) sum += v[face_node(n, f2, j, k)] * B1[j] * B2[k];
+      ua[l] += sum;
+    }
+  }
+  if (cnt > 1)
+    for (l = 0; l < NF; l++) ua[l] /= cnt;
+}
+
 static void face_fnum(const nmo_mesh *m, const nmo_pts *P, int e, int f, int ijk, int JK,
                       double t, const double *w, double fi[5], double fnum[5])
 {
@@ -463,6 +500,8 @@ static void face_fnum(const nmo_mesh *m, const nmo_pts *P, int e, int f, int ijk
     for (l = 0; l < NF; l++) ua[l] = w[(size_t)en * NF * np + l * np + in];
   } else if (nb == -2) {
     mixed_trace(m, P, e, f, JK % n, JK / n, w, ua);
+  } else if (nb == -3) {
+    hang_trace(m, P, e, f, JK, w, ua);
   } else if (m->bc == 0) {
     const double *X = m->xyz + (size_t)e * 3 * np;
     double xyz[3] = {X[ijk], X[np + ijk], X[2 * np + ijk]};

@@ -40,7 +40,8 @@ class _Mesh(ctypes.Structure):
                 ("k", ctypes.c_double * 3), ("fv", ctypes.c_void_p),
                 ("fv_rec", ctypes.c_int), ("fv_extrap", ctypes.c_int),
                 ("fv_w3ratio", ctypes.c_double), ("mixface", ctypes.c_void_p),
-                ("numflux", ctypes.c_int)]
+                ("numflux", ctypes.c_int), ("hang_off", ctypes.c_void_p),
+                ("hang_src", ctypes.c_void_p), ("hang_pos", ctypes.c_void_p)]
 
 # reconstruction modes (reference par fv_rec) and div(f) extrapolation
 # modes (par fv_divf_extrap) understood by the oracle
@@ -188,16 +189,151 @@ def match_faces(xyz, n, period=None, tol=1e-9, fv=None):
     return nb
 
 
+def match_hanging(xyz, n, pat, bbox, nbnode, tol=1e-9):
+    """Non-conforming faces of a mesh whose patches sit at different
+    uniform levels (the reference's amr_hrefine_p).
+
+    Faces left outer (-1) by match_faces are tested: a face that lies on its
+    parent element's face is the quarter of a coarser element's face when
+    the parent face's corners (carried by the four siblings on it) are that
+    face's corners.  Elements are located by their bbox within the patch
+    (level and integer position), the orientation between the parent face
+    and the coarse face from the corners.  Each node of a fine face takes
+    the coarse face at its position; each node of a coarse face averages
+    the fine faces that contain it (set_ajsurf_vl,
+    src/main/amr/surface.c:1160-1340).  Returns (nbnode with -3 on those
+    faces, (hang_off, hang_src, hang_pos)) or (nbnode, None)."""
+    E = xyz.shape[0]
+    nn = n * n
+    planes = [face_plane_index(n, f) for f in range(6)]
+    corners = [0, n - 1, n * (n - 1), n * n - 1]
+    x = lgl(n)[0]
+    nbnode = np.array(nbnode, copy=True)
+
+    def pkey(q):
+        return tuple(np.round(np.asarray(q) / tol).astype(np.int64))
+
+    # level and integer position of each element in its patch
+    ext = {}
+    for e in range(E):
+        lo, hi = ext.get(int(pat[e]), (bbox[e, 0::2].copy(), bbox[e, 1::2].copy()))
+        ext[int(pat[e])] = (np.minimum(lo, bbox[e, 0::2]), np.maximum(hi, bbox[e, 1::2]))
+    lev = np.zeros(E, np.int64)
+    pos = np.zeros((E, 3), np.int64)
+    where = {}
+    for e in range(E):
+        lo, hi = ext[int(pat[e])]
+        h = bbox[e, 1::2] - bbox[e, 0::2]
+        lev[e] = int(round(np.log2((hi[0] - lo[0]) / h[0])))
+        pos[e] = np.round((bbox[e, 0::2] - lo) / h).astype(np.int64)
+        where[(int(pat[e]), int(lev[e])) + tuple(pos[e])] = e
+    # centre keys of the faces still outer
+    free = {}
+    for e in range(E):
+        for f in range(6):
+            if nbnode[e, f, 0] == -1:
+                free.setdefault(pkey(xyz[e][:, planes[f][corners]].mean(axis=1)), []).append((e, f))
+
+    def orient(o, a, b):
+        aa, bb = (b, a) if o & 1 else (a, b)
+        return (n - 1 - aa if o & 2 else aa), (n - 1 - bb if o & 4 else bb)
+
+    pairs = []   # (fine e, f, coarse e2, f2, A, B, o)
+    for e in range(E):
+        for f in range(6):
+            if nbnode[e, f, 0] != -1 or lev[e] < 1:
+                continue
+            d, s = f // 2, f % 2
+            d1, d2 = (1, 2) if d == 0 else ((0, 2) if d == 1 else (0, 1))
+            if pos[e, d] % 2 != s:
+                continue
+            cpts = []
+            for t in range(4):
+                q = pos[e].copy()
+                q[d1] = (q[d1] & ~1) | (t & 1)
+                q[d2] = (q[d2] & ~1) | (t >> 1)
+                sib = where[(int(pat[e]), int(lev[e])) + tuple(q)]
+                cpts.append(xyz[sib][:, planes[f][corners[t]]])
+            cand = [g for g in free.get(pkey(np.mean(cpts, axis=0)), [])
+                    if lev[g[0]] == lev[e] - 1]
+            if not cand:
+                continue
+            e2, f2 = cand[0]
+            found = None
+            for o in range(8):
+                ok = True
+                for t in range(4):
+                    a2, b2 = orient(o, (t & 1) * (n - 1), (t >> 1) * (n - 1))
+                    ok = ok and pkey(cpts[t]) == pkey(xyz[e2][:, planes[f2][a2 + n * b2]])
+                if ok:
+                    found = o
+                    break
+            if found is None:
+                raise ValueError("non-conforming face: corners do not match")
+            pairs.append((e, f, e2, f2, int(pos[e, d1] & 1), int(pos[e, d2] & 1), found))
+    if not pairs:
+        return nbnode, None
+    lists = {}
+    for (e, f, e2, f2, A, B, o) in pairs:
+        sw, fa, fb = o & 1, (o >> 1) & 1, (o >> 2) & 1
+        L = []
+        for b in range(n):
+            for a in range(n):
+                pa, pb = (x[a] + (2 * A - 1)) * 0.5, (x[b] + (2 * B - 1)) * 0.5
+                u, v = (pb, pa) if sw else (pa, pb)
+                L.append([(e2, f2, -u if fa else u, -v if fb else v)])
+        lists[(e, f)] = L
+    coarse = {}
+    for P in pairs:
+        coarse.setdefault((P[2], P[3]), []).append(P)
+    for (e2, f2), ps in coarse.items():
+        ps = sorted(ps, key=lambda P: P[4] + 2 * P[5])
+        o = ps[0][6]
+        sw, fa, fb = o & 1, (o >> 1) & 1, (o >> 2) & 1
+        L = []
+        for b2 in range(n):
+            for a2 in range(n):
+                u, v = (-x[a2] if fa else x[a2]), (-x[b2] if fb else x[b2])
+                pa, pb = (v, u) if sw else (u, v)
+                lst = []
+                for (e, f, _, _, A, B, _) in ps:
+                    ina = pa >= -1e-10 if A else pa <= 1e-10
+                    inb = pb >= -1e-10 if B else pb <= 1e-10
+                    if ina and inb:
+                        lst.append((e, f, 2 * pa - (2 * A - 1), 2 * pb - (2 * B - 1)))
+                L.append(lst)
+        lists[(e2, f2)] = L
+    off = np.zeros(E * 6 * nn + 1, np.int32)
+    src, hp = [], []
+    cnt = np.zeros(E * 6 * nn, np.int32)
+    for (e, f), L in lists.items():
+        nbnode[e, f, :] = -3
+        for jk, lst in enumerate(L):
+            cnt[(e * 6 + f) * nn + jk] = len(lst)
+    off[1:] = np.cumsum(cnt)
+    src = np.zeros((int(off[-1]), 2), np.int32)
+    hp = np.zeros((int(off[-1]), 2))
+    for (e, f), L in lists.items():
+        for jk, lst in enumerate(L):
+            q = off[(e * 6 + f) * nn + jk]
+            for i, (es, fs, u, v) in enumerate(lst):
+                src[q + i] = (es, fs)
+                hp[q + i] = (u, v)
+    return nbnode, (off, src, hp)
+
+
 class OracleMesh:
     """Arrays describing a mesh for the oracle, kept alive with the struct."""
 
     def __init__(self, bbox, curvi, dXdx, xyz, nbnode, n, bc=0,
                  k=(1.0, 1.0, 1.0), fv=None, fv_rec="WENOm5_2",
-                 fv_extrap="dnfn_extrap1", fv_w3ratio=2.0, mixface=None, numflux="LLF"):
+                 fv_extrap="dnfn_extrap1", fv_w3ratio=2.0, mixface=None, numflux="LLF",
+                 hang=None):
         """fv: per-element finite-volume flags (None: all DG); fv_rec and
         fv_extrap name the reference's fv_rec / fv_divf_extrap modes;
         mixface: faces between the two point types (see match_faces);
-        numflux: "LLF" or "upwind" (the reference's scalarwave1_numflux)."""
+        numflux: "LLF" or "upwind" (the reference's scalarwave1_numflux);
+        hang: non-conforming face lists (see match_hanging)."""
         self.n = int(n)
         self.bbox = np.ascontiguousarray(bbox, np.float64)
         self.curvi = np.ascontiguousarray(curvi, np.int32)
@@ -207,6 +343,7 @@ class OracleMesh:
         self.nelem = self.bbox.shape[0]
         self.fv = None if fv is None else np.ascontiguousarray(fv, np.int32)
         self.mixface = None if mixface is None else np.ascontiguousarray(mixface, np.int32)
+        self.hang = None if hang is None else tuple(np.ascontiguousarray(a) for a in hang)
         self.s = _Mesh(self.nelem, self.n, self.bbox.ctypes.data,
                        self.curvi.ctypes.data, self.dXdx.ctypes.data,
                        self.xyz.ctypes.data, self.nbnode.ctypes.data, int(bc),
@@ -214,7 +351,9 @@ class OracleMesh:
                        None if self.fv is None else self.fv.ctypes.data,
                        FV_REC[fv_rec], FV_EXTRAP[fv_extrap], float(fv_w3ratio),
                        None if self.mixface is None else self.mixface.ctypes.data,
-                       1 if numflux == "upwind" else 0)
+                       1 if numflux == "upwind" else 0,
+                       *((None,) * 3 if self.hang is None else
+                         tuple(a.ctypes.data for a in self.hang)))
 
     def rhs(self, w, t=0.0):
         w = np.ascontiguousarray(w, np.float64)

@@ -99,6 +99,17 @@ CASES = {
                            dt=0.01, steps=1, eps=0.01, seed=36, checkpoint=True),
     "ckpt_cs7_l1_n3": dict(mesh="cs7", n=3, luni=1, k=(0.3, -0.2, 0.1),
                            dt=0.002, steps=1, eps=0.01, seed=37, checkpoint=True),
+    # non-conforming faces: the listed patches refined one level further
+    # (amr_hrefine_p), face traces interpolated across the level jump
+    "nc_cs7_l0_n5_h0": dict(mesh="cs7", n=5, luni=0, k=(0.3, -0.2, 0.1),
+                            dt=0.002, steps=2, eps=0.02, seed=38, hrefine="0"),
+    "nc_cs7_l0_n4_h1": dict(mesh="cs7", n=4, luni=0, k=(0.25, 0.15, -0.3),
+                            dt=0.002, steps=2, eps=0.02, seed=39, hrefine="1"),
+    "nc_cs7_l1_n5_h02": dict(mesh="cs7", n=5, luni=1, k=(0.3, -0.2, 0.1),
+                             dt=0.002, steps=2, eps=0.02, seed=40, hrefine="0 2"),
+    "nc_upw_cs7_l0_n6_h35": dict(mesh="cs7", n=6, luni=0, k=(0.3, 0.2, -0.1),
+                                 dt=0.002, steps=2, eps=0.02, seed=41, hrefine="3 5",
+                                 numflux="upwind"),
 }
 
 
@@ -133,6 +144,8 @@ def parfile(case, prefix):
         pats = "0 1 2 3 4 5 6"
     if c.get("checkpoint"):
         lines += ["checkpoint = yes"]
+    if c.get("hrefine"):
+        lines += [f"amr_hrefine_p = {c['hrefine']}"]
     if "fv" in c:
         pats = c["fv"].get("patches", pats)
         lines += [f"amr_uniform_p = {pats}", f"amr_fv_p = {pats}",

@@ -16,6 +16,12 @@ FV_CASES = ["fvbox_l1_n7_w5no", "fvbox_l1_n7_w5dnfn", "fvbox_l2_n5_w3dnfn",
 MIX_CASES = ["mixcs7_l0_n7_w5dnfn", "mixcs7_l1_n5_w3no"]
 # the reference's default upwind flux (DG, mixed, finite volume)
 UPW_CASES = ["upw_cs7_l1_n5", "upw_box_l1_n6", "upw_mixcs7_l0_n7_w5dnfn", "upw_fvbox_l1_n7_w5no"]
+# non-conforming faces: patches refined one level further (amr_hrefine_p)
+NC_CASES = ["nc_cs7_l0_n5_h0", "nc_cs7_l0_n4_h1", "nc_cs7_l1_n5_h02", "nc_upw_cs7_l0_n6_h35"]
+# the oracle's non-conforming traces take the neighbour positions from the
+# element structure, the reference from its inverse coordinate maps: equal
+# to a few ulp of the position, so the oracle matches those fixtures to
+RTOL_NC_ORACLE = 1e-14
 
 # relative L2 tolerance of the CUDA path against the reference / oracle for
 # one RHS evaluation and for a few RK4 steps (FP64; FMA contraction and a
@@ -32,6 +38,7 @@ def load(case):
 
 def build_mesh(meta, periodic=False):
     import nmesh_gb300 as ng
+    href = [int(p) for p in meta.get("hrefine", "").split()]
     fv = "fv" in meta
     if fv and "patches" in meta["fv"]:
         fv = [int(p) for p in meta["fv"]["patches"].split()]
@@ -39,7 +46,7 @@ def build_mesh(meta, periodic=False):
         return ng.Mesh.build(ng.MESH_BOX, n=meta["n"], luni=meta["luni"],
                              xc=(PI, PI, PI), box_dout=PI, periodic=periodic, fv=fv)
     return ng.Mesh.build(ng.MESH_CUBEDSPHERES7, n=meta["n"], luni=meta["luni"],
-                         cs_dc=1.0, cs_r0fac=20.0, fv=fv)
+                         cs_dc=1.0, cs_r0fac=20.0, fv=fv, hrefine=href)
 
 
 def perm_to_mesh(mesh, d):
@@ -72,15 +79,17 @@ def oracle_for(mesh, bc=0, k=(1.0, 1.0, 1.0), period=None, fv_rec="WENOm3_2",
                                                           mesh.np, 1)) else 1
                       for e in range(mesh.nelem)], np.int32)
     fv = mesh.fv()
-    mix = None
+    mix = hang = None
     if fv.any():
         nb, mix = nmo.match_faces(xyz, mesh.n, period=period, fv=fv)
     else:
         nb = nmo.match_faces(xyz, mesh.n, period=period)
+    if (mesh.faces()[1] & 128).any():
+        nb, hang = nmo.match_hanging(xyz, mesh.n, pat, bbox, nb)
     return nmo.OracleMesh(bbox, curvi, dXdx, xyz, nb, mesh.n, bc=bc, k=k,
                           fv=fv if fv.any() else None, fv_rec=fv_rec,
                           fv_extrap=fv_extrap, fv_w3ratio=fv_w3ratio, mixface=mix,
-                          numflux=numflux)
+                          numflux=numflux, hang=hang)
 
 
 def gaussian_pulses(xyz, seed, npulse=8, rmin=3.0, rmax=10.0, wmin=0.5, wmax=2.0,

@@ -5,11 +5,11 @@ import numpy as np
 import pytest
 
 import nmesh_gb300 as ng
-from helpers import CASES, FV_CASES, MIX_CASES, PI, build_mesh, load, perm_to_mesh
+from helpers import CASES, FV_CASES, MIX_CASES, NC_CASES, PI, build_mesh, load, perm_to_mesh
 from oracle import nmo
 
 
-@pytest.mark.parametrize("case", CASES + FV_CASES + MIX_CASES)
+@pytest.mark.parametrize("case", CASES + FV_CASES + MIX_CASES + NC_CASES)
 def test_geometry_bitexact(case):
     """Coordinates and metric on LGL points (DG) and on equally spaced
     points (finite-volume meshes) equal the reference's."""
@@ -115,6 +115,51 @@ def test_desc_roundtrip_with_explicit_node_table():
         nb2, code2 = mm.faces()
         nb1, code1 = m.faces()
         assert np.array_equal(nb1, nb2) and np.array_equal(code1, code2)
+
+
+@pytest.mark.parametrize("case", NC_CASES)
+def test_nonconforming_lists_match_oracle(case):
+    """The packer's non-conforming face lists equal the oracle's (found
+    independently from bboxes and node coordinates): the same sources per
+    face node and the same positions on the source faces."""
+    d, meta = load(case)
+    m = build_mesh(meta)
+    n, nn = m.n, m.n * m.n
+    nbm, code = m.faces()
+    hface, hoff, hsrc, hpos = m.hanging()
+    assert len(hface) == int(((code & 128) != 0).sum()) > 0
+    pat, bbox = m.elements()
+    nb = nmo.match_faces(m.coords(), n)
+    nb2, (off, src, pos) = nmo.match_hanging(m.coords(), n, pat, bbox, nb)
+    assert (nb2[:, :, 0] == -3).sum() == len(hface)
+    for h, (e, f) in enumerate(hface):
+        assert nb2[e, f, 0] == -3
+        for jk in range(nn):
+            a0, a1 = hoff[h * nn + jk], hoff[h * nn + jk + 1]
+            q = (e * 6 + f) * nn + jk
+            b0, b1 = off[q], off[q + 1]
+            mine = sorted(zip(map(tuple, hsrc[a0:a1]), map(tuple, hpos[a0:a1])))
+            theirs = sorted(zip(map(tuple, src[b0:b1]), map(tuple, pos[b0:b1])))
+            assert [s_ for s_, _ in mine] == [s_ for s_, _ in theirs]
+            assert np.allclose([p_ for _, p_ in mine], [p_ for _, p_ in theirs],
+                               rtol=0, atol=1e-14)
+    # element names carry each patch's own level
+    names = m.names()
+    for e in range(m.nelem):
+        lev = len(names[e].split("_")[1])
+        assert lev == meta["luni"] + (str(pat[e]) in meta["hrefine"].split())
+
+
+def test_nonconforming_concat_keeps_lists():
+    a = build_mesh(load("nc_cs7_l0_n5_h0")[1])
+    b = build_mesh(load("nc_cs7_l1_n5_h02")[1])
+    c = ng.Mesh.concat([a, b])
+    ha, hb, hc = a.hanging(), b.hanging(), c.hanging()
+    assert len(hc[0]) == len(ha[0]) + len(hb[0])
+    assert np.array_equal(hc[0][len(ha[0]):, 0], hb[0][:, 0] + a.nelem)
+    assert np.array_equal(hc[2][len(ha[2]):, 0], hb[2][:, 0] + a.nelem)
+    assert np.array_equal(hc[3], np.concatenate([ha[3], hb[3]]))
+    assert np.array_equal(np.diff(hc[1]), np.concatenate([np.diff(ha[1]), np.diff(hb[1])]))
 
 
 def test_mesh_errors():

@@ -5,7 +5,8 @@ operation order and must match it bit for bit."""
 import numpy as np
 import pytest
 
-from helpers import CASES, FV_CASES, MIX_CASES, UPW_CASES, load
+from helpers import (CASES, FV_CASES, MIX_CASES, NC_CASES, RTOL_NC_ORACLE, UPW_CASES, load,
+                     rel_l2)
 from oracle import nmo
 
 
@@ -20,6 +21,8 @@ def _oracle_mesh(d, meta):
                   fv_extrap=meta["fv"]["extrap"], mixface=mix)
     else:
         nb = nmo.match_faces(d["x"], n)
+    if meta.get("hrefine"):
+        nb, fv["hang"] = nmo.match_hanging(d["x"], n, d["pat"], d["bbox"], nb)
     return nmo.OracleMesh(d["bbox"], curvi, d["dXdx"], d["x"], nb, n, bc=0,
                           k=meta["k"], numflux=meta.get("numflux", "LLF"), **fv)
 
@@ -49,6 +52,42 @@ def test_oracle_mixed_dg_fv_bitexact(case):
     m = _oracle_mesh(d, meta)
     assert np.array_equal(m.rhs(d["u0"], 0.0), d["r0"])
     assert np.array_equal(m.rk4(d["u0"], meta["dt"], meta["steps"]), d["u_final"])
+
+
+@pytest.mark.parametrize("case", NC_CASES)
+def test_oracle_nonconforming_matches_reference(case):
+    """Patches one level finer than their neighbours (amr_hrefine_p): each
+    node of a fine face interpolates the coarse face, each node of a coarse
+    face averages the fine faces containing it.  The neighbour positions
+    come from the element structure here and from inverse coordinate maps
+    in the reference, so the match is to a few ulp (bitwise where both
+    positions round alike)."""
+    d, meta = load(case)
+    m = _oracle_mesh(d, meta)
+    assert rel_l2(m.rhs(d["u0"], 0.0), d["r0"]) <= RTOL_NC_ORACLE
+    assert rel_l2(m.rk4(d["u0"], meta["dt"], meta["steps"]), d["u_final"]) <= RTOL_NC_ORACLE
+
+
+def test_nonconforming_face_lists():
+    """Structure of the non-conforming lists: inner cube refined once
+    against six single-element shells, n = 5 (a node on the middle lines)."""
+    d, meta = load("nc_cs7_l0_n5_h0")
+    n = 5
+    nb = nmo.match_faces(d["x"], n)
+    nb2, (off, src, pos) = nmo.match_hanging(d["x"], n, d["pat"], d["bbox"], nb)
+    hang = nb2[:, :, 0] == -3
+    # 24 fine faces of the cube's outside, the 6 shells' inner faces
+    assert hang[:8].sum() == 24 and hang[8:].sum() == 6
+    assert (nb[hang] == -1).all() and (nb2[~hang] == nb[~hang]).all()
+    cnt = np.diff(off).reshape(len(d["pat"]), 6, n * n)
+    assert (cnt[:8][hang[:8]] == 1).all()
+    coarse = cnt[8:][hang[8:]]          # [6, n*n]
+    # interior nodes 1 source, middle-line nodes 2, the centre 4
+    want = np.ones((n, n), int)
+    want[2, :] = want[:, 2] = 2
+    want[2, 2] = 4
+    assert (coarse == want.ravel()[None, :]).all()
+    assert np.abs(pos).max() <= 1 + 1e-14
 
 
 def test_lgl_basis_properties():
