@@ -129,7 +129,6 @@ int nmg_mesh_get_fv(const nmg_mesh *m, int32_t *fv);
 /* LGL nodes and weights on [-1,1] and D[i*n+j] = l_j'(x_i)
    (src/main/basis/Legendre.c:149-213, Lagrange.c:126-147) */
 int nmg_basis(int32_t n, double *x, double *w, double *D);
-/* equally spaced points on [-1,1] (uniform_x, src/main/basis/Legendre.c:626) */
 /* Non-conforming faces of the mesh (patches at different levels): counts,
  * and if the arrays are given, per face (element, face) [nface][2], per face
  * node the offsets of its contributions [nface*n*n + 1], per contribution
@@ -139,6 +138,7 @@ int nmg_basis(int32_t n, double *x, double *w, double *D);
  * src/main/amr/surface.c:799-1360). */
 int nmg_mesh_get_hanging(const nmg_mesh *m, int64_t *nface, int64_t *ncontrib, int32_t *hface,
                          int32_t *hoff, int32_t *hsrc, double *hpos);
+/* equally spaced points on [-1,1] (uniform_x, src/main/basis/Legendre.c:626) */
 int nmg_uniform_points(int32_t n, double *x);
 void nmg_mesh_free(nmg_mesh *m);
 const char *nmg_mesh_last_error(void);
@@ -185,16 +185,27 @@ typedef struct nmg_trouble_params {
   double persson_uscale;   /* u_scale of the indicator (< 0: keep c_0) */
   int32_t notroubles;      /* quiet steps before switching back to DG
                               (NOTROUBLES = 11, src/main/evolve/evolve.h:60) */
+  int32_t redo;            /* NMG_REDO_STEP or NMG_REDO_SUBSTEP (the
+                              parameter evolve_redo_troubled) */
 } nmg_trouble_params;
+/* evolve_redo_troubled = step: detect after the whole RK4 step, go back to
+ * u_p, switch, redo the step; = substep (the reference's default): detect
+ * after every RK4 substep and redo that substep on the troubled elements
+ * (evolve_trouble_redo_u_step_mesh, src/main/evolve/RungeKutta.c:19-80,
+ * 221-330); quiet elements then switch back after notroubles * 4 substeps
+ * (evolve_notroubles, RungeKutta.c:206-211) */
+#define NMG_REDO_STEP 0
+#define NMG_REDO_SUBSTEP 1
 /* flags[e]: DG troubled 1, DG fine 0, FV troubled 0, FV fine -1 (the
  * reference's TROUBLE return convention, trouble.c:17-26) for state u_dev
  * against u_p_dev; persson[E][5] (may be NULL): the indicators (0 on FV) */
 int nmg_trouble_check(nmg_ctx *c, const double *u_dev, const double *u_p_dev,
                       const nmg_trouble_params *tp, int32_t *flags, double *persson);
 /* One RK4 step of the resident state with trouble detection and element
- * switching (evolve_mesh with evolve_redo_troubled = step,
- * src/main/evolve/evolve.c:74-140); switched[0] = elements switched to FV
- * (the step was then redone), switched[1] = elements switched back to DG */
+ * switching (evolve_mesh, src/main/evolve/evolve.c:74-140, with
+ * evolve_redo_troubled = tp->redo: the whole step redone, or each troubled
+ * substep redone on the troubled elements); switched[0] = elements switched
+ * to FV, switched[1] = elements switched back to DG */
 int nmg_rk4_step_trouble(nmg_ctx *c, double t, double dt, const nmg_trouble_params *tp,
                          int32_t *switched);
 int nmg_get_trouble_scores(nmg_ctx *c, int32_t *scores);

@@ -47,12 +47,14 @@ class TroubleParams(ctypes.Structure):
     """Trouble detection parameters (include/nmg.h nmg_trouble_params)."""
     _fields_ = [("rdmp_deltafac", ctypes.c_double), ("rdmp_delta0", ctypes.c_double),
                 ("rdmp_epsilon", ctypes.c_double), ("persson_max", ctypes.c_double),
-                ("persson_uscale", ctypes.c_double), ("notroubles", ctypes.c_int32)]
+                ("persson_uscale", ctypes.c_double), ("notroubles", ctypes.c_int32),
+                ("redo", ctypes.c_int32)]
 
     def __init__(self, rdmp_deltafac=1.0, rdmp_delta0=1e-4, rdmp_epsilon=1e-3,
-                 persson_max=1e300, persson_uscale=-1.0, notroubles=11):
+                 persson_max=1e300, persson_uscale=-1.0, notroubles=11, redo="step"):
+        """redo: "step" or "substep" (the reference's evolve_redo_troubled)."""
         super().__init__(rdmp_deltafac, rdmp_delta0, rdmp_epsilon, persson_max,
-                         persson_uscale, notroubles)
+                         persson_uscale, notroubles, {"step": 0, "substep": 1}[redo])
 
 
 class GrhdParams(ctypes.Structure):

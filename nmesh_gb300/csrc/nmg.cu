@@ -235,6 +235,12 @@ struct nmg_ctx {
   int *d_trb = nullptr;        // [E] trouble flag of the last check
   int *d_score = nullptr;      // [E] trouble score (node->dat->info->trbl_score)
   double *d_up = nullptr;      // u_p: state at the start of a checked step
+  // substep redo (evolve_redo_troubled = substep): the stage's r, the stage
+  // input with the troubled elements converted, and the face tables of the
+  // troubled elements as finite-volume elements among old-type neighbours
+  double *d_r = nullptr, *d_w2 = nullptr, *d_ghost2 = nullptr;
+  int *d_tlist = nullptr, *d_code2 = nullptr, *d_bslot2 = nullptr, *d_gtab2 = nullptr;
+  int ghost2_cap = 0;
   double *d_pers = nullptr;    // [E][5] Persson indicators of the last check
   double *d_wq = nullptr;      // [2][n] LGL and trapezoid (equally spaced) weights
   double *d_npart = nullptr;   // [E][6][4] partial norms
@@ -1098,6 +1104,194 @@ int nmg_get_trouble_scores(nmg_ctx *c, int32_t *scores) {
   return NMG_OK;
 }
 
+// evolve_set_trouble_score (src/main/evolve/trouble.c:27-110) on every
+// element from its flag, then the global score of
+// evolve_read_trouble_score_mesh (trouble.c:132-160)
+static int score_update(nmg_ctx *c, const std::vector<int32_t> &fl) {
+  const int maxt = 1073741824;
+  int smax = INT32_MIN, smin = INT32_MAX;
+  for (int64_t e = 0; e < c->nelem; e++) {
+    int32_t &sc = c->h_score[e];
+    if (fl[e] > 0) sc = sc <= 0 ? 1 : sc + 1;
+    else if (fl[e] == 0) sc = 0;
+    else sc = sc >= 0 ? -1 : sc - 1;
+    if (sc < -maxt) sc = -maxt;
+    if (sc > maxt) sc = maxt;
+    smax = std::max(smax, sc);
+    smin = std::min(smin, sc);
+  }
+  return smax > 0 ? smax : smin;
+}
+
+// y = x + a z over whole elements: all elements (list null) or the listed
+__global__ void elem_axpy_kernel(int64_t count, int per, const int *list, double *y,
+                                 const double *x, double a, const double *z) {
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < count * per;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t k = q / per;
+    const int64_t e = list ? list[k] : k;
+    const size_t idx = (size_t)e * per + (size_t)(q - k * per);
+    y[idx] = x[idx] + a * z[idx];
+  }
+}
+
+static cudaError_t elem_axpy(nmg_ctx *c, int64_t count, const int *list, double *y,
+                             const double *x, double a, const double *z) {
+  if (count <= 0) return cudaSuccess;
+  const int per = NF * c->np;
+  const int64_t grid = std::min<int64_t>((count * per + 255) / 256, 152 * 32);
+  elem_axpy_kernel<<<(unsigned)grid, 256, 0, c->stream>>>(count, per, list, y, x, a, z);
+  c->launches++;
+  return cudaGetLastError();
+}
+
+// r of the troubled elements T (T[0, ndg) were DG, now finite volume) with
+// every neighbour in its old type and with its old data, as the reference's
+// per-element redo does (each redone element is swapped back until all are
+// done, RungeKutta.c:221-330): a face towards a neighbour of the old DG type
+// takes its trace interpolated from that neighbour's old data w_old, the
+// element's own data is the converted w_new.
+static int redo_rhs(nmg_ctx *c, const std::vector<int> &T, const double *w_old,
+                    const double *w_new, double *R, double t) {
+  const int64_t E = c->nelem;
+  const int nn = c->nn;
+  std::vector<int32_t> code(c->h_code0), bslot(c->h_bslot0);
+  std::vector<int> gtab;
+  for (int e : T)
+    for (int f = 0; f < 6; f++) {
+      const int64_t q = (int64_t)e * 6 + f;
+      const int nbe = c->h_nb[q];
+      if (nbe < 0) continue;
+      if (!c->h_fv[nbe]) {  // old type DG (h_fv still holds the old types)
+        code[q] = c->h_code0[q] | NMG_CODE_MIXED;
+        bslot[q] = (int)(gtab.size() / 4);
+        gtab.insert(gtab.end(), {e, f, nbe, code[q]});
+      }
+    }
+  const int ng = (int)(gtab.size() / 4);
+  if (!c->d_code2) {
+    CK(cudaMalloc((void **)&c->d_code2, sizeof(int) * E * 6));
+    CK(cudaMalloc((void **)&c->d_bslot2, sizeof(int) * E * 6));
+    CK(cudaMalloc((void **)&c->d_gtab2, sizeof(int) * E * 6 * 4));
+  }
+  if (ng > c->ghost2_cap) {
+    CK(cudaStreamSynchronize(c->stream));
+    cudaFree(c->d_ghost2);
+    c->d_ghost2 = nullptr;
+    CK(cudaMalloc((void **)&c->d_ghost2, sizeof(double) * 4 * nn * ng));
+    c->ghost2_cap = ng;
+  }
+  CK(cudaMemcpyAsync(c->d_code2, code.data(), sizeof(int) * E * 6, cudaMemcpyHostToDevice,
+                     c->stream));
+  CK(cudaMemcpyAsync(c->d_bslot2, bslot.data(), sizeof(int) * E * 6, cudaMemcpyHostToDevice,
+                     c->stream));
+  if (ng > 0) {
+    CK(cudaMemcpyAsync(c->d_gtab2, gtab.data(), sizeof(int) * gtab.size(),
+                       cudaMemcpyHostToDevice, c->stream));
+    CK(nmgk::ghost_launch(ng, c->n, c->d_gtab2, c->d_isfv, c->d_gM, w_old, c->d_ghost2,
+                          c->stream));
+    c->launches++;
+  }
+  StageParams Q = base_params(c);
+  Q.win = w_new;
+  Q.mode = 0;
+  Q.rout = R;
+  Q.t = t;
+  Q.code = c->d_code2;
+  Q.bslot = c->d_bslot2;
+  Q.ghost = c->d_ghost2;
+  Q.fvlist = c->d_tlist;
+  Q.nfvel = (int)T.size();
+  CK(c->variants[c->fsel >= 0 ? c->fsel : c->ndg].launch(Q, c->stream));
+  c->launches++;
+  // the host tables above must live until the copies are done
+  CK(cudaStreamSynchronize(c->stream));
+  return NMG_OK;
+}
+
+// One RK4 step with evolve_redo_troubled = substep (evolve_RK4_mesh,
+// src/main/evolve/RungeKutta.c:19-80): after each substep u += c_s r the
+// elements are scored; if the global score is positive, every element with
+// a positive score takes the substep back (u -= c_s r), the DG ones are
+// switched to finite volume (u, u_p and w converted), r is recomputed on
+// them and the substep applied again (evolve_trouble_redo_u_step_mesh,
+// RungeKutta.c:221-330).  At the end of the step finite-volume elements
+// whose score reached -4 notroubles switch back to DG (evolve.c:98-140).
+static int rk4_step_substep(nmg_ctx *c, double t, double dt, const nmg_trouble_params *tp,
+                            int32_t *switched) {
+  int rc = autotune(c);
+  if (rc) return rc;
+  if (c->fsel < 0) c->fsel = c->ndg;
+  const int64_t E = c->nelem;
+  const size_t bytes = c->state_len * sizeof(double);
+  if (!c->d_r) CK(cudaMalloc((void **)&c->d_r, bytes));
+  if (!c->d_w2) CK(cudaMalloc((void **)&c->d_w2, bytes));
+  if (!c->d_tlist) CK(cudaMalloc((void **)&c->d_tlist, sizeof(int) * E));
+  const int cur = c->cur;
+  double *U = c->d_buf[cur], *ACC = c->d_buf[1 - cur], *W = c->d_buf[2], *R = c->d_r,
+         *W2 = c->d_w2;
+  const double cacc[4] = {dt / 6., dt / 3., dt / 3., dt / 6.};
+  const double cw[3] = {dt / 2., dt / 2., dt};
+  const double ts[4] = {t, t + 0.5 * dt, t + 0.5 * dt, t + dt};
+  int nfv = 0;
+  CK(cudaMemcpyAsync(W, U, bytes, cudaMemcpyDeviceToDevice, c->stream));  // w = u
+  for (int s = 0; s < 4; s++) {
+    StageParams P = base_params(c);
+    P.win = W;
+    P.mode = 0;
+    P.rout = R;
+    P.t = ts[s];
+    CK(run_stage(c, c->sel, P));                                    // r = RHS(w)
+    CK(elem_axpy(c, E, nullptr, ACC, s == 0 ? W : ACC, cacc[s], R));  // u += c_s r
+    std::vector<int32_t> fl;
+    if ((rc = trouble_flags(c, ACC, U, tp, &fl))) return rc;
+    if (score_update(c, fl) > 0) {
+      std::vector<int> T;
+      for (int64_t e = 0; e < E; e++)
+        if (c->h_score[e] > 0 && !c->h_fv[e]) T.push_back((int)e);
+      const int ndgT = (int)T.size();
+      for (int64_t e = 0; e < E; e++)
+        if (c->h_score[e] > 0 && c->h_fv[e]) T.push_back((int)e);
+      CK(cudaMemcpyAsync(c->d_tlist, T.data(), sizeof(int) * T.size(), cudaMemcpyHostToDevice,
+                         c->stream));
+      CK(elem_axpy(c, (int64_t)T.size(), c->d_tlist, ACC, ACC, -cacc[s], R));  // u -= c_s r
+      CK(cudaMemcpyAsync(W2, W, bytes, cudaMemcpyDeviceToDevice, c->stream));
+      for (double *buf : {W2, ACC, U}) {
+        CK(nmgk::convert_launch(c->n, c->d_tlist, ndgT, c->d_PR, buf, c->stream));
+        c->launches += ndgT > 0;
+      }
+      if ((rc = redo_rhs(c, T, W, W2, R, ts[s]))) return rc;
+      CK(elem_axpy(c, (int64_t)T.size(), c->d_tlist, ACC, ACC, cacc[s], R));  // u += c_s r
+      for (int i = 0; i < ndgT; i++) c->h_fv[T[i]] = 1;
+      nfv += ndgT;
+      CK(cudaStreamSynchronize(c->stream));
+      if ((rc = upload_type_tables(c))) return rc;
+    }
+    if (s < 3) CK(elem_axpy(c, E, nullptr, W, U, cw[s], R));  // w = u_p + a r
+  }
+  c->cur = 1 - cur;
+  int smax = INT32_MIN, smin = INT32_MAX;
+  for (int64_t e = 0; e < E; e++) {
+    smax = std::max(smax, c->h_score[e]);
+    smin = std::min(smin, c->h_score[e]);
+  }
+  const int global = smax > 0 ? smax : smin;
+  const int notr = tp->notroubles * 4;
+  int ndg = 0;
+  if (global > 0 || global <= -notr) {
+    std::vector<int32_t> types(c->h_fv);
+    for (int64_t e = 0; e < E; e++)
+      if (c->h_fv[e] && c->h_score[e] <= -notr) types[e] = 0;
+    if ((rc = switch_types(c, types.data(), nullptr, &ndg))) return rc;
+  }
+  if (switched) {
+    switched[0] = nfv;
+    switched[1] = ndg;
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  return NMG_OK;
+}
+
 // One RK4 step with trouble detection, as evolve_mesh does with
 // evolve_redo_troubled = step (src/main/evolve/evolve.c:74-140): step,
 // score every element (evolve_set_trouble_score, trouble.c:27-110), and if
@@ -1110,27 +1304,18 @@ int nmg_rk4_step_trouble(nmg_ctx *c, double t, double dt, const nmg_trouble_para
   if (!c || !tp) return set_err(c, NMG_EINVAL, "nmg_rk4_step_trouble: null argument");
   if (!c->switchable)
     return set_err(c, NMG_EUNSUP, "nmg_rk4_step_trouble: context is not switchable");
+  if (tp->redo != NMG_REDO_STEP && tp->redo != NMG_REDO_SUBSTEP)
+    return set_err(c, NMG_EINVAL, "nmg_rk4_step_trouble: unknown redo mode");
   int rc = ensure_trouble_buffers(c);
   if (rc) return rc;
+  if (tp->redo == NMG_REDO_SUBSTEP) return rk4_step_substep(c, t, dt, tp, switched);
   const int64_t E = c->nelem;
   const size_t bytes = c->state_len * sizeof(double);
   CK(cudaMemcpyAsync(c->d_up, c->d_buf[c->cur], bytes, cudaMemcpyDeviceToDevice, c->stream));
   if ((rc = nmg_rk4_step(c, t, dt))) return rc;
   std::vector<int32_t> fl;
   if ((rc = trouble_flags(c, c->d_buf[c->cur], c->d_up, tp, &fl))) return rc;
-  const int maxt = 1073741824;
-  int smax = INT32_MIN, smin = INT32_MAX;
-  for (int64_t e = 0; e < E; e++) {
-    int32_t &sc = c->h_score[e];
-    if (fl[e] > 0) sc = sc <= 0 ? 1 : sc + 1;
-    else if (fl[e] == 0) sc = 0;
-    else sc = sc >= 0 ? -1 : sc - 1;
-    if (sc < -maxt) sc = -maxt;
-    if (sc > maxt) sc = maxt;
-    smax = std::max(smax, sc);
-    smin = std::min(smin, sc);
-  }
-  const int global = smax > 0 ? smax : smin;
+  const int global = score_update(c, fl);
   int nfv = 0, ndg = 0;
   if (global > 0) {
     // go back to u_p, switch the troubled elements, redo the step
@@ -1224,6 +1409,8 @@ void nmg_destroy(nmg_ctx *c) {
   cudaFree(c->d_hoff); cudaFree(c->d_hsrc); cudaFree(c->d_hw);
   cudaFree(c->d_gM); cudaFree(c->d_fvbxyz); cudaFree(c->d_fvbnrm); cudaFree(c->d_PR);
   cudaFree(c->d_conv); cudaFree(c->d_mm); cudaFree(c->d_trb); cudaFree(c->d_score);
+  cudaFree(c->d_r); cudaFree(c->d_w2); cudaFree(c->d_ghost2); cudaFree(c->d_tlist);
+  cudaFree(c->d_code2); cudaFree(c->d_bslot2); cudaFree(c->d_gtab2);
   cudaFree(c->d_up); cudaFree(c->d_pers); cudaFree(c->d_wq); cudaFree(c->d_npart);
   for (int b = 0; b < 4; b++) cudaFree(c->d_buf[b]);
   cudaFree(c->d_times); cudaFree(c->d_step);
