@@ -340,17 +340,21 @@ def run_ours(args, rank, world, local):
 
 def batch_problem_specs(count, seed=4242):
     """Seeded set of independent problems: element counts log-uniform in
-    [64, 32768] (realised by the nearest box (8^L) or 7-cubed-sphere (7*8^L)
-    mesh), orders N uniform in {3..9} (n = N+1 nodes)."""
+    [64, 32768] (realised by the nearest box (8^L) mesh or 7-cubed-sphere
+    mesh with k of its patches one level finer, (7-k) 8^L + k 8^(L+1)
+    elements, k in 0..3: refinement levels 0..5 with non-conforming faces
+    between levels), orders N uniform in {3..9} (n = N+1 nodes)."""
     rng = np.random.default_rng(seed)
     specs = []
-    opts = [("box", L, 8 ** L) for L in range(2, 6)] + \
-        [("cs7", L, 7 * 8 ** L) for L in range(1, 5)]
+    opts = [("box", L, 0, 8 ** L) for L in range(2, 6)] + \
+        [("cs7", L, k, (7 - k) * 8 ** L + k * 8 ** (L + 1)) for L in range(0, 5)
+         for k in range(4) if (7 - k) * 8 ** L + k * 8 ** (L + 1) <= 40000]
     for _ in range(count):
         target = np.exp(rng.uniform(np.log(64), np.log(32768)))
-        kind, L, E = min(opts, key=lambda o: abs(np.log(o[2]) - np.log(target)))
+        kind, L, k, E = min(opts, key=lambda o: abs(np.log(o[3]) - np.log(target)))
         n = int(rng.integers(3, 10)) + 1
-        specs.append((kind, L, n, E))
+        href = tuple(sorted(int(p) for p in rng.choice(7, k, replace=False))) if k else ()
+        specs.append((kind, L, n, E, href))
     return specs
 
 
@@ -363,13 +367,13 @@ def batched_bench(args):
     import nmesh_gb300 as ng
     specs = batch_problem_specs(args.batch_problems)
     meshes = []
-    for kind, L, n, E in specs:
+    for kind, L, n, E, href in specs:
         if kind == "box":
             meshes.append(ng.Mesh.build(ng.MESH_BOX, n=n, luni=L, xc=(PI, PI, PI),
                                         box_dout=PI, periodic=True))
         else:
             meshes.append(ng.Mesh.build(ng.MESH_CUBEDSPHERES7, n=n, luni=L, cs_dc=1.0,
-                                        cs_r0fac=20.0))
+                                        cs_r0fac=20.0, hrefine=href))
     rng = np.random.default_rng(7)
     states = [1e-3 * rng.standard_normal((m.nelem, NFIELDS, m.np)) for m in meshes]
     dof = sum(m.nelem * m.np * NFIELDS for m in meshes)
@@ -419,8 +423,12 @@ def batched_bench(args):
             "speedup_vs_plain_launches": t_plain / t_batch,
             "speedup_vs_per_problem_graphs": t_graphs / t_batch,
             "batch_info": info,
-            "note": "orders are per problem (faces between elements of different n or "
-                    "level are not conforming); all problems share dt"}
+            "refinement_levels": sorted(set(int(L) + d for _, L, _, _, h in specs
+                                            for d in ((0, 1) if h else (0,)))),
+            "problems_with_level_jumps": int(sum(1 for s_ in specs if s_[4])),
+            "note": "orders are per problem; problems with level jumps have patches one "
+                    "level finer than their neighbours (non-conforming faces, traces "
+                    "interpolated each stage); all problems share dt"}
 
 
 PI = 3.141592653589793
