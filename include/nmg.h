@@ -57,6 +57,8 @@ extern "C" {
 #define NMG_FV_REC_1 0        /* "1": first order (rec1d_p_1 / rec1d_m_1) */
 #define NMG_FV_REC_WENOM3_2 1 /* "WENOm3_2" (reference default) */
 #define NMG_FV_REC_WENOM5_2 2 /* "WENOm5_2": WENO5 inside, WENOm3_2 near ends */
+#define NMG_FV_REC_WENOMZ_2 3 /* "WENOmZ_2": WENO-Z inside, WENOm3_2 near ends
+                                 (rec1d_p/m_WENOmZ_2, rec1d.c:1627-1796) */
 /* how div(f) is completed on face points, the reference's par fv_divf_extrap
  * (src/main/dg/dg.c:341-361) */
 #define NMG_FV_EXTRAP_NO 0    /* "no": face fluxes weighted by 1/|distXb| */

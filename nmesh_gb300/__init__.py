@@ -24,7 +24,7 @@ BC_EXACT_PLANEWAVE = 0
 BC_OUTGOING = 1
 # finite-volume reconstruction (reference par fv_rec) and div(f) completion
 # on face points (par fv_divf_extrap)
-FV_REC = {"1": 0, "WENOm3_2": 1, "WENOm5_2": 2}
+FV_REC = {"1": 0, "WENOm3_2": 1, "WENOm5_2": 2, "WENOmZ_2": 3}
 FV_EXTRAP = {"no": 0, "dnfn_extrap1": 1}
 
 _c_dp = ctypes.POINTER(ctypes.c_double)

@@ -1385,7 +1385,7 @@ int nmg_set_numflux(nmg_ctx *c, int32_t kind) {
 int nmg_set_fv(nmg_ctx *c, int32_t rec, int32_t extrap, double w3ratio) {
   if (!c) return NMG_EINVAL;
   if (!c->fv) return set_err(c, NMG_EUNSUP, "nmg_set_fv: the mesh has no finite-volume elements");
-  if (rec < NMG_FV_REC_1 || rec > NMG_FV_REC_WENOM5_2)
+  if (rec < NMG_FV_REC_1 || rec > NMG_FV_REC_WENOMZ_2)
     return set_err(c, NMG_EINVAL, "nmg_set_fv: unknown reconstruction");
   if (extrap != NMG_FV_EXTRAP_NO && extrap != NMG_FV_EXTRAP_DNFN1)
     return set_err(c, NMG_EINVAL, "nmg_set_fv: unknown div(f) extrapolation");

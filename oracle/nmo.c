@@ -102,7 +102,7 @@ typedef struct nmo_pts {
   double xl[64], wl[64], xu[64];
 } nmo_pts;
 
-enum { NMO_REC_1 = 0, NMO_REC_WENOM3_2 = 1, NMO_REC_WENOM5_2 = 2 };
+enum { NMO_REC_1 = 0, NMO_REC_WENOM3_2 = 1, NMO_REC_WENOM5_2 = 2, NMO_REC_WENOMZ_2 = 3 };
 
 /* ------------------------------------------------------------------ */
 /* basis: LGL points, weights and differentiation matrix               */
@@ -692,11 +692,59 @@ static double weno5_m(const double *u, int im)
   return w0 * q0 + w1 * q1 + w2 * q2;
 }
 
+/* rec1d_p_WENOZ_uniform (rec1d.c:1627-1679,1732-1754): WENO5 with the
+   WENO-Z weights optw_k (1 + tau5 / (b_k + eps)), tau5 = |b0 - b2| */
+static double wenoz_p(const double *u, int im)
+{
+  const double oo6 = 1 / 6.;
+  double u_im2 = u[im - 2], u_im1 = u[im - 1], u_i = u[im];
+  double u_ip1 = u[im + 1], u_ip2 = u[im + 2];
+  double b01 = u_im2 - 2. * u_im1 + u_i, b02 = u_im2 - 4. * u_im1 + 3. * u_i;
+  double b11 = u_im1 - 2. * u_i + u_ip1, b12 = u_im1 - u_ip1;
+  double b21 = u_i - 2. * u_ip1 + u_ip2, b22 = 3. * u_i - 4. * u_ip1 + u_ip2;
+  double b0 = C1312 * b01 * b01 + 0.25 * b02 * b02;
+  double b1 = C1312 * b11 * b11 + 0.25 * b12 * b12;
+  double b2 = C1312 * b21 * b21 + 0.25 * b22 * b22;
+  double e0 = b0 + 1e-40 * 1.0, e1 = b1 + 1e-40 * 1.0, e2 = b2 + 1e-40 * 1.0;
+  double tau5 = fabs(b0 - b2);
+  double o0 = 1. * (1. + tau5 / e0), o1 = 6. * (1. + tau5 / e1), o2 = 3. * (1. + tau5 / e2);
+  double oos = 1. / (o0 + o1 + o2);
+  double w0 = o0 * oos, w1 = o1 * oos, w2 = o2 * oos;
+  double q0 = (2. * oo6) * u_im2 + (-7. * oo6) * u_im1 + (11. * oo6) * u_i;
+  double q1 = (-oo6) * u_im1 + (5. * oo6) * u_i + (2. * oo6) * u_ip1;
+  double q2 = (2. * oo6) * u_i + (5. * oo6) * u_ip1 + (-oo6) * u_ip2;
+  return w0 * q0 + w1 * q1 + w2 * q2;
+}
+
+/* rec1d_m_WENOZ_uniform (rec1d.c:1681-1730,1756-1780) */
+static double wenoz_m(const double *u, int im)
+{
+  const double oo6 = 1 / 6.;
+  double u_im1 = u[im - 1], u_i = u[im], u_ip1 = u[im + 1];
+  double u_ip2 = u[im + 2], u_ip3 = u[im + 3];
+  double b21 = u_ip1 - 2. * u_ip2 + u_ip3, b22 = 3. * u_ip1 - 4. * u_ip2 + u_ip3;
+  double b11 = u_i - 2. * u_ip1 + u_ip2, b12 = u_i - u_ip2;
+  double b01 = u_im1 - 2. * u_i + u_ip1, b02 = u_im1 - 4. * u_i + 3. * u_ip1;
+  double b2 = C1312 * b21 * b21 + 0.25 * b22 * b22;
+  double b1 = C1312 * b11 * b11 + 0.25 * b12 * b12;
+  double b0 = C1312 * b01 * b01 + 0.25 * b02 * b02;
+  double e2 = b2 + 1e-40 * 1.0, e1 = b1 + 1e-40 * 1.0, e0 = b0 + 1e-40 * 1.0;
+  double tau5 = fabs(b0 - b2);
+  double o2 = 1. * (1. + tau5 / e2), o1 = 6. * (1. + tau5 / e1), o0 = 3. * (1. + tau5 / e0);
+  double oos = 1. / (o0 + o1 + o2);
+  double w2 = o2 * oos, w1 = o1 * oos, w0 = o0 * oos;
+  double q2 = (11. * oo6) * u_ip1 + (-7. * oo6) * u_ip2 + (2. * oo6) * u_ip3;
+  double q1 = (2. * oo6) * u_i + (5. * oo6) * u_ip1 + (-oo6) * u_ip2;
+  double q0 = (-oo6) * u_im1 + (5. * oo6) * u_i + (2. * oo6) * u_ip1;
+  return w0 * q0 + w1 * q1 + w2 * q2;
+}
+
 /* left state at midpoint im (0..n-2) of a pencil of n values */
 static double rec_p(int mode, int n, const double *u, int im, double r3)
 {
   if (mode == NMO_REC_1) return u[im];
   if (mode == NMO_REC_WENOM5_2 && im >= 2 && im <= n - 3) return weno5_p(u, im);
+  if (mode == NMO_REC_WENOMZ_2 && im >= 2 && im <= n - 3) return wenoz_p(u, im);
   /* rec1d_p_WENOm3_2 */
   if (im >= 1 && im <= n - 2) return weno3_p(u, im, 1., r3, -0.5, 1.5, 0.5, 0.5);
   if (n < 3) return u[im];
@@ -708,6 +756,7 @@ static double rec_m(int mode, int n, const double *u, int im, double r3)
 {
   if (mode == NMO_REC_1) return u[im + 1];
   if (mode == NMO_REC_WENOM5_2 && im >= 1 && im <= n - 4) return weno5_m(u, im);
+  if (mode == NMO_REC_WENOMZ_2 && im >= 1 && im <= n - 4) return wenoz_m(u, im);
   /* rec1d_m_WENOm3_2 */
   if (im >= 0 && im <= n - 3) return weno3_m(u, im, r3, 1., 0.5, 0.5, 1.5, -0.5);
   if (n < 3) return u[im + 1];

@@ -45,7 +45,7 @@ class _Mesh(ctypes.Structure):
 
 # reconstruction modes (reference par fv_rec) and div(f) extrapolation
 # modes (par fv_divf_extrap) understood by the oracle
-FV_REC = {"1": 0, "WENOm3_2": 1, "WENOm5_2": 2}
+FV_REC = {"1": 0, "WENOm3_2": 1, "WENOm5_2": 2, "WENOmZ_2": 3}
 FV_EXTRAP = {"no": 0, "dnfn_extrap1": 1}
 
 

@@ -99,6 +99,18 @@ CASES = {
                            dt=0.01, steps=1, eps=0.01, seed=36, checkpoint=True),
     "ckpt_cs7_l1_n3": dict(mesh="cs7", n=3, luni=1, k=(0.3, -0.2, 0.1),
                            dt=0.002, steps=1, eps=0.01, seed=37, checkpoint=True),
+    # WENO-Z reconstruction inside, WENOm3_2 near the ends (fv_rec = WENOmZ_2,
+    # the reconstruction of the reference's own mixed DG/FV test parfile)
+    "fvcs7_l0_n7_wZdnfn": dict(mesh="cs7", n=7, luni=0, k=(0.3, -0.2, 0.1),
+                               dt=0.002, steps=2, eps=0.05, seed=42,
+                               fv=dict(rec="WENOmZ_2", extrap="dnfn_extrap1")),
+    "fvbox_l1_n8_wZno": dict(mesh="box", n=8, luni=1, k=(1.0, -0.5, 0.25),
+                             dt=0.004, steps=2, eps=0.1, seed=43,
+                             fv=dict(rec="WENOmZ_2", extrap="no")),
+    "mixcs7_l1_n6_wZdnfn": dict(mesh="cs7", n=6, luni=1, k=(0.25, 0.15, -0.3),
+                                dt=0.002, steps=2, eps=0.02, seed=44,
+                                fv=dict(rec="WENOmZ_2", extrap="dnfn_extrap1",
+                                        patches="0 2 4")),
     # non-conforming faces: the listed patches refined one level further
     # (amr_hrefine_p), face traces interpolated across the level jump
     "nc_cs7_l0_n5_h0": dict(mesh="cs7", n=5, luni=0, k=(0.3, -0.2, 0.1),

@@ -11,16 +11,23 @@ PI = 3.141592653589793
 CASES = ["box_l1_n5", "box_l2_n4", "cs7_l0_n9", "cs7_l1_n5", "cs7_l1_n4"]
 # all-finite-volume fixtures (uniform points, WENO at the midpoints)
 FV_CASES = ["fvbox_l1_n7_w5no", "fvbox_l1_n7_w5dnfn", "fvbox_l2_n5_w3dnfn",
-            "fvbox_l0_n13_w5dnfn", "fvcs7_l0_n7_w5dnfn", "fvcs7_l0_n6_w5no"]
+            "fvbox_l0_n13_w5dnfn", "fvcs7_l0_n7_w5dnfn", "fvcs7_l0_n6_w5no",
+            "fvcs7_l0_n7_wZdnfn", "fvbox_l1_n8_wZno"]
 # mixed fixtures: inner cube finite-volume, cubed-sphere shells DG
-MIX_CASES = ["mixcs7_l0_n7_w5dnfn", "mixcs7_l1_n5_w3no"]
+MIX_CASES = ["mixcs7_l0_n7_w5dnfn", "mixcs7_l1_n5_w3no", "mixcs7_l1_n6_wZdnfn"]
+# mixed fixtures where the oracle is a few ulp off the reference: the
+# interface positions come from the point sets here and from coordinate
+# conversions (X -> the neighbour's Xb) in the reference; they round
+# differently on the equally spaced points of even n
+MIX_NEAR_CASES = ["mixcs7_l1_n6_wZdnfn"]
 # the reference's default upwind flux (DG, mixed, finite volume)
 UPW_CASES = ["upw_cs7_l1_n5", "upw_box_l1_n6", "upw_mixcs7_l0_n7_w5dnfn", "upw_fvbox_l1_n7_w5no"]
 # non-conforming faces: patches refined one level further (amr_hrefine_p)
 NC_CASES = ["nc_cs7_l0_n5_h0", "nc_cs7_l0_n4_h1", "nc_cs7_l1_n5_h02", "nc_upw_cs7_l0_n6_h35"]
-# the oracle's non-conforming traces take the neighbour positions from the
-# element structure, the reference from its inverse coordinate maps: equal
-# to a few ulp of the position, so the oracle matches those fixtures to
+# the oracle's non-conforming (and even-n DG/FV interface) traces take the
+# neighbour positions from the element structure, the reference from its
+# coordinate maps: equal to a few ulp of the position, so the oracle matches
+# those fixtures to
 RTOL_NC_ORACLE = 1e-14
 
 # relative L2 tolerance of the CUDA path against the reference / oracle for
