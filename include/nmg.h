@@ -220,6 +220,20 @@ int nmg_get_trouble_scores(nmg_ctx *c, int32_t *scores);
  * u_dev NULL: the resident state.  Only the 31 numbers leave the GPU. */
 int nmg_norms(nmg_ctx *c, const double *u_dev, double *out);
 
+/* ---- other time integrators of the reference ----------------------------
+ * The reference's evolve_method = Euler or sspRK3 (evolve_Euler_mesh,
+ * evolve_sspRK3_mesh, src/main/evolve/RungeKutta.c:84-200) besides RK4:
+ * nmg_set_evolve_method picks the integrator of nmg_evolve_steps(_host),
+ * which step the resident state like nmg_rk4_steps (graph-captured steps,
+ * step times accumulated as evolve_mesh does).  The nmg_rk4_* entry points
+ * always use RK4. */
+#define NMG_EVOLVE_RK4 0
+#define NMG_EVOLVE_EULER 1
+#define NMG_EVOLVE_SSPRK3 2
+int nmg_set_evolve_method(nmg_ctx *c, int32_t method);
+int nmg_evolve_steps(nmg_ctx *c, double t, double dt, int32_t nsteps);
+int nmg_evolve_steps_host(nmg_ctx *c, double t, double dt, int32_t nsteps, double *host_u);
+
 /* ---- checkpoints in the reference's variable file format ---------------
  * The state as the reference's checkpoint "variables.bin"
  * (checkpoint_save_EvoVars / checkpoint_load_Vars,

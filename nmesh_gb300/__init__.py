@@ -24,6 +24,7 @@ BC_EXACT_PLANEWAVE = 0
 BC_OUTGOING = 1
 # finite-volume reconstruction (reference par fv_rec) and div(f) completion
 # on face points (par fv_divf_extrap)
+EVOLVE_METHOD = {"RK4": 0, "Euler": 1, "sspRK3": 2}
 FV_REC = {"1": 0, "WENOm3_2": 1, "WENOm5_2": 2, "WENOmZ_2": 3}
 FV_EXTRAP = {"no": 0, "dnfn_extrap1": 1}
 
@@ -187,6 +188,9 @@ def lib(build_if_missing=True):
         "nmg_get_trouble_scores": (ctypes.c_int, [vp, vp]),
         "nmg_norms": (ctypes.c_int, [vp, vp, vp]),
         "nmg_set_numflux": (ctypes.c_int, [vp, i32]),
+        "nmg_set_evolve_method": (ctypes.c_int, [vp, i32]),
+        "nmg_evolve_steps": (ctypes.c_int, [vp, f64, f64, i32]),
+        "nmg_evolve_steps_host": (ctypes.c_int, [vp, f64, f64, i32, vp]),
         "nmg_checkpoint_write": (ctypes.c_int, [vp, vp, ctypes.c_char_p, vp]),
         "nmg_checkpoint_read": (ctypes.c_int, [vp, vp, ctypes.c_char_p, vp]),
         "nmg_checkpoint_write_host": (ctypes.c_int, [vp, vp, ctypes.c_char_p, vp]),
@@ -496,6 +500,23 @@ class Evolution:
             res[name] = dict(zip(("VolInt", "mean", "rms", "min", "max", "maxAbs"),
                                  out[1 + 6 * l: 7 + 6 * l]))
         return res
+
+    def set_evolve_method(self, method="RK4"):
+        """The reference's evolve_method ("RK4", "Euler", "sspRK3") used by
+        evolve_steps / evolve_steps_host."""
+        self._check(lib().nmg_set_evolve_method(self._h, EVOLVE_METHOD[method]),
+                    "nmg_set_evolve_method")
+
+    def evolve_steps(self, t, dt, nsteps):
+        self._check(lib().nmg_evolve_steps(self._h, float(t), float(dt), int(nsteps)),
+                    "nmg_evolve_steps")
+
+    def evolve_steps_host(self, u, t, dt, nsteps):
+        u = np.array(u, np.float64, copy=True, order="C")
+        assert u.size == self.size
+        self._check(lib().nmg_evolve_steps_host(self._h, float(t), float(dt), int(nsteps),
+                                                _ptr(u)), "nmg_evolve_steps_host")
+        return u
 
     def checkpoint_write(self, path, names=None):
         """Resident state -> the reference's checkpoint variables.bin."""

@@ -261,6 +261,8 @@ struct nmg_ctx {
   int64_t h2d_chunk = 0;      // elements per copy chunk
   double graph_dt = 0;
   int graph_sel = -1;
+  int method = NMG_EVOLVE_RK4;   // time integrator of nmg_evolve_steps
+  int graph_method = -1;         // the one the step graphs were captured with
   int64_t graph_launches = 5;
   int64_t launches = 0;
 };
@@ -484,8 +486,47 @@ static int launch_stage(nmg_ctx *c, const StageParams &P) {
   return NMG_OK;
 }
 
-// enqueue the 4 stage launches of one RK4 step with u in d_buf[cur]
-static int enqueue_step(nmg_ctx *c, int cur, double t, double dt, bool devtime) {
+// Stages of Euler and sspRK3 (evolve_Euler_mesh, evolve_sspRK3_mesh,
+// src/main/evolve/RungeKutta.c:84-200): Euler u = u_p + dt r(u_p, t);
+// sspRK3 u += dt/6 r1 with w = u_p + dt r1; u += dt/6 r2 with
+// w = 0.75 u_p + 0.25 (w + dt r2) at t + dt; u += (dt 2/3) r3 at t + dt/2.
+static int enqueue_step_other(nmg_ctx *c, int cur, double t, double dt, bool devtime,
+                              int method) {
+  double *U = c->d_buf[cur], *ACC = c->d_buf[1 - cur], *WA = c->d_buf[2], *WB = c->d_buf[3];
+  const int ns = method == NMG_EVOLVE_EULER ? 1 : 3;
+  const int mode[3] = {method == NMG_EVOLVE_EULER ? 5 : 1, 6, 4};
+  const double cacc[3] = {method == NMG_EVOLVE_EULER ? dt : dt / 6., dt / 6., dt * 2. / 3.};
+  const double cw[3] = {dt, dt, 0.};
+  const double tofs[3] = {0., dt, 0.5 * dt};
+  const double *win[3] = {U, WA, WB};
+  double *wout[3] = {method == NMG_EVOLVE_EULER ? nullptr : WA, WB, nullptr};
+  for (int s = 0; s < ns; s++) {
+    StageParams P = base_params(c);
+    P.win = win[s];
+    P.u0 = U;
+    P.acc = ACC;
+    P.wout = wout[s];
+    P.mode = mode[s];
+    P.cacc = cacc[s];
+    P.cw = cw[s];
+    if (devtime) {
+      P.tdev = c->d_times;
+      P.stepdev = c->d_step;
+      P.tofs_dt = tofs[s];
+    } else {
+      P.t = (s == 0) ? t : (s == 1) ? t + dt : t + 0.5 * dt;
+    }
+    int rc = launch_stage(c, P);
+    if (rc) return rc;
+  }
+  return NMG_OK;
+}
+
+// enqueue the 4 stage launches of one RK4 step with u in d_buf[cur] (or the
+// stages of another time integrator)
+static int enqueue_step(nmg_ctx *c, int cur, double t, double dt, bool devtime,
+                        int method = NMG_EVOLVE_RK4) {
+  if (method != NMG_EVOLVE_RK4) return enqueue_step_other(c, cur, t, dt, devtime, method);
   double *U = c->d_buf[cur], *ACC = c->d_buf[1 - cur], *WA = c->d_buf[2], *WB = c->d_buf[3];
   const double cacc[4] = {dt / 6., dt / 3., dt / 3., dt / 6.};
   const double cw[4] = {dt / 2., dt / 2., dt, 0.};
@@ -1540,14 +1581,14 @@ int nmg_rk4_step(nmg_ctx *c, double t, double dt) {
   return NMG_OK;
 }
 
-// capture one RK4 step (u in d_buf[cur]) reading its time from the device
-static int capture_step_graph(nmg_ctx *c, int cur, double dt) {
+// capture one step (u in d_buf[cur]) reading its time from the device
+static int capture_step_graph(nmg_ctx *c, int cur, double dt, int method) {
   int rc = autotune(c);  // never tune inside a capture
   if (rc) return rc;
   cudaGraph_t g;
   CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
   int64_t l0 = c->launches;
-  rc = enqueue_step(c, cur, 0., dt, true);
+  rc = enqueue_step(c, cur, 0., dt, true, method);
   advance_step_kernel<<<1, 1, 0, c->stream>>>(c->d_step);
   cudaError_t e1 = cudaGetLastError();
   cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
@@ -1563,8 +1604,39 @@ static int capture_step_graph(nmg_ctx *c, int cur, double dt) {
   return NMG_OK;
 }
 
+static int steps_impl(nmg_ctx *c, double t, double dt, int32_t nsteps, int method);
+
 int nmg_rk4_steps(nmg_ctx *c, double t, double dt, int32_t nsteps) {
   if (!c || nsteps < 0) return set_err(c, NMG_EINVAL, "nmg_rk4_steps: bad argument");
+  return steps_impl(c, t, dt, nsteps, NMG_EVOLVE_RK4);
+}
+
+int nmg_set_evolve_method(nmg_ctx *c, int32_t method) {
+  if (!c) return NMG_EINVAL;
+  if (method != NMG_EVOLVE_RK4 && method != NMG_EVOLVE_EULER && method != NMG_EVOLVE_SSPRK3)
+    return set_err(c, NMG_EINVAL, "nmg_set_evolve_method: unknown method");
+  c->method = method;
+  return NMG_OK;
+}
+
+int nmg_evolve_steps(nmg_ctx *c, double t, double dt, int32_t nsteps) {
+  if (!c || nsteps < 0) return set_err(c, NMG_EINVAL, "nmg_evolve_steps: bad argument");
+  return steps_impl(c, t, dt, nsteps, c->method);
+}
+
+int nmg_evolve_steps_host(nmg_ctx *c, double t, double dt, int32_t nsteps, double *host_u) {
+  if (!c || !host_u || nsteps < 0)
+    return set_err(c, NMG_EINVAL, "nmg_evolve_steps_host: bad argument");
+  const size_t bytes = c->state_len * sizeof(double);
+  CK(cudaMemcpyAsync(c->d_buf[c->cur], host_u, bytes, cudaMemcpyHostToDevice, c->stream));
+  int rc = steps_impl(c, t, dt, nsteps, c->method);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(host_u, c->d_buf[c->cur], bytes, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return NMG_OK;
+}
+
+static int steps_impl(nmg_ctx *c, double t, double dt, int32_t nsteps, int method) {
   if (nsteps == 0) return NMG_OK;
   // step times as evolve_mesh accumulates them (long double), main.c:610-626
   std::vector<double> times(nsteps);
@@ -1580,13 +1652,15 @@ int nmg_rk4_steps(nmg_ctx *c, double t, double dt, int32_t nsteps) {
     c->times_cap = nsteps;
     drop_graphs(c);
   }
-  if (dt != c->graph_dt || c->graph_sel != c->sel * 64 + c->fsel) {
+  if (dt != c->graph_dt || c->graph_sel != c->sel * 64 + c->fsel ||
+      c->graph_method != method) {
     drop_graphs(c);
     c->graph_dt = dt;
+    c->graph_method = method;
   }
   for (int g = 0; g < 2; g++)
     if (!c->graph[g]) {
-      int rc = capture_step_graph(c, g, dt);
+      int rc = capture_step_graph(c, g, dt, method);
       if (rc) return rc;
     }
   c->graph_sel = c->sel * 64 + c->fsel;

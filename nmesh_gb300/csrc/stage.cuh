@@ -34,7 +34,11 @@ struct StageParams {
   double *acc;          // u accumulator
   double *wout;         // next stage's w
   double *rout;         // RHS output (mode 0)
-  int mode;             // 0: r only; 1..4: RK4 stage
+  int mode;             // 0: r only; 1..4: RK4 stage (1: acc = u0 + cacc r,
+                        // w = u0 + cw r; 2, 3: acc += cacc r, w = u0 + cw r;
+                        // 4: acc += cacc r); 5: acc = u0 + cacc r (Euler);
+                        // 6: acc += cacc r, w = 0.75 u0 + 0.25 (win + cw r)
+                        // (sspRK3 stage 2)
   double t;             // time of this RHS evaluation
   double cacc, cw;      // stage coefficients: acc += cacc*r, wout = u0 + cw*r
   const double *tdev;   // if non-null: step time read from tdev[*stepdev]
@@ -335,6 +339,11 @@ __device__ __forceinline__ void epilogue(const StageParams &P, const double *sW,
       P.wout[idx] = fma(P.cw, r, u);
     } else if (P.mode == 4) {
       P.acc[idx] = fma(P.cacc, r, P.acc[idx]);
+    } else if (P.mode == 5) {
+      P.acc[idx] = fma(P.cacc, r, __ldg(P.u0 + idx));
+    } else if (P.mode == 6) {
+      P.acc[idx] = fma(P.cacc, r, P.acc[idx]);
+      P.wout[idx] = fma(0.25, fma(P.cw, r, __ldg(P.win + idx)), 0.75 * __ldg(P.u0 + idx));
     } else {
       P.acc[idx] = fma(P.cacc, r, P.acc[idx]);
       P.wout[idx] = fma(P.cw, r, __ldg(P.u0 + idx));

@@ -314,6 +314,11 @@ __device__ __forceinline__ void eof_body(const StageParams &P, int blk) {
       P.wout[idx] = fma(P.cw, r, u);
     } else if (P.mode == 4) {
       P.acc[idx] = fma(P.cacc, r, P.acc[idx]);
+    } else if (P.mode == 5) {
+      P.acc[idx] = fma(P.cacc, r, __ldg(P.u0 + idx));
+    } else if (P.mode == 6) {
+      P.acc[idx] = fma(P.cacc, r, P.acc[idx]);
+      P.wout[idx] = fma(0.25, fma(P.cw, r, __ldg(P.win + idx)), 0.75 * __ldg(P.u0 + idx));
     } else {
       P.acc[idx] = fma(P.cacc, r, P.acc[idx]);
       P.wout[idx] = fma(P.cw, r, __ldg(P.u0 + idx));

@@ -529,6 +529,12 @@ __global__ void __launch_bounds__(NT) fv_kernel(const StageParams P) {
       P.wout[idx] = u + P.cw * r;
     } else if (P.mode == 4) {
       P.acc[idx] = P.acc[idx] + P.cacc * r;
+    } else if (P.mode == 5) {
+      P.acc[idx] = __ldg(P.u0 + idx) + P.cacc * r;
+    } else if (P.mode == 6) {
+      P.acc[idx] = P.acc[idx] + P.cacc * r;
+      const double w = __ldg(P.win + idx) + P.cw * r;
+      P.wout[idx] = 0.75 * __ldg(P.u0 + idx) + 0.25 * w;
     } else {
       P.acc[idx] = P.acc[idx] + P.cacc * r;
       P.wout[idx] = __ldg(P.u0 + idx) + P.cw * r;

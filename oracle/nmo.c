@@ -1114,6 +1114,54 @@ int nmo_rk4_step(const nmo_mesh *m, double t, double dt, double *u,
   return 0;
 }
 
+/* One Euler (method 1) or sspRK3 (method 2) step (evolve_Euler_mesh,
+   evolve_sspRK3_mesh, src/main/evolve/RungeKutta.c:84-200), the vector
+   operations in the reference's order. */
+static int nmo_other_step(const nmo_mesh *m, int method, double t, double dt, double *u,
+                          double *work)
+{
+  size_t N = (size_t)m->nelem * NF * m->n * m->n * m->n, i;
+  double *u_p = work, *w = work + N, *r = work + 2 * N;
+  memcpy(u_p, u, N * sizeof(double));
+  memcpy(w, u, N * sizeof(double));
+  if (nmo_rhs(m, t, w, r)) return 1;                       /* r = RHS(w, t) */
+  if (method == 1) {
+    for (i = 0; i < N; i++) u[i] += dt * r[i];             /* u += r dt */
+    return 0;
+  }
+  for (i = 0; i < N; i++) {
+    u[i] += dt / 6. * r[i];                                /* u += r dt/6 */
+    w[i] = 1. * u_p[i] + dt * r[i];                        /* w = u_p + r dt */
+  }
+  if (nmo_rhs(m, t + dt, w, r)) return 1;                  /* r = RHS(w, t+dt) */
+  for (i = 0; i < N; i++) {
+    u[i] += dt / 6. * r[i];                                /* u += r dt/6 */
+    w[i] += dt * r[i];                                     /* w += r dt */
+    w[i] = 0.75 * u_p[i] + 0.25 * w[i];                    /* w = 0.75 u_p + 0.25 w */
+  }
+  if (nmo_rhs(m, t + 0.5 * dt, w, r)) return 1;            /* r = RHS(w, t+dt/2) */
+  for (i = 0; i < N; i++) u[i] += dt * 2. / 3. * r[i];     /* u += r dt*2/3 */
+  return 0;
+}
+
+/* nsteps steps of method 0 (RK4), 1 (Euler) or 2 (sspRK3), times
+   accumulated as in evolve_mesh */
+int nmo_evolve(const nmo_mesh *m, int method, double t, double dt, int nsteps, double *u)
+{
+  size_t N = (size_t)m->nelem * NF * m->n * m->n * m->n;
+  double *work = (double *)malloc(3 * N * sizeof(double));
+  long double Te = t, te = 0.;
+  int s, rc = 0;
+  if (!work) return 2;
+  for (s = 0; s < nsteps && !rc; s++) {
+    double ts = (double)(Te + te);
+    rc = method == 0 ? nmo_rk4_step(m, ts, dt, u, work) : nmo_other_step(m, method, ts, dt, u, work);
+    te += dt;
+  }
+  free(work);
+  return rc;
+}
+
 /* nsteps RK4 steps; the time of each step is accumulated in long double as
    in evolve_mesh (src/main/main/main.c:610-626) */
 int nmo_rk4(const nmo_mesh *m, double t, double dt, int nsteps, double *u)

@@ -383,6 +383,17 @@ class OracleMesh:
             raise RuntimeError(f"nmo_trouble failed ({rc})")
         return fl, pe
 
+    def evolve(self, u, dt, nsteps, t=0.0, method="RK4"):
+        """nsteps steps of the reference's evolve_method RK4, Euler or sspRK3."""
+        u = np.array(u, np.float64, copy=True, order="C")
+        rc = lib().nmo_evolve(ctypes.byref(self.s), ctypes.c_int({"RK4": 0, "Euler": 1,
+                                                                   "sspRK3": 2}[method]),
+                              ctypes.c_double(t), ctypes.c_double(dt), ctypes.c_int(nsteps),
+                              u.ctypes.data_as(ctypes.c_void_p))
+        if rc:
+            raise RuntimeError(f"nmo_evolve failed ({rc})")
+        return u
+
     def rk4(self, u, dt, nsteps, t=0.0):
         u = np.array(u, np.float64, copy=True, order="C")
         rc = lib().nmo_rk4(ctypes.byref(self.s), ctypes.c_double(t),

@@ -111,6 +111,17 @@ CASES = {
                                 dt=0.002, steps=2, eps=0.02, seed=44,
                                 fv=dict(rec="WENOmZ_2", extrap="dnfn_extrap1",
                                         patches="0 2 4")),
+    # the reference's other time integrators (evolve_method = sspRK3 / Euler);
+    # the mixed case follows its own FV-DG test parfile (FV patches 0 2 4,
+    # WENOmZ_2, sspRK3) with one n for all directions
+    "ssp3_cs7_l1_n5": dict(mesh="cs7", n=5, luni=1, k=(0.3, -0.2, 0.1),
+                           dt=0.002, steps=3, eps=0.02, seed=45, method="sspRK3"),
+    "eul_box_l1_n5": dict(mesh="box", n=5, luni=1, k=(1.0, -0.5, 0.25),
+                          dt=0.002, steps=3, eps=0.02, seed=46, method="Euler"),
+    "ssp3_mixcs7_l1_n6_wZdnfn": dict(mesh="cs7", n=6, luni=1, k=(0.8, -0.5, 0.33166247903554),
+                                     dt=0.002, steps=3, eps=0.02, seed=47, method="sspRK3",
+                                     fv=dict(rec="WENOmZ_2", extrap="dnfn_extrap1",
+                                             patches="0 2 4")),
     # non-conforming faces: the listed patches refined one level further
     # (amr_hrefine_p), face traces interpolated across the level jump
     "nc_cs7_l0_n5_h0": dict(mesh="cs7", n=5, luni=0, k=(0.3, -0.2, 0.1),
@@ -129,7 +140,7 @@ def parfile(case, prefix):
     c = CASES[case]
     lines = [
         "physics = scalarwave1 nmgdump",
-        "evolve_method = RK4",
+        f"evolve_method = {c.get('method', 'RK4')}",
         f"dt = {c['dt']!r}",
         f"iterations = {c['steps']}",
         f"amr_luni = {c['luni']}",

@@ -22,6 +22,10 @@ MIX_CASES = ["mixcs7_l0_n7_w5dnfn", "mixcs7_l1_n5_w3no", "mixcs7_l1_n6_wZdnfn"]
 MIX_NEAR_CASES = ["mixcs7_l1_n6_wZdnfn"]
 # the reference's default upwind flux (DG, mixed, finite volume)
 UPW_CASES = ["upw_cs7_l1_n5", "upw_box_l1_n6", "upw_mixcs7_l0_n7_w5dnfn", "upw_fvbox_l1_n7_w5no"]
+# the reference's other time integrators (evolve_method = sspRK3, Euler);
+# the mixed one is a few ulp off in the oracle like MIX_NEAR_CASES
+METHOD_CASES = ["ssp3_cs7_l1_n5", "eul_box_l1_n5", "ssp3_mixcs7_l1_n6_wZdnfn"]
+METHOD_NEAR_CASES = ["ssp3_mixcs7_l1_n6_wZdnfn"]
 # non-conforming faces: patches refined one level further (amr_hrefine_p)
 NC_CASES = ["nc_cs7_l0_n5_h0", "nc_cs7_l0_n4_h1", "nc_cs7_l1_n5_h02", "nc_upw_cs7_l0_n6_h35"]
 # the oracle's non-conforming (and even-n DG/FV interface) traces take the

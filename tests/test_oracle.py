@@ -5,8 +5,8 @@ operation order and must match it bit for bit."""
 import numpy as np
 import pytest
 
-from helpers import (CASES, FV_CASES, MIX_CASES, MIX_NEAR_CASES, NC_CASES, RTOL_NC_ORACLE,
-                     UPW_CASES, load, rel_l2)
+from helpers import (CASES, FV_CASES, METHOD_CASES, METHOD_NEAR_CASES, MIX_CASES,
+                     MIX_NEAR_CASES, NC_CASES, RTOL_NC_ORACLE, UPW_CASES, load, rel_l2)
 from oracle import nmo
 
 
@@ -52,6 +52,19 @@ def test_oracle_mixed_dg_fv_bitexact(case):
     m = _oracle_mesh(d, meta)
     assert np.array_equal(m.rhs(d["u0"], 0.0), d["r0"])
     assert np.array_equal(m.rk4(d["u0"], meta["dt"], meta["steps"]), d["u_final"])
+
+
+@pytest.mark.parametrize("case", METHOD_CASES)
+def test_oracle_other_integrators_match_reference(case):
+    """evolve_method = sspRK3 and Euler: bit for bit (a few ulp on the mixed
+    even-n mesh, whose interface traces are a few ulp off)."""
+    d, meta = load(case)
+    m = _oracle_mesh(d, meta)
+    u = m.evolve(d["u0"], meta["dt"], meta["steps"], method=meta["method"])
+    if case in METHOD_NEAR_CASES:
+        assert rel_l2(u, d["u_final"]) <= RTOL_NC_ORACLE
+    else:
+        assert np.array_equal(u, d["u_final"])
 
 
 @pytest.mark.parametrize("case", MIX_NEAR_CASES)
