@@ -8,6 +8,10 @@
  *     else if(Getv(evolve_method, "RK4gpu"))
  *       Evolve_mesh = evolve_RK4gpu_mesh;
  *
+ * (and likewise "sspRK3gpu" / "Eulergpu" for evolve_sspRK3gpu_mesh and
+ * evolve_Eulergpu_mesh, the GPU forms of evolve_sspRK3_mesh and
+ * evolve_Euler_mesh)
+ *
  * evolve_RK4gpu_mesh has the signature and the time semantics of
  * evolve_RK4_mesh (src/main/evolve/RungeKutta.c:19-82): on the first call it
  * packs the mesh (element bboxes, Cartesian/curvilinear flag, x/y/z and
@@ -92,8 +96,9 @@ static void nmg_evolve_setup(tMesh *mesh)
   free(pat); free(curvi); free(bbox); free(xyz); free(dXdx);
 }
 
-/* same signature and time semantics as evolve_RK4_mesh */
-void evolve_RK4gpu_mesh(tMesh *mesh)
+/* one step of u of scalarwave1 through the context: method -1 is RK4
+   (nmg_rk4_steps_host), otherwise an NMG_EVOLVE_* integrator */
+static void nmg_evolve_step(tMesh *mesh, int method)
 {
   int E, np, e, f, iu[5];
   double t = mesh->time, dt = mesh->dt;
@@ -106,11 +111,24 @@ void evolve_RK4gpu_mesh(tMesh *mesh)
     for(f = 0; f < 5; f++)
       memcpy(nmg_evolve_u + ((size_t)e * 5 + f) * np, Vard_(mesh->myelm[e], iu[f]),
              np * sizeof(double));
-  nmg_evolve_check(nmg_rk4_steps_host(nmg_evolve_ctx, t, dt, 1, nmg_evolve_u),
-                   "nmg_rk4_steps_host");
+  if(method < 0)
+    nmg_evolve_check(nmg_rk4_steps_host(nmg_evolve_ctx, t, dt, 1, nmg_evolve_u),
+                     "nmg_rk4_steps_host");
+  else
+  {
+    nmg_evolve_check(nmg_set_evolve_method(nmg_evolve_ctx, method), "nmg_set_evolve_method");
+    nmg_evolve_check(nmg_evolve_steps_host(nmg_evolve_ctx, t, dt, 1, nmg_evolve_u),
+                     "nmg_evolve_steps_host");
+  }
   for(e = 0; e < E; e++)
     for(f = 0; f < 5; f++)
       memcpy(Vard_(mesh->myelm[e], iu[f]), nmg_evolve_u + ((size_t)e * 5 + f) * np,
              np * sizeof(double));
   mesh->time = t + dt; /* as RungeKutta.c:76 */
 }
+
+/* same signatures and time semantics as evolve_RK4_mesh, evolve_sspRK3_mesh
+   and evolve_Euler_mesh (src/main/evolve/RungeKutta.c:19-200) */
+void evolve_RK4gpu_mesh(tMesh *mesh) { nmg_evolve_step(mesh, -1); }
+void evolve_sspRK3gpu_mesh(tMesh *mesh) { nmg_evolve_step(mesh, NMG_EVOLVE_SSPRK3); }
+void evolve_Eulergpu_mesh(tMesh *mesh) { nmg_evolve_step(mesh, NMG_EVOLVE_EULER); }
