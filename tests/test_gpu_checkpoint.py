@@ -32,3 +32,29 @@ def test_restart_from_reference_checkpoint(case, tmp_path):
     assert rel_l2(got, want) <= RTOL_RK4
     ev.checkpoint_write(tmp_path / "next.bin")
     assert np.array_equal(ng.checkpoint_read_host(m, tmp_path / "next.bin"), got)
+
+
+def test_restarts_every_step_match_an_uninterrupted_run(tmp_path):
+    """The reference's checkpoint test: a run written to a checkpoint every
+    iteration and restarted from it each time matches the uninterrupted run
+    (here bit for bit: the file holds the doubles exactly)."""
+    d, meta = load("ckpt_cs7_l1_n3")
+    m = build_mesh(meta)
+    u0 = to_mesh_order(d["u0"], perm_to_mesh(m, d))
+    dt, nsteps = meta["dt"], 4
+    a = ng.Evolution(m, ng.BC_EXACT_PLANEWAVE, k=meta["k"])
+    a.set_kernel("eo")
+    a.set_state(u0)
+    for s in range(nsteps):
+        a.rk4_step(s * dt, dt)
+    ev = ng.Evolution(m, ng.BC_EXACT_PLANEWAVE, k=meta["k"])
+    ev.set_kernel("eo")
+    ev.set_state(u0)
+    for s in range(nsteps):
+        ev.rk4_step(s * dt, dt)
+        ev.checkpoint_write(tmp_path / "variables.bin")
+        ev.close()
+        ev = ng.Evolution(m, ng.BC_EXACT_PLANEWAVE, k=meta["k"])
+        ev.set_kernel("eo")
+        ev.checkpoint_read(tmp_path / "variables.bin")
+    assert np.array_equal(ev.get_state(), a.get_state())
