@@ -299,6 +299,12 @@ int nmg_set_numflux(nmg_ctx *c, int32_t kind);
  * fv_WENOm3_opt_weightratio (src/main/dg/dg.c:286-400; defaults WENOm3_2,
  * dnfn_extrap1, 2).  NMG_EUNSUP on a DG context. */
 int nmg_set_fv(nmg_ctx *c, int32_t rec, int32_t extrap, double w3ratio);
+/* traces of finite-volume neighbours on DG faces, the reference's par
+ * fv_surface_interp (src/main/dg/dg.c:369-379, basis_pw_linear /
+ * basis_pw_parab in set_ajsurf_vl, src/main/amr/surface.c:1200-1240) */
+#define NMG_FV_SURF_LINEAR 0    /* "linear" (reference default) */
+#define NMG_FV_SURF_PARABOLIC 1 /* "parabolic" */
+int nmg_set_fv_surface_interp(nmg_ctx *c, int32_t mode);
 
 /* r = RHS(w, t) with w, r device pointers of nmg_state_size() doubles.
  * Replaces evolve_setrhs_mesh (src/main/evolve/evolve.c:182-232) for the

@@ -189,6 +189,7 @@ def lib(build_if_missing=True):
         "nmg_norms": (ctypes.c_int, [vp, vp, vp]),
         "nmg_set_numflux": (ctypes.c_int, [vp, i32]),
         "nmg_set_evolve_method": (ctypes.c_int, [vp, i32]),
+        "nmg_set_fv_surface_interp": (ctypes.c_int, [vp, i32]),
         "nmg_evolve_steps": (ctypes.c_int, [vp, f64, f64, i32]),
         "nmg_evolve_steps_host": (ctypes.c_int, [vp, f64, f64, i32, vp]),
         "nmg_checkpoint_write": (ctypes.c_int, [vp, vp, ctypes.c_char_p, vp]),
@@ -500,6 +501,13 @@ class Evolution:
             res[name] = dict(zip(("VolInt", "mean", "rms", "min", "max", "maxAbs"),
                                  out[1 + 6 * l: 7 + 6 * l]))
         return res
+
+    def set_fv_surface_interp(self, mode="linear"):
+        """Traces of finite-volume neighbours on DG faces: "linear" or
+        "parabolic" (the reference's fv_surface_interp)."""
+        self._check(lib().nmg_set_fv_surface_interp(self._h, {"linear": 0,
+                                                              "parabolic": 1}[mode]),
+                    "nmg_set_fv_surface_interp")
 
     def set_evolve_method(self, method="RK4"):
         """The reference's evolve_method ("RK4", "Euler", "sspRK3") used by

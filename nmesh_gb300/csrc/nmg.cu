@@ -245,6 +245,8 @@ struct nmg_ctx {
   double *d_wq = nullptr;      // [2][n] LGL and trapezoid (equally spaced) weights
   double *d_npart = nullptr;   // [E][6][4] partial norms
   int fv_rec = NMG_FV_REC_WENOM3_2, fv_extrap = NMG_FV_EXTRAP_DNFN1;
+  int fv_surf = NMG_FV_SURF_LINEAR;   // traces from FV neighbours (fv_surface_interp)
+  std::vector<double> h_xl, h_xu;     // LGL and equally spaced points
   double fv_w3ratio = 2.;
   double *d_fvgeo = nullptr, *d_fvdist = nullptr, *d_fvdxb = nullptr;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // one RK4 step, u in d_buf[0] / d_buf[1]
@@ -596,6 +598,90 @@ static void fv_pack_element(const nmg_mesh &m, int64_t e, int cs, const double *
   }
 }
 
+/* piecewise-linear basis function k of the points xp at x
+   (basis_pw_linear, src/main/basis/interpolate.c:53-100) */
+static double pw_linear_basis(int k, double x, int n, const double *xu) {
+  if (n <= 1) return 1.;
+  if (x < xu[1]) {
+    if (k == 0) return (x - xu[1]) / (xu[0] - xu[1]);
+    if (k == 1) return (x - xu[0]) / (xu[1] - xu[0]);
+    return 0.;
+  }
+  if (x >= xu[n - 2]) {
+    const int n0 = n - 2, n1 = n - 1, l = k - n0;
+    if (l == 0) return (x - xu[n1]) / (xu[n0] - xu[n1]);
+    if (l == 1) return (x - xu[n0]) / (xu[n1] - xu[n0]);
+    return 0.;
+  }
+  if (k < n - 1 && x >= xu[k] && x < xu[k + 1]) return (x - xu[k + 1]) / (xu[k] - xu[k + 1]);
+  if (k > 0 && x >= xu[k - 1] && x < xu[k]) return (x - xu[k - 1]) / (xu[k] - xu[k - 1]);
+  return 0.;
+}
+
+/* piecewise-parabolic basis function k of the points xp at x
+   (basis_pw_parab, src/main/basis/interpolate.c:106-224) */
+static double pw_parab_basis(int k, double x, int np, const double *xp)
+{
+  int m, m1, m2;
+  double xml, xmr, xmll, xmrr;
+  if (np < 3) return pw_linear_basis(k, x, np, xp);
+  if (np == 3) {
+    if (k == 0) return (x - xp[1]) * (x - xp[2]) / ((xp[0] - xp[1]) * (xp[0] - xp[2]));
+    if (k == 1) return (x - xp[0]) * (x - xp[2]) / ((xp[1] - xp[0]) * (xp[1] - xp[2]));
+    if (k == 2) return (x - xp[0]) * (x - xp[1]) / ((xp[2] - xp[0]) * (xp[2] - xp[1]));
+    return 0.;
+  }
+  xmr = 0.5 * (xp[0] + xp[1]);
+  if (x < xmr) {
+    if (k == 0) return (x - xp[1]) * (x - xp[2]) / ((xp[0] - xp[1]) * (xp[0] - xp[2]));
+    if (k == 1) return (x - xp[0]) * (x - xp[2]) / ((xp[1] - xp[0]) * (xp[1] - xp[2]));
+    if (k == 2) return (x - xp[0]) * (x - xp[1]) / ((xp[2] - xp[0]) * (xp[2] - xp[1]));
+    return 0.;
+  }
+  xml = 0.5 * (xp[np - 2] + xp[np - 1]);
+  if (x >= xml) {
+    int n0 = np - 3, n1 = np - 2, n2 = np - 1, l = k - n0;
+    if (l == 0) return (x - xp[n1]) * (x - xp[n2]) / ((xp[n0] - xp[n1]) * (xp[n0] - xp[n2]));
+    if (l == 1) return (x - xp[n0]) * (x - xp[n2]) / ((xp[n1] - xp[n0]) * (xp[n1] - xp[n2]));
+    if (l == 2) return (x - xp[n0]) * (x - xp[n1]) / ((xp[n2] - xp[n0]) * (xp[n2] - xp[n1]));
+    return 0.;
+  }
+  if (k <= 0) {
+    m = 0;
+    xmr = 0.5 * (xp[m] + xp[m + 1]);
+    xml = xp[m] - (xmr - xp[m]);
+    xmll = xml - (xmr - xml);
+    xmrr = 0.5 * (xp[m + 1] + xp[m + 2]);
+    m1 = 1;
+    m2 = 2;
+  } else if (k < np - 1) {
+    m = k;
+    xml = 0.5 * (xp[m] + xp[m - 1]);
+    xmr = 0.5 * (xp[m] + xp[m + 1]);
+    if (k < np - 2) xmrr = 0.5 * (xp[m + 1] + xp[m + 2]);
+    else xmrr = xmr + (xmr - xml);
+    if (k >= 2) xmll = 0.5 * (xp[m - 1] + xp[m - 2]);
+    else xmll = xml - (xmr - xml);
+    m1 = k - 1;
+    m2 = k + 1;
+  } else {
+    m = np - 1;
+    xml = 0.5 * (xp[m - 1] + xp[m]);
+    xmr = xp[m] + (xp[m] - xml);
+    xmll = 0.5 * (xp[m - 2] + xp[m - 1]);
+    xmrr = xmr + (xmr - xml);
+    m1 = m - 2;
+    m2 = m - 1;
+  }
+  if (x >= xml && x < xmr)
+    return (x - xp[m1]) * (x - xp[m2]) / ((xp[m] - xp[m1]) * (xp[m] - xp[m2]));
+  if (x >= xmll && x < xml)
+    return (x - xp[m - 2]) * (x - xp[m - 1]) / ((xp[m] - xp[m - 2]) * (xp[m] - xp[m - 1]));
+  if (x >= xmr && x < xmrr)
+    return (x - xp[m + 1]) * (x - xp[m + 2]) / ((xp[m] - xp[m + 1]) * (xp[m] - xp[m + 2]));
+  return 0.;
+}
+
 static void drop_graphs(nmg_ctx *c) {
   for (int g = 0; g < 2; g++)
     if (c->graph[g]) {
@@ -702,6 +788,8 @@ static int create_impl(const nmg_mesh *m, int32_t bc_kind, const double k[3], bo
   c->bc = bc_kind;
   if (k) for (int d = 0; d < 3; d++) c->k[d] = k[d];
   c->state_len = (size_t)E * NF * np;
+  c->h_xl = m->x;
+  c->h_xu = m->xu;
 
   // element types and the type-independent face table
   c->h_fv.assign(E, 0);
@@ -845,30 +933,13 @@ static int create_impl(const nmg_mesh *m, int32_t bc_kind, const double k[3], bo
         if (j != i) denom *= (xl[i] - xl[j]);
       wl[i] = 1. / denom;
     }
-    auto pwlin = [&](int k, double x) -> double {
-      if (n <= 1) return 1.;
-      if (x < xu[1]) {
-        if (k == 0) return (x - xu[1]) / (xu[0] - xu[1]);
-        if (k == 1) return (x - xu[0]) / (xu[1] - xu[0]);
-        return 0.;
-      }
-      if (x >= xu[n - 2]) {
-        const int n0 = n - 2, n1 = n - 1, l = k - n0;
-        if (l == 0) return (x - xu[n1]) / (xu[n0] - xu[n1]);
-        if (l == 1) return (x - xu[n0]) / (xu[n1] - xu[n0]);
-        return 0.;
-      }
-      if (k < n - 1 && x >= xu[k] && x < xu[k + 1]) return (x - xu[k + 1]) / (xu[k] - xu[k + 1]);
-      if (k > 0 && x >= xu[k - 1] && x < xu[k]) return (x - xu[k - 1]) / (xu[k] - xu[k - 1]);
-      return 0.;
-    };
     for (int p = 0; p < n; p++)
       for (int j = 0; j < n; j++) {
         double prod = 1.;
         for (int q = 0; q < n; q++)
           if (q != j) prod *= (xu[p] - xl[q]);
         gM[p * n + j] = prod * wl[j];
-        gM[nn + p * n + j] = pwlin(j, xl[p]);
+        gM[nn + p * n + j] = pw_linear_basis(j, xl[p], n, xu);
       }
     // element switches: P = the same Lagrange matrix (LGL -> equally spaced,
     // gridpoints.c:158-178) and R = P^{-1} (uniform -> LGL; the reference's
@@ -1420,6 +1491,26 @@ int nmg_set_numflux(nmg_ctx *c, int32_t kind) {
     return set_err(c, NMG_EINVAL, "nmg_set_numflux: unknown numerical flux");
   c->numflux = kind;
   drop_graphs(c);
+  return NMG_OK;
+}
+
+int nmg_set_fv_surface_interp(nmg_ctx *c, int32_t mode) {
+  if (!c) return NMG_EINVAL;
+  if (!c->mixed)
+    return set_err(c, NMG_EUNSUP, "nmg_set_fv_surface_interp: no DG / finite-volume faces");
+  if (mode != NMG_FV_SURF_LINEAR && mode != NMG_FV_SURF_PARABOLIC)
+    return set_err(c, NMG_EINVAL, "nmg_set_fv_surface_interp: unknown mode");
+  // M[1][p][j]: weight of equally spaced point j at LGL point p
+  const int n = c->n, nn = c->nn;
+  std::vector<double> M1(nn);
+  for (int p = 0; p < n; p++)
+    for (int j = 0; j < n; j++)
+      M1[p * n + j] = mode == NMG_FV_SURF_PARABOLIC
+                          ? pw_parab_basis(j, c->h_xl[p], n, c->h_xu.data())
+                          : pw_linear_basis(j, c->h_xl[p], n, c->h_xu.data());
+  CK(cudaStreamSynchronize(c->stream));
+  CK(cudaMemcpy(c->d_gM + nn, M1.data(), sizeof(double) * nn, cudaMemcpyHostToDevice));
+  c->fv_surf = mode;
   return NMG_OK;
 }
 

@@ -94,6 +94,8 @@ typedef struct nmo_mesh {
   const int32_t *hang_off;  /* [e*6*n*n + 1] */
   const int32_t *hang_src;  /* [c][2] */
   const double *hang_pos;   /* [c][2] */
+  int surf_interp;          /* traces from FV neighbours: 0 piecewise linear,
+                               1 piecewise parabolic (par fv_surface_interp) */
 } nmo_mesh;
 
 /* points of both point types: LGL (DG) with their Lagrange weights, and
@@ -416,6 +418,70 @@ static double pw_linear(int k, double x, int np, const double *xp)
   return 0.;
 }
 
+/* piecewise-parabolic basis function k of the points xp at x
+   (basis_pw_parab, src/main/basis/interpolate.c:106-224) */
+static double pw_parab(int k, double x, int np, const double *xp)
+{
+  int m, m1, m2;
+  double xml, xmr, xmll, xmrr;
+  if (np < 3) return pw_linear(k, x, np, xp);
+  if (np == 3) {
+    if (k == 0) return (x - xp[1]) * (x - xp[2]) / ((xp[0] - xp[1]) * (xp[0] - xp[2]));
+    if (k == 1) return (x - xp[0]) * (x - xp[2]) / ((xp[1] - xp[0]) * (xp[1] - xp[2]));
+    if (k == 2) return (x - xp[0]) * (x - xp[1]) / ((xp[2] - xp[0]) * (xp[2] - xp[1]));
+    return 0.;
+  }
+  xmr = 0.5 * (xp[0] + xp[1]);
+  if (x < xmr) {
+    if (k == 0) return (x - xp[1]) * (x - xp[2]) / ((xp[0] - xp[1]) * (xp[0] - xp[2]));
+    if (k == 1) return (x - xp[0]) * (x - xp[2]) / ((xp[1] - xp[0]) * (xp[1] - xp[2]));
+    if (k == 2) return (x - xp[0]) * (x - xp[1]) / ((xp[2] - xp[0]) * (xp[2] - xp[1]));
+    return 0.;
+  }
+  xml = 0.5 * (xp[np - 2] + xp[np - 1]);
+  if (x >= xml) {
+    int n0 = np - 3, n1 = np - 2, n2 = np - 1, l = k - n0;
+    if (l == 0) return (x - xp[n1]) * (x - xp[n2]) / ((xp[n0] - xp[n1]) * (xp[n0] - xp[n2]));
+    if (l == 1) return (x - xp[n0]) * (x - xp[n2]) / ((xp[n1] - xp[n0]) * (xp[n1] - xp[n2]));
+    if (l == 2) return (x - xp[n0]) * (x - xp[n1]) / ((xp[n2] - xp[n0]) * (xp[n2] - xp[n1]));
+    return 0.;
+  }
+  if (k <= 0) {
+    m = 0;
+    xmr = 0.5 * (xp[m] + xp[m + 1]);
+    xml = xp[m] - (xmr - xp[m]);
+    xmll = xml - (xmr - xml);
+    xmrr = 0.5 * (xp[m + 1] + xp[m + 2]);
+    m1 = 1;
+    m2 = 2;
+  } else if (k < np - 1) {
+    m = k;
+    xml = 0.5 * (xp[m] + xp[m - 1]);
+    xmr = 0.5 * (xp[m] + xp[m + 1]);
+    if (k < np - 2) xmrr = 0.5 * (xp[m + 1] + xp[m + 2]);
+    else xmrr = xmr + (xmr - xml);
+    if (k >= 2) xmll = 0.5 * (xp[m - 1] + xp[m - 2]);
+    else xmll = xml - (xmr - xml);
+    m1 = k - 1;
+    m2 = k + 1;
+  } else {
+    m = np - 1;
+    xml = 0.5 * (xp[m - 1] + xp[m]);
+    xmr = xp[m] + (xp[m] - xml);
+    xmll = 0.5 * (xp[m - 2] + xp[m - 1]);
+    xmrr = xmr + (xmr - xml);
+    m1 = m - 2;
+    m2 = m - 1;
+  }
+  if (x >= xml && x < xmr)
+    return (x - xp[m1]) * (x - xp[m2]) / ((xp[m] - xp[m1]) * (xp[m] - xp[m2]));
+  if (x >= xmll && x < xml)
+    return (x - xp[m - 2]) * (x - xp[m - 1]) / ((xp[m] - xp[m - 2]) * (xp[m] - xp[m - 1]));
+  if (x >= xmr && x < xmrr)
+    return (x - xp[m + 1]) * (x - xp[m + 2]) / ((xp[m] - xp[m + 1]) * (xp[m] - xp[m + 2]));
+  return 0.;
+}
+
 /* Lagrange basis function k at x (Lagrange_of_x) */
 static double lagrange_of_x(int k, double x, int np, const double *xp, const double *wl)
 {
@@ -444,8 +510,13 @@ static void mixed_trace(const nmo_mesh *m, const nmo_pts *P, int e, int f, int a
   c1 = xme[aa];
   c2 = xme[bb];
   for (k = 0; k < n; k++) {
-    B1[k] = nbfv ? pw_linear(k, c1, n, P->xu) : lagrange_of_x(k, c1, n, P->xl, P->wl);
-    B2[k] = nbfv ? pw_linear(k, c2, n, P->xu) : lagrange_of_x(k, c2, n, P->xl, P->wl);
+    if (nbfv && m->surf_interp == 1) {
+      B1[k] = pw_parab(k, c1, n, P->xu);
+      B2[k] = pw_parab(k, c2, n, P->xu);
+    } else {
+      B1[k] = nbfv ? pw_linear(k, c1, n, P->xu) : lagrange_of_x(k, c1, n, P->xl, P->wl);
+      B2[k] = nbfv ? pw_linear(k, c2, n, P->xu) : lagrange_of_x(k, c2, n, P->xl, P->wl);
+    }
   }
   for (l = 0; l < NF; l++) {
     const double *v = w + ((size_t)e2 * NF + l) * np;

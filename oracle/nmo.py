@@ -41,7 +41,8 @@ class _Mesh(ctypes.Structure):
                 ("fv_rec", ctypes.c_int), ("fv_extrap", ctypes.c_int),
                 ("fv_w3ratio", ctypes.c_double), ("mixface", ctypes.c_void_p),
                 ("numflux", ctypes.c_int), ("hang_off", ctypes.c_void_p),
-                ("hang_src", ctypes.c_void_p), ("hang_pos", ctypes.c_void_p)]
+                ("hang_src", ctypes.c_void_p), ("hang_pos", ctypes.c_void_p),
+                ("surf_interp", ctypes.c_int)]
 
 # reconstruction modes (reference par fv_rec) and div(f) extrapolation
 # modes (par fv_divf_extrap) understood by the oracle
@@ -328,7 +329,7 @@ class OracleMesh:
     def __init__(self, bbox, curvi, dXdx, xyz, nbnode, n, bc=0,
                  k=(1.0, 1.0, 1.0), fv=None, fv_rec="WENOm5_2",
                  fv_extrap="dnfn_extrap1", fv_w3ratio=2.0, mixface=None, numflux="LLF",
-                 hang=None):
+                 hang=None, fv_surface_interp="linear"):
         """fv: per-element finite-volume flags (None: all DG); fv_rec and
         fv_extrap name the reference's fv_rec / fv_divf_extrap modes;
         mixface: faces between the two point types (see match_faces);
@@ -353,7 +354,8 @@ class OracleMesh:
                        None if self.mixface is None else self.mixface.ctypes.data,
                        1 if numflux == "upwind" else 0,
                        *((None,) * 3 if self.hang is None else
-                         tuple(a.ctypes.data for a in self.hang)))
+                         tuple(a.ctypes.data for a in self.hang)),
+                       {"linear": 0, "parabolic": 1}[fv_surface_interp])
 
     def rhs(self, w, t=0.0):
         w = np.ascontiguousarray(w, np.float64)

@@ -122,6 +122,15 @@ CASES = {
                                      dt=0.002, steps=3, eps=0.02, seed=47, method="sspRK3",
                                      fv=dict(rec="WENOmZ_2", extrap="dnfn_extrap1",
                                              patches="0 2 4")),
+    # fv_surface_interp = parabolic (as in the reference's FV-DG test parfile)
+    "mixcs7_l0_n7_w5parab": dict(mesh="cs7", n=7, luni=0, k=(0.3, -0.2, 0.1),
+                                 dt=0.002, steps=2, eps=0.02, seed=48,
+                                 fv=dict(rec="WENOm5_2", extrap="dnfn_extrap1",
+                                         patches="0", surf="parabolic")),
+    "ssp3_mixcs7_l0_n7_wZparab": dict(mesh="cs7", n=7, luni=0, k=(0.8, -0.5, 0.33166247903554),
+                                      dt=0.002, steps=3, eps=0.02, seed=49, method="sspRK3",
+                                      fv=dict(rec="WENOmZ_2", extrap="dnfn_extrap1",
+                                              patches="0 2 4", surf="parabolic")),
     # non-conforming faces: the listed patches refined one level further
     # (amr_hrefine_p), face traces interpolated across the level jump
     "nc_cs7_l0_n5_h0": dict(mesh="cs7", n=5, luni=0, k=(0.3, -0.2, 0.1),
@@ -173,7 +182,8 @@ def parfile(case, prefix):
         pats = c["fv"].get("patches", pats)
         lines += [f"amr_uniform_p = {pats}", f"amr_fv_p = {pats}",
                   f"fv_rec = {c['fv']['rec']}",
-                  f"fv_divf_extrap = {c['fv']['extrap']}"]
+                  f"fv_divf_extrap = {c['fv']['extrap']}",
+                  f"fv_surface_interp = {c['fv'].get('surf', 'linear')}"]
     return "\n".join(lines) + "\n"
 
 

@@ -14,7 +14,8 @@ FV_CASES = ["fvbox_l1_n7_w5no", "fvbox_l1_n7_w5dnfn", "fvbox_l2_n5_w3dnfn",
             "fvbox_l0_n13_w5dnfn", "fvcs7_l0_n7_w5dnfn", "fvcs7_l0_n6_w5no",
             "fvcs7_l0_n7_wZdnfn", "fvbox_l1_n8_wZno"]
 # mixed fixtures: inner cube finite-volume, cubed-sphere shells DG
-MIX_CASES = ["mixcs7_l0_n7_w5dnfn", "mixcs7_l1_n5_w3no", "mixcs7_l1_n6_wZdnfn"]
+MIX_CASES = ["mixcs7_l0_n7_w5dnfn", "mixcs7_l1_n5_w3no", "mixcs7_l1_n6_wZdnfn",
+             "mixcs7_l0_n7_w5parab"]
 # mixed fixtures where the oracle is a few ulp off the reference: the
 # interface positions come from the point sets here and from coordinate
 # conversions (X -> the neighbour's Xb) in the reference; they round
@@ -24,8 +25,9 @@ MIX_NEAR_CASES = ["mixcs7_l1_n6_wZdnfn"]
 UPW_CASES = ["upw_cs7_l1_n5", "upw_box_l1_n6", "upw_mixcs7_l0_n7_w5dnfn", "upw_fvbox_l1_n7_w5no"]
 # the reference's other time integrators (evolve_method = sspRK3, Euler);
 # the mixed one is a few ulp off in the oracle like MIX_NEAR_CASES
-METHOD_CASES = ["ssp3_cs7_l1_n5", "eul_box_l1_n5", "ssp3_mixcs7_l1_n6_wZdnfn"]
-METHOD_NEAR_CASES = ["ssp3_mixcs7_l1_n6_wZdnfn"]
+METHOD_CASES = ["ssp3_cs7_l1_n5", "eul_box_l1_n5", "ssp3_mixcs7_l1_n6_wZdnfn",
+                "ssp3_mixcs7_l0_n7_wZparab"]
+METHOD_NEAR_CASES = ["ssp3_mixcs7_l1_n6_wZdnfn", "ssp3_mixcs7_l0_n7_wZparab"]
 # non-conforming faces: patches refined one level further (amr_hrefine_p)
 NC_CASES = ["nc_cs7_l0_n5_h0", "nc_cs7_l0_n4_h1", "nc_cs7_l1_n5_h02", "nc_upw_cs7_l0_n6_h35"]
 # the oracle's non-conforming (and even-n DG/FV interface) traces take the
@@ -78,7 +80,8 @@ def rel_l2(a, b):
 
 
 def oracle_for(mesh, bc=0, k=(1.0, 1.0, 1.0), period=None, fv_rec="WENOm3_2",
-               fv_extrap="dnfn_extrap1", fv_w3ratio=2.0, numflux="LLF"):
+               fv_extrap="dnfn_extrap1", fv_w3ratio=2.0, numflux="LLF",
+               fv_surface_interp="linear"):
     """Oracle mesh built from the product mesh's geometry, with its own
     coordinate-matching neighbour table (and the mesh's finite-volume flags
     with the given fin.-vol. options)."""
@@ -100,7 +103,7 @@ def oracle_for(mesh, bc=0, k=(1.0, 1.0, 1.0), period=None, fv_rec="WENOm3_2",
     return nmo.OracleMesh(bbox, curvi, dXdx, xyz, nb, mesh.n, bc=bc, k=k,
                           fv=fv if fv.any() else None, fv_rec=fv_rec,
                           fv_extrap=fv_extrap, fv_w3ratio=fv_w3ratio, mixface=mix,
-                          numflux=numflux, hang=hang)
+                          numflux=numflux, hang=hang, fv_surface_interp=fv_surface_interp)
 
 
 def gaussian_pulses(xyz, seed, npulse=8, rmin=3.0, rmax=10.0, wmin=0.5, wmax=2.0,

@@ -20,6 +20,8 @@ def _ev(m, meta, bc=ng.BC_EXACT_PLANEWAVE):
     ev = ng.Evolution(m, bc, k=meta["k"])
     if "fv" in meta:
         ev.set_fv(meta["fv"]["rec"], meta["fv"]["extrap"])
+        if ev.mesh.fv().min() == 0:
+            ev.set_fv_surface_interp(meta["fv"].get("surf", "linear"))
     ev.set_evolve_method(meta["method"])
     return ev
 

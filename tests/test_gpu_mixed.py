@@ -37,6 +37,7 @@ def test_mixed_matches_reference(case, dg, fv):
     assert np.array_equal(m.fv()[perm], d["use_fv"])
     ev = ng.Evolution(m, ng.BC_EXACT_PLANEWAVE, k=meta["k"])
     ev.set_fv(meta["fv"]["rec"], meta["fv"]["extrap"])
+    ev.set_fv_surface_interp(meta["fv"].get("surf", "linear"))
     _set(ev, dg, fv)
     r = ev.rhs(to_mesh_order(d["u0"], perm), 0.0)
     assert rel_l2(r[perm], d["r0"]) <= RTOL_RHS
@@ -109,3 +110,23 @@ def test_mixed_single_steps_equal_graph_steps():
     for s in range(3):
         ev.rk4_step(0.01 * s, 0.01)
     assert np.array_equal(ev.get_state(), ug)
+
+
+def test_parabolic_surface_interpolation_matches_oracle():
+    """fv_surface_interp = parabolic on an outgoing mixed mesh, every DG
+    variant, against the oracle; switching back to linear restores the
+    linear traces."""
+    m = ng.Mesh.build(ng.MESH_CUBEDSPHERES7, n=7, luni=1, cs_dc=1.0, cs_r0fac=20.0, fv=[0, 3])
+    u = gaussian_pulses(m.coords(), seed=8, rmin=1.0, rmax=4.0)
+    for surf in ("parabolic", "linear"):
+        o = oracle_for(m, bc=1, fv_rec="WENOm5_2", fv_extrap="dnfn_extrap1",
+                       fv_surface_interp=surf)
+        ev = ng.Evolution(m, ng.BC_OUTGOING)
+        ev.set_fv("WENOm5_2", "dnfn_extrap1")
+        ev.set_fv_surface_interp("parabolic")
+        ev.set_fv_surface_interp(surf)
+        assert rel_l2(ev.rhs(u, 0.0), o.rhs(u, 0.0)) <= RTOL_RHS
+        assert rel_l2(ev.rk4_steps_host(u, 0.0, 0.002, 2), o.rk4(u, 0.002, 2)) <= RTOL_RK4
+    with pytest.raises(ng.NmgError):
+        ng.Evolution(ng.Mesh.build(ng.MESH_BOX, n=5, luni=1), ng.BC_OUTGOING) \
+            .set_fv_surface_interp("parabolic")

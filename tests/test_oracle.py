@@ -18,7 +18,8 @@ def _oracle_mesh(d, meta):
     if "fv" in meta:
         nb, mix = nmo.match_faces(d["x"], n, fv=d["use_fv"])
         fv = dict(fv=d["use_fv"], fv_rec=meta["fv"]["rec"],
-                  fv_extrap=meta["fv"]["extrap"], mixface=mix)
+                  fv_extrap=meta["fv"]["extrap"], mixface=mix,
+                  fv_surface_interp=meta["fv"].get("surf", "linear"))
     else:
         nb = nmo.match_faces(d["x"], n)
     if meta.get("hrefine"):
