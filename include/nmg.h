@@ -140,6 +140,11 @@ int nmg_basis(int32_t n, double *x, double *w, double *D);
  * src/main/amr/surface.c:799-1360). */
 int nmg_mesh_get_hanging(const nmg_mesh *m, int64_t *nface, int64_t *ncontrib, int32_t *hface,
                          int32_t *hoff, int32_t *hsrc, double *hpos);
+/* [nelem][3][9][n^3]: dX^a/dx^i at the midpoints between the equally spaced
+ * points (coordinates_midpoint_data, src/main/coordinates/coordinates.c:
+ * 283-375): block d at node (i,j,k) holds the value at the midpoint to the
+ * right of that node in direction d (last plane unused); generated meshes */
+int nmg_mesh_get_midpoint_dXdx(const nmg_mesh *m, double *dXdxm);
 /* equally spaced points on [-1,1] (uniform_x, src/main/basis/Legendre.c:626) */
 int nmg_uniform_points(int32_t n, double *x);
 void nmg_mesh_free(nmg_mesh *m);
@@ -305,6 +310,11 @@ int nmg_set_fv(nmg_ctx *c, int32_t rec, int32_t extrap, double w3ratio);
 #define NMG_FV_SURF_LINEAR 0    /* "linear" (reference default) */
 #define NMG_FV_SURF_PARABOLIC 1 /* "parabolic" */
 int nmg_set_fv_surface_interp(nmg_ctx *c, int32_t mode);
+/* the reference's par coordinates_midpoint_data = yes (on != 0): the
+ * finite-volume flux factors J sqrtgdiag of the midpoints and the normals of
+ * the midpoint fluxes come from the map at the midpoints (fv.c:384-411,
+ * coordinates.c:283-437) instead of the grid points; generated meshes */
+int nmg_set_fv_midpoint_data(nmg_ctx *c, int32_t on);
 
 /* r = RHS(w, t) with w, r device pointers of nmg_state_size() doubles.
  * Replaces evolve_setrhs_mesh (src/main/evolve/evolve.c:182-232) for the

@@ -190,6 +190,8 @@ def lib(build_if_missing=True):
         "nmg_set_numflux": (ctypes.c_int, [vp, i32]),
         "nmg_set_evolve_method": (ctypes.c_int, [vp, i32]),
         "nmg_set_fv_surface_interp": (ctypes.c_int, [vp, i32]),
+        "nmg_set_fv_midpoint_data": (ctypes.c_int, [vp, i32]),
+        "nmg_mesh_get_midpoint_dXdx": (ctypes.c_int, [vp, vp]),
         "nmg_evolve_steps": (ctypes.c_int, [vp, f64, f64, i32]),
         "nmg_evolve_steps_host": (ctypes.c_int, [vp, f64, f64, i32, vp]),
         "nmg_checkpoint_write": (ctypes.c_int, [vp, vp, ctypes.c_char_p, vp]),
@@ -333,6 +335,14 @@ class Mesh:
         if lib().nmg_mesh_concat(arr, len(meshes), ctypes.byref(h)):
             raise NmgError(f"nmg_mesh_concat: {lib().nmg_mesh_last_error().decode()}")
         return cls(h.value)
+
+    def midpoint_dXdx(self):
+        """dX^a/dx^i [E, 3, 9, np] at the midpoints right of each node in
+        each direction (coordinates_midpoint_data)."""
+        out = np.zeros((self.nelem, 3, 9, self.np))
+        if lib().nmg_mesh_get_midpoint_dXdx(self._h, _ptr(out)):
+            raise NmgError(lib().nmg_mesh_last_error().decode())
+        return out
 
     def hanging(self):
         """Non-conforming faces: (hface [H,2], hoff [H*n*n+1], hsrc [C,2],
@@ -508,6 +518,12 @@ class Evolution:
         self._check(lib().nmg_set_fv_surface_interp(self._h, {"linear": 0,
                                                               "parabolic": 1}[mode]),
                     "nmg_set_fv_surface_interp")
+
+    def set_fv_midpoint_data(self, on=True):
+        """The reference's coordinates_midpoint_data = yes: FV midpoint flux
+        factors and normals from the map at the midpoints."""
+        self._check(lib().nmg_set_fv_midpoint_data(self._h, int(bool(on))),
+                    "nmg_set_fv_midpoint_data")
 
     def set_evolve_method(self, method="RK4"):
         """The reference's evolve_method ("RK4", "Euler", "sspRK3") used by

@@ -343,6 +343,40 @@ bool element_geometry(const nmg_mesh &m, int64_t e, bool uniform, double *xyz, d
   return true;
 }
 
+// midpoint positions set_nodemidpoint_XbYbZb (src/main/coordinates/
+// get_coords.c:1703-1740) and the map as at the grid points
+// (coordinates.c:283-375)
+bool element_midpoint_dXdx(const nmg_mesh &m, int64_t e, double *dXdxm) {
+  const int n = m.n, np = n * n * n;
+  const double *bb = &m.bbox[e * 6];
+  const double *px = m.xu.data();
+  const Patch *pat = nullptr;
+  if (!m.patches.empty()) pat = &m.patches[m.pat[e]];
+  else if (m.curvi[e]) return false;
+  for (int q = 0; q < 3 * 9 * np; q++) dXdxm[q] = 0.;
+  for (int d = 0; d < 3; d++)
+    for (int k = 0; k < n; k++)
+      for (int j = 0; j < n; j++)
+        for (int i = 0; i < n; i++) {
+          const int id[3] = {i, j, k};
+          if (id[d] >= n - 1) continue;
+          const int ijk = i + n * (j + n * k);
+          double Xb[3] = {px[i], px[j], px[k]}, X[3], x[3], J[3][3];
+          Xb[d] = 0.5 * (px[id[d]] + px[id[d] + 1]);
+          for (int c = 0; c < 3; c++)
+            X[c] = 0.5 * ((bb[2 * c + 1] - bb[2 * c]) * Xb[c] + (bb[2 * c + 1] + bb[2 * c]));
+          if (pat && pat->cubed) {
+            cubsph_x_dXdx(*pat, X, x, J);
+          } else {
+            for (int a = 0; a < 3; a++)
+              for (int c = 0; c < 3; c++) J[a][c] = (a == c) ? 1. : 0.;
+          }
+          for (int a = 0; a < 3; a++)
+            for (int c = 0; c < 3; c++) dXdxm[((d * 9) + a * 3 + c) * np + ijk] = J[a][c];
+        }
+  return true;
+}
+
 std::string pack_faces(nmg_mesh &m, const int64_t *nbnode, const double period[3]) {
   const int n = m.n, np = n * n * n, nn = n * n;
   const int64_t E = m.nelem;
@@ -828,6 +862,15 @@ int nmg_mesh_get_hanging(const nmg_mesh *m, int64_t *nface, int64_t *ncontrib, i
   if (hoff) std::copy(m->hoff.begin(), m->hoff.end(), hoff);
   if (hsrc) std::copy(m->hsrc.begin(), m->hsrc.end(), hsrc);
   if (hpos) std::copy(m->hpos.begin(), m->hpos.end(), hpos);
+  return NMG_OK;
+}
+
+int nmg_mesh_get_midpoint_dXdx(const nmg_mesh *m, double *dXdxm) {
+  if (!m || !dXdxm) return fail(NMG_EINVAL, "nmg_mesh_get_midpoint_dXdx: null argument");
+  const size_t per = (size_t)27 * m->n * m->n * m->n;
+  for (int64_t e = 0; e < m->nelem; e++)
+    if (!nmg::element_midpoint_dXdx(*m, e, dXdxm + e * per))
+      return fail(NMG_EUNSUP, "nmg_mesh_get_midpoint_dXdx: element map unknown");
   return NMG_OK;
 }
 

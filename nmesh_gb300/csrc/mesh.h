@@ -72,6 +72,11 @@ inline int face_node(int n, int f, int a, int b) {
 // (uniform = false) or equally spaced points; false if the element's patch
 // map is not known (a described curvilinear element)
 bool element_geometry(const nmg_mesh &m, int64_t e, bool uniform, double *xyz, double *dXdx);
+// dX^a/dx^i [3][9][np] of element e at the midpoints between its equally
+// spaced points: block d holds, at node (i, j, k), the values at the
+// midpoint to the right of that node in direction d (the last plane of each
+// direction is unused, zero); false if the element's map is unknown
+bool element_midpoint_dXdx(const nmg_mesh &m, int64_t e, double *dXdxm);
 // apply a dihedral orientation code to an in-plane index pair
 inline void orient_map(int n, int o, int a, int b, int *a2, int *b2) {
   int s = o & 1, fa = (o >> 1) & 1, fb = (o >> 2) & 1;

@@ -246,6 +246,11 @@ struct nmg_ctx {
   double *d_npart = nullptr;   // [E][6][4] partial norms
   int fv_rec = NMG_FV_REC_WENOM3_2, fv_extrap = NMG_FV_EXTRAP_DNFN1;
   int fv_surf = NMG_FV_SURF_LINEAR;   // traces from FV neighbours (fv_surface_interp)
+  // coordinates_midpoint_data = yes: midpoint factors of curvilinear elements
+  bool fv_mid = false;
+  double *d_fvmid = nullptr;          // [cslot][3][5][np]
+  nmg_mesh geom;                      // element bboxes, patches and point sets
+  std::vector<int> h_cslot;
   std::vector<double> h_xl, h_xu;     // LGL and equally spaced points
   double fv_w3ratio = 2.;
   double *d_fvgeo = nullptr, *d_fvdist = nullptr, *d_fvdxb = nullptr;
@@ -391,6 +396,7 @@ static StageParams base_params(nmg_ctx *c) {
   P.fvdist = c->d_fvdist;
   P.fvdxb = c->d_fvdxb;
   P.ghost = c->d_ghost;
+  P.fvmid = c->fv_mid ? c->d_fvmid : nullptr;
   P.numflux = c->numflux;
   P.fvbxyz = c->d_fvbxyz;
   P.fvbnrm = c->d_fvbnrm;
@@ -813,6 +819,15 @@ static int create_impl(const nmg_mesh *m, int32_t bc_kind, const double k[3], bo
   }
   c->ncurvi = C;
   c->nbface = B;
+  c->h_cslot = cslot;
+  // what the midpoint factors need later: the maps, not the node arrays
+  c->geom.n = m->n;
+  c->geom.nelem = m->nelem;
+  c->geom.pat = m->pat;
+  c->geom.bbox = m->bbox;
+  c->geom.curvi = m->curvi;
+  c->geom.xu = m->xu;
+  c->geom.patches = m->patches;
   // which geometries are needed: DG (LGL points) for DG elements, FV
   // (equally spaced points) for FV elements, both for every element of a
   // switchable context
@@ -1514,6 +1529,53 @@ int nmg_set_fv_surface_interp(nmg_ctx *c, int32_t mode) {
   return NMG_OK;
 }
 
+int nmg_set_fv_midpoint_data(nmg_ctx *c, int32_t on) {
+  if (!c) return NMG_EINVAL;
+  if (!c->fv) return set_err(c, NMG_EUNSUP, "nmg_set_fv_midpoint_data: no finite-volume elements");
+  if (on && !c->d_fvmid && c->ncurvi > 0) {
+    // per curvilinear element and direction d, at the midpoint right of each
+    // node: sqrtgdiag_d, det(dXb/dx) and the unit normal of direction d, in
+    // the operation order of the grid-point values (coordinates.c:174-223,
+    // 337-420, utilities.c:48-80)
+    const int n = c->n, np = c->np;
+    std::vector<double> mid((size_t)c->ncurvi * 15 * np, 0.), dX((size_t)27 * np);
+    for (int64_t e = 0; e < c->nelem; e++) {
+      const int cs = c->h_cslot[e];
+      if (cs < 0) continue;
+      if (!nmg::element_midpoint_dXdx(c->geom, e, dX.data()))
+        return set_err(c, NMG_EUNSUP,
+                       "nmg_set_fv_midpoint_data: needs the maps of a generated mesh");
+      const double *bb = &c->geom.bbox[e * 6];
+      const double d0 = 2. / (bb[1] - bb[0]), d1 = 2. / (bb[3] - bb[2]), d2 = 2. / (bb[5] - bb[4]);
+      const double dXbdX[3] = {d0, d1, d2};
+      double *Gm = &mid[(size_t)cs * 15 * np];
+      for (int d = 0; d < 3; d++)
+        for (int q = 0; q < np; q++) {
+          const int id[3] = {q % n, (q / n) % n, q / (n * n)};
+          if (id[d] >= n - 1) continue;
+          double M[3][3];
+          for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++) M[a][b] = dX[((size_t)d * 9 + a * 3 + b) * np + q];
+          const double det = M[0][0] * M[1][1] * M[2][2] - M[0][2] * M[1][1] * M[2][0] +
+                             M[0][1] * M[1][2] * M[2][0] + M[0][2] * M[1][0] * M[2][1] -
+                             M[0][0] * M[1][2] * M[2][1] - M[0][1] * M[1][0] * M[2][2];
+          double g = 0.0;
+          for (int l = 0; l < 3; l++) g += M[d][l] * M[d][l];
+          double smag = sqrt(M[d][0] * M[d][0] + M[d][1] * M[d][1] + M[d][2] * M[d][2]);
+          if (smag == 0.0) smag = 1.;
+          Gm[(d * 5 + 0) * np + q] = dXbdX[d] * sqrt(g);
+          Gm[(d * 5 + 1) * np + q] = d0 * d1 * d2 * det;
+          for (int l = 0; l < 3; l++) Gm[(d * 5 + 2 + l) * np + q] = M[d][l] / smag;
+        }
+    }
+    CK(cudaMalloc((void **)&c->d_fvmid, sizeof(double) * mid.size()));
+    CK(cudaMemcpy(c->d_fvmid, mid.data(), sizeof(double) * mid.size(), cudaMemcpyHostToDevice));
+  }
+  c->fv_mid = on != 0;
+  drop_graphs(c);
+  return NMG_OK;
+}
+
 int nmg_set_fv(nmg_ctx *c, int32_t rec, int32_t extrap, double w3ratio) {
   if (!c) return NMG_EINVAL;
   if (!c->fv) return set_err(c, NMG_EUNSUP, "nmg_set_fv: the mesh has no finite-volume elements");
@@ -1538,7 +1600,7 @@ void nmg_destroy(nmg_ctx *c) {
   cudaFree(c->d_D);
   cudaFree(c->d_fvgeo); cudaFree(c->d_fvdist); cudaFree(c->d_fvdxb);
   cudaFree(c->d_fvlist); cudaFree(c->d_gtab); cudaFree(c->d_isfv); cudaFree(c->d_ghost);
-  cudaFree(c->d_hoff); cudaFree(c->d_hsrc); cudaFree(c->d_hw);
+  cudaFree(c->d_hoff); cudaFree(c->d_hsrc); cudaFree(c->d_hw); cudaFree(c->d_fvmid);
   cudaFree(c->d_gM); cudaFree(c->d_fvbxyz); cudaFree(c->d_fvbnrm); cudaFree(c->d_PR);
   cudaFree(c->d_conv); cudaFree(c->d_mm); cudaFree(c->d_trb); cudaFree(c->d_score);
   cudaFree(c->d_r); cudaFree(c->d_w2); cudaFree(c->d_ghost2); cudaFree(c->d_tlist);

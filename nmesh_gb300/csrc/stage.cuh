@@ -72,6 +72,8 @@ struct StageParams {
   const unsigned char *skip;  // [E] 1: finite-volume element (DG kernels write nothing)
   const int *fvlist;    // [nfvel] finite-volume elements (FV kernel grid), or null: all
   int nfvel;
+  const double *fvmid;  // [cslot][3][5][np] midpoint sqrtgdiag_d, 1/J, normal_d
+                        // (coordinates_midpoint_data = yes), or null
   const double *ghost;  // [G][4][nn] interpolated traces of faces with code & 64;
                         // slot G = bslot[e*6+f]
   int numflux;          // NMG_NUMFLUX_LLF or NMG_NUMFLUX_UPWIND

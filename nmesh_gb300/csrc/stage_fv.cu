@@ -367,21 +367,28 @@ __device__ void face_fnum(const StageParams &P, int e, int f, int a, int b, cons
 }
 
 // J sqrtgdiag / dXb factors of node i0 of a pencil (fv.c:384-411)
-__device__ __forceinline__ void jgdow(const double *G, int np, const double *sc, double oojc,
-                                      int d, int n, int base, int st, int i0, double wc,
-                                      bool addsurf, double &JR, double &JL) {
+__device__ __forceinline__ void jgdow(const double *G, const double *Gm, int np,
+                                      const double *sc, double oojc, int d, int n, int base,
+                                      int st, int i0, double wc, bool addsurf, double &JR,
+                                      double &JL) {
   const int g0 = i0 > 0, lN = i0 < n - 1;
   const int ccc = base + i0 * st;
   const int cccL = base + (g0 ? i0 - 1 : i0) * st, cccR = base + (lN ? i0 : i0 - 1) * st;
+  // the factors of the midpoints (indices cccR, cccL): from the midpoint
+  // data when given, else those of the grid points there
+  const double sgR = Gm ? __ldg(Gm + (d * 5 + 0) * np + cccR) : sg_at(G, np, sc, d, cccR);
+  const double ojR = Gm ? __ldg(Gm + (d * 5 + 1) * np + cccR) : ooj_at(G, np, oojc, cccR);
+  const double sgL = Gm ? __ldg(Gm + (d * 5 + 0) * np + cccL) : sg_at(G, np, sc, d, cccL);
+  const double ojL = Gm ? __ldg(Gm + (d * 5 + 1) * np + cccL) : ooj_at(G, np, oojc, cccL);
   if (g0 && lN) {
-    JR = sg_at(G, np, sc, d, cccR) / (ooj_at(G, np, oojc, cccR) * wc);
-    JL = sg_at(G, np, sc, d, cccL) / (ooj_at(G, np, oojc, cccL) * wc);
+    JR = sgR / (ojR * wc);
+    JL = sgL / (ojL * wc);
   } else if (!g0 && lN) {
-    JR = sg_at(G, np, sc, d, cccR) / (ooj_at(G, np, oojc, cccR) * wc);
+    JR = sgR / (ojR * wc);
     JL = sg_at(G, np, sc, d, ccc) / (ooj_at(G, np, oojc, ccc) * wc);
   } else if (g0 && !lN) {
     JR = sg_at(G, np, sc, d, ccc) / (ooj_at(G, np, oojc, ccc) * wc);
-    JL = sg_at(G, np, sc, d, cccL) / (ooj_at(G, np, oojc, cccL) * wc);
+    JL = sgL / (ojL * wc);
   } else {
     JR = JL = sg_at(G, np, sc, d, ccc) / (ooj_at(G, np, oojc, ccc) * wc);
   }
@@ -418,6 +425,8 @@ __global__ void __launch_bounds__(NT) fv_kernel(const StageParams P) {
   }
   __syncthreads();
   const double *G = sCs >= 0 ? P.fvgeo + (size_t)sCs * kGeo * np : nullptr;
+  // midpoint data of a curvilinear element (affine maps: equal to the grid's)
+  const double *Gm = (sCs >= 0 && P.fvmid) ? P.fvmid + (size_t)sCs * 15 * np : nullptr;
   const double oojc = sOoJc;
 
 #pragma unroll 1
@@ -441,7 +450,12 @@ __global__ void __launch_bounds__(NT) fv_kernel(const StageParams P) {
         ua[l] = rec_m(P.fv_rec, n, v, im, r3);
       }
       double nr[3], fn[4];
-      normal_at(P, G, np, d, base + im * st, nr);
+      if (Gm) {
+#pragma unroll
+        for (int c = 0; c < 3; c++) nr[c] = __ldg(Gm + (d * 5 + 2 + c) * np + base + im * st);
+      } else {
+        normal_at(P, G, np, d, base + im * st, nr);
+      }
       numflux4(P.numflux, ui, ua, nr, fn);
 #pragma unroll
       for (int l = 0; l < 4; l++) sF[(l * nm + im) * nn + Pn] = fn[l];
@@ -454,7 +468,7 @@ __global__ void __launch_bounds__(NT) fv_kernel(const StageParams P) {
       const int node = base + i0 * st;
       const double wc = i0 == 0 ? sDist[2 * d] : i0 == n - 1 ? sDist[2 * d + 1] : __ldg(P.fvdxb + i0);
       double JR, JL;
-      jgdow(G, np, sSc, oojc, d, n, base, st, i0, wc, addsurf, JR, JL);
+      jgdow(G, Gm, np, sSc, oojc, d, n, base, st, i0, wc, addsurf, JR, JL);
       double fR[4], fL[4];
       if (i0 < n - 1) {
         for (int l = 0; l < 4; l++) fR[l] = sF[(l * nm + i0) * nn + Pn];
@@ -483,7 +497,7 @@ __global__ void __launch_bounds__(NT) fv_kernel(const StageParams P) {
         const int i1 = i0 == 0 ? 1 : n - 2;
         const double wc1 = (i1 == 0 || i1 == n - 1) ? sDist[2 * d + (i1 != 0)] : __ldg(P.fvdxb + i1);
         double JR1, JL1;
-        jgdow(G, np, sSc, oojc, d, n, base, st, i1, wc1, addsurf, JR1, JL1);
+        jgdow(G, Gm, np, sSc, oojc, d, n, base, st, i1, wc1, addsurf, JR1, JL1);
         const double w0 = 1. / 0.75, w1 = 1. - w0;
         for (int l = 0; l < 4; l++) {
           const double fR1 = sF[(l * nm + i1) * nn + Pn], fL1 = -sF[(l * nm + i1 - 1) * nn + Pn];

@@ -96,6 +96,9 @@ typedef struct nmo_mesh {
   const double *hang_pos;   /* [c][2] */
   int surf_interp;          /* traces from FV neighbours: 0 piecewise linear,
                                1 piecewise parabolic (par fv_surface_interp) */
+  const double *dXdxm;      /* [e][3][9][np] dX^a/dx^i at the midpoint right of
+                               each node in each direction (par
+                               coordinates_midpoint_data = yes), or NULL */
 } nmo_mesh;
 
 /* points of both point types: LGL (DG) with their Lagrange weights, and
@@ -852,6 +855,28 @@ static double det_dXbdx(const nmo_mesh *m, int e, int ijk)
 
 /* RHS of one fin.-vol. element (scalarwave1_vol_rhs_u / _surf_rhs_u with
    use_fv: fv_divf, then the surface terms).  tmp holds 8*np doubles. */
+/* coordinates_midpoint_data = yes on a curvilinear element: sqrtgdiag_d,
+   det(dXb/dx) and the unit normal of direction d at the midpoint right of
+   node ijk (coordinates.c:337-420, utilities.c:48-80,90-103) */
+static void midpoint_factors(const nmo_mesh *m, int e, int d, int ijk, double *sgm,
+                             double *oojm, double nrm[3])
+{
+  int np = m->n * m->n * m->n, a, b, l;
+  const double *bb = m->bbox + 6 * e;
+  double d0 = 2. / (bb[1] - bb[0]), d1 = 2. / (bb[3] - bb[2]), d2 = 2. / (bb[5] - bb[4]);
+  double dXbdX[3] = {d0, d1, d2}, M[3][3], g = 0., smag;
+  for (a = 0; a < 3; a++)
+    for (b = 0; b < 3; b++) M[a][b] = m->dXdxm[(((size_t)e * 3 + d) * 9 + a * 3 + b) * np + ijk];
+  for (l = 0; l < 3; l++) g += M[d][l] * M[d][l];
+  *sgm = dXbdX[d] * sqrt(g);
+  *oojm = d0 * d1 * d2 * (M[0][0] * M[1][1] * M[2][2] - M[0][2] * M[1][1] * M[2][0] +
+                          M[0][1] * M[1][2] * M[2][0] + M[0][2] * M[1][0] * M[2][1] -
+                          M[0][0] * M[1][2] * M[2][1] - M[0][1] * M[1][0] * M[2][2]);
+  smag = 1. * sqrt(M[d][0] * M[d][0] + M[d][1] * M[d][1] + M[d][2] * M[d][2]);
+  if (smag == 0.0) smag = 1.;
+  for (l = 0; l < 3; l++) nrm[l] = M[d][l] / smag;
+}
+
 static void rhs_elem_fv(const nmo_mesh *m, const nmo_pts *P, double t,
                         const double *w, double *r, int e, double *tmp)
 {
@@ -897,16 +922,22 @@ static void rhs_elem_fv(const nmo_mesh *m, const nmo_pts *P, double t,
           const int cccL = base + (g0 ? i0 - 1 : i0) * st;
           const int cccR = base + (lN ? i0 : i0 - 1) * st;
           const double wc = dXb[i0];
-          double JR, JL;
+          const int mid = m->dXdxm && m->curvi[e];
+          double JR, JL, sgR = sgd[cccR], ojR = ooJ[cccR], sgL = sgd[cccL], ojL = ooJ[cccL];
+          if (mid) {   /* the midpoint arrays replace the grid ones (fv.c:126-137) */
+            double nn_[3];
+            if (lN) midpoint_factors(m, e, dir, cccR, &sgR, &ojR, nn_);
+            if (g0) midpoint_factors(m, e, dir, cccL, &sgL, &ojL, nn_);
+          }
           if (g0 && lN) {
-            JR = sgd[cccR] / (ooJ[cccR] * wc);
-            JL = sgd[cccL] / (ooJ[cccL] * wc);
+            JR = sgR / (ojR * wc);
+            JL = sgL / (ojL * wc);
           } else if (!g0 && lN) {
-            JR = sgd[cccR] / (ooJ[cccR] * wc);
+            JR = sgR / (ojR * wc);
             JL = sgd[ccc] / (ooJ[ccc] * wc);
           } else if (g0 && !lN) {
             JR = sgd[ccc] / (ooJ[ccc] * wc);
-            JL = sgd[cccL] / (ooJ[cccL] * wc);
+            JL = sgL / (ojL * wc);
           } else {
             JR = JL = sgd[ccc] / (ooJ[ccc] * wc);
           }
@@ -920,7 +951,12 @@ static void rhs_elem_fv(const nmo_mesh *m, const nmo_pts *P, double t,
           }
           if (lN) {
             double ui[5], ua[5], fi[5], fa[5], fn[5], norm[3];
-            node_normal(m, e, 2 * dir + 1, ccc, norm);
+            if (mid) {   /* DGINFO_MIDPTNORM: normal at the midpoint */
+              double s_, o_;
+              midpoint_factors(m, e, dir, ccc, &s_, &o_, norm);
+            } else {
+              node_normal(m, e, 2 * dir + 1, ccc, norm);
+            }
             for (l = 0; l < NF; l++) {
               ui[l] = rec_p(m->fv_rec, n, qc[l], i0, r3);
               ua[l] = rec_m(m->fv_rec, n, qc[l], i0, r3);

@@ -42,7 +42,7 @@ class _Mesh(ctypes.Structure):
                 ("fv_w3ratio", ctypes.c_double), ("mixface", ctypes.c_void_p),
                 ("numflux", ctypes.c_int), ("hang_off", ctypes.c_void_p),
                 ("hang_src", ctypes.c_void_p), ("hang_pos", ctypes.c_void_p),
-                ("surf_interp", ctypes.c_int)]
+                ("surf_interp", ctypes.c_int), ("dXdxm", ctypes.c_void_p)]
 
 # reconstruction modes (reference par fv_rec) and div(f) extrapolation
 # modes (par fv_divf_extrap) understood by the oracle
@@ -329,7 +329,7 @@ class OracleMesh:
     def __init__(self, bbox, curvi, dXdx, xyz, nbnode, n, bc=0,
                  k=(1.0, 1.0, 1.0), fv=None, fv_rec="WENOm5_2",
                  fv_extrap="dnfn_extrap1", fv_w3ratio=2.0, mixface=None, numflux="LLF",
-                 hang=None, fv_surface_interp="linear"):
+                 hang=None, fv_surface_interp="linear", dXdxm=None):
         """fv: per-element finite-volume flags (None: all DG); fv_rec and
         fv_extrap name the reference's fv_rec / fv_divf_extrap modes;
         mixface: faces between the two point types (see match_faces);
@@ -345,6 +345,7 @@ class OracleMesh:
         self.fv = None if fv is None else np.ascontiguousarray(fv, np.int32)
         self.mixface = None if mixface is None else np.ascontiguousarray(mixface, np.int32)
         self.hang = None if hang is None else tuple(np.ascontiguousarray(a) for a in hang)
+        self.dXdxm = None if dXdxm is None else np.ascontiguousarray(dXdxm, np.float64)
         self.s = _Mesh(self.nelem, self.n, self.bbox.ctypes.data,
                        self.curvi.ctypes.data, self.dXdx.ctypes.data,
                        self.xyz.ctypes.data, self.nbnode.ctypes.data, int(bc),
@@ -355,7 +356,8 @@ class OracleMesh:
                        1 if numflux == "upwind" else 0,
                        *((None,) * 3 if self.hang is None else
                          tuple(a.ctypes.data for a in self.hang)),
-                       {"linear": 0, "parabolic": 1}[fv_surface_interp])
+                       {"linear": 0, "parabolic": 1}[fv_surface_interp],
+                       None if self.dXdxm is None else self.dXdxm.ctypes.data)
 
     def rhs(self, w, t=0.0):
         w = np.ascontiguousarray(w, np.float64)

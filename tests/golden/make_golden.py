@@ -131,6 +131,20 @@ CASES = {
                                       dt=0.002, steps=3, eps=0.02, seed=49, method="sspRK3",
                                       fv=dict(rec="WENOmZ_2", extrap="dnfn_extrap1",
                                               patches="0 2 4", surf="parabolic")),
+    # coordinates_midpoint_data = yes: FV flux factors and normals at the
+    # midpoints (the reference's FV-DG test parfile sets it)
+    "fvcs7_l0_n7_w5dnfn_mid": dict(mesh="cs7", n=7, luni=0, k=(0.3, -0.2, 0.1),
+                                   dt=0.002, steps=2, eps=0.05, seed=50,
+                                   fv=dict(rec="WENOm5_2", extrap="dnfn_extrap1", mid=True)),
+    "fvcs7_l1_n6_w3no_mid": dict(mesh="cs7", n=6, luni=1, k=(0.25, 0.15, -0.3),
+                                 dt=0.002, steps=2, eps=0.05, seed=51,
+                                 fv=dict(rec="WENOm3_2", extrap="no", mid=True)),
+    "ssp3_mixcs7_l0_n7_wZparab_mid": dict(mesh="cs7", n=7, luni=0,
+                                          k=(0.8, -0.5, 0.33166247903554), dt=0.002, steps=3,
+                                          eps=0.02, seed=52, method="sspRK3",
+                                          fv=dict(rec="WENOmZ_2", extrap="dnfn_extrap1",
+                                                  patches="0 2 4", surf="parabolic",
+                                                  mid=True)),
     # non-conforming faces: the listed patches refined one level further
     # (amr_hrefine_p), face traces interpolated across the level jump
     "nc_cs7_l0_n5_h0": dict(mesh="cs7", n=5, luni=0, k=(0.3, -0.2, 0.1),
@@ -183,7 +197,8 @@ def parfile(case, prefix):
         lines += [f"amr_uniform_p = {pats}", f"amr_fv_p = {pats}",
                   f"fv_rec = {c['fv']['rec']}",
                   f"fv_divf_extrap = {c['fv']['extrap']}",
-                  f"fv_surface_interp = {c['fv'].get('surf', 'linear')}"]
+                  f"fv_surface_interp = {c['fv'].get('surf', 'linear')}",
+                  f"coordinates_midpoint_data = {'yes' if c['fv'].get('mid') else 'no'}"]
     return "\n".join(lines) + "\n"
 
 

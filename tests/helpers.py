@@ -28,6 +28,10 @@ UPW_CASES = ["upw_cs7_l1_n5", "upw_box_l1_n6", "upw_mixcs7_l0_n7_w5dnfn", "upw_f
 METHOD_CASES = ["ssp3_cs7_l1_n5", "eul_box_l1_n5", "ssp3_mixcs7_l1_n6_wZdnfn",
                 "ssp3_mixcs7_l0_n7_wZparab"]
 METHOD_NEAR_CASES = ["ssp3_mixcs7_l1_n6_wZdnfn", "ssp3_mixcs7_l0_n7_wZparab"]
+# coordinates_midpoint_data = yes (FV midpoint factors and normals from the
+# map at the midpoints); the mixed one is a few ulp off in the oracle
+MID_CASES = ["fvcs7_l0_n7_w5dnfn_mid", "fvcs7_l1_n6_w3no_mid", "ssp3_mixcs7_l0_n7_wZparab_mid"]
+MID_NEAR_CASES = ["ssp3_mixcs7_l0_n7_wZparab_mid"]
 # non-conforming faces: patches refined one level further (amr_hrefine_p)
 NC_CASES = ["nc_cs7_l0_n5_h0", "nc_cs7_l0_n4_h1", "nc_cs7_l1_n5_h02", "nc_upw_cs7_l0_n6_h35"]
 # the oracle's non-conforming (and even-n DG/FV interface) traces take the
@@ -81,7 +85,7 @@ def rel_l2(a, b):
 
 def oracle_for(mesh, bc=0, k=(1.0, 1.0, 1.0), period=None, fv_rec="WENOm3_2",
                fv_extrap="dnfn_extrap1", fv_w3ratio=2.0, numflux="LLF",
-               fv_surface_interp="linear"):
+               fv_surface_interp="linear", midpoint_data=False):
     """Oracle mesh built from the product mesh's geometry, with its own
     coordinate-matching neighbour table (and the mesh's finite-volume flags
     with the given fin.-vol. options)."""
@@ -103,7 +107,8 @@ def oracle_for(mesh, bc=0, k=(1.0, 1.0, 1.0), period=None, fv_rec="WENOm3_2",
     return nmo.OracleMesh(bbox, curvi, dXdx, xyz, nb, mesh.n, bc=bc, k=k,
                           fv=fv if fv.any() else None, fv_rec=fv_rec,
                           fv_extrap=fv_extrap, fv_w3ratio=fv_w3ratio, mixface=mix,
-                          numflux=numflux, hang=hang, fv_surface_interp=fv_surface_interp)
+                          numflux=numflux, hang=hang, fv_surface_interp=fv_surface_interp,
+                          dXdxm=mesh.midpoint_dXdx() if midpoint_data else None)
 
 
 def gaussian_pulses(xyz, seed, npulse=8, rmin=3.0, rmax=10.0, wmin=0.5, wmax=2.0,

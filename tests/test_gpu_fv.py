@@ -11,7 +11,7 @@ import numpy as np
 import pytest
 
 import nmesh_gb300 as ng
-from helpers import (FV_CASES, PI, RTOL_RHS, RTOL_RK4, build_mesh, gaussian_pulses,
+from helpers import (FV_CASES, MID_CASES, PI, RTOL_RHS, RTOL_RK4, build_mesh, gaussian_pulses,
                      load, oracle_for, perm_to_mesh, rel_l2, to_mesh_order)
 
 pytestmark = pytest.mark.gpu
@@ -171,3 +171,54 @@ def test_fv_rejections():
     ev2 = ng.Evolution(dg, ng.BC_OUTGOING)
     with pytest.raises(ng.NmgError):
         ev2.set_fv("WENOm5_2", "no")
+
+
+@pytest.mark.parametrize("variant", ["fvx", "fv"])
+@pytest.mark.parametrize("case", MID_CASES)
+def test_midpoint_data_matches_reference(case, variant):
+    """coordinates_midpoint_data = yes against the reference's own runs."""
+    d, meta = load(case)
+    m = build_mesh(meta)
+    perm = perm_to_mesh(m, d)
+    ev = ng.Evolution(m, ng.BC_EXACT_PLANEWAVE, k=meta["k"])
+    ev.set_fv(meta["fv"]["rec"], meta["fv"]["extrap"])
+    if m.fv().min() == 0:
+        ev.set_fv_surface_interp(meta["fv"].get("surf", "linear"))
+    ev.set_fv_midpoint_data(True)
+    ev.set_kernel(variant)
+    ev.set_evolve_method(meta.get("method", "RK4"))
+    u0 = to_mesh_order(d["u0"], perm)
+    assert rel_l2(ev.rhs(u0, 0.0)[perm], d["r0"]) <= RTOL_RHS
+    u = ev.evolve_steps_host(u0, 0.0, meta["dt"], meta["steps"])
+    assert rel_l2(u[perm], d["u_final"]) <= RTOL_RK4
+    # switching it off gives the grid-point factors again
+    ev.set_fv_midpoint_data(False)
+    plain = ng.Evolution(m, ng.BC_EXACT_PLANEWAVE, k=meta["k"])
+    plain.set_fv(meta["fv"]["rec"], meta["fv"]["extrap"])
+    if m.fv().min() == 0:
+        plain.set_fv_surface_interp(meta["fv"].get("surf", "linear"))
+    plain.set_kernel(variant)
+    assert np.array_equal(ev.rhs(u0, 0.0), plain.rhs(u0, 0.0))
+
+
+@pytest.mark.parametrize("extrap,min_rate", [("dnfn_extrap1", 1.8), ("no", 0.9)])
+def test_midpoint_data_constant_flux_converges(extrap, min_rate):
+    """With the midpoint map the FV divergence of a constant flux on the
+    curvilinear shells converges to zero (fv_tests, src/main/dg/fv_tests.c:
+    second order with dnfn_extrap1, first order at the faces with "no")."""
+    errs = []
+    for luni in (1, 2):
+        m = ng.Mesh.build(ng.MESH_CUBEDSPHERES7, n=7, luni=luni, cs_dc=1.0, cs_r0fac=4.0,
+                          fv=True)
+        u = np.zeros((m.nelem, 5, m.np))
+        u[:, 0], u[:, 1], u[:, 2], u[:, 3] = 0.3, -0.5, 0.8, 0.2
+        ev = ng.Evolution(m, ng.BC_OUTGOING)
+        ev.set_fv("WENOm5_2", extrap)
+        ev.set_fv_midpoint_data(True)
+        r = ev.rhs(u, 0.0)
+        nb, _ = m.faces()
+        pat, _ = m.elements()
+        inner = (nb >= 0).all(axis=1) & (pat > 0)
+        errs.append(np.abs(r[inner, :4]).max())
+    rate = np.log2(errs[0] / errs[1])
+    assert rate > min_rate, (errs, rate)

@@ -5,8 +5,10 @@ operation order and must match it bit for bit."""
 import numpy as np
 import pytest
 
-from helpers import (CASES, FV_CASES, METHOD_CASES, METHOD_NEAR_CASES, MIX_CASES,
-                     MIX_NEAR_CASES, NC_CASES, RTOL_NC_ORACLE, UPW_CASES, load, rel_l2)
+from helpers import (CASES, FV_CASES, METHOD_CASES, METHOD_NEAR_CASES, MID_CASES,
+                     MID_NEAR_CASES, MIX_CASES, MIX_NEAR_CASES, NC_CASES, RTOL_NC_ORACLE,
+                     UPW_CASES, build_mesh, load, oracle_for, perm_to_mesh, rel_l2,
+                     to_mesh_order)
 from oracle import nmo
 
 
@@ -66,6 +68,27 @@ def test_oracle_other_integrators_match_reference(case):
         assert rel_l2(u, d["u_final"]) <= RTOL_NC_ORACLE
     else:
         assert np.array_equal(u, d["u_final"])
+
+
+@pytest.mark.parametrize("case", MID_CASES)
+def test_oracle_midpoint_data_matches_reference(case):
+    """coordinates_midpoint_data = yes: the midpoint map values come from the
+    product's mesh packer (nmg_mesh_get_midpoint_dXdx), the factors and
+    normals from the oracle; bit for bit on all-FV meshes."""
+    d, meta = load(case)
+    m = build_mesh(meta)
+    perm = perm_to_mesh(m, d)
+    o = oracle_for(m, bc=0, k=meta["k"], fv_rec=meta["fv"]["rec"],
+                   fv_extrap=meta["fv"]["extrap"],
+                   fv_surface_interp=meta["fv"].get("surf", "linear"), midpoint_data=True)
+    u0 = to_mesh_order(d["u0"], perm)
+    r = o.rhs(u0)[perm]
+    u = o.evolve(u0, meta["dt"], meta["steps"], method=meta.get("method", "RK4"))[perm]
+    if case in MID_NEAR_CASES:
+        assert rel_l2(r, d["r0"]) <= RTOL_NC_ORACLE
+        assert rel_l2(u, d["u_final"]) <= RTOL_NC_ORACLE
+    else:
+        assert np.array_equal(r, d["r0"]) and np.array_equal(u, d["u_final"])
 
 
 @pytest.mark.parametrize("case", MIX_NEAR_CASES)
