@@ -145,6 +145,11 @@ int nmg_mesh_get_hanging(const nmg_mesh *m, int64_t *nface, int64_t *ncontrib, i
  * 283-375): block d at node (i,j,k) holds the value at the midpoint to the
  * right of that node in direction d (last plane unused); generated meshes */
 int nmg_mesh_get_midpoint_dXdx(const nmg_mesh *m, double *dXdxm);
+/* the reference's dt = auto (dtfac, default 0.25, and uniform_dtfac, default
+ * 0.125 on finite-volume elements, times the smallest corner spacing;
+ * src/main/amr/storage.c:1305-1385, src/main/coordinates/utilities.c:
+ * 972-1300) */
+int nmg_mesh_auto_dt(const nmg_mesh *m, double dtfac, double uniform_dtfac, double *dt);
 /* equally spaced points on [-1,1] (uniform_x, src/main/basis/Legendre.c:626) */
 int nmg_uniform_points(int32_t n, double *x);
 void nmg_mesh_free(nmg_mesh *m);

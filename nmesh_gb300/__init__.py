@@ -192,6 +192,7 @@ def lib(build_if_missing=True):
         "nmg_set_fv_surface_interp": (ctypes.c_int, [vp, i32]),
         "nmg_set_fv_midpoint_data": (ctypes.c_int, [vp, i32]),
         "nmg_mesh_get_midpoint_dXdx": (ctypes.c_int, [vp, vp]),
+        "nmg_mesh_auto_dt": (ctypes.c_int, [vp, f64, f64, vp]),
         "nmg_evolve_steps": (ctypes.c_int, [vp, f64, f64, i32]),
         "nmg_evolve_steps_host": (ctypes.c_int, [vp, f64, f64, i32, vp]),
         "nmg_checkpoint_write": (ctypes.c_int, [vp, vp, ctypes.c_char_p, vp]),
@@ -335,6 +336,13 @@ class Mesh:
         if lib().nmg_mesh_concat(arr, len(meshes), ctypes.byref(h)):
             raise NmgError(f"nmg_mesh_concat: {lib().nmg_mesh_last_error().decode()}")
         return cls(h.value)
+
+    def auto_dt(self, dtfac=0.25, uniform_dtfac=0.125):
+        """The reference's dt = auto for this mesh."""
+        v = ctypes.c_double()
+        if lib().nmg_mesh_auto_dt(self._h, float(dtfac), float(uniform_dtfac), ctypes.byref(v)):
+            raise NmgError(lib().nmg_mesh_last_error().decode())
+        return v.value
 
     def midpoint_dXdx(self):
         """dX^a/dx^i [E, 3, 9, np] at the midpoints right of each node in

@@ -24,6 +24,7 @@
 #include "../../include/nmg.h"
 
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -862,6 +863,79 @@ int nmg_mesh_get_hanging(const nmg_mesh *m, int64_t *nface, int64_t *ncontrib, i
   if (hoff) std::copy(m->hoff.begin(), m->hoff.end(), hoff);
   if (hsrc) std::copy(m->hsrc.begin(), m->hsrc.end(), hsrc);
   if (hpos) std::copy(m->hpos.begin(), m->hpos.end(), hpos);
+  return NMG_OK;
+}
+
+// dt = auto (update_elm_eid_dt -> adapt_node_dt_and_mesh_dt,
+// src/main/amr/storage.c:1305-1365, src/main/coordinates/utilities.c:
+// 972-1124,1225-1300): per element hmin = the smallest distance between a
+// corner point and its axis neighbours (starting from the bbox diagonal /
+// sqrt(3)), dt = dtfac hmin, or uniform_dtfac hmin when that pair lies along
+// a direction of equally spaced points; the mesh dt is the minimum.
+int nmg_mesh_auto_dt(const nmg_mesh *m, double dtfac, double uniform_dtfac, double *dt) {
+  if (!m || !dt) return fail(NMG_EINVAL, "nmg_mesh_auto_dt: null argument");
+  const int n = m->n, np = n * n * n;
+  double mdt = DBL_MAX * 0.1;
+  auto dist = [](const double a[3], const double b[3]) {
+    double d2 = 0.;
+    for (int d = 0; d < 3; d++) {
+      const double dx = b[d] - a[d];
+      d2 += dx * dx;
+    }
+    return sqrt(d2);
+  };
+  for (int64_t e = 0; e < m->nelem; e++) {
+    const double *X = &m->xyz[(size_t)e * 3 * np];
+    auto pt = [&](int i, int j, int k, double p[3]) {
+      const int ijk = i + n * (j + n * k);
+      for (int d = 0; d < 3; d++) p[d] = X[d * np + ijk];
+    };
+    // space diagonal of the bbox through the patch map (the corner points
+    // of an element without a known map)
+    const double *bb = &m->bbox[e * 6];
+    double c0[3], c1[3];
+    const Patch *pat = m->patches.empty() ? nullptr : &m->patches[m->pat[e]];
+    if (pat) {
+      const double X0[3] = {bb[0], bb[2], bb[4]}, X1[3] = {bb[1], bb[3], bb[5]};
+      double J[3][3];
+      if (pat->cubed) {
+        cubsph_x_dXdx(*pat, X0, c0, J);
+        cubsph_x_dXdx(*pat, X1, c1, J);
+      } else {
+        for (int d = 0; d < 3; d++) { c0[d] = X0[d]; c1[d] = X1[d]; }
+      }
+    } else {
+      pt(0, 0, 0, c0);
+      pt(n - 1, n - 1, n - 1, c1);
+    }
+    double hmin = dist(c0, c1) / sqrt(3.);
+    int best0 = -1, best1 = -1;
+    for (int c = 0; c < 8; c++) {
+      const int i = (c & 1) * (n - 1), j = ((c >> 1) & 1) * (n - 1), k = ((c >> 2) & 1) * (n - 1);
+      double p0[3];
+      pt(i, j, k, p0);
+      for (int kk = -1; kk <= 1; kk++)
+        for (int jj = -1; jj <= 1; jj++)
+          for (int ii = -1; ii <= 1; ii++) {
+            const int in = i + ii, jn = j + jj, kn = k + kk;
+            if (in < 0 || in >= n || jn < 0 || jn >= n || kn < 0 || kn >= n) continue;
+            if (in == i && jn == j && kn == k) continue;
+            if ((in != i) + (jn != j) + (kn != k) != 1) continue;
+            double p1[3];
+            pt(in, jn, kn, p1);
+            const double dd = dist(p0, p1);
+            if (dd < hmin) {
+              hmin = dd;
+              best0 = i + n * (j + n * k);
+              best1 = in + n * (jn + n * kn);
+            }
+          }
+    }
+    const bool uni = !m->fv.empty() && m->fv[e] && best0 >= 0 && best1 >= 0;
+    const double dtm = (uni ? uniform_dtfac : dtfac) * hmin;
+    if (dtm < mdt) mdt = dtm;
+  }
+  *dt = mdt;
   return NMG_OK;
 }
 

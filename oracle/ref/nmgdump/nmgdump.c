@@ -199,6 +199,14 @@ int nmgdump_rhs(tMesh *mesh)
     vlcopy(NULL, ListEntry(evosys->w, i), ListEntry(evosys->u, i));
   evolve_setrhs_mesh(mesh, evosys->rhs, evosys->w);
   nmgdump_write(mesh, "rhs", 1);
+  {
+    /* the time step of the run (dt = auto: the reference's dtfac * hmin) */
+    char fn[1000];
+    FILE *fp;
+    snprintf(fn, sizeof fn, "%s_dt.bin", Gets(Par("nmgdump_prefix")));
+    fp = fopen(fn, "wb");
+    if(fp) { fwrite(&mesh->dt, sizeof(double), 1, fp); fclose(fp); }
+  }
   if(Getb(Par("nmgdump_persson"))) nmgdump_persson(mesh);
   if(Getb(Par("nmgdump_norms"))) nmgdump_norms(mesh);
   return 0;

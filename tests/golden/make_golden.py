@@ -145,6 +145,14 @@ CASES = {
                                           fv=dict(rec="WENOmZ_2", extrap="dnfn_extrap1",
                                                   patches="0 2 4", surf="parabolic",
                                                   mid=True)),
+    # dt = auto: the reference's dtfac * hmin (uniform_dtfac on FV elements)
+    "dtauto_cs7_l1_n5": dict(mesh="cs7", n=5, luni=1, k=(0.3, -0.2, 0.1),
+                             dt="auto", steps=1, eps=0.02, seed=53),
+    "dtauto_box_l2_n6": dict(mesh="box", n=6, luni=2, k=(1.0, -0.5, 0.25),
+                             dt="auto", steps=1, eps=0.02, seed=54),
+    "dtauto_mixcs7_l0_n7": dict(mesh="cs7", n=7, luni=0, k=(0.3, -0.2, 0.1),
+                                dt="auto", steps=1, eps=0.02, seed=55,
+                                fv=dict(rec="WENOm5_2", extrap="dnfn_extrap1", patches="2")),
     # non-conforming faces: the listed patches refined one level further
     # (amr_hrefine_p), face traces interpolated across the level jump
     "nc_cs7_l0_n5_h0": dict(mesh="cs7", n=5, luni=0, k=(0.3, -0.2, 0.1),
@@ -164,7 +172,7 @@ def parfile(case, prefix):
     lines = [
         "physics = scalarwave1 nmgdump",
         f"evolve_method = {c.get('method', 'RK4')}",
-        f"dt = {c['dt']!r}",
+        f"dt = {c['dt'] if c['dt'] == 'auto' else repr(c['dt'])}",
         f"iterations = {c['steps']}",
         f"amr_luni = {c['luni']}",
         f"amr_n0 = {c['n']}", f"amr_n1 = {c['n']}", f"amr_n2 = {c['n']}",
@@ -220,6 +228,7 @@ def run_case(case, exe, outdir):
             raw = np.fromfile(prefix + "_persson.bin", dtype="<i4", count=1)
             pers = np.fromfile(prefix + "_persson.bin", dtype="<f8", offset=4)
             pers = pers.reshape(int(raw[0]), 5)
+        dt_ref = np.fromfile(prefix + "_dt.bin", dtype="<f8")
         norms = None
         if CASES[case].get("norms"):
             norms = np.fromfile(prefix + "_norms.bin", dtype="<f8")
@@ -236,6 +245,8 @@ def run_case(case, exe, outdir):
         extra["persson"] = pers
     if norms is not None:      # Vol, then per field VolInt, Int v^2, min, max
         extra["norms"] = norms
+    if c["dt"] == "auto":      # the reference's automatic dt of the run
+        extra["dt_ref"] = dt_ref
     np.savez_compressed(
         os.path.join(outdir, case + ".npz"),
         meta=json.dumps(meta), pat=d0["pat"], n=d0["n"], bbox=d0["bbox"],

@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 import nmesh_gb300 as ng
-from helpers import (CASES, PI, RTOL_RHS, RTOL_RK4, build_mesh, gaussian_pulses,
+from helpers import (CASES, DTAUTO_CASES, PI, RTOL_RHS, RTOL_RK4, build_mesh, gaussian_pulses,
                      load, oracle_for, perm_to_mesh, rel_l2, to_mesh_order)
 
 pytestmark = pytest.mark.gpu
@@ -188,3 +188,17 @@ def test_periodic_cube_plane_wave_workload():
     o = oracle_for(m, bc=1, period=2 * PI)
     assert rel_l2(u, o.rk4(u0, dt, 10)) <= RTOL_RK4
     assert rel_l2(u, exact(10 * dt)) <= 1e-3
+
+
+@pytest.mark.parametrize("case", DTAUTO_CASES)
+def test_step_with_auto_dt_matches_reference(case):
+    """A step of the reference's run with dt = auto, taken with the mesh's
+    own automatic dt."""
+    d, meta = load(case)
+    m = build_mesh(meta)
+    perm = perm_to_mesh(m, d)
+    ev = ng.Evolution(m, ng.BC_EXACT_PLANEWAVE, k=meta["k"])
+    if "fv" in meta:
+        ev.set_fv(meta["fv"]["rec"], meta["fv"]["extrap"])
+    u = ev.rk4_steps_host(to_mesh_order(d["u0"], perm), 0.0, m.auto_dt(), meta["steps"])
+    assert rel_l2(u[perm], d["u_final"]) <= RTOL_RK4

@@ -5,7 +5,8 @@ import numpy as np
 import pytest
 
 import nmesh_gb300 as ng
-from helpers import CASES, FV_CASES, MIX_CASES, NC_CASES, PI, build_mesh, load, perm_to_mesh
+from helpers import (CASES, DTAUTO_CASES, FV_CASES, MIX_CASES, NC_CASES, PI, build_mesh, load,
+                     perm_to_mesh)
 from oracle import nmo
 
 
@@ -160,6 +161,14 @@ def test_nonconforming_concat_keeps_lists():
     assert np.array_equal(hc[2][len(ha[2]):, 0], hb[2][:, 0] + a.nelem)
     assert np.array_equal(hc[3], np.concatenate([ha[3], hb[3]]))
     assert np.array_equal(np.diff(hc[1]), np.concatenate([np.diff(ha[1]), np.diff(hb[1])]))
+
+
+@pytest.mark.parametrize("case", DTAUTO_CASES)
+def test_auto_dt_equals_the_references(case):
+    """dt = auto: the smallest corner spacing times dtfac (uniform_dtfac
+    where that spacing lies on equally spaced points), bit for bit."""
+    d, meta = load(case)
+    assert build_mesh(meta).auto_dt() == d["dt_ref"][0]
 
 
 def test_mesh_errors():
