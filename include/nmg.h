@@ -320,6 +320,17 @@ int nmg_set_fv_surface_interp(nmg_ctx *c, int32_t mode);
  * the midpoint fluxes come from the map at the midpoints (fv.c:384-411,
  * coordinates.c:283-437) instead of the grid points; generated meshes */
 int nmg_set_fv_midpoint_data(nmg_ctx *c, int32_t on);
+/* the reference's evolve_filter_all = yes: after every step each field of
+ * every element is filtered, u -> J^-p F(J^p u) with the exponential modal
+ * filter c_ijk -> c_ijk f_i f_j f_k, f_k = exp(-alp (k/(n-1-dn))^s)
+ * (expfilter_var, src/main/basis/filter.c:15-96; pars evolve_filter_alp,
+ * _s, _dn, basis_expfilter_JacobianPower = p (0 or 1), basis_filter_fv;
+ * evolve_filter_evosys_mesh, src/main/evolve/evolve.c:656-700).  on = 0
+ * switches it off.  Applied by the step entry points (nmg_rk4_step(s),
+ * nmg_evolve_steps, the host round trips, nmg_rk4_step_trouble); not by
+ * the adjoint, the batches and the allocation-free step. */
+int nmg_set_filter(nmg_ctx *c, int32_t on, double alp, double s, int32_t dn, int32_t jpower,
+                   int32_t filter_fv);
 
 /* r = RHS(w, t) with w, r device pointers of nmg_state_size() doubles.
  * Replaces evolve_setrhs_mesh (src/main/evolve/evolve.c:182-232) for the

@@ -191,6 +191,7 @@ def lib(build_if_missing=True):
         "nmg_set_evolve_method": (ctypes.c_int, [vp, i32]),
         "nmg_set_fv_surface_interp": (ctypes.c_int, [vp, i32]),
         "nmg_set_fv_midpoint_data": (ctypes.c_int, [vp, i32]),
+        "nmg_set_filter": (ctypes.c_int, [vp, i32, f64, f64, i32, i32, i32]),
         "nmg_mesh_get_midpoint_dXdx": (ctypes.c_int, [vp, vp]),
         "nmg_mesh_auto_dt": (ctypes.c_int, [vp, f64, f64, vp]),
         "nmg_evolve_steps": (ctypes.c_int, [vp, f64, f64, i32]),
@@ -526,6 +527,12 @@ class Evolution:
         self._check(lib().nmg_set_fv_surface_interp(self._h, {"linear": 0,
                                                               "parabolic": 1}[mode]),
                     "nmg_set_fv_surface_interp")
+
+    def set_filter(self, on=True, alp=36.0, s=32.0, dn=0, jpower=1, filter_fv=True):
+        """The reference's evolve_filter_all = yes (exponential modal filter
+        after every step; defaults as the reference's parameters)."""
+        self._check(lib().nmg_set_filter(self._h, int(bool(on)), float(alp), float(s), int(dn),
+                                         int(jpower), int(bool(filter_fv))), "nmg_set_filter")
 
     def set_fv_midpoint_data(self, on=True):
         """The reference's coordinates_midpoint_data = yes: FV midpoint flux

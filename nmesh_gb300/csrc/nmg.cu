@@ -248,6 +248,11 @@ struct nmg_ctx {
   int fv_surf = NMG_FV_SURF_LINEAR;   // traces from FV neighbours (fv_surface_interp)
   // coordinates_midpoint_data = yes: midpoint factors of curvilinear elements
   bool fv_mid = false;
+  // exponential filter after each step (evolve_filter_all = yes)
+  bool filter_on = false;
+  int filter_jpow = 1, filter_fv = 1;
+  double *d_filt = nullptr;   // [2][nn] F of LGL and of equally spaced points
+  double *d_fooj = nullptr;   // [cslot][np] det(dXb/dx) on the LGL points
   double *d_fvmid = nullptr;          // [cslot][3][5][np]
   nmg_mesh geom;                      // element bboxes, patches and point sets
   std::vector<int> h_cslot;
@@ -283,6 +288,9 @@ static int set_err(nmg_ctx *c, int code, const std::string &msg) {
 }
 
 static StageParams base_params(nmg_ctx *c);
+extern "C" {
+static int rk4_step_plain(nmg_ctx *c, double t, double dt);
+}
 
 size_t nmg_ctx_state_len(const nmg_ctx *c) { return c->state_len; }
 
@@ -487,6 +495,16 @@ static int autotune(nmg_ctx *c) {
   return NMG_OK;
 }
 
+// the exponential filter of the state in buf (after a step)
+static cudaError_t apply_filter(nmg_ctx *c, double *buf) {
+  if (!c->filter_on) return cudaSuccess;
+  cudaError_t e = nmgk::filter_launch(c->n, (int)c->nelem, buf, c->mixed ? c->d_isfv : nullptr,
+                                      c->d_filt, c->d_cslot, c->d_fooj, c->d_fvgeo,
+                                      c->d_scale, c->filter_jpow, c->filter_fv, c->stream);
+  if (e == cudaSuccess) c->launches++;
+  return e;
+}
+
 static int launch_stage(nmg_ctx *c, const StageParams &P) {
   int rc = autotune(c);
   if (rc) return rc;
@@ -686,6 +704,20 @@ static double pw_parab_basis(int k, double x, int np, const double *xp)
   if (x >= xmr && x < xmrr)
     return (x - xp[m + 1]) * (x - xp[m + 2]) / ((xp[m] - xp[m + 1]) * (xp[m] - xp[m + 2]));
   return 0.;
+}
+
+// Legendre polynomial P_i(x) by the recurrence of LegendreP
+// (src/main/basis/Legendre.c:14-38)
+static double legendre_p(int i, double x) {
+  double Pk = 0., P0 = 1., P1 = x;
+  if (i == 0) return P0;
+  if (i == 1) return P1;
+  for (int kk = 2; kk <= i; kk++) {
+    Pk = (x * (2 * kk - 1) * P1 - (kk - 1) * P0) / kk;
+    P0 = P1;
+    P1 = Pk;
+  }
+  return Pk;
 }
 
 static void drop_graphs(nmg_ctx *c) {
@@ -1415,6 +1447,7 @@ static int rk4_step_substep(nmg_ctx *c, double t, double dt, const nmg_trouble_p
     switched[0] = nfv;
     switched[1] = ndg;
   }
+  CK(apply_filter(c, c->d_buf[c->cur]));  // evolve_filter_evosys_mesh after the step
   CK(cudaStreamSynchronize(c->stream));
   return NMG_OK;
 }
@@ -1439,7 +1472,7 @@ int nmg_rk4_step_trouble(nmg_ctx *c, double t, double dt, const nmg_trouble_para
   const int64_t E = c->nelem;
   const size_t bytes = c->state_len * sizeof(double);
   CK(cudaMemcpyAsync(c->d_up, c->d_buf[c->cur], bytes, cudaMemcpyDeviceToDevice, c->stream));
-  if ((rc = nmg_rk4_step(c, t, dt))) return rc;
+  if ((rc = rk4_step_plain(c, t, dt))) return rc;
   std::vector<int32_t> fl;
   if ((rc = trouble_flags(c, c->d_buf[c->cur], c->d_up, tp, &fl))) return rc;
   const int global = score_update(c, fl);
@@ -1451,7 +1484,7 @@ int nmg_rk4_step_trouble(nmg_ctx *c, double t, double dt, const nmg_trouble_para
     for (int64_t e = 0; e < E; e++)
       if (c->h_score[e] > 0) types[e] = 1;
     if ((rc = switch_types(c, types.data(), &nfv, nullptr))) return rc;
-    if ((rc = nmg_rk4_step(c, t, dt))) return rc;
+    if ((rc = rk4_step_plain(c, t, dt))) return rc;
   }
   if (global > 0 || global <= -tp->notroubles) {
     std::vector<int32_t> types(c->h_fv);
@@ -1463,6 +1496,7 @@ int nmg_rk4_step_trouble(nmg_ctx *c, double t, double dt, const nmg_trouble_para
     switched[0] = nfv;
     switched[1] = ndg;
   }
+  CK(apply_filter(c, c->d_buf[c->cur]));  // evolve_filter_evosys_mesh after the step
   CK(cudaStreamSynchronize(c->stream));
   return NMG_OK;
 }
@@ -1526,6 +1560,106 @@ int nmg_set_fv_surface_interp(nmg_ctx *c, int32_t mode) {
   CK(cudaStreamSynchronize(c->stream));
   CK(cudaMemcpy(c->d_gM + nn, M1.data(), sizeof(double) * nn, cudaMemcpyHostToDevice));
   c->fv_surf = mode;
+  return NMG_OK;
+}
+
+int nmg_set_filter(nmg_ctx *c, int32_t on, double alp, double s, int32_t dn, int32_t jpower,
+                   int32_t filter_fv) {
+  if (!c) return NMG_EINVAL;
+  if (jpower != 0 && jpower != 1)
+    return set_err(c, NMG_EINVAL, "nmg_set_filter: jpower must be 0 or 1");
+  drop_graphs(c);
+  if (!on) {
+    c->filter_on = false;
+    return NMG_OK;
+  }
+  const int n = c->n, np = c->np, nn = c->nn;
+  // F = S diag(f) A per point type: S_ij = P_j(x_i)/sqrt(c_j) with
+  // 1/c_j = (2j+1)/2 (j/2 for j = N); A = w_j S_ji on LGL points
+  // (LGL_AT_ST_matrices) and A = S^-1 on equally spaced points
+  // (Legendre_AT_ST_matrices, src/main/basis/Legendre.c:277-310,723-729);
+  // f_k = exp(-alp (k/N')^s), N' = n - 1 - dn (1 if <= 0) (filter.c:19-56)
+  double Nf = n - 1 - dn;
+  if (Nf <= 0.) Nf = 1.;
+  std::vector<double> F(2 * (size_t)nn), f(n);
+  for (int k = 0; k < n; k++) f[k] = exp(-alp * pow(k / Nf, s));
+  for (int typ = 0; typ < 2; typ++) {
+    const double *x = typ == 0 ? c->h_xl.data() : c->h_xu.data();
+    std::vector<long double> S(nn), A(nn);
+    for (int i = 0; i < n; i++)
+      for (int j = 0; j < n; j++) {
+        double ooc = 0.5 * (2 * j + 1);
+        if (j == n - 1 && n - 1 != 0) ooc = 0.5 * j;
+        S[i * n + j] = legendre_p(j, x[i]) * sqrt(ooc);
+      }
+    if (typ == 0) {
+      std::vector<double> w(n), D((size_t)nn), xx(n);
+      nmg::lgl_basis(n, xx.data(), w.data(), D.data());
+      for (int i = 0; i < n; i++)
+        for (int j = 0; j < n; j++) A[i * n + j] = w[j] * (double)S[j * n + i];
+    } else {
+      std::vector<long double> M(S), I(nn, 0.L);
+      for (int i = 0; i < n; i++) I[i * n + i] = 1.L;
+      for (int col = 0; col < n; col++) {
+        int piv = col;
+        for (int r = col + 1; r < n; r++)
+          if (fabsl(M[r * n + col]) > fabsl(M[piv * n + col])) piv = r;
+        for (int q = 0; q < n; q++) {
+          std::swap(M[col * n + q], M[piv * n + q]);
+          std::swap(I[col * n + q], I[piv * n + q]);
+        }
+        const long double d = M[col * n + col];
+        for (int q = 0; q < n; q++) {
+          M[col * n + q] /= d;
+          I[col * n + q] /= d;
+        }
+        for (int r = 0; r < n; r++)
+          if (r != col) {
+            const long double fac = M[r * n + col];
+            for (int q = 0; q < n; q++) {
+              M[r * n + q] -= fac * M[col * n + q];
+              I[r * n + q] -= fac * I[col * n + q];
+            }
+          }
+      }
+      A = I;
+    }
+    for (int p = 0; p < n; p++)
+      for (int q = 0; q < n; q++) {
+        long double sum = 0.L;
+        for (int k = 0; k < n; k++) sum += S[p * n + k] * (long double)f[k] * A[k * n + q];
+        F[typ * nn + p * n + q] = (double)sum;
+      }
+  }
+  if (!c->d_filt) CK(cudaMalloc((void **)&c->d_filt, sizeof(double) * 2 * nn));
+  CK(cudaMemcpy(c->d_filt, F.data(), sizeof(double) * 2 * nn, cudaMemcpyHostToDevice));
+  if (jpower && !c->d_fooj && c->ncurvi > 0) {
+    // det(dXb/dx) on the LGL points of the curvilinear elements
+    std::vector<double> J((size_t)c->ncurvi * np), xyz(3 * (size_t)np), dX(9 * (size_t)np);
+    for (int64_t e = 0; e < c->nelem; e++) {
+      const int cs = c->h_cslot[e];
+      if (cs < 0) continue;
+      if (!nmg::element_geometry(c->geom, e, false, xyz.data(), dX.data()))
+        return set_err(c, NMG_EUNSUP, "nmg_set_filter: needs the maps of a generated mesh");
+      const double *bb = &c->geom.bbox[e * 6];
+      const double d0 = 2. / (bb[1] - bb[0]), d1 = 2. / (bb[3] - bb[2]), d2 = 2. / (bb[5] - bb[4]);
+      for (int q = 0; q < np; q++) {
+        double M[3][3];
+        for (int a = 0; a < 3; a++)
+          for (int b = 0; b < 3; b++) M[a][b] = dX[(a * 3 + b) * np + q];
+        const double det = M[0][0] * M[1][1] * M[2][2] - M[0][2] * M[1][1] * M[2][0] +
+                           M[0][1] * M[1][2] * M[2][0] + M[0][2] * M[1][0] * M[2][1] -
+                           M[0][0] * M[1][2] * M[2][1] - M[0][1] * M[1][0] * M[2][2];
+        J[(size_t)cs * np + q] = d0 * d1 * d2 * det;
+      }
+    }
+    CK(cudaMalloc((void **)&c->d_fooj, sizeof(double) * J.size()));
+    CK(cudaMemcpy(c->d_fooj, J.data(), sizeof(double) * J.size(), cudaMemcpyHostToDevice));
+  }
+  CK(nmgk::filter_prepare(n));
+  c->filter_jpow = jpower;
+  c->filter_fv = filter_fv ? 1 : 0;
+  c->filter_on = true;
   return NMG_OK;
 }
 
@@ -1601,6 +1735,7 @@ void nmg_destroy(nmg_ctx *c) {
   cudaFree(c->d_fvgeo); cudaFree(c->d_fvdist); cudaFree(c->d_fvdxb);
   cudaFree(c->d_fvlist); cudaFree(c->d_gtab); cudaFree(c->d_isfv); cudaFree(c->d_ghost);
   cudaFree(c->d_hoff); cudaFree(c->d_hsrc); cudaFree(c->d_hw); cudaFree(c->d_fvmid);
+  cudaFree(c->d_filt); cudaFree(c->d_fooj);
   cudaFree(c->d_gM); cudaFree(c->d_fvbxyz); cudaFree(c->d_fvbnrm); cudaFree(c->d_PR);
   cudaFree(c->d_conv); cudaFree(c->d_mm); cudaFree(c->d_trb); cudaFree(c->d_score);
   cudaFree(c->d_r); cudaFree(c->d_w2); cudaFree(c->d_ghost2); cudaFree(c->d_tlist);
@@ -1725,11 +1860,20 @@ int nmg_rhs_host(nmg_ctx *c, double t, const double *w_host, double *r_host) {
   return NMG_OK;
 }
 
-int nmg_rk4_step(nmg_ctx *c, double t, double dt) {
-  if (!c) return NMG_EINVAL;
+// one RK4 step of the resident state without the filter
+static int rk4_step_plain(nmg_ctx *c, double t, double dt) {
   int rc = enqueue_step(c, c->cur, t, dt, false);
   if (rc) return rc;
   c->cur = 1 - c->cur;
+  CK(cudaStreamSynchronize(c->stream));
+  return NMG_OK;
+}
+
+int nmg_rk4_step(nmg_ctx *c, double t, double dt) {
+  if (!c) return NMG_EINVAL;
+  int rc = rk4_step_plain(c, t, dt);
+  if (rc) return rc;
+  CK(apply_filter(c, c->d_buf[c->cur]));
   CK(cudaStreamSynchronize(c->stream));
   return NMG_OK;
 }
@@ -1742,6 +1886,7 @@ static int capture_step_graph(nmg_ctx *c, int cur, double dt, int method) {
   CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
   int64_t l0 = c->launches;
   rc = enqueue_step(c, cur, 0., dt, true, method);
+  if (!rc && apply_filter(c, c->d_buf[1 - cur]) != cudaSuccess) rc = NMG_ECUDA;
   advance_step_kernel<<<1, 1, 0, c->stream>>>(c->d_step);
   cudaError_t e1 = cudaGetLastError();
   cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
@@ -1942,10 +2087,10 @@ int nmg_rk4_steps_host(nmg_ctx *c, double t, double dt, int32_t nsteps, double *
   if (nsteps < 0) return set_err(c, NMG_EINVAL, "nmg_rk4_steps_host: bad argument");
   const size_t bytes = c->state_len * sizeof(double);
   int rc;
-  if (!c->fv && !c->nhang && nsteps == 1)  // copy in, step and copy out overlapped
+  if (!c->fv && !c->nhang && !c->filter_on && nsteps == 1)  // copy in, step, copy out overlapped
     return last_step_streamed(c, t, dt, host_u, host_u);
   CK(cudaMemcpyAsync(c->d_buf[c->cur], host_u, bytes, cudaMemcpyHostToDevice, c->stream));
-  if (c->mixed || nsteps == 0) {
+  if (c->mixed || c->filter_on || nsteps == 0) {
     rc = nmg_rk4_steps(c, t, dt, nsteps);
     if (rc) return rc;
     CK(cudaMemcpyAsync(host_u, c->d_buf[c->cur], bytes, cudaMemcpyDeviceToHost, c->stream));

@@ -711,6 +711,40 @@ __global__ void __launch_bounds__(256) convert_kernel(int n, const int *list, co
   }
 }
 
+// Exponential filter of every field of every element (expfilter_var,
+// src/main/basis/filter.c:15-96): u -> u J^p, (F x F x F) u with
+// F = S diag(exp(-alp (k/N)^s)) A in the element's point type, u -> u J^-p
+// (1/J = det(dXb/dx) per node: oojdg on curvilinear DG elements, the FV
+// geometry on FV ones, constant on Cartesian ones).
+__global__ void __launch_bounds__(256) filter_kernel(int n, double *u, const unsigned char *isfv,
+                                                    const double *F, const int *cslot,
+                                                    const double *oojdg, const double *fvgeo,
+                                                    const double *scale, int jpow,
+                                                    int filter_fv) {
+  extern __shared__ double sm[];
+  const int np = n * n * n, nn = n * n;
+  double *a = sm, *b = sm + np, *sM = sm + 2 * np, *sJ = sm + 2 * np + nn;
+  const int e = blockIdx.x;
+  const bool efv = isfv && isfv[e];
+  if (efv && !filter_fv) return;
+  for (int q = threadIdx.x; q < nn; q += blockDim.x) sM[q] = F[(efv ? nn : 0) + q];
+  const int cs = __ldg(cslot + e);
+  const double ojc = __ldg(scale + 3 * e) * __ldg(scale + 3 * e + 1) * __ldg(scale + 3 * e + 2);
+  for (int q = threadIdx.x; q < np; q += blockDim.x)
+    sJ[q] = cs < 0 ? ojc : efv ? __ldg(fvgeo + (size_t)cs * 13 * np + q)
+                               : __ldg(oojdg + (size_t)cs * np + q);
+  for (int l = 0; l < NF; l++) {
+    double *v = u + ((size_t)e * NF + l) * np;
+    __syncthreads();
+    for (int q = threadIdx.x; q < np; q += blockDim.x) a[q] = jpow ? v[q] / sJ[q] : v[q];
+    __syncthreads();
+    apply_dir(n, sM, 0, a, b);
+    apply_dir(n, sM, 1, b, a);
+    apply_dir(n, sM, 2, a, b);
+    for (int q = threadIdx.x; q < np; q += blockDim.x) v[q] = jpow ? b[q] * sJ[q] : b[q];
+  }
+}
+
 // min and max of each field over each element (limdata_MRS)
 __global__ void __launch_bounds__(256) minmax_kernel(int n, int nelem, const double *u,
                                                     double *mm) {
@@ -820,6 +854,22 @@ __global__ void __launch_bounds__(256) trouble_kernel(int n, int nelem, const do
   if (threadIdx.x == 0) flag[e] = efv ? (bad ? 0 : -1) : (bad ? 1 : 0);
 }
 }  // namespace
+
+size_t filter_smem(int n) { return sizeof(double) * (3 * (size_t)n * n * n + (size_t)n * n); }
+
+cudaError_t filter_prepare(int n) {
+  return cudaFuncSetAttribute(filter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)filter_smem(n));
+}
+
+cudaError_t filter_launch(int n, int nelem, double *u, const unsigned char *isfv, const double *F,
+                          const int *cslot, const double *oojdg, const double *fvgeo,
+                          const double *scale, int jpow, int filter_fv, cudaStream_t st) {
+  if (nelem <= 0) return cudaSuccess;
+  filter_kernel<<<nelem, 256, filter_smem(n), st>>>(n, u, isfv, F, cslot, oojdg, fvgeo, scale,
+                                                    jpow, filter_fv);
+  return cudaGetLastError();
+}
 
 cudaError_t convert_launch(int n, const int *list, int count, const double *M, double *u,
                            cudaStream_t st) {

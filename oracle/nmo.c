@@ -1269,6 +1269,100 @@ int nmo_evolve(const nmo_mesh *m, int method, double t, double dt, int nsteps, d
   return rc;
 }
 
+/* u of one 1D direction d of an element array: out = M in along d */
+static void mm_dir(int n, const double *M, int d, const double *in, double *out)
+{
+  int np = n * n * n, st = d == 0 ? 1 : d == 1 ? n : n * n, q, j;
+  for (q = 0; q < np; q++) {
+    int i = d == 0 ? q % n : d == 1 ? (q / n) % n : q / (n * n);
+    const double *line = in + q - i * st;
+    double s = 0.;
+    for (j = 0; j < n; j++) s += M[i * n + j] * line[j * st];
+    out[q] = s;
+  }
+}
+
+/* Exponential filter of every field of every element after a step
+   (evolve_filter_evosys_mesh -> expfilter_var, src/main/basis/filter.c:
+   15-96, src/main/evolve/evolve.c:656-700): u -> u / (1/J) (jpow = 1),
+   coefficients c = A^3 u, c_ijk *= f_i f_j f_k with f_k = exp(-alp
+   (k/(n-1-dn))^s), u = S^3 c, u -> u (1/J); A, S the normalised-Legendre
+   analysis and synthesis matrices of the element's points (LGL: A_ij =
+   w_j S_ji; equally spaced: A = S^-1, Legendre.c:277-310,723-729). */
+int nmo_filter(const nmo_mesh *m, double *u, double alp, double s, int dn, int jpow,
+               int filter_fv)
+{
+  int n = m->n, np = n * n * n, nn = n * n, e, l, i, j, k, q, typ;
+  double S[2][4096], A[2][4096], f[64], Nf = n - 1 - dn, x[64], w[64];
+  double *a = (double *)malloc(sizeof(double) * np), *b = (double *)malloc(sizeof(double) * np);
+  double *ooJ = (double *)malloc(sizeof(double) * np);
+  if (!a || !b || !ooJ) return 2;
+  if (Nf <= 0.) Nf = 1.;
+  for (k = 0; k < n; k++) f[k] = exp(-alp * pow(k / Nf, s));
+  for (typ = 0; typ < 2; typ++) {
+    if (typ == 0) nmo_lgl(n, x, w);
+    else nmo_uniform(n, x);
+    for (i = 0; i < n; i++)
+      for (j = 0; j < n; j++) {
+        double ooc = 0.5 * (2 * j + 1);
+        if (j == n - 1 && n - 1 != 0) ooc = 0.5 * j;
+        S[typ][i * n + j] = legendre_p(j, x[i]) * sqrt(ooc);
+      }
+    if (typ == 0) {
+      for (i = 0; i < n; i++)
+        for (j = 0; j < n; j++) A[0][i * n + j] = w[j] * S[0][j * n + i];
+    } else {   /* Gauss-Jordan inverse with partial pivoting */
+      double M[4096], I[4096];
+      int col, r;
+      for (q = 0; q < nn; q++) { M[q] = S[1][q]; I[q] = 0.; }
+      for (i = 0; i < n; i++) I[i * n + i] = 1.;
+      for (col = 0; col < n; col++) {
+        int piv = col;
+        double dd;
+        for (r = col + 1; r < n; r++)
+          if (fabs(M[r * n + col]) > fabs(M[piv * n + col])) piv = r;
+        for (q = 0; q < n; q++) {
+          double t1 = M[col * n + q], t2 = I[col * n + q];
+          M[col * n + q] = M[piv * n + q]; M[piv * n + q] = t1;
+          I[col * n + q] = I[piv * n + q]; I[piv * n + q] = t2;
+        }
+        dd = M[col * n + col];
+        for (q = 0; q < n; q++) { M[col * n + q] /= dd; I[col * n + q] /= dd; }
+        for (r = 0; r < n; r++)
+          if (r != col) {
+            double fac = M[r * n + col];
+            for (q = 0; q < n; q++) {
+              M[r * n + q] -= fac * M[col * n + q];
+              I[r * n + q] -= fac * I[col * n + q];
+            }
+          }
+      }
+      for (q = 0; q < nn; q++) A[1][q] = I[q];
+    }
+  }
+  for (e = 0; e < m->nelem; e++) {
+    int efv = m->fv && m->fv[e];
+    if (efv && !filter_fv) continue;
+    for (q = 0; q < np; q++) ooJ[q] = det_dXbdx(m, e, q);
+    for (l = 0; l < NF; l++) {
+      double *v = u + ((size_t)e * NF + l) * np;
+      for (q = 0; q < np; q++) a[q] = jpow ? v[q] / ooJ[q] : v[q];
+      mm_dir(n, A[efv], 0, a, b);
+      mm_dir(n, A[efv], 1, b, a);
+      mm_dir(n, A[efv], 2, a, b);
+      for (k = 0; k < n; k++)
+        for (j = 0; j < n; j++)
+          for (i = 0; i < n; i++) b[i + n * (j + n * k)] *= f[i] * f[j] * f[k];
+      mm_dir(n, S[efv], 0, b, a);
+      mm_dir(n, S[efv], 1, a, b);
+      mm_dir(n, S[efv], 2, b, a);
+      for (q = 0; q < np; q++) v[q] = jpow ? a[q] * ooJ[q] : a[q];
+    }
+  }
+  free(a); free(b); free(ooJ);
+  return 0;
+}
+
 /* nsteps RK4 steps; the time of each step is accumulated in long double as
    in evolve_mesh (src/main/main/main.c:610-626) */
 int nmo_rk4(const nmo_mesh *m, double t, double dt, int nsteps, double *u)

@@ -398,6 +398,16 @@ class OracleMesh:
             raise RuntimeError(f"nmo_evolve failed ({rc})")
         return u
 
+    def filter(self, u, alp=36.0, s=32.0, dn=0, jpow=1, filter_fv=True):
+        """The reference's exponential filter of every element (evolve_filter_all)."""
+        u = np.array(u, np.float64, copy=True, order="C")
+        rc = lib().nmo_filter(ctypes.byref(self.s), u.ctypes.data_as(ctypes.c_void_p),
+                              ctypes.c_double(alp), ctypes.c_double(s), ctypes.c_int(dn),
+                              ctypes.c_int(jpow), ctypes.c_int(int(bool(filter_fv))))
+        if rc:
+            raise RuntimeError(f"nmo_filter failed ({rc})")
+        return u
+
     def rk4(self, u, dt, nsteps, t=0.0):
         u = np.array(u, np.float64, copy=True, order="C")
         rc = lib().nmo_rk4(ctypes.byref(self.s), ctypes.c_double(t),

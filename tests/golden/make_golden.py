@@ -153,6 +153,12 @@ CASES = {
     "dtauto_mixcs7_l0_n7": dict(mesh="cs7", n=7, luni=0, k=(0.3, -0.2, 0.1),
                                 dt="auto", steps=1, eps=0.02, seed=55,
                                 fv=dict(rec="WENOm5_2", extrap="dnfn_extrap1", patches="2")),
+    # evolve_filter_all = yes: the exponential modal filter after every step
+    "filt_cs7_l1_n6": dict(mesh="cs7", n=6, luni=1, k=(0.3, -0.2, 0.1),
+                           dt=0.002, steps=3, eps=0.05, seed=56, filter=True),
+    "filt_mixcs7_l0_n7": dict(mesh="cs7", n=7, luni=0, k=(0.3, -0.2, 0.1),
+                              dt=0.002, steps=2, eps=0.05, seed=57, filter=True,
+                              fv=dict(rec="WENOm5_2", extrap="dnfn_extrap1", patches="0")),
     # non-conforming faces: the listed patches refined one level further
     # (amr_hrefine_p), face traces interpolated across the level jump
     "nc_cs7_l0_n5_h0": dict(mesh="cs7", n=5, luni=0, k=(0.3, -0.2, 0.1),
@@ -198,6 +204,8 @@ def parfile(case, prefix):
         pats = "0 1 2 3 4 5 6"
     if c.get("checkpoint"):
         lines += ["checkpoint = yes"]
+    if c.get("filter"):
+        lines += ["evolve_filter_all = yes"]
     if c.get("hrefine"):
         lines += [f"amr_hrefine_p = {c['hrefine']}"]
     if "fv" in c:

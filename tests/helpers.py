@@ -28,6 +28,11 @@ UPW_CASES = ["upw_cs7_l1_n5", "upw_box_l1_n6", "upw_mixcs7_l0_n7_w5dnfn", "upw_f
 METHOD_CASES = ["ssp3_cs7_l1_n5", "eul_box_l1_n5", "ssp3_mixcs7_l1_n6_wZdnfn",
                 "ssp3_mixcs7_l0_n7_wZparab"]
 METHOD_NEAR_CASES = ["ssp3_mixcs7_l1_n6_wZdnfn", "ssp3_mixcs7_l0_n7_wZparab"]
+# evolve_filter_all = yes (exponential modal filter after every step); the
+# oracle's matrix products sum in another order than the reference's
+# mm_array routines, so it matches these to
+FILT_CASES = ["filt_cs7_l1_n6", "filt_mixcs7_l0_n7"]
+RTOL_FILT_ORACLE = 1e-13
 # dt = auto (the reference's dtfac * hmin; uniform_dtfac on FV elements)
 DTAUTO_CASES = ["dtauto_cs7_l1_n5", "dtauto_box_l2_n6", "dtauto_mixcs7_l0_n7"]
 # coordinates_midpoint_data = yes (FV midpoint factors and normals from the

@@ -5,7 +5,7 @@ operation order and must match it bit for bit."""
 import numpy as np
 import pytest
 
-from helpers import (CASES, FV_CASES, METHOD_CASES, METHOD_NEAR_CASES, MID_CASES,
+from helpers import (CASES, FILT_CASES, RTOL_FILT_ORACLE, FV_CASES, METHOD_CASES, METHOD_NEAR_CASES, MID_CASES,
                      MID_NEAR_CASES, MIX_CASES, MIX_NEAR_CASES, NC_CASES, RTOL_NC_ORACLE,
                      UPW_CASES, build_mesh, load, oracle_for, perm_to_mesh, rel_l2,
                      to_mesh_order)
@@ -202,3 +202,20 @@ def test_oracle_persson_matches_reference():
     assert (fl == 0).all()                      # u == u_p: inside its own bounds
     fl, _ = m.trouble(d["u0"], d["u0"], persson_max=-2.0)
     assert np.array_equal(fl, (d["persson"] > -2.0).any(axis=1).astype(np.int32))
+
+
+@pytest.mark.parametrize("case", FILT_CASES)
+def test_oracle_filter_matches_reference(case):
+    """evolve_filter_all = yes: RK4 step, then the exponential filter of
+    every element (J-weighted on curvilinear elements, FV elements too)."""
+    d, meta = load(case)
+    m = build_mesh(meta)
+    perm = perm_to_mesh(m, d)
+    kw = {}
+    if "fv" in meta:
+        kw = dict(fv_rec=meta["fv"]["rec"], fv_extrap=meta["fv"]["extrap"])
+    o = oracle_for(m, bc=0, k=meta["k"], **kw)
+    u = to_mesh_order(d["u0"], perm)
+    for s in range(meta["steps"]):
+        u = o.filter(o.rk4(u, meta["dt"], 1, t=s * meta["dt"]))
+    assert rel_l2(u[perm], d["u_final"]) <= RTOL_FILT_ORACLE
