@@ -500,7 +500,8 @@ static cudaError_t apply_filter(nmg_ctx *c, double *buf) {
   if (!c->filter_on) return cudaSuccess;
   cudaError_t e = nmgk::filter_launch(c->n, (int)c->nelem, buf, c->mixed ? c->d_isfv : nullptr,
                                       c->d_filt, c->d_cslot, c->d_fooj, c->d_fvgeo,
-                                      c->d_scale, c->filter_jpow, c->filter_fv, c->stream);
+                                      c->d_scale, c->filter_jpow, c->filter_fv,
+                                      (c->fv && !c->mixed) ? 1 : 0, c->stream);
   if (e == cudaSuccess) c->launches++;
   return e;
 }
@@ -852,12 +853,14 @@ static int create_impl(const nmg_mesh *m, int32_t bc_kind, const double k[3], bo
   c->ncurvi = C;
   c->nbface = B;
   c->h_cslot = cslot;
-  // what the midpoint factors need later: the maps, not the node arrays
+  // what the midpoint factors and the filter's Jacobian need later: the
+  // maps, not the node arrays
   c->geom.n = m->n;
   c->geom.nelem = m->nelem;
   c->geom.pat = m->pat;
   c->geom.bbox = m->bbox;
   c->geom.curvi = m->curvi;
+  c->geom.x = m->x;
   c->geom.xu = m->xu;
   c->geom.patches = m->patches;
   // which geometries are needed: DG (LGL points) for DG elements, FV

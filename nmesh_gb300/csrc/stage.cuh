@@ -386,7 +386,8 @@ int fv_variants(int n, Variant *out, int cap);
 cudaError_t filter_prepare(int n);
 cudaError_t filter_launch(int n, int nelem, double *u, const unsigned char *isfv, const double *F,
                           const int *cslot, const double *oojdg, const double *fvgeo,
-                          const double *scale, int jpow, int filter_fv, cudaStream_t st);
+                          const double *scale, int jpow, int filter_fv, int allfv,
+                          cudaStream_t st);
 // traces of non-conforming faces: per slot, field and face node the average
 // over its contributions of the source face interpolated at the node
 cudaError_t hang_launch(int nhang, int n, const int *hoff, const int *hsrc, const double *hw,

@@ -720,17 +720,17 @@ __global__ void __launch_bounds__(256) filter_kernel(int n, double *u, const uns
                                                     const double *F, const int *cslot,
                                                     const double *oojdg, const double *fvgeo,
                                                     const double *scale, int jpow,
-                                                    int filter_fv) {
+                                                    int filter_fv, int allfv) {
   extern __shared__ double sm[];
   const int np = n * n * n, nn = n * n;
   double *a = sm, *b = sm + np, *sM = sm + 2 * np, *sJ = sm + 2 * np + nn;
   const int e = blockIdx.x;
-  const bool efv = isfv && isfv[e];
+  const bool efv = allfv || (isfv && isfv[e]);
   if (efv && !filter_fv) return;
   for (int q = threadIdx.x; q < nn; q += blockDim.x) sM[q] = F[(efv ? nn : 0) + q];
   const int cs = __ldg(cslot + e);
   const double ojc = __ldg(scale + 3 * e) * __ldg(scale + 3 * e + 1) * __ldg(scale + 3 * e + 2);
-  for (int q = threadIdx.x; q < np; q += blockDim.x)
+  for (int q = threadIdx.x; q < np && jpow; q += blockDim.x)
     sJ[q] = cs < 0 ? ojc : efv ? __ldg(fvgeo + (size_t)cs * 13 * np + q)
                                : __ldg(oojdg + (size_t)cs * np + q);
   for (int l = 0; l < NF; l++) {
@@ -864,10 +864,11 @@ cudaError_t filter_prepare(int n) {
 
 cudaError_t filter_launch(int n, int nelem, double *u, const unsigned char *isfv, const double *F,
                           const int *cslot, const double *oojdg, const double *fvgeo,
-                          const double *scale, int jpow, int filter_fv, cudaStream_t st) {
+                          const double *scale, int jpow, int filter_fv, int allfv,
+                          cudaStream_t st) {
   if (nelem <= 0) return cudaSuccess;
   filter_kernel<<<nelem, 256, filter_smem(n), st>>>(n, u, isfv, F, cslot, oojdg, fvgeo, scale,
-                                                    jpow, filter_fv);
+                                                    jpow, filter_fv, allfv);
   return cudaGetLastError();
 }
 

@@ -42,9 +42,11 @@ def test_filter_matches_reference(case, path):
     assert rel_l2(u[perm], d["u_final"]) <= RTOL_RK4
 
 
-@pytest.mark.parametrize("jpow,filter_fv", [(1, True), (0, True), (1, False)])
-def test_filter_options_match_oracle(jpow, filter_fv):
-    m = ng.Mesh.build(ng.MESH_CUBEDSPHERES7, n=7, luni=1, cs_dc=1.0, cs_r0fac=20.0, fv=[0, 2])
+@pytest.mark.parametrize("jpow,filter_fv,fv", [(1, True, [0, 2]), (0, True, [0, 2]),
+                                               (1, False, [0, 2]), (1, True, True),
+                                               (0, True, False)])
+def test_filter_options_match_oracle(jpow, filter_fv, fv):
+    m = ng.Mesh.build(ng.MESH_CUBEDSPHERES7, n=7, luni=1, cs_dc=1.0, cs_r0fac=20.0, fv=fv)
     u = gaussian_pulses(m.coords(), seed=4, rmin=1.0, rmax=4.0)
     u += 1e-2 * np.random.default_rng(4).standard_normal(u.shape)
     o = oracle_for(m, bc=1, fv_rec="WENOm5_2", fv_extrap="dnfn_extrap1")
