@@ -51,7 +51,8 @@ def test_filter_options_match_oracle(jpow, filter_fv, fv):
     u += 1e-2 * np.random.default_rng(4).standard_normal(u.shape)
     o = oracle_for(m, bc=1, fv_rec="WENOm5_2", fv_extrap="dnfn_extrap1")
     ev = ng.Evolution(m, ng.BC_OUTGOING)
-    ev.set_fv("WENOm5_2", "dnfn_extrap1")
+    if fv is not False:
+        ev.set_fv("WENOm5_2", "dnfn_extrap1")
     ev.set_filter(True, alp=30.0, s=8.0, dn=1, jpower=jpow, filter_fv=filter_fv)
     dt = 0.002
     got = ev.rk4_steps_host(u, 0.0, dt, 2)
