@@ -85,6 +85,12 @@ typedef struct nmg_mesh_params {
   int32_t hrefine;    /* bit p set: patch p is refined one level further
                          (amr_hrefine_p, src/main/amr/mesh.c:269-284); its
                          faces against other patches are non-conforming */
+  int32_t sphere_levels; /* amr_hrefine_sphere_levels: nested spheres about
+                            x = 0 in which elements are refined further
+                            (hrefine_sphere_loadbalance, src/main/amr/
+                            refine.c:1087-1100); 0: none */
+  double sphere_radius;  /* amr_hrefine_sphere_radius: innermost radius (the
+                            reference reads it as an integer) */
 } nmg_mesh_params;
 
 /* A mesh given element by element, e.g. packed from the reference's tMesh

@@ -41,7 +41,8 @@ class _MeshParams(ctypes.Structure):
                 ("luni", ctypes.c_int32), ("periodic", ctypes.c_int32),
                 ("xc", ctypes.c_double * 3), ("box_dout", ctypes.c_double),
                 ("cs_dc", ctypes.c_double), ("cs_r0fac", ctypes.c_double),
-                ("fv", ctypes.c_int32), ("hrefine", ctypes.c_int32)]
+                ("fv", ctypes.c_int32), ("hrefine", ctypes.c_int32),
+                ("sphere_levels", ctypes.c_int32), ("sphere_radius", ctypes.c_double)]
 
 
 class TroubleParams(ctypes.Structure):
@@ -248,13 +249,16 @@ class Mesh:
     @classmethod
     def build(cls, mesh_type=MESH_BOX, n=5, luni=0, xc=(0.0, 0.0, 0.0),
               box_dout=1.0, cs_dc=1.0, cs_r0fac=20.0, periodic=False, fv=False,
-              hrefine=()):
+              hrefine=(), sphere_levels=0, sphere_radius=10.0):
         """Mesh from the reference's parameters: amr_mesh_type (1 BoxMesh /
         7 CubedSpheres), amr_n0..2 = n, amr_luni, amr_mesh_xc,
         amr_BoxMesh_dout, amr_CubedSphere_dc, amr_CubedSphere_r0fac;
         fv=True puts every patch in amr_uniform_p and amr_fv_p, a list of
         patch indices puts those patches there; hrefine lists the patches
-        of amr_hrefine_p (refined one level further)."""
+        of amr_hrefine_p (refined one level further); sphere_levels and
+        sphere_radius are amr_hrefine_sphere_levels / _radius (elements
+        whose centre lies within radius 2^(levels-1-i) of x = 0 are refined
+        in pass i)."""
         hmask = 0
         for p_ in hrefine:
             hmask |= 1 << int(p_)
@@ -268,7 +272,8 @@ class Mesh:
                 mask |= 1 << int(p_)
         p = _MeshParams(int(mesh_type), int(n), int(luni), int(bool(periodic)),
                         (ctypes.c_double * 3)(*xc), float(box_dout),
-                        float(cs_dc), float(cs_r0fac), int(mask), hmask)
+                        float(cs_dc), float(cs_r0fac), int(mask), hmask,
+                        int(sphere_levels), float(sphere_radius))
         h = ctypes.c_void_p()
         rc = lib().nmg_mesh_build(ctypes.byref(p), ctypes.byref(h))
         if rc:

@@ -152,6 +152,12 @@ void ab_range(int dom, const double Din[6], double r[4]) {
   r[3] = Din[ia[dom][3]] / Din[dom];
 }
 
+// one element of a generated mesh: patch, level, integer position
+struct Leaf {
+  int p, L;
+  int ix[3];
+};
+
 // element bbox at level L and integer location (ix,iy,iz) by successive
 // halving of the patch bbox (amr_set_elm0_bbox)
 void elem_bbox(const double pb[6], int L, const int ixyz[3], double bb[6]) {
@@ -168,14 +174,70 @@ void elem_bbox(const double pb[6], int L, const int ixyz[3], double bb[6]) {
   }
 }
 
-// fill geometry for all elements of the given patches, patch p at uniform
-// level L[p], elements of a patch in Morton (Z) order; patches in fvmask get
-// equally spaced points
-void fill_geometry(nmg_mesh &m, const std::vector<Patch> &pats, const std::vector<int> &L,
+// Cartesian position of the patch coordinates X (set_xyz)
+void patch_x(const Patch &P, const double X[3], double x[3]) {
+  if (P.cubed) {
+    double J[3][3];
+    cubsph_x_dXdx(P, X, x, J);
+  } else {
+    for (int d = 0; d < 3; d++) x[d] = X[d];
+  }
+}
+
+// the elements of patch p at uniform level L, in Morton (Z) order
+void uniform_leaves(int p, int L, std::vector<Leaf> &out) {
+  const int64_t per = (int64_t)1 << (3 * L);
+  for (int64_t mc = 0; mc < per; mc++) {
+    Leaf lf{p, L, {0, 0, 0}};
+    for (int bit = 0; bit < L; bit++)
+      for (int d = 0; d < 3; d++) lf.ix[d] |= (int)((mc >> (3 * bit + d)) & 1) << bit;
+    out.push_back(lf);
+  }
+}
+
+// Nested-sphere refinement (hrefine_sphere_loadbalance and
+// hrefine_once_within_sphere, src/main/amr/refine.c:1025-1100): pass i
+// refines every element whose centre -- the patch map of its bbox centre
+// (set_nodecenter_xyz, src/main/coordinates/utilities.c:1308-1327) -- lies
+// within r_i = radius 2^(levels-1-i) of x = 0 (Cart_distance_x0_x1); a
+// refined element is replaced by its eight children (child digit: bit d set
+// for the upper half in direction d).
+void refine_spheres(const std::vector<Patch> &pats, int levels, double radius,
+                    std::vector<Leaf> &leaves) {
+  double r = radius * std::pow(2., levels - 1);
+  for (int i = 0; i < levels; i++, r *= 0.5) {
+    std::vector<Leaf> next;
+    next.reserve(leaves.size());
+    for (const Leaf &lf : leaves) {
+      double bb[6], X[3], x[3];
+      elem_bbox(pats[lf.p].bbox, lf.L, lf.ix, bb);
+      for (int d = 0; d < 3; d++) X[d] = 0.5 * (bb[2 * d + 1] + bb[2 * d]);
+      patch_x(pats[lf.p], X, x);
+      double dist2 = 0.;
+      for (int d = 0; d < 3; d++) {
+        const double tmp = 0. - x[d];
+        dist2 += tmp * tmp;
+      }
+      if (std::sqrt(dist2) <= r) {
+        for (int dig = 0; dig < 8; dig++) {
+          Leaf c{lf.p, lf.L + 1, {0, 0, 0}};
+          for (int d = 0; d < 3; d++) c.ix[d] = 2 * lf.ix[d] + ((dig >> d) & 1);
+          next.push_back(c);
+        }
+      } else {
+        next.push_back(lf);
+      }
+    }
+    leaves.swap(next);
+  }
+}
+
+// fill geometry for the given elements (patch, level, position); elements
+// of patches in fvmask get equally spaced points
+void fill_geometry(nmg_mesh &m, const std::vector<Patch> &pats, const std::vector<Leaf> &leaves,
                    int32_t fvmask) {
   const int n = m.n, np = n * n * n;
-  m.nelem = 0;
-  for (size_t p = 0; p < pats.size(); p++) m.nelem += (int64_t)1 << (3 * L[p]);
+  m.nelem = (int64_t)leaves.size();
   m.patches = pats;
   m.pat.resize(m.nelem);
   m.bbox.resize(m.nelem * 6);
@@ -186,32 +248,26 @@ void fill_geometry(nmg_mesh &m, const std::vector<Patch> &pats, const std::vecto
   m.names.assign(m.nelem, std::string());
   m.level.assign(m.nelem, 0);
   m.ixyz.assign(m.nelem * 3, 0);
-  int64_t e = 0;
-  for (size_t p = 0; p < pats.size(); p++) {
-    const int Lp = L[p];
-    const int64_t per = (int64_t)1 << (3 * Lp);
-    for (int64_t mc = 0; mc < per; mc++, e++) {
-      int ixyz[3] = {0, 0, 0};
-      for (int bit = 0; bit < Lp; bit++)
-        for (int d = 0; d < 3; d++) ixyz[d] |= (int)((mc >> (3 * bit + d)) & 1) << bit;
-      elem_bbox(pats[p].bbox, Lp, ixyz, &m.bbox[e * 6]);
-      // elmname: patch, then one octree child digit per level, bit d set
-      // for the upper half in direction d (connections.c:819-866,1186-1200)
-      std::string nm = std::to_string(p) + "_";
-      for (int ll = 1; ll <= Lp; ll++) {
-        int dig = 0;
-        for (int d = 0; d < 3; d++) dig |= ((ixyz[d] >> (Lp - ll)) & 1) << d;
-        nm += (char)('0' + dig);
-      }
-      m.names[e] = nm;
-      m.level[e] = Lp;
-      for (int d = 0; d < 3; d++) m.ixyz[e * 3 + d] = ixyz[d];
-      m.pat[e] = (int32_t)p;
-      m.curvi[e] = pats[p].cubed ? 1 : 0;
-      const bool isfv = (fvmask >> p) & 1;
-      if (isfv) m.fv[e] = 1;
-      nmg::element_geometry(m, e, isfv, &m.xyz[e * 3 * np], &m.dXdx[e * 9 * np]);
+  for (int64_t e = 0; e < m.nelem; e++) {
+    const int p = leaves[e].p, Lp = leaves[e].L;
+    const int *ixyz = leaves[e].ix;
+    elem_bbox(pats[p].bbox, Lp, ixyz, &m.bbox[e * 6]);
+    // elmname: patch, then one octree child digit per level, bit d set
+    // for the upper half in direction d (connections.c:819-866,1186-1200)
+    std::string nm = std::to_string(p) + "_";
+    for (int ll = 1; ll <= Lp; ll++) {
+      int dig = 0;
+      for (int d = 0; d < 3; d++) dig |= ((ixyz[d] >> (Lp - ll)) & 1) << d;
+      nm += (char)('0' + dig);
     }
+    m.names[e] = nm;
+    m.level[e] = Lp;
+    for (int d = 0; d < 3; d++) m.ixyz[e * 3 + d] = ixyz[d];
+    m.pat[e] = (int32_t)p;
+    m.curvi[e] = pats[p].cubed ? 1 : 0;
+    const bool isfv = (fvmask >> p) & 1;
+    if (isfv) m.fv[e] = 1;
+    nmg::element_geometry(m, e, isfv, &m.xyz[e * 3 * np], &m.dXdx[e * 9 * np]);
   }
 }
 
@@ -536,22 +592,48 @@ std::string pack_faces(nmg_mesh &m, const int64_t *nbnode, const double period[3
     }
   if (m.level.empty()) return "";
 
-  // Non-conforming faces of a generated mesh (patches at different levels):
-  // a face without a conforming neighbour that lies on its parent's face is
-  // matched against the coarser elements' faces by the parent face's
-  // corners, which the four siblings on that face carry.  The neighbour
-  // relation set_ajsurf_vl (src/main/amr/surface.c:799-1360) works with:
-  // each face node takes the average of the neighbour faces that contain it,
-  // each interpolated at the node's position (basis_interp2d_toIpoints).
-  std::vector<int64_t> pstart;
-  for (int64_t e = 0; e < E; e++)
-    if (pstart.empty() || m.pat[e] != m.pat[pstart.back()]) pstart.push_back(e);
-  auto elem_of = [&](int p, const int q[3], int L) {
-    int64_t mc = 0;
-    for (int bit = 0; bit < L; bit++)
-      for (int d = 0; d < 3; d++) mc |= (int64_t)((q[d] >> bit) & 1) << (3 * bit + d);
-    return pstart[p] + mc;
+  // Non-conforming faces of a generated mesh (elements of different levels:
+  // patch-wise, amr_hrefine_p, or nested spheres): a face without a
+  // conforming neighbour that lies on its parent's face is matched against
+  // the coarser elements' faces by the parent face's corners (the patch map
+  // of the parent bbox's corners).  The neighbour relation set_ajsurf_vl
+  // (src/main/amr/surface.c:799-1360) works with: each face node takes the
+  // average of the neighbour faces that contain it, each interpolated at the
+  // node's position (basis_interp2d_toIpoints).  Only jumps of one level
+  // are built: a coarse face must meet exactly four finer faces.
+  auto ancestor_face = [&](int64_t e, int f, int up, double corner[4][3], double pc[3]) {
+    const int d = f >> 1, s = f & 1, d1 = d == 0 ? 1 : 0, d2 = d == 2 ? 1 : 2;
+    const int La = m.level[e] - up;
+    int qa[3];
+    for (int dd = 0; dd < 3; dd++) qa[dd] = m.ixyz[e * 3 + dd] >> up;
+    double bb[6];
+    elem_bbox(m.patches[m.pat[e]].bbox, La, qa, bb);
+    for (int dd = 0; dd < 3; dd++) pc[dd] = 0.;
+    for (int t = 0; t < 4; t++) {
+      double X[3];
+      X[d] = bb[2 * d + s];
+      X[d1] = bb[2 * d1 + (t & 1)];
+      X[d2] = bb[2 * d2 + (t >> 1)];
+      patch_x(m.patches[m.pat[e]], X, corner[t]);
+      for (int dd = 0; dd < 3; dd++) pc[dd] += corner[t][dd];
+    }
+    for (int dd = 0; dd < 3; dd++) pc[dd] = wrap1(0.25 * pc[dd], per[dd]);
   };
+  // an outer face of an element of level Lc whose centre is pc
+  auto find_outer = [&](const double pc[3], int Lc) {
+    for (int dz = -1; dz <= 1; dz++)
+      for (int dy = -1; dy <= 1; dy++)
+        for (int dx = -1; dx <= 1; dx++) {
+          int off[3] = {dx, dy, dz};
+          auto it = h.find(kcell(pc, off));
+          if (it == h.end()) continue;
+          for (int64_t g : it->second)
+            if (m.nb[g] < 0 && m.level[g / 6] == Lc && dist2(pc, &cen[g * 3]) < tol * tol)
+              return g;
+        }
+    return (int64_t)-1;
+  };
+  if (m.patches.empty()) return "";
   struct HPair { int64_t fe; int ff; int64_t ce; int cf; int A, B, o; };
   std::vector<HPair> pairs;
   for (int64_t e = 0; e < E; e++)
@@ -561,36 +643,20 @@ std::string pack_faces(nmg_mesh &m, const int64_t *nbnode, const double period[3
       const int d = f >> 1, s = f & 1, d1 = d == 0 ? 1 : 0, d2 = d == 2 ? 1 : 2;
       const int *q = &m.ixyz[e * 3];
       if ((q[d] & 1) != s) continue;  // not on the parent's face f
-      int64_t sib[4];
       double corner[4][3], pc[3];
-      for (int t = 0; t < 4; t++) {
-        int qs[3] = {q[0], q[1], q[2]};
-        qs[d1] = (qs[d1] & ~1) | (t & 1);
-        qs[d2] = (qs[d2] & ~1) | (t >> 1);
-        sib[t] = elem_of(m.pat[e], qs, L);
-        pos(sib[t], face_node(n, f, (t & 1) * (n - 1), (t >> 1) * (n - 1)), corner[t]);
+      ancestor_face(e, f, 1, corner, pc);
+      const int64_t match = find_outer(pc, L - 1);
+      if (match < 0) {
+        // no coarser neighbour one level up: a face two or more levels up
+        // that meets an element is a level jump this mesh does not build
+        for (int up = 2; up <= L && ((q[d] >> (up - 1)) & 1) == s; up++) {
+          ancestor_face(e, f, up, corner, pc);
+          if (find_outer(pc, L - up) >= 0)
+            return "element " + std::to_string(e) + " face " + std::to_string(f) +
+                   ": a level jump of more than one across a face is not supported";
+        }
+        continue;  // outer face
       }
-      for (int dd = 0; dd < 3; dd++) {
-        double sum = 0;
-        for (int t = 0; t < 4; t++)
-          sum += m.xyz[(sib[t] * 3 + dd) * np +
-                       face_node(n, f, (t & 1) * (n - 1), (t >> 1) * (n - 1))];
-        pc[dd] = wrap1(0.25 * sum, per[dd]);
-      }
-      int64_t match = -1;
-      for (int dz = -1; dz <= 1 && match < 0; dz++)
-        for (int dy = -1; dy <= 1 && match < 0; dy++)
-          for (int dx = -1; dx <= 1 && match < 0; dx++) {
-            int off[3] = {dx, dy, dz};
-            auto it = h.find(kcell(pc, off));
-            if (it == h.end()) continue;
-            for (int64_t g : it->second)
-              if (m.nb[g] < 0 && m.level[g / 6] == L - 1 && dist2(pc, &cen[g * 3]) < tol * tol) {
-                match = g;
-                break;
-              }
-          }
-      if (match < 0) continue;  // outer face
       const int64_t e2 = match / 6;
       const int f2 = (int)(match % 6);
       int found = -1;
@@ -692,6 +758,8 @@ int nmg_mesh_build(const nmg_mesh_params *p, nmg_mesh **out) {
   *out = nullptr;
   if (p->n < 2 || p->n > 16) return fail(NMG_EUNSUP, "nmg_mesh_build: n must be in [2,16]");
   if (p->luni < 0 || p->luni > 8) return fail(NMG_EINVAL, "nmg_mesh_build: luni must be in [0,8]");
+  if (p->sphere_levels < 0 || p->sphere_levels > 8 || !(p->sphere_radius >= 0.))
+    return fail(NMG_EINVAL, "nmg_mesh_build: sphere_levels must be in [0,8], sphere_radius >= 0");
   nmg_mesh *m = new (std::nothrow) nmg_mesh;
   if (!m) return fail(NMG_ENOMEM, "nmg_mesh_build: out of memory");
   try {
@@ -745,10 +813,11 @@ int nmg_mesh_build(const nmg_mesh_params *p, nmg_mesh **out) {
       delete m;
       return fail(NMG_EUNSUP, "nmg_mesh_build: unknown mesh_type");
     }
-    std::vector<int> L(pats.size(), p->luni);
+    std::vector<Leaf> leaves;
     for (size_t q = 0; q < pats.size(); q++)
-      if ((p->hrefine >> q) & 1) L[q]++;
-    fill_geometry(*m, pats, L, p->fv);
+      uniform_leaves((int)q, p->luni + (((p->hrefine >> q) & 1) ? 1 : 0), leaves);
+    if (p->sphere_levels > 0) refine_spheres(pats, p->sphere_levels, p->sphere_radius, leaves);
+    fill_geometry(*m, pats, leaves, p->fv);
     bool anyfv = false;
     for (int64_t e = 0; e < m->nelem; e++) anyfv = anyfv || m->fv[e];
     if (!anyfv) m->fv.clear();

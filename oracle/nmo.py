@@ -191,8 +191,8 @@ def match_faces(xyz, n, period=None, tol=1e-9, fv=None):
 
 
 def match_hanging(xyz, n, pat, bbox, nbnode, tol=1e-9):
-    """Non-conforming faces of a mesh whose patches sit at different
-    uniform levels (the reference's amr_hrefine_p).
+    """Non-conforming faces of a mesh whose elements sit at different levels
+    (the reference's amr_hrefine_p and amr_hrefine_sphere_levels).
 
     Faces left outer (-1) by match_faces are tested: a face that lies on its
     parent element's face is the quarter of a coarser element's face when
@@ -253,7 +253,13 @@ def match_hanging(xyz, n, pat, bbox, nbnode, tol=1e-9):
                 q = pos[e].copy()
                 q[d1] = (q[d1] & ~1) | (t & 1)
                 q[d2] = (q[d2] & ~1) | (t >> 1)
-                sib = where[(int(pat[e]), int(lev[e])) + tuple(q)]
+                # the sibling, or (refined further) its descendant at the corner
+                lv = int(lev[e])
+                bits = np.zeros(3, np.int64)
+                bits[d], bits[d1], bits[d2] = s, t & 1, t >> 1
+                while (int(pat[e]), lv) + tuple(q) not in where:
+                    q, lv = 2 * q + bits, lv + 1
+                sib = where[(int(pat[e]), lv) + tuple(q)]
                 cpts.append(xyz[sib][:, planes[f][corners[t]]])
             cand = [g for g in free.get(pkey(np.mean(cpts, axis=0)), [])
                     if lev[g[0]] == lev[e] - 1]

@@ -170,6 +170,14 @@ CASES = {
     "nc_upw_cs7_l0_n6_h35": dict(mesh="cs7", n=6, luni=0, k=(0.3, 0.2, -0.1),
                                  dt=0.002, steps=2, eps=0.02, seed=41, hrefine="3 5",
                                  numflux="upwind"),
+    # non-conforming faces inside patches: nested-sphere refinement about
+    # x = 0 (amr_hrefine_sphere_levels / _radius)
+    "sph_box_l1_n5_s2r2": dict(mesh="box", n=5, luni=1, k=(1.0, -0.5, 0.25),
+                               dt=0.002, steps=2, eps=0.02, seed=42, sphere=(2, 2)),
+    "sph_box_l2_n4_s1r3": dict(mesh="box", n=4, luni=2, k=(0.5, 1.0, -1.0),
+                               dt=0.002, steps=2, eps=0.02, seed=43, sphere=(1, 3)),
+    "sph_cs7_l1_n4_s1r6": dict(mesh="cs7", n=4, luni=1, k=(0.3, -0.2, 0.1),
+                               dt=0.002, steps=2, eps=0.02, seed=44, sphere=(1, 6)),
 }
 
 
@@ -208,6 +216,9 @@ def parfile(case, prefix):
         lines += ["evolve_filter_all = yes"]
     if c.get("hrefine"):
         lines += [f"amr_hrefine_p = {c['hrefine']}"]
+    if c.get("sphere"):
+        lines += [f"amr_hrefine_sphere_levels = {c['sphere'][0]}",
+                  f"amr_hrefine_sphere_radius = {c['sphere'][1]}"]
     if "fv" in c:
         pats = c["fv"].get("patches", pats)
         lines += [f"amr_uniform_p = {pats}", f"amr_fv_p = {pats}",

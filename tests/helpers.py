@@ -40,7 +40,8 @@ DTAUTO_CASES = ["dtauto_cs7_l1_n5", "dtauto_box_l2_n6", "dtauto_mixcs7_l0_n7"]
 MID_CASES = ["fvcs7_l0_n7_w5dnfn_mid", "fvcs7_l1_n6_w3no_mid", "ssp3_mixcs7_l0_n7_wZparab_mid"]
 MID_NEAR_CASES = ["ssp3_mixcs7_l0_n7_wZparab_mid"]
 # non-conforming faces: patches refined one level further (amr_hrefine_p)
-NC_CASES = ["nc_cs7_l0_n5_h0", "nc_cs7_l0_n4_h1", "nc_cs7_l1_n5_h02", "nc_upw_cs7_l0_n6_h35"]
+NC_CASES = ["nc_cs7_l0_n5_h0", "nc_cs7_l0_n4_h1", "nc_cs7_l1_n5_h02", "nc_upw_cs7_l0_n6_h35",
+            "sph_box_l1_n5_s2r2", "sph_box_l2_n4_s1r3", "sph_cs7_l1_n4_s1r6"]
 # the oracle's non-conforming (and even-n DG/FV interface) traces take the
 # neighbour positions from the element structure, the reference from its
 # coordinate maps: equal to a few ulp of the position, so the oracle matches
@@ -63,14 +64,17 @@ def load(case):
 def build_mesh(meta, periodic=False):
     import nmesh_gb300 as ng
     href = [int(p) for p in meta.get("hrefine", "").split()]
+    sph = meta.get("sphere", (0, 10))
     fv = "fv" in meta
     if fv and "patches" in meta["fv"]:
         fv = [int(p) for p in meta["fv"]["patches"].split()]
     if meta["mesh"] == "box":
         return ng.Mesh.build(ng.MESH_BOX, n=meta["n"], luni=meta["luni"],
-                             xc=(PI, PI, PI), box_dout=PI, periodic=periodic, fv=fv)
+                             xc=(PI, PI, PI), box_dout=PI, periodic=periodic, fv=fv,
+                             sphere_levels=sph[0], sphere_radius=sph[1])
     return ng.Mesh.build(ng.MESH_CUBEDSPHERES7, n=meta["n"], luni=meta["luni"],
-                         cs_dc=1.0, cs_r0fac=20.0, fv=fv, hrefine=href)
+                         cs_dc=1.0, cs_r0fac=20.0, fv=fv, hrefine=href,
+                         sphere_levels=sph[0], sphere_radius=sph[1])
 
 
 def perm_to_mesh(mesh, d):

@@ -144,11 +144,17 @@ def test_nonconforming_lists_match_oracle(case):
             assert [s_ for s_, _ in mine] == [s_ for s_, _ in theirs]
             assert np.allclose([p_ for _, p_ in mine], [p_ for _, p_ in theirs],
                                rtol=0, atol=1e-14)
-    # element names carry each patch's own level
+    # element names carry each element's own level: the halvings of its
+    # patch's extent, and the names are the fixture's
     names = m.names()
+    lo = {p_: bbox[pat == p_, 0].min() for p_ in set(pat.tolist())}
+    hi = {p_: bbox[pat == p_, 1].max() for p_ in set(pat.tolist())}
     for e in range(m.nelem):
         lev = len(names[e].split("_")[1])
-        assert lev == meta["luni"] + (str(pat[e]) in meta["hrefine"].split())
+        ext = (hi[pat[e]] - lo[pat[e]]) / (bbox[e, 1] - bbox[e, 0])
+        assert 2 ** lev == round(ext)
+        if "hrefine" in meta:
+            assert lev == meta["luni"] + (str(pat[e]) in meta["hrefine"].split())
 
 
 def test_nonconforming_concat_keeps_lists():

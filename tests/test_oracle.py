@@ -24,7 +24,7 @@ def _oracle_mesh(d, meta):
                   fv_surface_interp=meta["fv"].get("surf", "linear"))
     else:
         nb = nmo.match_faces(d["x"], n)
-    if meta.get("hrefine"):
+    if meta.get("hrefine") or meta.get("sphere"):
         nb, fv["hang"] = nmo.match_hanging(d["x"], n, d["pat"], d["bbox"], nb)
     return nmo.OracleMesh(d["bbox"], curvi, d["dXdx"], d["x"], nb, n, bc=0,
                           k=meta["k"], numflux=meta.get("numflux", "LLF"), **fv)
@@ -102,7 +102,8 @@ def test_oracle_mixed_even_n_matches_reference(case):
 
 @pytest.mark.parametrize("case", NC_CASES)
 def test_oracle_nonconforming_matches_reference(case):
-    """Patches one level finer than their neighbours (amr_hrefine_p): each
+    """Elements one level finer than their neighbours (patch-wise,
+    amr_hrefine_p, and inside patches, amr_hrefine_sphere_levels): each
     node of a fine face interpolates the coarse face, each node of a coarse
     face averages the fine faces containing it.  The neighbour positions
     come from the element structure here and from inverse coordinate maps
