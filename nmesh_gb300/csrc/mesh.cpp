@@ -24,6 +24,7 @@
 #include "../../include/nmg.h"
 
 #include <algorithm>
+#include <array>
 #include <cfloat>
 #include <cmath>
 #include <cstring>
@@ -269,6 +270,49 @@ void fill_geometry(nmg_mesh &m, const std::vector<Patch> &pats, const std::vecto
     if (isfv) m.fv[e] = 1;
     nmg::element_geometry(m, e, isfv, &m.xyz[e * 3 * np], &m.dXdx[e * 9 * np]);
   }
+}
+
+// Level and integer position of each element of a mesh given element by
+// element, from its bbox within its patch's extent (the union of the
+// patch's element bboxes): the halvings must agree in the three directions
+// and land on integer positions, else the mesh keeps no levels (and is
+// matched as conforming only).
+void derive_levels(nmg_mesh &m) {
+  const int64_t E = m.nelem;
+  std::unordered_map<int, std::array<double, 6>> ext;
+  for (int64_t e = 0; e < E; e++) {
+    const double *bb = &m.bbox[e * 6];
+    auto it = ext.find(m.pat[e]);
+    if (it == ext.end()) {
+      std::array<double, 6> a;
+      for (int q = 0; q < 6; q++) a[q] = bb[q];
+      ext[m.pat[e]] = a;
+    } else {
+      for (int d = 0; d < 3; d++) {
+        it->second[2 * d] = std::min(it->second[2 * d], bb[2 * d]);
+        it->second[2 * d + 1] = std::max(it->second[2 * d + 1], bb[2 * d + 1]);
+      }
+    }
+  }
+  std::vector<int32_t> level(E), ixyz(E * 3);
+  for (int64_t e = 0; e < E; e++) {
+    const double *bb = &m.bbox[e * 6];
+    const std::array<double, 6> &a = ext[m.pat[e]];
+    int L = -1;
+    for (int d = 0; d < 3; d++) {
+      const double h = bb[2 * d + 1] - bb[2 * d], ratio = (a[2 * d + 1] - a[2 * d]) / h;
+      const int Ld = (int)std::lround(std::log2(ratio));
+      const double q = (bb[2 * d] - a[2 * d]) / h;
+      if (Ld < 0 || Ld > 20 || std::fabs(ratio - std::ldexp(1., Ld)) > 1e-6 * ratio ||
+          std::fabs(q - std::round(q)) > 1e-6 || (L >= 0 && Ld != L))
+        return;
+      L = Ld;
+      ixyz[e * 3 + d] = (int32_t)std::lround(q);
+    }
+    level[e] = L;
+  }
+  m.level.swap(level);
+  m.ixyz.swap(ixyz);
 }
 
 // quantised coordinates for the spatial hash of face centres
@@ -592,32 +636,58 @@ std::string pack_faces(nmg_mesh &m, const int64_t *nbnode, const double period[3
     }
   if (m.level.empty()) return "";
 
-  // Non-conforming faces of a generated mesh (elements of different levels:
-  // patch-wise, amr_hrefine_p, or nested spheres): a face without a
-  // conforming neighbour that lies on its parent's face is matched against
-  // the coarser elements' faces by the parent face's corners (the patch map
-  // of the parent bbox's corners).  The neighbour relation set_ajsurf_vl
+  // Non-conforming faces (elements of different levels: patch-wise,
+  // amr_hrefine_p, or nested spheres): a face without a conforming
+  // neighbour that lies on its parent's face is matched against the coarser
+  // elements' faces by the parent face's corners, which the elements at
+  // those corners carry (the siblings, or their descendants where the
+  // siblings are refined further).  The neighbour relation set_ajsurf_vl
   // (src/main/amr/surface.c:799-1360) works with: each face node takes the
   // average of the neighbour faces that contain it, each interpolated at the
   // node's position (basis_interp2d_toIpoints).  Only jumps of one level
   // are built: a coarse face must meet exactly four finer faces.
+  struct LKey {
+    int64_t v[2];
+    bool operator==(const LKey &o) const { return v[0] == o.v[0] && v[1] == o.v[1]; }
+  };
+  struct LKeyHash {
+    size_t operator()(const LKey &k) const {
+      return (size_t)(k.v[0] * 0x9e3779b97f4a7c15ULL ^ (k.v[1] + 0x632be59bd9b4e019ULL));
+    }
+  };
+  auto lkey = [](int p, int L, const int q[3]) {
+    return LKey{{((int64_t)p << 8) | L, ((int64_t)q[0] << 42) | ((int64_t)q[1] << 21) | q[2]}};
+  };
+  std::unordered_map<LKey, int64_t, LKeyHash> where;
+  int levmax = 0;
+  for (int64_t e = 0; e < E; e++) {
+    where[lkey(m.pat[e], m.level[e], &m.ixyz[e * 3])] = e;
+    levmax = std::max(levmax, (int)m.level[e]);
+  }
+  // corners (and their centre) of face f of e's ancestor `up` levels up;
+  // false if the patch is not tiled there
   auto ancestor_face = [&](int64_t e, int f, int up, double corner[4][3], double pc[3]) {
     const int d = f >> 1, s = f & 1, d1 = d == 0 ? 1 : 0, d2 = d == 2 ? 1 : 2;
-    const int La = m.level[e] - up;
-    int qa[3];
-    for (int dd = 0; dd < 3; dd++) qa[dd] = m.ixyz[e * 3 + dd] >> up;
-    double bb[6];
-    elem_bbox(m.patches[m.pat[e]].bbox, La, qa, bb);
     for (int dd = 0; dd < 3; dd++) pc[dd] = 0.;
     for (int t = 0; t < 4; t++) {
-      double X[3];
-      X[d] = bb[2 * d + s];
-      X[d1] = bb[2 * d1 + (t & 1)];
-      X[d2] = bb[2 * d2 + (t >> 1)];
-      patch_x(m.patches[m.pat[e]], X, corner[t]);
-      for (int dd = 0; dd < 3; dd++) pc[dd] += corner[t][dd];
+      int bits[3], q[3];
+      bits[d] = s;
+      bits[d1] = t & 1;
+      bits[d2] = t >> 1;
+      int lv = m.level[e] - up;
+      for (int dd = 0; dd < 3; dd++) q[dd] = m.ixyz[e * 3 + dd] >> up;
+      auto it = where.find(lkey(m.pat[e], lv, q));
+      while (it == where.end() && lv < levmax) {
+        for (int dd = 0; dd < 3; dd++) q[dd] = 2 * q[dd] + bits[dd];
+        it = where.find(lkey(m.pat[e], ++lv, q));
+      }
+      if (it == where.end()) return false;
+      const int node = face_node(n, f, (t & 1) * (n - 1), (t >> 1) * (n - 1));
+      pos(it->second, node, corner[t]);
+      for (int dd = 0; dd < 3; dd++) pc[dd] += m.xyz[(it->second * 3 + dd) * np + node];
     }
     for (int dd = 0; dd < 3; dd++) pc[dd] = wrap1(0.25 * pc[dd], per[dd]);
+    return true;
   };
   // an outer face of an element of level Lc whose centre is pc
   auto find_outer = [&](const double pc[3], int Lc) {
@@ -633,7 +703,6 @@ std::string pack_faces(nmg_mesh &m, const int64_t *nbnode, const double period[3
         }
     return (int64_t)-1;
   };
-  if (m.patches.empty()) return "";
   struct HPair { int64_t fe; int ff; int64_t ce; int cf; int A, B, o; };
   std::vector<HPair> pairs;
   for (int64_t e = 0; e < E; e++)
@@ -644,13 +713,13 @@ std::string pack_faces(nmg_mesh &m, const int64_t *nbnode, const double period[3
       const int *q = &m.ixyz[e * 3];
       if ((q[d] & 1) != s) continue;  // not on the parent's face f
       double corner[4][3], pc[3];
-      ancestor_face(e, f, 1, corner, pc);
+      if (!ancestor_face(e, f, 1, corner, pc)) return "element levels do not tile the patch";
       const int64_t match = find_outer(pc, L - 1);
       if (match < 0) {
         // no coarser neighbour one level up: a face two or more levels up
         // that meets an element is a level jump this mesh does not build
         for (int up = 2; up <= L && ((q[d] >> (up - 1)) & 1) == s; up++) {
-          ancestor_face(e, f, up, corner, pc);
+          if (!ancestor_face(e, f, up, corner, pc)) return "element levels do not tile the patch";
           if (find_outer(pc, L - up) >= 0)
             return "element " + std::to_string(e) + " face " + std::to_string(f) +
                    ": a level jump of more than one across a face is not supported";
@@ -878,6 +947,7 @@ int nmg_mesh_from_desc(const nmg_mesh_desc *d, nmg_mesh **out) {
           return fail(NMG_EINVAL, "element bbox must have positive extent");
         }
     }
+    if (!d->nbnode) derive_levels(*m);  // non-conforming faces are found from the levels
     std::string err = nmg::pack_faces(*m, d->nbnode, d->period);
     if (!err.empty()) { delete m; return fail(NMG_EMESH, err); }
   } catch (const std::bad_alloc &) {

@@ -223,3 +223,26 @@ def test_periodic_self_neighbour_face_table(luni):
             assert f2 == (f ^ 1) and o == 0
             idx = nmo.face_plane_index(4, f2)
             assert np.array_equal(ref[e, f], nb[e, f] * npt + idx)
+
+
+@pytest.mark.parametrize("case", NC_CASES)
+def test_described_mesh_finds_nonconforming_faces(case):
+    """A mesh given element by element (what the nmesh adapter packs from a
+    tMesh: patch, bbox, x, dXdx) gets each element's level from its bbox
+    and the same face table and non-conforming lists as the generated mesh."""
+    d, meta = load(case)
+    m = build_mesh(meta)
+    pat, bbox = m.elements()
+    curvi = (pat > 0).astype(np.int32) if meta["mesh"] == "cs7" else np.zeros(len(pat), np.int32)
+    md = ng.Mesh.from_arrays(bbox, curvi, m.coords(), m.dXdx(), pat=pat)
+    for a, b in zip(m.faces() + m.hanging(), md.faces() + md.hanging()):
+        assert np.array_equal(a, b)
+
+
+def test_level_jump_of_two_rejected():
+    """Two nested spheres of radius 2 and 4 on a level-1 cubed-sphere mesh
+    put level-3 cube elements against level-1 shells: not built, and the
+    build says so instead of leaving those faces outer."""
+    with pytest.raises(ng.NmgError, match="level jump"):
+        ng.Mesh.build(ng.MESH_CUBEDSPHERES7, n=4, luni=1, cs_dc=1.0, cs_r0fac=20.0,
+                      sphere_levels=2, sphere_radius=2)
