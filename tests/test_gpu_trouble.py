@@ -165,7 +165,10 @@ def _oracle_step(S, u, types, scores, t, dt, kw, notroubles):
     return u, types, scores, (nfv, ndg)
 
 
-def test_rk4_step_trouble_matches_oracle_flow():
+@pytest.mark.parametrize("filt", [False, True])
+def test_rk4_step_trouble_matches_oracle_flow(filt):
+    """With filt the exponential filter (evolve_filter_all) follows every
+    step, on the element types the step ended with."""
     S = Setup(6, 2)
     xyz = S.mdg.coords()
     # a smooth wave in phi plus a ball of pi = 1: the ball's elements are
@@ -179,6 +182,8 @@ def test_rk4_step_trouble_matches_oracle_flow():
                           notroubles=2)
     ev = ng.Evolution(S.mdg, ng.BC_OUTGOING, switchable=True)
     ev.set_fv("WENOm5_2", "dnfn_extrap1")
+    if filt:
+        ev.set_filter(True, alp=36.0, s=4.0)
     ev.set_state(u)
     types = np.zeros(S.E, np.int32)
     scores = np.zeros(S.E, np.int64)
@@ -188,6 +193,8 @@ def test_rk4_step_trouble_matches_oracle_flow():
     for step in range(6):
         sw = ev.rk4_step_trouble(t, dt, tp)
         uo, types, scores, swo = _oracle_step(S, uo, types, scores, t, dt, kw, 2)
+        if filt:
+            uo = S.oracle(types).filter(uo, alp=36.0, s=4.0)
         assert sw == swo, step
         seen.add(sw)
         assert np.array_equal(ev.element_types(), types)
