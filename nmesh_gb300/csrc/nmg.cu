@@ -223,6 +223,12 @@ struct nmg_ctx {
   int *d_hoff = nullptr;    // [H*nn + 1] contribution offsets per face node
   int *d_hsrc = nullptr;    // [C][2] source element, source face
   double *d_hw = nullptr;   // [C][2][n] Lagrange weights at the node's position
+  // the transposed lists (adjoint): per slot and source-face node, the
+  // (slot * nn + node) pairs that read it and their weights; slot owners
+  int *d_toff = nullptr, *d_tsrc = nullptr, *d_hface = nullptr;
+  double *d_tw = nullptr;
+  std::vector<int32_t> h_hoff, h_hsrc, h_hface;
+  std::vector<double> h_hw;
   // switchable contexts: element types can change (nmg_set_element_types)
   bool switchable = false;
   std::vector<int32_t> h_nb, h_code0, h_bslot0, h_fv;  // face table without the mixed bit,
@@ -333,6 +339,21 @@ static cudaError_t run_stage(nmg_ctx *c, int v, StageParams P, bool traces = tru
 
 // one RK4 step u_in -> u_out with explicit stage buffers s1, s2, forward
 // (the selected variants) or transposed (vjp), enqueued on the context stream
+// one transposed stage: the non-conforming faces' adjoint slots from rbar,
+// then the transposed stage kernel
+static cudaError_t vjp_stage(nmg_ctx *c, const StageParams &P) {
+  cudaError_t e;
+  if (c->nhang > 0) {
+    e = nmgk::hang_adj_launch(c->nhang, c->n, c->d_toff, c->d_tsrc, c->d_tw, c->d_hface,
+                              c->d_cslot, c->d_fac, c->d_gcart, P.win, c->d_ghost, c->stream);
+    if (e != cudaSuccess) return e;
+    c->launches++;
+  }
+  e = c->vjp.launch(P, c->stream);
+  if (e == cudaSuccess) c->launches++;
+  return e;
+}
+
 static int step_buffers(nmg_ctx *c, bool vjp, double t, double dt, const double *u_in,
                         double *u_out, double *s1, double *s2) {
   const double cacc[4] = {dt / 6., dt / 3., dt / 3., dt / 6.};
@@ -352,8 +373,7 @@ static int step_buffers(nmg_ctx *c, bool vjp, double t, double dt, const double 
     P.t = ts[s];
     cudaError_t e;
     if (vjp) {
-      e = c->vjp.launch(P, c->stream);
-      if (e == cudaSuccess) c->launches++;
+      e = vjp_stage(c, P);
     } else {
       e = run_stage(c, c->sel >= 0 ? c->sel : 0, P);
     }
@@ -1138,6 +1158,11 @@ static int create_impl(const nmg_mesh *m, int32_t bc_kind, const double k[3], bo
     CK(up(&c->d_hoff, m->hoff));
     CK(up(&c->d_hsrc, m->hsrc));
     CK(up(&c->d_hw, hw));
+    // host copies for the transposed lists, built on the first adjoint call
+    c->h_hoff = m->hoff;
+    c->h_hsrc = m->hsrc;
+    c->h_hface = m->hface;
+    c->h_hw = hw;
     CK(cudaMalloc((void **)&c->d_ghost, sizeof(double) * 4 * nn * H));
     CK(cudaMemset(c->d_ghost, 0, sizeof(double) * 4 * nn * H));
     c->ghost_cap = (int)H;
@@ -1737,7 +1762,8 @@ void nmg_destroy(nmg_ctx *c) {
   cudaFree(c->d_D);
   cudaFree(c->d_fvgeo); cudaFree(c->d_fvdist); cudaFree(c->d_fvdxb);
   cudaFree(c->d_fvlist); cudaFree(c->d_gtab); cudaFree(c->d_isfv); cudaFree(c->d_ghost);
-  cudaFree(c->d_hoff); cudaFree(c->d_hsrc); cudaFree(c->d_hw); cudaFree(c->d_fvmid);
+  cudaFree(c->d_hoff); cudaFree(c->d_hsrc); cudaFree(c->d_hw);
+  cudaFree(c->d_toff); cudaFree(c->d_tsrc); cudaFree(c->d_tw); cudaFree(c->d_hface); cudaFree(c->d_fvmid);
   cudaFree(c->d_filt); cudaFree(c->d_fooj);
   cudaFree(c->d_gM); cudaFree(c->d_fvbxyz); cudaFree(c->d_fvbnrm); cudaFree(c->d_PR);
   cudaFree(c->d_conv); cudaFree(c->d_mm); cudaFree(c->d_trb); cudaFree(c->d_score);
@@ -2111,6 +2137,62 @@ int nmg_rk4_steps_host(nmg_ctx *c, double t, double dt, int32_t nsteps, double *
 // ---------------------------------------------------------------------------
 // adjoint (vector-Jacobian) entry points
 // ---------------------------------------------------------------------------
+// The transposed non-conforming lists (first adjoint call): contribution q
+// of slot h, node t reads source node (j, k) of the source face, which is
+// itself slot h2, with weight B1[j] B2[k] / (contributions of the node).
+static int ensure_hang_transpose(nmg_ctx *c) {
+  if (c->nhang <= 0 || c->d_toff) return NMG_OK;
+  const int n = c->n, nn = n * n;
+  const int64_t H = c->nhang;
+  std::vector<int64_t> slot_of(c->nelem * 6, -1);
+  for (int64_t h = 0; h < H; h++) slot_of[(int64_t)c->h_hface[2 * h] * 6 + c->h_hface[2 * h + 1]] = h;
+  std::vector<int> cnt((size_t)H * nn + 1, 0);
+  for (int pass = 0; pass < 2; pass++) {
+    std::vector<int> toff, tsrc;
+    std::vector<double> tw;
+    if (pass == 1) {
+      toff.assign((size_t)H * nn + 1, 0);
+      for (size_t q = 0; q < (size_t)H * nn; q++) toff[q + 1] = toff[q] + cnt[q];
+      tsrc.assign(std::max(toff.back(), 1), 0);
+      tw.assign(tsrc.size(), 0.);
+    }
+    std::vector<int> fill(pass == 1 ? toff.begin() : toff.end(), toff.end());
+    for (int64_t h = 0; h < H; h++)
+      for (int t = 0; t < nn; t++) {
+        const int c0 = c->h_hoff[h * nn + t], c1 = c->h_hoff[h * nn + t + 1];
+        const double inv = c1 - c0 > 1 ? 1. / (c1 - c0) : 1.;
+        for (int q = c0; q < c1; q++) {
+          const int64_t h2 = slot_of[(int64_t)c->h_hsrc[2 * q] * 6 + c->h_hsrc[2 * q + 1]];
+          if (h2 < 0) return set_err(c, NMG_EMESH, "non-conforming source face without a slot");
+          for (int k = 0; k < n; k++)
+            for (int j = 0; j < n; j++) {
+              const size_t at = (size_t)h2 * nn + j + n * k;
+              if (pass == 0) {
+                cnt[at]++;
+              } else {
+                const int i = fill[at]++;
+                tsrc[i] = (int)(h * nn + t);
+                tw[i] = c->h_hw[(q * 2) * n + j] * c->h_hw[(q * 2 + 1) * n + k] * inv;
+              }
+            }
+        }
+      }
+    if (pass == 1) {
+      auto up = [&](auto **dst, const auto &vec) -> cudaError_t {
+        const size_t bytes = vec.size() * sizeof(vec[0]);
+        cudaError_t e2 = cudaMalloc((void **)dst, std::max<size_t>(bytes, 16));
+        if (e2 != cudaSuccess || bytes == 0) return e2;
+        return cudaMemcpy(*dst, vec.data(), bytes, cudaMemcpyHostToDevice);
+      };
+      CK(up(&c->d_tsrc, tsrc));
+      CK(up(&c->d_tw, tw));
+      CK(up(&c->d_hface, c->h_hface));
+      CK(up(&c->d_toff, toff));  // last: marks the lists complete
+    }
+  }
+  return NMG_OK;
+}
+
 int nmg_rhs_vjp(nmg_ctx *c, double t, const double *w_dev, const double *rbar_dev,
                 double *wbar_dev) {
   (void)t;
@@ -2118,15 +2200,14 @@ int nmg_rhs_vjp(nmg_ctx *c, double t, const double *w_dev, const double *rbar_de
   if (!c || !rbar_dev || !wbar_dev || rbar_dev == wbar_dev)
     return set_err(c, NMG_EINVAL, "nmg_rhs_vjp: need distinct rbar and wbar device buffers");
   if (c->fv) return set_err(c, NMG_EUNSUP, "nmg_rhs_vjp: finite-volume RHS is nonlinear");
-  if (c->nhang) return set_err(c, NMG_EUNSUP, "nmg_rhs_vjp: no transposed non-conforming faces");
   if (c->numflux != NMG_NUMFLUX_LLF)
     return set_err(c, NMG_EUNSUP, "nmg_rhs_vjp: the transposed kernel implements LLF only");
+  if (int rc = ensure_hang_transpose(c)) return rc;
   StageParams P = base_params(c);
   P.win = rbar_dev;
   P.rout = wbar_dev;
   P.mode = 0;
-  CK(c->vjp.launch(P, c->stream));
-  c->launches++;
+  CK(vjp_stage(c, P));
   CK(cudaStreamSynchronize(c->stream));
   return NMG_OK;
 }
@@ -2135,11 +2216,12 @@ int nmg_rk4_step_vjp(nmg_ctx *c, double t, double dt, const double *u_n_dev, dou
   (void)u_n_dev;  // linear RHS: the step's Jacobian is P(dt L), independent of u_n
   if (!c || !ubar_dev) return set_err(c, NMG_EINVAL, "nmg_rk4_step_vjp: null argument");
   if (c->fv) return set_err(c, NMG_EUNSUP, "nmg_rk4_step_vjp: finite-volume RHS is nonlinear");
-  if (c->nhang) return set_err(c, NMG_EUNSUP, "nmg_rk4_step_vjp: no transposed non-conforming faces");
   if (c->numflux != NMG_NUMFLUX_LLF)
     return set_err(c, NMG_EUNSUP, "nmg_rk4_step_vjp: the transposed kernel implements LLF only");
+  int rc = ensure_hang_transpose(c);
+  if (rc) return rc;
   double *acc = c->d_buf[1 - c->cur];  // free between steps
-  int rc = step_buffers(c, true, t, dt, ubar_dev, acc, c->d_buf[2], c->d_buf[3]);
+  rc = step_buffers(c, true, t, dt, ubar_dev, acc, c->d_buf[2], c->d_buf[3]);
   if (rc) return rc;
   CK(cudaMemcpyAsync(ubar_dev, acc, c->state_len * sizeof(double), cudaMemcpyDeviceToDevice,
                      c->stream));
@@ -2153,14 +2235,13 @@ int nmg_rk4_step_vjp(nmg_ctx *c, double t, double dt, const double *u_n_dev, dou
 int nmg_adjoint_gradient(nmg_ctx *c, double t0, double dt, int32_t nsteps, int32_t ckpt_every,
                          const double *weight_dev, double *J, double *grad_dev) {
   if (c && c->fv) return set_err(c, NMG_EUNSUP, "nmg_adjoint_gradient: finite-volume RHS is nonlinear");
-  if (c && c->nhang)
-    return set_err(c, NMG_EUNSUP, "nmg_adjoint_gradient: no transposed non-conforming faces");
   if (c && c->numflux != NMG_NUMFLUX_LLF)
     return set_err(c, NMG_EUNSUP, "nmg_adjoint_gradient: the transposed kernel implements LLF only");
   if (!c || !weight_dev || !J || !grad_dev || nsteps <= 0 || ckpt_every <= 0)
     return set_err(c, NMG_EINVAL, "nmg_adjoint_gradient: bad argument");
   int rc = autotune(c);
   if (rc) return rc;
+  if ((rc = ensure_hang_transpose(c))) return rc;
   const size_t L = c->state_len, bytes = L * sizeof(double);
   const int K = ckpt_every, nck = (nsteps + K - 1) / K;
   const int np = c->np, E = (int)c->nelem;

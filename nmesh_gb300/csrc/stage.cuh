@@ -392,6 +392,13 @@ cudaError_t filter_launch(int n, int nelem, double *u, const unsigned char *isfv
 // over its contributions of the source face interpolated at the node
 cudaError_t hang_launch(int nhang, int n, const int *hoff, const int *hsrc, const double *hw,
                         const double *win, double *ghost, cudaStream_t st);
+// adjoint of those traces: per slot, field and face node, the sum over the
+// (slot, node) pairs that read that source-face node of weight times the
+// lift adjoint of rbar there (toff/tsrc/tw: the transposed list)
+cudaError_t hang_adj_launch(int nhang, int n, const int *toff, const int *tsrc, const double *tw,
+                            const int *hface, const int *cslot, const double *fac,
+                            const double *gcart, const double *rbar, double *out,
+                            cudaStream_t st);
 cudaError_t ghost_launch(int nghost, int n, const int *gtab, const unsigned char *isfv,
                          const double *M, const double *win, double *ghost, cudaStream_t st);
 // u of the listed elements <- (M x M x M) u (all fields), in place

@@ -526,8 +526,17 @@ __global__ void __launch_bounds__(NT) vjp_kernel(StageParams P) {
         dc0 = -fma(gn0, rp, g * rc0);
         dc1 = -fma(gn1, rp, g * rc1);
         dc2 = -fma(gn2, rp, g * rc2);
-        if (nbe >= 0) {
-          const int cd = __ldg(P.code + e * 6 + f), f2 = cd & 7, o = cd >> 3;
+        const int cdh = nbe >= 0 ? __ldg(P.code + e * 6 + f) : 0;
+        if (cdh & kCodeMixed) {
+          // non-conforming face: the neighbours' part, transposed through
+          // the trace interpolation, waits in this face's slot
+          const double *T = P.ghost + (size_t)__ldg(P.bslot + e * 6 + f) * 4 * NN + ab;
+          dp += T[0];
+          dc0 += T[NN];
+          dc1 += T[2 * NN];
+          dc2 += T[3 * NN];
+        } else if (nbe >= 0) {
+          const int cd = cdh, f2 = cd & 7, o = cd >> 3;
           const int sw = o & 1, fa = (o >> 1) & 1, fb = (o >> 2) & 1;
           int aa = sw ? b : a, bb = sw ? a : b;
           aa = fa ? N - 1 - aa : aa;

@@ -663,7 +663,70 @@ __global__ void __launch_bounds__(256) hang_kernel(int nhang, int n, const int *
     ghost[(size_t)h * 4 * nn + l * nn + ab] = acc;
   }
 }
+
+// Transpose of the non-conforming traces for the adjoint: the neighbour part
+// of a face lift (g d pi + gn . d c, gn d pi + g d c) on slot h's face, with
+// d the trace, becomes, per field, the adjoint tb = (g rbar_pi + gn . rbar_c,
+// gn rbar_pi + g rbar_c) at the owner's face node; every trace value is a
+// weighted sum of source-face values, so each source-face node of each
+// non-conforming face gathers sum w tb over the (slot, node) pairs that read
+// it (toff/tsrc/tw: that list, built on the host from the forward one).
+// The sums land in the slot of the source face, where the transposed stage
+// kernel adds them to the face's interior-side terms.
+__global__ void __launch_bounds__(256) hang_adj_kernel(int nhang, int n, const int *toff,
+                                                      const int *tsrc, const double *tw,
+                                                      const int *hface, const int *cslot,
+                                                      const double *fac, const double *gcart,
+                                                      const double *rbar, double *out) {
+  const int nn = n * n, np = nn * n;
+  const int64_t total = (int64_t)nhang * 4 * nn;
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    const int h2 = (int)(q / (4 * nn)), rem = (int)(q - (int64_t)h2 * 4 * nn);
+    const int l = rem / nn, jk = rem - l * nn;
+    const int i0 = __ldg(toff + (size_t)h2 * nn + jk), i1 = __ldg(toff + (size_t)h2 * nn + jk + 1);
+    double acc = 0.;
+    for (int i = i0; i < i1; i++) {
+      const int src = __ldg(tsrc + i), h = src / nn, t = src - h * nn;
+      const int e = __ldg(hface + 2 * h), f = __ldg(hface + 2 * h + 1), d = f >> 1;
+      const int node = fv_exact::fnode(n, f, t % n, t / n);
+      const double *R = rbar + (size_t)e * NF * np + node;
+      const double rp = __ldg(R), r0 = __ldg(R + np), r1 = __ldg(R + 2 * np), r2 = __ldg(R + 3 * np);
+      double gn0, gn1, gn2, g;
+      const int cs = __ldg(cslot + e);
+      if (cs < 0) {
+        g = __ldg(gcart + e * 3 + d);
+        const double sg = (f & 1) ? g : -g;
+        gn0 = d == 0 ? sg : 0.;
+        gn1 = d == 1 ? sg : 0.;
+        gn2 = d == 2 ? sg : 0.;
+      } else {
+        const double *F4 = fac + (((size_t)cs * 6 + f) * nn + t) * 4;
+        gn0 = __ldg(F4); gn1 = __ldg(F4 + 1); gn2 = __ldg(F4 + 2); g = __ldg(F4 + 3);
+      }
+      double tb;
+      if (l == 0) tb = g * rp + (gn0 * r0 + gn1 * r1 + gn2 * r2);
+      else if (l == 1) tb = gn0 * rp + g * r0;
+      else if (l == 2) tb = gn1 * rp + g * r1;
+      else tb = gn2 * rp + g * r2;
+      acc += __ldg(tw + i) * tb;
+    }
+    out[(size_t)h2 * 4 * nn + l * nn + jk] = acc;
+  }
+}
 }  // namespace
+
+cudaError_t hang_adj_launch(int nhang, int n, const int *toff, const int *tsrc, const double *tw,
+                            const int *hface, const int *cslot, const double *fac,
+                            const double *gcart, const double *rbar, double *out,
+                            cudaStream_t st) {
+  if (nhang <= 0) return cudaSuccess;
+  const int64_t total = (int64_t)nhang * 4 * n * n;
+  const int grid = (int)std::min<int64_t>((total + 255) / 256, 152 * 16);
+  hang_adj_kernel<<<grid, 256, 0, st>>>(nhang, n, toff, tsrc, tw, hface, cslot, fac, gcart, rbar,
+                                        out);
+  return cudaGetLastError();
+}
 
 cudaError_t hang_launch(int nhang, int n, const int *hoff, const int *hsrc, const double *hw,
                         const double *win, double *ghost, cudaStream_t st) {

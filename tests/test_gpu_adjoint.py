@@ -24,6 +24,12 @@ def _dev(a):
 def _mesh(kind, n, luni):
     if kind == "cs7":
         return ng.Mesh.build(ng.MESH_CUBEDSPHERES7, n=n, luni=luni, cs_dc=1.0, cs_r0fac=20.0)
+    if kind == "cs7h":   # inner cube one level finer (non-conforming faces)
+        return ng.Mesh.build(ng.MESH_CUBEDSPHERES7, n=n, luni=luni, cs_dc=1.0, cs_r0fac=20.0,
+                             hrefine=(0,))
+    if kind == "boxs":   # nested spheres about the corner x = 0: jumps inside the patch
+        return ng.Mesh.build(ng.MESH_BOX, n=n, luni=luni, xc=(PI, PI, PI), box_dout=PI,
+                             sphere_levels=2, sphere_radius=2)
     return ng.Mesh.build(ng.MESH_BOX, n=n, luni=luni, xc=(PI, PI, PI), box_dout=PI,
                          periodic=True)
 
@@ -35,7 +41,10 @@ def _rel(a, b):
 @pytest.mark.parametrize("kind,n,luni,bc", [("cs7", 5, 1, ng.BC_OUTGOING),
                                             ("cs7", 9, 0, ng.BC_EXACT_PLANEWAVE),
                                             ("cs7", 4, 1, ng.BC_EXACT_PLANEWAVE),
-                                            ("box", 6, 1, ng.BC_EXACT_PLANEWAVE)])
+                                            ("box", 6, 1, ng.BC_EXACT_PLANEWAVE),
+                                            ("cs7h", 5, 0, ng.BC_OUTGOING),
+                                            ("cs7h", 4, 1, ng.BC_EXACT_PLANEWAVE),
+                                            ("boxs", 5, 1, ng.BC_OUTGOING)])
 def test_rhs_vjp_dot_product(kind, n, luni, bc):
     import torch
     m = _mesh(kind, n, luni)
@@ -52,7 +61,8 @@ def test_rhs_vjp_dot_product(kind, n, luni, bc):
     assert _rel(np.vdot(w, Lv), np.vdot(LTw, v)) < 1e-12
 
 
-@pytest.mark.parametrize("kind,n,luni", [("cs7", 5, 1), ("box", 4, 2)])
+@pytest.mark.parametrize("kind,n,luni", [("cs7", 5, 1), ("box", 4, 2), ("cs7h", 5, 0),
+                                         ("boxs", 4, 1)])
 def test_rk4_step_vjp_dot_product(kind, n, luni):
     import torch
     m = _mesh(kind, n, luni)
@@ -90,10 +100,11 @@ def _oracle_J(o, u0, W, dt, nsteps):
     return J
 
 
-@pytest.mark.parametrize("nsteps,ckpt", [(12, 5), (8, 1), (6, 6)])
-def test_gradient_matches_central_differences(nsteps, ckpt):
+@pytest.mark.parametrize("kind,nsteps,ckpt", [("cs7", 12, 5), ("cs7", 8, 1), ("cs7", 6, 6),
+                                              ("cs7h", 6, 4)])
+def test_gradient_matches_central_differences(kind, nsteps, ckpt):
     import torch
-    m = _mesh("cs7", 5, 1)
+    m = _mesh(kind, 5, 1)
     ev = ng.Evolution(m, ng.BC_OUTGOING)
     u0 = gaussian_pulses(m.coords(), seed=7, rmin=2.0, rmax=5.0)
     W = _shell_weight(m)

@@ -84,12 +84,6 @@ def test_unsupported_combinations_rejected():
     fvm = ng.Mesh.build(ng.MESH_CUBEDSPHERES7, n=5, luni=0, fv=[0], hrefine=(0,))
     with pytest.raises(ng.NmgError):
         ng.Evolution(fvm, ng.BC_OUTGOING)
-    ev = ng.Evolution(m, ng.BC_OUTGOING)
-    import torch
-    x = torch.zeros(ev.size, dtype=torch.float64, device="cuda")
-    y = torch.zeros_like(x)
-    with pytest.raises(ng.NmgError):
-        ev.rhs_vjp_device(x.data_ptr(), y.data_ptr())
 
 
 @pytest.mark.parametrize("mode", [0, 1])
