@@ -386,7 +386,9 @@ void *nmg_batch_stream(nmg_batch *b);
 /* The reference has no adjoint; these are the hand-written transposes of
  * the RHS and of the RK4 step above.  The scalar-wave RHS is linear in w, so
  * wbar = (dRHS/dw)^T rbar does not depend on w (w_dev may be NULL) and the
- * exterior plane-wave data (constant in w) drops out.
+ * exterior plane-wave data (constant in w) drops out.  Non-conforming faces
+ * are transposed too (their lists are built on the first adjoint call);
+ * finite-volume contexts are rejected (NMG_EUNSUP).
  *   nmg_rhs_vjp:       wbar_dev = J^T rbar_dev (device buffers, distinct)
  *   nmg_rk4_step_vjp:  ubar_dev <- (du_{n+1}/du_n)^T ubar_dev, in place; the
  *                      step Jacobian is the RK4 polynomial of dt L, so this is
