@@ -335,6 +335,22 @@ int nmg_set_fv_midpoint_data(nmg_ctx *c, int32_t on);
  * switches it off.  Applied by the step entry points (nmg_rk4_step(s),
  * nmg_evolve_steps, the host round trips, nmg_rk4_step_trouble); not by
  * the adjoint, the batches and the allocation-free step. */
+/* The reference's scalarwave1_limiter = MRS with limiter_alpha (limdata_MRS
+ * / limiter_MRS, src/main/limiter/limiter.c:61-204, applied as
+ * evolve_limiter_mesh does: to w before every later stage, RungeKutta.c:
+ * 45-67,161,173, and to the new u after the step, evolve.c:143-144).  Per
+ * element theta = min(1, min over fields of phi((M - wbar) / (wM - wbar)),
+ * phi(y) = min(y/1.1, 1) (0 for y < 0), with M the neighbours' extrema
+ * widened to wbar +- alpha h^1.5) and u <- wbar + theta (u - wbar).  kind:
+ * NMG_LIMITER_NONE or NMG_LIMITER_MRS (minmodB is not built).  Applied by
+ * nmg_rk4_step(s), nmg_evolve_steps and the host round trips; the trouble
+ * flow and the adjoint reject a context with the limiter on (NMG_EUNSUP).
+ * nmg_get_limited: per element 1 if the last limiter call limited it. */
+#define NMG_LIMITER_NONE 0
+#define NMG_LIMITER_MRS 1
+int nmg_set_limiter(nmg_ctx *c, int32_t kind, double alpha);
+int nmg_get_limited(nmg_ctx *c, int32_t *limited);
+
 int nmg_set_filter(nmg_ctx *c, int32_t on, double alp, double s, int32_t dn, int32_t jpower,
                    int32_t filter_fv);
 

@@ -193,6 +193,8 @@ def lib(build_if_missing=True):
         "nmg_set_fv_surface_interp": (ctypes.c_int, [vp, i32]),
         "nmg_set_fv_midpoint_data": (ctypes.c_int, [vp, i32]),
         "nmg_set_filter": (ctypes.c_int, [vp, i32, f64, f64, i32, i32, i32]),
+        "nmg_set_limiter": (ctypes.c_int, [vp, i32, f64]),
+        "nmg_get_limited": (ctypes.c_int, [vp, vp]),
         "nmg_mesh_get_midpoint_dXdx": (ctypes.c_int, [vp, vp]),
         "nmg_mesh_auto_dt": (ctypes.c_int, [vp, f64, f64, vp]),
         "nmg_evolve_steps": (ctypes.c_int, [vp, f64, f64, i32]),
@@ -538,6 +540,18 @@ class Evolution:
         after every step; defaults as the reference's parameters)."""
         self._check(lib().nmg_set_filter(self._h, int(bool(on)), float(alp), float(s), int(dn),
                                          int(jpower), int(bool(filter_fv))), "nmg_set_filter")
+
+    def set_limiter(self, kind="MRS", alpha=5.0):
+        """The reference's scalarwave1_limiter ("none" or "MRS") with
+        limiter_alpha (default 5)."""
+        k = {"none": 0, "MRS": 1, "minmodB": 2}[kind]  # minmodB: rejected by the library
+        self._check(lib().nmg_set_limiter(self._h, k, float(alpha)), "nmg_set_limiter")
+
+    def limited(self):
+        """Per element 1 if the last limiter call limited it."""
+        out = np.zeros(self.shape[0], np.int32)
+        self._check(lib().nmg_get_limited(self._h, _ptr(out)), "nmg_get_limited")
+        return out
 
     def set_fv_midpoint_data(self, on=True):
         """The reference's coordinates_midpoint_data = yes: FV midpoint flux

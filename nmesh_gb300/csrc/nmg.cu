@@ -256,6 +256,11 @@ struct nmg_ctx {
   bool fv_mid = false;
   // exponential filter after each step (evolve_filter_all = yes)
   bool filter_on = false;
+  // MRS limiter (scalarwave1_limiter = MRS): node averages / extrema, the
+  // face neighbours of every element (CSR), alpha h^1.5 per element
+  bool lim_on = false;
+  double *d_lim = nullptr, *d_alpha_h = nullptr, *d_wl = nullptr, *d_wu = nullptr;
+  int *d_lnboff = nullptr, *d_lnb = nullptr, *d_limited = nullptr;
   int filter_jpow = 1, filter_fv = 1;
   double *d_filt = nullptr;   // [2][nn] F of LGL and of equally spaced points
   double *d_fooj = nullptr;   // [cslot][np] det(dXb/dx) on the LGL points
@@ -526,6 +531,17 @@ static cudaError_t apply_filter(nmg_ctx *c, double *buf) {
   return e;
 }
 
+// evolve_limiter_mesh with the MRS limiter on buf (all elements)
+static cudaError_t apply_limiter(nmg_ctx *c, double *buf) {
+  if (!c->lim_on) return cudaSuccess;
+  cudaError_t e = nmgk::limiter_launch(c->n, (int)c->nelem, buf, c->mixed ? c->d_isfv : nullptr,
+                                       (c->fv && !c->mixed) ? 1 : 0, c->d_wl, c->d_wu, c->d_lim,
+                                       c->d_lnboff, c->d_lnb, c->d_alpha_h, c->d_limited,
+                                       c->stream);
+  if (e == cudaSuccess) c->launches += 2;
+  return e;
+}
+
 static int launch_stage(nmg_ctx *c, const StageParams &P) {
   int rc = autotune(c);
   if (rc) return rc;
@@ -565,7 +581,9 @@ static int enqueue_step_other(nmg_ctx *c, int cur, double t, double dt, bool dev
     }
     int rc = launch_stage(c, P);
     if (rc) return rc;
+    if (P.wout) CK(apply_limiter(c, P.wout));  // RungeKutta.c:161,173
   }
+  CK(apply_limiter(c, ACC));
   return NMG_OK;
 }
 
@@ -599,7 +617,10 @@ static int enqueue_step(nmg_ctx *c, int cur, double t, double dt, bool devtime,
     }
     int rc = launch_stage(c, P);
     if (rc) return rc;
+    // the reference limits w before each later stage (RungeKutta.c:45-67)
+    if (P.wout) CK(apply_limiter(c, P.wout));
   }
+  CK(apply_limiter(c, ACC));  // and the new u after the step (evolve.c:143-144)
   return NMG_OK;
 }
 
@@ -1492,6 +1513,8 @@ int nmg_rk4_step_trouble(nmg_ctx *c, double t, double dt, const nmg_trouble_para
   if (!c || !tp) return set_err(c, NMG_EINVAL, "nmg_rk4_step_trouble: null argument");
   if (!c->switchable)
     return set_err(c, NMG_EUNSUP, "nmg_rk4_step_trouble: context is not switchable");
+  if (c->lim_on)
+    return set_err(c, NMG_EUNSUP, "nmg_rk4_step_trouble: the limiter is not built into the trouble flow");
   if (tp->redo != NMG_REDO_STEP && tp->redo != NMG_REDO_SUBSTEP)
     return set_err(c, NMG_EINVAL, "nmg_rk4_step_trouble: unknown redo mode");
   int rc = ensure_trouble_buffers(c);
@@ -1588,6 +1611,78 @@ int nmg_set_fv_surface_interp(nmg_ctx *c, int32_t mode) {
   CK(cudaStreamSynchronize(c->stream));
   CK(cudaMemcpy(c->d_gM + nn, M1.data(), sizeof(double) * nn, cudaMemcpyHostToDevice));
   c->fv_surf = mode;
+  return NMG_OK;
+}
+
+int nmg_set_limiter(nmg_ctx *c, int32_t kind, double alpha) {
+  if (!c) return NMG_EINVAL;
+  if (kind != NMG_LIMITER_NONE && kind != NMG_LIMITER_MRS)
+    return set_err(c, NMG_EUNSUP, "nmg_set_limiter: only none and MRS are built");
+  if (kind == NMG_LIMITER_MRS && !(alpha >= 0.))
+    return set_err(c, NMG_EINVAL, "nmg_set_limiter: alpha must be >= 0");
+  drop_graphs(c);
+  if (kind == NMG_LIMITER_NONE) {
+    c->lim_on = false;
+    return NMG_OK;
+  }
+  const int n = c->n;
+  const int64_t E = c->nelem;
+  if (!c->d_lnboff) {
+    // face neighbours (nfnb / nbindc): the neighbour element of a
+    // conforming face, every source element of a non-conforming one
+    std::vector<std::vector<int>> extra(E * 6);
+    const int nn = n * n;
+    for (int64_t h = 0; h < c->nhang; h++) {
+      const int64_t q = (int64_t)c->h_hface[2 * h] * 6 + c->h_hface[2 * h + 1];
+      for (int cidx = c->h_hoff[h * nn]; cidx < c->h_hoff[(h + 1) * nn]; cidx++) {
+        const int e2 = c->h_hsrc[2 * cidx];
+        if (std::find(extra[q].begin(), extra[q].end(), e2) == extra[q].end())
+          extra[q].push_back(e2);
+      }
+    }
+    std::vector<int> off(1, 0), nbl;
+    for (int64_t e = 0; e < E; e++) {
+      for (int f = 0; f < 6; f++) {
+        const int64_t q = e * 6 + f;
+        if (!extra[q].empty()) nbl.insert(nbl.end(), extra[q].begin(), extra[q].end());
+        else if (c->h_nb[q] >= 0) nbl.push_back(c->h_nb[q]);
+      }
+      off.push_back((int)nbl.size());
+    }
+    if (nbl.empty()) nbl.push_back(0);
+    std::vector<double> x(n), wl(n), wu(n), D((size_t)n * n);
+    nmg::lgl_basis(n, x.data(), wl.data(), D.data());
+    nmg::uniform_basis(n, x.data(), wu.data(), D.data());
+    auto up = [&](auto **dst, const auto &vec) -> cudaError_t {
+      const size_t bytes = vec.size() * sizeof(vec[0]);
+      cudaError_t e2 = cudaMalloc((void **)dst, std::max<size_t>(bytes, 16));
+      if (e2 != cudaSuccess || bytes == 0) return e2;
+      return cudaMemcpy(*dst, vec.data(), bytes, cudaMemcpyHostToDevice);
+    };
+    CK(up(&c->d_lnb, nbl));
+    CK(up(&c->d_wl, wl));
+    CK(up(&c->d_wu, wu));
+    CK(cudaMalloc((void **)&c->d_lim, sizeof(double) * E * NF * 3));
+    CK(cudaMalloc((void **)&c->d_alpha_h, sizeof(double) * E));
+    CK(cudaMalloc((void **)&c->d_limited, sizeof(int) * E));
+    CK(up(&c->d_lnboff, off));  // last: marks the tables complete
+  }
+  // alpha_h = alpha h^1.5, h the largest bbox extent (limiter.c:121-124)
+  std::vector<double> ah(E);
+  for (int64_t e = 0; e < E; e++) {
+    const double *bb = &c->geom.bbox[e * 6];
+    const double h = std::max(bb[1] - bb[0], std::max(bb[3] - bb[2], bb[5] - bb[4]));
+    ah[e] = alpha * pow(h, 1.5);
+  }
+  CK(cudaMemcpy(c->d_alpha_h, ah.data(), sizeof(double) * E, cudaMemcpyHostToDevice));
+  c->lim_on = true;
+  return NMG_OK;
+}
+
+int nmg_get_limited(nmg_ctx *c, int32_t *limited) {
+  if (!c || !limited) return set_err(c, NMG_EINVAL, "nmg_get_limited: null argument");
+  if (!c->d_limited) return set_err(c, NMG_EUNSUP, "nmg_get_limited: no limiter set");
+  CK(cudaMemcpy(limited, c->d_limited, sizeof(int) * c->nelem, cudaMemcpyDeviceToHost));
   return NMG_OK;
 }
 
@@ -1765,6 +1860,8 @@ void nmg_destroy(nmg_ctx *c) {
   cudaFree(c->d_hoff); cudaFree(c->d_hsrc); cudaFree(c->d_hw);
   cudaFree(c->d_toff); cudaFree(c->d_tsrc); cudaFree(c->d_tw); cudaFree(c->d_hface); cudaFree(c->d_fvmid);
   cudaFree(c->d_filt); cudaFree(c->d_fooj);
+  cudaFree(c->d_lim); cudaFree(c->d_alpha_h); cudaFree(c->d_wl); cudaFree(c->d_wu);
+  cudaFree(c->d_lnboff); cudaFree(c->d_lnb); cudaFree(c->d_limited);
   cudaFree(c->d_gM); cudaFree(c->d_fvbxyz); cudaFree(c->d_fvbnrm); cudaFree(c->d_PR);
   cudaFree(c->d_conv); cudaFree(c->d_mm); cudaFree(c->d_trb); cudaFree(c->d_score);
   cudaFree(c->d_r); cudaFree(c->d_w2); cudaFree(c->d_ghost2); cudaFree(c->d_tlist);
@@ -2116,10 +2213,10 @@ int nmg_rk4_steps_host(nmg_ctx *c, double t, double dt, int32_t nsteps, double *
   if (nsteps < 0) return set_err(c, NMG_EINVAL, "nmg_rk4_steps_host: bad argument");
   const size_t bytes = c->state_len * sizeof(double);
   int rc;
-  if (!c->fv && !c->nhang && !c->filter_on && nsteps == 1)  // copy in, step, copy out overlapped
+  if (!c->fv && !c->nhang && !c->filter_on && !c->lim_on && nsteps == 1)  // copy in, step, copy out overlapped
     return last_step_streamed(c, t, dt, host_u, host_u);
   CK(cudaMemcpyAsync(c->d_buf[c->cur], host_u, bytes, cudaMemcpyHostToDevice, c->stream));
-  if (c->mixed || c->filter_on || nsteps == 0) {
+  if (c->mixed || c->filter_on || c->lim_on || nsteps == 0) {
     rc = nmg_rk4_steps(c, t, dt, nsteps);
     if (rc) return rc;
     CK(cudaMemcpyAsync(host_u, c->d_buf[c->cur], bytes, cudaMemcpyDeviceToHost, c->stream));
@@ -2200,6 +2297,7 @@ int nmg_rhs_vjp(nmg_ctx *c, double t, const double *w_dev, const double *rbar_de
   if (!c || !rbar_dev || !wbar_dev || rbar_dev == wbar_dev)
     return set_err(c, NMG_EINVAL, "nmg_rhs_vjp: need distinct rbar and wbar device buffers");
   if (c->fv) return set_err(c, NMG_EUNSUP, "nmg_rhs_vjp: finite-volume RHS is nonlinear");
+  if (c->lim_on) return set_err(c, NMG_EUNSUP, "nmg_rhs_vjp: the limiter is nonlinear");
   if (c->numflux != NMG_NUMFLUX_LLF)
     return set_err(c, NMG_EUNSUP, "nmg_rhs_vjp: the transposed kernel implements LLF only");
   if (int rc = ensure_hang_transpose(c)) return rc;
@@ -2216,6 +2314,7 @@ int nmg_rk4_step_vjp(nmg_ctx *c, double t, double dt, const double *u_n_dev, dou
   (void)u_n_dev;  // linear RHS: the step's Jacobian is P(dt L), independent of u_n
   if (!c || !ubar_dev) return set_err(c, NMG_EINVAL, "nmg_rk4_step_vjp: null argument");
   if (c->fv) return set_err(c, NMG_EUNSUP, "nmg_rk4_step_vjp: finite-volume RHS is nonlinear");
+  if (c->lim_on) return set_err(c, NMG_EUNSUP, "nmg_rk4_step_vjp: the limiter is nonlinear");
   if (c->numflux != NMG_NUMFLUX_LLF)
     return set_err(c, NMG_EUNSUP, "nmg_rk4_step_vjp: the transposed kernel implements LLF only");
   int rc = ensure_hang_transpose(c);
@@ -2235,6 +2334,7 @@ int nmg_rk4_step_vjp(nmg_ctx *c, double t, double dt, const double *u_n_dev, dou
 int nmg_adjoint_gradient(nmg_ctx *c, double t0, double dt, int32_t nsteps, int32_t ckpt_every,
                          const double *weight_dev, double *J, double *grad_dev) {
   if (c && c->fv) return set_err(c, NMG_EUNSUP, "nmg_adjoint_gradient: finite-volume RHS is nonlinear");
+  if (c && c->lim_on) return set_err(c, NMG_EUNSUP, "nmg_adjoint_gradient: the limiter is nonlinear");
   if (c && c->numflux != NMG_NUMFLUX_LLF)
     return set_err(c, NMG_EUNSUP, "nmg_adjoint_gradient: the transposed kernel implements LLF only");
   if (!c || !weight_dev || !J || !grad_dev || nsteps <= 0 || ckpt_every <= 0)

@@ -388,6 +388,11 @@ cudaError_t filter_launch(int n, int nelem, double *u, const unsigned char *isfv
                           const int *cslot, const double *oojdg, const double *fvgeo,
                           const double *scale, int jpow, int filter_fv, int allfv,
                           cudaStream_t st);
+// MRS limiter of every element of u: node averages and extrema (lim,
+// [e][field][3]), then u <- ubar + theta (u - ubar); limited[e] = theta < 1
+cudaError_t limiter_launch(int n, int nelem, double *u, const unsigned char *isfv, int allfv,
+                           const double *wl, const double *wu, double *lim, const int *nboff,
+                           const int *nbl, const double *alpha_h, int *limited, cudaStream_t st);
 // traces of non-conforming faces: per slot, field and face node the average
 // over its contributions of the source face interpolated at the node
 cudaError_t hang_launch(int nhang, int n, const int *hoff, const int *hsrc, const double *hw,

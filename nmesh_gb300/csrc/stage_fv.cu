@@ -34,6 +34,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cfloat>
 #include <cstdint>
 
 #include "stage.cuh"
@@ -918,11 +919,119 @@ __global__ void __launch_bounds__(256) trouble_kernel(int n, int nelem, const do
 }
 }  // namespace
 
+// MRS limiter (limdata_MRS / limiter_MRS, src/main/limiter/limiter.c:61-204):
+// per element and field the node average (the LGL or uniform quadrature
+// along x, then y, then z, times 1/8: var_nodeaverage, src/main/basis/
+// basis.c:462-510), the minimum and the maximum.
+__global__ void __launch_bounds__(256) limdata_kernel(int n, const double *u,
+                                                     const unsigned char *isfv, int allfv,
+                                                     const double *wl, const double *wu,
+                                                     double *lim) {
+  __shared__ double s1[256], red[2][256];
+  const int np = n * n * n, nn = n * n, e = blockIdx.x;
+  const bool efv = allfv || (isfv && isfv[e]);
+  const double *w = efv ? wu : wl;
+  for (int l = 0; l < NF; l++) {
+    const double *v = u + ((size_t)e * NF + l) * np;
+    for (int q = threadIdx.x; q < nn; q += blockDim.x) {  // q = j + n k
+      double s = 0.;
+      for (int i = 0; i < n; i++) s += __ldg(w + i) * v[i + n * q];
+      s1[q] = s;
+    }
+    double lo = v[0], hi = v[0];
+    for (int q = threadIdx.x; q < np; q += blockDim.x) {
+      lo = fmin(lo, v[q]);
+      hi = fmax(hi, v[q]);
+    }
+    red[0][threadIdx.x] = lo;
+    red[1][threadIdx.x] = hi;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+      if (threadIdx.x < h) {
+        red[0][threadIdx.x] = fmin(red[0][threadIdx.x], red[0][threadIdx.x + h]);
+        red[1][threadIdx.x] = fmax(red[1][threadIdx.x], red[1][threadIdx.x + h]);
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      double I = 0.;
+      for (int k = 0; k < n; k++) {
+        double t = 0.;
+        for (int j = 0; j < n; j++) t += __ldg(w + j) * s1[j + n * k];
+        I += __ldg(w + k) * t;
+      }
+      double *L = lim + ((size_t)e * NF + l) * 3;
+      L[0] = I * 0.125;
+      L[1] = red[0][0];
+      L[2] = red[1][0];
+    }
+    __syncthreads();
+  }
+}
+
+__device__ __forceinline__ double mrs_theta(double M, double wbar, double wM) {
+  const double den = wM - wbar;
+  if (den == 0.) return 1.;
+  const double y = (M - wbar) / den;
+  if (y < 0.) return 0.;
+  return fmin(y / 1.1, 1.);
+}
+
+// u <- ubar + theta (u - ubar) with theta = min(1, min over fields of the
+// MRS ratios against the neighbours' extrema widened by alpha h^1.5)
+__global__ void __launch_bounds__(256) limiter_kernel(int n, double *u, const double *lim,
+                                                     const int *nboff, const int *nbl,
+                                                     const double *alpha_h, int *limited) {
+  __shared__ double sth;
+  const int np = n * n * n, e = blockIdx.x;
+  if (threadIdx.x == 0) {
+    double thM = DBL_MAX, thm = DBL_MAX;
+    const double ah = __ldg(alpha_h + e);
+    for (int l = 0; l < NF; l++) {
+      const double *L = lim + ((size_t)e * NF + l) * 3;
+      const double wbar = L[0], wmi = L[1], wMi = L[2];
+      double Mi = -DBL_MAX, mi = DBL_MAX;
+      for (int k = __ldg(nboff + e); k < __ldg(nboff + e + 1); k++) {
+        const double *N = lim + ((size_t)__ldg(nbl + k) * NF + l) * 3;
+        if (N[1] < mi) mi = N[1];
+        if (N[2] > Mi) Mi = N[2];
+      }
+      mi = fmin(wbar - ah, mi);
+      Mi = fmax(wbar + ah, Mi);
+      const double a = mrs_theta(Mi, wbar, wMi), b = mrs_theta(mi, wbar, wmi);
+      if (a < thM) thM = a;
+      if (b < thm) thm = b;
+    }
+    sth = fmin(1., fmin(thm, thM));
+    limited[e] = sth < 1. ? 1 : 0;
+  }
+  __syncthreads();
+  const double th = sth;
+  if (th >= 1.) return;
+  for (int q = threadIdx.x; q < NF * np; q += blockDim.x) {
+    const int l = q / np;
+    const double qbar = lim[((size_t)e * NF + l) * 3];
+    double *v = u + (size_t)e * NF * np + q;
+    *v = qbar + th * (*v - qbar);
+  }
+}
+
 size_t filter_smem(int n) { return sizeof(double) * (3 * (size_t)n * n * n + (size_t)n * n); }
 
 cudaError_t filter_prepare(int n) {
   return cudaFuncSetAttribute(filter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)filter_smem(n));
+}
+
+cudaError_t limiter_launch(int n, int nelem, double *u, const unsigned char *isfv, int allfv,
+                           const double *wl, const double *wu, double *lim, const int *nboff,
+                           const int *nbl, const double *alpha_h, int *limited, cudaStream_t st) {
+  if (nelem <= 0) return cudaSuccess;
+  limdata_kernel<<<nelem, 256, 0, st>>>(n, u, isfv, allfv, wl, wu, lim);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  limiter_kernel<<<nelem, 256, 0, st>>>(n, u, lim, nboff, nbl, alpha_h, limited);
+  return cudaGetLastError();
 }
 
 cudaError_t filter_launch(int n, int nelem, double *u, const unsigned char *isfv, const double *F,

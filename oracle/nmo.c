@@ -60,6 +60,7 @@
  * Data layout: state arrays are [element][field][node], node = i + n*(j + n*k),
  * fields (pi, cx, cy, cz, phi) as in the reference's vlu (scalarwave1.c:669).
  */
+#include <float.h>
 #include <math.h>
 #include <stdint.h>
 #include <stdlib.h>
@@ -1289,6 +1290,107 @@ static void mm_dir(int n, const double *M, int d, const double *in, double *out)
    (k/(n-1-dn))^s), u = S^3 c, u -> u (1/J); A, S the normalised-Legendre
    analysis and synthesis matrices of the element's points (LGL: A_ij =
    w_j S_ji; equally spaced: A = S^-1, Legendre.c:277-310,723-729). */
+/* The MRS limiter of every element (limdata_MRS and limiter_MRS,
+   src/main/limiter/limiter.c:61-204, with var_nodeaverage,
+   src/main/basis/basis.c:462-510): node averages and extrema of all
+   elements first, then per element theta = min(1, min over fields of the
+   ratios against the face neighbours' extrema widened by alpha h^1.5) and
+   u <- ubar + theta (u - ubar).  limited (may be NULL): 1 where theta < 1. */
+static double mrs_theta(double M, double wbar, double wM)
+{
+  double den = wM - wbar, y;
+  if (den == 0.) return 1.;
+  y = (M - wbar) / den;
+  if (y < 0.) return 0.;
+  return y / 1.1 < 1. ? y / 1.1 : 1.;
+}
+
+int nmo_limiter_mrs(const nmo_mesh *m, double *u, double alpha, int32_t *limited)
+{
+  int n = m->n, np = n * n * n, nn = n * n, e, l, i, j, k, f, N = n - 1;
+  double wl[64], wu[64], x[64];
+  double *lim = (double *)malloc(sizeof(double) * (size_t)m->nelem * NF * 3);
+  int *nbs = (int *)malloc(sizeof(int) * 6 * 4 * nn);
+  if (!lim || !nbs) return 2;
+  nmo_lgl(n, x, wl);
+  for (i = 0; i <= N; i++) wu[i] = (i == 0 || i == N) ? 1. / N : 2. / N;
+  for (e = 0; e < m->nelem; e++) {
+    const double *w = (m->fv && m->fv[e]) ? wu : wl;
+    for (l = 0; l < NF; l++) {
+      const double *v = u + ((size_t)e * NF + l) * np;
+      double I = 0., lo = v[0], hi = v[0];
+      for (k = 0; k < n; k++) {
+        double t = 0.;
+        for (j = 0; j < n; j++) {
+          double s = 0.;
+          for (i = 0; i < n; i++) s += w[i] * v[i + n * (j + n * k)];
+          t += w[j] * s;
+        }
+        I += w[k] * t;
+      }
+      for (i = 0; i < np; i++) {
+        if (v[i] < lo) lo = v[i];
+        if (v[i] > hi) hi = v[i];
+      }
+      lim[((size_t)e * NF + l) * 3] = I * 0.125;
+      lim[((size_t)e * NF + l) * 3 + 1] = lo;
+      lim[((size_t)e * NF + l) * 3 + 2] = hi;
+    }
+  }
+  for (e = 0; e < m->nelem; e++) {
+    const double *bb = m->bbox + (size_t)e * 6;
+    double h = bb[1] - bb[0], ah, thM = DBL_MAX, thm = DBL_MAX, th;
+    int nnb = 0, q, c;
+    if (bb[3] - bb[2] > h) h = bb[3] - bb[2];
+    if (bb[5] - bb[4] > h) h = bb[5] - bb[4];
+    ah = alpha * pow(h, 1.5);
+    /* face neighbours: the element across a conforming face, every source
+       element of a non-conforming one */
+    for (f = 0; f < 6; f++) {
+      int64_t nb = m->nbnode[((size_t)e * 6 + f) * nn];
+      if (nb >= 0) nbs[nnb++] = (int)(nb / np);
+      else if (nb == -2) nbs[nnb++] = m->mixface[((size_t)e * 6 + f) * 3];
+      else if (nb == -3) {
+        int first = nnb;
+        for (q = 0; q < nn; q++) {
+          size_t qq = ((size_t)e * 6 + f) * nn + q;
+          for (c = m->hang_off[qq]; c < m->hang_off[qq + 1]; c++) {
+            int e2 = m->hang_src[2 * c], seen = 0, z;
+            for (z = first; z < nnb; z++) seen |= nbs[z] == e2;
+            if (!seen) nbs[nnb++] = e2;
+          }
+        }
+      }
+    }
+    for (l = 0; l < NF; l++) {
+      const double *L = lim + ((size_t)e * NF + l) * 3;
+      double wbar = L[0], wmi = L[1], wMi = L[2], Mi = -DBL_MAX, mi = DBL_MAX, a, b;
+      for (q = 0; q < nnb; q++) {
+        const double *B = lim + ((size_t)nbs[q] * NF + l) * 3;
+        if (B[1] < mi) mi = B[1];
+        if (B[2] > Mi) Mi = B[2];
+      }
+      mi = wbar - ah < mi ? wbar - ah : mi;
+      Mi = wbar + ah > Mi ? wbar + ah : Mi;
+      a = mrs_theta(Mi, wbar, wMi);
+      b = mrs_theta(mi, wbar, wmi);
+      if (a < thM) thM = a;
+      if (b < thm) thm = b;
+    }
+    th = thm < thM ? thm : thM;
+    if (th > 1.) th = 1.;
+    if (limited) limited[e] = th < 1.;
+    if (th < 1.)
+      for (l = 0; l < NF; l++) {
+        double qbar = lim[((size_t)e * NF + l) * 3], *v = u + ((size_t)e * NF + l) * np;
+        for (i = 0; i < np; i++) v[i] = qbar + th * (v[i] - qbar);
+      }
+  }
+  free(lim);
+  free(nbs);
+  return 0;
+}
+
 int nmo_filter(const nmo_mesh *m, double *u, double alp, double s, int dn, int jpow,
                int filter_fv)
 {

@@ -404,6 +404,40 @@ class OracleMesh:
             raise RuntimeError(f"nmo_evolve failed ({rc})")
         return u
 
+    def limit_mrs(self, u, alpha=5.0):
+        """The reference's MRS limiter of every element (limiter_MRS);
+        returns (limited u, per-element flag theta < 1)."""
+        u = np.array(u, np.float64, copy=True, order="C")
+        flags = np.zeros(self.s.nelem, np.int32)
+        rc = lib().nmo_limiter_mrs(ctypes.byref(self.s), u.ctypes.data_as(ctypes.c_void_p),
+                                   ctypes.c_double(alpha), flags.ctypes.data_as(ctypes.c_void_p))
+        if rc:
+            raise RuntimeError(f"nmo_limiter_mrs failed ({rc})")
+        return u, flags
+
+    def rk4_limited(self, u, dt, nsteps, alpha=5.0, t=0.0):
+        """RK4 steps as nmo_rk4 takes them, with the MRS limiter on w before
+        every later stage and on the new u (evolve_RK4_mesh with
+        scalarwave1_limiter = MRS, src/main/evolve/RungeKutta.c:19-82)."""
+        u = np.array(u, np.float64, copy=True)
+        c = (dt / 6., dt / 3., dt / 3., dt / 6.)
+        a = (dt / 2., dt / 2., dt)
+        te = np.longdouble(0.)
+        for _ in range(nsteps):
+            ts0 = float(np.longdouble(t) + te)
+            ts = (ts0, ts0 + 0.5 * dt, ts0 + 0.5 * dt, ts0 + dt)
+            u_p = u.copy()
+            w = u.copy()
+            for s in range(4):
+                r = self.rhs(w, ts[s])
+                u = u + c[s] * r
+                if s < 3:
+                    w = 1. * u_p + a[s] * r
+                    w = self.limit_mrs(w, alpha)[0]
+            u = self.limit_mrs(u, alpha)[0]
+            te += np.longdouble(dt)
+        return u
+
     def filter(self, u, alp=36.0, s=32.0, dn=0, jpow=1, filter_fv=True):
         """The reference's exponential filter of every element (evolve_filter_all)."""
         u = np.array(u, np.float64, copy=True, order="C")

@@ -178,6 +178,15 @@ CASES = {
                                dt=0.002, steps=2, eps=0.02, seed=43, sphere=(1, 3)),
     "sph_cs7_l1_n4_s1r6": dict(mesh="cs7", n=4, luni=1, k=(0.3, -0.2, 0.1),
                                dt=0.002, steps=2, eps=0.02, seed=44, sphere=(1, 6)),
+    # the MRS limiter (scalarwave1_limiter = MRS) with a small limiter_alpha
+    # so that noisy elements are limited
+    "lim_box_l1_n5_a0.01": dict(mesh="box", n=5, luni=1, k=(1.0, -0.5, 0.25),
+                                dt=0.002, steps=3, eps=0.3, seed=45, limiter=0.01),
+    "lim_cs7_l1_n4_a0.05": dict(mesh="cs7", n=4, luni=1, k=(0.3, -0.2, 0.1),
+                                dt=0.002, steps=2, eps=0.3, seed=46, limiter=0.05),
+    "lim_nc_cs7_l0_n5_h0_a0.02": dict(mesh="cs7", n=5, luni=0, k=(0.3, -0.2, 0.1),
+                                      dt=0.002, steps=2, eps=0.3, seed=47, hrefine="0",
+                                      limiter=0.02),
 }
 
 
@@ -216,6 +225,8 @@ def parfile(case, prefix):
         lines += ["evolve_filter_all = yes"]
     if c.get("hrefine"):
         lines += [f"amr_hrefine_p = {c['hrefine']}"]
+    if "limiter" in c:
+        lines += ["scalarwave1_limiter = MRS", f"limiter_alpha = {c['limiter']!r}"]
     if c.get("sphere"):
         lines += [f"amr_hrefine_sphere_levels = {c['sphere'][0]}",
                   f"amr_hrefine_sphere_radius = {c['sphere'][1]}"]

@@ -32,6 +32,8 @@ METHOD_NEAR_CASES = ["ssp3_mixcs7_l1_n6_wZdnfn", "ssp3_mixcs7_l0_n7_wZparab"]
 # oracle's matrix products sum in another order than the reference's
 # mm_array routines, so it matches these to
 FILT_CASES = ["filt_cs7_l1_n6", "filt_mixcs7_l0_n7"]
+# scalarwave1_limiter = MRS (limiter_alpha in meta["limiter"])
+LIM_CASES = ["lim_box_l1_n5_a0.01", "lim_cs7_l1_n4_a0.05", "lim_nc_cs7_l0_n5_h0_a0.02"]
 RTOL_FILT_ORACLE = 1e-13
 # dt = auto (the reference's dtfac * hmin; uniform_dtfac on FV elements)
 DTAUTO_CASES = ["dtauto_cs7_l1_n5", "dtauto_box_l2_n6", "dtauto_mixcs7_l0_n7"]

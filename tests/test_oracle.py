@@ -5,7 +5,7 @@ operation order and must match it bit for bit."""
 import numpy as np
 import pytest
 
-from helpers import (CASES, FILT_CASES, RTOL_FILT_ORACLE, FV_CASES, METHOD_CASES, METHOD_NEAR_CASES, MID_CASES,
+from helpers import (CASES, FILT_CASES, LIM_CASES, RTOL_FILT_ORACLE, FV_CASES, METHOD_CASES, METHOD_NEAR_CASES, MID_CASES,
                      MID_NEAR_CASES, MIX_CASES, MIX_NEAR_CASES, NC_CASES, RTOL_NC_ORACLE,
                      UPW_CASES, build_mesh, load, oracle_for, perm_to_mesh, rel_l2,
                      to_mesh_order)
@@ -220,3 +220,15 @@ def test_oracle_filter_matches_reference(case):
     for s in range(meta["steps"]):
         u = o.filter(o.rk4(u, meta["dt"], 1, t=s * meta["dt"]))
     assert rel_l2(u[perm], d["u_final"]) <= RTOL_FILT_ORACLE
+
+
+@pytest.mark.parametrize("case", LIM_CASES)
+def test_oracle_mrs_limiter_matches_reference(case):
+    """scalarwave1_limiter = MRS: w limited before every later RK4 stage and
+    the new u after the step (limiter_MRS with limiter_alpha)."""
+    d, meta = load(case)
+    m = _oracle_mesh(d, meta)
+    u = m.rk4_limited(d["u0"], meta["dt"], meta["steps"], alpha=meta["limiter"])
+    assert rel_l2(u, d["u_final"]) <= RTOL_NC_ORACLE
+    # without the limiter the run is far off: the limiter acts
+    assert rel_l2(m.rk4(d["u0"], meta["dt"], meta["steps"]), d["u_final"]) > 1e-3
