@@ -103,6 +103,12 @@ static void nmg_evolve_step(tMesh *mesh, int method)
   int E, np, e, f, iu[5];
   double t = mesh->time, dt = mesh->dt;
 
+  /* the reference limits w inside its own RK stages (RungeKutta.c:45-67)
+     and u again in evolve_mesh (evolve.c:144), which keeps running here:
+     the GPU stages would have to limit w only, so a limiter is refused */
+  if(!Getv(Par("scalarwave1_limiter"), "none"))
+    errorexit("nmg_evolve: use scalarwave1_limiter = none, or keep u resident and call "
+              "nmg_set_limiter");
   if(!nmg_evolve_ctx) nmg_evolve_setup(mesh);
   E = (int)mesh->nmyelm;
   np = mesh->myelm[0]->np;
