@@ -68,3 +68,25 @@ def test_limiter_flags_and_options_match_oracle():
     assert rel_l2(ev.rk4_steps_host(u, 0.0, dt, 2), o.rk4(u, dt, 2)) <= RTOL_RK4
     with pytest.raises(ng.NmgError):
         ng.Evolution(m, ng.BC_OUTGOING).set_limiter("minmodB")
+
+
+def test_limiter_rejected_where_not_built():
+    """The trouble flow and the adjoint refuse a context with the limiter on
+    (the limiter is nonlinear; the trouble flow's own limiter calls are not
+    built) instead of silently skipping it."""
+    import torch
+    m = ng.Mesh.build(ng.MESH_BOX, n=4, luni=1, xc=(0.0, 0.0, 0.0), box_dout=1.0, periodic=True)
+    ev = ng.Evolution(m, ng.BC_OUTGOING, switchable=True)
+    ev.set_fv("WENOm5_2", "dnfn_extrap1")
+    ev.set_limiter("MRS", 1.0)
+    ev.set_state(np.zeros(ev.shape))
+    with pytest.raises(ng.NmgError):
+        ev.rk4_step_trouble(0.0, 0.01, ng.TroubleParams())
+    dg = ng.Evolution(m, ng.BC_OUTGOING)
+    dg.set_limiter("MRS", 1.0)
+    x = torch.zeros(dg.size, dtype=torch.float64, device="cuda")
+    y = torch.zeros_like(x)
+    with pytest.raises(ng.NmgError):
+        dg.rhs_vjp_device(x.data_ptr(), y.data_ptr())
+    dg.set_limiter("none")
+    dg.rhs_vjp_device(x.data_ptr(), y.data_ptr())
