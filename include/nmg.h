@@ -333,8 +333,8 @@ int nmg_set_fv_midpoint_data(nmg_ctx *c, int32_t on);
  * _s, _dn, basis_expfilter_JacobianPower = p (0 or 1), basis_filter_fv;
  * evolve_filter_evosys_mesh, src/main/evolve/evolve.c:656-700).  on = 0
  * switches it off.  Applied by the step entry points (nmg_rk4_step(s),
- * nmg_evolve_steps, the host round trips, nmg_rk4_step_trouble); not by
- * the adjoint, the batches and the allocation-free step. */
+ * nmg_evolve_steps, the host round trips, nmg_rk4_step_trouble,
+ * nmg_rk4_step_noalloc); not by the adjoint and the batches. */
 /* The reference's scalarwave1_limiter = MRS with limiter_alpha (limdata_MRS
  * / limiter_MRS, src/main/limiter/limiter.c:61-204, applied as
  * evolve_limiter_mesh does: to w before every later stage, RungeKutta.c:
@@ -343,7 +343,8 @@ int nmg_set_fv_midpoint_data(nmg_ctx *c, int32_t on);
  * phi(y) = min(y/1.1, 1) (0 for y < 0), with M the neighbours' extrema
  * widened to wbar +- alpha h^1.5) and u <- wbar + theta (u - wbar).  kind:
  * NMG_LIMITER_NONE or NMG_LIMITER_MRS (minmodB is not built).  Applied by
- * nmg_rk4_step(s), nmg_evolve_steps and the host round trips; the trouble
+ * nmg_rk4_step(s), nmg_evolve_steps, the host round trips and
+ * nmg_rk4_step_noalloc; the trouble
  * flow and the adjoint reject a context with the limiter on (NMG_EUNSUP).
  * nmg_get_limited: per element 1 if the last limiter call limited it. */
 #define NMG_LIMITER_NONE 0
@@ -434,7 +435,9 @@ int nmg_adjoint_gradient(nmg_ctx *c, double t0, double dt, int32_t nsteps, int32
  * states are rejected with NMG_EINVAL.  The first call on a device looks up
  * that array (cudaGetSymbolAddress) and should come before any stream
  * capture.  All calls share the array: calls that overlap on the GPU race.
- * Nothing in it needs to start at zero.  Waits for the step to finish. */
+ * Nothing in it needs to start at zero.  The step is nmg_rk4_step's,
+ * including the context's limiter and filter.  The context's device must be
+ * current (NMG_EINVAL otherwise).  Waits for the step to finish. */
 #define NMG_NOALLOC_MAX_STATE 2097152
 int nmg_rk4_step_noalloc(nmg_ctx *c, double t, double dt, const double *u_in_dev,
                          double *u_out_dev);

@@ -165,8 +165,19 @@ int nmg_checkpoint_read_host(const nmg_mesh *m, const char *path, double *u,
       int vli = -1, n0 = 0, n1 = 0, n2 = 0;
       const int got = std::sscanf(line.c_str(), "%d %d %d %d", &vli, &n0, &n1, &n2);
       if (got < 1 || vli < 0 || vli >= nv) return fail(NMG_EINVAL, "bad variable index");
-      const size_t cnt = got == 4 ? (size_t)n0 * n1 * n2 : (size_t)np;
-      if (pos + cnt * 8 > b.size()) return fail(NMG_EINVAL, "truncated variable data");
+      if (got == 4 && (n0 <= 0 || n1 <= 0 || n2 <= 0))
+        return fail(NMG_EINVAL, "bad variable dimensions");
+      // the doubles left in the file bound every partial product, so the
+      // element count is formed without overflow
+      const size_t avail = pos <= b.size() ? (b.size() - pos) / 8 : 0;
+      size_t cnt = (size_t)np;
+      if (got == 4) {
+        if ((size_t)n0 > avail || (size_t)n1 > avail / (size_t)n0 ||
+            (size_t)n2 > avail / ((size_t)n0 * (size_t)n1))
+          return fail(NMG_EINVAL, "truncated variable data");
+        cnt = (size_t)n0 * (size_t)n1 * (size_t)n2;
+      }
+      if (cnt > avail) return fail(NMG_EINVAL, "truncated variable data");
       if (field[vli] >= 0) {
         if (cnt != (size_t)np) return fail(NMG_EMESH, "variable size differs from n^3");
         from_le(b.data() + pos, cnt, u + ((size_t)e * NMG_NFIELDS + field[vli]) * np);

@@ -184,6 +184,7 @@ struct nmg_ctx {
   std::string err;
   const char *err_static = nullptr;  // set instead of err by allocation-free paths
   int n = 0, np = 0, nn = 0;
+  int device = -1;   // CUDA device the context's memory lives on
   int64_t nelem = 0, ncurvi = 0, nbface = 0;
   size_t state_len = 0;
   int bc = 0;
@@ -304,6 +305,7 @@ static int rk4_step_plain(nmg_ctx *c, double t, double dt);
 }
 
 size_t nmg_ctx_state_len(const nmg_ctx *c) { return c->state_len; }
+int nmg_ctx_device(const nmg_ctx *c) { return c->device; }
 
 int nmg_ctx_fail_static(nmg_ctx *c, int code, const char *msg) {
   c->err_static = msg;
@@ -359,8 +361,13 @@ static cudaError_t vjp_stage(nmg_ctx *c, const StageParams &P) {
   return e;
 }
 
+static cudaError_t apply_filter(nmg_ctx *c, double *buf);
+static cudaError_t apply_limiter(nmg_ctx *c, double *buf);
+
+// limiter (bool lim): the context's MRS limiter on every stage output and on
+// u_out, as enqueue_step applies it (the adjoint paths never set it)
 static int step_buffers(nmg_ctx *c, bool vjp, double t, double dt, const double *u_in,
-                        double *u_out, double *s1, double *s2) {
+                        double *u_out, double *s1, double *s2, bool lim = false) {
   const double cacc[4] = {dt / 6., dt / 3., dt / 3., dt / 6.};
   const double cw[4] = {dt / 2., dt / 2., dt, 0.};
   const double ts[4] = {t, t + 0.5 * dt, t + 0.5 * dt, t + dt};
@@ -381,7 +388,12 @@ static int step_buffers(nmg_ctx *c, bool vjp, double t, double dt, const double 
       e = vjp_stage(c, P);
     } else {
       e = run_stage(c, c->sel >= 0 ? c->sel : 0, P);
+      if (e == cudaSuccess && lim && P.wout) e = apply_limiter(c, P.wout);
     }
+    if (e != cudaSuccess) return nmg_ctx_fail_static(c, NMG_ECUDA, cudaGetErrorString(e));
+  }
+  if (lim) {
+    cudaError_t e = apply_limiter(c, u_out);
     if (e != cudaSuccess) return nmg_ctx_fail_static(c, NMG_ECUDA, cudaGetErrorString(e));
   }
   return NMG_OK;
@@ -390,9 +402,13 @@ static int step_buffers(nmg_ctx *c, bool vjp, double t, double dt, const double 
 int nmg_ctx_rk4_step_buffers(nmg_ctx *c, double t, double dt, const double *u_in,
                              double *u_out, double *s1, double *s2) {
   if (c->mixed && c->fsel < 0) c->fsel = c->ndg;
-  int rc = step_buffers(c, false, t, dt, u_in, u_out, s1, s2);
+  // the same step as nmg_rk4_step: limiter inside the step, filter after it
+  // (both use buffers the context allocated when they were switched on)
+  int rc = step_buffers(c, false, t, dt, u_in, u_out, s1, s2, true);
   if (rc) return rc;
-  cudaError_t e = cudaStreamSynchronize(c->stream);
+  cudaError_t e = apply_filter(c, u_out);
+  if (e != cudaSuccess) return nmg_ctx_fail_static(c, NMG_ECUDA, cudaGetErrorString(e));
+  e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return nmg_ctx_fail_static(c, NMG_ECUDA, cudaGetErrorString(e));
   return NMG_OK;
 }
@@ -861,6 +877,7 @@ static int create_impl(const nmg_mesh *m, int32_t bc_kind, const double k[3], bo
   }
   int dev = 0;
   CK(cudaGetDevice(&dev));
+  c->device = dev;
   const int n = m->n, np = n * n * n, nn = n * n;
   const int64_t E = m->nelem;
   if (E <= 0 || E > (int64_t)1 << 30) return set_err(c, NMG_EINVAL, "nmg_create: bad element count");

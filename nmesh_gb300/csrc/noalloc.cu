@@ -26,6 +26,12 @@
 //  - If the context has not been tuned yet, the step uses the first
 //    compiled kernel variant instead of running the autotuner (which would
 //    create CUDA events).
+//  - The step is the one nmg_rk4_step takes: a context's MRS limiter and
+//    exponential filter, if switched on, are applied where that entry point
+//    applies them (their buffers were allocated when they were switched on).
+//  - The context's device must be the current device; a call made with
+//    another device current is rejected with NMG_EINVAL (the scratch address
+//    is per device).
 #include <cuda_runtime.h>
 
 #include "../../include/nmg.h"
@@ -50,6 +56,9 @@ extern "C" int nmg_rk4_step_noalloc(nmg_ctx *c, double t, double dt, const doubl
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
     return nmg_ctx_fail_static(c, NMG_ECUDA, "nmg_rk4_step_noalloc: no usable current device");
+  if (dev != nmg_ctx_device(c))
+    return nmg_ctx_fail_static(c, NMG_EINVAL,
+                               "nmg_rk4_step_noalloc: the context's device is not the current device");
   if (!g_scratch_ptr[dev]) {
     // one-time set-up on this device (keep it outside stream capture)
     double *p = nullptr;

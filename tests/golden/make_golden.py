@@ -187,6 +187,14 @@ CASES = {
     "lim_nc_cs7_l0_n5_h0_a0.02": dict(mesh="cs7", n=5, luni=0, k=(0.3, -0.2, 0.1),
                                       dt=0.002, steps=2, eps=0.3, seed=47, hrefine="0",
                                       limiter=0.02),
+    # the benchmark's mesh family and order at level 2 (448 elements of 9^3
+    # LGL nodes, 1.6 M DOF) with the benchmark's dt formula at that level,
+    # 0.25 (2 / 2^2) / 8^2, and 10 steps.  amp = 0: the initial data is the
+    # seeded noise alone, which the tests regenerate bit for bit
+    # (helpers.dump_noise), so u0 is not stored; r0 and u_final are kept
+    # for every `keep`-th element (reference order) plus their full norms
+    "cs7_l2_n9_noise": dict(mesh="cs7", n=9, luni=2, k=(0.3, -0.2, 0.1),
+                            dt=0.001953125, steps=10, eps=0.01, seed=60, amp=0.0, keep=14),
 }
 
 
@@ -202,7 +210,7 @@ def parfile(case, prefix):
         "scalarwave1_k = %r %r %r" % tuple(c["k"]),
         f"scalarwave1_numflux = {c.get('numflux', 'LLF')}",
         f"nmgdump_prefix = {prefix}",
-        "nmgdump_amp = 1.0",
+        f"nmgdump_amp = {c.get('amp', 1.0)!r}",
         f"nmgdump_perturb = {c['eps']!r}",
         f"nmgdump_seed = {c['seed']}",
         f"nmgdump_persson = {'yes' if c.get('persson') else 'no'}",
@@ -277,6 +285,17 @@ def run_case(case, exe, outdir):
         extra["norms"] = norms
     if c["dt"] == "auto":      # the reference's automatic dt of the run
         extra["dt_ref"] = dt_ref
+    if "keep" in c:   # slim fixture: u0 is regenerated, r0 / u_final sampled
+        sel = np.arange(0, len(d0["pat"]), c["keep"])
+        np.savez_compressed(
+            os.path.join(outdir, case + ".npz"),
+            meta=json.dumps(meta), pat=d0["pat"], n=d0["n"], bbox=d0["bbox"], sel=sel,
+            r0_sel=d0["r"][sel], u_final_sel=d1["u"][sel],
+            r0_norm=np.linalg.norm(d0["r"].ravel()),
+            u_final_norm=np.linalg.norm(d1["u"].ravel()),
+            u0_sum=np.sum(d0["u"]))
+        print(f"{case}: {len(d0['pat'])} elements, {len(sel)} kept")
+        return
     np.savez_compressed(
         os.path.join(outdir, case + ".npz"),
         meta=json.dumps(meta), pat=d0["pat"], n=d0["n"], bbox=d0["bbox"],

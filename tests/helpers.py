@@ -9,6 +9,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 GOLDEN = os.path.join(HERE, "golden")
 PI = 3.141592653589793
 CASES = ["box_l1_n5", "box_l2_n4", "cs7_l0_n9", "cs7_l1_n5", "cs7_l1_n4"]
+# the benchmark's mesh family and order at level 2 (slim fixture: u0 is the
+# dump module's seeded noise, regenerated by dump_noise; r0 and u_final kept
+# on a sample of the elements)
+BIG_CASE = "cs7_l2_n9_noise"
 # all-finite-volume fixtures (uniform points, WENO at the midpoints)
 FV_CASES = ["fvbox_l1_n7_w5no", "fvbox_l1_n7_w5dnfn", "fvbox_l2_n5_w3dnfn",
             "fvbox_l0_n13_w5dnfn", "fvcs7_l0_n7_w5dnfn", "fvcs7_l0_n6_w5no",
@@ -144,3 +148,28 @@ def gaussian_pulses(xyz, seed, npulse=8, rmin=3.0, rmax=10.0, wmin=0.5, wmax=2.0
         u[:, 1:4] += -2.0 * dx / (w * w) * g[:, None, :]
         u[:, 0] += 0.0
     return u
+
+
+def dump_noise(seed, eps, nelem, npt):
+    """The reference-side dump module's initial perturbation with amplitude 0
+    for the plane wave: u[e, f, ijk] = eps * hash(seed * 1000003 + (e << 24) +
+    (f << 20) + ijk), hash a splitmix64 finaliser mapped to [-1, 1)
+    (oracle/ref/nmgdump/nmgdump.c: nmgdump_hash, nmgdump_perturb); bit for
+    bit, e in the reference's element order."""
+    e = np.arange(nelem, dtype=np.uint64)[:, None, None]
+    f = np.arange(5, dtype=np.uint64)[None, :, None]
+    q = np.arange(npt, dtype=np.uint64)[None, None, :]
+    a = np.uint64(seed) * np.uint64(1000003) + (e << np.uint64(24)) + \
+        (f << np.uint64(20)) + q
+    a = a + np.uint64(0x9E3779B97F4A7C15)
+    a = (a ^ (a >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+    a = (a ^ (a >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+    a = a ^ (a >> np.uint64(31))
+    h = (a >> np.uint64(11)).astype(np.float64) * (2.0 / 9007199254740992.0) - 1.0
+    return eps * h
+
+
+def big_case_u0(d, meta):
+    """u0 of the slim fixture in the reference's element order."""
+    n = meta["n"]
+    return dump_noise(meta["seed"], meta["eps"], len(d["pat"]), n ** 3)

@@ -92,6 +92,11 @@ def test_malformed_files_are_rejected(tmp_path):
         "missing_var": raw.replace(b"scalarwave1_cz", b"scalarwave1_qq", 1),
         "missing_elem": raw.replace(b"{\n0_7\n", b"{\n0_6\n", 1),
         "unknown_elem": raw.replace(b"{\n0_7\n", b"{\n9_7\n", 1),
+        # variable lines with explicit dimensions: negative, and a product
+        # that wraps around 64 bits
+        "negative_dims": raw.replace(b"{\n0_7\n64\n0\n", b"{\n0_7\n64\n0 -4 4 4\n", 1),
+        "huge_dims": raw.replace(b"{\n0_7\n64\n0\n",
+                                 b"{\n0_7\n64\n0 2147483647 2147483647 2147483647\n", 1),
     }
     for name, blob in cases.items():
         p = tmp_path / name
