@@ -298,7 +298,7 @@ def run_ours(args, rank, world, local):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(args, mesh, n, luni)
+        cpu = cpu_baseline(args, n, luni)
 
     if rank == 0:
         out = {
@@ -307,7 +307,8 @@ def run_ours(args, rank, world, local):
             "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded Gaussian pulses on the generated mesh)",
-            "config": dict(cfg, parallelism=f"replicas x{world}"),
+            "config": cfg,
+            "parallelism": f"replicas x{world}",
             "e2e": {"value": e2e_value, "unit": UNIT,
                     "h2d_bytes_per_step": state_bytes,
                     "d2h_bytes_per_step": state_bytes},
@@ -477,94 +478,81 @@ def fv_bench(args):
            "gpu_launches": int(launches)}
     if not args.no_cpu_baseline:
         cl = args.fv_cpu_luni
-        cm, om = cpu_mesh(n, cl, fv=True, fv_rec=rec, fv_extrap=ex)
-        u = gaussian_pulses(cm.coords(), seed=99)
+        cxyz, om = cpu_mesh(n, cl, fv=True, fv_rec=rec, fv_extrap=ex)
+        u = gaussian_pulses(cxyz, seed=99)
         cdt = 0.1 * (2.0 / 2 ** cl) / (n - 1)
         om.rk4(u, cdt, 1)
         t0 = time.perf_counter()
         om.rk4(u, cdt, args.fv_cpu_steps)
         t = time.perf_counter() - t0
-        cdof = cm.nelem * cm.np * NFIELDS
+        cdof = om.nelem * n ** 3 * NFIELDS
         threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count()))
         out["cpu_baseline"] = {
             "value": cdof * 4 * args.fv_cpu_steps / t, "unit": UNIT, "cores": threads,
             "kind": "port",
             "sample": f"{args.fv_cpu_steps} RK4 steps of the same workload at level {cl} "
-                      f"({cm.nelem} elements, {cdof} DOF), {t:.2f} s"}
+                      f"({om.nelem} elements, {cdof} DOF), {t:.2f} s"}
     return out
 
 
 def cpu_mesh(n, luni, fv=False, fv_rec="WENOm5_2", fv_extrap="dnfn_extrap1"):
-    """Oracle mesh of the workload, neighbour table from the packed mesh."""
-    import nmesh_gb300 as ng
+    """The oracle's own mesh of the workload (oracle/nmo_mesh.c: geometry
+    restated from the reference, neighbour table by face matching); no
+    product code is loaded."""
     from oracle import nmo
-    mesh = ng.Mesh.build(ng.MESH_CUBEDSPHERES7, n=n, luni=luni, cs_dc=1.0, cs_r0fac=20.0,
-                         fv=fv)
-    pat, bbox = mesh.elements()
-    xyz = mesh.coords()
-    nb, code = mesh.faces()
-    npt = n ** 3
-    planes = [nmo.face_plane_index(n, f) for f in range(6)]
-    a = np.tile(np.arange(n), n)
-    b = np.repeat(np.arange(n), n)
-    nbnode = np.full((mesh.nelem, 6, n * n), -1, np.int64)
-    for o in range(8):
-        s, fa, fb = o & 1, (o >> 1) & 1, (o >> 2) & 1
-        aa, bb = (b, a) if s else (a, b)
-        aa = n - 1 - aa if fa else aa
-        bb = n - 1 - bb if fb else bb
-        for f2 in range(6):
-            sel = (nb >= 0) & ((code & 7) == f2) & ((code >> 3) == o)
-            if not sel.any():
-                continue
-            idx2 = planes[f2][aa + n * bb]
-            es, fs = np.nonzero(sel)
-            nbnode[es, fs, :] = nb[es, fs][:, None] * npt + idx2[None, :]
-    fvk = dict(fv=mesh.fv(), fv_rec=fv_rec, fv_extrap=fv_extrap) if fv else {}
-    om = nmo.OracleMesh(bbox, (pat > 0).astype(np.int32), mesh.dXdx(), xyz, nbnode, n, bc=1,
-                        **fvk)
-    return mesh, om
+    pat, bbox, curvi, xyz, dXdx = nmo.generate_mesh(nmo.MESH_CUBEDSPHERES7, n, luni,
+                                                    uniform=fv, cs_dc=1.0, cs_r0fac=20.0)
+    nbnode = nmo.match_faces_conforming(xyz, n)
+    fvk = dict(fv=np.ones(len(pat), np.int32), fv_rec=fv_rec, fv_extrap=fv_extrap) if fv else {}
+    om = nmo.OracleMesh(bbox, curvi, dXdx, xyz, nbnode, n, bc=1, **fvk)
+    return xyz, om
 
 
-def cpu_baseline(args, mesh_gpu, n, luni, steps=None):
+def cpu_baseline(args, n, luni, steps=None):
     """Time the oracle (C restatement of the reference path, OpenMP over all
-    host cores) on a bounded sample of the workload: the same mesh family,
-    order, data and boundary at level `--cpu-luni` for `--cpu-steps` RK4
-    steps."""
+    host cores) on a bounded sample of the workload: the same mesh, order,
+    data, boundary and dt for `--cpu-steps` RK4 steps."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from helpers import gaussian_pulses
-    cl = args.cpu_luni
-    mesh, om = cpu_mesh(n, cl)
-    u = gaussian_pulses(mesh.coords(), seed=1234)
-    dt = 0.25 * (2.0 / 2 ** cl) / (n - 1) ** 2
+    xyz, om = cpu_mesh(n, luni)
+    u = gaussian_pulses(xyz, seed=1234)
+    del xyz
+    dt = 0.25 * (2.0 / 2 ** luni) / (n - 1) ** 2
     nsteps = steps if steps is not None else args.cpu_steps
-    om.rk4(u, dt, 1)  # warm-up (page-in, OpenMP threads)
+    u = om.rk4(u, dt, 1)  # warm-up (page-in, OpenMP threads)
     t0 = time.perf_counter()
     om.rk4(u, dt, nsteps)
     t = time.perf_counter() - t0
-    dof = mesh.nelem * n ** 3 * NFIELDS
+    dof = om.nelem * n ** 3 * NFIELDS
     threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count()))
     return {"value": dof * 4 * nsteps / t, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{nsteps} RK4 steps of the same workload at level {cl} "
-                      f"({mesh.nelem} elements, {dof} DOF), {t:.2f} s"}
+            "sample": f"{nsteps} RK4 steps of the full workload ({om.nelem} elements, "
+                      f"{dof} DOF), {t:.2f} s"}
 
 
 def run_reference(args, rank, world):
+    """The reference arm: the oracle's C restatement of the reference's RHS
+    and RK4 step (bit-exact against the reference's own runs), OpenMP over
+    all host cores, on the full workload (same mesh, order, data, boundary,
+    dt and config as the GPU arm); its mesh comes from the oracle's own
+    generator, so no product code is loaded."""
     if rank != 0:
         return
     n, luni = args.n, args.luni
     cfg = workload_config(n, luni)
-    mesh, om = cpu_mesh(n, args.cpu_luni)
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from helpers import gaussian_pulses
-    u = gaussian_pulses(mesh.coords(), seed=1234)
-    dt = 0.25 * (2.0 / 2 ** args.cpu_luni) / (n - 1) ** 2
-    dof = mesh.nelem * n ** 3 * NFIELDS
-    for _ in range(args.warmup):
-        u = om.rk4(u, dt, 1)
+    xyz, om = cpu_mesh(n, luni)
+    u = gaussian_pulses(xyz, seed=1234)
+    del xyz
+    dt = 0.25 * (2.0 / 2 ** luni) / (n - 1) ** 2
+    dof = om.nelem * n ** 3 * NFIELDS
+    assert dof == cfg["dof"]
+    for s in range(args.warmup):
+        u = om.rk4(u, dt, 1, t=s * dt)
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        u = om.rk4(u, dt, 1)
+    for s in range(args.steps):
+        u = om.rk4(u, dt, 1, t=(args.warmup + s) * dt)
     t = time.perf_counter() - t0
     value = dof * 4 * args.steps / t
     threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count()))
@@ -574,10 +562,11 @@ def run_reference(args, rank, world):
         "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded Gaussian pulses on the generated mesh)",
-        "config": dict(cfg, parallelism="host CPU, OpenMP"),
+        "config": cfg,
+        "parallelism": f"host CPU, OpenMP x{threads}",
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"each step: one RK4 step of the workload at level "
-                                   f"{args.cpu_luni} ({mesh.nelem} elements, {dof} DOF)"},
+                         "sample": f"each step: one RK4 step of the full workload "
+                                   f"({om.nelem} elements, {dof} DOF)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out))
@@ -591,8 +580,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=9)
     ap.add_argument("--luni", type=int, default=4)
-    ap.add_argument("--cpu-luni", type=int, default=3)
-    ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--cpu-steps", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-batched", action="store_true")

@@ -14,17 +14,19 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libnmo.so")
+# the restated RHS / steps / GRHD pieces, and the oracle's own mesh generator
+SOURCES = ["nmo.c", "nmo_mesh.c"]
 
 
 def build(verbose=False):
     """Compile oracle/nmo.c into oracle/_build/libnmo.so (gcc, OpenMP,
     -ffp-contract=off so that x86-64 and aarch64 results agree bitwise)."""
     os.makedirs(BUILD, exist_ok=True)
-    src = os.path.join(HERE, "nmo.c")
-    if os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(src):
+    srcs = [os.path.join(HERE, f) for f in SOURCES]
+    if os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(s) for s in srcs):
         return LIB
     cmd = ["gcc", "-O2", "-std=gnu99", "-fopenmp", "-ffp-contract=off",
-           "-fPIC", "-shared", "-o", LIB + ".tmp", src, "-lm"]
+           "-fPIC", "-shared", "-o", LIB + ".tmp"] + srcs + ["-lm"]
     if verbose:
         print(" ".join(cmd))
     subprocess.run(cmd, check=True)
@@ -94,6 +96,58 @@ def diffmat(n):
     lib().nmo_diffmat(ctypes.c_int(n), x.ctypes.data_as(ctypes.c_void_p),
                       D.ctypes.data_as(ctypes.c_void_p))
     return D
+
+
+MESH_BOX, MESH_SHELL6, MESH_CUBEDSPHERES7 = 1, 6, 7
+
+
+def generate_mesh(kind, n, luni, uniform=False, xc=(0.0, 0.0, 0.0), box_dout=1.0, cs_dc=1.0,
+                  cs_r0fac=20.0, r_in=2.0, r_out=20.0):
+    """The oracle's own uniform mesh (oracle/nmo_mesh.c): a box
+    (MESH_BOX: centre xc, half edge box_dout), the 7-patch cubed spheres
+    (MESH_CUBEDSPHERES7: cube of half edge cs_dc, outer radius cs_r0fac cs_dc)
+    or 6 cubed-sphere shells between radii r_in and r_out (MESH_SHELL6), at
+    level luni with n LGL (or equally spaced) points per direction.
+    Returns (pat [E], bbox [E,6], curvi [E], xyz [E,3,np], dXdx [E,9,np])."""
+    f = lib().nmo_mesh_count
+    f.restype = ctypes.c_int64
+    E = int(f(ctypes.c_int(kind), ctypes.c_int(luni)))
+    if E < 0:
+        raise ValueError("unknown mesh kind or level")
+    prm = {MESH_BOX: (xc[0], xc[1], xc[2], box_dout),
+           MESH_CUBEDSPHERES7: (cs_dc, cs_r0fac, 0.0, 0.0),
+           MESH_SHELL6: (r_in, r_out, 0.0, 0.0)}[kind]
+    npt = n ** 3
+    pat = np.zeros(E, np.int32)
+    bbox = np.zeros((E, 6))
+    curvi = np.zeros(E, np.int32)
+    xyz = np.zeros((E, 3, npt))
+    dXdx = np.zeros((E, 9, npt))
+    rc = lib().nmo_mesh_generate(ctypes.c_int(kind), ctypes.c_int(n), ctypes.c_int(luni),
+                                 (ctypes.c_double * 4)(*prm), ctypes.c_int(int(uniform)),
+                                 pat.ctypes.data_as(ctypes.c_void_p),
+                                 bbox.ctypes.data_as(ctypes.c_void_p),
+                                 curvi.ctypes.data_as(ctypes.c_void_p),
+                                 xyz.ctypes.data_as(ctypes.c_void_p),
+                                 dXdx.ctypes.data_as(ctypes.c_void_p))
+    if rc:
+        raise RuntimeError("nmo_mesh_generate failed")
+    return pat, bbox, curvi, xyz, dXdx
+
+
+def match_faces_conforming(xyz, n, period=None):
+    """Neighbour table nbnode[E, 6, n*n] of a conforming mesh, as
+    match_faces, computed in C (oracle/nmo_mesh.c: nmo_match_faces)."""
+    xyz = np.ascontiguousarray(xyz, np.float64)
+    E = xyz.shape[0]
+    nb = np.empty((E, 6, n * n), np.int64)
+    per = None if period is None else (ctypes.c_double * 3)(*([float(period)] * 3))
+    rc = lib().nmo_match_faces(ctypes.c_int64(E), ctypes.c_int(n),
+                               xyz.ctypes.data_as(ctypes.c_void_p), per,
+                               nb.ctypes.data_as(ctypes.c_void_p))
+    if rc:
+        raise ValueError("nmo_match_faces: faces do not match conformingly")
+    return nb
 
 
 def face_plane_index(n, f):

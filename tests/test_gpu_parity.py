@@ -6,8 +6,9 @@ import numpy as np
 import pytest
 
 import nmesh_gb300 as ng
-from helpers import (CASES, DTAUTO_CASES, PI, RTOL_RHS, RTOL_RK4, build_mesh, gaussian_pulses,
-                     load, oracle_for, perm_to_mesh, rel_l2, to_mesh_order)
+from helpers import (BIG_CASE, CASES, DTAUTO_CASES, PI, RTOL_RHS, RTOL_RK4, big_case_u0,
+                     build_mesh, gaussian_pulses, load, oracle_for, perm_to_mesh, rel_l2,
+                     to_mesh_order)
 
 pytestmark = pytest.mark.gpu
 
@@ -53,7 +54,8 @@ def test_rk4_matches_reference(case, variant):
     assert rel_l2(ev.get_state()[perm], d["u_final"]) <= RTOL_RK4
 
 
-@pytest.mark.parametrize("n,luni", [(2, 1), (3, 2), (6, 1), (7, 0), (8, 1), (10, 0), (11, 0), (12, 0)])
+@pytest.mark.parametrize("n,luni", [(2, 1), (3, 2), (4, 1), (5, 1), (6, 1), (7, 0), (8, 1), (9, 1),
+                                    (10, 0), (11, 0), (12, 0)])
 @pytest.mark.parametrize("variant", VARIANTS)
 def test_cubed_spheres_outgoing_vs_oracle(n, luni, variant):
     """Every compiled order: Gaussian pulses, outgoing-radiation outer
@@ -202,3 +204,52 @@ def test_step_with_auto_dt_matches_reference(case):
         ev.set_fv(meta["fv"]["rec"], meta["fv"]["extrap"])
     u = ev.rk4_steps_host(to_mesh_order(d["u0"], perm), 0.0, m.auto_dt(), meta["steps"])
     assert rel_l2(u[perm], d["u_final"]) <= RTOL_RK4
+
+
+@pytest.mark.parametrize("variant", ["auto", "eo", "gather"])
+def test_benchmark_order_level2_matches_reference(variant):
+    """The benchmark's mesh family and order (7 CubedSpheres, 9 LGL nodes)
+    at level 2, 448 elements, 1.6 M DOF, against the reference's own run:
+    the RHS and 10 RK4 steps with the benchmark's dt formula, on the
+    elements the fixture keeps and through the full norms."""
+    d, meta = load(BIG_CASE)
+    m = build_mesh(meta)
+    perm = perm_to_mesh(m, d)
+    u0 = to_mesh_order(big_case_u0(d, meta), perm)
+    ev = ng.Evolution(m, ng.BC_EXACT_PLANEWAVE, k=meta["k"])
+    ev.set_kernel(variant)
+    sel = d["sel"]
+    r = ev.rhs(u0, 0.0)[perm]
+    assert rel_l2(r[sel], d["r0_sel"]) <= RTOL_RHS
+    assert abs(np.linalg.norm(r.ravel()) / float(d["r0_norm"]) - 1) <= RTOL_RHS
+    ev.set_state(u0)
+    ev.rk4_steps(0.0, meta["dt"], meta["steps"])
+    u = ev.get_state()[perm]
+    assert rel_l2(u[sel], d["u_final_sel"]) <= RTOL_RK4
+    assert abs(np.linalg.norm(u.ravel()) / float(d["u_final_norm"]) - 1) <= RTOL_RK4
+
+
+def test_benchmark_workload_drift_over_100_steps():
+    """The benchmark's workload at level 2 (7 CubedSpheres, n = 9, 448
+    elements): 8 seeded Gaussian pulses (the benchmark's seed), outgoing
+    boundary, dt = 0.25 (2 / 2^2) / 8^2, graph-captured RK4 steps with the
+    autotuned kernel as the benchmark takes them, against the oracle after
+    1, 10 and 100 steps: relative L2 <= 1e-12 at every checkpoint (the
+    measured drift is printed)."""
+    n, L = 9, 2
+    m = ng.Mesh.build(ng.MESH_CUBEDSPHERES7, n=n, luni=L, cs_dc=1.0, cs_r0fac=20.0)
+    u0 = gaussian_pulses(m.coords(), seed=1234)
+    dt = 0.25 * (2.0 / 2 ** L) / (n - 1) ** 2
+    o = oracle_for(m, bc=1)
+    ev = ng.Evolution(m, ng.BC_OUTGOING)
+    ev.set_state(u0)
+    assert rel_l2(ev.rhs(u0, 0.0), o.rhs(u0, 0.0)) <= RTOL_RHS
+    uo, done, drift = u0, 0, {}
+    for target in (1, 10, 100):
+        ev.rk4_steps(done * dt, dt, target - done)
+        uo = o.rk4(uo, dt, target - done, t=done * dt)
+        done = target
+        drift[target] = rel_l2(ev.get_state(), uo)
+    print(f"\nbenchmark workload at level 2, relative L2 GPU vs oracle after 1/10/100 steps: "
+          f"{drift[1]:.3e} {drift[10]:.3e} {drift[100]:.3e}")
+    assert max(drift.values()) <= RTOL_RK4

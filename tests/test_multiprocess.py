@@ -50,7 +50,7 @@ def test_reference_arm_under_torchrun_prints_once():
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(port),
            os.path.join(ROOT, "bench.py"), "--impl", "reference", "--gpus", "2",
-           "--steps", "1", "--warmup", "3", "--cpu-luni", "1"]
+           "--steps", "1", "--warmup", "3", "--luni", "1"]
     env = dict(os.environ, OMP_NUM_THREADS="2")
     res = subprocess.run(cmd, capture_output=True, text=True, env=env, cwd=ROOT, timeout=600)
     assert res.returncode == 0, res.stderr[-2000:]
@@ -59,3 +59,23 @@ def test_reference_arm_under_torchrun_prints_once():
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
     assert d["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def test_reference_arm_loads_no_product_code():
+    """The reference arm runs the oracle on the oracle's own mesh: neither
+    the product package nor its library is loaded, and its config is the
+    GPU arm's config."""
+    code = (
+        "import sys, json, io, contextlib; sys.path.insert(0, %r); import bench\n"
+        "a = type('A', (), dict(n=5, luni=1, steps=1, warmup=3))()\n"
+        "buf = io.StringIO()\n"
+        "with contextlib.redirect_stdout(buf): bench.run_reference(a, 0, 1)\n"
+        "maps = open('/proc/self/maps').read()\n"
+        "d = json.loads(buf.getvalue())\n"
+        "print(json.dumps(dict(pkg='nmesh_gb300' in sys.modules, so='libnmg' in maps, "
+        "cfg=d['config'] == bench.workload_config(5, 1), v=d['value'] > 0)))\n" % ROOT)
+    env = dict(os.environ, OMP_NUM_THREADS="2")
+    res = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env,
+                         cwd=ROOT, timeout=300)
+    assert res.returncode == 0, res.stderr[-2000:]
+    assert json.loads(res.stdout.splitlines()[-1]) == dict(pkg=False, so=False, cfg=True, v=True)

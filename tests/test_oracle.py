@@ -5,10 +5,10 @@ operation order and must match it bit for bit."""
 import numpy as np
 import pytest
 
-from helpers import (CASES, FILT_CASES, LIM_CASES, RTOL_FILT_ORACLE, FV_CASES, METHOD_CASES, METHOD_NEAR_CASES, MID_CASES,
+from helpers import (BIG_CASE, CASES, FILT_CASES, LIM_CASES, RTOL_FILT_ORACLE, FV_CASES, METHOD_CASES, METHOD_NEAR_CASES, MID_CASES,
                      MID_NEAR_CASES, MIX_CASES, MIX_NEAR_CASES, NC_CASES, RTOL_NC_ORACLE,
-                     UPW_CASES, build_mesh, load, oracle_for, perm_to_mesh, rel_l2,
-                     to_mesh_order)
+                     UPW_CASES, big_case_u0, build_mesh, load, oracle_for, perm_to_mesh,
+                     rel_l2, to_mesh_order)
 from oracle import nmo
 
 
@@ -232,3 +232,56 @@ def test_oracle_mrs_limiter_matches_reference(case):
     assert rel_l2(u, d["u_final"]) <= RTOL_NC_ORACLE
     # without the limiter the run is far off: the limiter acts
     assert rel_l2(m.rk4(d["u0"], meta["dt"], meta["steps"]), d["u_final"]) > 1e-3
+
+
+def _generated(meta, uniform=False):
+    """The oracle's own mesh of a fixture's case and the permutation that
+    takes fixture element i to generated element perm[i]."""
+    n, L = meta["n"], meta["luni"]
+    if meta["mesh"] == "box":
+        g = nmo.generate_mesh(nmo.MESH_BOX, n, L, uniform=uniform, xc=(np.pi,) * 3,
+                              box_dout=np.pi)
+    else:
+        g = nmo.generate_mesh(nmo.MESH_CUBEDSPHERES7, n, L, uniform=uniform)
+    return g
+
+
+def _perm(pat, bbox, d):
+    key = {(int(a),) + tuple(b): i for i, (a, b) in enumerate(zip(pat, bbox))}
+    return np.array([key[(int(a),) + tuple(b)] for a, b in zip(d["pat"], d["bbox"])])
+
+
+@pytest.mark.parametrize("case", CASES + FV_CASES)
+def test_oracle_mesh_generator_matches_reference_geometry(case):
+    """The oracle's own mesh generator (oracle/nmo_mesh.c) gives the
+    reference's element bboxes, coordinates and dX/dx bit for bit, and its
+    C face matcher the coordinate-matching neighbour table."""
+    d, meta = load(case)
+    pat, bbox, curvi, xyz, dXdx = _generated(meta, uniform="fv" in meta)
+    perm = _perm(pat, bbox, d)
+    assert len(perm) == len(pat)
+    assert np.array_equal(xyz[perm], d["x"])
+    assert np.array_equal(dXdx[perm], d["dXdx"])
+    if "fv" not in meta:
+        assert np.array_equal(nmo.match_faces_conforming(d["x"], meta["n"]),
+                              nmo.match_faces(d["x"], meta["n"]))
+
+
+def test_oracle_benchmark_order_level2_fixture():
+    """The benchmark's mesh family and order at level 2 (448 elements of 9^3
+    nodes) on the oracle's own mesh: RHS and 10 RK4 steps equal the
+    reference's run on the kept elements bit for bit, and the full norms."""
+    d, meta = load(BIG_CASE)
+    n = meta["n"]
+    pat, bbox, curvi, xyz, dXdx = _generated(meta)
+    perm = _perm(pat, bbox, d)
+    u0 = to_mesh_order(big_case_u0(d, meta), perm)
+    om = nmo.OracleMesh(bbox, curvi, dXdx, xyz, nmo.match_faces_conforming(xyz, n), n, bc=0,
+                        k=meta["k"])
+    sel = d["sel"]
+    r = om.rhs(u0, 0.0)[perm]
+    assert np.array_equal(r[sel], d["r0_sel"])
+    assert np.linalg.norm(r.ravel()) == pytest.approx(float(d["r0_norm"]), rel=1e-15)
+    u = om.rk4(u0, meta["dt"], meta["steps"])[perm]
+    assert np.array_equal(u[sel], d["u_final_sel"])
+    assert np.linalg.norm(u.ravel()) == pytest.approx(float(d["u_final_norm"]), rel=1e-15)
