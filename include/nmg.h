@@ -40,6 +40,10 @@ extern "C" {
 /* mesh types, as the reference's amr_mesh_type (src/main/amr/mesh.c:181) */
 #define NMG_MESH_BOX 1           /* "1 BoxMesh": one Cartesian box patch */
 #define NMG_MESH_CUBEDSPHERES7 7 /* "7 CubedSpheres": box + 6 cubed spheres */
+#define NMG_MESH_CUBEDSHELL6 6   /* 6 cubed-sphere patches between two spheres
+                                    (the reference's CubedShell map,
+                                    src/main/coordinates/coordtrans_CubedSphere.c:
+                                    84-92,236-245, with constant radii) */
 
 /* outer-boundary treatment */
 #define NMG_BC_EXACT_PLANEWAVE 0 /* exterior state = exact plane wave
@@ -91,6 +95,9 @@ typedef struct nmg_mesh_params {
                             refine.c:1087-1100); 0: none */
   double sphere_radius;  /* amr_hrefine_sphere_radius: innermost radius (the
                             reference reads it as an integer) */
+  int32_t ndiv;          /* > 0: every patch split into ndiv^3 equal elements
+                            (instead of 2^luni per direction); 0: luni */
+  double shell_rin, shell_rout; /* NMG_MESH_CUBEDSHELL6: inner and outer radius */
 } nmg_mesh_params;
 
 /* A mesh given element by element, e.g. packed from the reference's tMesh

@@ -20,6 +20,7 @@ NFIELDS = 5
 FIELDS = ("pi", "cx", "cy", "cz", "phi")
 MESH_BOX = 1
 MESH_CUBEDSPHERES7 = 7
+MESH_CUBEDSHELL6 = 6
 BC_EXACT_PLANEWAVE = 0
 BC_OUTGOING = 1
 # finite-volume reconstruction (reference par fv_rec) and div(f) completion
@@ -42,7 +43,9 @@ class _MeshParams(ctypes.Structure):
                 ("xc", ctypes.c_double * 3), ("box_dout", ctypes.c_double),
                 ("cs_dc", ctypes.c_double), ("cs_r0fac", ctypes.c_double),
                 ("fv", ctypes.c_int32), ("hrefine", ctypes.c_int32),
-                ("sphere_levels", ctypes.c_int32), ("sphere_radius", ctypes.c_double)]
+                ("sphere_levels", ctypes.c_int32), ("sphere_radius", ctypes.c_double),
+                ("ndiv", ctypes.c_int32), ("shell_rin", ctypes.c_double),
+                ("shell_rout", ctypes.c_double)]
 
 
 class TroubleParams(ctypes.Structure):
@@ -251,7 +254,8 @@ class Mesh:
     @classmethod
     def build(cls, mesh_type=MESH_BOX, n=5, luni=0, xc=(0.0, 0.0, 0.0),
               box_dout=1.0, cs_dc=1.0, cs_r0fac=20.0, periodic=False, fv=False,
-              hrefine=(), sphere_levels=0, sphere_radius=10.0):
+              hrefine=(), sphere_levels=0, sphere_radius=10.0, ndiv=0, shell_rin=2.0,
+              shell_rout=20.0):
         """Mesh from the reference's parameters: amr_mesh_type (1 BoxMesh /
         7 CubedSpheres), amr_n0..2 = n, amr_luni, amr_mesh_xc,
         amr_BoxMesh_dout, amr_CubedSphere_dc, amr_CubedSphere_r0fac;
@@ -260,7 +264,9 @@ class Mesh:
         of amr_hrefine_p (refined one level further); sphere_levels and
         sphere_radius are amr_hrefine_sphere_levels / _radius (elements
         whose centre lies within radius 2^(levels-1-i) of x = 0 are refined
-        in pass i)."""
+        in pass i).  MESH_CUBEDSHELL6: six cubed-sphere patches between the
+        spheres of radius shell_rin and shell_rout; ndiv > 0 splits every
+        patch into ndiv^3 equal elements instead of 2^luni per direction."""
         hmask = 0
         for p_ in hrefine:
             hmask |= 1 << int(p_)
@@ -275,7 +281,8 @@ class Mesh:
         p = _MeshParams(int(mesh_type), int(n), int(luni), int(bool(periodic)),
                         (ctypes.c_double * 3)(*xc), float(box_dout),
                         float(cs_dc), float(cs_r0fac), int(mask), hmask,
-                        int(sphere_levels), float(sphere_radius))
+                        int(sphere_levels), float(sphere_radius), int(ndiv), float(shell_rin),
+                        float(shell_rout))
         h = ctypes.c_void_p()
         rc = lib().nmg_mesh_build(ctypes.byref(p), ctypes.byref(h))
         if rc:

@@ -74,6 +74,14 @@ void cubsph_x_dXdx(const Patch &P, const double X[3], double x[3],
   double da0_dx = 0.0, da0_dy = 0.0, da0_dz = 0.0;
   double da1_dx = a1, da1_dy = a1, da1_dz = a1;
   double dsigma_dA_osigma0 = 0.0, dsigma_dB_osigma0 = 0.0;
+  if (P.shell) {
+    // CubedShell: the inner surface is the sphere of radius s0 too
+    double dsig0[2] = {0., 0.};
+    dsigma_dA_osigma0 = dsig0[0] / P.s0;
+    dsigma_dB_osigma0 = dsig0[1] / P.s0;
+    a0 = pm * P.s0 / sqrt_1_A2_B2;
+    da0_dx = a0; da0_dy = a0; da0_dz = a0;
+  }
   double rx, ry, rz, rx2, ry2, rz2, rc2, mx, my, mz, mx0, my0, mz0, mx1, my1,
       mz1;
   double *dlamdx = &dXdx[0][0], *dlamdy = &dXdx[0][1], *dlamdz = &dXdx[0][2];
@@ -252,7 +260,19 @@ void fill_geometry(nmg_mesh &m, const std::vector<Patch> &pats, const std::vecto
   for (int64_t e = 0; e < m.nelem; e++) {
     const int p = leaves[e].p, Lp = leaves[e].L;
     const int *ixyz = leaves[e].ix;
-    elem_bbox(pats[p].bbox, Lp, ixyz, &m.bbox[e * 6]);
+    if (m.ndiv > 0) {
+      // ndiv equal parts per direction
+      const double *pb = pats[p].bbox;
+      double *bb = &m.bbox[e * 6];
+      for (int d = 0; d < 3; d++) {
+        bb[2 * d] = pb[2 * d] + (pb[2 * d + 1] - pb[2 * d]) * (double)ixyz[d] / m.ndiv;
+        bb[2 * d + 1] = ixyz[d] + 1 == m.ndiv
+                            ? pb[2 * d + 1]
+                            : pb[2 * d] + (pb[2 * d + 1] - pb[2 * d]) * (double)(ixyz[d] + 1) / m.ndiv;
+      }
+    } else {
+      elem_bbox(pats[p].bbox, Lp, ixyz, &m.bbox[e * 6]);
+    }
     // elmname: patch, then one octree child digit per level, bit d set
     // for the upper half in direction d (connections.c:819-866,1186-1200)
     std::string nm = std::to_string(p) + "_";
@@ -261,6 +281,9 @@ void fill_geometry(nmg_mesh &m, const std::vector<Patch> &pats, const std::vecto
       for (int d = 0; d < 3; d++) dig |= ((ixyz[d] >> (Lp - ll)) & 1) << d;
       nm += (char)('0' + dig);
     }
+    if (m.ndiv > 0)
+      nm = std::to_string(p) + "_" + std::to_string(ixyz[0]) + "_" + std::to_string(ixyz[1]) +
+           "_" + std::to_string(ixyz[2]);
     m.names[e] = nm;
     m.level[e] = Lp;
     for (int d = 0; d < 3; d++) m.ixyz[e * 3 + d] = ixyz[d];
@@ -878,18 +901,53 @@ int nmg_mesh_build(const nmg_mesh_params *p, nmg_mesh **out) {
         c.s1 = r0;
         pats.push_back(c);
       }
+    } else if (p->mesh_type == NMG_MESH_CUBEDSHELL6) {
+      if (!(p->shell_rin > 0) || !(p->shell_rout > p->shell_rin)) {
+        delete m;
+        return fail(NMG_EINVAL, "cubed shells need 0 < shell_rin < shell_rout");
+      }
+      if (p->periodic) { delete m; return fail(NMG_EINVAL, "periodic only for the box"); }
+      double Din[6], r[4];
+      for (int f = 0; f < 6; f++) Din[f] = p->shell_rin;
+      for (int dom = 0; dom < 6; dom++) {
+        Patch c;
+        ab_range(dom, Din, r);
+        double bb[6] = {0., 1., r[0], r[1], r[2], r[3]};
+        std::memcpy(c.bbox, bb, sizeof(bb));
+        c.cubed = true;
+        c.shell = true;
+        c.dom = dom;
+        for (int d = 0; d < 3; d++) c.xc[d] = p->xc[d];
+        c.s0 = p->shell_rin;
+        c.s1 = p->shell_rout;
+        pats.push_back(c);
+      }
     } else {
       delete m;
       return fail(NMG_EUNSUP, "nmg_mesh_build: unknown mesh_type");
     }
+    if (p->ndiv < 0 || p->ndiv > 256 ||
+        (p->ndiv > 0 && (p->hrefine || p->sphere_levels > 0))) {
+      delete m;
+      return fail(NMG_EINVAL, "nmg_mesh_build: ndiv must be in [0,256], without refinement");
+    }
+    m->ndiv = p->ndiv;
     std::vector<Leaf> leaves;
-    for (size_t q = 0; q < pats.size(); q++)
-      uniform_leaves((int)q, p->luni + (((p->hrefine >> q) & 1) ? 1 : 0), leaves);
+    if (p->ndiv > 0) {
+      for (size_t q = 0; q < pats.size(); q++)
+        for (int k = 0; k < p->ndiv; k++)
+          for (int j = 0; j < p->ndiv; j++)
+            for (int i = 0; i < p->ndiv; i++) leaves.push_back(Leaf{(int)q, 0, {i, j, k}});
+    } else {
+      for (size_t q = 0; q < pats.size(); q++)
+        uniform_leaves((int)q, p->luni + (((p->hrefine >> q) & 1) ? 1 : 0), leaves);
+    }
     if (p->sphere_levels > 0) refine_spheres(pats, p->sphere_levels, p->sphere_radius, leaves);
     fill_geometry(*m, pats, leaves, p->fv);
     bool anyfv = false;
     for (int64_t e = 0; e < m->nelem; e++) anyfv = anyfv || m->fv[e];
     if (!anyfv) m->fv.clear();
+    if (m->ndiv > 0) m->level.clear();  // not an octree: conforming faces only
     std::string err = nmg::pack_faces(*m, nullptr, period);
     if (!err.empty()) { delete m; return fail(NMG_EMESH, err); }
   } catch (const std::bad_alloc &) {

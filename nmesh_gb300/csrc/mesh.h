@@ -11,6 +11,7 @@ namespace nmg {
 struct Patch {
   double bbox[6];
   bool cubed = false;  // outer cubed-sphere patch (else Cartesian box)
+  bool shell = false;  // ... with a curved inner surface too (radius s0)
   int dom = 0;         // cubed-sphere domain 0..5
   double xc[3] = {0, 0, 0};
   double s0 = 0, s1 = 0;  // inner flat distance and outer sphere radius
@@ -35,6 +36,7 @@ struct nmg_mesh {
                                     // for a described one)
   std::vector<std::string> names;   // [E] the reference's element names
                                     // "<patch>_<octree digits>" (generated meshes)
+  int ndiv = 0;                     // > 0: patches split into ndiv^3 equal elements
   std::vector<int32_t> level;       // [E] refinement level (generated meshes)
   std::vector<int32_t> ixyz;        // [E][3] integer position at that level
   // Non-conforming faces (a level jump between neighbours): per such face

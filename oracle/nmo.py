@@ -102,18 +102,21 @@ MESH_BOX, MESH_SHELL6, MESH_CUBEDSPHERES7 = 1, 6, 7
 
 
 def generate_mesh(kind, n, luni, uniform=False, xc=(0.0, 0.0, 0.0), box_dout=1.0, cs_dc=1.0,
-                  cs_r0fac=20.0, r_in=2.0, r_out=20.0):
+                  cs_r0fac=20.0, r_in=2.0, r_out=20.0, ndiv=0):
     """The oracle's own uniform mesh (oracle/nmo_mesh.c): a box
     (MESH_BOX: centre xc, half edge box_dout), the 7-patch cubed spheres
     (MESH_CUBEDSPHERES7: cube of half edge cs_dc, outer radius cs_r0fac cs_dc)
     or 6 cubed-sphere shells between radii r_in and r_out (MESH_SHELL6), at
-    level luni with n LGL (or equally spaced) points per direction.
+    level luni (or, ndiv > 0, ndiv^3 equal elements per patch) with n LGL
+    (or equally spaced) points per direction.
     Returns (pat [E], bbox [E,6], curvi [E], xyz [E,3,np], dXdx [E,9,np])."""
     f = lib().nmo_mesh_count
     f.restype = ctypes.c_int64
     E = int(f(ctypes.c_int(kind), ctypes.c_int(luni)))
     if E < 0:
         raise ValueError("unknown mesh kind or level")
+    if ndiv > 0:
+        E = E // 8 ** luni * ndiv ** 3
     prm = {MESH_BOX: (xc[0], xc[1], xc[2], box_dout),
            MESH_CUBEDSPHERES7: (cs_dc, cs_r0fac, 0.0, 0.0),
            MESH_SHELL6: (r_in, r_out, 0.0, 0.0)}[kind]
@@ -124,7 +127,7 @@ def generate_mesh(kind, n, luni, uniform=False, xc=(0.0, 0.0, 0.0), box_dout=1.0
     xyz = np.zeros((E, 3, npt))
     dXdx = np.zeros((E, 9, npt))
     rc = lib().nmo_mesh_generate(ctypes.c_int(kind), ctypes.c_int(n), ctypes.c_int(luni),
-                                 (ctypes.c_double * 4)(*prm), ctypes.c_int(int(uniform)),
+                                 ctypes.c_int(ndiv), (ctypes.c_double * 4)(*prm), ctypes.c_int(int(uniform)),
                                  pat.ctypes.data_as(ctypes.c_void_p),
                                  bbox.ctypes.data_as(ctypes.c_void_p),
                                  curvi.ctypes.data_as(ctypes.c_void_p),

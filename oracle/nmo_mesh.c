@@ -186,6 +186,24 @@ static void cs_map(const opatch *P, const double X[3], double x[3], double J[3][
   J[2][ib] = J[1][ia];
 }
 
+/* x and dX/dx at patch coordinates X of patch p of a generated mesh */
+int nmo_mesh_map(int type, const double prm[4], int p, const double X[3], double x[3],
+                 double J[3][3])
+{
+  opatch P[8];
+  int npat = make_patches(type, prm, P), d, c;
+  if (npat < 0 || p < 0 || p >= npat) return 1;
+  if (P[p].kind != OP_BOX) {
+    cs_map(&P[p], X, x, J);
+  } else {
+    for (d = 0; d < 3; d++) {
+      x[d] = X[d];
+      for (c = 0; c < 3; c++) J[d][c] = (d == c) ? 1. : 0.;
+    }
+  }
+  return 0;
+}
+
 /* elements of one patch at uniform level L: count per patch */
 int64_t nmo_mesh_count(int type, int luni)
 {
@@ -200,16 +218,16 @@ int64_t nmo_mesh_count(int type, int luni)
    with uniform != 0) at level luni: per element its patch, bbox (patch
    coordinates), a curvilinear flag, x [3][np] and dX/dx [9][np] (identity
    on Cartesian elements); elements patch by patch, Morton order inside. */
-int nmo_mesh_generate(int type, int n, int luni, const double prm[4], int uniform,
+int nmo_mesh_generate(int type, int n, int luni, int ndiv, const double prm[4], int uniform,
                       int32_t *pat, double *bbox, int32_t *curvi, double *xyz, double *dXdx)
 {
   opatch P[8];
   double px[64], pw[64];
   const int npts = n * n * n;
-  const int64_t per = (int64_t)1 << (3 * luni);
+  const int64_t per = ndiv > 0 ? (int64_t)ndiv * ndiv * ndiv : (int64_t)1 << (3 * luni);
   int npat, p;
   int64_t e = 0, mc;
-  if (n < 2 || n > 64 || nmo_mesh_count(type, luni) < 0) return 1;
+  if (n < 2 || n > 64 || nmo_mesh_count(type, luni) < 0 || ndiv < 0) return 1;
   npat = make_patches(type, prm, P);
   if (npat < 0) return 1;
   if (uniform) nmo_uniform(n, px);
@@ -218,17 +236,31 @@ int nmo_mesh_generate(int type, int n, int luni, const double prm[4], int unifor
     for (mc = 0; mc < per; mc++, e++) {
       double *bb = bbox + e * 6, LX[3];
       int ix[3] = {0, 0, 0}, bit, d, ll, i, j, k;
-      for (bit = 0; bit < luni; bit++)
-        for (d = 0; d < 3; d++) ix[d] |= (int)((mc >> (3 * bit + d)) & 1) << bit;
-      /* amr_set_elm0_bbox */
-      for (d = 0; d < 6; d++) bb[d] = P[p].bbox[d];
-      for (d = 0; d < 3; d++) LX[d] = bb[2 * d + 1] - bb[2 * d];
-      for (ll = 1; ll <= luni; ll++)
+      if (ndiv > 0) {
+        /* ndiv equal parts per direction, i fastest */
+        const double *pb = P[p].bbox;
+        ix[0] = (int)(mc % ndiv);
+        ix[1] = (int)((mc / ndiv) % ndiv);
+        ix[2] = (int)(mc / ((int64_t)ndiv * ndiv));
         for (d = 0; d < 3; d++) {
-          LX[d] /= 2.;
-          if ((ix[d] >> (luni - ll)) & 1) bb[2 * d] = bb[2 * d + 1] - LX[d];
-          else bb[2 * d + 1] = bb[2 * d] + LX[d];
+          bb[2 * d] = pb[2 * d] + (pb[2 * d + 1] - pb[2 * d]) * (double)ix[d] / ndiv;
+          bb[2 * d + 1] = ix[d] + 1 == ndiv
+                              ? pb[2 * d + 1]
+                              : pb[2 * d] + (pb[2 * d + 1] - pb[2 * d]) * (double)(ix[d] + 1) / ndiv;
         }
+      } else {
+        for (bit = 0; bit < luni; bit++)
+          for (d = 0; d < 3; d++) ix[d] |= (int)((mc >> (3 * bit + d)) & 1) << bit;
+        /* amr_set_elm0_bbox */
+        for (d = 0; d < 6; d++) bb[d] = P[p].bbox[d];
+        for (d = 0; d < 3; d++) LX[d] = bb[2 * d + 1] - bb[2 * d];
+        for (ll = 1; ll <= luni; ll++)
+          for (d = 0; d < 3; d++) {
+            LX[d] /= 2.;
+            if ((ix[d] >> (luni - ll)) & 1) bb[2 * d] = bb[2 * d + 1] - LX[d];
+            else bb[2 * d + 1] = bb[2 * d] + LX[d];
+          }
+      }
       pat[e] = p;
       curvi[e] = P[p].kind != OP_BOX;
       for (k = 0; k < n; k++)
