@@ -313,6 +313,61 @@ int nmg_grhd_sources(const nmg_grhd_params *g, int64_t npts, const double *alpha
                      const double *psi_dev, const double *dalpha_dev, const double *dpsi_dev,
                      const double *prim_dev, double *src_dev, void *stream);
 
+/* ---- GRHD evolution in the Cowling approximation ------------------------
+ * No counterpart in the reference (its GRHD is external; parity unpinned,
+ * checked against the oracle's restatement).  Densitized conserved fields
+ * (D, S_1, S_2, S_3, tau) on a fixed isotropic Schwarzschild background of
+ * mass `mass` (psi = 1 + M/(2r), alpha = (1 - M/(2r))/(1 + M/(2r)), zero
+ * shift; mass 0: flat), on an NMG_MESH_CUBEDSHELL6 mesh.  DG elements use
+ * the mesh's n LGL points: strong-form divergence with the chain rule
+ * (src/main/coordinates/derivs.c:102-181,756-815), LLF face flux and lift
+ * (src/main/dg/numflux1d.c:85-112, src/main/dg/dg.c:30-151), Cowling
+ * sources.  Elements in finite-volume mode use nf equally spaced points
+ * (nf = 0: 2n, the reference's PARENT_2n_P_UNIFORM, src/main/amr/refine.h:
+ * 32): primitives reconstructed at the midpoints (rec, NMG_FV_REC_*,
+ * src/main/dg/rec1d.c), LLF midpoint fluxes, conservative differences.
+ * Every stage runs con2prim (newton1d_brak, atmosphere floors) on its input.
+ * Outer faces (r_in, r_out) copy the interior state.  Host layouts: DG
+ * [nelem][5][n^3], finite volume [nfv][5][nf^3] for the finite-volume
+ * elements in ascending order. */
+typedef struct nmg_grhd_evolve_params {
+  nmg_grhd_params eos;
+  double mass;   /* background mass M (>= 0) */
+  int32_t nf;    /* finite-volume points per direction (0: 2n; 4..16) */
+  int32_t rec;   /* NMG_FV_REC_* midpoint reconstruction */
+} nmg_grhd_evolve_params;
+typedef struct nmg_grhd_ctx nmg_grhd_ctx;
+int nmg_grhd_create(const nmg_mesh *m, const nmg_grhd_evolve_params *p, nmg_grhd_ctx **out);
+void nmg_grhd_destroy(nmg_grhd_ctx *c);
+const char *nmg_grhd_last_error(const nmg_grhd_ctx *c);
+int nmg_grhd_sizes(const nmg_grhd_ctx *c, int32_t *n, int32_t *nf, int64_t *nelem);
+/* element modes (fv[e] = 1: finite volume) with the state transferred
+ * (trouble.c:162-183, gridpoints.c:158-200): to finite volume by Lagrange
+ * interpolation P from the LGL points to the nf equally spaced points in
+ * each direction, back by the pseudo-inverse R = (P^T P)^-1 P^T */
+int nmg_grhd_set_fv_elements(nmg_grhd_ctx *c, const int32_t *fv);
+int nmg_grhd_get_fv_elements(nmg_grhd_ctx *c, int32_t *fv);
+int64_t nmg_grhd_fv_count(const nmg_grhd_ctx *c);
+/* state from primitives (rho, v^1, v^2, v^3, p) (U = prim2con; the
+ * primitives are also the root finder's starting guesses) */
+int nmg_grhd_set_prim(nmg_grhd_ctx *c, const double *prim_dg, const double *prim_fv);
+/* conserved state in/out, with the primitives (guesses; may be NULL) */
+int nmg_grhd_set_state(nmg_grhd_ctx *c, const double *u_dg, const double *u_fv,
+                       const double *prim_dg, const double *prim_fv);
+int nmg_grhd_get_state(nmg_grhd_ctx *c, double *u_dg, double *u_fv, double *prim_dg,
+                       double *prim_fv);
+/* r = RHS of the resident state after its con2prim (which, as in the first
+ * stage of a step, may reset atmosphere points of the state) */
+int nmg_grhd_rhs(nmg_grhd_ctx *c, double *r_dg, double *r_fv);
+/* nsteps RK4 steps (RungeKutta.c:19-82), graph-captured */
+int nmg_grhd_rk4_steps(nmg_grhd_ctx *c, double dt, int32_t nsteps);
+/* root-finder iterations and atmosphere points summed over every con2prim
+ * since the last reset, and the kernels launched */
+int nmg_grhd_stats(nmg_grhd_ctx *c, int64_t *c2p_iterations, int64_t *atmosphere_points,
+                   int64_t *launches);
+int nmg_grhd_reset_stats(nmg_grhd_ctx *c);
+void *nmg_grhd_stream(nmg_grhd_ctx *c);
+
 /* numerical flux of a context (default NMG_NUMFLUX_LLF, what the workloads
  * use); the adjoint entry points support LLF only */
 int nmg_set_numflux(nmg_ctx *c, int32_t kind);

@@ -213,6 +213,21 @@ def lib(build_if_missing=True):
         "nmg_grhd_con2prim": (ctypes.c_int, [vp, i64, vp, vp, vp, vp, vp]),
         "nmg_grhd_fluxes": (ctypes.c_int, [vp, i64, i32, vp, vp, vp, vp, vp, vp]),
         "nmg_grhd_sources": (ctypes.c_int, [vp, i64, vp, vp, vp, vp, vp, vp, vp]),
+        "nmg_grhd_create": (ctypes.c_int, [vp, vp, vp]),
+        "nmg_grhd_destroy": (None, [vp]),
+        "nmg_grhd_last_error": (ctypes.c_char_p, [vp]),
+        "nmg_grhd_sizes": (ctypes.c_int, [vp, vp, vp, vp]),
+        "nmg_grhd_set_fv_elements": (ctypes.c_int, [vp, vp]),
+        "nmg_grhd_get_fv_elements": (ctypes.c_int, [vp, vp]),
+        "nmg_grhd_fv_count": (i64, [vp]),
+        "nmg_grhd_set_prim": (ctypes.c_int, [vp, vp, vp]),
+        "nmg_grhd_set_state": (ctypes.c_int, [vp, vp, vp, vp, vp]),
+        "nmg_grhd_get_state": (ctypes.c_int, [vp, vp, vp, vp, vp]),
+        "nmg_grhd_rhs": (ctypes.c_int, [vp, vp, vp]),
+        "nmg_grhd_rk4_steps": (ctypes.c_int, [vp, f64, i32]),
+        "nmg_grhd_stats": (ctypes.c_int, [vp, vp, vp, vp]),
+        "nmg_grhd_reset_stats": (ctypes.c_int, [vp]),
+        "nmg_grhd_stream": (vp, [vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -726,3 +741,108 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+class _GrhdEvolveParams(ctypes.Structure):
+    _fields_ = [("eos", GrhdParams), ("mass", ctypes.c_double), ("nf", ctypes.c_int32),
+                ("rec", ctypes.c_int32)]
+
+
+class GrhdEvolution:
+    """GRHD in the Cowling approximation on a cubed-shell mesh
+    (include/nmg.h nmg_grhd_*): DG elements on the mesh's LGL points,
+    finite-volume elements on nf equally spaced points.  States on the host
+    are (u_dg [E, 5, n^3], u_fv [nfv, 5, nf^3]) with the finite-volume rows
+    in ascending element order."""
+
+    def __init__(self, mesh, mass=1.0, gamma=2.0, rho_atm=1e-10, p_atm=1e-16, tol=1e-15,
+                 maxits=100, nf=0, rec="WENOm5_2"):
+        self.mesh = mesh
+        p = _GrhdEvolveParams(GrhdParams(gamma, rho_atm, p_atm, tol, maxits), float(mass),
+                              int(nf), FV_REC[rec])
+        h = ctypes.c_void_p()
+        rc = lib().nmg_grhd_create(mesh._h, ctypes.byref(p), ctypes.byref(h))
+        self._h = h
+        if rc:
+            msg = lib().nmg_grhd_last_error(h).decode() if h.value else ""
+            self.close()
+            raise NmgError(f"nmg_grhd_create failed ({rc}): {msg}")
+        n, nf_, E = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int64()
+        lib().nmg_grhd_sizes(self._h, ctypes.byref(n), ctypes.byref(nf_), ctypes.byref(E))
+        self.n, self.nf, self.nelem = n.value, nf_.value, E.value
+
+    def _check(self, rc, what):
+        if rc:
+            raise NmgError(f"{what} failed ({rc}): {lib().nmg_grhd_last_error(self._h).decode()}")
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            lib().nmg_grhd_destroy(self._h)
+        self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def nfv(self):
+        return int(lib().nmg_grhd_fv_count(self._h))
+
+    @property
+    def stream(self):
+        return lib().nmg_grhd_stream(self._h)
+
+    def set_fv_elements(self, fv):
+        fv = np.ascontiguousarray(fv, np.int32)
+        self._check(lib().nmg_grhd_set_fv_elements(self._h, _ptr(fv)), "nmg_grhd_set_fv_elements")
+
+    def fv_elements(self):
+        fv = np.zeros(self.nelem, np.int32)
+        self._check(lib().nmg_grhd_get_fv_elements(self._h, _ptr(fv)), "nmg_grhd_get_fv_elements")
+        return fv
+
+    def _shapes(self):
+        return (self.nelem, 5, self.n ** 3), (self.nfv, 5, self.nf ** 3)
+
+    def set_prim(self, prim_dg, prim_fv=None):
+        sd, sf = self._shapes()
+        pd = np.ascontiguousarray(np.broadcast_to(prim_dg, sd), np.float64)
+        pf = np.ascontiguousarray(np.zeros(sf) if prim_fv is None else prim_fv, np.float64)
+        self._check(lib().nmg_grhd_set_prim(self._h, _ptr(pd), _ptr(pf)), "nmg_grhd_set_prim")
+
+    def set_state(self, u_dg, u_fv, prim_dg=None, prim_fv=None):
+        sd, sf = self._shapes()
+        arr = [np.ascontiguousarray(a, np.float64) if a is not None else None
+               for a in (u_dg, u_fv, prim_dg, prim_fv)]
+        ptrs = [_ptr(a) if a is not None else None for a in arr]
+        self._check(lib().nmg_grhd_set_state(self._h, *ptrs), "nmg_grhd_set_state")
+
+    def get_state(self):
+        """(u_dg, u_fv, prim_dg, prim_fv)"""
+        sd, sf = self._shapes()
+        out = [np.zeros(sd), np.zeros(sf), np.zeros(sd), np.zeros(sf)]
+        self._check(lib().nmg_grhd_get_state(self._h, *(_ptr(a) for a in out)),
+                    "nmg_grhd_get_state")
+        return tuple(out)
+
+    def rhs(self):
+        sd, sf = self._shapes()
+        r_dg, r_fv = np.zeros(sd), np.zeros(sf)
+        self._check(lib().nmg_grhd_rhs(self._h, _ptr(r_dg), _ptr(r_fv)), "nmg_grhd_rhs")
+        return r_dg, r_fv
+
+    def rk4_steps(self, dt, nsteps):
+        self._check(lib().nmg_grhd_rk4_steps(self._h, float(dt), int(nsteps)),
+                    "nmg_grhd_rk4_steps")
+
+    def stats(self):
+        """(con2prim iterations, atmosphere points, kernel launches)"""
+        a, b, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        self._check(lib().nmg_grhd_stats(self._h, ctypes.byref(a), ctypes.byref(b),
+                                         ctypes.byref(c)), "nmg_grhd_stats")
+        return a.value, b.value, c.value
+
+    def reset_stats(self):
+        self._check(lib().nmg_grhd_reset_stats(self._h), "nmg_grhd_reset_stats")

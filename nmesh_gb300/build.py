@@ -12,11 +12,11 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libnmg.so")
 SOURCES = ["nmg.cu", "stage_eo.cu", "stage_gather.cu", "stage_fv.cu", "stage_fv_fast.cu",
-           "grhd.cu", "noalloc.cu", "mesh.cpp", "ckpt.cpp"]
+           "grhd.cu", "grhd_evolve.cu", "noalloc.cu", "mesh.cpp", "ckpt.cpp"]
 # per-file extra flags: the finite-volume kernel rounds every product and sum
 # separately, in the reference's order (no FMA contraction)
 EXTRA_FLAGS = {"stage_fv.cu": ["-fmad=false"], "grhd.cu": ["-fmad=false"]}
-HEADERS = ["mesh.h", "stage.cuh", "ctx.h",os.path.join("..", "..", "include", "nmg.h")]
+HEADERS = ["mesh.h", "stage.cuh", "ctx.h", "weno.cuh", "grhd.cuh",os.path.join("..", "..", "include", "nmg.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
                      "-Xcompiler", "-fPIC,-ffp-contract=off", "-Xptxas", "-v"]

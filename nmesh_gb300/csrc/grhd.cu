@@ -27,89 +27,16 @@
 
 namespace {
 
-struct C2P {
-  double D, tau, S2, gm1, gam;
-  __device__ void operator()(double p, double *f, double *df) const {
-    const double E = tau + D + p;
-    const double v2 = S2 / (E * E);
-    const double W = 1. / sqrt(1. - v2);
-    const double rho = D / W;
-    const double eps = (tau + D * (1. - W) + p * (1. - W * W)) / (D * W);
-    const double cs2 = gam * gm1 * eps / (1. + gam * eps);
-    *f = gm1 * rho * eps - p;
-    *df = v2 * cs2 - 1.;
-  }
-};
-
-// newton1d_brak: iterations (>= 0) or a negative error code, root in *x0
-template <class F>
-__device__ int newton1d_brak(double *x0, const F &fdf, double x1, double x2, int maxits,
-                             double xacc) {
-  int j, bisect;
-  double f, fh, fl, df, xh, xl, xrt, dx, dxold, tmp;
-  if (!isfinite(x1) || !isfinite(x2)) return -2 * maxits - 2;
-  if ((x1 <= *x0 && *x0 <= x2) || (x2 <= *x0 && *x0 <= x1)) xrt = *x0;
-  else xrt = 0.5 * (x1 + x2);
-  fdf(x1, &fl, &df);
-  fdf(x2, &fh, &df);
-  j = 0;
-  if (fl <= 0.0 && fh >= 0.0) j = 1;
-  if (fl >= 0.0 && fh <= 0.0) j = 1;
-  if (!j) return -2 * maxits - 3;
-  if (fl == 0.0) { *x0 = x1; return 0; }
-  if (fh == 0.0) { *x0 = x2; return 0; }
-  if (fl < 0.0) { xl = x1; xh = x2; }
-  else { xh = x1; xl = x2; }
-  dxold = fabs(x2 - x1);
-  dx = dxold;
-  for (j = 1; j <= maxits; j++) {
-    fdf(xrt, &f, &df);
-    if (!isfinite(f)) return -j;
-    if (f == 0.0) { *x0 = xrt; return j; }
-    if (f < 0.0) xl = xrt;
-    else xh = xrt;
-    if (!isfinite(df)) bisect = 1;
-    else bisect = (fabs(2.0 * f) > fabs(dxold * df));
-    if (bisect == 0) {
-      dxold = dx;
-      dx = f / df;
-      tmp = xrt;
-      xrt -= dx;
-      if (((xrt - xh) * (xrt - xl) > 0.0) || (tmp == xrt)) {
-        bisect = 1; xrt = tmp; dx = dxold;
-      }
-    }
-    if (bisect) {
-      dxold = dx;
-      dx = 0.5 * (xh - xl);
-      xrt = xl + dx;
-      if (xl == xrt) { *x0 = xrt; return j; }
-    }
-    if (fabs(dx) < xacc) { *x0 = xrt; return j; }
-  }
-  *x0 = xrt;
-  return j;
-}
+#include "grhd.cuh"
 
 __global__ void prim2con_kernel(nmg_grhd_params g, int64_t npts, const double *psi,
                                 const double *prim, double *cons) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < npts;
        i += (int64_t)gridDim.x * blockDim.x) {
-    const double ps = psi ? psi[i] : 1.;
-    const double ps4 = ps * ps * ps * ps, ps6 = ps4 * ps * ps;
-    const double rho = prim[i], vx = prim[npts + i], vy = prim[2 * npts + i];
-    const double vz = prim[3 * npts + i], p = prim[4 * npts + i];
-    const double v2 = ps4 * (vx * vx + vy * vy + vz * vz);
-    const double W = 1. / sqrt(1. - v2);
-    const double eps = p / ((g.gamma - 1.) * rho);
-    const double h = 1. + eps + p / rho;
-    const double rhW2 = rho * h * W * W;
-    const double D = ps6 * rho * W;
-    cons[i] = D;
-    cons[npts + i] = ps6 * rhW2 * ps4 * vx;
-    cons[2 * npts + i] = ps6 * rhW2 * ps4 * vy;
-    cons[3 * npts + i] = ps6 * rhW2 * ps4 * vz;
-    cons[4 * npts + i] = ps6 * (rhW2 - p) - D;
+    double P[5], U[5];
+    for (int f = 0; f < 5; f++) P[f] = prim[f * npts + i];
+    p2c_point(g, psi ? psi[i] : 1., P, U);
+    for (int f = 0; f < 5; f++) cons[f * npts + i] = U[f];
   }
 }
 
@@ -117,56 +44,15 @@ __global__ void con2prim_kernel(nmg_grhd_params g, int64_t npts, const double *p
                                 double *cons, double *prim, int32_t *status) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < npts;
        i += (int64_t)gridDim.x * blockDim.x) {
-    const double ps = psi ? psi[i] : 1.;
-    const double ps4 = ps * ps * ps * ps, ps6 = ps4 * ps * ps;
-    const double D = cons[i] / ps6, Sx = cons[npts + i] / ps6, Sy = cons[2 * npts + i] / ps6;
-    const double Sz = cons[3 * npts + i] / ps6, tau = cons[4 * npts + i] / ps6;
-    const double S2 = (Sx * Sx + Sy * Sy + Sz * Sz) / ps4;
-    C2P q{D, tau, S2, g.gamma - 1., g.gamma};
-    int rc = -1;
-    if (D >= g.rho_atm && isfinite(D) && isfinite(tau) && isfinite(S2)) {
-      const double S = sqrt(S2);
-      double plo = S - tau - D;
-      plo = plo > 0. ? plo * (1. + 1e-14) : 0.;
-      double phi = q.gm1 * (tau + D);
-      if (phi < plo) phi = 2. * plo;
-      if (phi <= 0.) phi = 1e-300;
-      for (int k = 0; k < 200; k++) {
-        double f, df;
-        q(phi, &f, &df);
-        if (f < 0.) break;
-        phi *= 2.;
-      }
-      double p = prim[4 * npts + i];
-      const double xacc = g.tol * phi;
-      rc = newton1d_brak(&p, q, plo, phi, g.maxits, xacc);
-      if (rc >= 0) {
-        const double E = tau + D + p;
-        const double v2 = S2 / (E * E);
-        const double W = 1. / sqrt(1. - v2);
-        const double rho = D / W;
-        if (!(rho >= g.rho_atm) || !(p > 0.) || !isfinite(W)) {
-          rc = -1;
-        } else {
-          const double fac = 1. / (E * ps4);
-          prim[i] = rho;
-          prim[npts + i] = Sx * fac;
-          prim[2 * npts + i] = Sy * fac;
-          prim[3 * npts + i] = Sz * fac;
-          prim[4 * npts + i] = p;
-        }
-      }
+    double P[5], U[5];
+    for (int f = 0; f < 5; f++) {
+      U[f] = cons[f * npts + i];
+      P[f] = prim[f * npts + i];
     }
-    if (rc < 0) {
-      const double eps_atm = g.p_atm / ((g.gamma - 1.) * g.rho_atm);
-      const double h = 1. + eps_atm + g.p_atm / g.rho_atm;
-      prim[i] = g.rho_atm;
-      prim[npts + i] = prim[2 * npts + i] = prim[3 * npts + i] = 0.;
-      prim[4 * npts + i] = g.p_atm;
-      const double Da = ps6 * g.rho_atm;
-      cons[i] = Da;
-      cons[npts + i] = cons[2 * npts + i] = cons[3 * npts + i] = 0.;
-      cons[4 * npts + i] = ps6 * (g.rho_atm * h - g.p_atm) - Da;
+    const int rc = c2p_point(g, psi ? psi[i] : 1., U, P);
+    for (int f = 0; f < 5; f++) {
+      cons[f * npts + i] = U[f];
+      prim[f * npts + i] = P[f];
     }
     status[i] = rc;
   }

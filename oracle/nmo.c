@@ -1720,3 +1720,14 @@ void nmo_grhd_sources(const nmo_grhd *g, int64_t npts, const double *alpha, cons
     src[4 * npts + i] = -ps6 * rhW2 * vda;
   }
 }
+
+/* the midpoint reconstructions for other translation units of the oracle */
+double nmo_rec_p(int mode, int n, const double *u, int im, double r3)
+{
+  return rec_p(mode, n, u, im, r3);
+}
+
+double nmo_rec_m(int mode, int n, const double *u, int im, double r3)
+{
+  return rec_m(mode, n, u, im, r3);
+}

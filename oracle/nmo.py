@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libnmo.so")
 # the restated RHS / steps / GRHD pieces, and the oracle's own mesh generator
-SOURCES = ["nmo.c", "nmo_mesh.c"]
+SOURCES = ["nmo.c", "nmo_mesh.c", "nmo_grhd.c"]
 
 
 def build(verbose=False):
@@ -147,10 +147,29 @@ def match_faces_conforming(xyz, n, period=None):
     per = None if period is None else (ctypes.c_double * 3)(*([float(period)] * 3))
     rc = lib().nmo_match_faces(ctypes.c_int64(E), ctypes.c_int(n),
                                xyz.ctypes.data_as(ctypes.c_void_p), per,
-                               nb.ctypes.data_as(ctypes.c_void_p))
+                               nb.ctypes.data_as(ctypes.c_void_p), None, None)
     if rc:
         raise ValueError("nmo_match_faces: faces do not match conformingly")
     return nb
+
+
+def face_table(xyz, n, period=None):
+    """Face table of a conforming mesh: nb[E, 6] neighbour element (-1
+    outer) and code[E, 6] = neighbour face | orientation << 3."""
+    xyz = np.ascontiguousarray(xyz, np.float64)
+    E = xyz.shape[0]
+    nbn = np.empty((E, 6, n * n), np.int64)
+    nb = np.empty((E, 6), np.int32)
+    code = np.empty((E, 6), np.int32)
+    per = None if period is None else (ctypes.c_double * 3)(*([float(period)] * 3))
+    rc = lib().nmo_match_faces(ctypes.c_int64(E), ctypes.c_int(n),
+                               xyz.ctypes.data_as(ctypes.c_void_p), per,
+                               nbn.ctypes.data_as(ctypes.c_void_p),
+                               nb.ctypes.data_as(ctypes.c_void_p),
+                               code.ctypes.data_as(ctypes.c_void_p))
+    if rc:
+        raise ValueError("nmo_match_faces: faces do not match conformingly")
+    return nb, code
 
 
 def face_plane_index(n, f):
@@ -600,3 +619,140 @@ def grhd_sources(prim, alpha, psi, dalpha, dpsi, gamma=2.0):
                            prim.ctypes.data_as(ctypes.c_void_p),
                            src.ctypes.data_as(ctypes.c_void_p))
     return src
+
+
+class _GrMesh(ctypes.Structure):
+    _fields_ = [("nelem", ctypes.c_int), ("n", ctypes.c_int), ("nf", ctypes.c_int),
+                ("mesh_type", ctypes.c_int), ("prm", ctypes.c_double * 4),
+                ("pat", ctypes.c_void_p), ("bbox", ctypes.c_void_p), ("xyz", ctypes.c_void_p),
+                ("dXdx", ctypes.c_void_p), ("nb", ctypes.c_void_p), ("code", ctypes.c_void_p),
+                ("fv", ctypes.c_void_p), ("g", _Grhd), ("mass", ctypes.c_double),
+                ("rec", ctypes.c_int)]
+
+
+class GrhdOracle:
+    """The GRHD Cowling evolution restated in C (oracle/nmo_grhd.c) on the
+    oracle's own cubed-shell mesh (oracle/nmo_mesh.c): six CubedShell
+    patches between r_in and r_out, ndiv^3 elements each, n LGL points per
+    direction on DG elements and nf equally spaced points on the
+    finite-volume elements fv[e] = 1.
+
+    States are kept per point type for every element, [E, 5, n^3] and
+    [E, 5, nf^3]; only the DG rows of DG elements and the FV rows of FV
+    elements are used.  prim_* hold the root finder's starting guesses."""
+
+    def __init__(self, n, nf, ndiv, r_in=2.0, r_out=20.0, fv=None, mass=1.0, gamma=2.0,
+                 rho_atm=1e-10, p_atm=1e-16, tol=1e-15, maxits=100, rec="WENOm5_2"):
+        self.n, self.nf = int(n), int(nf)
+        self.prm = (float(r_in), float(r_out), 0.0, 0.0)
+        self.pat, self.bbox, curvi, self.xyz, self.dXdx = generate_mesh(
+            MESH_SHELL6, self.n, 0, r_in=r_in, r_out=r_out, ndiv=ndiv)
+        self.nelem = len(self.pat)
+        self.nb, self.code = face_table(self.xyz, self.n)
+        self.fv = np.zeros(self.nelem, np.int32) if fv is None else \
+            np.ascontiguousarray(fv, np.int32)
+        self.g = _Grhd(gamma, rho_atm, p_atm, tol, maxits)
+        self.mass, self.rec = float(mass), FV_REC[rec]
+        self._sync()
+
+    def _sync(self):
+        self.s = _GrMesh(self.nelem, self.n, self.nf, MESH_SHELL6, (ctypes.c_double * 4)(*self.prm),
+                         self.pat.ctypes.data, self.bbox.ctypes.data, self.xyz.ctypes.data,
+                         self.dXdx.ctypes.data, self.nb.ctypes.data, self.code.ctypes.data,
+                         self.fv.ctypes.data, self.g, self.mass, self.rec)
+
+    @property
+    def shapes(self):
+        return (self.nelem, 5, self.n ** 3), (self.nelem, 5, self.nf ** 3)
+
+    def points(self, e, fvpts):
+        """Cartesian coordinates [3, npts] of element e's LGL nodes or
+        equally spaced points."""
+        npts = (self.nf if fvpts else self.n) ** 3
+        out = np.zeros((3, npts))
+        lib().nmo_gr_points(ctypes.byref(self.s), ctypes.c_int(int(e)), ctypes.c_int(int(fvpts)),
+                            out.ctypes.data_as(ctypes.c_void_p))
+        return out
+
+    def background(self, xyz):
+        """alpha, psi, d alpha [3], d psi [3] at points xyz [3, npts]."""
+        out = np.zeros((8, xyz.shape[1]))
+        bg = (ctypes.c_double * 8)()
+        f = lib().nmo_gr_background
+        f.restype = None
+        for q in range(xyz.shape[1]):
+            f(ctypes.c_double(self.mass), (ctypes.c_double * 3)(*xyz[:, q]), bg)
+            out[:, q] = list(bg)
+        return out
+
+    def psi(self, xyz):
+        """psi = 1 + M/(2r) at points xyz [3, npts] (as the background)."""
+        r = np.sqrt(xyz[0] * xyz[0] + xyz[1] * xyz[1] + xyz[2] * xyz[2])
+        return 1. + 0.5 * self.mass / r
+
+    def set_fv(self, fv):
+        self.fv = np.ascontiguousarray(fv, np.int32)
+        self._sync()
+
+    def prim2con(self, prim, psi):
+        prim = np.ascontiguousarray(prim, np.float64)
+        cons = np.zeros_like(prim)
+        psi = np.ascontiguousarray(psi, np.float64)
+        lib().nmo_grhd_prim2con(ctypes.byref(self.g), ctypes.c_int64(prim.shape[-1]),
+                                psi.ctypes.data_as(ctypes.c_void_p),
+                                prim.ctypes.data_as(ctypes.c_void_p),
+                                cons.ctypes.data_as(ctypes.c_void_p))
+        return cons
+
+    def con2prim(self, u_dg, u_fv, prim_dg, prim_fv):
+        """In place; returns (atmosphere points, root-finder iterations)."""
+        it = ctypes.c_int64(0)
+        f = lib().nmo_gr_con2prim
+        f.restype = ctypes.c_int64
+        natm = f(ctypes.byref(self.s), *(a.ctypes.data_as(ctypes.c_void_p)
+                                         for a in (u_dg, u_fv, prim_dg, prim_fv)),
+                 ctypes.byref(it))
+        return int(natm), int(it.value)
+
+    def rhs(self, u_dg, u_fv, prim_dg, prim_fv):
+        """(r_dg, r_fv) of copies of the states after their con2prim."""
+        w_dg, w_fv = u_dg.copy(), u_fv.copy()
+        p_dg, p_fv = prim_dg.copy(), prim_fv.copy()
+        self.con2prim(w_dg, w_fv, p_dg, p_fv)
+        r_dg, r_fv = np.zeros_like(w_dg), np.zeros_like(w_fv)
+        rc = lib().nmo_gr_rhs(ctypes.byref(self.s), *(a.ctypes.data_as(ctypes.c_void_p) for a in
+                                                      (w_dg, w_fv, p_dg, p_fv, r_dg, r_fv)))
+        if rc:
+            raise RuntimeError("nmo_gr_rhs failed")
+        return r_dg, r_fv
+
+    def rk4(self, u_dg, u_fv, prim_dg, prim_fv, dt, nsteps):
+        """nsteps RK4 steps of copies; returns (u_dg, u_fv, prim_dg, prim_fv)."""
+        out = [np.array(a, np.float64, copy=True, order="C")
+               for a in (u_dg, u_fv, prim_dg, prim_fv)]
+        rc = lib().nmo_gr_rk4(ctypes.byref(self.s), ctypes.c_double(dt), ctypes.c_int(nsteps),
+                              *(a.ctypes.data_as(ctypes.c_void_p) for a in out))
+        if rc:
+            raise RuntimeError("nmo_gr_rk4 failed")
+        return tuple(out)
+
+    def transfer(self):
+        """(P [nf, n], R [n, nf]): LGL -> equally spaced and back."""
+        P = np.zeros((self.nf, self.n))
+        R = np.zeros((self.n, self.nf))
+        lib().nmo_gr_transfer(ctypes.c_int(self.n), ctypes.c_int(self.nf),
+                              P.ctypes.data_as(ctypes.c_void_p), R.ctypes.data_as(ctypes.c_void_p))
+        return P, R
+
+    def apply3(self, A, v):
+        """(A x A x A) v for every field of one element: v [5, ni^3]."""
+        no, ni = A.shape
+        A = np.ascontiguousarray(A)
+        out = np.zeros((v.shape[0], no ** 3))
+        for f in range(v.shape[0]):
+            src = np.ascontiguousarray(v[f])
+            dst = np.zeros(no ** 3)
+            lib().nmo_gr_apply3(ctypes.c_int(ni), ctypes.c_int(no), A.ctypes.data_as(ctypes.c_void_p),
+                                src.ctypes.data_as(ctypes.c_void_p), dst.ctypes.data_as(ctypes.c_void_p))
+            out[f] = dst
+        return out

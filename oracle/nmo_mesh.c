@@ -343,9 +343,13 @@ static int same_point(const double p[3], const double q[3], const double *period
 }
 
 /* nbnode[E][6][n*n]: global index e'*np + ijk' of the coincident node across
-   each face node, -1 on outer faces.  period may be NULL.  Returns 0, or 1
+   each face node, -1 on outer faces; nb[E][6] / code[E][6] (may be NULL):
+   the neighbour element (-1 outer) and its face | orientation << 3, node
+   (a, b) lying at the neighbour's (a', b') = (s ? b : a, s ? a : b),
+   reversed per axis by bits 1 and 2 (s = bit 0).  period may be NULL.  Returns 0, or 1
    when a face is matched more than once or its corners do not coincide. */
-int nmo_match_faces(int64_t E, int n, const double *xyz, const double *period, int64_t *nbnode)
+int nmo_match_faces(int64_t E, int n, const double *xyz, const double *period, int64_t *nbnode,
+                    int32_t *nb, int32_t *code)
 {
   const int npts = n * n * n, nn = n * n;
   const double h = 1e-6, tol = 1e-9;
@@ -354,6 +358,10 @@ int nmo_match_faces(int64_t E, int n, const double *xyz, const double *period, i
   int rc = 0;
   if (!keys) return 2;
   for (q = 0; q < E * 6 * nn; q++) nbnode[q] = -1;
+  if (nb)
+    for (q = 0; q < E * 6; q++) nb[q] = -1;
+  if (code)
+    for (q = 0; q < E * 6; q++) code[q] = 0;
   for (q = 0; q < E * 6; q++) {
     const int64_t e = q / 6;
     const int f = (int)(q % 6);
@@ -404,6 +412,8 @@ int nmo_match_faces(int64_t E, int n, const double *xyz, const double *period, i
           rc = 1;
           break;
         }
+        if (nb) nb[e * 6 + f] = (int32_t)e2;
+        if (code) code[e * 6 + f] = f2 | (found << 3);
         for (b = 0; b < n; b++)
           for (a = 0; a < n; a++) {
             int aa = (found & 1) ? b : a, bb = (found & 1) ? a : b;

@@ -173,3 +173,29 @@ def big_case_u0(d, meta):
     """u0 of the slim fixture in the reference's element order."""
     n = meta["n"]
     return dump_noise(meta["seed"], meta["eps"], len(d["pat"]), n ** 3)
+
+
+def grhd_blob(o, seed, rho0=1e-3, K=100.0, center=(8.0, 0.0, 0.0), width=2.0, pert=0.01,
+              vel=(0.0, 0.0, 0.0)):
+    """Seeded Gaussian density blob on the GRHD oracle's mesh `o`
+    (oracle.nmo.GrhdOracle): rho = rho_atm + rho0 exp(-|x - c|^2 / width^2)
+    (1 + pert U(-1, 1)), polytropic p = K rho^2, velocity `vel`; on every
+    element's LGL nodes and equally spaced points.  Returns (prim_dg [E, 5,
+    n^3], prim_fv [E, 5, nf^3], u_dg, u_fv) (conserved via the oracle)."""
+    rng = np.random.default_rng(seed)
+    (E, _, npd), (_, _, npf) = o.shapes
+    out = [np.zeros((E, 5, npd)), np.zeros((E, 5, npf))]
+    cons = [np.zeros((E, 5, npd)), np.zeros((E, 5, npf))]
+    c = np.asarray(center, float)[:, None]
+    for e in range(E):
+        for k, fvp in enumerate((False, True)):
+            x = o.points(e, fvp)
+            r2 = ((x - c) ** 2).sum(0)
+            rho = o.g.rho_atm + rho0 * np.exp(-r2 / width ** 2) * \
+                (1.0 + pert * rng.uniform(-1.0, 1.0, x.shape[1]))
+            P = out[k][e]
+            P[0] = rho
+            P[1], P[2], P[3] = vel
+            P[4] = K * rho * rho
+            cons[k][e] = o.prim2con(P, o.psi(x))
+    return out[0], out[1], cons[0], cons[1]

@@ -1,0 +1,121 @@
+"""The GRHD Cowling evolution on the GPU (include/nmg.h nmg_grhd_*) against
+the oracle's restatement (oracle/nmo_grhd.c) on the same cubed shell:
+right-hand side and RK4 steps on mixed DG / finite-volume meshes (relative
+L2 <= 1e-12 per field group), the DG <-> finite-volume transfer, and the
+known answers (a uniform state at rest keeps a zero DG right-hand side)."""
+import numpy as np
+import pytest
+
+import nmesh_gb300 as ng
+from helpers import grhd_blob, rel_l2
+from oracle import nmo
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-12
+
+
+@pytest.fixture(autouse=True)
+def _gpu(cuda_ok):
+    yield
+
+
+def _case(n, nf, ndiv, fv_elems, mass=1.0, rec="WENOm5_2", seed=3, vel=(0.0, 0.0, 0.0)):
+    E = 6 * ndiv ** 3
+    fv = np.zeros(E, np.int32)
+    fv[list(fv_elems)] = 1
+    kw = dict(mass=mass, p_atm=1e-18, rho_atm=1e-10, tol=1e-15, maxits=100)
+    o = nmo.GrhdOracle(n=n, nf=nf, ndiv=ndiv, fv=fv, rec=rec, **kw)
+    pd, pf, ud, uf = grhd_blob(o, seed=seed, vel=vel)
+    m = ng.Mesh.build(ng.MESH_CUBEDSHELL6, n=n, ndiv=ndiv, shell_rin=2.0, shell_rout=20.0)
+    ev = ng.GrhdEvolution(m, nf=nf, rec=rec, **kw)
+    ev.set_fv_elements(fv)
+    ev.set_prim(pd, pf[fv == 1])
+    return o, ev, fv, (ud, uf, pd, pf)
+
+
+def _compare(fv, got_dg, got_fv, want_dg, want_fv, tol):
+    dg = fv == 0
+    for f in range(5):
+        assert rel_l2(got_dg[dg][:, f], want_dg[dg][:, f]) <= tol, ("dg", f)
+        if fv.any():
+            assert rel_l2(got_fv[:, f], want_fv[fv == 1][:, f]) <= tol, ("fv", f)
+
+
+@pytest.mark.parametrize("n,nf,rec", [(5, 9, "WENOm5_2"), (5, 10, "WENOm3_2"), (7, 13, "WENOm5_2"),
+                                      (4, 8, "WENOmZ_2")])
+def test_rhs_matches_oracle(n, nf, rec):
+    o, ev, fv, (ud, uf, pd, pf) = _case(n, nf, 2, [1, 3, 10, 11, 20, 33, 47], rec=rec)
+    u_dg, u_fv, _, _ = ev.get_state()
+    _compare(fv, u_dg, u_fv, ud, uf, 1e-14)
+    r_dg, r_fv = ev.rhs()
+    want_dg, want_fv = o.rhs(ud, uf, pd, pf)
+    _compare(fv, r_dg, r_fv, want_dg, want_fv, RTOL)
+
+
+@pytest.mark.parametrize("mass", [1.0, 0.0])
+def test_rk4_steps_match_oracle(mass):
+    """Three RK4 steps with con2prim every stage, a moving blob crossing DG
+    and finite-volume elements (nf = 2n - 1 points)."""
+    o, ev, fv, (ud, uf, pd, pf) = _case(5, 9, 2, [0, 4, 9, 10, 22, 40], mass=mass,
+                                         vel=(0.05, -0.03, 0.02))
+    dt = 0.02
+    ev.rk4_steps(dt, 3)
+    got = ev.get_state()
+    want = o.rk4(ud, uf, pd, pf, dt, 3)
+    _compare(fv, got[0], got[1], want[0], want[1], RTOL)
+    it, natm, launches = ev.stats()
+    assert it > 0 and launches >= 3 * 4 * 3
+
+
+def test_switch_transfers_the_state_like_the_oracle():
+    """DG -> finite volume by P x P x P (Lagrange to 2n equally spaced
+    points, the reference's PARENT_2n_P_UNIFORM), back by R = (P^T P)^-1 P^T;
+    the round trip returns the DG state."""
+    n, nf = 5, 10
+    o, ev, fv, (ud, uf, pd, pf) = _case(n, nf, 2, [])
+    u0 = ev.get_state()[0]
+    P, R = o.transfer()
+    sel = [2, 7, 30]
+    fv2 = np.zeros(48, np.int32)
+    fv2[sel] = 1
+    ev.set_fv_elements(fv2)
+    u_dg, u_fv, _, _ = ev.get_state()
+    for k, e in enumerate(sel):
+        want = o.apply3(P, u0[e])
+        assert rel_l2(u_fv[k], want) <= 1e-14
+    ev.set_fv_elements(np.zeros(48, np.int32))
+    back = ev.get_state()[0]
+    for e in sel:
+        assert rel_l2(back[e], u0[e]) <= 1e-13
+        assert rel_l2(back[e], o.apply3(R, o.apply3(P, u0[e]))) <= 1e-14
+    others = np.setdiff1d(np.arange(48), sel)
+    assert np.array_equal(back[others], u0[others])
+
+
+def test_uniform_state_at_rest_keeps_a_zero_dg_rhs():
+    n = 5
+    m = ng.Mesh.build(ng.MESH_CUBEDSHELL6, n=n, ndiv=2, shell_rin=2.0, shell_rout=20.0)
+    ev = ng.GrhdEvolution(m, mass=0.0, p_atm=1e-18)
+    prim = np.zeros((48, 5, n ** 3))
+    prim[:, 0], prim[:, 4] = 1.0, 0.01
+    ev.set_prim(prim)
+    r_dg, _ = ev.rhs()
+    assert np.abs(r_dg).max() <= 1e-13
+    ev.rk4_steps(0.05, 4)
+    u, _, p, _ = ev.get_state()
+    assert np.abs(p[:, 0] - 1.0).max() <= 1e-12 and np.abs(p[:, 1:4]).max() <= 1e-12
+
+
+def test_bad_arguments_are_rejected():
+    m = ng.Mesh.build(ng.MESH_CUBEDSPHERES7, n=5, luni=0, cs_dc=1.0, cs_r0fac=20.0)
+    with pytest.raises(ng.NmgError):
+        ng.GrhdEvolution(m)
+    m = ng.Mesh.build(ng.MESH_CUBEDSHELL6, n=5, ndiv=1, shell_rin=2.0, shell_rout=20.0)
+    with pytest.raises(ng.NmgError):
+        ng.GrhdEvolution(m, nf=40)
+    with pytest.raises(ng.NmgError):
+        ng.GrhdEvolution(m, gamma=1.0)
+    ev = ng.GrhdEvolution(m)
+    with pytest.raises(ng.NmgError):
+        ev.rk4_steps(-1.0, 1)

@@ -37,7 +37,7 @@ def _worker(rank, world, port, out):
 def test_max_over_ranks_with_gloo():
     import torch.multiprocessing as mp
     port = _free_port()
-    out = mp.Manager().dict()
+    out = mp.get_context("spawn").Manager().dict()
     mp.start_processes(_worker, args=(2, port, out), nprocs=2, join=True, start_method="spawn")
     assert dict(out) == {0: 15.0, 1: 15.0}
 
