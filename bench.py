@@ -269,12 +269,15 @@ def run_ours(args, rank, world, local):
     state_bytes = int(ev.size * 8)
     batched = None
     fvres = None
-    if rank == 0 and (not args.no_batched or not args.no_fv):
+    grhd = None
+    if rank == 0 and (not args.no_batched or not args.no_fv or not args.no_grhd):
         ev.close()  # free the workload's buffers for the sub-benchmarks
         if not args.no_batched:
             batched = batched_bench(args)
         if not args.no_fv:
             fvres = fv_bench(args)
+        if not args.no_grhd:
+            grhd = grhd_bench(args)
 
     fp64_peak = ng.fp64_peak_gflops()
     peaks = {}
@@ -332,6 +335,7 @@ def run_ours(args, rank, world, local):
             "adjoint": adjoint,
             "batched": batched,
             "fv": fvres,
+            "grhd": grhd,
         }
         print(json.dumps(out))
     ev.close()
@@ -495,6 +499,142 @@ def fv_bench(args):
     return out
 
 
+GRHD_K = 100.0       # polytropic constant of the initial data, p = K rho^2
+GRHD_RHO_ATM = 1e-10
+
+
+def grhd_initial_prim(xyz, seed, rho0=1e-3, center=(8.0, 0.0, 0.0), width=2.0):
+    """Primitives [E, 5, npts] of the GRHD workload at points xyz [E, 3,
+    npts]: a Gaussian density blob rho0 exp(-|x - c|^2 / width^2) with 1 %
+    seeded uniform perturbations on the atmosphere density, at rest, p = K
+    rho^2."""
+    rng = np.random.default_rng(seed)
+    c = np.asarray(center)[None, :, None]
+    r2 = ((xyz - c) ** 2).sum(1)
+    rho = GRHD_RHO_ATM + rho0 * np.exp(-r2 / width ** 2) * \
+        (1.0 + 0.01 * rng.uniform(-1.0, 1.0, r2.shape))
+    prim = np.zeros((xyz.shape[0], 5, xyz.shape[2]))
+    prim[:, 0] = rho
+    prim[:, 4] = GRHD_K * rho * rho
+    return prim
+
+
+def grhd_flops_per_stage(ndg, nfv, n, nf, c2p_iterations_per_stage):
+    """Model of the FP64 work of one GRHD stage (add, mul, FMA, division and
+    square root counted as one flop each, FMA as two), from the kernels'
+    source: per DG node 3 directional fluxes (45), Cowling sources (35),
+    45 derivatives of n terms plus the chain rule (90 n + 90), the RK4
+    update (20), and per face node of the element a two-sided LLF with its
+    speeds and the lift (170); per finite-volume point the sources (35),
+    per direction and midpoint two 5-field WENO5 reconstructions (600),
+    two prim2con (50), the LLF (95), the divergence (60 for all three
+    directions) and the update (20); con2prim 40 per point plus 30 per
+    root-finder iteration (counted on the device)."""
+    npd, npf = n ** 3, nf ** 3
+    dg = ndg * (npd * (45 + 35 + 90 * n + 90 + 20) + 6 * n * n * 170)
+    fv = nfv * npf * (35 + 3 * 745 + 60 + 20)
+    c2p = (ndg * npd + nfv * npf) * 40 + 30 * c2p_iterations_per_stage
+    return dg + fv + c2p
+
+
+def grhd_bench(args):
+    """GRHD in the Cowling approximation (isotropic Schwarzschild, M = 1,
+    Gamma = 2, atmosphere 1e-10): cubed shell r in [2, 20] of 6 x ndiv^3
+    elements at n = 7 LGL points (N = 6), a seeded ~10 % of the elements
+    switched to finite volume on nf = 13 equally spaced points (2N + 1),
+    Gaussian blob at r = 8, graph-captured RK4 steps; with the oracle's
+    restatement timed on a bounded sample."""
+    import torch
+    import nmesh_gb300 as ng
+    n, nf, nd, K = 7, 13, args.grhd_ndiv, args.grhd_steps
+    m = ng.Mesh.build(ng.MESH_CUBEDSHELL6, n=n, ndiv=nd, shell_rin=2.0, shell_rout=20.0)
+    E = m.nelem
+    prim = grhd_initial_prim(m.coords(), seed=33)
+    ev = ng.GrhdEvolution(m, mass=1.0, gamma=2.0, rho_atm=GRHD_RHO_ATM,
+                          p_atm=GRHD_K * GRHD_RHO_ATM ** 2, nf=nf)
+    ev.set_prim(prim)
+    flags = np.zeros(E, np.int32)
+    flags[np.random.default_rng(34).choice(E, int(round(0.1 * E)), replace=False)] = 1
+    ev.set_fv_elements(flags)
+    # dt = 0.25 min dx / N^2, min dx the smallest element edge (the arc of
+    # the angular edge on the inner sphere)
+    hmin = 2.0 * (PI / 2.0) / nd
+    dt = 0.25 * hmin / (n - 1) ** 2
+    ev.rk4_steps(dt, 2)  # graphs captured, warm-up
+    torch.cuda.synchronize()
+    ev.reset_stats()
+    stream = torch.cuda.ExternalStream(ev.stream)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    _, _, l0 = ev.stats()
+    e0.record(stream)
+    ev.rk4_steps(dt, K)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    iters, natm, l1 = ev.stats()
+    shares = ev.profile_step(dt)
+    tot = sum(shares.values())
+    ndg, nfv = E - ev.nfv, ev.nfv
+    dof = 5 * (ndg * n ** 3 + nfv * nf ** 3)
+    u_dg, u_fv, p_dg, _ = ev.get_state()
+    finite = bool(np.isfinite(u_dg).all() and np.isfinite(u_fv).all())
+    ev.close()
+    flops = grhd_flops_per_stage(ndg, nfv, n, nf, iters / (4.0 * K))
+    peak = ng.fp64_peak_gflops()
+    achieved = flops / (ms / 1e3 / (4 * K)) / 1e9
+    out = {"workload": f"GRHD Cowling, isotropic Schwarzschild M=1, Gamma=2, cubed shell "
+                       f"r in [2,20], 6x{nd}^3 elements, n={n} (N={n - 1}), {nfv} elements "
+                       f"({100.0 * nfv / E:.1f} %) finite volume on {nf}^3 points, WENOm5_2, "
+                       f"Gaussian blob rho0=1e-3 at r=8, atmosphere 1e-10, dt={dt:.4g}",
+           "elements": int(E), "fv_elements": int(nfv), "dof": int(dof), "steps": K,
+           "ms_per_step": ms / K, "value": dof * 4 * K / (ms / 1e3), "unit": UNIT,
+           "gpu_launches": int(l1 - l0), "finite": finite,
+           "con2prim_iterations_per_point": iters / (4.0 * K) / (ndg * n ** 3 + nfv * nf ** 3),
+           "atmosphere_points_per_stage": natm / (4.0 * K),
+           "kernel_ms_per_step": shares,
+           "con2prim_share": shares["con2prim"] / tot if tot > 0 else None,
+           "roofline_fp64": {"bound": "fp64", "achieved": achieved, "peak": peak,
+                             "unit": "GFLOP/s", "frac": achieved / peak,
+                             "flops_per_stage_model": flops,
+                             "peak_source": "FP64 FMA probe run live (nmg_fp64_peak)"}}
+    if not args.no_cpu_baseline:
+        out["cpu_baseline"] = grhd_cpu_baseline(args, n, nf)
+    return out
+
+
+def grhd_cpu_baseline(args, n, nf):
+    """The oracle's GRHD restatement (OpenMP over the host cores) on a
+    bounded sample: the same workload at ndiv = --grhd-cpu-ndiv, the same
+    10 % switch, two RK4 steps."""
+    from oracle import nmo
+    nd = args.grhd_cpu_ndiv
+    E = 6 * nd ** 3
+    flags = np.zeros(E, np.int32)
+    flags[np.random.default_rng(34).choice(E, int(round(0.1 * E)), replace=False)] = 1
+    o = nmo.GrhdOracle(n=n, nf=nf, ndiv=nd, fv=flags, mass=1.0, gamma=2.0, rho_atm=GRHD_RHO_ATM,
+                       p_atm=GRHD_K * GRHD_RHO_ATM ** 2)
+    pd = grhd_initial_prim(o.xyz, seed=33)
+    (_, _, npd), (_, _, npf) = o.shapes
+    ud = np.stack([o.prim2con(pd[e], o.psi(o.xyz[e])) for e in range(E)])
+    Pm, _ = o.transfer()
+    uf, pf = np.zeros((E, 5, npf)), np.zeros((E, 5, npf))
+    for e in np.nonzero(flags)[0]:
+        uf[e] = o.apply3(Pm, ud[e])
+        pf[e] = o.apply3(Pm, pd[e])
+    dt = 0.25 * (2.0 * (PI / 2.0) / nd) / (n - 1) ** 2
+    steps = 2
+    t0 = time.perf_counter()
+    o.rk4(ud, uf, pd, pf, dt, steps)
+    t = time.perf_counter() - t0
+    nfv = int(flags.sum())
+    dof = 5 * ((E - nfv) * npd + nfv * npf)
+    threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count()))
+    return {"value": dof * 4 * steps / t, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{steps} RK4 steps of the same workload at 6x{nd}^3 elements ({nfv} "
+                      f"finite volume, {dof} DOF), {t:.2f} s"}
+
+
 def cpu_mesh(n, luni, fv=False, fv_rec="WENOm5_2", fv_extrap="dnfn_extrap1"):
     """The oracle's own mesh of the workload (oracle/nmo_mesh.c: geometry
     restated from the reference, neighbour table by face matching); no
@@ -592,6 +732,10 @@ def main():
     ap.add_argument("--fv-steps", type=int, default=5)
     ap.add_argument("--fv-cpu-luni", type=int, default=2)
     ap.add_argument("--fv-cpu-steps", type=int, default=2)
+    ap.add_argument("--no-grhd", action="store_true")
+    ap.add_argument("--grhd-ndiv", type=int, default=12)
+    ap.add_argument("--grhd-steps", type=int, default=50)
+    ap.add_argument("--grhd-cpu-ndiv", type=int, default=6)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

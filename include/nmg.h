@@ -366,6 +366,11 @@ int nmg_grhd_rk4_steps(nmg_grhd_ctx *c, double dt, int32_t nsteps);
 int nmg_grhd_stats(nmg_grhd_ctx *c, int64_t *c2p_iterations, int64_t *atmosphere_points,
                    int64_t *launches);
 int nmg_grhd_reset_stats(nmg_grhd_ctx *c);
+/* one RK4 step, launched stage by stage with CUDA events around each kernel
+ * class: ms[0] con2prim, ms[1] DG / finite-volume traces, ms[2] DG
+ * elements, ms[3] finite-volume elements (milliseconds, summed over the
+ * four stages) */
+int nmg_grhd_profile_step(nmg_grhd_ctx *c, double dt, double *ms);
 void *nmg_grhd_stream(nmg_grhd_ctx *c);
 
 /* numerical flux of a context (default NMG_NUMFLUX_LLF, what the workloads

@@ -228,6 +228,7 @@ def lib(build_if_missing=True):
         "nmg_grhd_stats": (ctypes.c_int, [vp, vp, vp, vp]),
         "nmg_grhd_reset_stats": (ctypes.c_int, [vp]),
         "nmg_grhd_stream": (vp, [vp]),
+        "nmg_grhd_profile_step": (ctypes.c_int, [vp, f64, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -846,3 +847,10 @@ class GrhdEvolution:
 
     def reset_stats(self):
         self._check(lib().nmg_grhd_reset_stats(self._h), "nmg_grhd_reset_stats")
+
+    def profile_step(self, dt):
+        """One RK4 step timed per kernel class: dict of milliseconds."""
+        ms = np.zeros(4)
+        self._check(lib().nmg_grhd_profile_step(self._h, float(dt), _ptr(ms)),
+                    "nmg_grhd_profile_step")
+        return dict(zip(("con2prim", "traces", "dg", "fv"), ms.tolist()))

@@ -816,39 +816,57 @@ int grid_for(int64_t work) {
   return (int)std::max<int64_t>(1, std::min<int64_t>((work + kNT - 1) / kNT, 152 * 16));
 }
 
-// one stage: con2prim of the input (in place), traces, DG and FV kernels
-int enqueue_stage(nmg_grhd_ctx *c, GrP P, double *win_d, double *win_f) {
+// one stage: con2prim of the input (in place), traces, DG and FV kernels;
+// with ev (8 events), each kernel class is bracketed by a pair of events
+int enqueue_stage(nmg_grhd_ctx *c, GrP P, double *win_d, double *win_f,
+                  cudaEvent_t *ev = nullptr) {
   P.win_d = win_d;
   P.win_f = win_f;
   P.prim_d = c->d_pd;
   P.prim_f = c->d_pf;
+  auto mark = [&](int k) {
+    if (ev) cudaEventRecord(ev[k], c->stream);
+  };
   const int64_t work = (int64_t)c->ndg * c->np + (int64_t)c->nfv * c->npf;
+  mark(0);
   if (work > 0) {
     c2p_kernel<<<grid_for(work), kNT, 0, c->stream>>>(P, win_d, win_f, c->d_pd, c->d_pf,
                                                       c->d_stats);
     GCK(cudaGetLastError());
     c->launches++;
   }
+  mark(1);
+  mark(2);
   if (c->ntr > 0) {
     trace_kernel<<<grid_for((int64_t)c->ntr * c->tpts), kNT, 0, c->stream>>>(P, c->d_pd, c->d_pf);
     GCK(cudaGetLastError());
     c->launches++;
   }
+  mark(3);
+  mark(4);
   if (c->ndg > 0) {
     dg_kernel<<<c->ndg, kNT, c->smem_dg, c->stream>>>(P);
     GCK(cudaGetLastError());
     c->launches++;
   }
+  mark(5);
+  mark(6);
   if (c->nfv > 0) {
     fv_kernel<<<c->nfv, kNT, c->smem_fv, c->stream>>>(P);
     GCK(cudaGetLastError());
     c->launches++;
   }
+  mark(7);
   return NMG_OK;
 }
 
-// one RK4 step of the state in buffer cur (the result goes to 1 - cur)
-int enqueue_step(nmg_grhd_ctx *c, int cur, double dt) {
+// one RK4 step of the state in buffer cur (the result goes to 1 - cur);
+// with ms, the step runs stage by stage and ms[k] accumulates the time of
+// kernel class k (con2prim, traces, DG, finite volume)
+int enqueue_step(nmg_grhd_ctx *c, int cur, double dt, double *ms = nullptr) {
+  cudaEvent_t ev[8];
+  if (ms)
+    for (int k = 0; k < 8; k++) GCK(cudaEventCreate(&ev[k]));
   double *Ud = c->d_ud[cur], *Ad = c->d_ud[1 - cur], *WAd = c->d_ud[2], *WBd = c->d_ud[3];
   double *Uf = c->d_uf[cur], *Af = c->d_uf[1 - cur], *WAf = c->d_uf[2], *WBf = c->d_uf[3];
   const double cacc[4] = {dt / 6., dt / 3., dt / 3., dt / 6.};
@@ -863,9 +881,19 @@ int enqueue_step(nmg_grhd_ctx *c, int cur, double dt) {
     P.mode = s + 1;
     P.cacc = cacc[s];
     P.cw = cw[s];
-    int rc = enqueue_stage(c, P, wind[s], winf[s]);
+    int rc = enqueue_stage(c, P, wind[s], winf[s], ms ? ev : nullptr);
     if (rc) return rc;
+    if (ms) {
+      GCK(cudaEventSynchronize(ev[7]));
+      for (int k = 0; k < 4; k++) {
+        float t = 0.f;
+        GCK(cudaEventElapsedTime(&t, ev[2 * k], ev[2 * k + 1]));
+        ms[k] += t;
+      }
+    }
   }
+  if (ms)
+    for (int k = 0; k < 8; k++) cudaEventDestroy(ev[k]);
   return NMG_OK;
 }
 
@@ -1243,6 +1271,16 @@ int nmg_grhd_rk4_steps(nmg_grhd_ctx *c, double dt, int32_t nsteps) {
     c->launches += c->graph_launches;
     c->cur = 1 - c->cur;
   }
+  GCK(cudaStreamSynchronize(c->stream));
+  return NMG_OK;
+}
+
+int nmg_grhd_profile_step(nmg_grhd_ctx *c, double dt, double *ms) {
+  if (!c || !ms || !(dt > 0.)) return gset(c, NMG_EINVAL, "nmg_grhd_profile_step: bad argument");
+  for (int k = 0; k < 4; k++) ms[k] = 0.;
+  int rc = enqueue_step(c, c->cur, dt, ms);
+  if (rc) return rc;
+  c->cur = 1 - c->cur;
   GCK(cudaStreamSynchronize(c->stream));
   return NMG_OK;
 }
