@@ -250,7 +250,7 @@ def run_ours(args, rank, world, local):
         Wt = torch.from_numpy(np.where((r >= 17.0) & (r <= 19.0), 1.0, 0.0)).cuda()
         del r
         g = torch.empty_like(lam)
-        nsteps_adj, ckpt = 20, 5
+        nsteps_adj, ckpt = args.adj_steps, args.adj_ckpt
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         Jv = ev.adjoint_gradient_device(Wt.data_ptr(), g.data_ptr(), 0.0, dt, nsteps_adj, ckpt)
@@ -270,7 +270,9 @@ def run_ours(args, rank, world, local):
     batched = None
     fvres = None
     grhd = None
-    if rank == 0 and (not args.no_batched or not args.no_fv or not args.no_grhd):
+    config1 = None
+    if rank == 0 and (not args.no_batched or not args.no_fv or not args.no_grhd or
+                      not args.no_config1):
         ev.close()  # free the workload's buffers for the sub-benchmarks
         if not args.no_batched:
             batched = batched_bench(args)
@@ -278,8 +280,11 @@ def run_ours(args, rank, world, local):
             fvres = fv_bench(args)
         if not args.no_grhd:
             grhd = grhd_bench(args)
+        if not args.no_config1:
+            config1 = config1_bench(args)
 
     fp64_peak = ng.fp64_peak_gflops()
+    dmma_peak = ng.fp64_dmma_peak_gflops()
     peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fp:
@@ -289,6 +294,7 @@ def run_ours(args, rank, world, local):
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     per_launch_ms = ms / stages
     alg_bytes = alg_bytes_per_stage(mesh.nelem, ncurvi, n)
+    alg_bytes_stage1 = mesh.nelem * n ** 3 * NFIELDS * 3 * 8 + ncurvi * n ** 3 * 9 * 8
     variant = kinfo.split(" | ")[0]
     flops, fp64_ins = fp64_work_per_stage(variant, mesh.nelem, ncurvi, n)
     achieved_gbs = alg_bytes / (per_launch_ms / 1e3) / 1e9
@@ -319,6 +325,12 @@ def run_ours(args, rank, world, local):
             "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak,
                          "unit": "GB/s", "frac": achieved_gbs / hbm_peak,
                          "traffic": traffic,
+                         "traffic_launch": "stage 1 of the RK4 step (reads u, writes the "
+                                           "accumulator and w: 3 state streams + metric), "
+                                           "captured at level 3 and scaled x8; "
+                                           "alg_bytes_per_launch is the 4-stage average "
+                                           "(3, 5, 5, 3 state streams)",
+                         "alg_bytes_stage1": alg_bytes_stage1,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
                          "alg_bytes_per_launch": alg_bytes,
                          "kernel": kinfo.split(" | ")[0],
@@ -329,13 +341,15 @@ def run_ours(args, rank, world, local):
                               "flops_per_launch": flops,
                               "fp64_instructions_per_launch": fp64_ins,
                               "issue_frac": fp64_ins / (per_launch_ms / 1e3) / (fp64_peak * 1e9 / 2),
-                              "peak_source": "FP64 FMA probe run live (nmg_fp64_peak)"},
+                              "peak_source": "FP64 FMA probe run live (nmg_fp64_peak)",
+                              "dmma_probe_gflops": dmma_peak},
             "clocks": clk,
             "cpu_baseline": cpu,
             "adjoint": adjoint,
             "batched": batched,
             "fv": fvres,
             "grhd": grhd,
+            "config1": config1,
         }
         print(json.dumps(out))
     ev.close()
@@ -439,6 +453,87 @@ def batched_bench(args):
 PI = 3.141592653589793
 
 
+def fv_flops_per_stage(nelem, n):
+    """Model of the FP64 work of one finite-volume stage (the fast variant;
+    add, mul and division one flop, FMA two): per midpoint and direction 8
+    WENO5 reconstructions with one-division weights (60 each) and the LLF
+    flux with its normal (20); per point the flux differences, the
+    J sqrtgdiag factors and the RK4 update (70)."""
+    return nelem * (3 * (n - 1) * n * n * (8 * 60 + 20) + n ** 3 * 70)
+
+
+def config1_bench(args):
+    """The periodic-cube workload: [0, 2 pi]^3, 8^3 elements at n = 5 (N = 4),
+    plane wave psi = A sin(x + y + z) with a seeded amplitude, LLF, RK4 with
+    dt = 0.25 (2 pi / 8) / 16, 10 steps; the 10-step run repeated to time it
+    (2.56 MB per state: launch- and latency-bound), resident and through
+    host buffers, with the oracle on the same cores."""
+    import torch
+    import nmesh_gb300 as ng
+    n, L, K, reps = 5, 3, 10, args.c1_reps
+    m = ng.Mesh.build(ng.MESH_BOX, n=n, luni=L, xc=(PI, PI, PI), box_dout=PI, periodic=True)
+    A = np.random.default_rng(2024).uniform(0.5, 1.5)
+    xyz = m.coords()
+    arg = xyz.sum(axis=1)
+    om = np.sqrt(3.0)
+    u0 = A * np.stack([-om * np.cos(arg), np.cos(arg), np.cos(arg), np.cos(arg), np.sin(arg)], 1)
+    dt = 0.25 * (2 * PI / 8) / 16
+    ev = ng.Evolution(m, ng.BC_OUTGOING)
+    ev.set_state(u0)
+    ev.rk4_steps(0.0, dt, K)  # autotune, graphs, warm-up
+    stream = torch.cuda.ExternalStream(ev.stream)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    l0 = ev.launches
+    e0.record(stream)
+    for _ in range(reps):
+        ev.rk4_steps(0.0, dt, K)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / (reps * K)
+    launches = ev.launches - l0
+    dof = m.nelem * m.np * NFIELDS
+    host_u = torch.empty(ev.size, dtype=torch.float64, pin_memory=True).numpy()
+    host_u[:] = u0.ravel()
+    ev.rk4_steps_host(host_u, 0.0, dt, K, inplace=True)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        host_u[:] = u0.ravel()
+        ev.rk4_steps_host(host_u, 0.0, dt, K, inplace=True)
+    t_e2e = (time.perf_counter() - t0) / (reps * K)
+    kinfo = ev.kernel_info()
+    ev.close()
+    out = {"workload": "scalarwave1 RK4, periodic box [0,2pi]^3, 8^3 elements, n=5 (N=4), "
+                       "plane wave psi = A sin(x+y+z), LLF, dt = 0.25 (2pi/8)/16, 10 steps",
+           "elements": int(m.nelem), "dof": int(dof), "steps": K, "repeats": reps,
+           "ms_per_step": ms, "value": dof * 4 / (ms / 1e3), "unit": UNIT,
+           "e2e": {"value": dof * 4 / t_e2e, "unit": UNIT,
+                   "h2d_bytes_per_step": dof * 8 / K, "d2h_bytes_per_step": dof * 8 / K,
+                   "note": "one host round trip per 10-step run"},
+           "kernel": kinfo.split(" | ")[0], "gpu_launches": int(launches)}
+    if not args.no_cpu_baseline:
+        from oracle import nmo
+        pat, bbox, curvi, oxyz, dXdx = nmo.generate_mesh(nmo.MESH_BOX, n, L, xc=(PI, PI, PI),
+                                                         box_dout=PI)
+        nb = nmo.match_faces_conforming(oxyz, n, period=2 * PI)
+        o = nmo.OracleMesh(bbox, curvi, dXdx, oxyz, nb, n, bc=1)
+        a = oxyz.sum(axis=1)
+        cu = A * np.stack([-om * np.cos(a), np.cos(a), np.cos(a), np.cos(a), np.sin(a)], 1)
+        o.rk4(cu, dt, K)
+        creps = 5
+        t0 = time.perf_counter()
+        for _ in range(creps):
+            o.rk4(cu, dt, K)
+        t = (time.perf_counter() - t0) / (creps * K)
+        threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count()))
+        out["cpu_baseline"] = {"value": dof * 4 / t, "unit": UNIT, "cores": threads,
+                               "kind": "port",
+                               "sample": f"{creps} runs of the 10-step workload, "
+                                         f"{1e3 * t:.2f} ms per step"}
+    return out
+
+
 def fv_bench(args):
     """All-finite-volume workload: the 7-patch cubed-sphere mesh with every
     element a finite-volume element on n^3 equally spaced points, WENOm5_2
@@ -480,6 +575,16 @@ def fv_bench(args):
            "value": dof * 4 * K / (ms / 1e3), "unit": UNIT,
            "kernel": kinfo.split(" | ")[0], "autotune": kinfo.split(" | timings: ")[-1],
            "gpu_launches": int(launches)}
+    flops = fv_flops_per_stage(mesh.nelem, n)
+    peak = ng.fp64_peak_gflops()
+    achieved = flops / (ms / 1e3 / (4 * K)) / 1e9
+    out["roofline_fp64"] = {"bound": "fp64", "achieved": achieved, "peak": peak,
+                            "unit": "GFLOP/s", "frac": achieved / peak,
+                            "flops_per_launch_model": flops,
+                            "peak_source": "FP64 FMA probe run live (nmg_fp64_peak)",
+                            "note": "divisions count one flop here but issue several FP64 "
+                                    "instructions; the FP64 pipe utilization from ncu is in "
+                                    "profiles/fv_fast_kernel_n13_cubedspheres_l2_rhs.md"}
     if not args.no_cpu_baseline:
         cl = args.fv_cpu_luni
         cxyz, om = cpu_mesh(n, cl, fv=True, fv_rec=rec, fv_extrap=ex)
@@ -732,7 +837,11 @@ def main():
     ap.add_argument("--fv-steps", type=int, default=5)
     ap.add_argument("--fv-cpu-luni", type=int, default=2)
     ap.add_argument("--fv-cpu-steps", type=int, default=2)
+    ap.add_argument("--adj-steps", type=int, default=200)
+    ap.add_argument("--adj-ckpt", type=int, default=20)
     ap.add_argument("--no-grhd", action="store_true")
+    ap.add_argument("--no-config1", action="store_true")
+    ap.add_argument("--c1-reps", type=int, default=20)
     ap.add_argument("--grhd-ndiv", type=int, default=12)
     ap.add_argument("--grhd-steps", type=int, default=50)
     ap.add_argument("--grhd-cpu-ndiv", type=int, default=6)

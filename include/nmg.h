@@ -528,6 +528,10 @@ void *nmg_stream(nmg_ctx *c);
 /* measured FP64 FMA throughput of the current device in GFLOP/s (the roof
    of this FP64 path on GB300); runs a ~10 ms probe kernel */
 int nmg_fp64_peak(double *gflops);
+/* measured FP64 tensor-core throughput (mma.sync m8n8k4 f64, DMMA) of the
+   current device in GFLOP/s: the other FP64 roof, reported beside the FMA
+   one (on GB300 both share one FP64 rate) */
+int nmg_fp64_dmma_peak(double *gflops);
 
 #ifdef __cplusplus
 }

@@ -164,6 +164,7 @@ def lib(build_if_missing=True):
         "nmg_kernel_launches": (i64, [vp]),
         "nmg_stream": (vp, [vp]),
         "nmg_fp64_peak": (ctypes.c_int, [vp]),
+        "nmg_fp64_dmma_peak": (ctypes.c_int, [vp]),
         "nmg_set_kernel": (ctypes.c_int, [vp, ctypes.c_char_p]),
         "nmg_rk4_step_noalloc": (ctypes.c_int, [vp, f64, f64, vp, vp]),
         "nmg_mesh_concat": (ctypes.c_int, [vp, i32, vp]),
@@ -247,6 +248,14 @@ def fp64_peak_gflops():
     v = ctypes.c_double(0.0)
     if lib().nmg_fp64_peak(ctypes.byref(v)):
         raise NmgError("nmg_fp64_peak failed")
+    return v.value
+
+
+def fp64_dmma_peak_gflops():
+    """Measured FP64 tensor-core (DMMA) throughput of the current GPU (GFLOP/s)."""
+    v = ctypes.c_double(0.0)
+    if lib().nmg_fp64_dmma_peak(ctypes.byref(v)):
+        raise NmgError("nmg_fp64_dmma_peak failed")
     return v.value
 
 

@@ -53,6 +53,28 @@ __global__ void __launch_bounds__(256) fp64_peak_kernel(double *out, int iters, 
   out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
+// FP64 tensor-core (DMMA, mma.sync m8n8k4 f64) throughput probe: 4
+// independent accumulator chains per warp; one mma is 8 x 8 x 4 FMA
+__global__ void __launch_bounds__(256) dmma_peak_kernel(double *out, int iters, double a,
+                                                        double b) {
+  const double av = a + threadIdx.x * 1e-9, bv = b;
+  double c[4][2];
+#pragma unroll
+  for (int k = 0; k < 4; k++) c[k][0] = c[k][1] = k * 1e-3;
+  for (int it = 0; it < iters; it++) {
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+      asm volatile(
+          "mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0, %1}, {%2}, {%3}, {%0, %1};"
+          : "+d"(c[k][0]), "+d"(c[k][1])
+          : "d"(av), "d"(bv));
+  }
+  double s = 0;
+#pragma unroll
+  for (int k = 0; k < 4; k++) s += c[k][0] + c[k][1];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
 constexpr int kMaxVariants = 16;
 
 // Objective J = dt sum_nodes W phi^2 of one state, in two deterministic
@@ -2447,6 +2469,38 @@ int nmg_adjoint_gradient(nmg_ctx *c, double t0, double dt, int32_t nsteps, int32
   if ((e = cudaGetLastError()) != cudaSuccess) return fail(e, "nmg_adjoint_gradient launch");
   *J = Jh;
   cleanup();
+  return NMG_OK;
+}
+
+int nmg_fp64_dmma_peak(double *gflops) {
+  nmg_ctx *c = nullptr;  // for CK: errors are returned without a context
+  if (!gflops) return NMG_EINVAL;
+  int dev = 0, sms = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int blocks = sms * 4, threads = 256, iters = 256;
+  double *out = nullptr;
+  CK(cudaMalloc((void **)&out, sizeof(double) * blocks * threads));
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  dmma_peak_kernel<<<blocks, threads>>>(out, 32, 1.0, 1e-9);
+  CK(cudaGetLastError());
+  float best = 1e30f;
+  for (int r = 0; r < 5; r++) {
+    CK(cudaEventRecord(e0));
+    dmma_peak_kernel<<<blocks, threads>>>(out, iters, 1.0, 1e-9);
+    CK(cudaEventRecord(e1));
+    CK(cudaEventSynchronize(e1));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    best = std::min(best, ms);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  // per warp and iteration: 4 mma of 8 x 8 x 4 FMA (2 flops each)
+  *gflops = 2.0 * 256 * 4 * iters * (double)blocks * (threads / 32) / (best * 1e6);
   return NMG_OK;
 }
 

@@ -125,3 +125,36 @@ def test_gradient_matches_central_differences(kind, nsteps, ckpt):
         fd = (_oracle_J(o, u0 + eps * v, W, dt, nsteps) -
               _oracle_J(o, u0 - eps * v, W, dt, nsteps)) / (2 * eps)
         assert _rel(np.vdot(grad, v), fd) < 1e-6
+
+
+def test_gradient_of_the_outer_shell_objective_16_directions():
+    """The adjoint workload on a reduced mesh: 7 CubedSpheres at n = 9,
+    level 1 (56 elements), J = sum_s dt sum W phi^2 over the shell
+    17 <= r <= 19 (the outer shell r = 18), 50 RK4 steps with checkpoints
+    every 10, against central differences (eps = 1e-6) of the oracle's
+    forward run along 16 seeded directions in the initial psi and pi."""
+    import torch
+    m = _mesh("cs7", 9, 1)
+    ev = ng.Evolution(m, ng.BC_OUTGOING)
+    u0 = gaussian_pulses(m.coords(), seed=11, rmin=15.0, rmax=18.0)
+    W = _shell_weight(m, 17.0, 19.0)
+    dt = 0.25 * (2.0 / 2 ** 1) / 8 ** 2
+    nsteps, ckpt = 50, 10
+    ev.set_state(u0)
+    Wd = _dev(W)
+    g = torch.zeros(ev.size, dtype=torch.float64, device="cuda")
+    J = ev.adjoint_gradient_device(Wd.data_ptr(), g.data_ptr(), 0.0, dt, nsteps, ckpt)
+    grad = g.cpu().numpy().reshape(ev.shape)
+    o = oracle_for(m, bc=1)
+    assert J > 0 and _rel(J, _oracle_J(o, u0, W, dt, nsteps)) < 1e-12
+    rng = np.random.default_rng(2016)
+    eps = 1e-6
+    worst = 0.0
+    for _ in range(16):
+        v = rng.standard_normal(ev.shape)
+        v[:, 1:4] = 0.0
+        fd = (_oracle_J(o, u0 + eps * v, W, dt, nsteps) -
+              _oracle_J(o, u0 - eps * v, W, dt, nsteps)) / (2 * eps)
+        worst = max(worst, _rel(np.vdot(grad, v), fd))
+    print(f"\nworst relative gradient / central-difference mismatch over 16 directions: {worst:.2e}")
+    assert worst < 1e-6
