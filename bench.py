@@ -377,26 +377,14 @@ def batch_problem_specs(count, seed=4242):
     return specs
 
 
-def batched_bench(args):
-    """Batched persistent execution of many independent problems (one launch
-    per RK4 stage for all of them, graph-captured) against the same problems
-    stepped one after the other through their own contexts (4 launches per
-    problem and step)."""
+def _batch_compare(meshes, states, K):
+    """Times of K RK4 steps of the problems: batched (one launch per stage
+    for all orders, or one per order, graph-captured), plain (each problem
+    its own context, 4 launches per problem and step) and per-problem
+    graphs (each problem's step captured)."""
     import torch
     import nmesh_gb300 as ng
-    specs = batch_problem_specs(args.batch_problems)
-    meshes = []
-    for kind, L, n, E, href in specs:
-        if kind == "box":
-            meshes.append(ng.Mesh.build(ng.MESH_BOX, n=n, luni=L, xc=(PI, PI, PI),
-                                        box_dout=PI, periodic=True))
-        else:
-            meshes.append(ng.Mesh.build(ng.MESH_CUBEDSPHERES7, n=n, luni=L, cs_dc=1.0,
-                                        cs_r0fac=20.0, hrefine=href))
-    rng = np.random.default_rng(7)
-    states = [1e-3 * rng.standard_normal((m.nelem, NFIELDS, m.np)) for m in meshes]
-    dof = sum(m.nelem * m.np * NFIELDS for m in meshes)
-    dt, K = 1e-4, args.batch_steps
+    dt = 1e-4
     b = ng.Batch(meshes, ng.BC_OUTGOING)
     for p, u in enumerate(states):
         b.set_state(p, u)
@@ -431,23 +419,50 @@ def batched_bench(args):
     t_graphs = time.perf_counter() - t0
     for ev in evs:
         ev.close()
-    nelem = [m.nelem for m in meshes]
-    return {"problems": len(meshes), "elements": int(sum(nelem)), "dof": int(dof),
-            "orders_n": sorted(set(int(m.n) for m in meshes)),
-            "element_counts_min_max": [int(min(nelem)), int(max(nelem))],
-            "steps": K,
+    dof = sum(m.nelem * m.np * NFIELDS for m in meshes)
+    return {"problems": len(meshes), "elements": int(sum(m.nelem for m in meshes)),
+            "dof": int(dof), "steps": K,
             "batched_dof_stage_per_s": dof * 4 * K / t_batch,
             "plain_dof_stage_per_s": dof * 4 * K / t_plain,
             "per_problem_graphs_dof_stage_per_s": dof * 4 * K / t_graphs,
             "speedup_vs_plain_launches": t_plain / t_batch,
             "speedup_vs_per_problem_graphs": t_graphs / t_batch,
-            "batch_info": info,
-            "refinement_levels": sorted(set(int(L) + d for _, L, _, _, h in specs
-                                            for d in ((0, 1) if h else (0,)))),
-            "problems_with_level_jumps": int(sum(1 for s_ in specs if s_[4])),
-            "note": "orders are per problem; problems with level jumps have patches one "
-                    "level finer than their neighbours (non-conforming faces, traces "
-                    "interpolated each stage); all problems share dt"}
+            "batch_info": info}
+
+
+def batched_bench(args):
+    """Batched execution of many independent problems against the same
+    problems stepped one after the other through their own contexts; for
+    all 64 problems, and for the ones of at most 4096 elements, where the
+    per-problem launches rather than the arithmetic set the time."""
+    import nmesh_gb300 as ng
+    specs = batch_problem_specs(args.batch_problems)
+    meshes = []
+    for kind, L, n, E, href in specs:
+        if kind == "box":
+            meshes.append(ng.Mesh.build(ng.MESH_BOX, n=n, luni=L, xc=(PI, PI, PI),
+                                        box_dout=PI, periodic=True))
+        else:
+            meshes.append(ng.Mesh.build(ng.MESH_CUBEDSPHERES7, n=n, luni=L, cs_dc=1.0,
+                                        cs_r0fac=20.0, hrefine=href))
+    rng = np.random.default_rng(7)
+    states = [1e-3 * rng.standard_normal((m.nelem, NFIELDS, m.np)) for m in meshes]
+    out = _batch_compare(meshes, states, args.batch_steps)
+    small = [p for p, m in enumerate(meshes) if m.nelem <= 4096]
+    sub = _batch_compare([meshes[p] for p in small], [states[p] for p in small],
+                         args.batch_small_steps)
+    nelem = [m.nelem for m in meshes]
+    out.update({
+        "orders_n": sorted(set(int(m.n) for m in meshes)),
+        "element_counts_min_max": [int(min(nelem)), int(max(nelem))],
+        "refinement_levels": sorted(set(int(L) + d for _, L, _, _, h in specs
+                                        for d in ((0, 1) if h else (0,)))),
+        "problems_with_level_jumps": int(sum(1 for s_ in specs if s_[4])),
+        "note": "orders are per problem; problems with level jumps have patches one "
+                "level finer than their neighbours (non-conforming faces, traces "
+                "interpolated each stage); all problems share dt",
+        "small_problems": dict(sub, selection="the problems of at most 4096 elements")})
+    return out
 
 
 PI = 3.141592653589793
@@ -831,6 +846,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batch-problems", type=int, default=64)
     ap.add_argument("--batch-steps", type=int, default=5)
+    ap.add_argument("--batch-small-steps", type=int, default=50)
     ap.add_argument("--no-fv", action="store_true")
     ap.add_argument("--fv-n", type=int, default=13)
     ap.add_argument("--fv-luni", type=int, default=3)
