@@ -98,6 +98,12 @@ typedef struct nmg_mesh_params {
   int32_t ndiv;          /* > 0: every patch split into ndiv^3 equal elements
                             (instead of 2^luni per direction); 0: luni */
   double shell_rin, shell_rout; /* NMG_MESH_CUBEDSHELL6: inner and outer radius */
+  int32_t patch_mask;    /* bit p set: build only the elements of patch p
+                            (0: every patch); faces towards the patches left
+                            out are outer faces of this mesh.  Parts of one
+                            mesh with different n are joined again by
+                            nmg_batch_create_linked (p-refinement by patch,
+                            the reference's amr_prefine_p) */
 } nmg_mesh_params;
 
 /* A mesh given element by element, e.g. packed from the reference's tMesh
@@ -453,6 +459,18 @@ typedef struct nmg_batch nmg_batch;
 int nmg_mesh_concat(const nmg_mesh *const *meshes, int32_t count, nmg_mesh **out);
 int nmg_batch_create(const nmg_mesh *const *meshes, int32_t count, int32_t bc_kind,
                      const double k[3], nmg_batch **out);
+/* The same, with meshes that are parts of one problem: meshes with equal
+ * problem[i] are joined across their coinciding outer faces (all four
+ * corners coincide; the parts may have different n, each face between them
+ * is then p-nonconforming).  A face node's exterior state is the
+ * neighbour part's face plane interpolated at the node's position (Lagrange
+ * in both in-plane directions), as set_ajsurf_vl's interpolation branch
+ * does (src/main/amr/surface.c:900-1460), filled by one launch per stage for
+ * every such face of the batch.  States stay per part (mesh index). */
+int nmg_batch_create_linked(const nmg_mesh *const *meshes, int32_t count, const int32_t *problem,
+                            int32_t bc_kind, const double k[3], nmg_batch **out);
+/* number of faces joined across parts (each side counted) */
+int64_t nmg_batch_linked_faces(const nmg_batch *b);
 void nmg_batch_destroy(nmg_batch *b);
 const char *nmg_batch_last_error(const nmg_batch *b);
 int64_t nmg_batch_problem_size(const nmg_batch *b, int32_t p); /* doubles of problem p */

@@ -45,7 +45,7 @@ class _MeshParams(ctypes.Structure):
                 ("fv", ctypes.c_int32), ("hrefine", ctypes.c_int32),
                 ("sphere_levels", ctypes.c_int32), ("sphere_radius", ctypes.c_double),
                 ("ndiv", ctypes.c_int32), ("shell_rin", ctypes.c_double),
-                ("shell_rout", ctypes.c_double)]
+                ("shell_rout", ctypes.c_double), ("patch_mask", ctypes.c_int32)]
 
 
 class TroubleParams(ctypes.Structure):
@@ -169,6 +169,8 @@ def lib(build_if_missing=True):
         "nmg_rk4_step_noalloc": (ctypes.c_int, [vp, f64, f64, vp, vp]),
         "nmg_mesh_concat": (ctypes.c_int, [vp, i32, vp]),
         "nmg_batch_create": (ctypes.c_int, [vp, i32, i32, vp, vp]),
+        "nmg_batch_create_linked": (ctypes.c_int, [vp, i32, vp, i32, vp, vp]),
+        "nmg_batch_linked_faces": (i64, [vp]),
         "nmg_batch_destroy": (None, [vp]),
         "nmg_batch_last_error": (ctypes.c_char_p, [vp]),
         "nmg_batch_problem_size": (i64, [vp, i32]),
@@ -280,7 +282,7 @@ class Mesh:
     def build(cls, mesh_type=MESH_BOX, n=5, luni=0, xc=(0.0, 0.0, 0.0),
               box_dout=1.0, cs_dc=1.0, cs_r0fac=20.0, periodic=False, fv=False,
               hrefine=(), sphere_levels=0, sphere_radius=10.0, ndiv=0, shell_rin=2.0,
-              shell_rout=20.0):
+              shell_rout=20.0, patches=None):
         """Mesh from the reference's parameters: amr_mesh_type (1 BoxMesh /
         7 CubedSpheres), amr_n0..2 = n, amr_luni, amr_mesh_xc,
         amr_BoxMesh_dout, amr_CubedSphere_dc, amr_CubedSphere_r0fac;
@@ -291,7 +293,11 @@ class Mesh:
         whose centre lies within radius 2^(levels-1-i) of x = 0 are refined
         in pass i).  MESH_CUBEDSHELL6: six cubed-sphere patches between the
         spheres of radius shell_rin and shell_rout; ndiv > 0 splits every
-        patch into ndiv^3 equal elements instead of 2^luni per direction."""
+        patch into ndiv^3 equal elements instead of 2^luni per direction.
+        patches: build only these patches (a part of the mesh)."""
+        pmask = 0
+        for p_ in (patches or ()):
+            pmask |= 1 << int(p_)
         hmask = 0
         for p_ in hrefine:
             hmask |= 1 << int(p_)
@@ -307,7 +313,7 @@ class Mesh:
                         (ctypes.c_double * 3)(*xc), float(box_dout),
                         float(cs_dc), float(cs_r0fac), int(mask), hmask,
                         int(sphere_levels), float(sphere_radius), int(ndiv), float(shell_rin),
-                        float(shell_rout))
+                        float(shell_rout), pmask)
         h = ctypes.c_void_p()
         rc = lib().nmg_mesh_build(ctypes.byref(p), ctypes.byref(h))
         if rc:
@@ -694,12 +700,19 @@ class Evolution:
 class Batch:
     """Many independent problems stepped together (nmg_batch_*)."""
 
-    def __init__(self, meshes, bc=BC_OUTGOING, k=(1.0, 1.0, 1.0)):
+    def __init__(self, meshes, bc=BC_OUTGOING, k=(1.0, 1.0, 1.0), problems=None):
+        """problems: per mesh a problem id; meshes of one problem are parts
+        joined across their coinciding outer faces (their n may differ)."""
         self.meshes = list(meshes)
         arr = (ctypes.c_void_p * len(self.meshes))(*[m._h.value for m in self.meshes])
         kk = np.ascontiguousarray(k, np.float64)
         h = ctypes.c_void_p()
-        rc = lib().nmg_batch_create(arr, len(self.meshes), int(bc), _ptr(kk), ctypes.byref(h))
+        if problems is None:
+            rc = lib().nmg_batch_create(arr, len(self.meshes), int(bc), _ptr(kk), ctypes.byref(h))
+        else:
+            pr = np.ascontiguousarray(problems, np.int32)
+            rc = lib().nmg_batch_create_linked(arr, len(self.meshes), _ptr(pr), int(bc), _ptr(kk),
+                                               ctypes.byref(h))
         self._h = h
         if rc:
             msg = lib().nmg_batch_last_error(h).decode() if h.value else ""
@@ -727,6 +740,10 @@ class Batch:
     def rk4_steps(self, t, dt, nsteps):
         self._check(lib().nmg_rk4_steps_batched(self._h, float(t), float(dt), int(nsteps)),
                     "nmg_rk4_steps_batched")
+
+    @property
+    def linked_faces(self):
+        return int(lib().nmg_batch_linked_faces(self._h))
 
     def set_mode(self, mode):
         """0 autotune, 1 persistent single launch, 2 one launch per order."""

@@ -933,14 +933,20 @@ int nmg_mesh_build(const nmg_mesh_params *p, nmg_mesh **out) {
     }
     m->ndiv = p->ndiv;
     std::vector<Leaf> leaves;
+    auto wanted = [&](size_t q) { return p->patch_mask == 0 || ((p->patch_mask >> q) & 1); };
     if (p->ndiv > 0) {
       for (size_t q = 0; q < pats.size(); q++)
-        for (int k = 0; k < p->ndiv; k++)
-          for (int j = 0; j < p->ndiv; j++)
-            for (int i = 0; i < p->ndiv; i++) leaves.push_back(Leaf{(int)q, 0, {i, j, k}});
+        if (wanted(q))
+          for (int k = 0; k < p->ndiv; k++)
+            for (int j = 0; j < p->ndiv; j++)
+              for (int i = 0; i < p->ndiv; i++) leaves.push_back(Leaf{(int)q, 0, {i, j, k}});
     } else {
       for (size_t q = 0; q < pats.size(); q++)
-        uniform_leaves((int)q, p->luni + (((p->hrefine >> q) & 1) ? 1 : 0), leaves);
+        if (wanted(q)) uniform_leaves((int)q, p->luni + (((p->hrefine >> q) & 1) ? 1 : 0), leaves);
+    }
+    if (leaves.empty()) {
+      delete m;
+      return fail(NMG_EINVAL, "nmg_mesh_build: patch_mask selects no patch");
     }
     if (p->sphere_levels > 0) refine_spheres(pats, p->sphere_levels, p->sphere_radius, leaves);
     fill_geometry(*m, pats, leaves, p->fv);

@@ -23,6 +23,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/nmg.h"
@@ -73,6 +74,56 @@ __global__ void __launch_bounds__(256) dmma_peak_kernel(double *out, int iters, 
 #pragma unroll
   for (int k = 0; k < 4; k++) s += c[k][0] + c[k][1];
   out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+// Traces of faces joined across the parts of a batched problem: per link
+// (target group, ghost slot, source group, element, face, orientation),
+// field (pi, c) and target face node, the source face plane interpolated at
+// the node's position, sum_b l_b(t) sum_a l_a(s) W[a, b] with the source's
+// LGL Lagrange basis in barycentric form (weights btab).
+__global__ void plink_kernel(const int *links, int nlink, const int *gn, double *const *ghost,
+                             const double *const *wsrc, const double *xtab, const double *btab) {
+  constexpr int M = nmgk::kBatchMaxN;
+  const int64_t tot = (int64_t)nlink * 4 * M * M;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < tot;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int l = (int)(i / (4 * M * M)), rem = (int)(i % (4 * M * M));
+    const int fld = rem / (M * M), ab = rem % (M * M);
+    const int *L = links + 6 * l;
+    const int tg = L[0], ts = L[1], sg = L[2], se = L[3], sf = L[4], o = L[5];
+    const int nt = gn[tg], ns = gn[sg];
+    const int a = ab % M, b = ab / M;
+    if (a >= nt || b >= nt) continue;
+    const double *xt = xtab + nt * M, *xs = xtab + ns * M, *bs = btab + ns * M;
+    double u = (o & 1) ? xt[b] : xt[a], v = (o & 1) ? xt[a] : xt[b];
+    if (o & 2) u = -u;
+    if (o & 4) v = -v;
+    double la[M], lb[M];
+    for (int k = 0; k < ns; k++) {
+      double pa = bs[k], pb = bs[k];
+      for (int j = 0; j < ns; j++)
+        if (j != k) {
+          pa *= u - xs[j];
+          pb *= v - xs[j];
+        }
+      la[k] = pa;
+      lb[k] = pb;
+    }
+    const int nps = ns * ns * ns;
+    const double *W = wsrc[sg] + ((size_t)se * NF + fld) * nps;
+    const int d = sf >> 1, pq = (sf & 1) * (ns - 1);
+    double val = 0.;
+    for (int kb = 0; kb < ns; kb++) {
+      double row = 0.;
+      for (int ka = 0; ka < ns; ka++) {
+        const int node = d == 0 ? pq + ns * (ka + ns * kb)
+                                : (d == 1 ? ka + ns * (pq + ns * kb) : ka + ns * (kb + ns * pq));
+        row = fma(la[ka], W[node], row);
+      }
+      val = fma(lb[kb], row, val);
+    }
+    ghost[tg][((size_t)ts * 4 + fld) * nt * nt + a + nt * b] = val;
+  }
 }
 
 constexpr int kMaxVariants = 16;
@@ -2565,6 +2616,15 @@ struct nmg_batch {
   double graph_dt = 0;
   int cur = 0;
   int64_t launches = 0;
+  // faces joined across the parts of one problem (p-nonconforming when the
+  // parts' n differ): per face the target group and ghost slot, the source
+  // group, element, face and orientation (nmg_batch_create_linked)
+  int nlink = 0;
+  int *d_links = nullptr;          // [nlink][6]
+  double **d_ghostp = nullptr;     // [G] ghost arrays of the groups
+  const double **d_wsrc = nullptr; // [2 parities][4 stages][G] stage inputs
+  double *d_xtab = nullptr;        // [kBatchMaxN + 1][kBatchMaxN]: LGL points per n
+  double *d_btab = nullptr;        // ... and their barycentric weights
 };
 
 static int batch_err(nmg_batch *b, int code, const std::string &msg) {
@@ -2624,6 +2684,11 @@ static int batch_upload_params(nmg_batch *b, double dt) {
   BK(cudaMemcpy(b->d_params, ps.data(), ps.size() * sizeof(StageParams),
                 cudaMemcpyHostToDevice));
   b->hparams = ps;
+  if (b->nlink > 0) {
+    std::vector<const double *> ws(8 * G);
+    for (int q = 0; q < 8 * G; q++) ws[q] = ps[q].win;
+    BK(cudaMemcpy(b->d_wsrc, ws.data(), sizeof(double *) * 8 * G, cudaMemcpyHostToDevice));
+  }
   return NMG_OK;
 }
 
@@ -2634,6 +2699,15 @@ static int batch_enqueue_stage(nmg_batch *b, int par, int s) {
     if (c->nhang <= 0) continue;
     BK(nmgk::hang_launch(c->nhang, c->n, c->d_hoff, c->d_hsrc, c->d_hw,
                          b->hparams[(par * 4 + s) * G + g].win, c->d_ghost, b->stream));
+    b->launches++;
+  }
+  if (b->nlink > 0) {  // faces joined across parts
+    const int64_t work = (int64_t)b->nlink * 4 * nmgk::kBatchMaxN * nmgk::kBatchMaxN;
+    const int grid = (int)std::min<int64_t>((work + 255) / 256, 152 * 8);
+    plink_kernel<<<grid, 256, 0, b->stream>>>(b->d_links, b->nlink, b->d_gn, b->d_ghostp,
+                                              b->d_wsrc + (par * 4 + s) * G, b->d_xtab,
+                                              b->d_btab);
+    BK(cudaGetLastError());
     b->launches++;
   }
   if (b->grouped) {
@@ -2725,8 +2799,11 @@ static int batch_autotune(nmg_batch *b, double dt) {
 
 extern "C" {
 
-int nmg_batch_create(const nmg_mesh *const *meshes, int32_t count, int32_t bc_kind,
-                     const double k[3], nmg_batch **out) {
+static int batch_link_parts(nmg_batch *b, const nmg_mesh *const *meshes, int count,
+                            const int32_t *problem);
+
+static int batch_create_impl(const nmg_mesh *const *meshes, int32_t count, const int32_t *problem,
+                             int32_t bc_kind, const double k[3], nmg_batch **out) {
   if (!out) return NMG_EINVAL;
   *out = nullptr;
   nmg_batch *b = new (std::nothrow) nmg_batch;
@@ -2786,12 +2863,168 @@ int nmg_batch_create(const nmg_mesh *const *meshes, int32_t count, int32_t bc_ki
   BK(cudaMalloc((void **)&b->d_step, sizeof(int)));
   BK(cudaMalloc((void **)&b->d_times, sizeof(double)));
   b->times_cap = 1;
+  if (problem) return batch_link_parts(b, meshes, count, problem);
   return NMG_OK;
 }
+
+int nmg_batch_create(const nmg_mesh *const *meshes, int32_t count, int32_t bc_kind,
+                     const double k[3], nmg_batch **out) {
+  return batch_create_impl(meshes, count, nullptr, bc_kind, k, out);
+}
+
+int nmg_batch_create_linked(const nmg_mesh *const *meshes, int32_t count, const int32_t *problem,
+                            int32_t bc_kind, const double k[3], nmg_batch **out) {
+  if (!problem) return NMG_EINVAL;
+  return batch_create_impl(meshes, count, problem, bc_kind, k, out);
+}
+
+int64_t nmg_batch_linked_faces(const nmg_batch *b) { return b ? b->nlink : -1; }
+
+}  // extern "C"
+
+// Join the parts of each problem across their coinciding outer faces: each
+// such face of part i becomes a face of its group's context whose exterior
+// state is read from a ghost slot (the mixed-face path of the stage
+// kernels), filled every stage by plink_kernel from part j's stage input.
+static int batch_link_parts(nmg_batch *b, const nmg_mesh *const *meshes, int count,
+                            const int32_t *problem) {
+  struct OFace {
+    int part;
+    int64_t e;
+    int f;
+    double c[4][3];
+  };
+  auto corner = [&](const nmg_mesh *m, int64_t e, int f, int ca, int cb, double x[3]) {
+    const int n = m->n, np = n * n * n;
+    const int node = nmg::face_node(n, f, ca * (n - 1), cb * (n - 1));
+    for (int d = 0; d < 3; d++) x[d] = m->xyz[((size_t)e * 3 + d) * np + node];
+  };
+  const double h = 1e-6, tol = 1e-9;
+  auto key = [&](const double c[3]) {
+    return std::to_string(std::llround(c[0] / h)) + "," + std::to_string(std::llround(c[1] / h)) +
+           "," + std::to_string(std::llround(c[2] / h));
+  };
+  // outer faces of every part, hashed by their corner centroid
+  std::vector<OFace> faces;
+  std::unordered_map<std::string, std::vector<size_t>> where;
+  for (int i = 0; i < count; i++) {
+    const nmg_mesh *m = meshes[i];
+    for (int64_t e = 0; e < m->nelem; e++)
+      for (int f = 0; f < 6; f++) {
+        if (m->nb[e * 6 + f] >= 0) continue;
+        OFace F{i, e, f, {}};
+        double cen[3] = {0, 0, 0};
+        for (int t = 0; t < 4; t++) {
+          corner(m, e, f, t & 1, t >> 1, F.c[t]);
+          for (int d = 0; d < 3; d++) cen[d] += 0.25 * F.c[t][d];
+        }
+        where[key(cen)].push_back(faces.size());
+        faces.push_back(F);
+      }
+  }
+  const int G = (int)b->gctx.size();
+  std::vector<std::vector<int64_t>> gfaces(G);  // per group: e * 6 + f of its joined faces
+  std::vector<int> links;                       // [L][6] before slot numbers
+  std::vector<int> link_group;
+  for (const auto &kv : where) {
+    const std::vector<size_t> &lst = kv.second;
+    for (size_t x : lst)
+      for (size_t y : lst) {
+        if (x == y) continue;
+        const OFace &A = faces[x], &B = faces[y];
+        if (A.part == B.part || problem[A.part] != problem[B.part]) continue;
+        int found = -1;
+        for (int o = 0; o < 8 && found < 0; o++) {
+          bool ok = true;
+          for (int t = 0; t < 4 && ok; t++) {
+            const int ca = t & 1, cb = t >> 1;
+            int aa = (o & 1) ? cb : ca, bb = (o & 1) ? ca : cb;
+            if (o & 2) aa = 1 - aa;
+            if (o & 4) bb = 1 - bb;
+            const double *p = B.c[aa + 2 * bb];
+            double d2 = 0.;
+            for (int d = 0; d < 3; d++) d2 += (A.c[t][d] - p[d]) * (A.c[t][d] - p[d]);
+            ok = d2 <= tol * tol;
+          }
+          if (ok) found = o;
+        }
+        if (found < 0) continue;
+        const int ga = b->pgroup[A.part], gb = b->pgroup[B.part];
+        const int64_t ea = b->pelem0[A.part] + A.e, eb = b->pelem0[B.part] + B.e;
+        gfaces[ga].push_back(ea * 6 + A.f);
+        links.insert(links.end(), {ga, (int)(gfaces[ga].size() - 1), gb, (int)eb, B.f, found});
+      }
+  }
+  b->nlink = (int)(links.size() / 6);
+  if (b->nlink == 0) return NMG_OK;
+  // the joined faces of each group read ghost slots after its hang slots
+  std::vector<double *> ghostp(G, nullptr);
+  for (int g = 0; g < G; g++) {
+    nmg_ctx *c = b->gctx[g];
+    const int64_t E = c->nelem;
+    const int nh = c->nhang, nl = (int)gfaces[g].size();
+    if (nl > 0) {
+      std::vector<int> nb(E * 6), code(E * 6), bslot(E * 6);
+      BK(cudaMemcpy(nb.data(), c->d_nb, sizeof(int) * E * 6, cudaMemcpyDeviceToHost));
+      BK(cudaMemcpy(code.data(), c->d_code, sizeof(int) * E * 6, cudaMemcpyDeviceToHost));
+      BK(cudaMemcpy(bslot.data(), c->d_bslot, sizeof(int) * E * 6, cudaMemcpyDeviceToHost));
+      for (int q = 0; q < nl; q++) {
+        const int64_t ef = gfaces[g][q];
+        nb[ef] = (int)(ef / 6);  // any element: the ghost path reads the slot
+        code[ef] = nmgk::kCodeMixed;
+        bslot[ef] = nh + q;
+      }
+      BK(cudaMemcpy(c->d_nb, nb.data(), sizeof(int) * E * 6, cudaMemcpyHostToDevice));
+      BK(cudaMemcpy(c->d_code, code.data(), sizeof(int) * E * 6, cudaMemcpyHostToDevice));
+      BK(cudaMemcpy(c->d_bslot, bslot.data(), sizeof(int) * E * 6, cudaMemcpyHostToDevice));
+      const size_t slots = (size_t)nh + nl;
+      double *ng = nullptr;
+      BK(cudaMalloc((void **)&ng, sizeof(double) * 4 * c->nn * slots));
+      BK(cudaMemset(ng, 0, sizeof(double) * 4 * c->nn * slots));
+      cudaFree(c->d_ghost);
+      c->d_ghost = ng;
+      c->ghost_cap = (int)slots;
+      drop_graphs(c);
+    }
+    ghostp[g] = c->d_ghost;
+  }
+  for (int l = 0; l < b->nlink; l++) links[6 * l + 1] += b->gctx[links[6 * l]]->nhang;
+  // LGL points and barycentric weights of every order (Lagrange.c:15-27)
+  constexpr int M = nmgk::kBatchMaxN;
+  std::vector<double> xt((M + 1) * M, 0.), bt((M + 1) * M, 0.);
+  for (int n = 2; n <= M; n++) {
+    std::vector<double> x(n), w(n), D(n * n);
+    nmg::lgl_basis(n, x.data(), w.data(), D.data());
+    for (int i = 0; i < n; i++) {
+      double den = 1.;
+      for (int j = 0; j < n; j++)
+        if (j != i) den *= (x[i] - x[j]);
+      xt[n * M + i] = x[i];
+      bt[n * M + i] = 1. / den;
+    }
+  }
+  BK(cudaMalloc((void **)&b->d_links, sizeof(int) * links.size()));
+  BK(cudaMemcpy(b->d_links, links.data(), sizeof(int) * links.size(), cudaMemcpyHostToDevice));
+  BK(cudaMalloc((void **)&b->d_ghostp, sizeof(double *) * G));
+  BK(cudaMemcpy(b->d_ghostp, ghostp.data(), sizeof(double *) * G, cudaMemcpyHostToDevice));
+  BK(cudaMalloc((void **)&b->d_wsrc, sizeof(double *) * 8 * G));
+  BK(cudaMalloc((void **)&b->d_xtab, sizeof(double) * xt.size()));
+  BK(cudaMalloc((void **)&b->d_btab, sizeof(double) * bt.size()));
+  BK(cudaMemcpy(b->d_xtab, xt.data(), sizeof(double) * xt.size(), cudaMemcpyHostToDevice));
+  BK(cudaMemcpy(b->d_btab, bt.data(), sizeof(double) * bt.size(), cudaMemcpyHostToDevice));
+  return NMG_OK;
+}
+
+extern "C" {
 
 void nmg_batch_destroy(nmg_batch *b) {
   if (!b) return;
   batch_drop_graphs(b);
+  cudaFree(b->d_links);
+  cudaFree(b->d_ghostp);
+  cudaFree(b->d_wsrc);
+  cudaFree(b->d_xtab);
+  cudaFree(b->d_btab);
   for (auto c : b->gctx) nmg_destroy(c);
   for (auto m : b->gmesh) nmg_mesh_free(m);
   cudaFree(b->d_params);

@@ -100,6 +100,9 @@ typedef struct nmo_mesh {
   const double *dXdxm;      /* [e][3][9][np] dX^a/dx^i at the midpoint right of
                                each node in each direction (par
                                coordinates_midpoint_data = yes), or NULL */
+  const double *ext;        /* [e][6][n*n][5] exterior states of the face
+                               nodes marked -4 in nbnode (faces joined to a
+                               part of the problem held elsewhere), or NULL */
 } nmo_mesh;
 
 /* points of both point types: LGL (DG) with their Lagrange weights, and
@@ -577,6 +580,9 @@ static void face_fnum(const nmo_mesh *m, const nmo_pts *P, int e, int f, int ijk
     mixed_trace(m, P, e, f, JK % n, JK / n, w, ua);
   } else if (nb == -3) {
     hang_trace(m, P, e, f, JK, w, ua);
+  } else if (nb == -4) {
+    const double *X = m->ext + (((size_t)e * 6 + f) * n * n + JK) * NF;
+    for (l = 0; l < NF; l++) ua[l] = X[l];
   } else if (m->bc == 0) {
     const double *X = m->xyz + (size_t)e * 3 * np;
     double xyz[3] = {X[ijk], X[np + ijk], X[2 * np + ijk]};

@@ -44,7 +44,8 @@ class _Mesh(ctypes.Structure):
                 ("fv_w3ratio", ctypes.c_double), ("mixface", ctypes.c_void_p),
                 ("numflux", ctypes.c_int), ("hang_off", ctypes.c_void_p),
                 ("hang_src", ctypes.c_void_p), ("hang_pos", ctypes.c_void_p),
-                ("surf_interp", ctypes.c_int), ("dXdxm", ctypes.c_void_p)]
+                ("surf_interp", ctypes.c_int), ("dXdxm", ctypes.c_void_p),
+                ("ext", ctypes.c_void_p)]
 
 # reconstruction modes (reference par fv_rec) and div(f) extrapolation
 # modes (par fv_divf_extrap) understood by the oracle
@@ -439,7 +440,13 @@ class OracleMesh:
                        *((None,) * 3 if self.hang is None else
                          tuple(a.ctypes.data for a in self.hang)),
                        {"linear": 0, "parabolic": 1}[fv_surface_interp],
-                       None if self.dXdxm is None else self.dXdxm.ctypes.data)
+                       None if self.dXdxm is None else self.dXdxm.ctypes.data, None)
+        self.ext = None
+
+    def set_ext(self, ext):
+        """Exterior states [E, 6, n*n, 5] of the face nodes marked -4."""
+        self.ext = np.ascontiguousarray(ext, np.float64)
+        self.s.ext = self.ext.ctypes.data
 
     def rhs(self, w, t=0.0):
         w = np.ascontiguousarray(w, np.float64)
@@ -756,3 +763,106 @@ class GrhdOracle:
                                 src.ctypes.data_as(ctypes.c_void_p), dst.ctypes.data_as(ctypes.c_void_p))
             out[f] = dst
         return out
+
+
+
+class LinkedOracle:
+    """Parts of one problem, each an OracleMesh with its own n (the
+    reference's p-refinement by patch, amr_prefine_p), joined across their
+    coinciding outer faces: a face node's exterior state is the other
+    part's face plane interpolated at the node's position, Lagrange in both
+    in-plane directions (set_ajsurf_vl's interpolation branch,
+    src/main/amr/surface.c:900-1460)."""
+
+    def __init__(self, parts, xyzs):
+        """parts: OracleMesh of each part; xyzs: their coordinates [E,3,np]."""
+        self.parts = list(parts)
+        self.links = []   # (part, e, f, src part, e2, f2, o)
+        keyof = {}
+        h, tol = 1e-6, 1e-9
+        corners = []
+        for i, (om, xyz) in enumerate(zip(self.parts, xyzs)):
+            n = om.n
+            nbn = om.nbnode.reshape(om.nelem, 6, n * n)
+            for e in range(om.nelem):
+                for f in range(6):
+                    if nbn[e, f, 0] != -1:
+                        continue
+                    pl = face_plane_index(n, f)
+                    c = xyz[e][:, pl[[0, n - 1, n * (n - 1), n * n - 1]]].T
+                    k = tuple(np.round(c.mean(0) / h).astype(np.int64))
+                    keyof.setdefault(k, []).append((i, e, f, c))
+        for lst in keyof.values():
+            for (i, e, f, c) in lst:
+                for (j, e2, f2, c2) in lst:
+                    if i == j:
+                        continue
+                    for o in range(8):
+                        ok = True
+                        for t in range(4):
+                            ca, cb = t & 1, t >> 1
+                            aa, bb = (cb, ca) if o & 1 else (ca, cb)
+                            aa = 1 - aa if o & 2 else aa
+                            bb = 1 - bb if o & 4 else bb
+                            if np.abs(c[t] - c2[aa + 2 * bb]).max() > tol:
+                                ok = False
+                                break
+                        if ok:
+                            self.links.append((i, e, f, j, e2, f2, o))
+                            break
+        for (i, e, f, j, e2, f2, o) in self.links:
+            om = self.parts[i]
+            om.nbnode.reshape(om.nelem, 6, om.n * om.n)[e, f, :] = -4
+        self.exts = [np.zeros((om.nelem, 6, om.n * om.n, 5)) for om in self.parts]
+        for om, ext in zip(self.parts, self.exts):
+            om.set_ext(ext)
+
+    @staticmethod
+    def _bary(n):
+        x, _ = lgl(n)
+        b = np.array([1.0 / np.prod([x[i] - x[j] for j in range(n) if j != i]) for i in range(n)])
+        return x, b
+
+    def _fill(self, us):
+        for ext in self.exts:
+            ext[:] = 0.0
+        for (i, e, f, j, e2, f2, o) in self.links:
+            nt, ns = self.parts[i].n, self.parts[j].n
+            xt, _ = lgl(nt)
+            xs, bs = self._bary(ns)
+            pl = face_plane_index(ns, f2)
+            W = us[j][e2][:, pl].reshape(5, ns, ns)   # [field][b][a]
+            for b_ in range(nt):
+                for a_ in range(nt):
+                    u, v = (xt[b_], xt[a_]) if o & 1 else (xt[a_], xt[b_])
+                    u = -u if o & 2 else u
+                    v = -v if o & 4 else v
+                    la = np.array([bs[k] * np.prod([u - xs[q] for q in range(ns) if q != k])
+                                   for k in range(ns)])
+                    lb = np.array([bs[k] * np.prod([v - xs[q] for q in range(ns) if q != k])
+                                   for k in range(ns)])
+                    self.exts[i][e, f, a_ + nt * b_] = np.einsum("fba,a,b->f", W, la, lb)
+
+    def rhs(self, us, t=0.0):
+        self._fill(us)
+        return [om.rhs(u, t) for om, u in zip(self.parts, us)]
+
+    def rk4(self, us, dt, nsteps, t=0.0):
+        """Classic RK4 steps of all parts together (evolve_RK4_mesh)."""
+        us = [np.array(u, np.float64, copy=True) for u in us]
+        c = (dt / 6., dt / 3., dt / 3., dt / 6.)
+        a = (dt / 2., dt / 2., dt)
+        te = np.longdouble(0.)
+        for _ in range(nsteps):
+            ts0 = float(np.longdouble(t) + te)
+            ts = (ts0, ts0 + 0.5 * dt, ts0 + 0.5 * dt, ts0 + dt)
+            up = [u.copy() for u in us]
+            w = [u.copy() for u in us]
+            for s in range(4):
+                r = self.rhs(w, ts[s])
+                for k in range(len(us)):
+                    us[k] = us[k] + c[s] * r[k]
+                    if s < 3:
+                        w[k] = up[k] + a[s] * r[k]
+            te += np.longdouble(dt)
+        return us
