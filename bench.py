@@ -362,7 +362,9 @@ def batch_problem_specs(count, seed=4242):
     [64, 32768] (realised by the nearest box (8^L) mesh or 7-cubed-sphere
     mesh with k of its patches one level finer, (7-k) 8^L + k 8^(L+1)
     elements, k in 0..3: refinement levels 0..5 with non-conforming faces
-    between levels), orders N uniform in {3..9} (n = N+1 nodes)."""
+    between levels), orders N uniform in {3..9} (n = N+1 nodes): per patch
+    on the cubed spheres without level jumps (parts of different n joined
+    by interpolated traces), per problem otherwise."""
     rng = np.random.default_rng(seed)
     specs = []
     opts = [("box", L, 0, 8 ** L) for L in range(2, 6)] + \
@@ -373,19 +375,45 @@ def batch_problem_specs(count, seed=4242):
         kind, L, k, E = min(opts, key=lambda o: abs(np.log(o[3]) - np.log(target)))
         n = int(rng.integers(3, 10)) + 1
         href = tuple(sorted(int(p) for p in rng.choice(7, k, replace=False))) if k else ()
-        specs.append((kind, L, n, E, href))
+        orders = (n,)
+        if kind == "cs7" and not k:
+            orders = tuple(int(rng.integers(3, 10)) + 1 for _ in range(7))
+        specs.append((kind, L, orders, E, href))
     return specs
 
 
-def _batch_compare(meshes, states, K):
+def batch_meshes(specs):
+    """Meshes of the problems (one per part) and each mesh's problem."""
+    import nmesh_gb300 as ng
+    meshes, owner = [], []
+    for pid, (kind, L, orders, E, href) in enumerate(specs):
+        if kind == "box":
+            meshes.append(ng.Mesh.build(ng.MESH_BOX, n=orders[0], luni=L, xc=(PI, PI, PI),
+                                        box_dout=PI, periodic=True))
+            owner.append(pid)
+        elif len(orders) == 1:
+            meshes.append(ng.Mesh.build(ng.MESH_CUBEDSPHERES7, n=orders[0], luni=L, cs_dc=1.0,
+                                        cs_r0fac=20.0, hrefine=href))
+            owner.append(pid)
+        else:
+            for n in sorted(set(orders)):
+                pats = [p for p in range(7) if orders[p] == n]
+                meshes.append(ng.Mesh.build(ng.MESH_CUBEDSPHERES7, n=n, luni=L, cs_dc=1.0,
+                                            cs_r0fac=20.0, patches=pats))
+                owner.append(pid)
+    return meshes, owner
+
+
+def _batch_compare(meshes, owner, states, K):
     """Times of K RK4 steps of the problems: batched (one launch per stage
-    for all orders, or one per order, graph-captured), plain (each problem
-    its own context, 4 launches per problem and step) and per-problem
-    graphs (each problem's step captured)."""
+    for all orders, or one per order, graph-captured; parts of one problem
+    joined), plain (each problem on its own: a context, or a batch of its
+    parts, 4 stage launches per step) and per-problem graphs (each
+    single-part problem's step captured; the multi-part ones as in plain)."""
     import torch
     import nmesh_gb300 as ng
     dt = 1e-4
-    b = ng.Batch(meshes, ng.BC_OUTGOING)
+    b = ng.Batch(meshes, ng.BC_OUTGOING, problems=owner)
     for p, u in enumerate(states):
         b.set_state(p, u)
     b.rk4_steps(0.0, dt, 2)  # autotune + graph capture + warm-up
@@ -395,33 +423,47 @@ def _batch_compare(meshes, states, K):
     torch.cuda.synchronize()
     t_batch = time.perf_counter() - t0
     info = b.info()
+    linked = b.linked_faces
     b.close()
-    evs = []
-    for m, u in zip(meshes, states):
-        ev = ng.Evolution(m, ng.BC_OUTGOING)
-        ev.set_state(u)
-        ev.rk4_step(0.0, dt)  # autotune + warm-up
-        evs.append(ev)
+    runs = []   # (kind, object)
+    for pid in sorted(set(owner)):
+        idx = [p for p in range(len(meshes)) if owner[p] == pid]
+        if len(idx) == 1:
+            ev = ng.Evolution(meshes[idx[0]], ng.BC_OUTGOING)
+            ev.set_state(states[idx[0]])
+            ev.rk4_step(0.0, dt)  # autotune + warm-up
+            runs.append(("ctx", ev))
+        else:
+            pb = ng.Batch([meshes[p] for p in idx], ng.BC_OUTGOING, problems=[0] * len(idx))
+            for q, p in enumerate(idx):
+                pb.set_state(q, states[p])
+            pb.rk4_steps(0.0, dt, 1)
+            runs.append(("batch", pb))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for s in range(K):
-        for ev in evs:
-            ev.rk4_step((2 + s) * dt, dt)
+        for kind, obj in runs:
+            if kind == "ctx":
+                obj.rk4_step((2 + s) * dt, dt)
+            else:
+                obj.rk4_steps((2 + s) * dt, dt, 1)
     torch.cuda.synchronize()
     t_plain = time.perf_counter() - t0
-    for ev in evs:
-        ev.rk4_steps(0.0, dt, 1)  # per-problem graphs captured
+    for kind, obj in runs:
+        if kind == "ctx":
+            obj.rk4_steps(0.0, dt, 1)  # per-problem graphs captured
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for ev in evs:
-        ev.rk4_steps(0.0, dt, K)
+    for kind, obj in runs:
+        obj.rk4_steps(0.0, dt, K)
     torch.cuda.synchronize()
     t_graphs = time.perf_counter() - t0
-    for ev in evs:
-        ev.close()
+    for _, obj in runs:
+        obj.close()
     dof = sum(m.nelem * m.np * NFIELDS for m in meshes)
-    return {"problems": len(meshes), "elements": int(sum(m.nelem for m in meshes)),
-            "dof": int(dof), "steps": K,
+    return {"problems": len(runs), "parts": len(meshes),
+            "elements": int(sum(m.nelem for m in meshes)),
+            "dof": int(dof), "steps": K, "linked_faces": int(linked),
             "batched_dof_stage_per_s": dof * 4 * K / t_batch,
             "plain_dof_stage_per_s": dof * 4 * K / t_plain,
             "per_problem_graphs_dof_stage_per_s": dof * 4 * K / t_graphs,
@@ -432,35 +474,31 @@ def _batch_compare(meshes, states, K):
 
 def batched_bench(args):
     """Batched execution of many independent problems against the same
-    problems stepped one after the other through their own contexts; for
-    all 64 problems, and for the ones of at most 4096 elements, where the
-    per-problem launches rather than the arithmetic set the time."""
-    import nmesh_gb300 as ng
+    problems stepped one after the other; for all 64 problems, and for the
+    ones of at most 4096 elements, where the per-problem launches rather
+    than the arithmetic set the time."""
     specs = batch_problem_specs(args.batch_problems)
-    meshes = []
-    for kind, L, n, E, href in specs:
-        if kind == "box":
-            meshes.append(ng.Mesh.build(ng.MESH_BOX, n=n, luni=L, xc=(PI, PI, PI),
-                                        box_dout=PI, periodic=True))
-        else:
-            meshes.append(ng.Mesh.build(ng.MESH_CUBEDSPHERES7, n=n, luni=L, cs_dc=1.0,
-                                        cs_r0fac=20.0, hrefine=href))
+    meshes, owner = batch_meshes(specs)
     rng = np.random.default_rng(7)
     states = [1e-3 * rng.standard_normal((m.nelem, NFIELDS, m.np)) for m in meshes]
-    out = _batch_compare(meshes, states, args.batch_steps)
-    small = [p for p, m in enumerate(meshes) if m.nelem <= 4096]
-    sub = _batch_compare([meshes[p] for p in small], [states[p] for p in small],
-                         args.batch_small_steps)
-    nelem = [m.nelem for m in meshes]
+    out = _batch_compare(meshes, owner, states, args.batch_steps)
+    small_pids = {pid for pid, sp in enumerate(specs) if sp[3] <= 4096}
+    sel = [p for p in range(len(meshes)) if owner[p] in small_pids]
+    sub = _batch_compare([meshes[p] for p in sel], [owner[p] for p in sel],
+                         [states[p] for p in sel], args.batch_small_steps)
+    orders = sorted({int(m.n) for m in meshes})
     out.update({
-        "orders_n": sorted(set(int(m.n) for m in meshes)),
-        "element_counts_min_max": [int(min(nelem)), int(max(nelem))],
+        "orders_n": orders,
+        "element_counts_min_max": [int(min(sp[3] for sp in specs)),
+                                   int(max(sp[3] for sp in specs))],
+        "mixed_order_problems": int(sum(1 for sp in specs if len(sp[2]) > 1)),
         "refinement_levels": sorted(set(int(L) + d for _, L, _, _, h in specs
                                         for d in ((0, 1) if h else (0,)))),
         "problems_with_level_jumps": int(sum(1 for s_ in specs if s_[4])),
-        "note": "orders are per problem; problems with level jumps have patches one "
-                "level finer than their neighbours (non-conforming faces, traces "
-                "interpolated each stage); all problems share dt",
+        "note": "orders per patch on cubed spheres without level jumps (parts joined by "
+                "interpolated traces), per problem otherwise; problems with level jumps have "
+                "patches one level finer than their neighbours (non-conforming faces); all "
+                "problems share dt",
         "small_problems": dict(sub, selection="the problems of at most 4096 elements")})
     return out
 

@@ -14,6 +14,7 @@
 // vanish identically on an element (cubed-sphere maps have two) are never
 // loaded or multiplied.  r_pi is split over three partial sums so that the
 // three c-component tasks of one line never write the same address.
+#include <algorithm>
 #include <cstdio>
 
 #include "stage.cuh"
@@ -689,9 +690,14 @@ size_t batch_smem(int n) {
   return (n >= 2 && n <= kBatchMaxN) ? sizeof(double) * 10 * bEPB(n) * n * n * n : 0;
 }
 
+// the kernel's shared-memory limit is one setting per function for every
+// batch alive: set it to the largest tile of any order, so that creating a
+// batch of small orders never lowers it under a live batch of larger ones
 cudaError_t batch_prepare(size_t smem) {
+  size_t most = smem;
+  for (int n = 2; n <= kBatchMaxN; n++) most = std::max(most, batch_smem(n));
   return cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)smem);
+                              (int)most);
 }
 
 cudaError_t batch_launch(const StageParams *d_params, const int *d_gn, const int *d_gblk0,

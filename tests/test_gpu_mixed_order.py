@@ -123,3 +123,17 @@ def test_inner_cube_of_higher_order_matches_oracle():
     want = lo.rk4(us, dt, 2)
     for p in range(2):
         assert rel_l2(b.get_state(p), want[p]) <= RTOL_RK4
+
+
+def test_batches_of_different_orders_live_together():
+    """A batch of low orders created after one of high orders leaves the
+    first one steppable (the persistent kernel's shared-memory limit)."""
+    hi = ng.Batch([ng.Mesh.build(ng.MESH_BOX, n=10, luni=1, xc=(0.0,) * 3, box_dout=1.0)],
+                  ng.BC_OUTGOING)
+    hi.set_mode(1)
+    lo = ng.Batch([ng.Mesh.build(ng.MESH_BOX, n=3, luni=1, xc=(0.0,) * 3, box_dout=1.0)],
+                  ng.BC_OUTGOING)
+    lo.set_mode(1)
+    lo.rk4_steps(0.0, 1e-3, 1)
+    hi.rk4_steps(0.0, 1e-3, 1)
+    lo.rk4_steps(1e-3, 1e-3, 1)
