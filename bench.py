@@ -474,9 +474,9 @@ def _batch_compare(meshes, owner, states, K):
 
 def batched_bench(args):
     """Batched execution of many independent problems against the same
-    problems stepped one after the other; for all 64 problems, and for the
-    ones of at most 4096 elements, where the per-problem launches rather
-    than the arithmetic set the time."""
+    problems stepped one after the other; for all 64 problems, for the ones
+    of at most 4096 elements and for the ones of at most 512 elements, where
+    the per-problem launches rather than the arithmetic set the time."""
     specs = batch_problem_specs(args.batch_problems)
     meshes, owner = batch_meshes(specs)
     rng = np.random.default_rng(7)
@@ -486,6 +486,10 @@ def batched_bench(args):
     sel = [p for p in range(len(meshes)) if owner[p] in small_pids]
     sub = _batch_compare([meshes[p] for p in sel], [owner[p] for p in sel],
                          [states[p] for p in sel], args.batch_small_steps)
+    tiny_pids = {pid for pid, sp in enumerate(specs) if sp[3] <= 512}
+    sel = [p for p in range(len(meshes)) if owner[p] in tiny_pids]
+    tiny = _batch_compare([meshes[p] for p in sel], [owner[p] for p in sel],
+                          [states[p] for p in sel], args.batch_small_steps)
     orders = sorted({int(m.n) for m in meshes})
     out.update({
         "orders_n": orders,
@@ -499,7 +503,8 @@ def batched_bench(args):
                 "interpolated traces), per problem otherwise; problems with level jumps have "
                 "patches one level finer than their neighbours (non-conforming faces); all "
                 "problems share dt",
-        "small_problems": dict(sub, selection="the problems of at most 4096 elements")})
+        "small_problems": dict(sub, selection="the problems of at most 4096 elements"),
+        "tiny_problems": dict(tiny, selection="the problems of at most 512 elements")})
     return out
 
 
