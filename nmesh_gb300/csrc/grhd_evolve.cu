@@ -38,7 +38,11 @@
 namespace {
 
 #include "grhd.cuh"
+// the finite-volume midpoint reconstructions with one division per
+// reconstruction (the nonlinear weights normalised together)
+#define NMG_FV_FAST
 #include "weno.cuh"
+#undef NMG_FV_FAST
 
 constexpr int NF = 5;
 constexpr int kMaxN = 10;   // DG points per direction
@@ -48,6 +52,7 @@ constexpr int kMaxNF = 16;  // finite-volume points per direction
 // of the point: unit normal, J |grad Xb^a|, alpha, psi (6 x 3)
 constexpr int kGeo = 39;
 constexpr int kNT = 256;
+constexpr int kNTF = 512;  // finite-volume kernel: one CTA per SM, 16 warps
 
 struct ShellMap {
   int dom[6];
@@ -203,7 +208,7 @@ struct GrP {
   const double *dXdx;    // [E][9][np]
   const double *bgd;     // [E][8][np]
   const double *bbox;    // [E][6]
-  const double *basis;   // D [n*n], wl [n], xl [n], xu [nf]
+  const double *basis;   // D [n*n], wl [n], xl [n], xu [nf], barycentric weights [n]
   const double *geo;     // [slot][kGeo][npf]
   double *trace;         // [ntr][5][tpts]
   // stage buffers
@@ -304,14 +309,16 @@ __global__ void trace_kernel(GrP P, const double *prim_d, const double *prim_f) 
     if (o & 4) u = -u;
     double *out = P.trace + (size_t)t * NF * P.tpts;
     if (fv) {
-      // DG neighbour: Lagrange basis of the LGL points at (s, u)
+      // DG neighbour: Lagrange basis of the LGL points at (s, u), in the
+      // barycentric form (weights bw = 1 / prod_{j != k} (x_k - x_j))
+      const double *bw = xu + P.nf;
       double la[kMaxN], lb[kMaxN];
       for (int k = 0; k < P.n; k++) {
-        double va = 1., vb = 1.;
+        double va = bw[k], vb = bw[k];
         for (int j = 0; j < P.n; j++)
           if (j != k) {
-            va *= (s - xl[j]) / (xl[k] - xl[j]);
-            vb *= (u - xl[j]) / (xl[k] - xl[j]);
+            va *= s - xl[j];
+            vb *= u - xl[j];
           }
         la[k] = va;
         lb[k] = vb;
@@ -456,7 +463,7 @@ __global__ void __launch_bounds__(kNT) dg_kernel(GrP P) {
 }
 
 // finite-volume elements: one CTA per slot
-__global__ void __launch_bounds__(kNT) fv_kernel(GrP P) {
+__global__ void __launch_bounds__(kNTF, 1) fv_kernel(GrP P) {
   extern __shared__ double sm[];
   const int nf = P.nf, npf = P.npf, nnf = P.nnf;
   const int slot = blockIdx.x, e = P.slotelem[slot];
@@ -852,7 +859,7 @@ int enqueue_stage(nmg_grhd_ctx *c, GrP P, double *win_d, double *win_f,
   mark(5);
   mark(6);
   if (c->nfv > 0) {
-    fv_kernel<<<c->nfv, kNT, c->smem_fv, c->stream>>>(P);
+    fv_kernel<<<c->nfv, kNTF, c->smem_fv, c->stream>>>(P);
     GCK(cudaGetLastError());
     c->launches++;
   }
@@ -1012,6 +1019,12 @@ int nmg_grhd_create(const nmg_mesh *m, const nmg_grhd_evolve_params *p, nmg_grhd
     nmg::uniform_basis(c->nf, xu.data(), wu.data(), Du.data());
   }
   basis.insert(basis.end(), xu.begin(), xu.end());
+  for (int k = 0; k < c->n; k++) {  // barycentric weights of the LGL points
+    double den = 1.;
+    for (int j = 0; j < c->n; j++)
+      if (j != k) den *= m->x[k] - m->x[j];
+    basis.push_back(1. / den);
+  }
   std::vector<double> Pm, Rm;
   transfer_matrices(c->n, c->nf, m->x, xu, Pm, Rm);
   int rc;
