@@ -119,3 +119,30 @@ def test_bad_arguments_are_rejected():
     ev = ng.GrhdEvolution(m)
     with pytest.raises(ng.NmgError):
         ev.rk4_steps(-1.0, 1)
+
+
+def test_twenty_steps_with_a_switch_midway_match_oracle():
+    """Ten RK4 steps, elements switched to and from finite volume, ten more
+    steps: the GPU state against the oracle's, which applies the same
+    transfer (P x P x P to finite volume, R x R x R back)."""
+    n, nf = 5, 10
+    o, ev, fv, (ud, uf, pd, pf) = _case(n, nf, 2, [4, 9, 22], vel=(0.04, 0.02, -0.03))
+    dt = 0.02
+    ev.rk4_steps(dt, 10)
+    ud, uf, pd, pf = o.rk4(ud, uf, pd, pf, dt, 10)
+    got = ev.get_state()
+    _compare(fv, got[0], got[1], ud, uf, RTOL)
+    # switch: 4 back to DG, 30 and 31 to finite volume
+    P, R = o.transfer()
+    fv2 = fv.copy()
+    fv2[4] = 0
+    fv2[[30, 31]] = 1
+    ev.set_fv_elements(fv2)
+    ud[4], pd[4] = o.apply3(R, uf[4]), o.apply3(R, pf[4])
+    for e in (30, 31):
+        uf[e], pf[e] = o.apply3(P, ud[e]), o.apply3(P, pd[e])
+    o.set_fv(fv2)
+    ev.rk4_steps(dt, 10)
+    ud, uf, pd, pf = o.rk4(ud, uf, pd, pf, dt, 10)
+    got = ev.get_state()
+    _compare(fv2, got[0], got[1], ud, uf, RTOL)
