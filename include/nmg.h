@@ -353,6 +353,18 @@ int nmg_grhd_sizes(const nmg_grhd_ctx *c, int32_t *n, int32_t *nf, int64_t *nele
  * each direction, back by the pseudo-inverse R = (P^T P)^-1 P^T */
 int nmg_grhd_set_fv_elements(nmg_grhd_ctx *c, const int32_t *fv);
 int nmg_grhd_get_fv_elements(nmg_grhd_ctx *c, int32_t *fv);
+/* Persson's modal indicator of D per element (evolve_Persson_array_indicator,
+ * src/main/evolve/trouble.c:505-564): log10 of the share of the squared
+ * normalised Legendre coefficients in the highest modes, on the LGL points
+ * (a finite-volume element's state projected back by R x R x R first);
+ * ind[nelem] on the host */
+int nmg_grhd_trouble_indicators(nmg_grhd_ctx *c, double *ind);
+/* DG elements whose indicator exceeds persson_max switch to finite volume,
+ * finite-volume elements whose indicator fell below persson_max -
+ * back_margin switch back (the state transferred as nmg_grhd_set_fv_elements
+ * does); switched[0] / [1] (may be NULL): elements switched to FV / to DG */
+int nmg_grhd_update_troubled(nmg_grhd_ctx *c, double persson_max, double back_margin,
+                             int32_t *switched);
 int64_t nmg_grhd_fv_count(const nmg_grhd_ctx *c);
 /* state from primitives (rho, v^1, v^2, v^3, p) (U = prim2con; the
  * primitives are also the root finder's starting guesses) */

@@ -232,6 +232,8 @@ def lib(build_if_missing=True):
         "nmg_grhd_reset_stats": (ctypes.c_int, [vp]),
         "nmg_grhd_stream": (vp, [vp]),
         "nmg_grhd_profile_step": (ctypes.c_int, [vp, f64, vp]),
+        "nmg_grhd_trouble_indicators": (ctypes.c_int, [vp, vp]),
+        "nmg_grhd_update_troubled": (ctypes.c_int, [vp, f64, f64, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -824,6 +826,21 @@ class GrhdEvolution:
     def set_fv_elements(self, fv):
         fv = np.ascontiguousarray(fv, np.int32)
         self._check(lib().nmg_grhd_set_fv_elements(self._h, _ptr(fv)), "nmg_grhd_set_fv_elements")
+
+    def trouble_indicators(self):
+        """Persson's indicator of D per element (log10)."""
+        ind = np.zeros(self.nelem)
+        self._check(lib().nmg_grhd_trouble_indicators(self._h, _ptr(ind)),
+                    "nmg_grhd_trouble_indicators")
+        return ind
+
+    def update_troubled(self, persson_max, back_margin=1.0):
+        """Switch by the indicator; returns (to finite volume, to DG)."""
+        sw = np.zeros(2, np.int32)
+        self._check(lib().nmg_grhd_update_troubled(self._h, float(persson_max),
+                                                   float(back_margin), _ptr(sw)),
+                    "nmg_grhd_update_troubled")
+        return int(sw[0]), int(sw[1])
 
     def fv_elements(self):
         fv = np.zeros(self.nelem, np.int32)

@@ -658,6 +658,78 @@ __global__ void copy_rows_kernel(int64_t rowlen, const int *isrc, const int *ids
     out[i] = in[i];
 }
 
+// Persson's modal indicator of D (field 0) per element (the reference's
+// evolve_Persson_array_indicator, src/main/evolve/trouble.c:505-564): the
+// LGL nodal values (a finite-volume element's projected back by R x R x R)
+// analysed into normalised Legendre coefficients c by A x A x A, then
+// log10(sum of c^2 over the modes of highest degree in some direction /
+// sum of all c^2).  One CTA per element.
+__global__ void persson_kernel(GrP P, const double *u_d, const double *u_f, const double *A,
+                               const double *R, double *ind) {
+  extern __shared__ double sm[];
+  const int n = P.n, np = P.np, nf = P.nf;
+  const int e = blockIdx.x, slot = P.fvslot[e];
+  double *sU = sm, *t1 = sU + max(np, P.npf), *t2 = t1 + max(n * nf * nf, np);
+  double *sC = t2 + max(n * n * nf, np), *red = sC + np;
+  // nodal values of D on the LGL points
+  if (slot < 0) {
+    for (int q = threadIdx.x; q < np; q += blockDim.x) sU[q] = u_d[(size_t)e * NF * np + q];
+  } else {
+    const int npf = P.npf;
+    for (int q = threadIdx.x; q < npf; q += blockDim.x) sU[q] = u_f[(size_t)slot * NF * npf + q];
+    __syncthreads();
+    for (int t = threadIdx.x; t < n * nf * nf; t += blockDim.x) {
+      const int i = t % n, jk = t / n;
+      double s = 0.;
+      for (int m = 0; m < nf; m++) s += R[i * nf + m] * sU[m + nf * jk];
+      t1[t] = s;
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < n * n * nf; t += blockDim.x) {
+      const int i = t % n, j = (t / n) % n, k = t / (n * n);
+      double s = 0.;
+      for (int m = 0; m < nf; m++) s += R[j * nf + m] * t1[i + n * (m + nf * k)];
+      t2[t] = s;
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < np; t += blockDim.x) {
+      const int i = t % n, j = (t / n) % n, k = t / (n * n);
+      double s = 0.;
+      for (int m = 0; m < nf; m++) s += R[k * nf + m] * t2[i + n * (j + n * m)];
+      sC[t] = s;
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < np; t += blockDim.x) sU[t] = sC[t];
+  }
+  __syncthreads();
+  // modal analysis, one direction at a time (as nmo_persson)
+  for (int d = 0; d < 3; d++) {
+    const int st = d == 0 ? 1 : (d == 1 ? n : n * n);
+    for (int k = threadIdx.x; k < np; k += blockDim.x) {
+      const int ii = d == 0 ? k % n : (d == 1 ? (k / n) % n : k / (n * n));
+      const double *line = sU + k - ii * st;
+      double sum = 0.;
+      for (int l = 0; l < n; l++) sum += A[ii * n + l] * line[l * st];
+      sC[k] = sum;
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < np; k += blockDim.x) sU[k] = sC[k];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    double all = 0., hi = 0.;
+    for (int k = 0; k < n; k++)
+      for (int j = 0; j < n; j++)
+        for (int i = 0; i < n; i++) {
+          const double co = sU[i + n * (j + n * k)];
+          all += co * co;
+          if (i == n - 1 || j == n - 1 || k == n - 1) hi += co * co;
+        }
+    ind[e] = log10(hi / (all + 2.2250738585072014e-308) + 1e-50);
+  }
+  (void)red;
+}
+
 __global__ void p2c_kernel(nmg_grhd_params g, int64_t nrows, int npts, const double *psi_rows,
                            int psi_stride, const int *psi_row_of, const double *prim,
                            double *cons) {
@@ -693,7 +765,7 @@ struct nmg_grhd_ctx {
   // device mesh
   int *d_nb = nullptr, *d_code = nullptr, *d_pat = nullptr;
   double *d_dXdx = nullptr, *d_bgd = nullptr, *d_bbox = nullptr, *d_basis = nullptr;
-  double *d_Pm = nullptr, *d_Rm = nullptr;
+  double *d_Pm = nullptr, *d_Rm = nullptr, *d_A = nullptr, *d_ind = nullptr;
   // DG states and guesses
   double *d_ud[4] = {nullptr, nullptr, nullptr, nullptr};
   double *d_pd = nullptr;
@@ -799,6 +871,34 @@ void transfer_matrices(int n, int nf, const std::vector<double> &xl, const std::
   }
   for (int i = 0; i < n; i++)
     for (int q = 0; q < nf; q++) Rm[(size_t)i * nf + q] = (double)A[(size_t)i * w + n + q];
+}
+
+// normalised Legendre analysis of n LGL points: A[i][j] = w_j P_i(x_j)
+// sqrt(c_i), c_i = (2i+1)/2 and n/2-1/2 ... (N/2 for the top mode), as the
+// reference's LGL_AT_ST_matrices (src/main/basis/Legendre.c:277-310)
+std::vector<double> analysis_matrix(const std::vector<double> &x, const std::vector<double> &w) {
+  const int n = (int)x.size(), N = n - 1;
+  std::vector<double> A((size_t)n * n);
+  for (int i = 0; i < n; i++) {
+    double ooci = 0.5 * (2 * i + 1);
+    if (i == N && N != 0) ooci = 0.5 * i;
+    const double oosci = std::sqrt(ooci);
+    for (int j = 0; j < n; j++) {
+      double Pk = 0., P0 = 1.0, P1 = x[j], Pi;
+      if (i == 0) Pi = P0;
+      else if (i == 1) Pi = P1;
+      else {
+        for (int k = 2; k <= i; k++) {
+          Pk = (x[j] * (2 * k - 1) * P1 - (k - 1) * P0) / k;
+          P0 = P1;
+          P1 = Pk;
+        }
+        Pi = Pk;
+      }
+      A[(size_t)i * n + j] = w[j] * (Pi * oosci);
+    }
+  }
+  return A;
 }
 
 GrP base_params(nmg_grhd_ctx *c) {
@@ -1032,7 +1132,8 @@ int nmg_grhd_create(const nmg_mesh *m, const nmg_grhd_evolve_params *p, nmg_grhd
       (rc = upload(c, &c->d_pat, m->pat)) || (rc = upload(c, &c->d_dXdx, m->dXdx)) ||
       (rc = upload(c, &c->d_bgd, bgd)) || (rc = upload(c, &c->d_bbox, m->bbox)) ||
       (rc = upload(c, &c->d_basis, basis)) || (rc = upload(c, &c->d_Pm, Pm)) ||
-      (rc = upload(c, &c->d_Rm, Rm)))
+      (rc = upload(c, &c->d_Rm, Rm)) || (rc = upload(c, &c->d_A, analysis_matrix(m->x, m->w))) ||
+      (rc = dalloc(c, &c->d_ind, (size_t)m->nelem)))
     return rc;
   const size_t ld = (size_t)E * NF * c->np;
   for (int b = 0; b < 4; b++)
@@ -1051,7 +1152,7 @@ void nmg_grhd_destroy(nmg_grhd_ctx *c) {
   drop_graphs(c);
   if (c->stream) cudaStreamSynchronize(c->stream);
   void *ptrs[] = {c->d_nb, c->d_code, c->d_pat, c->d_dXdx, c->d_bgd, c->d_bbox, c->d_basis,
-                  c->d_Pm, c->d_Rm, c->d_ud[0], c->d_ud[1], c->d_ud[2], c->d_ud[3], c->d_pd,
+                  c->d_Pm, c->d_Rm, c->d_A, c->d_ind, c->d_ud[0], c->d_ud[1], c->d_ud[2], c->d_ud[3], c->d_pd,
                   c->d_uf[0], c->d_uf[1], c->d_uf[2], c->d_uf[3], c->d_pf, c->d_rbuf, c->d_geo,
                   c->d_slotelem, c->d_fvslot, c->d_dglist, c->d_tslot, c->d_tface, c->d_trace,
                   c->d_stats};
@@ -1165,6 +1266,46 @@ int nmg_grhd_set_fv_elements(nmg_grhd_ctx *c, const int32_t *fv) {
   GCK(cudaStreamSynchronize(c->stream));
   drop_graphs(c);
   return NMG_OK;
+}
+
+int nmg_grhd_trouble_indicators(nmg_grhd_ctx *c, double *ind) {
+  if (!c || !ind) return gset(c, NMG_EINVAL, "nmg_grhd_trouble_indicators: null argument");
+  const int n = c->n, nf = c->nf, np = c->np;
+  const size_t smem = sizeof(double) * ((size_t)std::max(np, c->npf) +
+                                        std::max(n * nf * nf, np) + std::max(n * n * nf, np) + np);
+  GCK(cudaFuncSetAttribute(persson_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  GrP P = base_params(c);
+  persson_kernel<<<(unsigned)c->E, kNT, smem, c->stream>>>(P, c->d_ud[c->cur], c->d_uf[c->cur],
+                                                          c->d_A, c->d_Rm, c->d_ind);
+  GCK(cudaGetLastError());
+  GCK(cudaMemcpyAsync(ind, c->d_ind, sizeof(double) * c->E, cudaMemcpyDeviceToHost, c->stream));
+  GCK(cudaStreamSynchronize(c->stream));
+  return NMG_OK;
+}
+
+int nmg_grhd_update_troubled(nmg_grhd_ctx *c, double persson_max, double back_margin,
+                             int32_t *switched) {
+  if (!c || !(back_margin >= 0.))
+    return gset(c, NMG_EINVAL, "nmg_grhd_update_troubled: bad argument");
+  std::vector<double> ind(c->E);
+  int rc = nmg_grhd_trouble_indicators(c, ind.data());
+  if (rc) return rc;
+  std::vector<int32_t> fv = c->h_fv;
+  int to_fv = 0, to_dg = 0;
+  for (int64_t e = 0; e < c->E; e++) {
+    if (!fv[e] && ind[e] > persson_max) {
+      fv[e] = 1;
+      to_fv++;
+    } else if (fv[e] && ind[e] < persson_max - back_margin) {
+      fv[e] = 0;
+      to_dg++;
+    }
+  }
+  if (switched) {
+    switched[0] = to_fv;
+    switched[1] = to_dg;
+  }
+  return (to_fv || to_dg) ? nmg_grhd_set_fv_elements(c, fv.data()) : NMG_OK;
 }
 
 int nmg_grhd_get_fv_elements(nmg_grhd_ctx *c, int32_t *fv) {

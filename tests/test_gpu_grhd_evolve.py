@@ -146,3 +146,25 @@ def test_twenty_steps_with_a_switch_midway_match_oracle():
     ud, uf, pd, pf = o.rk4(ud, uf, pd, pf, dt, 10)
     got = ev.get_state()
     _compare(fv2, got[0], got[1], ud, uf, RTOL)
+
+
+def test_trouble_indicator_and_switching_by_it():
+    """Persson's indicator of D per element against the oracle's restatement
+    (nmo_persson on the LGL values; finite-volume elements projected back by
+    R x R x R first), then switching by the indicator with a margin."""
+    n, nf = 5, 10
+    o, ev, fv, (ud, uf, pd, pf) = _case(n, nf, 2, [3, 10, 33])
+    ind = ev.trouble_indicators()
+    _, R = o.transfer()
+    want = np.array([nmo.persson(n, o.apply3(R, uf[e])[0] if fv[e] else ud[e, 0])
+                     for e in range(48)])
+    assert np.abs(ind - want).max() <= 1e-9
+    thr = float(np.median(ind))
+    to_fv, to_dg = ev.update_troubled(thr, back_margin=0.5)
+    new = ev.fv_elements()
+    exp = fv.copy()
+    exp[(fv == 0) & (ind > thr)] = 1
+    exp[(fv == 1) & (ind < thr - 0.5)] = 0
+    assert np.array_equal(new, exp)
+    assert to_fv == int(((fv == 0) & (ind > thr)).sum())
+    assert to_dg == int(((fv == 1) & (ind < thr - 0.5)).sum())
