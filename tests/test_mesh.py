@@ -246,3 +246,29 @@ def test_level_jump_of_two_rejected():
     with pytest.raises(ng.NmgError, match="level jump"):
         ng.Mesh.build(ng.MESH_CUBEDSPHERES7, n=4, luni=1, cs_dc=1.0, cs_r0fac=20.0,
                       sphere_levels=2, sphere_radius=2)
+
+
+def test_patch_parts_cover_the_mesh():
+    """Meshes of patch subsets (patch_mask) hold exactly the elements of
+    those patches with the whole mesh's geometry; the faces between parts
+    become outer faces of each part."""
+    full = ng.Mesh.build(ng.MESH_CUBEDSPHERES7, n=4, luni=1, cs_dc=1.0, cs_r0fac=20.0)
+    a = ng.Mesh.build(ng.MESH_CUBEDSPHERES7, n=4, luni=1, cs_dc=1.0, cs_r0fac=20.0,
+                      patches=[0, 2, 4])
+    b = ng.Mesh.build(ng.MESH_CUBEDSPHERES7, n=4, luni=1, cs_dc=1.0, cs_r0fac=20.0,
+                      patches=[1, 3, 5, 6])
+    assert a.nelem + b.nelem == full.nelem
+    P, B = full.elements()
+    key = {(int(p),) + tuple(bb): i for i, (p, bb) in enumerate(zip(P, B))}
+    outer_full = (full.faces()[0] < 0).sum()
+    outer_parts = 0
+    for part, pats in ((a, {0, 2, 4}), (b, {1, 3, 5, 6})):
+        pp, bb = part.elements()
+        assert set(int(p) for p in pp) == pats
+        idx = np.array([key[(int(p),) + tuple(x)] for p, x in zip(pp, bb)])
+        assert np.array_equal(part.coords(), full.coords()[idx])
+        assert np.array_equal(part.dXdx(), full.dXdx()[idx])
+        outer_parts += (part.faces()[0] < 0).sum()
+    assert outer_parts > outer_full
+    with pytest.raises(ng.NmgError):
+        ng.Mesh.build(ng.MESH_BOX, n=4, luni=1, xc=(0.0,) * 3, box_dout=1.0, patches=[3])
