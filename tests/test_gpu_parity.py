@@ -253,3 +253,40 @@ def test_benchmark_workload_drift_over_100_steps():
     print(f"\nbenchmark workload at level 2, relative L2 GPU vs oracle after 1/10/100 steps: "
           f"{drift[1]:.3e} {drift[10]:.3e} {drift[100]:.3e}")
     assert max(drift.values()) <= RTOL_RK4
+
+
+def test_full_benchmark_workload_against_oracle_and_properties():
+    """The benchmark's workload at its full size (7 x 16^3 elements, n = 9,
+    104.5 M DOF, 8 seeded pulses, outgoing boundary, its dt): the RHS and
+    one RK4 step with the autotuned kernel against the oracle on the
+    oracle's own mesh (within 1e-12), two runs of a step bitwise equal, and
+    the linearity of the step, step(a u + b v) = a step(u) + b step(v)."""
+    n, L = 9, 4
+    m = ng.Mesh.build(ng.MESH_CUBEDSPHERES7, n=n, luni=L, cs_dc=1.0, cs_r0fac=20.0)
+    from oracle import nmo
+    pat, bbox, curvi, xyz, dXdx = nmo.generate_mesh(nmo.MESH_CUBEDSPHERES7, n, L)
+    assert np.array_equal(m.elements()[1], bbox)
+    o = nmo.OracleMesh(bbox, curvi, dXdx, xyz, nmo.match_faces_conforming(xyz, n), n, bc=1)
+    del dXdx
+    u = gaussian_pulses(xyz, seed=1234)
+    del xyz
+    dt = 0.25 * (2.0 / 2 ** L) / (n - 1) ** 2
+    ev = ng.Evolution(m, ng.BC_OUTGOING)
+    r = ev.rhs(u, 0.0)
+    assert rel_l2(r, o.rhs(u, 0.0)) <= RTOL_RHS
+    del r
+    ev.set_state(u)
+    ev.rk4_steps(0.0, dt, 1)
+    s1 = ev.get_state()
+    assert rel_l2(s1, o.rk4(u, dt, 1)) <= RTOL_RK4
+    ev.set_state(u)
+    ev.rk4_steps(0.0, dt, 1)
+    assert np.array_equal(ev.get_state(), s1)
+    v = np.random.default_rng(5).standard_normal(u.shape) * 1e-3
+    ev.set_state(v)
+    ev.rk4_steps(0.0, dt, 1)
+    sv = ev.get_state()
+    ev.set_state(2.0 * u - 3.0 * v)
+    ev.rk4_steps(0.0, dt, 1)
+    assert rel_l2(ev.get_state(), 2.0 * s1 - 3.0 * sv) <= 1e-13
+    ev.close()
