@@ -1,7 +1,8 @@
 """The GRHD Cowling evolution on the GPU (include/nmg.h nmg_grhd_*) against
 the oracle's restatement (oracle/nmo_grhd.c) on the same cubed shell:
 right-hand side and RK4 steps on mixed DG / finite-volume meshes (relative
-L2 <= 1e-12 per field group), the DG <-> finite-volume transfer, and the
+L2 <= 1e-12 over the DG and over the finite-volume states, 1e-11 per
+field), the DG <-> finite-volume transfer, and the
 known answers (a uniform state at rest keeps a zero DG right-hand side)."""
 import numpy as np
 import pytest
@@ -35,11 +36,20 @@ def _case(n, nf, ndiv, fv_elems, mass=1.0, rec="WENOm5_2", seed=3, vel=(0.0, 0.0
 
 
 def _compare(fv, got_dg, got_fv, want_dg, want_fv, tol):
+    """Relative L2 over all five fields of the DG elements and of the
+    finite-volume elements within tol (as the scalar-wave tests measure a
+    state), and per field within 10 tol: tau = psi^6 (rho h W^2 - p) - D
+    cancels most of its digits against D (tau / D ~ eps ~ 1e-4 in the blob),
+    so rounding differences of 1e-16 in the reconstructed primitives show
+    in tau's right-hand side at ~1e-12."""
     dg = fv == 0
+    assert rel_l2(got_dg[dg], want_dg[dg]) <= tol, "dg"
+    if fv.any():
+        assert rel_l2(got_fv, want_fv[fv == 1]) <= tol, "fv"
     for f in range(5):
-        assert rel_l2(got_dg[dg][:, f], want_dg[dg][:, f]) <= tol, ("dg", f)
+        assert rel_l2(got_dg[dg][:, f], want_dg[dg][:, f]) <= 10 * tol, ("dg", f)
         if fv.any():
-            assert rel_l2(got_fv[:, f], want_fv[fv == 1][:, f]) <= tol, ("fv", f)
+            assert rel_l2(got_fv[:, f], want_fv[fv == 1][:, f]) <= 10 * tol, ("fv", f)
 
 
 @pytest.mark.parametrize("n,nf,rec", [(5, 9, "WENOm5_2"), (5, 10, "WENOm3_2"), (7, 13, "WENOm5_2"),
@@ -168,3 +178,40 @@ def test_trouble_indicator_and_switching_by_it():
     assert np.array_equal(new, exp)
     assert to_fv == int(((fv == 0) & (ind > thr)).sum())
     assert to_dg == int(((fv == 1) & (ind < thr - 0.5)).sum())
+
+
+def test_full_grhd_workload_against_oracle():
+    """The benchmark's GRHD workload at its full size (6 x 12^3 elements at
+    n = 7, the seeded 10 % on 13^3 finite-volume points, blob at r = 8,
+    M = 1): the RHS and one RK4 step against the oracle from the same
+    conserved state."""
+    import bench
+    n, nf, nd = 7, 13, 12
+    E = 6 * nd ** 3
+    flags = np.zeros(E, np.int32)
+    flags[np.random.default_rng(34).choice(E, int(round(0.1 * E)), replace=False)] = 1
+    kw = dict(mass=1.0, gamma=2.0, rho_atm=bench.GRHD_RHO_ATM,
+              p_atm=bench.GRHD_K * bench.GRHD_RHO_ATM ** 2)
+    o = nmo.GrhdOracle(n=n, nf=nf, ndiv=nd, fv=flags, **kw)
+    pd = bench.grhd_initial_prim(o.xyz, seed=33)
+    ud = np.stack([o.prim2con(pd[e], o.psi(o.xyz[e])) for e in range(E)])
+    P, _ = o.transfer()
+    uf = np.zeros((E, 5, nf ** 3))
+    pf = np.zeros((E, 5, nf ** 3))
+    for e in np.nonzero(flags)[0]:
+        uf[e] = o.apply3(P, ud[e])
+        pf[e] = o.apply3(P, pd[e])
+    m = ng.Mesh.build(ng.MESH_CUBEDSHELL6, n=n, ndiv=nd, shell_rin=2.0, shell_rout=20.0)
+    ev = ng.GrhdEvolution(m, nf=nf, **kw)
+    ev.set_fv_elements(flags)
+    ev.set_state(ud, uf[flags == 1], pd, pf[flags == 1])
+    r_dg, r_fv = ev.rhs()
+    w_dg, w_fv = o.rhs(ud, uf, pd, pf)
+    _compare(flags, r_dg, r_fv, w_dg, w_fv, RTOL)
+    ev.set_state(ud, uf[flags == 1], pd, pf[flags == 1])
+    dt = 0.25 * (2.0 * (np.pi / 2.0) / nd) / (n - 1) ** 2
+    ev.rk4_steps(dt, 1)
+    got = ev.get_state()
+    want = o.rk4(ud, uf, pd, pf, dt, 1)
+    _compare(flags, got[0], got[1], want[0], want[1], RTOL)
+    ev.close()
