@@ -472,6 +472,41 @@ def _batch_compare(meshes, owner, states, K):
             "batch_info": info}
 
 
+def batch_cpu_baseline(specs, count=8):
+    """The oracle (OpenMP over the host cores) on a bounded sample of the
+    batched workload: the first `count` problems that are single-order and
+    without level jumps (meshes from the oracle's own generator), one RK4
+    step each, one after the other, as the reference runs one mesh per
+    process."""
+    from oracle import nmo
+    rng = np.random.default_rng(7)
+    dof, t, used = 0, 0.0, 0
+    for kind, L, orders, E, href in specs:
+        if len(orders) > 1 or href or used >= count:
+            continue
+        n = orders[0]
+        if kind == "box":
+            g = nmo.generate_mesh(nmo.MESH_BOX, n, L, xc=(PI, PI, PI), box_dout=PI)
+            period = 2 * PI
+        else:
+            g = nmo.generate_mesh(nmo.MESH_CUBEDSPHERES7, n, L)
+            period = None
+        pat, bbox, curvi, xyz, dXdx = g
+        om = nmo.OracleMesh(bbox, curvi, dXdx, xyz,
+                            nmo.match_faces_conforming(xyz, n, period=period), n, bc=1)
+        u = 1e-3 * rng.standard_normal((len(pat), NFIELDS, n ** 3))
+        om.rk4(u, 1e-4, 1)  # warm-up
+        t0 = time.perf_counter()
+        om.rk4(u, 1e-4, 1)
+        t += time.perf_counter() - t0
+        dof += len(pat) * NFIELDS * n ** 3
+        used += 1
+    threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count()))
+    return {"value": dof * 4 / t, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"one RK4 step of each of {used} single-order problems without level "
+                      f"jumps, one after the other ({dof} DOF), {t:.2f} s"}
+
+
 def batched_bench(args):
     """Batched execution of many independent problems against the same
     problems stepped one after the other; for all 64 problems, for the ones
@@ -503,6 +538,7 @@ def batched_bench(args):
                 "interpolated traces), per problem otherwise; problems with level jumps have "
                 "patches one level finer than their neighbours (non-conforming faces); all "
                 "problems share dt",
+        "cpu_baseline": None if args.no_cpu_baseline else batch_cpu_baseline(specs),
         "small_problems": dict(sub, selection="the problems of at most 4096 elements"),
         "tiny_problems": dict(tiny, selection="the problems of at most 512 elements")})
     return out
