@@ -420,21 +420,33 @@ int nmg_set_fv_midpoint_data(nmg_ctx *c, int32_t on);
  * switches it off.  Applied by the step entry points (nmg_rk4_step(s),
  * nmg_evolve_steps, the host round trips, nmg_rk4_step_trouble,
  * nmg_rk4_step_noalloc); not by the adjoint and the batches. */
-/* The reference's scalarwave1_limiter = MRS with limiter_alpha (limdata_MRS
- * / limiter_MRS, src/main/limiter/limiter.c:61-204, applied as
- * evolve_limiter_mesh does: to w before every later stage, RungeKutta.c:
- * 45-67,161,173, and to the new u after the step, evolve.c:143-144).  Per
+/* The reference's scalarwave1_limiter (src/tests/scalarwave1/scalarwave1.c:
+ * 687-697) with limiter_alpha, limiter_beta and limiter_scaleBound, applied
+ * as evolve_limiter_mesh does: to w before every later stage, RungeKutta.c:
+ * 45-67,161,173, and to the new u after the step, evolve.c:143-144.
+ *   MRS (limdata_MRS / limiter_MRS, src/main/limiter/limiter.c:61-204): per
  * element theta = min(1, min over fields of phi((M - wbar) / (wM - wbar)),
  * phi(y) = min(y/1.1, 1) (0 for y < 0), with M the neighbours' extrema
- * widened to wbar +- alpha h^1.5) and u <- wbar + theta (u - wbar).  kind:
- * NMG_LIMITER_NONE or NMG_LIMITER_MRS (minmodB is not built).  Applied by
- * nmg_rk4_step(s), nmg_evolve_steps, the host round trips and
- * nmg_rk4_step_noalloc; the trouble
- * flow and the adjoint reject a context with the limiter on (NMG_EUNSUP).
+ * widened to wbar +- alpha h^1.5) and u <- wbar + theta (u - wbar).
+ *   minmodB (limdata_c000_100_010_001 / limiter_minmodB, limiter.c:201-380):
+ * per element and field the normalised-Legendre coefficients c000, c100,
+ * c010, c001; the face averages w0[f] (mean c000 of the neighbours across
+ * face f, 0 on outer faces); slopes limited by minmod3B(c100, beta/sqrt3
+ * (c000 - w0[0]), beta/sqrt3 (w0[1] - c000), bound) (likewise in y, z) with
+ * bound = alpha h (times the mean |w0[f]| if scale_bound); a field whose
+ * slopes move by more than 1e-10 becomes c000 plus the limited linear modes.
+ * kind: NMG_LIMITER_NONE, NMG_LIMITER_MRS or NMG_LIMITER_MINMODB;
+ * nmg_set_limiter takes beta = 0.5 and scale_bound = 0 (the reference's
+ * defaults).  Applied by nmg_rk4_step(s), nmg_evolve_steps, the host round
+ * trips and nmg_rk4_step_noalloc; the trouble flow and the adjoint reject a
+ * context with the limiter on (NMG_EUNSUP).
  * nmg_get_limited: per element 1 if the last limiter call limited it. */
 #define NMG_LIMITER_NONE 0
 #define NMG_LIMITER_MRS 1
+#define NMG_LIMITER_MINMODB 2
 int nmg_set_limiter(nmg_ctx *c, int32_t kind, double alpha);
+int nmg_set_limiter_ex(nmg_ctx *c, int32_t kind, double alpha, double beta,
+                       int32_t scale_bound);
 int nmg_get_limited(nmg_ctx *c, int32_t *limited);
 
 int nmg_set_filter(nmg_ctx *c, int32_t on, double alp, double s, int32_t dn, int32_t jpower,

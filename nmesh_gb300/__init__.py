@@ -200,6 +200,7 @@ def lib(build_if_missing=True):
         "nmg_set_fv_midpoint_data": (ctypes.c_int, [vp, i32]),
         "nmg_set_filter": (ctypes.c_int, [vp, i32, f64, f64, i32, i32, i32]),
         "nmg_set_limiter": (ctypes.c_int, [vp, i32, f64]),
+        "nmg_set_limiter_ex": (ctypes.c_int, [vp, i32, f64, f64, i32]),
         "nmg_get_limited": (ctypes.c_int, [vp, vp]),
         "nmg_mesh_get_midpoint_dXdx": (ctypes.c_int, [vp, vp]),
         "nmg_mesh_auto_dt": (ctypes.c_int, [vp, f64, f64, vp]),
@@ -581,11 +582,13 @@ class Evolution:
         self._check(lib().nmg_set_filter(self._h, int(bool(on)), float(alp), float(s), int(dn),
                                          int(jpower), int(bool(filter_fv))), "nmg_set_filter")
 
-    def set_limiter(self, kind="MRS", alpha=5.0):
-        """The reference's scalarwave1_limiter ("none" or "MRS") with
-        limiter_alpha (default 5)."""
-        k = {"none": 0, "MRS": 1, "minmodB": 2}[kind]  # minmodB: rejected by the library
-        self._check(lib().nmg_set_limiter(self._h, k, float(alpha)), "nmg_set_limiter")
+    def set_limiter(self, kind="MRS", alpha=5.0, beta=0.5, scale_bound=False):
+        """The reference's scalarwave1_limiter ("none", "MRS" or "minmodB")
+        with limiter_alpha (default 5), limiter_beta (minmodB, default 0.5)
+        and limiter_scaleBound (minmodB, default no)."""
+        k = {"none": 0, "MRS": 1, "minmodB": 2}[kind]
+        self._check(lib().nmg_set_limiter_ex(self._h, k, float(alpha), float(beta),
+                                             int(bool(scale_bound))), "nmg_set_limiter_ex")
 
     def limited(self):
         """Per element 1 if the last limiter call limited it."""

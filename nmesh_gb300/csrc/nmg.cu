@@ -330,10 +330,16 @@ struct nmg_ctx {
   bool fv_mid = false;
   // exponential filter after each step (evolve_filter_all = yes)
   bool filter_on = false;
-  // MRS limiter (scalarwave1_limiter = MRS): node averages / extrema, the
-  // face neighbours of every element (CSR), alpha h^1.5 per element
+  // limiter (scalarwave1_limiter = MRS or minmodB): per element and field
+  // the MRS node average / extrema or the minmodB coefficients c000, c100,
+  // c010, c001 (d_lim, [E][NF][4]), the face neighbours of every element
+  // face (CSR [E*6+1]), alpha h^1.5 (MRS) or alpha h (minmodB) per element;
+  // d_mmb: [2 analysis rows; 2 synthesis columns][typ][n] for minmodB
   bool lim_on = false;
+  int lim_kind = NMG_LIMITER_NONE, lim_scale_bound = 0;
+  double lim_bos3 = 0.;
   double *d_lim = nullptr, *d_alpha_h = nullptr, *d_wl = nullptr, *d_wu = nullptr;
+  double *d_mmb = nullptr;
   int *d_lnboff = nullptr, *d_lnb = nullptr, *d_limited = nullptr;
   int filter_jpow = 1, filter_fv = 1;
   double *d_filt = nullptr;   // [2][nn] F of LGL and of equally spaced points
@@ -620,13 +626,19 @@ static cudaError_t apply_filter(nmg_ctx *c, double *buf) {
   return e;
 }
 
-// evolve_limiter_mesh with the MRS limiter on buf (all elements)
+// evolve_limiter_mesh with the MRS or minmodB limiter on buf (all elements)
 static cudaError_t apply_limiter(nmg_ctx *c, double *buf) {
   if (!c->lim_on) return cudaSuccess;
-  cudaError_t e = nmgk::limiter_launch(c->n, (int)c->nelem, buf, c->mixed ? c->d_isfv : nullptr,
-                                       (c->fv && !c->mixed) ? 1 : 0, c->d_wl, c->d_wu, c->d_lim,
-                                       c->d_lnboff, c->d_lnb, c->d_alpha_h, c->d_limited,
-                                       c->stream);
+  const unsigned char *isfv = c->mixed ? c->d_isfv : nullptr;
+  const int allfv = (c->fv && !c->mixed) ? 1 : 0, n = c->n;
+  cudaError_t e =
+      c->lim_kind == NMG_LIMITER_MINMODB
+          ? nmgk::mmb_limiter_launch(n, (int)c->nelem, buf, isfv, allfv, c->d_mmb,
+                                     c->d_mmb + 4 * n, c->d_lim, c->d_lnboff, c->d_lnb,
+                                     c->d_alpha_h, c->lim_bos3, c->lim_scale_bound,
+                                     c->d_limited, c->stream)
+          : nmgk::limiter_launch(n, (int)c->nelem, buf, isfv, allfv, c->d_wl, c->d_wu, c->d_lim,
+                                 c->d_lnboff, c->d_lnb, c->d_alpha_h, c->d_limited, c->stream);
   if (e == cudaSuccess) c->launches += 2;
   return e;
 }
@@ -1704,22 +1716,76 @@ int nmg_set_fv_surface_interp(nmg_ctx *c, int32_t mode) {
   return NMG_OK;
 }
 
+// S_ij = P_j(x_i) / sqrt(c_j), 1/c_j = (2j+1)/2 (j/2 for j = N), and the
+// analysis matrix A: w_j S_ji on LGL points (typ 0), S^-1 by Gauss-Jordan
+// elimination with partial pivoting on equally spaced points (typ 1)
+// (LGL_AT_ST_matrices, Legendre_AT_ST_matrices, src/main/basis/
+// Legendre.c:277-310,723-729); plain double arithmetic, as the oracle's
+static void legendre_sa(int n, int typ, const double *x, const double *w, double *S, double *A) {
+  const int nn = n * n;
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++) {
+      double ooc = 0.5 * (2 * j + 1);
+      if (j == n - 1 && n - 1 != 0) ooc = 0.5 * j;
+      S[i * n + j] = legendre_p(j, x[i]) * sqrt(ooc);
+    }
+  if (typ == 0) {
+    for (int i = 0; i < n; i++)
+      for (int j = 0; j < n; j++) A[i * n + j] = w[j] * S[j * n + i];
+    return;
+  }
+  std::vector<double> M(S, S + nn), I(nn, 0.);
+  for (int i = 0; i < n; i++) I[i * n + i] = 1.;
+  for (int col = 0; col < n; col++) {
+    int piv = col;
+    for (int r = col + 1; r < n; r++)
+      if (fabs(M[r * n + col]) > fabs(M[piv * n + col])) piv = r;
+    for (int q = 0; q < n; q++) {
+      std::swap(M[col * n + q], M[piv * n + q]);
+      std::swap(I[col * n + q], I[piv * n + q]);
+    }
+    const double d = M[col * n + col];
+    for (int q = 0; q < n; q++) {
+      M[col * n + q] /= d;
+      I[col * n + q] /= d;
+    }
+    for (int r = 0; r < n; r++)
+      if (r != col) {
+        const double fac = M[r * n + col];
+        for (int q = 0; q < n; q++) {
+          M[r * n + q] -= fac * M[col * n + q];
+          I[r * n + q] -= fac * I[col * n + q];
+        }
+      }
+  }
+  std::copy(I.begin(), I.end(), A);
+}
+
 int nmg_set_limiter(nmg_ctx *c, int32_t kind, double alpha) {
+  return nmg_set_limiter_ex(c, kind, alpha, 0.5, 0);
+}
+
+int nmg_set_limiter_ex(nmg_ctx *c, int32_t kind, double alpha, double beta, int32_t scale_bound) {
   if (!c) return NMG_EINVAL;
-  if (kind != NMG_LIMITER_NONE && kind != NMG_LIMITER_MRS)
-    return set_err(c, NMG_EUNSUP, "nmg_set_limiter: only none and MRS are built");
-  if (kind == NMG_LIMITER_MRS && !(alpha >= 0.))
+  if (kind != NMG_LIMITER_NONE && kind != NMG_LIMITER_MRS && kind != NMG_LIMITER_MINMODB)
+    return set_err(c, NMG_EUNSUP, "nmg_set_limiter: kind must be none, MRS or minmodB");
+  if (kind != NMG_LIMITER_NONE && !(alpha >= 0.))
     return set_err(c, NMG_EINVAL, "nmg_set_limiter: alpha must be >= 0");
+  if (kind == NMG_LIMITER_MINMODB && !(beta >= 0.))
+    return set_err(c, NMG_EINVAL, "nmg_set_limiter: beta must be >= 0");
+  if (scale_bound != 0 && scale_bound != 1)
+    return set_err(c, NMG_EINVAL, "nmg_set_limiter: scale_bound must be 0 or 1");
   drop_graphs(c);
   if (kind == NMG_LIMITER_NONE) {
     c->lim_on = false;
+    c->lim_kind = NMG_LIMITER_NONE;
     return NMG_OK;
   }
   const int n = c->n;
   const int64_t E = c->nelem;
   if (!c->d_lnboff) {
-    // face neighbours (nfnb / nbindc): the neighbour element of a
-    // conforming face, every source element of a non-conforming one
+    // face neighbours (nfnb / fnb): the neighbour element of a conforming
+    // face, every distinct source element of a non-conforming one
     std::vector<std::vector<int>> extra(E * 6);
     const int nn = n * n;
     for (int64_t h = 0; h < c->nhang; h++) {
@@ -1731,18 +1797,26 @@ int nmg_set_limiter(nmg_ctx *c, int32_t kind, double alpha) {
       }
     }
     std::vector<int> off(1, 0), nbl;
-    for (int64_t e = 0; e < E; e++) {
-      for (int f = 0; f < 6; f++) {
-        const int64_t q = e * 6 + f;
-        if (!extra[q].empty()) nbl.insert(nbl.end(), extra[q].begin(), extra[q].end());
-        else if (c->h_nb[q] >= 0) nbl.push_back(c->h_nb[q]);
-      }
+    for (int64_t q = 0; q < E * 6; q++) {
+      if (!extra[q].empty()) nbl.insert(nbl.end(), extra[q].begin(), extra[q].end());
+      else if (c->h_nb[q] >= 0) nbl.push_back(c->h_nb[q]);
       off.push_back((int)nbl.size());
     }
     if (nbl.empty()) nbl.push_back(0);
-    std::vector<double> x(n), wl(n), wu(n), D((size_t)n * n);
+    std::vector<double> x(n), wl(n), wu(n), xu(n), D((size_t)n * n);
     nmg::lgl_basis(n, x.data(), wl.data(), D.data());
-    nmg::uniform_basis(n, x.data(), wu.data(), D.data());
+    nmg::uniform_basis(n, xu.data(), wu.data(), D.data());
+    // minmodB tables: analysis rows 0, 1 and synthesis columns 0, 1
+    std::vector<double> mmb(8 * (size_t)n), S((size_t)n * n), A((size_t)n * n);
+    for (int typ = 0; typ < 2; typ++) {
+      legendre_sa(n, typ, typ ? xu.data() : x.data(), wl.data(), S.data(), A.data());
+      for (int i = 0; i < n; i++) {
+        mmb[(typ * 2 + 0) * n + i] = A[i];
+        mmb[(typ * 2 + 1) * n + i] = A[n + i];
+        mmb[4 * n + (typ * 2 + 0) * n + i] = S[i * n];
+        mmb[4 * n + (typ * 2 + 1) * n + i] = S[i * n + 1];
+      }
+    }
     auto up = [&](auto **dst, const auto &vec) -> cudaError_t {
       const size_t bytes = vec.size() * sizeof(vec[0]);
       cudaError_t e2 = cudaMalloc((void **)dst, std::max<size_t>(bytes, 16));
@@ -1752,19 +1826,24 @@ int nmg_set_limiter(nmg_ctx *c, int32_t kind, double alpha) {
     CK(up(&c->d_lnb, nbl));
     CK(up(&c->d_wl, wl));
     CK(up(&c->d_wu, wu));
-    CK(cudaMalloc((void **)&c->d_lim, sizeof(double) * E * NF * 3));
+    CK(up(&c->d_mmb, mmb));
+    CK(cudaMalloc((void **)&c->d_lim, sizeof(double) * E * NF * 4));
     CK(cudaMalloc((void **)&c->d_alpha_h, sizeof(double) * E));
     CK(cudaMalloc((void **)&c->d_limited, sizeof(int) * E));
     CK(up(&c->d_lnboff, off));  // last: marks the tables complete
   }
-  // alpha_h = alpha h^1.5, h the largest bbox extent (limiter.c:121-124)
+  // MRS: alpha h^1.5 (limiter.c:121-124); minmodB: alpha h
+  // (limiter.c:292-302); h the largest bbox extent
   std::vector<double> ah(E);
   for (int64_t e = 0; e < E; e++) {
     const double *bb = &c->geom.bbox[e * 6];
     const double h = std::max(bb[1] - bb[0], std::max(bb[3] - bb[2], bb[5] - bb[4]));
-    ah[e] = alpha * pow(h, 1.5);
+    ah[e] = kind == NMG_LIMITER_MRS ? alpha * pow(h, 1.5) : alpha * h;
   }
   CK(cudaMemcpy(c->d_alpha_h, ah.data(), sizeof(double) * E, cudaMemcpyHostToDevice));
+  c->lim_kind = kind;
+  c->lim_bos3 = beta / sqrt(3.);
+  c->lim_scale_bound = scale_bound;
   c->lim_on = true;
   return NMG_OK;
 }
@@ -1951,7 +2030,7 @@ void nmg_destroy(nmg_ctx *c) {
   cudaFree(c->d_toff); cudaFree(c->d_tsrc); cudaFree(c->d_tw); cudaFree(c->d_hface); cudaFree(c->d_fvmid);
   cudaFree(c->d_filt); cudaFree(c->d_fooj);
   cudaFree(c->d_lim); cudaFree(c->d_alpha_h); cudaFree(c->d_wl); cudaFree(c->d_wu);
-  cudaFree(c->d_lnboff); cudaFree(c->d_lnb); cudaFree(c->d_limited);
+  cudaFree(c->d_lnboff); cudaFree(c->d_lnb); cudaFree(c->d_limited); cudaFree(c->d_mmb);
   cudaFree(c->d_gM); cudaFree(c->d_fvbxyz); cudaFree(c->d_fvbnrm); cudaFree(c->d_PR);
   cudaFree(c->d_conv); cudaFree(c->d_mm); cudaFree(c->d_trb); cudaFree(c->d_score);
   cudaFree(c->d_r); cudaFree(c->d_w2); cudaFree(c->d_ghost2); cudaFree(c->d_tlist);

@@ -389,10 +389,19 @@ cudaError_t filter_launch(int n, int nelem, double *u, const unsigned char *isfv
                           const double *scale, int jpow, int filter_fv, int allfv,
                           cudaStream_t st);
 // MRS limiter of every element of u: node averages and extrema (lim,
-// [e][field][3]), then u <- ubar + theta (u - ubar); limited[e] = theta < 1
+// [e][field][3]; nboff: CSR over nbl per element face, [E*6+1]), then
+// u <- ubar + theta (u - ubar); limited[e] = theta < 1
 cudaError_t limiter_launch(int n, int nelem, double *u, const unsigned char *isfv, int allfv,
                            const double *wl, const double *wu, double *lim, const int *nboff,
                            const int *nbl, const double *alpha_h, int *limited, cudaStream_t st);
+// minmodB limiter of every element of u (n in [2, 16]): coefficients c000,
+// c100, c010, c001 (lim, [e][field][4]), then per field the bounded minmod
+// of the linear modes against the face neighbours' averages (foff: CSR over
+// nbl per element face, [E*6+1]); limited[e]: some field limited
+cudaError_t mmb_limiter_launch(int n, int nelem, double *u, const unsigned char *isfv, int allfv,
+                               const double *ana, const double *syn, double *lim,
+                               const int *foff, const int *nbl, const double *mt_h, double bos3,
+                               int scale_bound, int *limited, cudaStream_t st);
 // traces of non-conforming faces: per slot, field and face node the average
 // over its contributions of the source face interpolated at the node
 cudaError_t hang_launch(int nhang, int n, const int *hoff, const int *hsrc, const double *hw,

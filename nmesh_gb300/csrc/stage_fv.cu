@@ -833,7 +833,7 @@ __global__ void __launch_bounds__(256) limiter_kernel(int n, double *u, const do
       const double *L = lim + ((size_t)e * NF + l) * 3;
       const double wbar = L[0], wmi = L[1], wMi = L[2];
       double Mi = -DBL_MAX, mi = DBL_MAX;
-      for (int k = __ldg(nboff + e); k < __ldg(nboff + e + 1); k++) {
+      for (int k = __ldg(nboff + 6 * e); k < __ldg(nboff + 6 * e + 6); k++) {
         const double *N = lim + ((size_t)__ldg(nbl + k) * NF + l) * 3;
         if (N[1] < mi) mi = N[1];
         if (N[2] > Mi) Mi = N[2];
@@ -856,6 +856,160 @@ __global__ void __launch_bounds__(256) limiter_kernel(int n, double *u, const do
     double *v = u + (size_t)e * NF * np + q;
     *v = qbar + th * (*v - qbar);
   }
+}
+
+// minmodB limiter (limdata_c000_100_010_001 / limiter_minmodB, src/main/
+// limiter/limiter.c:201-380).  Products and sums are rounded one by one
+// (no contraction into FMAs) in the oracle's order, so that the limiter's
+// decisions and outputs are reproducible from the same input bit for bit.
+//
+// Data: the coefficients c000, c100, c010, c001 of every element's
+// normalised-Legendre expansion, analysis along x, then y, then z
+// (basis_array_analysis3, src/main/basis/basis.c:183-188).  ana = [typ][2][n]
+// rows 0 and 1 of the analysis matrix, typ 0 LGL and 1 equally spaced.
+__global__ void __launch_bounds__(256) mmb_limdata_kernel(int n, const double *u,
+                                                         const unsigned char *isfv, int allfv,
+                                                         const double *ana, double *lim) {
+  __shared__ double t0[256], t1[256], s3[3][16];
+  const int np = n * n * n, nn = n * n, e = blockIdx.x;
+  const bool efv = allfv || (isfv && isfv[e]);
+  const double *A0 = ana + (efv ? 2 * n : 0), *A1 = A0 + n;
+  for (int l = 0; l < NF; l++) {
+    const double *v = u + ((size_t)e * NF + l) * np;
+    for (int q = threadIdx.x; q < nn; q += blockDim.x) {  // q = j + n k
+      double a0 = 0., a1 = 0.;
+      for (int i = 0; i < n; i++) {
+        const double x = v[i + n * q];
+        a0 = __dadd_rn(a0, __dmul_rn(__ldg(A0 + i), x));
+        a1 = __dadd_rn(a1, __dmul_rn(__ldg(A1 + i), x));
+      }
+      t0[q] = a0;
+      t1[q] = a1;
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+      double s00 = 0., s10 = 0., s01 = 0.;
+      for (int j = 0; j < n; j++) {
+        s00 = __dadd_rn(s00, __dmul_rn(__ldg(A0 + j), t0[j + n * k]));
+        s10 = __dadd_rn(s10, __dmul_rn(__ldg(A0 + j), t1[j + n * k]));
+        s01 = __dadd_rn(s01, __dmul_rn(__ldg(A1 + j), t0[j + n * k]));
+      }
+      s3[0][k] = s00;
+      s3[1][k] = s10;
+      s3[2][k] = s01;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double c000 = 0., c100 = 0., c010 = 0., c001 = 0.;
+      for (int k = 0; k < n; k++) {
+        c000 = __dadd_rn(c000, __dmul_rn(__ldg(A0 + k), s3[0][k]));
+        c100 = __dadd_rn(c100, __dmul_rn(__ldg(A0 + k), s3[1][k]));
+        c010 = __dadd_rn(c010, __dmul_rn(__ldg(A0 + k), s3[2][k]));
+        c001 = __dadd_rn(c001, __dmul_rn(__ldg(A1 + k), s3[0][k]));
+      }
+      double *L = lim + ((size_t)e * NF + l) * 4;
+      L[0] = c000;
+      L[1] = c100;
+      L[2] = c010;
+      L[3] = c001;
+    }
+    __syncthreads();
+  }
+}
+
+__device__ __forceinline__ double mmb_minmod3(double a, double b, double c) {
+  if (__dmul_rn(a, b) >= 0. && __dmul_rn(b, c) >= 0.)
+    return (a > 0. ? 1. : -1.) * fmin(fabs(a), fmin(fabs(b), fabs(c)));
+  return 0.;
+}
+
+__device__ __forceinline__ double mmb_minmod3b(double a, double b, double c, double bound) {
+  return fabs(a) <= bound ? a : mmb_minmod3(a, b, c);
+}
+
+// dequal: equal within the absolute tolerance 1e-10
+// (src/main/main/nmesh_main.h:32-34)
+__device__ __forceinline__ bool mmb_dequal(double a, double b) {
+  return !(a < __dadd_rn(b, -1e-10) || b < __dadd_rn(a, -1e-10));
+}
+
+// per element and field: face averages w0[f] (mean of the neighbours' c000
+// across face f, foff = [E*6+1] CSR over nbl; 0 on outer faces), bound
+// mt_h (= alpha h) times the mean |w0[f]| if scale_bound, slopes limited by
+// minmod3B against bos3 (= beta/sqrt3) times the jumps of the averages;
+// where a slope moves by more than 1e-10 the field becomes c000 plus the
+// three limited linear modes (synthesis along x, y, z; syn = [typ][2][n]
+// columns 0 and 1 of the synthesis matrix).  limited[e]: any field limited.
+__global__ void __launch_bounds__(256) mmb_limiter_kernel(
+    int n, double *u, const unsigned char *isfv, int allfv, const double *syn, const double *lim,
+    const int *foff, const int *nbl, const double *mt_h, double bos3, int scale_bound,
+    int *limited) {
+  __shared__ double coef[NF][4];
+  __shared__ int flag[NF];
+  const int np = n * n * n, e = blockIdx.x;
+  const int l = threadIdx.x;
+  if (l < NF) {
+    double w0[6], w0L1 = 0.;
+    for (int f = 0; f < 6; f++) {
+      const int b = __ldg(foff + 6 * e + f), z = __ldg(foff + 6 * e + f + 1);
+      double av = 0.;
+      for (int k = b; k < z; k++)
+        av = __dadd_rn(av, lim[((size_t)__ldg(nbl + k) * NF + l) * 4]);
+      if (z > b) av = __ddiv_rn(av, (double)(z - b));
+      w0[f] = av;
+      w0L1 = __dadd_rn(w0L1, __dmul_rn(fabs(av), 0.166666666666667));
+    }
+    const double *L = lim + ((size_t)e * NF + l) * 4;
+    const double w0c = L[0];
+    const double mh = __ldg(mt_h + e);
+    const double bound = scale_bound ? __dmul_rn(mh, w0L1) : mh;
+    double wl[3];
+    bool lim_any = false;
+    for (int d = 0; d < 3; d++) {
+      const double lo = __dmul_rn(bos3, __dadd_rn(w0c, -w0[2 * d]));
+      const double hi = __dmul_rn(bos3, __dadd_rn(w0[2 * d + 1], -w0c));
+      wl[d] = mmb_minmod3b(L[1 + d], lo, hi, bound);
+      lim_any |= !mmb_dequal(wl[d], L[1 + d]);
+    }
+    coef[l][0] = w0c;
+    coef[l][1] = wl[0];
+    coef[l][2] = wl[1];
+    coef[l][3] = wl[2];
+    flag[l] = lim_any ? 1 : 0;
+  }
+  __syncthreads();
+  int any = 0;
+  for (int k = 0; k < NF; k++) any |= flag[k];
+  if (threadIdx.x == 0) limited[e] = any;
+  if (!any) return;
+  const bool efv = allfv || (isfv && isfv[e]);
+  const double *S0 = syn + (efv ? 2 * n : 0), *S1 = S0 + n;
+  for (int q = threadIdx.x; q < NF * np; q += blockDim.x) {
+    const int f = q / np, p = q - f * np;
+    if (!flag[f]) continue;
+    const int i = p % n, j = (p / n) % n, k = p / (n * n);
+    const double c0 = coef[f][0], cx = coef[f][1], cy = coef[f][2], cz = coef[f][3];
+    const double tx0 = __dadd_rn(__dmul_rn(__ldg(S0 + i), c0), __dmul_rn(__ldg(S1 + i), cx));
+    const double tx1 = __dmul_rn(__ldg(S0 + i), cy), tx2 = __dmul_rn(__ldg(S0 + i), cz);
+    const double ty0 = __dadd_rn(__dmul_rn(__ldg(S0 + j), tx0), __dmul_rn(__ldg(S1 + j), tx1));
+    const double ty1 = __dmul_rn(__ldg(S0 + j), tx2);
+    u[(size_t)e * NF * np + q] =
+        __dadd_rn(__dmul_rn(__ldg(S0 + k), ty0), __dmul_rn(__ldg(S1 + k), ty1));
+  }
+}
+
+cudaError_t mmb_limiter_launch(int n, int nelem, double *u, const unsigned char *isfv, int allfv,
+                               const double *ana, const double *syn, double *lim,
+                               const int *foff, const int *nbl, const double *mt_h, double bos3,
+                               int scale_bound, int *limited, cudaStream_t st) {
+  if (nelem <= 0) return cudaSuccess;
+  if (n < 2 || n > 16) return cudaErrorInvalidValue;
+  mmb_limdata_kernel<<<nelem, 256, 0, st>>>(n, u, isfv, allfv, ana, lim);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  mmb_limiter_kernel<<<nelem, 256, 0, st>>>(n, u, isfv, allfv, syn, lim, foff, nbl, mt_h, bos3,
+                                            scale_bound, limited);
+  return cudaGetLastError();
 }
 
 size_t filter_smem(int n) { return sizeof(double) * (3 * (size_t)n * n * n + (size_t)n * n); }

@@ -1397,57 +1397,67 @@ int nmo_limiter_mrs(const nmo_mesh *m, double *u, double alpha, int32_t *limited
   return 0;
 }
 
+/* S_ij = P_j(x_i) / sqrt(c_j), 1/c_j = (2j+1)/2 (j/2 for j = N), and the
+   analysis matrix A of the LGL points (typ 0: A_ij = w_j S_ji) or of the
+   equally spaced points (typ 1: A = S^-1 by Gauss-Jordan elimination with
+   partial pivoting) (LGL_AT_ST_matrices, Legendre_AT_ST_matrices,
+   src/main/basis/Legendre.c:277-310,723-729) */
+static void legendre_as(int n, int typ, double *S, double *A)
+{
+  int nn = n * n, i, j, q;
+  double x[64], w[64];
+  if (typ == 0) nmo_lgl(n, x, w);
+  else nmo_uniform(n, x);
+  for (i = 0; i < n; i++)
+    for (j = 0; j < n; j++) {
+      double ooc = 0.5 * (2 * j + 1);
+      if (j == n - 1 && n - 1 != 0) ooc = 0.5 * j;
+      S[i * n + j] = legendre_p(j, x[i]) * sqrt(ooc);
+    }
+  if (typ == 0) {
+    for (i = 0; i < n; i++)
+      for (j = 0; j < n; j++) A[i * n + j] = w[j] * S[j * n + i];
+  } else {
+    double M[4096], I[4096];
+    int col, r;
+    for (q = 0; q < nn; q++) { M[q] = S[q]; I[q] = 0.; }
+    for (i = 0; i < n; i++) I[i * n + i] = 1.;
+    for (col = 0; col < n; col++) {
+      int piv = col;
+      double dd;
+      for (r = col + 1; r < n; r++)
+        if (fabs(M[r * n + col]) > fabs(M[piv * n + col])) piv = r;
+      for (q = 0; q < n; q++) {
+        double t1 = M[col * n + q], t2 = I[col * n + q];
+        M[col * n + q] = M[piv * n + q]; M[piv * n + q] = t1;
+        I[col * n + q] = I[piv * n + q]; I[piv * n + q] = t2;
+      }
+      dd = M[col * n + col];
+      for (q = 0; q < n; q++) { M[col * n + q] /= dd; I[col * n + q] /= dd; }
+      for (r = 0; r < n; r++)
+        if (r != col) {
+          double fac = M[r * n + col];
+          for (q = 0; q < n; q++) {
+            M[r * n + q] -= fac * M[col * n + q];
+            I[r * n + q] -= fac * I[col * n + q];
+          }
+        }
+    }
+    for (q = 0; q < nn; q++) A[q] = I[q];
+  }
+}
+
 int nmo_filter(const nmo_mesh *m, double *u, double alp, double s, int dn, int jpow,
                int filter_fv)
 {
-  int n = m->n, np = n * n * n, nn = n * n, e, l, i, j, k, q, typ;
-  double S[2][4096], A[2][4096], f[64], Nf = n - 1 - dn, x[64], w[64];
+  int n = m->n, np = n * n * n, e, l, i, j, k, q, typ;
+  double S[2][4096], A[2][4096], f[64], Nf = n - 1 - dn;
   double *a = (double *)malloc(sizeof(double) * np), *b = (double *)malloc(sizeof(double) * np);
   double *ooJ = (double *)malloc(sizeof(double) * np);
   if (!a || !b || !ooJ) return 2;
   if (Nf <= 0.) Nf = 1.;
   for (k = 0; k < n; k++) f[k] = exp(-alp * pow(k / Nf, s));
-  for (typ = 0; typ < 2; typ++) {
-    if (typ == 0) nmo_lgl(n, x, w);
-    else nmo_uniform(n, x);
-    for (i = 0; i < n; i++)
-      for (j = 0; j < n; j++) {
-        double ooc = 0.5 * (2 * j + 1);
-        if (j == n - 1 && n - 1 != 0) ooc = 0.5 * j;
-        S[typ][i * n + j] = legendre_p(j, x[i]) * sqrt(ooc);
-      }
-    if (typ == 0) {
-      for (i = 0; i < n; i++)
-        for (j = 0; j < n; j++) A[0][i * n + j] = w[j] * S[0][j * n + i];
-    } else {   /* Gauss-Jordan inverse with partial pivoting */
-      double M[4096], I[4096];
-      int col, r;
-      for (q = 0; q < nn; q++) { M[q] = S[1][q]; I[q] = 0.; }
-      for (i = 0; i < n; i++) I[i * n + i] = 1.;
-      for (col = 0; col < n; col++) {
-        int piv = col;
-        double dd;
-        for (r = col + 1; r < n; r++)
-          if (fabs(M[r * n + col]) > fabs(M[piv * n + col])) piv = r;
-        for (q = 0; q < n; q++) {
-          double t1 = M[col * n + q], t2 = I[col * n + q];
-          M[col * n + q] = M[piv * n + q]; M[piv * n + q] = t1;
-          I[col * n + q] = I[piv * n + q]; I[piv * n + q] = t2;
-        }
-        dd = M[col * n + col];
-        for (q = 0; q < n; q++) { M[col * n + q] /= dd; I[col * n + q] /= dd; }
-        for (r = 0; r < n; r++)
-          if (r != col) {
-            double fac = M[r * n + col];
-            for (q = 0; q < n; q++) {
-              M[r * n + q] -= fac * M[col * n + q];
-              I[r * n + q] -= fac * I[col * n + q];
-            }
-          }
-      }
-      for (q = 0; q < nn; q++) A[1][q] = I[q];
-    }
-  }
+  for (typ = 0; typ < 2; typ++) legendre_as(n, typ, S[typ], A[typ]);
   for (e = 0; e < m->nelem; e++) {
     int efv = m->fv && m->fv[e];
     if (efv && !filter_fv) continue;
@@ -1468,6 +1478,147 @@ int nmo_filter(const nmo_mesh *m, double *u, double alp, double s, int dn, int j
     }
   }
   free(a); free(b); free(ooJ);
+  return 0;
+}
+
+/* The face neighbours of face f of element e (nfnb / fnb): the element
+   across a conforming face, every distinct source element of a
+   non-conforming one, none on an outer face; returns their number */
+static int face_neighbours(const nmo_mesh *m, int e, int f, int *nbs)
+{
+  int n = m->n, nn = n * n, np = nn * n, cnt = 0, q, c, z;
+  int64_t nb = m->nbnode[((size_t)e * 6 + f) * nn];
+  if (nb >= 0) nbs[cnt++] = (int)(nb / np);
+  else if (nb == -2) nbs[cnt++] = m->mixface[((size_t)e * 6 + f) * 3];
+  else if (nb == -3)
+    for (q = 0; q < nn; q++) {
+      size_t qq = ((size_t)e * 6 + f) * nn + q;
+      for (c = m->hang_off[qq]; c < m->hang_off[qq + 1]; c++) {
+        int e2 = m->hang_src[2 * c], seen = 0;
+        for (z = 0; z < cnt; z++) seen |= nbs[z] == e2;
+        if (!seen) nbs[cnt++] = e2;
+      }
+    }
+  return cnt;
+}
+
+static double minmod3(double a, double b, double c)
+{
+  if (a * b >= 0 && b * c >= 0) {
+    double m3 = fabs(a);
+    if (fabs(b) < m3) m3 = fabs(b);
+    if (fabs(c) < m3) m3 = fabs(c);
+    return (a > 0. ? 1. : -1.) * m3;
+  }
+  return 0.;
+}
+
+static double minmod3b(double a, double b, double c, double bound)
+{
+  return fabs(a) <= bound ? a : minmod3(a, b, c);
+}
+
+/* dequal with the reference's absolute tolerance 1e-10
+   (src/main/main/nmesh_main.h:32-34) */
+static int dequal10(double a, double b) { return !(a < b - 1e-10 || b < a - 1e-10); }
+
+/* The minmodB limiter of every element (limdata_c000_100_010_001 and
+   limiter_minmodB, src/main/limiter/limiter.c:201-380): the coefficients
+   c000, c100, c010, c001 of every element's normalised-Legendre expansion
+   (analysis along x, then y, then z: basis_array_analysis3,
+   src/main/basis/basis.c:183-188) first; then per element and field the
+   face averages w0[f] (mean of the neighbours' c000 across face f, 0 on an
+   outer face), the bound alpha h (times the mean of |w0[f]| if
+   scale_bound), and the slopes limited by minmod3B against beta/sqrt3 times
+   the jumps of the averages; where a slope changes by more than 1e-10 the
+   field becomes c000 + the three limited linear modes (synthesis along x,
+   y, z).  limited (may be NULL): 1 where any field was limited. */
+int nmo_limiter_minmodb(const nmo_mesh *m, double *u, double alpha, double beta,
+                        int scale_bound, int32_t *limited)
+{
+  int n = m->n, np = n * n * n, nn = n * n, e, l, i, j, k, f, typ;
+  double S[2][4096], A[2][4096];
+  const double bos3 = beta / sqrt(3.);
+  double *lim = (double *)malloc(sizeof(double) * (size_t)m->nelem * NF * 4);
+  double *t0 = (double *)malloc(sizeof(double) * 2 * nn), *t1 = t0 + nn;
+  int *nbs = (int *)malloc(sizeof(int) * 4 * nn);
+  if (!lim || !t0 || !nbs) return 2;
+  if (n < 2) return 3;
+  for (typ = 0; typ < 2; typ++) legendre_as(n, typ, S[typ], A[typ]);
+  for (e = 0; e < m->nelem; e++) {
+    const double *Ae = A[(m->fv && m->fv[e]) ? 1 : 0];
+    const double *A0 = Ae, *A1 = Ae + n;   /* rows 0 and 1 */
+    for (l = 0; l < NF; l++) {
+      const double *v = u + ((size_t)e * NF + l) * np;
+      double *L = lim + ((size_t)e * NF + l) * 4, c000 = 0., c100 = 0., c010 = 0., c001 = 0.;
+      for (k = 0; k < n; k++)
+        for (j = 0; j < n; j++) {
+          double a0 = 0., a1 = 0.;
+          for (i = 0; i < n; i++) {
+            a0 += A0[i] * v[i + n * (j + n * k)];
+            a1 += A1[i] * v[i + n * (j + n * k)];
+          }
+          t0[j + n * k] = a0;
+          t1[j + n * k] = a1;
+        }
+      for (k = 0; k < n; k++) {
+        double s00 = 0., s10 = 0., s01 = 0.;
+        for (j = 0; j < n; j++) {
+          s00 += A0[j] * t0[j + n * k];
+          s10 += A0[j] * t1[j + n * k];
+          s01 += A1[j] * t0[j + n * k];
+        }
+        c000 += A0[k] * s00;
+        c100 += A0[k] * s10;
+        c010 += A0[k] * s01;
+        c001 += A1[k] * s00;
+      }
+      L[0] = c000; L[1] = c100; L[2] = c010; L[3] = c001;
+    }
+  }
+  for (e = 0; e < m->nelem; e++) {
+    const double *bb = m->bbox + (size_t)e * 6, *Se = S[(m->fv && m->fv[e]) ? 1 : 0];
+    double h = bb[1] - bb[0], Mt_h, w0[6][NF], w0L1[NF];
+    int nlim = 0;
+    if (bb[3] - bb[2] > h) h = bb[3] - bb[2];
+    if (bb[5] - bb[4] > h) h = bb[5] - bb[4];
+    Mt_h = alpha * h;
+    for (l = 0; l < NF; l++) w0L1[l] = 0.;
+    for (f = 0; f < 6; f++) {
+      int cnt = face_neighbours(m, e, f, nbs), z;
+      for (l = 0; l < NF; l++) {
+        double av = 0.;
+        for (z = 0; z < cnt; z++) av += lim[((size_t)nbs[z] * NF + l) * 4];
+        if (cnt > 0) av = av / cnt;
+        w0[f][l] = av;
+        w0L1[l] += fabs(av) * 0.166666666666667;
+      }
+    }
+    for (l = 0; l < NF; l++) {
+      const double *L = lim + ((size_t)e * NF + l) * 4;
+      double w0c = L[0], bound = scale_bound ? Mt_h * w0L1[l] : Mt_h;
+      double wl100 = minmod3b(L[1], bos3 * (w0c - w0[0][l]), bos3 * (w0[1][l] - w0c), bound);
+      double wl010 = minmod3b(L[2], bos3 * (w0c - w0[2][l]), bos3 * (w0[3][l] - w0c), bound);
+      double wl001 = minmod3b(L[3], bos3 * (w0c - w0[4][l]), bos3 * (w0[5][l] - w0c), bound);
+      if (!dequal10(wl100, L[1]) || !dequal10(wl010, L[2]) || !dequal10(wl001, L[3])) {
+        double *v = u + ((size_t)e * NF + l) * np;
+        for (k = 0; k < n; k++)
+          for (j = 0; j < n; j++)
+            for (i = 0; i < n; i++) {
+              /* S^3 of the four non-zero coefficients, x, then y, then z */
+              double tx0 = Se[i * n] * w0c + Se[i * n + 1] * wl100;
+              double tx1 = Se[i * n] * wl010, tx2 = Se[i * n] * wl001;
+              double ty0 = Se[j * n] * tx0 + Se[j * n + 1] * tx1, ty1 = Se[j * n] * tx2;
+              v[i + n * (j + n * k)] = Se[k * n] * ty0 + Se[k * n + 1] * ty1;
+            }
+        nlim++;
+      }
+    }
+    if (limited) limited[e] = nlim > 0;
+  }
+  free(lim);
+  free(t0);
+  free(nbs);
   return 0;
 }
 

@@ -498,10 +498,33 @@ class OracleMesh:
             raise RuntimeError(f"nmo_limiter_mrs failed ({rc})")
         return u, flags
 
-    def rk4_limited(self, u, dt, nsteps, alpha=5.0, t=0.0):
-        """RK4 steps as nmo_rk4 takes them, with the MRS limiter on w before
-        every later stage and on the new u (evolve_RK4_mesh with
-        scalarwave1_limiter = MRS, src/main/evolve/RungeKutta.c:19-82)."""
+    def limit_minmodb(self, u, alpha=5.0, beta=0.5, scale_bound=False):
+        """The reference's minmodB limiter of every element (limiter_minmodB
+        with limiter_alpha, limiter_beta, limiter_scaleBound); returns
+        (limited u, per-element flag: some field limited)."""
+        u = np.array(u, np.float64, copy=True, order="C")
+        flags = np.zeros(self.s.nelem, np.int32)
+        rc = lib().nmo_limiter_minmodb(ctypes.byref(self.s), u.ctypes.data_as(ctypes.c_void_p),
+                                       ctypes.c_double(alpha), ctypes.c_double(beta),
+                                       ctypes.c_int(int(bool(scale_bound))),
+                                       flags.ctypes.data_as(ctypes.c_void_p))
+        if rc:
+            raise RuntimeError(f"nmo_limiter_minmodb failed ({rc})")
+        return u, flags
+
+    def limit(self, u, kind="MRS", alpha=5.0, beta=0.5, scale_bound=False):
+        """scalarwave1_limiter kind ("MRS" or "minmodB") on every element."""
+        if kind == "MRS":
+            return self.limit_mrs(u, alpha)
+        return self.limit_minmodb(u, alpha, beta, scale_bound)
+
+    def rk4_limited(self, u, dt, nsteps, alpha=5.0, t=0.0, kind="MRS", beta=0.5,
+                    scale_bound=False, flags=False):
+        """RK4 steps as nmo_rk4 takes them, with the limiter (MRS or
+        minmodB) on w before every later stage and on the new u
+        (evolve_RK4_mesh with scalarwave1_limiter set,
+        src/main/evolve/RungeKutta.c:19-82).  flags: also return the
+        per-element flags of the last limiter call."""
         u = np.array(u, np.float64, copy=True)
         c = (dt / 6., dt / 3., dt / 3., dt / 6.)
         a = (dt / 2., dt / 2., dt)
@@ -516,10 +539,10 @@ class OracleMesh:
                 u = u + c[s] * r
                 if s < 3:
                     w = 1. * u_p + a[s] * r
-                    w = self.limit_mrs(w, alpha)[0]
-            u = self.limit_mrs(u, alpha)[0]
+                    w = self.limit(w, kind, alpha, beta, scale_bound)[0]
+            u, last = self.limit(u, kind, alpha, beta, scale_bound)
             te += np.longdouble(dt)
-        return u
+        return (u, last) if flags else u
 
     def filter(self, u, alp=36.0, s=32.0, dn=0, jpow=1, filter_fv=True):
         """The reference's exponential filter of every element (evolve_filter_all)."""

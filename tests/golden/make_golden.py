@@ -187,6 +187,23 @@ CASES = {
     "lim_nc_cs7_l0_n5_h0_a0.02": dict(mesh="cs7", n=5, luni=0, k=(0.3, -0.2, 0.1),
                                       dt=0.002, steps=2, eps=0.3, seed=47, hrefine="0",
                                       limiter=0.02),
+    # the minmodB limiter (scalarwave1_limiter = minmodB): bound alpha h,
+    # slopes against beta/sqrt3 times the face neighbours' average jumps;
+    # scaleBound = yes scales the bound by the neighbours' mean |average|
+    "mmb_box_l1_n5_a0.05": dict(mesh="box", n=5, luni=1, k=(1.0, -0.5, 0.25),
+                                dt=0.002, steps=3, eps=0.3, seed=48, limiter=0.05,
+                                limname="minmodB"),
+    "mmb_cs7_l1_n4_a0.2_b0.8": dict(mesh="cs7", n=4, luni=1, k=(0.3, -0.2, 0.1),
+                                    dt=0.002, steps=2, eps=0.3, seed=49, limiter=0.2,
+                                    limname="minmodB", beta=0.8),
+    "mmb_nc_cs7_l0_n5_h0_a0.1_sb": dict(mesh="cs7", n=5, luni=0, k=(0.3, -0.2, 0.1),
+                                        dt=0.002, steps=2, eps=0.3, seed=50, hrefine="0",
+                                        limiter=0.1, limname="minmodB", scalebound=True),
+    "mmb_mixcs7_l0_n7_w5dnfn_a0.1": dict(mesh="cs7", n=7, luni=0, k=(0.3, -0.2, 0.1),
+                                         dt=0.002, steps=2, eps=0.3, seed=51, limiter=0.1,
+                                         limname="minmodB",
+                                         fv=dict(rec="WENOm5_2", extrap="dnfn_extrap1",
+                                                 patches="0")),
     # the benchmark's mesh family and order at level 2 (448 elements of 9^3
     # LGL nodes, 1.6 M DOF) with the benchmark's dt formula at that level,
     # 0.25 (2 / 2^2) / 8^2, and 10 steps.  amp = 0: the initial data is the
@@ -234,7 +251,10 @@ def parfile(case, prefix):
     if c.get("hrefine"):
         lines += [f"amr_hrefine_p = {c['hrefine']}"]
     if "limiter" in c:
-        lines += ["scalarwave1_limiter = MRS", f"limiter_alpha = {c['limiter']!r}"]
+        lines += [f"scalarwave1_limiter = {c.get('limname', 'MRS')}",
+                  f"limiter_alpha = {c['limiter']!r}",
+                  f"limiter_beta = {c.get('beta', 0.5)!r}",
+                  f"limiter_scaleBound = {'yes' if c.get('scalebound') else 'no'}"]
     if c.get("sphere"):
         lines += [f"amr_hrefine_sphere_levels = {c['sphere'][0]}",
                   f"amr_hrefine_sphere_radius = {c['sphere'][1]}"]

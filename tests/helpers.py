@@ -38,6 +38,16 @@ METHOD_NEAR_CASES = ["ssp3_mixcs7_l1_n6_wZdnfn", "ssp3_mixcs7_l0_n7_wZparab"]
 FILT_CASES = ["filt_cs7_l1_n6", "filt_mixcs7_l0_n7"]
 # scalarwave1_limiter = MRS (limiter_alpha in meta["limiter"])
 LIM_CASES = ["lim_box_l1_n5_a0.01", "lim_cs7_l1_n4_a0.05", "lim_nc_cs7_l0_n5_h0_a0.02"]
+# scalarwave1_limiter = minmodB (limiter_alpha, limiter_beta in meta["beta"],
+# limiter_scaleBound = yes where meta["scalebound"])
+MMB_CASES = ["mmb_box_l1_n5_a0.05", "mmb_cs7_l1_n4_a0.2_b0.8", "mmb_nc_cs7_l0_n5_h0_a0.1_sb",
+             "mmb_mixcs7_l0_n7_w5dnfn_a0.1"]
+
+
+def limiter_kwargs(meta):
+    """The limiter parameters of a limiter fixture (MRS or minmodB)."""
+    return dict(kind=meta.get("limname", "MRS"), alpha=meta["limiter"],
+                beta=meta.get("beta", 0.5), scale_bound=bool(meta.get("scalebound", False)))
 RTOL_FILT_ORACLE = 1e-13
 # dt = auto (the reference's dtfac * hmin; uniform_dtfac on FV elements)
 DTAUTO_CASES = ["dtauto_cs7_l1_n5", "dtauto_box_l2_n6", "dtauto_mixcs7_l0_n7"]

@@ -5,9 +5,9 @@ operation order and must match it bit for bit."""
 import numpy as np
 import pytest
 
-from helpers import (BIG_CASE, CASES, FILT_CASES, LIM_CASES, RTOL_FILT_ORACLE, FV_CASES, METHOD_CASES, METHOD_NEAR_CASES, MID_CASES,
+from helpers import (BIG_CASE, CASES, FILT_CASES, LIM_CASES, MMB_CASES, RTOL_FILT_ORACLE, FV_CASES, METHOD_CASES, METHOD_NEAR_CASES, MID_CASES,
                      MID_NEAR_CASES, MIX_CASES, MIX_NEAR_CASES, NC_CASES, RTOL_NC_ORACLE,
-                     UPW_CASES, big_case_u0, build_mesh, load, oracle_for, perm_to_mesh,
+                     UPW_CASES, big_case_u0, build_mesh, limiter_kwargs, load, oracle_for, perm_to_mesh,
                      rel_l2, to_mesh_order)
 from oracle import nmo
 
@@ -232,6 +232,26 @@ def test_oracle_mrs_limiter_matches_reference(case):
     assert rel_l2(u, d["u_final"]) <= RTOL_NC_ORACLE
     # without the limiter the run is far off: the limiter acts
     assert rel_l2(m.rk4(d["u0"], meta["dt"], meta["steps"]), d["u_final"]) > 1e-3
+
+
+@pytest.mark.parametrize("case", MMB_CASES)
+def test_oracle_minmodb_limiter_matches_reference(case):
+    """scalarwave1_limiter = minmodB: the same stage placement as MRS, with
+    limiter_minmodB's bounded minmod on the linear modes (limiter_alpha,
+    limiter_beta, limiter_scaleBound), on DG, non-conforming and mixed
+    DG / finite-volume meshes."""
+    d, meta = load(case)
+    m = _oracle_mesh(d, meta)
+    kw = limiter_kwargs(meta)
+    u = m.rk4_limited(d["u0"], meta["dt"], meta["steps"], **kw)
+    assert rel_l2(u, d["u_final"]) <= RTOL_NC_ORACLE
+    assert rel_l2(m.rk4(d["u0"], meta["dt"], meta["steps"]), d["u_final"]) > 1e-3
+    # limited elements hold c000 plus linear modes only: limiting twice
+    # changes nothing
+    u1, f1 = m.limit_minmodb(d["u0"], kw["alpha"], kw["beta"], kw["scale_bound"])
+    u2, f2 = m.limit_minmodb(u1, kw["alpha"], kw["beta"], kw["scale_bound"])
+    assert f1.sum() > 0
+    assert rel_l2(u2, u1) <= 1e-13
 
 
 def _generated(meta, uniform=False):

@@ -10,7 +10,8 @@ shared scratch array, and compares every step with the regular entry point
 (nmg_rk4_step) and the last one with the reference's own run of the same
 steps (the fixture's u_final).  The cases cover a conforming DG mesh, a mixed
 DG / finite-volume mesh and a mesh with non-conforming faces (both with the
-untuned default kernels), the MRS limiter and the exponential filter.
+untuned default kernels), the MRS and minmodB limiters and the exponential
+filter.
 This file is collected last on purpose."""
 import ctypes
 
@@ -18,12 +19,13 @@ import numpy as np
 import pytest
 
 import nmesh_gb300 as ng
-from helpers import RTOL_RK4, build_mesh, load, perm_to_mesh, rel_l2, to_mesh_order
+from helpers import (RTOL_RK4, build_mesh, limiter_kwargs, load, perm_to_mesh, rel_l2,
+                     to_mesh_order)
 
 pytestmark = pytest.mark.gpu
 
 CASES = ["cs7_l1_n5", "mixcs7_l0_n7_w5dnfn", "nc_cs7_l0_n5_h0", "lim_cs7_l1_n4_a0.05",
-         "filt_cs7_l1_n6"]
+         "mmb_cs7_l1_n4_a0.2_b0.8", "filt_cs7_l1_n6"]
 
 
 def _noalloc(ev, t, dt, u_in, u_out):
@@ -37,7 +39,7 @@ def _context(m, meta):
     if "fv" in meta:
         ev.set_fv(meta["fv"]["rec"], meta["fv"]["extrap"])
     if "limiter" in meta:
-        ev.set_limiter("MRS", meta["limiter"])
+        ev.set_limiter(**limiter_kwargs(meta))
     if meta.get("filter"):
         ev.set_filter(True)
     return ev
