@@ -725,13 +725,14 @@ def grhd_flops_per_stage(ndg, nfv, n, nf, c2p_iterations_per_stage):
     45 derivatives of n terms plus the chain rule (90 n + 90), the RK4
     update (20), and per face node of the element a two-sided LLF with its
     speeds and the lift (170); per finite-volume point the sources (35),
-    per direction and midpoint two 5-field WENO5 reconstructions (600),
-    two prim2con (50), the LLF (95), the divergence (60 for all three
-    directions) and the update (20); con2prim 40 per point plus 30 per
-    root-finder iteration (counted on the device)."""
+    per direction and cell both face values of the 5 fields from one set of
+    WENO5 smoothness indicators (450), per midpoint two prim2con (50) and
+    the LLF (95), the divergence (60 for all three directions) and the
+    update (20); con2prim 40 per point plus 30 per root-finder iteration
+    (counted on the device)."""
     npd, npf = n ** 3, nf ** 3
     dg = ndg * (npd * (45 + 35 + 90 * n + 90 + 20) + 6 * n * n * 170)
-    fv = nfv * npf * (35 + 3 * 745 + 60 + 20)
+    fv = nfv * npf * (35 + 3 * 595 + 60 + 20)
     c2p = (ndg * npd + nfv * npf) * 40 + 30 * c2p_iterations_per_stage
     return dg + fv + c2p
 

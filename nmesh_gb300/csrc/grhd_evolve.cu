@@ -497,16 +497,22 @@ __global__ void __launch_bounds__(kNT) dg_kernel(GrP P) {
     epilogue(P, sR[i], (size_t)e * NF * np + i, P.u0_d, P.acc_d, P.wout_d);
 }
 
-// finite-volume elements: one CTA per slot
+// finite-volume elements: one CTA per slot.  Per direction and chunk of
+// pencils: (1) per cell and field both face values of the cell's
+// reconstruction (the cell's smoothness indicators serve its two faces),
+// (2) per midpoint the LLF flux of the two states meeting there, per face
+// point the outward flux, (3) per point the flux difference.
 __global__ void __launch_bounds__(kNTF, 1) fv_kernel(GrP P) {
   extern __shared__ double sm[];
   const int nf = P.nf, npf = P.npf, nnf = P.nnf;
   const int slot = blockIdx.x, e = P.slotelem[slot];
+  const int per = nf + 1;  // nf - 1 midpoints + 2 face points per pencil
   double *sP = sm, *sG = sP + NF * npf;  // sG: [pencils][nf + 1][5]
+  double *sQ = sG + (size_t)P.pencils * per * NF;  // [pencils][nf][2][5]: left, right face
   const double *Pg = P.prim_f + (size_t)slot * NF * npf, *Ug = P.win_f + (size_t)slot * NF * npf;
   const double *G = P.geo + (size_t)slot * kGeo * npf;
   double *R = P.rbuf + (size_t)slot * NF * npf;
-  const double h = 2. / (nf - 1);
+  const double ih = (nf - 1) / 2., ih2 = 2. * ih;  // 1/h, 1/(h/2): h = 2/(nf-1)
   for (int i = threadIdx.x; i < NF * npf; i += blockDim.x) sP[i] = Pg[i];
   __syncthreads();
   for (int q = threadIdx.x; q < npf; q += blockDim.x) {
@@ -515,12 +521,26 @@ __global__ void __launch_bounds__(kNTF, 1) fv_kernel(GrP P) {
     sources(P.g, Pq, G + npf + q, npf, S);
     for (int f = 0; f < NF; f++) R[f * npf + q] = S[f];
   }
-  const int per = nf + 1;  // nf - 1 midpoints + 2 face points per pencil
   for (int a = 0; a < 3; a++) {
     const int str[3] = {1, nf, nnf};
     const int o1 = a == 0 ? 1 : 0, o2 = a == 2 ? 1 : 2;
     for (int c0 = 0; c0 < nnf; c0 += P.pencils) {
       const int cp = min(P.pencils, nnf - c0);
+      __syncthreads();
+      for (int task = threadIdx.x; task < cp * nf * NF; task += blockDim.x) {
+        const int f = task % NF, kc = task / NF, k = kc / nf, c = kc - k * nf, pen = c0 + k;
+        const int base = (pen % nf) * str[o1] + (pen / nf) * str[o2];
+        const double *u = sP + f * npf + base;
+        double v[5];
+        for (int j = 0; j < 5; j++) {
+          const int ii = c - 2 + j;
+          v[j] = (ii >= 0 && ii < nf) ? u[ii * str[a]] : 0.;
+        }
+        double lft, rgt;
+        rec_cell(P.rec, nf, v, c, 2., &lft, &rgt);
+        sQ[(kc * 2 + 0) * NF + f] = lft;
+        sQ[(kc * 2 + 1) * NF + f] = rgt;
+      }
       __syncthreads();
       for (int task = threadIdx.x; task < cp * per; task += blockDim.x) {
         const int k = task / per, t = task - k * per, pen = c0 + k;
@@ -534,15 +554,11 @@ __global__ void __launch_bounds__(kNTF, 1) fv_kernel(GrP P) {
           const double nr[3] = {gm[0], gm[npf], gm[2 * npf]};
           const double jg = gm[3 * npf], al = gm[4 * npf], ps = gm[5 * npf];
           double PL[NF], PR[NF], UL[NF], UR[NF];
+          const double *qL = sQ + ((k * nf + t) * 2 + 1) * NF;      // right face of cell t
+          const double *qR = sQ + ((k * nf + t + 1) * 2 + 0) * NF;  // left face of cell t+1
           for (int f = 0; f < NF; f++) {
-            const double *u = sP + f * npf + base;
-            double v[6];
-            for (int j = 0; j < 6; j++) {
-              const int ii = t - 2 + j;
-              v[j] = (ii >= 0 && ii < nf) ? u[ii * str[a]] : 0.;
-            }
-            PL[f] = rec_p(P.rec, nf, v, t, 2.);
-            PR[f] = rec_m(P.rec, nf, v, t, 2.);
+            PL[f] = qL[f];
+            PR[f] = qR[f];
           }
           if (!physical(PL, ps))
             for (int f = 0; f < NF; f++) PL[f] = sP[f * npf + qm];
@@ -584,14 +600,15 @@ __global__ void __launch_bounds__(kNTF, 1) fv_kernel(GrP P) {
         const int k = task / nf, t = task - k * nf, pen = c0 + k;
         const int i1 = pen % nf, i2 = pen / nf;
         const int qq = i1 * str[o1] + i2 * str[o2] + t * str[a];
-        const double det = G[qq];
         const double *g0 = sG + k * per * NF;
+        // det / h (det / (h/2) at the pencil ends) times the flux difference
+        const double dh = G[qq] * ((t == 0 || t == nf - 1) ? ih2 : ih);
         for (int f = 0; f < NF; f++) {
-          double dv;
-          if (t == 0) dv = (g0[f] + g0[(nf - 1) * NF + f]) / (0.5 * h);
-          else if (t == nf - 1) dv = (g0[nf * NF + f] - g0[(nf - 2) * NF + f]) / (0.5 * h);
-          else dv = (g0[t * NF + f] - g0[(t - 1) * NF + f]) / h;
-          R[f * npf + qq] -= det * dv;
+          double df;
+          if (t == 0) df = g0[f] + g0[(nf - 1) * NF + f];
+          else if (t == nf - 1) df = g0[nf * NF + f] - g0[(nf - 2) * NF + f];
+          else df = g0[t * NF + f] - g0[(t - 1) * NF + f];
+          R[f * npf + qq] -= dh * df;
         }
       }
     }
@@ -1125,7 +1142,9 @@ int nmg_grhd_create(const nmg_mesh *m, const nmg_grhd_evolve_params *p, nmg_grhd
   c->smem_dg = sizeof(double) * ((size_t)25 * c->np + c->nn);
   int optin = 0;
   GCK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
-  const size_t per_pencil = sizeof(double) * (size_t)(c->nf + 1) * NF;
+  // per pencil: the fluxes of its nf + 1 flux points and both face values
+  // of its nf cells
+  const size_t per_pencil = sizeof(double) * ((size_t)(c->nf + 1) * NF + (size_t)c->nf * 2 * NF);
   const size_t sp = sizeof(double) * (size_t)NF * c->npf;
   if (sp + per_pencil > (size_t)optin || c->smem_dg > (size_t)optin)
     return gset(c, NMG_EUNSUP, "nmg_grhd_create: element too large for shared memory");

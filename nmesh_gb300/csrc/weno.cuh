@@ -166,3 +166,41 @@ __device__ __forceinline__ double rec_m(int mode, int n, const double *v, int im
   return 0.5 * v[2] + 0.5 * v[3];  // im == n-2
 }
 
+
+// Both face values of cell c of a pencil of n values, v[j] = u[c - 2 + j]
+// for the indices inside the pencil: *lft = the right state of midpoint c-1
+// (rec_m there; c >= 1), *rgt = the left state of midpoint c (rec_p there;
+// c <= n - 2).  The same expressions as rec_p / rec_m on the same five
+// values, so the smoothness indicators and weight products of the cell are
+// computed once for both faces.
+__device__ __forceinline__ void rec_cell(int mode, int n, const double *v, int c, double r3,
+                                         double *lft, double *rgt) {
+  if (mode == NMG_FV_REC_1) {
+    *lft = v[2];
+    *rgt = v[2];
+    return;
+  }
+  if (mode == NMG_FV_REC_WENOM5_2 && c >= 2 && c <= n - 3) {
+    *rgt = weno5_p(v);
+    *lft = weno5_m(v);
+    return;
+  }
+  if (mode == NMG_FV_REC_WENOMZ_2 && c >= 2 && c <= n - 3) {
+    *rgt = wenoz_p(v);
+    *lft = wenoz_m(v);
+    return;
+  }
+  if (c >= 1 && c <= n - 2) {
+    *rgt = weno3_p(v + 1, 1., r3, -0.5, 1.5, 0.5, 0.5);
+    *lft = weno3_m(v + 1, r3, 1., 0.5, 0.5, 1.5, -0.5);
+    return;
+  }
+  // end cells: one face each (c == 0: midpoint 0; c == n-1: midpoint n-2)
+  if (n < 3) {
+    *lft = v[2];
+    *rgt = v[2];
+  } else {
+    *rgt = 0.5 * v[2] + 0.5 * v[3];
+    *lft = 0.5 * v[1] + 0.5 * v[2];
+  }
+}
