@@ -508,7 +508,8 @@ __global__ void __launch_bounds__(kNTF, 1) fv_kernel(GrP P) {
   const int slot = blockIdx.x, e = P.slotelem[slot];
   const int per = nf + 1;  // nf - 1 midpoints + 2 face points per pencil
   double *sP = sm, *sG = sP + NF * npf;  // sG: [pencils][nf + 1][5]
-  double *sQ = sG + (size_t)P.pencils * per * NF;  // [pencils][nf][2][5]: left, right face
+  double *sQ = sG + (size_t)P.pencils * per * NF;  // [2: left, right face][5][pencils][nf]
+  const int qst = P.pencils * nf;                   // stride of one (face, field) plane
   const double *Pg = P.prim_f + (size_t)slot * NF * npf, *Ug = P.win_f + (size_t)slot * NF * npf;
   const double *G = P.geo + (size_t)slot * kGeo * npf;
   double *R = P.rbuf + (size_t)slot * NF * npf;
@@ -528,7 +529,7 @@ __global__ void __launch_bounds__(kNTF, 1) fv_kernel(GrP P) {
       const int cp = min(P.pencils, nnf - c0);
       __syncthreads();
       for (int task = threadIdx.x; task < cp * nf * NF; task += blockDim.x) {
-        const int f = task % NF, kc = task / NF, k = kc / nf, c = kc - k * nf, pen = c0 + k;
+        const int c = task % nf, kf = task / nf, k = kf % cp, f = kf / cp, pen = c0 + k;
         const int base = (pen % nf) * str[o1] + (pen / nf) * str[o2];
         const double *u = sP + f * npf + base;
         double v[5];
@@ -538,8 +539,8 @@ __global__ void __launch_bounds__(kNTF, 1) fv_kernel(GrP P) {
         }
         double lft, rgt;
         rec_cell(P.rec, nf, v, c, 2., &lft, &rgt);
-        sQ[(kc * 2 + 0) * NF + f] = lft;
-        sQ[(kc * 2 + 1) * NF + f] = rgt;
+        sQ[f * qst + k * nf + c] = lft;
+        sQ[(NF + f) * qst + k * nf + c] = rgt;
       }
       __syncthreads();
       for (int task = threadIdx.x; task < cp * per; task += blockDim.x) {
@@ -554,11 +555,9 @@ __global__ void __launch_bounds__(kNTF, 1) fv_kernel(GrP P) {
           const double nr[3] = {gm[0], gm[npf], gm[2 * npf]};
           const double jg = gm[3 * npf], al = gm[4 * npf], ps = gm[5 * npf];
           double PL[NF], PR[NF], UL[NF], UR[NF];
-          const double *qL = sQ + ((k * nf + t) * 2 + 1) * NF;      // right face of cell t
-          const double *qR = sQ + ((k * nf + t + 1) * 2 + 0) * NF;  // left face of cell t+1
           for (int f = 0; f < NF; f++) {
-            PL[f] = qL[f];
-            PR[f] = qR[f];
+            PL[f] = sQ[(NF + f) * qst + k * nf + t];  // right face of cell t
+            PR[f] = sQ[f * qst + k * nf + t + 1];     // left face of cell t+1
           }
           if (!physical(PL, ps))
             for (int f = 0; f < NF; f++) PL[f] = sP[f * npf + qm];

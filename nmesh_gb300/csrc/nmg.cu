@@ -126,7 +126,7 @@ __global__ void plink_kernel(const int *links, int nlink, const int *gn, double 
   }
 }
 
-constexpr int kMaxVariants = 16;
+constexpr int kMaxVariants = 24;
 
 // Objective J = dt sum_nodes W phi^2 of one state, in two deterministic
 // passes: per-block partial sums (fixed-order tree), then one thread adds

@@ -26,11 +26,14 @@
 //         their sum, in exact arithmetic); within FP64 rounding of "fvx".
 //
 // Work split inside one CTA (one element): the element's pi, c state is
-// staged in shared memory; per direction, one thread per midpoint
-// reconstructs the left/right states of the four fluxed fields and forms
-// the LLF flux (stored in shared memory), then one thread per node forms
-// the conservative difference with the J sqrtgdiag / dXb factors and
-// accumulates div f; the face terms and the RK4 update follow.
+// staged in shared memory; per direction and chunk of pencils, one thread
+// per (cell, field) reconstructs both face values of the cell (its
+// smoothness indicators serve both faces; the same expressions as the
+// per-midpoint rec_p / rec_m), then one thread per midpoint forms the
+// flux of the two states meeting there (stored in shared memory); then one
+// thread per node forms the conservative difference with the J sqrtgdiag /
+// dXb factors and accumulates div f; the face terms and the RK4 update
+// follow.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -58,6 +61,16 @@ constexpr int kGeo = 13;  // per-node FV geometry of curvilinear elements
 __device__ __forceinline__ int fnode(int n, int f, int a, int b) {
   const int d = f >> 1, p = (f & 1) * (n - 1);
   return d == 0 ? p + n * (a + n * b) : d == 1 ? a + n * (p + n * b) : a + n * (b + n * p);
+}
+
+// pencils per chunk of the per-cell face-value phase ("fvc"): all pencils
+// of a direction, or as many as fit under the 227 KB limit per CTA
+__host__ __device__ inline int fv_chunk(int n) {
+  const int np = n * n * n, nn = n * n;
+  const int base = 8 * np + 4 * (n - 1) * nn;  // doubles
+  int c = (28900 - base) / (8 * n);
+  if (c > nn) c = nn;
+  return c < 1 ? 1 : c;
 }
 
 // pencil P (in-plane index a + n b of the face-2d plane) -> its i0 = 0 node
@@ -241,7 +254,7 @@ __device__ __forceinline__ void jgdow(const double *G, const double *Gm, int np,
   }
 }
 
-template <int NT>
+template <int NT, bool CELL>
 __global__ void __launch_bounds__(NT) fv_kernel(const StageParams P) {
   extern __shared__ double smem[];
   const int n = P.n, np = n * n * n, nn = n * n, nm = n - 1;
@@ -272,38 +285,88 @@ __global__ void __launch_bounds__(NT) fv_kernel(const StageParams P) {
   const double *Gm = (sCs >= 0 && P.fvmid) ? P.fvmid + (size_t)sCs * 15 * np : nullptr;
   const double oojc = sOoJc;
 
+  double *sQ = sF + 4 * nm * nn;  // CELL: [2 faces][4 fields][n cells][chunk pencils]
+  const int pch = CELL ? fv_chunk(n) : 0;
+
 #pragma unroll 1
   for (int d = 0; d < 3; d++) {
     const int st = d == 0 ? 1 : d == 1 ? n : nn;
-    // midpoint fluxes fnumR of midpoint im (normal at its left node)
-    for (int q = threadIdx.x; q < nm * nn; q += NT) {
-      const int im = q / nn, Pn = q - im * nn;
-      const int base = pencil_base(n, d, Pn);
-      double ui[4], ua[4];
+    if constexpr (!CELL) {
+      // midpoint fluxes fnumR of midpoint im (normal at its left node)
+      for (int q = threadIdx.x; q < nm * nn; q += NT) {
+        const int im = q / nn, Pn = q - im * nn;
+        const int base = pencil_base(n, d, Pn);
+        double ui[4], ua[4];
 #pragma unroll
-      for (int l = 0; l < 4; l++) {
-        const double *u = sW + l * np + base;
-        double v[6];
+        for (int l = 0; l < 4; l++) {
+          const double *u = sW + l * np + base;
+          double v[6];
 #pragma unroll
-        for (int j = 0; j < 6; j++) {
-          const int i = im - 2 + j;
-          v[j] = (i >= 0 && i < n) ? u[i * st] : 0.;
+          for (int j = 0; j < 6; j++) {
+            const int i = im - 2 + j;
+            v[j] = (i >= 0 && i < n) ? u[i * st] : 0.;
+          }
+          ui[l] = rec_p(P.fv_rec, n, v, im, r3);
+          ua[l] = rec_m(P.fv_rec, n, v, im, r3);
         }
-        ui[l] = rec_p(P.fv_rec, n, v, im, r3);
-        ua[l] = rec_m(P.fv_rec, n, v, im, r3);
-      }
-      double nr[3], fn[4];
-      if (Gm) {
+        double nr[3], fn[4];
+        if (Gm) {
 #pragma unroll
-        for (int c = 0; c < 3; c++) nr[c] = __ldg(Gm + (d * 5 + 2 + c) * np + base + im * st);
-      } else {
-        normal_at(P, G, np, d, base + im * st, nr);
-      }
-      numflux4(P.numflux, ui, ua, nr, fn);
+          for (int c = 0; c < 3; c++) nr[c] = __ldg(Gm + (d * 5 + 2 + c) * np + base + im * st);
+        } else {
+          normal_at(P, G, np, d, base + im * st, nr);
+        }
+        numflux4(P.numflux, ui, ua, nr, fn);
 #pragma unroll
-      for (int l = 0; l < 4; l++) sF[(l * nm + im) * nn + Pn] = fn[l];
+        for (int l = 0; l < 4; l++) sF[(l * nm + im) * nn + Pn] = fn[l];
+      }
+      __syncthreads();
+    } else {
+#pragma unroll 1
+      for (int c0 = 0; c0 < nn; c0 += pch) {
+        const int cp = min(pch, nn - c0);
+        // both face values of every cell of the chunk's pencils (one set of
+        // smoothness indicators per cell and field)
+        for (int q = threadIdx.x; q < cp * n * 4; q += NT) {
+          const int k = q % cp, lc = q / cp, c = lc % n, l = lc / n;
+          const double *u = sW + l * np + pencil_base(n, d, c0 + k);
+          double v[5];
+#pragma unroll
+          for (int j = 0; j < 5; j++) {
+            const int i = c - 2 + j;
+            v[j] = (i >= 0 && i < n) ? u[i * st] : 0.;
+          }
+          double lft, rgt;
+          rec_cell(P.fv_rec, n, v, c, r3, &lft, &rgt);
+          sQ[((0 * 4 + l) * n + c) * pch + k] = lft;
+          sQ[((1 * 4 + l) * n + c) * pch + k] = rgt;
+        }
+        __syncthreads();
+        // midpoint fluxes fnumR of midpoint im (normal at its left node): the
+        // right face of cell im meets the left face of cell im + 1
+        for (int q = threadIdx.x; q < cp * nm; q += NT) {
+          const int im = q / cp, k = q - im * cp, Pn = c0 + k;
+          const int base = pencil_base(n, d, Pn);
+          double ui[4], ua[4];
+#pragma unroll
+          for (int l = 0; l < 4; l++) {
+            ui[l] = sQ[((1 * 4 + l) * n + im) * pch + k];
+            ua[l] = sQ[((0 * 4 + l) * n + im + 1) * pch + k];
+          }
+          double nr[3], fn[4];
+          if (Gm) {
+#pragma unroll
+            for (int c = 0; c < 3; c++) nr[c] = __ldg(Gm + (d * 5 + 2 + c) * np + base + im * st);
+          } else {
+            normal_at(P, G, np, d, base + im * st, nr);
+          }
+          numflux4(P.numflux, ui, ua, nr, fn);
+#pragma unroll
+          for (int l = 0; l < 4; l++) sF[(l * nm + im) * nn + Pn] = fn[l];
+        }
+        __syncthreads();
+      }
     }
-    __syncthreads();
     // conservative difference at every node of the direction's pencils
     for (int q = threadIdx.x; q < np; q += NT) {
       const int i0 = q / nn, Pn = q - i0 * nn;
@@ -399,15 +462,15 @@ __global__ void __launch_bounds__(NT) fv_kernel(const StageParams P) {
   }
 }
 
-template <int NT>
+template <int NT, bool CELL>
 cudaError_t launch_fv(const StageParams &P, cudaStream_t st) {
-  const size_t smem = fv_smem(P.n);
+  const size_t smem = fv_smem(P.n) + (CELL ? sizeof(double) * 8 * P.n * fv_chunk(P.n) : 0);
   if (P.nelem == 0)
-    return cudaFuncSetAttribute(fv_kernel<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    return cudaFuncSetAttribute(fv_kernel<NT, CELL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)smem);
   const int grid = P.fvlist ? P.nfvel : (P.ecount > 0 ? P.ecount : P.nelem);
   if (grid == 0) return cudaSuccess;
-  fv_kernel<NT><<<grid, NT, smem, st>>>(P);
+  fv_kernel<NT, CELL><<<grid, NT, smem, st>>>(P);
   return cudaGetLastError();
 }
 
@@ -415,10 +478,20 @@ cudaError_t launch_fv(const StageParams &P, cudaStream_t st) {
 
 int variants(int n, Variant *out, int cap) {
   if (n < 2 || n > kFvMaxN || cap < 3) return 0;
-  out[0] = {NMG_FV_NAME, 1, 128, launch_fv<128>};
-  out[1] = {NMG_FV_NAME, 1, 256, launch_fv<256>};
-  out[2] = {NMG_FV_NAME, 1, 512, launch_fv<512>};
+  out[0] = {NMG_FV_NAME, 1, 128, launch_fv<128, false>};
+  out[1] = {NMG_FV_NAME, 1, 256, launch_fv<256, false>};
+  out[2] = {NMG_FV_NAME, 1, 512, launch_fv<512, false>};
+#ifdef NMG_FV_FAST
+  // "fvc": the per-cell face-value phase (fewer FP64 instructions, more
+  // shared memory and barriers); the autotuner chooses
+  if (cap < 6) return 3;
+  out[3] = {"fvc", 1, 128, launch_fv<128, true>};
+  out[4] = {"fvc", 1, 256, launch_fv<256, true>};
+  out[5] = {"fvc", 1, 512, launch_fv<512, true>};
+  return 6;
+#else
   return 3;
+#endif
 }
 
 }  // namespace NMG_FVNS

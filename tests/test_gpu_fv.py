@@ -17,9 +17,10 @@ from helpers import (FV_CASES, MID_CASES, PI, RTOL_RHS, RTOL_RK4, build_mesh, ga
 pytestmark = pytest.mark.gpu
 
 # "fvx": reference operation order, no FMA; "fv": FMA and one division per
-# WENO reconstruction (within FP64 rounding)
+# WENO reconstruction (within FP64 rounding); "fvc": "fv" with the face
+# values reconstructed per cell (both faces from one set of indicators)
 FV_EXACT = ["fvx:1:128", "fvx:1:256", "fvx:1:512"]
-FV_FAST = ["fv:1:128", "fv:1:256", "fv:1:512"]
+FV_FAST = ["fv:1:128", "fv:1:256", "fv:1:512", "fvc:1:128", "fvc:1:256", "fvc:1:512"]
 FV_VARIANTS = FV_EXACT + FV_FAST
 
 
@@ -47,7 +48,7 @@ def test_fv_rhs_matches_reference(case, variant):
     assert np.abs(r[perm] - d["r0"]).max() <= 1e-11 * np.abs(d["r0"]).max()
 
 
-@pytest.mark.parametrize("variant", ["fvx", "fv", "auto"])
+@pytest.mark.parametrize("variant", ["fvx", "fv", "fvc", "auto"])
 @pytest.mark.parametrize("case", FV_CASES)
 def test_fv_rk4_matches_reference(case, variant):
     d, meta = load(case)
@@ -102,9 +103,10 @@ def test_fv_periodic_box_bitexact_vs_oracle(n, luni, rec, extrap):
     dt = 0.05 * (2 * PI / 2 ** luni) / n
     uo = o.rk4(u, dt, 3)
     assert np.array_equal(ev.rk4_steps_host(u, 0.0, dt, 3), uo)
-    ev.set_kernel("fv")
-    assert rel_l2(ev.rhs(u, 0.0), ro) <= RTOL_RHS
-    assert rel_l2(ev.rk4_steps_host(u, 0.0, dt, 3), uo) <= RTOL_RK4
+    for v in ("fv", "fvc"):
+        ev.set_kernel(v)
+        assert rel_l2(ev.rhs(u, 0.0), ro) <= RTOL_RHS
+        assert rel_l2(ev.rk4_steps_host(u, 0.0, dt, 3), uo) <= RTOL_RK4
 
 
 @pytest.mark.parametrize("rec,extrap", [("WENOm5_2", "dnfn_extrap1"), ("WENOm3_2", "no")])
@@ -122,9 +124,10 @@ def test_fv_cubed_spheres_outgoing_bitexact_vs_oracle(n, luni, rec, extrap):
     dt = 0.02 / n
     uo = o.rk4(u, dt, 2)
     assert np.array_equal(ev.rk4_steps_host(u, 0.0, dt, 2), uo)
-    ev.set_kernel("fv")
-    assert rel_l2(ev.rhs(u, 0.0), ro) <= RTOL_RHS
-    assert rel_l2(ev.rk4_steps_host(u, 0.0, dt, 2), uo) <= RTOL_RK4
+    for v in ("fv", "fvc"):
+        ev.set_kernel(v)
+        assert rel_l2(ev.rhs(u, 0.0), ro) <= RTOL_RHS
+        assert rel_l2(ev.rk4_steps_host(u, 0.0, dt, 2), uo) <= RTOL_RK4
 
 
 def test_fv_variants_bitwise_identical_and_graph_steps():
@@ -139,9 +142,12 @@ def test_fv_variants_bitwise_identical_and_graph_steps():
     # the thread count does not change any thread's arithmetic
     for o in outs[1:3]:
         assert np.array_equal(o, outs[0])
-    for o in outs[4:]:
+    for o in outs[4:6]:
         assert np.array_equal(o, outs[3])
+    for o in outs[7:9]:
+        assert np.array_equal(o, outs[6])
     assert rel_l2(outs[3], outs[0]) <= RTOL_RK4
+    assert rel_l2(outs[6], outs[0]) <= RTOL_RK4
     ev.set_kernel("fvx:1:256")
     # the single-step path equals the graph-captured multi-step path
     ev.set_state(u)

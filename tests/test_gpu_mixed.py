@@ -19,7 +19,7 @@ def _gpu(cuda_ok):
     yield
 
 
-COMBOS = [("eo", "fvx"), ("eof", "fv"), ("gather", "fvx:1:512"), ("auto", None)]
+COMBOS = [("eo", "fvx"), ("eof", "fv"), ("eo", "fvc"), ("gather", "fvx:1:512"), ("auto", None)]
 
 
 def _set(ev, dg, fv):

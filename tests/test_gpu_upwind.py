@@ -20,8 +20,8 @@ def _kernels(meta):
     if "fv" not in meta:
         return ["eo", "eof", "gather"]
     if meta["fv"].get("patches"):
-        return [("eo", "fvx"), ("eof", "fv")]
-    return ["fvx", "fv"]
+        return [("eo", "fvx"), ("eof", "fv"), ("eo", "fvc:1:256")]
+    return ["fvx", "fv", "fvc"]
 
 
 @pytest.mark.parametrize("case", UPW_CASES)
