@@ -11,7 +11,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libnmg.so")
-SOURCES = ["nmg.cu", "stage_eo.cu", "stage_gather.cu", "stage_fv.cu", "stage_fv_fast.cu",
+SOURCES = ["nmg.cu", "stage_eo.cu", "stage_tc.cu", "stage_gather.cu", "stage_fv.cu", "stage_fv_fast.cu",
            "grhd.cu", "grhd_evolve.cu", "noalloc.cu", "mesh.cpp", "ckpt.cpp"]
 # per-file extra flags: the finite-volume kernel rounds every product and sum
 # separately, in the reference's order (no FMA contraction)

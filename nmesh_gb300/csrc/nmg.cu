@@ -945,6 +945,7 @@ static int create_impl(const nmg_mesh *m, int32_t bc_kind, const double k[3], bo
   if (c->mixed) {
     c->ndg = nmgk::eo_variants(m->n, c->variants, kMaxVariants);
     c->ndg += nmgk::gather_variants(m->n, c->variants + c->ndg, kMaxVariants - c->ndg);
+    c->ndg += nmgk::tc_variants(m->n, c->variants + c->ndg, kMaxVariants - c->ndg);
     const int nf = nmgk::fv_variants(m->n, c->variants + c->ndg, kMaxVariants - c->ndg);
     if (c->ndg == 0 || nf == 0)
       return set_err(c, NMG_EUNSUP, "nmg_create: mixed DG / finite-volume n must be in [2,12]");
@@ -956,6 +957,8 @@ static int create_impl(const nmg_mesh *m, int32_t bc_kind, const double k[3], bo
     c->nvariants = nmgk::eo_variants(m->n, c->variants, kMaxVariants);
     c->nvariants += nmgk::gather_variants(m->n, c->variants + c->nvariants,
                                           kMaxVariants - c->nvariants);
+    c->nvariants += nmgk::tc_variants(m->n, c->variants + c->nvariants,
+                                      kMaxVariants - c->nvariants);
     if (c->nvariants == 0) return set_err(c, NMG_EUNSUP, "nmg_create: n must be in [2,12]");
     if (nmgk::vjp_variants(m->n, &c->vjp, 1) != 1)
       return set_err(c, NMG_EUNSUP, "nmg_create: no transposed kernel for this n");
@@ -1245,6 +1248,7 @@ static int create_impl(const nmg_mesh *m, int32_t bc_kind, const double k[3], bo
     CK(up(&c->d_fvbnrm, fvbnrm));
   }
   if (anydg) CK(nmgk::eo_upload(n, m->D.data()));
+  if (anydg) CK(nmgk::tc_upload(n, m->D.data()));
   if (c->mixed) {
     CK(cudaMalloc((void **)&c->d_isfv, E));
     CK(cudaMalloc((void **)&c->d_fvlist, sizeof(int) * E));

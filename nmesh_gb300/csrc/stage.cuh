@@ -363,6 +363,10 @@ struct Variant {
 // all compiled variants for n (returns count, fills out[])
 int gather_variants(int n, Variant *out, int cap);
 int eo_variants(int n, Variant *out, int cap);
+// tensor-core variant: derivatives by exact integer digit products (n = 9)
+int tc_variants(int n, Variant *out, int cap);
+// digits of D for the tensor-core variant (no-op for other n)
+cudaError_t tc_upload(int n, const double *D);
 // transposed (vector-Jacobian) stage kernel for n
 int vjp_variants(int n, Variant *out, int cap);
 // batched persistent kernel over element groups of different n (2..10)

@@ -1,0 +1,476 @@
+// stage_tc.cu -- "tc" variant of the fused DG stage kernel (n = 9): the LGL
+// directional derivatives on the tensor cores, exactly, by integer digits.
+//
+// GB300 issues about two FP64 FMAs per clock per SM, so the 10 directional
+// line derivatives per node (two thirds of the FP64 work of the eo variant)
+// are moved to the FP16 tensor pipe, which runs beside the FP64 pipe.  The
+// arithmetic is exact-integer splitting (Ozaki, Ogita, Oishi and Rump's error-
+// free splitting of floating-point matrix products, with fixed-point digits):
+//
+// * each field of an element is put on one fixed-point grid: with Emax the
+//   largest biased exponent of the field's values, u = X 2^(Emax-1086) with
+//   X < 2^64 an integer (its top 56 bits are kept: 7 digits of 8 bits,
+//   d_s = byte 7-s of X, carrying u's sign);
+// * each row i of D is put on its own grid the same way (exponent FD_i, 7
+//   digits delta_t, rounded to nearest at the 56th bit);
+// * the tensor core forms, for every output i and digit group w = s + t
+//   <= 6, acc_w = sum_p sum_{s+t=w} delta_t(D_ip) d_s(u_p): at most 9 points x
+//   7 pairs of products below 2^16, so |acc_w| < 2^22 and every partial sum
+//   is an integer that FP32 holds exactly (the accumulators start at
+//   1.5 2^23, so their bit patterns are 0x4B400000 + acc_w: no conversion
+//   instruction is needed to read them back);
+// * T = sum_w acc_w 2^(40-8w) is formed in 64-bit integers and turned into
+//   the FP64 value T 2^(Emax+FD_i-2100) (one conversion, rounded to
+//   nearest, and an integer add to the exponent field).
+//
+// The dropped digit groups and digits leave an error of a few units of 2^-53
+// of max|u| x max|D_i.| per output, the size of the rounding error of the
+// FP64 dot product itself; the result is bitwise deterministic.  A field whose
+// largest exponent is 2047 (inf or NaN) yields NaN derivatives; values below
+// 2^-1022 (subnormals) count as zero, and derivatives below the normal range
+// flush to zero.
+//
+// Layout: the digits of element-field values are stored once per node, 16 B
+// each ([field][node][8 x fp16], slot 7 zero).  One MMA row is one line of
+// nodes along the pass direction; ldmatrix gathers the 16-B rows of a line
+// from that one layout for all three directions (bank-conflict free: the
+// node stride of a line is 1, 9 or 81).  K = (point, digit slot): 10 points x
+// 8 = 80 (the tenth point is a copy of the ninth with zero B rows); N =
+// (output, group): 9 x 7 = 63 of 64 columns, arranged so that each thread of
+// a quad holds all seven groups of the outputs it owns (t and t+4; output 8
+// is summed over the quad).  Everything after the derivatives (chain rule
+// with the metric, LLF face lift, RK update) is the FP64 code of the other
+// variants.
+//
+// Reference semantics (paths within nmeshsource/nmesh): the derivative is
+// src/main/coordinates/derivs.c:154-181 (D applied along each direction,
+// then the chain rule of src/tests/scalarwave1/scalarwave1.c:242-284).
+#include <cuda_fp16.h>
+
+#include <cstdint>
+#include <cstring>
+
+#include "stage.cuh"
+
+namespace nmgk {
+namespace {
+
+constexpr int TN = 9;            // points per direction
+constexpr int TNP = TN * TN * TN, TNN = TN * TN;
+constexpr int TKS = 5;           // k-steps of 16: 10 points x 8 digit slots
+constexpr int TNTILE = 8;        // n-tiles of 8 columns
+constexpr int TG = 7;            // digit groups kept
+constexpr int TTILES = 6;        // tiles of 16 lines per direction (81 lines)
+constexpr unsigned kMagic = 0x4B400000u;  // bit pattern of 1.5 * 2^23
+constexpr size_t kTcSmem = sizeof(double) * 4 * TNP + sizeof(uint4) * 4 * TNP;
+
+// B fragments per (k-step, pair of n-tiles, lane): {b01, b23} of n-tile 2q,
+// {b01, b23} of n-tile 2q+1 (mma.m16n8k16 B layout)
+__device__ uint4 gTcB[TKS][TNTILE / 2][32];
+__constant__ int cTcRowExp[TN];  // FD_i: biased exponent of max_p |D_ip|
+
+__device__ __forceinline__ void mma16816(float *d, const uint32_t *a, uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+      "{%8,%9}, {%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ void ldsm_x4(uint32_t *r, uint32_t addr) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(addr));
+}
+
+// 7 signed 8-bit digits of v on the grid of exponent Emax, as fp16 pairs
+__device__ __forceinline__ uint4 tc_digits(double v, int emax) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const int e = (int)(b >> 52) & 0x7FF;
+  const unsigned long long m = e ? ((b & 0xFFFFFFFFFFFFFull) | (1ull << 52)) : 0ull;
+  const int d = emax - e;  // >= 0
+  const unsigned long long X = d < 64 ? (m << 11) >> d : 0ull;
+  const unsigned hi = (unsigned)(X >> 32), lo = (unsigned)X;
+  // 0x64dd = fp16 of 1024 + dd (exact); subtracting 1024 leaves the digit
+  uint32_t h[4];
+  h[0] = __byte_perm(hi, 0x64u, 0x4243);
+  h[1] = __byte_perm(hi, 0x64u, 0x4041);
+  h[2] = __byte_perm(lo, 0x64u, 0x4243);
+  h[3] = __byte_perm(lo, 0x64u, 0x4541);  // digit 6, slot 7 = 1024 -> 0
+  const bool neg = (b >> 63) != 0;
+  const __half2 s2 = neg ? __floats2half2_rn(-1.f, -1.f) : __floats2half2_rn(1.f, 1.f);
+  const __half2 o2 = neg ? __floats2half2_rn(1024.f, 1024.f) : __floats2half2_rn(-1024.f, -1024.f);
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    __half2 x = *reinterpret_cast<__half2 *>(&h[k]);
+    x = __hfma2(x, s2, o2);
+    h[k] = *reinterpret_cast<uint32_t *>(&x);
+  }
+  return make_uint4(h[0], h[1], h[2], h[3]);
+}
+
+// T 2^delta as FP64: T converted with one rounding to nearest, then its
+// exponent field raised by delta (an integer add); a result outside the
+// normal range flushes to zero or saturates to infinity
+__device__ __forceinline__ double tc_to_double(long long T, int delta) {
+  const double d = __ll2double_rn(T);
+  const int hi = __double2hiint(d), ex = (hi >> 20) & 0x7FF, ne = ex + delta;
+  if (ex != 0 && ne > 0 && ne < 2047) return __hiloint2double(hi + (delta << 20), __double2loint(d));
+  if (ex == 0 || ne <= 0) return copysign(0., d);
+  return copysign(__longlong_as_double(0x7FF0000000000000ll), d);
+}
+
+__device__ __forceinline__ int tc_acc(float f) { return (int)(__float_as_uint(f) - kMagic); }
+
+// node of point p of line L (L = l0 + 9 l1) along direction a
+__device__ __forceinline__ int tc_node(int a, int L, int p) {
+  return a == 0 ? p + TN * L : (a == 1 ? (L % TN) + TN * p + TNN * (L / TN) : L + TNN * p);
+}
+
+// derivatives along a of field f at this lane's owned output slots (see
+// the kernel): the MMAs over the tile's 16 lines, then the digit groups
+// combined into FP64 values.  Groups are paired in 32 bits first:
+// p_k = acc_2k 2^8 + acc_2k+1 (|p_k| < 2^31), T = p_0 2^32 + p_1 2^16 + p_2 +
+// floor(acc_6 / 2^8).
+__device__ __forceinline__ int tc_pair(float hi, float lo) {
+  return (int)(__float_as_uint(hi) * 256u + __float_as_uint(lo) - 257u * kMagic);
+}
+
+__device__ __forceinline__ void tc_derivs(const uint4 *__restrict__ gB, uint32_t rowaddr,
+                                          uint32_t pstep, int chunk, int lane, int tq, int emax,
+                                          int fd0, int fd1, int fd8, double *dv) {
+  float acc[TNTILE][4];
+#pragma unroll
+  for (int i = 0; i < TNTILE; i++)
+#pragma unroll
+    for (int j = 0; j < 4; j++) acc[i][j] = 12582912.f;
+#pragma unroll 1
+  for (int kk = 0; kk < TKS; kk++) {
+    const int p = min(2 * kk + chunk, TN - 1);  // the tenth point repeats the ninth
+    uint32_t af[4];
+    ldsm_x4(af, rowaddr + (uint32_t)p * pstep);
+#pragma unroll
+    for (int q = 0; q < TNTILE / 2; q++) {
+      const uint4 bq = __ldg(gB + (kk * (TNTILE / 2) + q) * 32 + lane);
+      mma16816(acc[2 * q], af, bq.x, bq.y);
+      mma16816(acc[2 * q + 1], af, bq.z, bq.w);
+    }
+  }
+  const bool bad = emax >= 2047;  // inf or NaN in the field
+  // owned outputs t and t+4 of rows g (registers 0, 1) and g+8 (2, 3): slots
+  // sb..sb+6 hold groups 0..6
+#pragma unroll
+  for (int o = 0; o < 4; o++) {
+    const int rr = (o >> 1) * 2, sb = (o & 1) * 7;
+#define TC_A(w) acc[(sb + (w)) >> 1][rr + ((sb + (w)) & 1)]
+    const int p0 = tc_pair(TC_A(0), TC_A(1)), p1 = tc_pair(TC_A(2), TC_A(3));
+    const int p2 = tc_pair(TC_A(4), TC_A(5));
+    const int a6 = (int)(__float_as_uint(TC_A(6)) - kMagic);
+#undef TC_A
+    const long long T = ((long long)p0 << 32) + ((long long)p1 << 16) + (long long)p2 +
+                        (long long)(a6 >> 8);
+    dv[o] = bad ? __longlong_as_double(0x7FF8000000000000ll)
+                : tc_to_double(T, emax + ((o & 1) ? fd1 : fd0) - 2100);
+  }
+  // output 8: groups 2t, 2t+1 here (t = 3: group 6 and an empty column),
+  // summed over the quad
+  long long P8[2];
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    const int pp = tc_pair(acc[7][2 * h], acc[7][2 * h + 1]);
+    P8[h] = tq < 3 ? ((long long)pp << (32 - 16 * tq)) : (long long)(pp >> 16);
+    P8[h] += __shfl_xor_sync(0xffffffffu, P8[h], 1);
+    P8[h] += __shfl_xor_sync(0xffffffffu, P8[h], 2);
+  }
+  dv[4] = bad ? __longlong_as_double(0x7FF8000000000000ll)
+              : tc_to_double(tq == 0 ? P8[0] : P8[1], emax + fd8 - 2100);
+}
+
+// r out (mode 0) or the RK stage update (modes of StageParams), with the
+// loads of NB outputs per thread issued before their arithmetic
+template <int NT>
+__device__ __forceinline__ void tc_epilogue(const StageParams &P, const double *Wg,
+                                            const double *sR, int e) {
+  constexpr int TOT = NF * TNP, NB = 4;
+  if (P.skip && P.skip[e]) return;
+  const size_t base = (size_t)e * NF * TNP;
+  const int mode = P.mode;
+  const bool need_u0 = mode == 1 || mode == 2 || mode == 3 || mode == 5 || mode == 6;
+  const bool need_acc = mode == 2 || mode == 3 || mode == 4 || mode == 6;
+  for (int q0 = threadIdx.x; q0 < TOT; q0 += NB * NT) {
+    double r[NB], u[NB], ac[NB], wi[NB];
+#pragma unroll
+    for (int j = 0; j < NB; j++) {
+      const int q = q0 + j * NT;
+      r[j] = u[j] = ac[j] = wi[j] = 0.;
+      if (q < TOT) {
+        r[j] = q < 4 * TNP ? sR[q] : __ldg(Wg + (q - 4 * TNP));  // r_phi = pi
+        if (need_u0) u[j] = __ldg(P.u0 + base + q);
+        if (need_acc) ac[j] = P.acc[base + q];
+        if (mode == 6) wi[j] = __ldg(P.win + base + q);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < NB; j++) {
+      const int q = q0 + j * NT;
+      if (q >= TOT) continue;
+      const size_t idx = base + q;
+      if (mode == 0) {
+        P.rout[idx] = r[j];
+      } else if (mode == 1) {
+        P.acc[idx] = fma(P.cacc, r[j], u[j]);
+        P.wout[idx] = fma(P.cw, r[j], u[j]);
+      } else if (mode == 4) {
+        P.acc[idx] = fma(P.cacc, r[j], ac[j]);
+      } else if (mode == 5) {
+        P.acc[idx] = fma(P.cacc, r[j], u[j]);
+      } else if (mode == 6) {
+        P.acc[idx] = fma(P.cacc, r[j], ac[j]);
+        P.wout[idx] = fma(0.25, fma(P.cw, r[j], wi[j]), 0.75 * u[j]);
+      } else {
+        P.acc[idx] = fma(P.cacc, r[j], ac[j]);
+        P.wout[idx] = fma(P.cw, r[j], u[j]);
+      }
+    }
+  }
+}
+
+template <int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) tc_kernel(StageParams P) {
+  constexpr int NWARP = NT / 32;
+  constexpr int NLOAD = (4 * TNP + NT - 1) / NT;
+  extern __shared__ __align__(16) unsigned char tsm[];
+  double *sR = reinterpret_cast<double *>(tsm);           // [4][NP]: r_pi, r_c
+  uint4 *sDig = reinterpret_cast<uint4 *>(sR + 4 * TNP);  // [4][NP] digits
+  __shared__ int sCs[1];
+  __shared__ int sMask;
+  __shared__ int sEmax[4];
+  __shared__ double sScale[3];
+  __shared__ double sG[1][3];
+
+  const int e0 = P.ebase + blockIdx.x;
+  const int e = elem_at(P, e0);
+  if (e >= P.nelem) return;  // whole CTA (one element per CTA)
+  const int tid = threadIdx.x;
+  const double *Wg = P.win + (size_t)e * NF * TNP;  // w of this element, [field][node]
+  // all loads of w in flight at once
+  double v[NLOAD];
+#pragma unroll
+  for (int k = 0; k < NLOAD; k++) {
+    const int q = tid + k * NT;
+    v[k] = q < 4 * TNP ? __ldg(Wg + q) : 0.;
+  }
+  if (tid == 0) {
+    const int cs = P.cslot[e];
+    sCs[0] = cs;
+    sMask = cs >= 0 ? P.cmask[cs] : (1 | (1 << 4) | (1 << 8));
+    for (int d = 0; d < 3; d++) sScale[d] = P.scale[e * 3 + d];
+    for (int d = 0; d < 3; d++) sG[0][d] = P.gcart[e * 3 + d];
+  }
+  if (tid < 4) sEmax[tid] = 0;
+  for (int q = tid; q < 4 * TNP; q += NT) sR[q] = 0.;
+  __syncthreads();
+  {
+    int em[4] = {0, 0, 0, 0};
+#pragma unroll
+    for (int k = 0; k < NLOAD; k++) {
+      const int q = tid + k * NT, f = q / TNP;
+      const int ex = (int)((unsigned long long)__double_as_longlong(v[k]) >> 52) & 0x7FF;
+#pragma unroll
+      for (int j = 0; j < 4; j++)
+        if (f == j) em[j] = max(em[j], ex);
+    }
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      const unsigned m = __reduce_max_sync(0xffffffffu, (unsigned)em[j]);
+      if ((tid & 31) == 0) atomicMax(&sEmax[j], (int)m);
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < NLOAD; k++) {
+    const int q = tid + k * NT;
+    if (q < 4 * TNP) sDig[q] = tc_digits(v[k], sEmax[q / TNP]);
+  }
+  __syncthreads();
+
+  const double t = stage_time(P);
+  const int warp = tid >> 5, lane = tid & 31, g = lane >> 2, tq = lane & 3;
+  const int cs = sCs[0], mask = sMask;
+  const uint32_t digbase = (uint32_t)__cvta_generic_to_shared(sDig);
+  const int fd0 = cTcRowExp[tq], fd1 = cTcRowExp[tq + 4], fd8 = cTcRowExp[8];
+  const uint4 *gB = &gTcB[0][0][0];
+
+  // ---- volume terms, one direction per pass; warp w takes lines 16w..16w+15 ----
+#pragma unroll 1
+  for (int a = 0; a < 3; a++) {
+    const int row = (mask >> (3 * a)) & 7;
+#pragma unroll 1
+    for (int tile = warp; tile < TTILES; tile += NWARP) {
+      // ldmatrix row of this lane: line Lr, points 2kk + chunk (node nb + p ps)
+      const int Lr = min(tile * 16 + (lane & 15), TNN - 1), chunk = lane >> 4;
+      const int ps = a == 0 ? 1 : (a == 1 ? TN : TNN);
+      const int nb = a == 0 ? TN * Lr : (a == 1 ? (Lr % TN) + TNN * (Lr / TN) : Lr);
+      const uint32_t rowbase = digbase + (uint32_t)nb * 16u, pstep = (uint32_t)ps * 16u;
+      // owned output slots: (g, t), (g, t+4), (g+8, t), (g+8, t+4), and output 8
+      // of row g (t = 0) or g+8 (t = 1); their nodes and the chain-rule factors
+      // M[a][i](node) of every i with M[a][i] != 0, all loaded before the MMAs
+      int nodeS[5];
+      bool okS[5];
+      double m3[3][5];
+#pragma unroll
+      for (int sl = 0; sl < 5; sl++) {
+        const int L = tile * 16 + g + (sl < 4 ? (sl >> 1) * 8 : tq * 8);
+        const int i = sl < 4 ? tq + (sl & 1) * 4 : TN - 1;
+        okS[sl] = L < TNN && (sl < 4 || tq < 2);
+        nodeS[sl] = okS[sl] ? tc_node(a, L, i) : 0;
+#pragma unroll
+        for (int i3 = 0; i3 < 3; i3++) {
+          double m = 0.;
+          if (okS[sl] && ((row >> i3) & 1))
+            m = cs < 0 ? sScale[a]
+                       : __ldg(P.metricp + (((size_t)cs * 3 + a) * 3 + i3) * TN * TNN + i * TNN + L);
+          m3[i3][sl] = m;
+        }
+      }
+      double rp[5] = {0., 0., 0., 0., 0.};
+#pragma unroll 1
+      for (int f = 0; f < 4; f++) {  // pi, then c_x, c_y, c_z
+        if (f > 0 && !((row >> (f - 1)) & 1)) continue;
+        double dv[5];
+        tc_derivs(gB, rowbase + (uint32_t)(f * TNP) * 16u, pstep, chunk, lane, tq, sEmax[f], fd0,
+                  fd1, fd8, dv);
+        // chain rule: r_c_i += M[a][i] d_a pi, r_pi += sum_i M[a][i] d_a c_i
+#pragma unroll
+        for (int sl = 0; sl < 5; sl++) {
+          if (!okS[sl]) continue;
+          if (f == 0) {
+#pragma unroll
+            for (int i3 = 0; i3 < 3; i3++) {
+              if (!((row >> i3) & 1)) continue;
+              double *r = sR + (1 + i3) * TNP + nodeS[sl];
+              *r = fma(m3[i3][sl], dv[sl], *r);
+            }
+          } else {
+            const double m = f == 1 ? m3[0][sl] : (f == 2 ? m3[1][sl] : m3[2][sl]);
+            rp[sl] = fma(m, dv[sl], rp[sl]);
+          }
+        }
+      }
+#pragma unroll
+      for (int sl = 0; sl < 5; sl++)
+        if (okS[sl]) sR[nodeS[sl]] += rp[sl];
+    }
+    __syncthreads();
+  }
+  // interior states of the faces and r_phi = pi come from w in global memory
+  face_terms<TN, 1, NT>(P, Wg, sR, sCs, sG, e0, t);
+  tc_epilogue<NT>(P, Wg, sR, e);
+}
+
+template <int NT, int MINB>
+cudaError_t launch_tc(const StageParams &P, cudaStream_t st) {
+  if (P.nelem <= 0) {
+    cudaError_t e = cudaFuncSetAttribute(tc_kernel<NT, MINB>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(tc_kernel<NT, MINB>,
+                                cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  }
+  const int ne = P.ecount > 0 ? P.ecount : P.nelem;
+  tc_kernel<NT, MINB><<<ne, NT, kTcSmem, st>>>(P);
+  return cudaGetLastError();
+}
+
+// 56-bit rounded fixed-point magnitude of x on the grid of exponent fd
+// (the top 7 bytes of (m << 11) >> (fd - e), rounded at the dropped byte)
+unsigned long long digits56(double x, int fd) {
+  uint64_t b;
+  std::memcpy(&b, &x, 8);
+  const int e = (int)(b >> 52) & 0x7FF;
+  if (!e) return 0;
+  const uint64_t m = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+  const int d = fd - e;
+  const uint64_t X = d < 64 ? (m << 11) >> d : 0;
+  return (X + 0x80) >> 8;
+}
+
+uint16_t half_of_int(int v) {  // exact for |v| < 2048
+  if (v == 0) return 0;
+  const uint16_t s = v < 0 ? 0x8000 : 0;
+  int a = v < 0 ? -v : v, ex = 0;
+  while ((a >> ex) > 1) ex++;
+  const int mant = (a << (10 - ex)) & 0x3FF;
+  return (uint16_t)(s | ((ex + 15) << 10) | mant);
+}
+
+}  // namespace
+
+int tc_variants(int n, Variant *out, int cap) {
+  if (n != TN) return 0;
+  int k = 0;
+  // three CTAs of 192 threads (96 registers: 5 warps of a sub-partition's
+  // 16 K registers) or two of 256 per SM
+  if (k < cap) out[k++] = Variant{"tc", 1, 192, launch_tc<192, 3>};
+  if (k < cap) out[k++] = Variant{"tc", 1, 256, launch_tc<256, 2>};
+  return k;
+}
+
+cudaError_t tc_upload(int n, const double *D) {
+  if (n != TN) return cudaSuccess;
+  // per row: exponent and digits of |D_ip|
+  int fd[TN];
+  unsigned long long Y[TN][TN];
+  int sg[TN][TN];
+  for (int i = 0; i < TN; i++) {
+    int mx = 0;
+    for (int p = 0; p < TN; p++) {
+      uint64_t b;
+      std::memcpy(&b, &D[i * TN + p], 8);
+      mx = std::max(mx, (int)(b >> 52) & 0x7FF);
+    }
+    fd[i] = mx;
+    for (int p = 0; p < TN; p++) {
+      Y[i][p] = digits56(D[i * TN + p], mx);
+      sg[i][p] = D[i * TN + p] < 0 ? -1 : 1;
+    }
+  }
+  // B[K = 8 p + s][column], column = 8 nt + 2 t + j <-> slot 2 nt + j of quad thread t
+  static uint16_t B[TKS * 16][TNTILE * 8];
+  std::memset(B, 0, sizeof(B));
+  for (int col = 0; col < TNTILE * 8; col++) {
+    const int nt = col / 8, c8 = col % 8, t = c8 / 2, j = c8 % 2, sl = 2 * nt + j;
+    int i, w;
+    if (sl < 7) { i = t; w = sl; }
+    else if (sl < 14) { i = t + 4; w = sl - 7; }
+    else { i = 8; w = 2 * t + (sl - 14); }
+    if (i >= TN || w >= TG) continue;
+    for (int p = 0; p < TN; p++)
+      for (int s = 0; s < TG; s++) {
+        const int tt = w - s;
+        if (tt < 0 || tt >= TG) continue;
+        const int dig = (int)((Y[i][p] >> (8 * (6 - tt))) & 0xFF);
+        B[8 * p + s][col] = half_of_int(sg[i][p] * dig);
+      }
+  }
+  static uint4 F[TKS][TNTILE / 2][32];
+  for (int kk = 0; kk < TKS; kk++)
+    for (int q = 0; q < TNTILE / 2; q++)
+      for (int lane = 0; lane < 32; lane++) {
+        const int g = lane >> 2, t = lane & 3;
+        uint32_t r[4];
+        for (int h = 0; h < 2; h++) {
+          const int col = 8 * (2 * q + h) + g;
+          const uint32_t b0 = B[16 * kk + 2 * t][col], b1 = B[16 * kk + 2 * t + 1][col];
+          const uint32_t b2 = B[16 * kk + 2 * t + 8][col], b3 = B[16 * kk + 2 * t + 9][col];
+          r[2 * h] = b0 | (b1 << 16);
+          r[2 * h + 1] = b2 | (b3 << 16);
+        }
+        F[kk][q][lane] = make_uint4(r[0], r[1], r[2], r[3]);
+      }
+  cudaError_t err = cudaMemcpyToSymbol(gTcB, F, sizeof(F));
+  if (err != cudaSuccess) return err;
+  return cudaMemcpyToSymbol(cTcRowExp, fd, sizeof(fd));
+}
+
+}  // namespace nmgk
