@@ -137,7 +137,13 @@ def fp64_work_per_stage(variant, nelem, ncurvi, n, nnz_curvi=7):
     RK update: stage average 1.75 FMA per DOF."""
     np_, nn = n ** 3, n * n
     ncart = nelem - ncurvi
-    if variant.startswith("eo"):
+    if variant.startswith("tc"):
+        # derivatives on the tensor cores; FP64: the chain rule (one FMA per
+        # nonzero metric entry and derivative), one int64 -> FP64 conversion
+        # per derivative output (counted as an instruction, no flop)
+        vol_i = ncart * np_ * (6 + 6) + ncurvi * np_ * (2 * nnz_curvi + 3 + nnz_curvi)
+        vol_f = ncart * np_ * 12 + ncurvi * np_ * 4 * nnz_curvi
+    elif variant.startswith("eo"):
         M, odd = n // 2, n % 2
         # per line: e/o adds, S and T sums (first term a multiply), outputs
         ins = 2 * M + M * (M + odd) + M * M + 2 * M + odd * M
@@ -154,6 +160,14 @@ def fp64_work_per_stage(variant, nelem, ncurvi, n, nnz_curvi=7):
     surf_i, surf_f = nelem * 6 * nn * 14, nelem * 6 * nn * 24
     rk_i = nelem * np_ * NFIELDS * 1.75
     return vol_f + surf_f + 2 * rk_i, vol_i + surf_i + rk_i
+
+
+def tc_mma_per_stage(nelem, ncurvi, nnz_curvi=7):
+    """mma.m16n8k16 (FP16 in, FP32 accumulate) of the tensor-core variant per
+    stage: per element and pass one field per nonzero chain-rule row entry
+    plus pi, 6 tiles of 16 lines, 5 k-steps x 8 n-tiles."""
+    fields = (nelem - ncurvi) * 6 + ncurvi * (3 + nnz_curvi)
+    return fields * 6 * 40
 
 
 def alg_bytes_per_stage(nelem, ncurvi, n):
@@ -343,6 +357,13 @@ def run_ours(args, rank, world, local):
                               "issue_frac": fp64_ins / (per_launch_ms / 1e3) / (fp64_peak * 1e9 / 2),
                               "peak_source": "FP64 FMA probe run live (nmg_fp64_peak)",
                               "dmma_probe_gflops": dmma_peak},
+            "tensor": ({"mma_m16n8k16_per_launch": tc_mma_per_stage(mesh.nelem, ncurvi),
+                        "tflops": tc_mma_per_stage(mesh.nelem, ncurvi) * 4096 /
+                        (per_launch_ms / 1e3) / 1e12,
+                        "note": "FP16 tensor-core products of 8-bit digits (exact integers); "
+                                "the tensor pipe is not the bound (legacy mma.sync rate "
+                                "~0.5 per clock per SM, ncu tensor pipe ~10 % active)"}
+                       if variant.startswith("tc") else None),
             "clocks": clk,
             "cpu_baseline": cpu,
             "adjoint": adjoint,
