@@ -83,6 +83,18 @@ __device__ __forceinline__ void ldsm_x4(uint32_t *r, uint32_t addr) {
                : "r"(addr));
 }
 
+// one bulk prefetch into L2 of the 16-byte-aligned part of [p, p + bytes)
+// (the bulk copy wants a 16-byte-aligned start and a multiple of 16 bytes;
+// trimming keeps it inside the range)
+__device__ __forceinline__ void tc_prefetch_l2(const void *p, unsigned bytes) {
+  const unsigned long long a = (unsigned long long)p;
+  const unsigned long long lo = (a + 15ull) & ~15ull, hi = (a + bytes) & ~15ull;
+  if (hi > lo)
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(lo),
+                 "r"((unsigned)(hi - lo))
+                 : "memory");
+}
+
 // 7 signed 8-bit digits of v on the grid of exponent Emax, as fp16 pairs
 __device__ __forceinline__ uint4 tc_digits(double v, int emax) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(v);
@@ -261,7 +273,18 @@ __global__ void __launch_bounds__(NT, MINB) tc_kernel(StageParams P) {
     v[k] = q < 4 * TNP ? __ldg(Wg + q) : 0.;
   }
   if (tid == 0) {
+    // the element's u0 / accumulator blocks and its metric go to L2 now, so
+    // that the chain rule and the epilogue find them there
+    if (P.mode != 0) {
+      const size_t blk = (size_t)e * NF * TNP;
+      if (P.u0) tc_prefetch_l2(P.u0 + blk, sizeof(double) * NF * TNP);
+      if (P.acc) tc_prefetch_l2(P.acc + blk, sizeof(double) * NF * TNP);
+    }
     const int cs = P.cslot[e];
+    if (cs >= 0) {
+      tc_prefetch_l2(P.metricp + (size_t)cs * 9 * TNP, sizeof(double) * 9 * TNP);
+      tc_prefetch_l2(P.fac + (size_t)cs * 6 * TNN * 4, sizeof(double) * 6 * TNN * 4);
+    }
     sCs[0] = cs;
     sMask = cs >= 0 ? P.cmask[cs] : (1 | (1 << 4) | (1 << 8));
     for (int d = 0; d < 3; d++) sScale[d] = P.scale[e * 3 + d];
