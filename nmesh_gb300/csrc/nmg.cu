@@ -354,7 +354,7 @@ struct nmg_ctx {
   // host round trips: the last stage runs in element chunks whose results are
   // copied back on a second stream while later chunks compute
   static constexpr int kChunks = 32;   // capacity; nchunks are used
-  int nchunks = 8;                     // NMG_COPY_CHUNKS overrides (1..32)
+  int nchunks = 16;                    // NMG_COPY_CHUNKS overrides (1..32)
   cudaStream_t copy_stream = nullptr;
   cudaEvent_t chunk_ev[kChunks] = {}, h2d_ev[kChunks] = {};
   // first-stage element groups of a chunked host->device copy: group k holds
