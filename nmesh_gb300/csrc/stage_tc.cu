@@ -60,7 +60,8 @@ constexpr int TNP = TN * TN * TN, TNN = TN * TN;
 constexpr int TKS = 5;           // k-steps of 16: 10 points x 8 digit slots
 constexpr int TNTILE = 8;        // n-tiles of 8 columns
 constexpr int TG = 7;            // digit groups kept
-constexpr int TTILES = 6;        // tiles of 16 lines per direction (81 lines)
+constexpr int TTILES = 5;        // tiles of 16 lines per direction (lines 0..79;
+                                 // line 80 is one FP64 dot product per node)
 constexpr unsigned kMagic = 0x4B400000u;  // bit pattern of 1.5 * 2^23
 constexpr size_t kTcSmem = sizeof(double) * 4 * TNP + sizeof(uint4) * 4 * TNP;
 
@@ -68,6 +69,7 @@ constexpr size_t kTcSmem = sizeof(double) * 4 * TNP + sizeof(uint4) * 4 * TNP;
 // {b01, b23} of n-tile 2q+1 (mma.m16n8k16 B layout)
 __device__ uint4 gTcB[TKS][TNTILE / 2][32];
 __constant__ int cTcRowExp[TN];  // FD_i: biased exponent of max_p |D_ip|
+__device__ double gTcD[TN * TN];  // D itself, for the last line of each pass
 
 __device__ __forceinline__ void mma16816(float *d, const uint32_t *a, uint32_t b0, uint32_t b1) {
   asm volatile(
@@ -384,6 +386,30 @@ __global__ void __launch_bounds__(NT, MINB) tc_kernel(StageParams P) {
       for (int sl = 0; sl < 5; sl++)
         if (okS[sl]) sR[nodeS[sl]] += rp[sl];
     }
+    if (warp == TTILES % NWARP && lane < TN) {
+      // line 80 (l0 = l1 = 8): output i of lane i as an FP64 dot product with D
+      const int i = lane, L = TNN - 1, node = tc_node(a, L, i);
+      double d[4] = {0., 0., 0., 0.};
+#pragma unroll
+      for (int f = 0; f < 4; f++) {
+        if (f > 0 && !((row >> (f - 1)) & 1)) continue;
+#pragma unroll
+        for (int p = 0; p < TN; p++)
+          d[f] = fma(__ldg(gTcD + i * TN + p), __ldg(Wg + f * TNP + tc_node(a, L, p)), d[f]);
+      }
+      double rpl = 0.;
+#pragma unroll
+      for (int i3 = 0; i3 < 3; i3++) {
+        if (!((row >> i3) & 1)) continue;
+        const double m = cs < 0 ? sScale[a]
+                                : __ldg(P.metricp + (((size_t)cs * 3 + a) * 3 + i3) * TN * TNN +
+                                        i * TNN + L);
+        double *r = sR + (1 + i3) * TNP + node;
+        *r = fma(m, d[0], *r);
+        rpl = fma(m, d[1 + i3], rpl);
+      }
+      sR[node] += rpl;
+    }
     __syncthreads();
   }
   // interior states of the faces and r_phi = pi come from w in global memory
@@ -433,7 +459,8 @@ int tc_variants(int n, Variant *out, int cap) {
   if (n != TN) return 0;
   int k = 0;
   // three CTAs of 192 threads (96 registers: 5 warps of a sub-partition's
-  // 16 K registers) or two of 256 per SM
+  // 16 K registers) or two of 256 per SM; three of 160 threads without
+  // spills (128 registers) ran slower (3.51 vs 3.14 ms per stage)
   if (k < cap) out[k++] = Variant{"tc", 1, 192, launch_tc<192, 3>};
   if (k < cap) out[k++] = Variant{"tc", 1, 256, launch_tc<256, 2>};
   return k;
@@ -493,6 +520,7 @@ cudaError_t tc_upload(int n, const double *D) {
       }
   cudaError_t err = cudaMemcpyToSymbol(gTcB, F, sizeof(F));
   if (err != cudaSuccess) return err;
+  if ((err = cudaMemcpyToSymbol(gTcD, D, sizeof(double) * TN * TN)) != cudaSuccess) return err;
   return cudaMemcpyToSymbol(cTcRowExp, fd, sizeof(fd));
 }
 
