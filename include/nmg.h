@@ -553,11 +553,14 @@ int nmg_rk4_step_noalloc(nmg_ctx *c, double t, double dt, const double *u_in_dev
 
 /* ---- kernel selection (autotuner) --------------------------------------- */
 /* The first RHS/RK4 call of a context times every compiled variant of the
- * stage kernel ("eo": even-odd line derivatives, "gather": node-parallel dot
+ * stage kernel ("eo": even-odd line derivatives, "eof"/"eofu": with the face
+ * lift in the line passes, "gather": node-parallel dot products, "tc" at
+ * n = 9: line derivatives on the tensor cores as exact integer digit
  * products) and tile shape (elements and threads per CTA) on the context's
- * mesh and keeps the fastest.  spec = "auto" re-tunes; "eo", "gather" or
- * "eo:<elements per CTA>:<threads>" forces a variant (the environment
- * variable NMG_KERNEL does the same for new contexts). */
+ * mesh and keeps the fastest.  spec = "auto" re-tunes; a name such as "eo",
+ * "gather" or "tc", or "<name>:<elements per CTA>:<threads>", forces a
+ * variant (the environment variable NMG_KERNEL does the same for new
+ * contexts). */
 int nmg_set_kernel(nmg_ctx *c, const char *spec);
 /* selected variant, candidates and tuning timings as text */
 int nmg_kernel_info(nmg_ctx *c, char *buf, int32_t len);

@@ -277,11 +277,14 @@ __global__ void __launch_bounds__(NT, MINB) tc_kernel(StageParams P) {
   if (tid == 0) {
     // the element's u0 / accumulator blocks and its metric go to L2 now, so
     // that the chain rule and the epilogue find them there
-    if (P.mode != 0) {
-      const size_t blk = (size_t)e * NF * TNP;
-      if (P.u0) tc_prefetch_l2(P.u0 + blk, sizeof(double) * NF * TNP);
-      if (P.acc) tc_prefetch_l2(P.acc + blk, sizeof(double) * NF * TNP);
-    }
+    // (only what the stage mode reads: the accumulator is write-only in
+    // modes 1 and 5, and u0 is w itself in the first stage)
+    const int md = P.mode;
+    const size_t blk = (size_t)e * NF * TNP;
+    if ((md == 1 || md == 2 || md == 3 || md == 5 || md == 6) && P.u0 && P.u0 != P.win)
+      tc_prefetch_l2(P.u0 + blk, sizeof(double) * NF * TNP);
+    if ((md == 2 || md == 3 || md == 4 || md == 6) && P.acc)
+      tc_prefetch_l2(P.acc + blk, sizeof(double) * NF * TNP);
     const int cs = P.cslot[e];
     if (cs >= 0) {
       tc_prefetch_l2(P.metricp + (size_t)cs * 9 * TNP, sizeof(double) * 9 * TNP);
