@@ -165,3 +165,33 @@ def test_tc_mixed_mesh_vs_oracle():
     ev.set_kernel("fvx")
     assert rel_l2(ev.rhs(u, 0.0), o.rhs(u, 0.0)) <= RTOL_RHS
     assert rel_l2(ev.rk4_steps_host(u, 0.0, 0.002, 2), o.rk4(u, 0.002, 2)) <= RTOL_RK4
+
+
+def test_tc_nonconforming_faces_vs_oracle():
+    """Patches 0 and 3 one level finer (amr_hrefine_p): the traces of the
+    non-conforming faces reach the tensor-core kernel through the interface
+    slots, as they reach the FP64 variants."""
+    m = ng.Mesh.build(ng.MESH_CUBEDSPHERES7, n=9, luni=1, cs_dc=1.0, cs_r0fac=20.0,
+                      hrefine=(0, 3))
+    u = gaussian_pulses(m.coords(), seed=33, rmin=1.0, rmax=4.0)
+    u += 1e-3 * np.random.default_rng(33).standard_normal(u.shape)
+    o = oracle_for(m, bc=1)
+    ev = ng.Evolution(m, ng.BC_OUTGOING)
+    ev.set_kernel("tc")
+    assert rel_l2(ev.rhs(u, 0.0), o.rhs(u, 0.0)) <= RTOL_RHS
+    dt = 0.001
+    assert rel_l2(ev.rk4_steps_host(u, 0.0, dt, 3), o.rk4(u, dt, 3)) <= RTOL_RK4
+
+
+@pytest.mark.parametrize("method", ["Euler", "sspRK3"])
+def test_tc_other_integrators_vs_oracle(method):
+    """The Euler and sspRK3 epilogue modes of the tensor-core kernel."""
+    m = ng.Mesh.build(ng.MESH_CUBEDSPHERES7, n=9, luni=0, cs_dc=1.0, cs_r0fac=20.0)
+    u = gaussian_pulses(m.coords(), seed=8, rmin=1.0, rmax=4.0)
+    ev = ng.Evolution(m, ng.BC_OUTGOING)
+    ev.set_kernel("tc")
+    ev.set_evolve_method(method)
+    dt = 0.001
+    got = ev.evolve_steps_host(u, 0.0, dt, 4)
+    want = oracle_for(m, bc=1).evolve(u, dt, 4, method=method)
+    assert rel_l2(got, want) <= RTOL_RK4

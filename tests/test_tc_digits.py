@@ -1,0 +1,161 @@
+"""The arithmetic of the tensor-core stage kernel (nmesh_gb300/csrc/stage_tc.cu),
+restated in Python integers and checked against exact rational arithmetic on
+the CPU: the 8-bit digit split of the values and of D, the digit-group sums
+the FP16 tensor cores form (they must stay below 2^22, where FP32 holds every
+partial sum exactly, accumulators starting at 1.5 2^23), the 64-bit
+recombination and the conversion to FP64.  The bound checked is the one
+stated for the kernel: per output, a few units of 2^-53 of
+max|u| x sum_p |D_ip| (the size of the FP64 dot product's own rounding
+bound).  The GPU tests (tests/test_gpu_tc.py) check the kernel itself."""
+import struct
+from fractions import Fraction
+
+import numpy as np
+import pytest
+
+N, TG = 9, 7  # points per line, digit groups kept
+
+
+def _bits(v):
+    return struct.unpack("<Q", struct.pack("<d", float(v)))[0]
+
+
+def _from_bits(b):
+    return struct.unpack("<d", struct.pack("<Q", b & (2 ** 64 - 1)))[0]
+
+
+def _exp(v):
+    return (_bits(v) >> 52) & 0x7FF
+
+
+def _fixed(v, emax):
+    """X = (m << 11) >> (emax - e) as in tc_digits (m the 53-bit significand)"""
+    b = _bits(v)
+    e = (b >> 52) & 0x7FF
+    m = ((b & ((1 << 52) - 1)) | (1 << 52)) if e else 0
+    d = emax - e
+    return (((m << 11) & (2 ** 64 - 1)) >> d) if d < 64 else 0
+
+
+def u_digits(v, emax):
+    """7 signed digits of v (byte 7 - s of X), slot 7 zero"""
+    X = _fixed(v, emax)
+    sgn = -1 if _bits(v) >> 63 else 1
+    return [sgn * ((X >> (8 * (7 - s))) & 0xFF) for s in range(7)] + [0]
+
+
+def d_digits(x, fd):
+    """7 digits of |D_ip| on the row grid fd, rounded at the dropped byte"""
+    Y = (_fixed(x, fd) + 0x80) >> 8
+    return [(Y >> (8 * (6 - t))) & 0xFF for t in range(7)]
+
+
+def column(col):
+    """(output i, group w) of B column col = 8 nt + 2 t + j (slot 2 nt + j of
+    quad thread t), as tc_upload lays them out"""
+    nt, c8 = col // 8, col % 8
+    t, j = c8 // 2, c8 % 2
+    sl = 2 * nt + j
+    if sl < 7:
+        return t, sl
+    if sl < 14:
+        return t + 4, sl - 7
+    return 8, 2 * t + (sl - 14)
+
+
+def b_matrix(D):
+    fd = [max(_exp(D[i, p]) for p in range(N)) for i in range(N)]
+    B = np.zeros((80, 64), dtype=np.int64)
+    for col in range(64):
+        i, w = column(col)
+        if i >= N or w >= TG:
+            continue
+        for p in range(N):
+            dg = d_digits(D[i, p], fd[i])
+            sg = -1 if D[i, p] < 0 else 1
+            for s in range(TG):
+                t = w - s
+                if 0 <= t < TG:
+                    B[8 * p + s, col] = sg * dg[t]
+    return B, fd
+
+
+def to_double(T, delta):
+    """T 2^delta, rounded to nearest (cvt.rn.f64.s64 + exponent add)"""
+    if T == 0:
+        return 0.0
+    d = float(T)  # Python rounds int -> float to nearest even
+    return float(np.ldexp(d, delta))
+
+
+def line_derivative(u, D, B, fd):
+    emax = max(_exp(v) for v in u)
+    rows = [u_digits(v, emax) for v in u] + [u_digits(u[N - 1], emax)]  # tenth point
+    C = np.array(rows, dtype=np.int64).reshape(-1) @ B
+    assert np.abs(C).max() < 2 ** 22
+    out = np.zeros(N)
+    for t in range(4):
+        for o in range(2):
+            i = t + 4 * o
+            acc = []
+            for w in range(TG):
+                sl = 7 * o + w
+                acc.append(int(C[8 * (sl >> 1) + 2 * t + (sl & 1)]))
+            p = [acc[2 * k] * 256 + acc[2 * k + 1] for k in range(3)]
+            assert all(abs(x) < 2 ** 31 for x in p)
+            T = (p[0] << 32) + (p[1] << 16) + p[2] + (acc[6] >> 8)
+            assert abs(T) < 2 ** 63
+            out[i] = to_double(T, emax + fd[i] - 2100)
+    T8 = 0
+    for t in range(4):
+        a0, a1 = int(C[56 + 2 * t]), int(C[57 + 2 * t])
+        pp = a0 * 256 + a1
+        T8 += (pp << (32 - 16 * t)) if t < 3 else (pp >> 16)
+    out[8] = to_double(T8, emax + fd[8] - 2100)
+    return out
+
+
+@pytest.fixture(scope="module")
+def dmat():
+    from oracle import nmo
+    D = nmo.diffmat(N)
+    B, fd = b_matrix(D)
+    return D, B, fd
+
+
+def test_columns_hold_every_output_group_once():
+    seen = {}
+    for col in range(64):
+        i, w = column(col)
+        if i < N and w < TG:
+            assert (i, w) not in seen
+            seen[(i, w)] = col
+    assert len(seen) == N * TG
+
+
+def test_digit_products_are_exact_and_within_fp64_rounding(dmat):
+    D, B, fd = dmat
+    assert np.abs(B).max() <= 255
+    rng = np.random.default_rng(2024)
+    worst = 0.0
+    for trial in range(120):
+        scale = 10.0 ** rng.uniform(-250, 250)
+        u = rng.standard_normal(N) * scale
+        if trial % 3 == 0:
+            u *= 10.0 ** rng.uniform(-6, 6, N)
+        if trial % 5 == 0:
+            u[rng.integers(N)] = 0.0
+        got = line_derivative(u, D, B, fd)
+        bound = np.abs(u).max() * np.abs(D).sum(1)
+        for i in range(N):
+            exact = sum(Fraction(float(D[i, p])) * Fraction(float(u[p])) for p in range(N))
+            worst = max(worst, abs(float(Fraction(got[i]) - exact)) / bound[i])
+    assert worst <= 2.0 * 2.0 ** -53, worst / 2.0 ** -53
+
+
+def test_zero_and_constant_lines(dmat):
+    D, B, fd = dmat
+    assert np.array_equal(line_derivative(np.zeros(N), D, B, fd), np.zeros(N))
+    # the derivative of a constant is exactly what FP64 gives within the bound
+    c = np.full(N, 3.0)
+    assert np.abs(line_derivative(c, D, B, fd)).max() <= 2.0 * 2.0 ** -53 * 3 * np.abs(D).sum(1).max()

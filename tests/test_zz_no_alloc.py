@@ -8,7 +8,8 @@ Each case takes the fixture's steps through the C ABI, one call per step,
 every call after the first finding the previous call's stale contents in the
 shared scratch array, and compares every step with the regular entry point
 (nmg_rk4_step) and the last one with the reference's own run of the same
-steps (the fixture's u_final).  The cases cover a conforming DG mesh, a mixed
+steps (the fixture's u_final).  The cases cover conforming DG meshes (at
+n = 9 with the tensor-core stage kernel, set on both contexts), a mixed
 DG / finite-volume mesh and a mesh with non-conforming faces (both with the
 untuned default kernels), the MRS and minmodB limiters and the exponential
 filter.
@@ -24,8 +25,8 @@ from helpers import (RTOL_RK4, build_mesh, limiter_kwargs, load, perm_to_mesh, r
 
 pytestmark = pytest.mark.gpu
 
-CASES = ["cs7_l1_n5", "mixcs7_l0_n7_w5dnfn", "nc_cs7_l0_n5_h0", "lim_cs7_l1_n4_a0.05",
-         "mmb_cs7_l1_n4_a0.2_b0.8", "filt_cs7_l1_n6"]
+CASES = ["cs7_l1_n5", "cs7_l0_n9", "mixcs7_l0_n7_w5dnfn", "nc_cs7_l0_n5_h0",
+         "lim_cs7_l1_n4_a0.05", "mmb_cs7_l1_n4_a0.2_b0.8", "filt_cs7_l1_n6"]
 
 
 def _noalloc(ev, t, dt, u_in, u_out):
@@ -36,6 +37,8 @@ def _noalloc(ev, t, dt, u_in, u_out):
 
 def _context(m, meta):
     ev = ng.Evolution(m, ng.BC_EXACT_PLANEWAVE, k=meta["k"])
+    if m.n == 9:
+        ev.set_kernel("tc")
     if "fv" in meta:
         ev.set_fv(meta["fv"]["rec"], meta["fv"]["extrap"])
     if "limiter" in meta:
