@@ -357,6 +357,11 @@ struct nmg_ctx {
   int nchunks = 16;                    // NMG_COPY_CHUNKS overrides (1..32)
   cudaStream_t copy_stream = nullptr;
   cudaEvent_t chunk_ev[kChunks] = {}, h2d_ev[kChunks] = {};
+  // second compute stream of the streamed step: element groups / chunks of
+  // one stage alternate between the two so that one launch's tail overlaps
+  // the next one's start (they touch disjoint elements)
+  cudaStream_t stream2 = nullptr;
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   // first-stage element groups of a chunked host->device copy: group k holds
   // the elements whose face neighbourhood lies in the copy chunks 0..k
   int *d_elist = nullptr;
@@ -2048,6 +2053,9 @@ void nmg_destroy(nmg_ctx *c) {
   }
   cudaFree(c->d_elist);
   if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
+  if (c->stream2) cudaStreamDestroy(c->stream2);
+  if (c->fork_ev) cudaEventDestroy(c->fork_ev);
+  if (c->join_ev) cudaEventDestroy(c->join_ev);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -2310,6 +2318,9 @@ static int last_step_streamed(nmg_ctx *c, double t, double dt, double *host_u,
   if (rc) return rc;
   if (!c->copy_stream) {
     CK(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming));
     for (int k = 0; k < nmg_ctx::kChunks; k++) {
       CK(cudaEventCreateWithFlags(&c->chunk_ev[k], cudaEventDisableTiming));
       CK(cudaEventCreateWithFlags(&c->h2d_ev[k], cudaEventDisableTiming));
@@ -2343,16 +2354,22 @@ static int last_step_streamed(nmg_ctx *c, double t, double dt, double *host_u,
                              cudaMemcpyHostToDevice, c->copy_stream));
         CK(cudaEventRecord(c->h2d_ev[k], c->copy_stream));
       }
+      CK(cudaEventRecord(c->fork_ev, c->stream));
+      CK(cudaStreamWaitEvent(c->stream2, c->fork_ev, 0));
       for (int k = 0; k < c->nchunks; k++) {
-        CK(cudaStreamWaitEvent(c->stream, c->h2d_ev[k], 0));
+        cudaStream_t sk = (k & 1) ? c->stream2 : c->stream;
+        CK(cudaStreamWaitEvent(sk, c->h2d_ev[k], 0));
         const int n0 = c->h2d_off[k], n1 = c->h2d_off[k + 1];
         if (n1 == n0) continue;
         StageParams Q = P;
         Q.elist = c->d_elist;
         Q.ebase = n0;
         Q.ecount = n1 - n0;
-        CK(run_stage(c, c->sel, Q));
+        CK(c->variants[c->sel].launch(Q, sk));
+        c->launches++;
       }
+      CK(cudaEventRecord(c->join_ev, c->stream2));
+      CK(cudaStreamWaitEvent(c->stream, c->join_ev, 0));
       continue;
     }
     if (s < 3) {
@@ -2363,19 +2380,33 @@ static int last_step_streamed(nmg_ctx *c, double t, double dt, double *host_u,
     int64_t chunk = (E + c->nchunks - 1) / c->nchunks;
     chunk = (chunk + epb - 1) / epb * epb;
     const size_t per = (size_t)NF * c->np;
+    // the stage's face traces (non-conforming faces) once, before the chunks
+    if (c->nhang > 0) {
+      CK(nmgk::hang_launch(c->nhang, c->n, c->d_hoff, c->d_hsrc, c->d_hw, P.win, c->d_ghost,
+                           c->stream));
+      c->launches++;
+    }
+    CK(cudaEventRecord(c->fork_ev, c->stream));
+    CK(cudaStreamWaitEvent(c->stream2, c->fork_ev, 0));
     int k = 0;
     for (int64_t ea = 0; ea < E; ea += chunk, k++) {
       const int64_t eb = std::min(E, ea + chunk);
+      cudaStream_t sk = ((k & 1) && !c->mixed) ? c->stream2 : c->stream;
       P.ebase = (int)ea;
       P.ecount = (int)(eb - ea);
-      CK(run_stage(c, c->sel, P, ea == 0));  // traces once per stage
-      CK(cudaEventRecord(c->chunk_ev[k], c->stream));
+      if (c->mixed)
+        CK(run_stage(c, c->sel, P, ea == 0));  // (not reached: mixed meshes step unstreamed)
+      else
+        CK(c->variants[c->sel].launch(P, sk));
+      if (!c->mixed) c->launches++;
+      CK(cudaEventRecord(c->chunk_ev[k], sk));
       CK(cudaStreamWaitEvent(c->copy_stream, c->chunk_ev[k], 0));
       CK(cudaMemcpyAsync(host_u + ea * per, ACC + ea * per, (size_t)(eb - ea) * per * sizeof(double),
                          cudaMemcpyDeviceToHost, c->copy_stream));
     }
   }
   CK(cudaStreamSynchronize(c->copy_stream));
+  CK(cudaStreamSynchronize(c->stream2));
   CK(cudaStreamSynchronize(c->stream));
   c->cur = 1 - cur;
   return NMG_OK;
