@@ -4,8 +4,11 @@
 // GB300 issues about two FP64 FMAs per clock per SM, so the 10 directional
 // line derivatives per node (two thirds of the FP64 work of the eo variant)
 // are moved to the FP16 tensor pipe, which runs beside the FP64 pipe.  The
-// arithmetic is exact-integer splitting (Ozaki, Ogita, Oishi and Rump's error-
-// free splitting of floating-point matrix products, with fixed-point digits):
+// arithmetic is an error-free splitting of the matrix products into digit
+// products (the idea of Ozaki, Ogita, Oishi and Rump, "Error-free
+// transformations of matrix multiplication by using fast routines of matrix
+// multiplication and its applications", Numer. Algorithms 59, 2012), here
+// with fixed-point digits:
 //
 // * each field of an element is put on one fixed-point grid: with Emax the
 //   largest biased exponent of the field's values, u = X 2^(Emax-1086) with
@@ -23,9 +26,10 @@
 //   the FP64 value T 2^(Emax+FD_i-2100) (one conversion, rounded to
 //   nearest, and an integer add to the exponent field).
 //
-// The dropped digit groups and digits leave an error of a few units of 2^-53
-// of max|u| x max|D_i.| per output, the size of the rounding error of the
-// FP64 dot product itself; the result is bitwise deterministic.  A field whose
+// The dropped digit groups and digits leave an error of at most ~1.3 units of
+// 2^-53 of max|u| x sum_p |D_ip| per output (checked against exact rationals),
+// the size of the FP64 dot product's own rounding bound; the result is
+// bitwise deterministic.  A field whose
 // largest exponent is 2047 (inf or NaN) yields NaN derivatives; values below
 // 2^-1022 (subnormals) count as zero, and derivatives below the normal range
 // flush to zero.
@@ -38,9 +42,11 @@
 // 8 = 80 (the tenth point is a copy of the ninth with zero B rows); N =
 // (output, group): 9 x 7 = 63 of 64 columns, arranged so that each thread of
 // a quad holds all seven groups of the outputs it owns (t and t+4; output 8
-// is summed over the quad).  Everything after the derivatives (chain rule
-// with the metric, LLF face lift, RK update) is the FP64 code of the other
-// variants.
+// is summed over the quad).  The 81st line of each pass (81 = 5 x 16 + 1) is
+// an FP64 dot product in the sixth warp.  Everything after the derivatives
+// (chain rule with the metric, LLF face lift, RK update) is the FP64 code of
+// the other variants; the element's metric, lift factors and the u0 /
+// accumulator blocks the stage reads are bulk-prefetched to L2 at the start.
 //
 // Reference semantics (paths within nmeshsource/nmesh): the derivative is
 // src/main/coordinates/derivs.c:154-181 (D applied along each direction,
@@ -133,8 +139,6 @@ __device__ __forceinline__ double tc_to_double(long long T, int delta) {
   if (ex == 0 || ne <= 0) return copysign(0., d);
   return copysign(__longlong_as_double(0x7FF0000000000000ll), d);
 }
-
-__device__ __forceinline__ int tc_acc(float f) { return (int)(__float_as_uint(f) - kMagic); }
 
 // node of point p of line L (L = l0 + 9 l1) along direction a
 __device__ __forceinline__ int tc_node(int a, int L, int p) {
