@@ -555,7 +555,7 @@ int nmg_rk4_step_noalloc(nmg_ctx *c, double t, double dt, const double *u_in_dev
 /* The first RHS/RK4 call of a context times every compiled variant of the
  * stage kernel ("eo": even-odd line derivatives, "eof"/"eofu": with the face
  * lift in the line passes, "gather": node-parallel dot products, "tc" at
- * n = 9: line derivatives on the tensor cores as exact integer digit
+ * n = 7, 8, 9: line derivatives on the tensor cores as exact integer digit
  * products) and tile shape (elements and threads per CTA) on the context's
  * mesh and keeps the fastest.  spec = "auto" re-tunes; a name such as "eo",
  * "gather" or "tc", or "<name>:<elements per CTA>:<threads>", forces a

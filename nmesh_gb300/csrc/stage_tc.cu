@@ -1,5 +1,6 @@
-// stage_tc.cu -- "tc" variant of the fused DG stage kernel (n = 9): the LGL
-// directional derivatives on the tensor cores, exactly, by integer digits.
+// stage_tc.cu -- "tc" variant of the fused DG stage kernel (n = 7, 8, 9
+// points per direction): the LGL directional derivatives on the tensor
+// cores, exactly, by integer digits.
 //
 // GB300 issues about two FP64 FMAs per clock per SM, so the 10 directional
 // line derivatives per node (two thirds of the FP64 work of the eo variant)
@@ -37,13 +38,16 @@
 // Layout: the digits of element-field values are stored once per node, 16 B
 // each ([field][node][8 x fp16], slot 7 zero).  One MMA row is one line of
 // nodes along the pass direction; ldmatrix gathers the 16-B rows of a line
-// from that one layout for all three directions (bank-conflict free: the
-// node stride of a line is 1, 9 or 81).  K = (point, digit slot): 10 points x
-// 8 = 80 (the tenth point is a copy of the ninth with zero B rows); N =
+// from that one layout for all three directions (bank-conflict free at n = 9:
+// the node stride of a line is 1, 9 or 81).  K = (point, digit slot): n
+// points rounded up to even x 8 (at n = 9, 10 x 8 = 80; an added point is a
+// copy of the last with zero B rows); N =
 // (output, group): 9 x 7 = 63 of 64 columns, arranged so that each thread of
 // a quad holds all seven groups of the outputs it owns (t and t+4; output 8
-// is summed over the quad).  The 81st line of each pass (81 = 5 x 16 + 1) is
-// an FP64 dot product in the sixth warp.  Everything after the derivatives
+// is summed over the quad; at n = 7, 8 the columns of outputs >= n are zero).
+// A pass takes n^2 / 16 tiles of 16 lines, one warp each; the line left over
+// at n = 7, 9 (49 = 3 x 16 + 1, 81 = 5 x 16 + 1) is an FP64 dot product in
+// the next warp.  Everything after the derivatives
 // (chain rule with the metric, LLF face lift, RK update) is the FP64 code of
 // the other variants; the element's metric, lift factors and the u0 /
 // accumulator blocks the stage reads are bulk-prefetched to L2 at the start.
@@ -61,21 +65,28 @@
 namespace nmgk {
 namespace {
 
-constexpr int TN = 9;            // points per direction
-constexpr int TNP = TN * TN * TN, TNN = TN * TN;
-constexpr int TKS = 5;           // k-steps of 16: 10 points x 8 digit slots
-constexpr int TNTILE = 8;        // n-tiles of 8 columns
+constexpr int TNTILE = 8;        // n-tiles of 8 columns (9 outputs x 7 groups <= 64)
 constexpr int TG = 7;            // digit groups kept
-constexpr int TTILES = 5;        // tiles of 16 lines per direction (lines 0..79;
-                                 // line 80 is one FP64 dot product per node)
+constexpr int TKSMAX = 5;        // k-steps of 16 at n = 9: 10 points x 8 digit slots
 constexpr unsigned kMagic = 0x4B400000u;  // bit pattern of 1.5 * 2^23
-constexpr size_t kTcSmem = sizeof(double) * 4 * TNP + sizeof(uint4) * 4 * TNP;
 
-// B fragments per (k-step, pair of n-tiles, lane): {b01, b23} of n-tile 2q,
-// {b01, b23} of n-tile 2q+1 (mma.m16n8k16 B layout)
-__device__ uint4 gTcB[TKS][TNTILE / 2][32];
-__constant__ int cTcRowExp[TN];  // FD_i: biased exponent of max_p |D_ip|
-__device__ double gTcD[TN * TN];  // D itself, for the last line of each pass
+// per order n (7, 8, 9): nodes, k-steps (points padded to an even count),
+// full 16-line tiles per direction and whether one line is left over
+template <int N>
+struct TcShape {
+  static constexpr int NP = N * N * N, NN = N * N;
+  static constexpr int KS = (N + 1) / 2;
+  static constexpr int TILES = NN / 16;
+  static constexpr bool LAST = NN % 16 == 1;
+  static_assert(NN % 16 == 0 || NN % 16 == 1, "lines per direction: 16 k or 16 k + 1");
+  static constexpr size_t SMEM = sizeof(double) * 4 * NP + sizeof(uint4) * 4 * NP;
+};
+
+// B fragments per order, k-step, pair of n-tiles and lane: {b01, b23} of
+// n-tile 2q, {b01, b23} of n-tile 2q+1 (mma.m16n8k16 B layout)
+__device__ uint4 gTcB[3][TKSMAX][TNTILE / 2][32];
+__constant__ int cTcRowExp[3][9];  // FD_i: biased exponent of max_p |D_ip|
+__device__ double gTcD[3][81];     // D itself, for the line left over in a pass
 
 __device__ __forceinline__ void mma16816(float *d, const uint32_t *a, uint32_t b0, uint32_t b1) {
   asm volatile(
@@ -140,9 +151,10 @@ __device__ __forceinline__ double tc_to_double(long long T, int delta) {
   return copysign(__longlong_as_double(0x7FF0000000000000ll), d);
 }
 
-// node of point p of line L (L = l0 + 9 l1) along direction a
+// node of point p of line L (L = l0 + n l1) along direction a
+template <int N>
 __device__ __forceinline__ int tc_node(int a, int L, int p) {
-  return a == 0 ? p + TN * L : (a == 1 ? (L % TN) + TN * p + TNN * (L / TN) : L + TNN * p);
+  return a == 0 ? p + N * L : (a == 1 ? (L % N) + N * p + N * N * (L / N) : L + N * N * p);
 }
 
 // derivatives along a of field f at this lane's owned output slots (see
@@ -154,6 +166,7 @@ __device__ __forceinline__ int tc_pair(float hi, float lo) {
   return (int)(__float_as_uint(hi) * 256u + __float_as_uint(lo) - 257u * kMagic);
 }
 
+template <int N>
 __device__ __forceinline__ void tc_derivs(const uint4 *__restrict__ gB, uint32_t rowaddr,
                                           uint32_t pstep, int chunk, int lane, int tq, int emax,
                                           int fd0, int fd1, int fd8, double *dv) {
@@ -163,8 +176,8 @@ __device__ __forceinline__ void tc_derivs(const uint4 *__restrict__ gB, uint32_t
 #pragma unroll
     for (int j = 0; j < 4; j++) acc[i][j] = 12582912.f;
 #pragma unroll 1
-  for (int kk = 0; kk < TKS; kk++) {
-    const int p = min(2 * kk + chunk, TN - 1);  // the tenth point repeats the ninth
+  for (int kk = 0; kk < TcShape<N>::KS; kk++) {
+    const int p = min(2 * kk + chunk, N - 1);  // odd n: the padding point repeats the last
     uint32_t af[4];
     ldsm_x4(af, rowaddr + (uint32_t)p * pstep);
 #pragma unroll
@@ -190,25 +203,30 @@ __device__ __forceinline__ void tc_derivs(const uint4 *__restrict__ gB, uint32_t
     dv[o] = bad ? __longlong_as_double(0x7FF8000000000000ll)
                 : tc_to_double(T, emax + ((o & 1) ? fd1 : fd0) - 2100);
   }
-  // output 8: groups 2t, 2t+1 here (t = 3: group 6 and an empty column),
-  // summed over the quad
-  long long P8[2];
+  // output 8 (n = 9): groups 2t, 2t+1 here (t = 3: group 6 and an empty
+  // column), summed over the quad
+  if constexpr (N == 9) {
+    long long P8[2];
 #pragma unroll
-  for (int h = 0; h < 2; h++) {
-    const int pp = tc_pair(acc[7][2 * h], acc[7][2 * h + 1]);
-    P8[h] = tq < 3 ? ((long long)pp << (32 - 16 * tq)) : (long long)(pp >> 16);
-    P8[h] += __shfl_xor_sync(0xffffffffu, P8[h], 1);
-    P8[h] += __shfl_xor_sync(0xffffffffu, P8[h], 2);
+    for (int h = 0; h < 2; h++) {
+      const int pp = tc_pair(acc[7][2 * h], acc[7][2 * h + 1]);
+      P8[h] = tq < 3 ? ((long long)pp << (32 - 16 * tq)) : (long long)(pp >> 16);
+      P8[h] += __shfl_xor_sync(0xffffffffu, P8[h], 1);
+      P8[h] += __shfl_xor_sync(0xffffffffu, P8[h], 2);
+    }
+    dv[4] = bad ? __longlong_as_double(0x7FF8000000000000ll)
+                : tc_to_double(tq == 0 ? P8[0] : P8[1], emax + fd8 - 2100);
+  } else {
+    dv[4] = 0.;
   }
-  dv[4] = bad ? __longlong_as_double(0x7FF8000000000000ll)
-              : tc_to_double(tq == 0 ? P8[0] : P8[1], emax + fd8 - 2100);
 }
 
 // r out (mode 0) or the RK stage update (modes of StageParams), with the
 // loads of NB outputs per thread issued before their arithmetic
-template <int NT>
+template <int N, int NT>
 __device__ __forceinline__ void tc_epilogue(const StageParams &P, const double *Wg,
                                             const double *sR, int e) {
+  constexpr int TNP = TcShape<N>::NP;
   constexpr int TOT = NF * TNP, NB = 4;
   if (P.skip && P.skip[e]) return;
   const size_t base = (size_t)e * NF * TNP;
@@ -253,8 +271,10 @@ __device__ __forceinline__ void tc_epilogue(const StageParams &P, const double *
   }
 }
 
-template <int NT, int MINB>
+template <int N, int NT, int MINB>
 __global__ void __launch_bounds__(NT, MINB) tc_kernel(StageParams P) {
+  using S = TcShape<N>;
+  constexpr int TN = N, TNP = S::NP, TNN = S::NN, TTILES = S::TILES;
   constexpr int NWARP = NT / 32;
   constexpr int NLOAD = (4 * TNP + NT - 1) / NT;
   extern __shared__ __align__(16) unsigned char tsm[];
@@ -330,8 +350,10 @@ __global__ void __launch_bounds__(NT, MINB) tc_kernel(StageParams P) {
   const int warp = tid >> 5, lane = tid & 31, g = lane >> 2, tq = lane & 3;
   const int cs = sCs[0], mask = sMask;
   const uint32_t digbase = (uint32_t)__cvta_generic_to_shared(sDig);
-  const int fd0 = cTcRowExp[tq], fd1 = cTcRowExp[tq + 4], fd8 = cTcRowExp[8];
-  const uint4 *gB = &gTcB[0][0][0];
+  const int fd0 = cTcRowExp[N - 7][tq], fd1 = cTcRowExp[N - 7][min(tq + 4, 8)];
+  const int fd8 = cTcRowExp[N - 7][8];
+  const uint4 *gB = &gTcB[N - 7][0][0][0];
+  const double *gD = gTcD[N - 7];
 
   // ---- volume terms, one direction per pass; warp w takes lines 16w..16w+15 ----
 #pragma unroll 1
@@ -354,8 +376,8 @@ __global__ void __launch_bounds__(NT, MINB) tc_kernel(StageParams P) {
       for (int sl = 0; sl < 5; sl++) {
         const int L = tile * 16 + g + (sl < 4 ? (sl >> 1) * 8 : tq * 8);
         const int i = sl < 4 ? tq + (sl & 1) * 4 : TN - 1;
-        okS[sl] = L < TNN && (sl < 4 || tq < 2);
-        nodeS[sl] = okS[sl] ? tc_node(a, L, i) : 0;
+        okS[sl] = L < TNN && i < TN && (sl < 4 ? true : (TN == 9 && tq < 2));
+        nodeS[sl] = okS[sl] ? tc_node<N>(a, L, i) : 0;
 #pragma unroll
         for (int i3 = 0; i3 < 3; i3++) {
           double m = 0.;
@@ -370,8 +392,8 @@ __global__ void __launch_bounds__(NT, MINB) tc_kernel(StageParams P) {
       for (int f = 0; f < 4; f++) {  // pi, then c_x, c_y, c_z
         if (f > 0 && !((row >> (f - 1)) & 1)) continue;
         double dv[5];
-        tc_derivs(gB, rowbase + (uint32_t)(f * TNP) * 16u, pstep, chunk, lane, tq, sEmax[f], fd0,
-                  fd1, fd8, dv);
+        tc_derivs<N>(gB, rowbase + (uint32_t)(f * TNP) * 16u, pstep, chunk, lane, tq, sEmax[f],
+                     fd0, fd1, fd8, dv);
         // chain rule: r_c_i += M[a][i] d_a pi, r_pi += sum_i M[a][i] d_a c_i
 #pragma unroll
         for (int sl = 0; sl < 5; sl++) {
@@ -393,16 +415,17 @@ __global__ void __launch_bounds__(NT, MINB) tc_kernel(StageParams P) {
       for (int sl = 0; sl < 5; sl++)
         if (okS[sl]) sR[nodeS[sl]] += rp[sl];
     }
-    if (warp == TTILES % NWARP && lane < TN) {
-      // line 80 (l0 = l1 = 8): output i of lane i as an FP64 dot product with D
-      const int i = lane, L = TNN - 1, node = tc_node(a, L, i);
+    if (S::LAST && warp == TTILES % NWARP && lane < TN) {
+      // the line left over (l0 = l1 = n - 1): output i of lane i as an FP64
+      // dot product with D
+      const int i = lane, L = TNN - 1, node = tc_node<N>(a, L, i);
       double d[4] = {0., 0., 0., 0.};
 #pragma unroll
       for (int f = 0; f < 4; f++) {
         if (f > 0 && !((row >> (f - 1)) & 1)) continue;
 #pragma unroll
         for (int p = 0; p < TN; p++)
-          d[f] = fma(__ldg(gTcD + i * TN + p), __ldg(Wg + f * TNP + tc_node(a, L, p)), d[f]);
+          d[f] = fma(__ldg(gD + i * TN + p), __ldg(Wg + f * TNP + tc_node<N>(a, L, p)), d[f]);
       }
       double rpl = 0.;
 #pragma unroll
@@ -421,20 +444,21 @@ __global__ void __launch_bounds__(NT, MINB) tc_kernel(StageParams P) {
   }
   // interior states of the faces and r_phi = pi come from w in global memory
   face_terms<TN, 1, NT>(P, Wg, sR, sCs, sG, e0, t);
-  tc_epilogue<NT>(P, Wg, sR, e);
+  tc_epilogue<N, NT>(P, Wg, sR, e);
 }
 
-template <int NT, int MINB>
+template <int N, int NT, int MINB>
 cudaError_t launch_tc(const StageParams &P, cudaStream_t st) {
+  constexpr size_t smem = TcShape<N>::SMEM;
   if (P.nelem <= 0) {
-    cudaError_t e = cudaFuncSetAttribute(tc_kernel<NT, MINB>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
+    cudaError_t e = cudaFuncSetAttribute(tc_kernel<N, NT, MINB>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(tc_kernel<NT, MINB>,
+    return cudaFuncSetAttribute(tc_kernel<N, NT, MINB>,
                                 cudaFuncAttributePreferredSharedMemoryCarveout, 100);
   }
   const int ne = P.ecount > 0 ? P.ecount : P.nelem;
-  tc_kernel<NT, MINB><<<ne, NT, kTcSmem, st>>>(P);
+  tc_kernel<N, NT, MINB><<<ne, NT, smem, st>>>(P);
   return cudaGetLastError();
 }
 
@@ -463,37 +487,47 @@ uint16_t half_of_int(int v) {  // exact for |v| < 2048
 }  // namespace
 
 int tc_variants(int n, Variant *out, int cap) {
-  if (n != TN) return 0;
   int k = 0;
-  // three CTAs of 192 threads (96 registers: 5 warps of a sub-partition's
-  // 16 K registers) or two of 256 per SM; three of 160 threads without
-  // spills (128 registers) ran slower (3.51 vs 3.14 ms per stage)
-  if (k < cap) out[k++] = Variant{"tc", 1, 192, launch_tc<192, 3>};
-  if (k < cap) out[k++] = Variant{"tc", 1, 256, launch_tc<256, 2>};
+  if (n == 9) {
+    // three CTAs of 192 threads (96 registers: 5 warps of a sub-partition's
+    // 16 K registers) or two of 256 per SM; three of 160 threads without
+    // spills (128 registers) ran slower (3.51 vs 3.14 ms per stage)
+    if (k < cap) out[k++] = Variant{"tc", 1, 192, launch_tc<9, 192, 3>};
+    if (k < cap) out[k++] = Variant{"tc", 1, 256, launch_tc<9, 256, 2>};
+  } else if (n == 8) {  // 4 tiles of 16 lines: one warp each
+    if (k < cap) out[k++] = Variant{"tc", 1, 128, launch_tc<8, 128, 4>};
+    if (k < cap) out[k++] = Variant{"tc", 1, 256, launch_tc<8, 256, 2>};
+  } else if (n == 7) {  // 3 tiles and the line left over
+    if (k < cap) out[k++] = Variant{"tc", 1, 128, launch_tc<7, 128, 4>};
+    if (k < cap) out[k++] = Variant{"tc", 1, 256, launch_tc<7, 256, 2>};
+  }
   return k;
 }
 
 cudaError_t tc_upload(int n, const double *D) {
-  if (n != TN) return cudaSuccess;
+  if (n < 7 || n > 9) return cudaSuccess;
+  const int ks = (n + 1) / 2;
   // per row: exponent and digits of |D_ip|
-  int fd[TN];
-  unsigned long long Y[TN][TN];
-  int sg[TN][TN];
-  for (int i = 0; i < TN; i++) {
+  int fd[9] = {};
+  unsigned long long Y[9][9] = {};
+  int sg[9][9] = {};
+  for (int i = 0; i < n; i++) {
     int mx = 0;
-    for (int p = 0; p < TN; p++) {
+    for (int p = 0; p < n; p++) {
       uint64_t b;
-      std::memcpy(&b, &D[i * TN + p], 8);
+      std::memcpy(&b, &D[i * n + p], 8);
       mx = std::max(mx, (int)(b >> 52) & 0x7FF);
     }
     fd[i] = mx;
-    for (int p = 0; p < TN; p++) {
-      Y[i][p] = digits56(D[i * TN + p], mx);
-      sg[i][p] = D[i * TN + p] < 0 ? -1 : 1;
+    for (int p = 0; p < n; p++) {
+      Y[i][p] = digits56(D[i * n + p], mx);
+      sg[i][p] = D[i * n + p] < 0 ? -1 : 1;
     }
   }
-  // B[K = 8 p + s][column], column = 8 nt + 2 t + j <-> slot 2 nt + j of quad thread t
-  static uint16_t B[TKS * 16][TNTILE * 8];
+  // B[K = 8 p + s][column], column = 8 nt + 2 t + j <-> slot 2 nt + j of quad
+  // thread t: slots 0..6 groups of output t, 7..13 of output t+4, 14..15
+  // groups 2t, 2t+1 of output 8
+  static uint16_t B[TKSMAX * 16][TNTILE * 8];
   std::memset(B, 0, sizeof(B));
   for (int col = 0; col < TNTILE * 8; col++) {
     const int nt = col / 8, c8 = col % 8, t = c8 / 2, j = c8 % 2, sl = 2 * nt + j;
@@ -501,8 +535,8 @@ cudaError_t tc_upload(int n, const double *D) {
     if (sl < 7) { i = t; w = sl; }
     else if (sl < 14) { i = t + 4; w = sl - 7; }
     else { i = 8; w = 2 * t + (sl - 14); }
-    if (i >= TN || w >= TG) continue;
-    for (int p = 0; p < TN; p++)
+    if (i >= n || w >= TG) continue;
+    for (int p = 0; p < n; p++)
       for (int s = 0; s < TG; s++) {
         const int tt = w - s;
         if (tt < 0 || tt >= TG) continue;
@@ -510,8 +544,9 @@ cudaError_t tc_upload(int n, const double *D) {
         B[8 * p + s][col] = half_of_int(sg[i][p] * dig);
       }
   }
-  static uint4 F[TKS][TNTILE / 2][32];
-  for (int kk = 0; kk < TKS; kk++)
+  static uint4 F[TKSMAX][TNTILE / 2][32];
+  std::memset(F, 0, sizeof(F));
+  for (int kk = 0; kk < ks; kk++)
     for (int q = 0; q < TNTILE / 2; q++)
       for (int lane = 0; lane < 32; lane++) {
         const int g = lane >> 2, t = lane & 3;
@@ -525,10 +560,14 @@ cudaError_t tc_upload(int n, const double *D) {
         }
         F[kk][q][lane] = make_uint4(r[0], r[1], r[2], r[3]);
       }
-  cudaError_t err = cudaMemcpyToSymbol(gTcB, F, sizeof(F));
+  const size_t slot = (size_t)(n - 7);
+  cudaError_t err = cudaMemcpyToSymbol(gTcB, F, sizeof(F), sizeof(F) * slot);
   if (err != cudaSuccess) return err;
-  if ((err = cudaMemcpyToSymbol(gTcD, D, sizeof(double) * TN * TN)) != cudaSuccess) return err;
-  return cudaMemcpyToSymbol(cTcRowExp, fd, sizeof(fd));
+  double Dp[81] = {};
+  for (int q = 0; q < n * n; q++) Dp[q] = D[q];
+  if ((err = cudaMemcpyToSymbol(gTcD, Dp, sizeof(Dp), sizeof(Dp) * slot)) != cudaSuccess)
+    return err;
+  return cudaMemcpyToSymbol(cTcRowExp, fd, sizeof(fd), sizeof(fd) * slot);
 }
 
 }  // namespace nmgk

@@ -1,4 +1,4 @@
-"""The tensor-core stage kernel ("tc", n = 9).  Its directional derivatives
+"""The tensor-core stage kernel ("tc", n = 7, 8, 9; most cases at 9, the benchmark's order).  Its directional derivatives
 are exact integer digit products on the FP16 tensor cores: seven signed
 8-bit digits per value on a per-element-field fixed-point grid, seven digit
 groups summed in FP32 without rounding, recombined in 64-bit integers into
@@ -195,3 +195,48 @@ def test_tc_other_integrators_vs_oracle(method):
     got = ev.evolve_steps_host(u, 0.0, dt, 4)
     want = oracle_for(m, bc=1).evolve(u, dt, 4, method=method)
     assert rel_l2(got, want) <= RTOL_RK4
+
+
+@pytest.mark.parametrize("variant", ["tc:1:128", "tc:1:256"])
+@pytest.mark.parametrize("n", [7, 8])
+def test_tc_orders_7_8_outgoing_vs_oracle(n, variant):
+    """The tensor-core kernel at 7 and 8 points per direction (3 tiles and
+    the line left over; 4 tiles)."""
+    m = ng.Mesh.build(ng.MESH_CUBEDSPHERES7, n=n, luni=1, cs_dc=1.0, cs_r0fac=20.0)
+    u = gaussian_pulses(m.coords(), seed=70 + n, rmin=1.0, rmax=6.0)
+    u += 1e-3 * np.random.default_rng(n).standard_normal(u.shape)
+    o = oracle_for(m, bc=1)
+    ev = ng.Evolution(m, ng.BC_OUTGOING)
+    ev.set_kernel(variant)
+    assert rel_l2(ev.rhs(u, 0.0), o.rhs(u, 0.0)) <= RTOL_RHS
+    dt = 0.02 / n ** 2
+    assert rel_l2(ev.rk4_steps_host(u, 0.0, dt, 3), o.rk4(u, dt, 3)) <= RTOL_RK4
+    ev.set_state(u)
+    ev.rk4_steps(0.0, dt, 3)
+    assert np.array_equal(ev.rk4_steps_host(u, 0.0, dt, 3), ev.get_state())
+
+
+@pytest.mark.parametrize("n", [7, 8])
+def test_tc_orders_7_8_periodic_box_vs_oracle(n):
+    m = ng.Mesh.build(ng.MESH_BOX, n=n, luni=1, xc=(PI, PI, PI), box_dout=PI, periodic=True)
+    u = np.random.default_rng(n).standard_normal((m.nelem, 5, m.np))
+    o = oracle_for(m, bc=1, period=2 * PI)
+    ev = ng.Evolution(m, ng.BC_OUTGOING)
+    ev.set_kernel("tc")
+    assert rel_l2(ev.rhs(u, 0.0), o.rhs(u, 0.0)) <= RTOL_RHS
+
+
+def test_tc_order7_mixed_mesh_matches_reference():
+    """The reference's own run of a mixed mesh at 7 points (inner cube finite
+    volume, shells DG), with the tensor-core kernel for the DG elements."""
+    d, meta = load("mixcs7_l0_n7_w5dnfn")
+    m = build_mesh(meta)
+    perm = perm_to_mesh(m, d)
+    ev = ng.Evolution(m, ng.BC_EXACT_PLANEWAVE, k=meta["k"])
+    ev.set_fv(meta["fv"]["rec"], meta["fv"]["extrap"])
+    ev.set_kernel("tc")
+    ev.set_kernel("fvx")
+    r = ev.rhs(to_mesh_order(d["u0"], perm), 0.0)
+    assert rel_l2(r[perm], d["r0"]) <= RTOL_RHS
+    u = ev.rk4_steps_host(to_mesh_order(d["u0"], perm), 0.0, meta["dt"], meta["steps"])
+    assert rel_l2(u[perm], d["u_final"]) <= RTOL_RK4
