@@ -560,7 +560,9 @@ int nmg_rk4_step_noalloc(nmg_ctx *c, double t, double dt, const double *u_in_dev
  * mesh and keeps the fastest.  spec = "auto" re-tunes; a name such as "eo",
  * "gather" or "tc", or "<name>:<elements per CTA>:<threads>", forces a
  * variant (the environment variable NMG_KERNEL does the same for new
- * contexts). */
+ * contexts).  "vjp" and "tcvjp" choose the transposed kernel of the adjoint
+ * entry points (FP64 line transforms, or the tensor-core digit products,
+ * the default where compiled: n = 7, 8, 9). */
 int nmg_set_kernel(nmg_ctx *c, const char *spec);
 /* selected variant, candidates and tuning timings as text */
 int nmg_kernel_info(nmg_ctx *c, char *buf, int32_t len);

@@ -668,8 +668,10 @@ class Evolution:
         return s_
 
     def set_kernel(self, spec="auto"):
-        """Force a stage-kernel variant ("eo", "gather", "eo:<epb>:<threads>")
-        or re-enable the autotuner ("auto")."""
+        """Force a stage-kernel variant ("eo", "gather", "tc",
+        "<name>:<epb>:<threads>"), choose the transposed kernel of the
+        adjoint ("vjp": FP64, "tcvjp": tensor cores, the default at
+        n = 7..9), or re-enable the autotuner ("auto")."""
         self._check(lib().nmg_set_kernel(self._h, spec.encode()), "nmg_set_kernel")
 
     def kernel_info(self):

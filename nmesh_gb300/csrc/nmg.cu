@@ -264,7 +264,9 @@ struct nmg_ctx {
   double k[3] = {0, 0, 0};
   cudaStream_t stream = nullptr;
   Variant variants[kMaxVariants];
-  Variant vjp;  // transposed stage kernel
+  Variant vjp;  // transposed stage kernel (the tensor-core one where compiled)
+  Variant vjp_alt[2];  // the FP64 and the tensor-core transposed kernels
+  int nvjp_alt = 0;
   int nvariants = 0;
   int sel = -1;      // selected variant, -1: autotune on first use
   bool tuned = false;
@@ -965,8 +967,10 @@ static int create_impl(const nmg_mesh *m, int32_t bc_kind, const double k[3], bo
     c->nvariants += nmgk::tc_variants(m->n, c->variants + c->nvariants,
                                       kMaxVariants - c->nvariants);
     if (c->nvariants == 0) return set_err(c, NMG_EUNSUP, "nmg_create: n must be in [2,12]");
-    if (nmgk::vjp_variants(m->n, &c->vjp, 1) != 1)
+    if (nmgk::vjp_variants(m->n, &c->vjp_alt[0], 1) != 1)
       return set_err(c, NMG_EUNSUP, "nmg_create: no transposed kernel for this n");
+    c->nvjp_alt = 1 + nmgk::tcvjp_variants(m->n, &c->vjp_alt[1], 1);
+    c->vjp = c->vjp_alt[c->nvjp_alt - 1];  // the tensor-core one where it exists
   }
   int dev = 0;
   CK(cudaGetDevice(&dev));
@@ -1314,7 +1318,7 @@ static int create_impl(const nmg_mesh *m, int32_t bc_kind, const double k[3], bo
   if (!c->fv) {
     StageParams P0;
     std::memset(&P0, 0, sizeof(P0));
-    CK(c->vjp.launch(P0, c->stream));
+    for (int v = 0; v < c->nvjp_alt; v++) CK(c->vjp_alt[v].launch(P0, c->stream));
   } else {
     for (int v = c->mixed ? c->ndg : 0; v < c->nvariants; v++) {
       StageParams P0;
@@ -2078,6 +2082,12 @@ int nmg_set_kernel(nmg_ctx *c, const char *spec) {
     c->ftuned = false;
     drop_graphs(c);
     return NMG_OK;
+  }
+  for (int v = 0; v < c->nvjp_alt; v++) {  // the transposed kernel ("vjp" or "tcvjp")
+    if (!strcmp(spec, c->vjp_alt[v].name)) {
+      c->vjp = c->vjp_alt[v];
+      return NMG_OK;
+    }
   }
   for (int v = 0; v < c->nvariants; v++) {
     char buf[64];

@@ -353,6 +353,135 @@ __device__ __forceinline__ void epilogue(const StageParams &P, const double *sW,
   }
 }
 
+// Transposed face terms and epilogue of the vector-Jacobian stage (shared by
+// the FP64 and the tensor-core transposed kernels): sW holds rbar (pi, c) of
+// the CTA's elements ([field][EPB][NP]; for one element a pointer into rbar
+// in global memory works too), sR the transposed volume terms.
+template <int N, int EPB, int NT>
+__device__ __forceinline__ void vjp_faces_epilogue(const StageParams &P, const double *sW,
+                                                   double *sR, const int *sCs,
+                                                   const double (*sG)[3], int e0) {
+  constexpr int NP = N * N * N, NN = N * N;
+  const int tid = threadIdx.x;
+  // ---- transposed face terms, one direction at a time ----
+#pragma unroll 1
+  for (int d = 0; d < 3; d++) {
+    for (int q = tid; q < EPB * 2 * NN; q += NT) {
+      const int le = q / (2 * NN), rem = q - le * 2 * NN, s = rem / NN, ab = rem - s * NN;
+      const int e = e0 + le;
+      if (e >= P.nelem) continue;
+      const int a = ab % N, b = ab / N, f = 2 * d + s;
+      const int node = face_node_d<N>(f, a, b);
+      const double rp = sW[(0 * EPB + le) * NP + node];
+      const double rc0 = sW[(1 * EPB + le) * NP + node];
+      const double rc1 = sW[(2 * EPB + le) * NP + node];
+      const double rc2 = sW[(3 * EPB + le) * NP + node];
+      double gn0, gn1, gn2, g;
+      const int cs = sCs[le];
+      if (cs < 0) {
+        g = sG[le][d];
+        const double sg = (f & 1) ? g : -g;
+        gn0 = d == 0 ? sg : 0.;
+        gn1 = d == 1 ? sg : 0.;
+        gn2 = d == 2 ? sg : 0.;
+      } else {
+        const double2 *F2 = reinterpret_cast<const double2 *>(P.fac) +
+                            (((size_t)cs * 6 + f) * NN + ab) * 2;
+        const double2 fa = __ldg(F2), fb = __ldg(F2 + 1);
+        gn0 = fa.x; gn1 = fa.y; gn2 = fb.x; g = fb.y;
+      }
+      double dp, dc0, dc1, dc2;
+      const int nbe = __ldg(P.nb + e * 6 + f);
+      if (nbe >= 0 || P.bc == NMG_BC_EXACT_PLANEWAVE) {
+        dp = -fma(g, rp, fma(gn0, rc0, fma(gn1, rc1, gn2 * rc2)));
+        dc0 = -fma(gn0, rp, g * rc0);
+        dc1 = -fma(gn1, rp, g * rc1);
+        dc2 = -fma(gn2, rp, g * rc2);
+        const int cdh = nbe >= 0 ? __ldg(P.code + e * 6 + f) : 0;
+        if (cdh & kCodeMixed) {
+          // non-conforming face: the neighbours' part, transposed through
+          // the trace interpolation, waits in this face's slot
+          const double *T = P.ghost + (size_t)__ldg(P.bslot + e * 6 + f) * 4 * NN + ab;
+          dp += T[0];
+          dc0 += T[NN];
+          dc1 += T[2 * NN];
+          dc2 += T[3 * NN];
+        } else if (nbe >= 0) {
+          const int cd = cdh, f2 = cd & 7, o = cd >> 3;
+          const int sw = o & 1, fa = (o >> 1) & 1, fb = (o >> 2) & 1;
+          int aa = sw ? b : a, bb = sw ? a : b;
+          aa = fa ? N - 1 - aa : aa;
+          bb = fb ? N - 1 - bb : bb;
+          const double *W2 = P.win + (size_t)nbe * NF * NP + face_node_d<N>(f2, aa, bb);
+          const double yp = __ldg(W2), yc0 = __ldg(W2 + NP), yc1 = __ldg(W2 + 2 * NP),
+                       yc2 = __ldg(W2 + 3 * NP);
+          double hn0, hn1, hn2, h;
+          const int cs2 = __ldg(P.cslot + nbe);
+          if (cs2 < 0) {
+            const int d2 = f2 >> 1;
+            h = __ldg(P.gcart + nbe * 3 + d2);
+            const double sg = (f2 & 1) ? h : -h;
+            hn0 = d2 == 0 ? sg : 0.;
+            hn1 = d2 == 1 ? sg : 0.;
+            hn2 = d2 == 2 ? sg : 0.;
+          } else {
+            const double2 *F2 = reinterpret_cast<const double2 *>(P.fac) +
+                                (((size_t)cs2 * 6 + f2) * NN + aa + N * bb) * 2;
+            const double2 fa2 = __ldg(F2), fb2 = __ldg(F2 + 1);
+            hn0 = fa2.x; hn1 = fa2.y; hn2 = fb2.x; h = fb2.y;
+          }
+          dp += fma(h, yp, fma(hn0, yc0, fma(hn1, yc1, hn2 * yc2)));
+          dc0 += fma(hn0, yp, h * yc0);
+          dc1 += fma(hn1, yp, h * yc1);
+          dc2 += fma(hn2, yp, h * yc2);
+        }
+      } else {
+        // outgoing radiation
+        const int bs = __ldg(P.bslot + e * 6 + f);
+        const double *Nr = P.bnrm + (size_t)bs * 3 * NN + ab;
+        const double n0 = Nr[0], n1 = Nr[NN], n2 = Nr[2 * NN];
+        const double gsb = g * fma(n0, rc0, fma(n1, rc1, fma(n2, rc2, rp)));
+        dp = -gsb;
+        dc0 = -gsb * n0;
+        dc1 = -gsb * n1;
+        dc2 = -gsb * n2;
+      }
+      sR[(0 * EPB + le) * NP + node] += dp;
+      sR[(1 * EPB + le) * NP + node] += dc0;
+      sR[(2 * EPB + le) * NP + node] += dc1;
+      sR[(3 * EPB + le) * NP + node] += dc2;
+    }
+    __syncthreads();
+  }
+
+  // ---- epilogue: wbar = (pibar + rbar_phi, cbar, 0) ----
+  for (int q = tid; q < EPB * NF * NP; q += NT) {
+    const int le = q / (NF * NP), rem = q - le * NF * NP, f = rem / NP, node = rem - f * NP;
+    const int e = e0 + le;
+    if (e >= P.nelem) continue;
+    const size_t idx = ((size_t)e * NF + f) * NP + node;
+    double r;
+    if (f == 0)
+      r = sR[le * NP + node] + __ldg(P.win + ((size_t)e * NF + 4) * NP + node);
+    else if (f < 4)
+      r = sR[(f * EPB + le) * NP + node];
+    else
+      r = 0.;
+    if (P.mode == 0) {
+      P.rout[idx] = r;
+    } else if (P.mode == 1) {
+      const double u = __ldg(P.u0 + idx);
+      P.acc[idx] = fma(P.cacc, r, u);
+      P.wout[idx] = fma(P.cw, r, u);
+    } else if (P.mode == 4) {
+      P.acc[idx] = fma(P.cacc, r, P.acc[idx]);
+    } else {
+      P.acc[idx] = fma(P.cacc, r, P.acc[idx]);
+      P.wout[idx] = fma(P.cw, r, __ldg(P.u0 + idx));
+    }
+  }
+}
+
 // host-side launch entry points of the kernel variants
 typedef cudaError_t (*LaunchFn)(const StageParams &, cudaStream_t);
 struct Variant {
@@ -365,8 +494,10 @@ int gather_variants(int n, Variant *out, int cap);
 int eo_variants(int n, Variant *out, int cap);
 // tensor-core variant: derivatives by exact integer digit products (n = 9)
 int tc_variants(int n, Variant *out, int cap);
-// digits of D for the tensor-core variant (no-op for other n)
+// digits of D and D^T for the tensor-core variants (no-op for other n)
 cudaError_t tc_upload(int n, const double *D);
+// tensor-core transposed (vector-Jacobian) stage kernel for n = 7, 8, 9
+int tcvjp_variants(int n, Variant *out, int cap);
 // transposed (vector-Jacobian) stage kernel for n
 int vjp_variants(int n, Variant *out, int cap);
 // batched persistent kernel over element groups of different n (2..10)

@@ -87,6 +87,10 @@ struct TcShape {
 __device__ uint4 gTcB[3][TKSMAX][TNTILE / 2][32];
 __constant__ int cTcRowExp[3][9];  // FD_i: biased exponent of max_p |D_ip|
 __device__ double gTcD[3][81];     // D itself, for the line left over in a pass
+// the same for D^T (the transposed, vector-Jacobian stage)
+__device__ uint4 gTcBT[3][TKSMAX][TNTILE / 2][32];
+__constant__ int cTcRowExpT[3][9];
+__device__ double gTcDT[3][81];
 
 __device__ __forceinline__ void mma16816(float *d, const uint32_t *a, uint32_t b0, uint32_t b1) {
   asm volatile(
@@ -447,6 +451,169 @@ __global__ void __launch_bounds__(NT, MINB) tc_kernel(StageParams P) {
   tc_epilogue<N, NT>(P, Wg, sR, e);
 }
 
+// Transposed stage (vector-Jacobian product, wbar = L^T rbar; the FP64
+// form and the face terms are vjp_kernel's in stage_eo.cu): per direction a
+// the fields y_pi = sum_i M[a][i] rbar_c_i and y_c_i = M[a][i] rbar_pi are
+// formed in FP64 at every node, split into digits on their own grids, and
+// D^T applied along a on the tensor cores adds into pibar, cbar_i.
+template <int N, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) tcvjp_kernel(StageParams P) {
+  using S = TcShape<N>;
+  constexpr int TN = N, TNP = S::NP, TNN = S::NN, TTILES = S::TILES;
+  constexpr int NWARP = NT / 32;
+  constexpr int NLOAD = (4 * TNP + NT - 1) / NT;
+  extern __shared__ __align__(16) unsigned char tsm[];
+  double *sR = reinterpret_cast<double *>(tsm);           // [4][NP]: pibar, cbar
+  uint4 *sDig = reinterpret_cast<uint4 *>(sR + 4 * TNP);  // [4][NP] digits of y
+  __shared__ int sCs[1];
+  __shared__ int sMask;
+  __shared__ int sEmax[3][4];
+  __shared__ double sScale[3];
+  __shared__ double sG[1][3];
+
+  const int e = blockIdx.x;
+  if (e >= P.nelem) return;
+  const int tid = threadIdx.x;
+  const double *Wg = P.win + (size_t)e * NF * TNP;  // rbar of this element
+  if (tid == 0) {
+    const int cs = P.cslot[e];
+    if (cs >= 0) {
+      tc_prefetch_l2(P.metric + (size_t)cs * 9 * TNP, sizeof(double) * 9 * TNP);
+      tc_prefetch_l2(P.fac + (size_t)cs * 6 * TNN * 4, sizeof(double) * 6 * TNN * 4);
+    }
+    sCs[0] = cs;
+    sMask = cs >= 0 ? P.cmask[cs] : (1 | (1 << 4) | (1 << 8));
+    for (int d = 0; d < 3; d++) sScale[d] = P.scale[e * 3 + d];
+    for (int d = 0; d < 3; d++) sG[0][d] = P.gcart[e * 3 + d];
+  }
+  if (tid < 12) sEmax[tid / 4][tid % 4] = 0;
+  for (int q = tid; q < 4 * TNP; q += NT) sR[q] = 0.;
+  __syncthreads();
+  const int warp = tid >> 5, lane = tid & 31, g = lane >> 2, tq = lane & 3;
+  const int cs = sCs[0], mask = sMask;
+  const uint32_t digbase = (uint32_t)__cvta_generic_to_shared(sDig);
+  const int fd0 = cTcRowExpT[N - 7][tq], fd1 = cTcRowExpT[N - 7][min(tq + 4, 8)];
+  const int fd8 = cTcRowExpT[N - 7][8];
+  const uint4 *gB = &gTcBT[N - 7][0][0][0];
+  const double *gD = gTcDT[N - 7];
+  const double *Mg = cs >= 0 ? P.metric + (size_t)cs * 9 * TNP : nullptr;  // [a*3+i][node]
+
+#pragma unroll 1
+  for (int a = 0; a < 3; a++) {
+    const int row = (mask >> (3 * a)) & 7;
+    // y at every node, in FP64 (one thread takes all four fields of its
+    // nodes: rbar and the metric row read once), and each field's largest
+    // exponent
+    {
+      constexpr int NNODE = (TNP + NT - 1) / NT;
+      double y[4][NNODE];
+      int em[4] = {0, 0, 0, 0};
+#pragma unroll
+      for (int k = 0; k < NNODE; k++) {
+        const int node = tid + k * NT;
+        double rp = 0., rc[3] = {0., 0., 0.}, m[3] = {0., 0., 0.};
+        if (node < TNP) {
+          rp = __ldg(Wg + node);
+#pragma unroll
+          for (int i3 = 0; i3 < 3; i3++)
+            if ((row >> i3) & 1) {
+              rc[i3] = __ldg(Wg + (1 + i3) * TNP + node);
+              m[i3] = Mg ? __ldg(Mg + (a * 3 + i3) * TNP + node) : sScale[a];
+            }
+        }
+        double y0 = 0.;
+#pragma unroll
+        for (int i3 = 0; i3 < 3; i3++) {
+          y0 = fma(m[i3], rc[i3], y0);
+          y[1 + i3][k] = m[i3] * rp;
+        }
+        y[0][k] = y0;
+#pragma unroll
+        for (int f = 0; f < 4; f++)
+          em[f] = max(em[f], (int)((unsigned long long)__double_as_longlong(y[f][k]) >> 52) & 0x7FF);
+      }
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        const unsigned mx = __reduce_max_sync(0xffffffffu, (unsigned)em[j]);
+        if (lane == 0) atomicMax(&sEmax[a][j], (int)mx);
+      }
+      __syncthreads();
+#pragma unroll
+      for (int k = 0; k < NNODE; k++) {
+        const int node = tid + k * NT;
+        if (node < TNP)
+#pragma unroll
+          for (int f = 0; f < 4; f++) sDig[f * TNP + node] = tc_digits(y[f][k], sEmax[a][f]);
+      }
+      __syncthreads();
+    }
+#pragma unroll 1
+    for (int tile = warp; tile < TTILES; tile += NWARP) {
+      const int Lr = min(tile * 16 + (lane & 15), TNN - 1), chunk = lane >> 4;
+      const int ps = a == 0 ? 1 : (a == 1 ? TN : TNN);
+      const int nb = a == 0 ? TN * Lr : (a == 1 ? (Lr % TN) + TNN * (Lr / TN) : Lr);
+      const uint32_t rowbase = digbase + (uint32_t)nb * 16u, pstep = (uint32_t)ps * 16u;
+      int nodeS[5];
+      bool okS[5];
+#pragma unroll
+      for (int sl = 0; sl < 5; sl++) {
+        const int L = tile * 16 + g + (sl < 4 ? (sl >> 1) * 8 : tq * 8);
+        const int i = sl < 4 ? tq + (sl & 1) * 4 : TN - 1;
+        okS[sl] = L < TNN && i < TN && (sl < 4 ? true : (TN == 9 && tq < 2));
+        nodeS[sl] = okS[sl] ? tc_node<N>(a, L, i) : 0;
+      }
+#pragma unroll 1
+      for (int f = 0; f < 4; f++) {
+        if (f == 0 ? row == 0 : !((row >> (f - 1)) & 1)) continue;
+        double dv[5];
+        tc_derivs<N>(gB, rowbase + (uint32_t)(f * TNP) * 16u, pstep, chunk, lane, tq,
+                     sEmax[a][f], fd0, fd1, fd8, dv);
+#pragma unroll
+        for (int sl = 0; sl < 5; sl++)
+          if (okS[sl]) sR[f * TNP + nodeS[sl]] += dv[sl];
+      }
+    }
+    if (S::LAST && warp == TTILES % NWARP && lane < TN) {
+      // the line left over: output i of lane i, FP64, y formed again
+      const int i = lane, L = TNN - 1;
+      double d[4] = {0., 0., 0., 0.};
+#pragma unroll 1
+      for (int p = 0; p < TN; p++) {
+        const int nd = tc_node<N>(a, L, p);
+        const double dt = __ldg(gD + i * TN + p), rp = __ldg(Wg + nd);
+        double y0 = 0.;
+#pragma unroll
+        for (int i3 = 0; i3 < 3; i3++)
+          if ((row >> i3) & 1) {
+            const double m = Mg ? __ldg(Mg + (a * 3 + i3) * TNP + nd) : sScale[a];
+            y0 = fma(m, __ldg(Wg + (1 + i3) * TNP + nd), y0);
+            d[1 + i3] = fma(dt, m * rp, d[1 + i3]);
+          }
+        d[0] = fma(dt, y0, d[0]);
+      }
+      const int node = tc_node<N>(a, L, i);
+#pragma unroll
+      for (int f = 0; f < 4; f++) sR[f * TNP + node] += d[f];
+    }
+    __syncthreads();
+  }
+  vjp_faces_epilogue<N, 1, NT>(P, Wg, sR, sCs, sG, e);
+}
+
+template <int N, int NT, int MINB>
+cudaError_t launch_tcvjp(const StageParams &P, cudaStream_t st) {
+  constexpr size_t smem = TcShape<N>::SMEM;
+  if (P.nelem <= 0) {
+    cudaError_t e = cudaFuncSetAttribute(tcvjp_kernel<N, NT, MINB>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(tcvjp_kernel<N, NT, MINB>,
+                                cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  }
+  tcvjp_kernel<N, NT, MINB><<<P.nelem, NT, smem, st>>>(P);
+  return cudaGetLastError();
+}
+
 template <int N, int NT, int MINB>
 cudaError_t launch_tc(const StageParams &P, cudaStream_t st) {
   constexpr size_t smem = TcShape<N>::SMEM;
@@ -504,26 +671,36 @@ int tc_variants(int n, Variant *out, int cap) {
   return k;
 }
 
-cudaError_t tc_upload(int n, const double *D) {
-  if (n < 7 || n > 9) return cudaSuccess;
+namespace {
+
+// B fragments, row exponents and the matrix itself of an n x n matrix X
+// (row-major, rows = outputs) for the tensor-core kernels
+struct TcMatrix {
+  uint4 F[TKSMAX][TNTILE / 2][32];
+  int fd[9];
+  double X[81];
+};
+
+void tc_build(int n, const double *X, TcMatrix &out) {
   const int ks = (n + 1) / 2;
-  // per row: exponent and digits of |D_ip|
-  int fd[9] = {};
+  // per row: exponent and digits of |X_ip|
   unsigned long long Y[9][9] = {};
   int sg[9][9] = {};
+  std::memset(&out, 0, sizeof(out));
   for (int i = 0; i < n; i++) {
     int mx = 0;
     for (int p = 0; p < n; p++) {
       uint64_t b;
-      std::memcpy(&b, &D[i * n + p], 8);
+      std::memcpy(&b, &X[i * n + p], 8);
       mx = std::max(mx, (int)(b >> 52) & 0x7FF);
     }
-    fd[i] = mx;
+    out.fd[i] = mx;
     for (int p = 0; p < n; p++) {
-      Y[i][p] = digits56(D[i * n + p], mx);
-      sg[i][p] = D[i * n + p] < 0 ? -1 : 1;
+      Y[i][p] = digits56(X[i * n + p], mx);
+      sg[i][p] = X[i * n + p] < 0 ? -1 : 1;
     }
   }
+  for (int q = 0; q < n * n; q++) out.X[q] = X[q];
   // B[K = 8 p + s][column], column = 8 nt + 2 t + j <-> slot 2 nt + j of quad
   // thread t: slots 0..6 groups of output t, 7..13 of output t+4, 14..15
   // groups 2t, 2t+1 of output 8
@@ -544,8 +721,6 @@ cudaError_t tc_upload(int n, const double *D) {
         B[8 * p + s][col] = half_of_int(sg[i][p] * dig);
       }
   }
-  static uint4 F[TKSMAX][TNTILE / 2][32];
-  std::memset(F, 0, sizeof(F));
   for (int kk = 0; kk < ks; kk++)
     for (int q = 0; q < TNTILE / 2; q++)
       for (int lane = 0; lane < 32; lane++) {
@@ -558,16 +733,41 @@ cudaError_t tc_upload(int n, const double *D) {
           r[2 * h] = b0 | (b1 << 16);
           r[2 * h + 1] = b2 | (b3 << 16);
         }
-        F[kk][q][lane] = make_uint4(r[0], r[1], r[2], r[3]);
+        out.F[kk][q][lane] = make_uint4(r[0], r[1], r[2], r[3]);
       }
+}
+
+}  // namespace
+
+int tcvjp_variants(int n, Variant *out, int cap) {
+  if (cap < 1) return 0;
+  if (n == 9) { out[0] = Variant{"tcvjp", 1, 192, launch_tcvjp<9, 192, 3>}; return 1; }
+  if (n == 8) { out[0] = Variant{"tcvjp", 1, 128, launch_tcvjp<8, 128, 4>}; return 1; }
+  if (n == 7) { out[0] = Variant{"tcvjp", 1, 128, launch_tcvjp<7, 128, 4>}; return 1; }
+  return 0;
+}
+
+cudaError_t tc_upload(int n, const double *D) {
+  if (n < 7 || n > 9) return cudaSuccess;
   const size_t slot = (size_t)(n - 7);
-  cudaError_t err = cudaMemcpyToSymbol(gTcB, F, sizeof(F), sizeof(F) * slot);
-  if (err != cudaSuccess) return err;
-  double Dp[81] = {};
-  for (int q = 0; q < n * n; q++) Dp[q] = D[q];
-  if ((err = cudaMemcpyToSymbol(gTcD, Dp, sizeof(Dp), sizeof(Dp) * slot)) != cudaSuccess)
-    return err;
-  return cudaMemcpyToSymbol(cTcRowExp, fd, sizeof(fd), sizeof(fd) * slot);
+  static TcMatrix M;
+  double Dt[81];
+  for (int pass = 0; pass < 2; pass++) {
+    if (pass == 1)
+      for (int i = 0; i < n; i++)
+        for (int j = 0; j < n; j++) Dt[i * n + j] = D[j * n + i];
+    tc_build(n, pass ? Dt : D, M);
+    cudaError_t err =
+        cudaMemcpyToSymbol(pass ? gTcBT : gTcB, M.F, sizeof(M.F), sizeof(M.F) * slot);
+    if (err != cudaSuccess) return err;
+    if ((err = cudaMemcpyToSymbol(pass ? gTcDT : gTcD, M.X, sizeof(M.X), sizeof(M.X) * slot)) !=
+        cudaSuccess)
+      return err;
+    if ((err = cudaMemcpyToSymbol(pass ? cTcRowExpT : cTcRowExp, M.fd, sizeof(M.fd),
+                                  sizeof(M.fd) * slot)) != cudaSuccess)
+      return err;
+  }
+  return cudaSuccess;
 }
 
 }  // namespace nmgk
