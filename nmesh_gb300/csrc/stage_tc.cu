@@ -59,6 +59,7 @@
 
 #include <cstdint>
 #include <cstring>
+#include <vector>
 
 #include "stage.cuh"
 
@@ -704,8 +705,8 @@ void tc_build(int n, const double *X, TcMatrix &out) {
   // B[K = 8 p + s][column], column = 8 nt + 2 t + j <-> slot 2 nt + j of quad
   // thread t: slots 0..6 groups of output t, 7..13 of output t+4, 14..15
   // groups 2t, 2t+1 of output 8
-  static uint16_t B[TKSMAX * 16][TNTILE * 8];
-  std::memset(B, 0, sizeof(B));
+  std::vector<uint16_t> Bv(TKSMAX * 16 * TNTILE * 8, 0);  // B[K][column], per call
+  auto B = reinterpret_cast<uint16_t(*)[TNTILE * 8]>(Bv.data());
   for (int col = 0; col < TNTILE * 8; col++) {
     const int nt = col / 8, c8 = col % 8, t = c8 / 2, j = c8 % 2, sl = 2 * nt + j;
     int i, w;
@@ -750,7 +751,8 @@ int tcvjp_variants(int n, Variant *out, int cap) {
 cudaError_t tc_upload(int n, const double *D) {
   if (n < 7 || n > 9) return cudaSuccess;
   const size_t slot = (size_t)(n - 7);
-  static TcMatrix M;
+  std::vector<TcMatrix> Mv(1);  // per call: contexts may be created from several threads
+  TcMatrix &M = Mv[0];
   double Dt[81];
   for (int pass = 0; pass < 2; pass++) {
     if (pass == 1)
