@@ -62,6 +62,7 @@
 #include <vector>
 
 #include "stage.cuh"
+#include "tc_build.h"
 
 namespace nmgk {
 namespace {
@@ -630,28 +631,6 @@ cudaError_t launch_tc(const StageParams &P, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-// 56-bit rounded fixed-point magnitude of x on the grid of exponent fd
-// (the top 7 bytes of (m << 11) >> (fd - e), rounded at the dropped byte)
-unsigned long long digits56(double x, int fd) {
-  uint64_t b;
-  std::memcpy(&b, &x, 8);
-  const int e = (int)(b >> 52) & 0x7FF;
-  if (!e) return 0;
-  const uint64_t m = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-  const int d = fd - e;
-  const uint64_t X = d < 64 ? (m << 11) >> d : 0;
-  return (X + 0x80) >> 8;
-}
-
-uint16_t half_of_int(int v) {  // exact for |v| < 2048
-  if (v == 0) return 0;
-  const uint16_t s = v < 0 ? 0x8000 : 0;
-  int a = v < 0 ? -v : v, ex = 0;
-  while ((a >> ex) > 1) ex++;
-  const int mant = (a << (10 - ex)) & 0x3FF;
-  return (uint16_t)(s | ((ex + 15) << 10) | mant);
-}
-
 }  // namespace
 
 int tc_variants(int n, Variant *out, int cap) {
@@ -672,74 +651,6 @@ int tc_variants(int n, Variant *out, int cap) {
   return k;
 }
 
-namespace {
-
-// B fragments, row exponents and the matrix itself of an n x n matrix X
-// (row-major, rows = outputs) for the tensor-core kernels
-struct TcMatrix {
-  uint4 F[TKSMAX][TNTILE / 2][32];
-  int fd[9];
-  double X[81];
-};
-
-void tc_build(int n, const double *X, TcMatrix &out) {
-  const int ks = (n + 1) / 2;
-  // per row: exponent and digits of |X_ip|
-  unsigned long long Y[9][9] = {};
-  int sg[9][9] = {};
-  std::memset(&out, 0, sizeof(out));
-  for (int i = 0; i < n; i++) {
-    int mx = 0;
-    for (int p = 0; p < n; p++) {
-      uint64_t b;
-      std::memcpy(&b, &X[i * n + p], 8);
-      mx = std::max(mx, (int)(b >> 52) & 0x7FF);
-    }
-    out.fd[i] = mx;
-    for (int p = 0; p < n; p++) {
-      Y[i][p] = digits56(X[i * n + p], mx);
-      sg[i][p] = X[i * n + p] < 0 ? -1 : 1;
-    }
-  }
-  for (int q = 0; q < n * n; q++) out.X[q] = X[q];
-  // B[K = 8 p + s][column], column = 8 nt + 2 t + j <-> slot 2 nt + j of quad
-  // thread t: slots 0..6 groups of output t, 7..13 of output t+4, 14..15
-  // groups 2t, 2t+1 of output 8
-  std::vector<uint16_t> Bv(TKSMAX * 16 * TNTILE * 8, 0);  // B[K][column], per call
-  auto B = reinterpret_cast<uint16_t(*)[TNTILE * 8]>(Bv.data());
-  for (int col = 0; col < TNTILE * 8; col++) {
-    const int nt = col / 8, c8 = col % 8, t = c8 / 2, j = c8 % 2, sl = 2 * nt + j;
-    int i, w;
-    if (sl < 7) { i = t; w = sl; }
-    else if (sl < 14) { i = t + 4; w = sl - 7; }
-    else { i = 8; w = 2 * t + (sl - 14); }
-    if (i >= n || w >= TG) continue;
-    for (int p = 0; p < n; p++)
-      for (int s = 0; s < TG; s++) {
-        const int tt = w - s;
-        if (tt < 0 || tt >= TG) continue;
-        const int dig = (int)((Y[i][p] >> (8 * (6 - tt))) & 0xFF);
-        B[8 * p + s][col] = half_of_int(sg[i][p] * dig);
-      }
-  }
-  for (int kk = 0; kk < ks; kk++)
-    for (int q = 0; q < TNTILE / 2; q++)
-      for (int lane = 0; lane < 32; lane++) {
-        const int g = lane >> 2, t = lane & 3;
-        uint32_t r[4];
-        for (int h = 0; h < 2; h++) {
-          const int col = 8 * (2 * q + h) + g;
-          const uint32_t b0 = B[16 * kk + 2 * t][col], b1 = B[16 * kk + 2 * t + 1][col];
-          const uint32_t b2 = B[16 * kk + 2 * t + 8][col], b3 = B[16 * kk + 2 * t + 9][col];
-          r[2 * h] = b0 | (b1 << 16);
-          r[2 * h + 1] = b2 | (b3 << 16);
-        }
-        out.F[kk][q][lane] = make_uint4(r[0], r[1], r[2], r[3]);
-      }
-}
-
-}  // namespace
-
 int tcvjp_variants(int n, Variant *out, int cap) {
   if (cap < 1) return 0;
   if (n == 9) { out[0] = Variant{"tcvjp", 1, 192, launch_tcvjp<9, 192, 3>}; return 1; }
@@ -748,17 +659,20 @@ int tcvjp_variants(int n, Variant *out, int cap) {
   return 0;
 }
 
+static_assert(sizeof(tc::Frag) == sizeof(uint4), "fragment layout");
+static_assert(sizeof(tc::TcMatrix::F) == sizeof(gTcB[0]), "fragment array of one order");
+
 cudaError_t tc_upload(int n, const double *D) {
   if (n < 7 || n > 9) return cudaSuccess;
   const size_t slot = (size_t)(n - 7);
-  std::vector<TcMatrix> Mv(1);  // per call: contexts may be created from several threads
-  TcMatrix &M = Mv[0];
+  std::vector<tc::TcMatrix> Mv(1);  // per call: contexts may be created from several threads
+  tc::TcMatrix &M = Mv[0];
   double Dt[81];
   for (int pass = 0; pass < 2; pass++) {
     if (pass == 1)
       for (int i = 0; i < n; i++)
         for (int j = 0; j < n; j++) Dt[i * n + j] = D[j * n + i];
-    tc_build(n, pass ? Dt : D, M);
+    tc::tc_build(n, pass ? Dt : D, M);
     cudaError_t err =
         cudaMemcpyToSymbol(pass ? gTcBT : gTcB, M.F, sizeof(M.F), sizeof(M.F) * slot);
     if (err != cudaSuccess) return err;

@@ -170,3 +170,83 @@ def test_zero_and_constant_lines(dmat):
     # the derivative of a constant is zero up to the rounding bound
     c = np.full(N, 3.0)
     assert np.abs(line_derivative(c, D, B, fd)).max() <= 2.0 * 2.0 ** -53 * 3 * np.abs(D).sum(1).max()
+
+
+HARNESS = r"""
+#include <cstdio>
+#include <cstring>
+#include "tc_build.h"
+int main() {
+  int n;
+  if (scanf("%d", &n) != 1) return 1;
+  double X[81];
+  for (int i = 0; i < n * n; i++) {
+    unsigned long long b;
+    if (scanf("%llx", &b) != 1) return 1;
+    std::memcpy(&X[i], &b, 8);
+  }
+  static nmgk::tc::TcMatrix M;
+  nmgk::tc::tc_build(n, X, M);
+  for (int i = 0; i < 9; i++) printf("%d\n", M.fd[i]);
+  for (int kk = 0; kk < nmgk::tc::kKStepsMax; kk++)
+    for (int q = 0; q < nmgk::tc::kNTiles / 2; q++)
+      for (int l = 0; l < 32; l++) {
+        const nmgk::tc::Frag &f = M.F[kk][q][l];
+        printf("%08x %08x %08x %08x\n", f.x, f.y, f.z, f.w);
+      }
+  return 0;
+}
+"""
+
+
+@pytest.fixture(scope="module")
+def harness(tmp_path_factory):
+    import os
+    import shutil
+    import subprocess
+    cxx = shutil.which("g++")
+    if not cxx:
+        pytest.skip("no C++ compiler")
+    csrc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                        "nmesh_gb300", "csrc")
+    d = tmp_path_factory.mktemp("tcb")
+    src, exe = d / "h.cpp", d / "h"
+    src.write_text(HARNESS)
+    subprocess.run([cxx, "-O1", "-std=c++17", "-I", csrc, str(src), "-o", str(exe)], check=True)
+    return str(exe)
+
+
+def test_host_builder_matches_restatement(harness, dmat):
+    """The library's host builder (nmesh_gb300/csrc/tc_build.h) gives, for D
+    and D^T, the row exponents and the B fragments of the digit matrix
+    restated here: FP16 bit patterns of the digits, laid out as
+    mma.m16n8k16 wants its B operand (lane (g, t) holds rows 2t, 2t+1 and
+    2t+8, 2t+9 of column g of each 16 x 8 block)."""
+    import subprocess
+    D = dmat[0]
+    N = D.shape[0]
+    for X in (D, np.ascontiguousarray(D.T)):
+        B, fd = b_matrix(X)
+        inp = f"{N}\n" + " ".join(f"{_bits(v):016x}" for v in X.ravel()) + "\n"
+        out = subprocess.run([harness], input=inp, capture_output=True, text=True,
+                             check=True).stdout.split("\n")
+        assert [int(v) for v in out[:N]] == fd
+        frags = [[int(w, 16) for w in line.split()] for line in out[9:] if line.strip()]
+        h = np.zeros((80, 64), dtype=np.uint16)
+        h[:B.shape[0]] = B.astype(np.float16).view(np.uint16)
+        ks = (N + 1) // 2
+        for kk in range(5):
+            for q in range(4):
+                for lane in range(32):
+                    g, t = lane >> 2, lane & 3
+                    want = []
+                    for half in range(2):
+                        col = 8 * (2 * q + half) + g
+                        if kk < ks:
+                            rows = [16 * kk + 2 * t, 16 * kk + 2 * t + 1,
+                                    16 * kk + 2 * t + 8, 16 * kk + 2 * t + 9]
+                            b = [int(h[r, col]) for r in rows]
+                        else:
+                            b = [0, 0, 0, 0]
+                        want += [b[0] | (b[1] << 16), b[2] | (b[3] << 16)]
+                    assert frags[(kk * 4 + q) * 32 + lane] == want, (kk, q, lane)
