@@ -68,7 +68,6 @@ namespace nmgk {
 namespace {
 
 constexpr int TNTILE = 8;        // n-tiles of 8 columns (9 outputs x 7 groups <= 64)
-constexpr int TG = 7;            // digit groups kept
 constexpr int TKSMAX = 5;        // k-steps of 16 at n = 9: 10 points x 8 digit slots
 constexpr unsigned kMagic = 0x4B400000u;  // bit pattern of 1.5 * 2^23
 
@@ -350,9 +349,10 @@ __global__ void __launch_bounds__(NT, MINB) tc_kernel(StageParams P) {
     const int q = tid + k * NT;
     if (q < 4 * TNP) sDig[q] = tc_digits(v[k], sEmax[q / TNP]);
   }
-  __syncthreads();
-
   const double t = stage_time(P);
+  // face terms first: their loads overlap the digit stores; face_terms ends with a barrier
+  face_terms<N, 1, NT>(P, Wg, sR, sCs, sG, e0, t);
+
   const int warp = tid >> 5, lane = tid & 31, g = lane >> 2, tq = lane & 3;
   const int cs = sCs[0], mask = sMask;
   const uint32_t digbase = (uint32_t)__cvta_generic_to_shared(sDig);
@@ -449,7 +449,6 @@ __global__ void __launch_bounds__(NT, MINB) tc_kernel(StageParams P) {
     __syncthreads();
   }
   // interior states of the faces and r_phi = pi come from w in global memory
-  face_terms<TN, 1, NT>(P, Wg, sR, sCs, sG, e0, t);
   tc_epilogue<N, NT>(P, Wg, sR, e);
 }
 
@@ -463,7 +462,6 @@ __global__ void __launch_bounds__(NT, MINB) tcvjp_kernel(StageParams P) {
   using S = TcShape<N>;
   constexpr int TN = N, TNP = S::NP, TNN = S::NN, TTILES = S::TILES;
   constexpr int NWARP = NT / 32;
-  constexpr int NLOAD = (4 * TNP + NT - 1) / NT;
   extern __shared__ __align__(16) unsigned char tsm[];
   double *sR = reinterpret_cast<double *>(tsm);           // [4][NP]: pibar, cbar
   uint4 *sDig = reinterpret_cast<uint4 *>(sR + 4 * TNP);  // [4][NP] digits of y
