@@ -141,8 +141,13 @@ def fp64_work_per_stage(variant, nelem, ncurvi, n, nnz_curvi=7):
         # derivatives on the tensor cores; FP64: the chain rule (one FMA per
         # nonzero metric entry and derivative), one int64 -> FP64 conversion
         # per derivative output (counted as an instruction, no flop)
-        vol_i = ncart * np_ * (6 + 6) + ncurvi * np_ * (2 * nnz_curvi + 3 + nnz_curvi)
-        vol_f = ncart * np_ * 12 + ncurvi * np_ * 4 * nnz_curvi
+        # plus the line left over in each pass at odd n (n^2 = 16 k + 1): an
+        # FP64 dot product per output
+        left = n * n if (n * n) % 16 == 1 else 0
+        fields = ncart * 6 + ncurvi * (3 + nnz_curvi)
+        vol_i = ncart * np_ * (6 + 6) + ncurvi * np_ * (2 * nnz_curvi + 3 + nnz_curvi) + \
+            fields * left
+        vol_f = ncart * np_ * 12 + ncurvi * np_ * 4 * nnz_curvi + fields * left * 2
     elif variant.startswith("eo"):
         M, odd = n // 2, n % 2
         # per line: e/o adds, S and T sums (first term a multiply), outputs
@@ -164,10 +169,11 @@ def fp64_work_per_stage(variant, nelem, ncurvi, n, nnz_curvi=7):
 
 def tc_mma_per_stage(nelem, ncurvi, nnz_curvi=7):
     """mma.m16n8k16 (FP16 in, FP32 accumulate) of the tensor-core variant per
-    stage: per element and pass one field per nonzero chain-rule row entry
-    plus pi, 6 tiles of 16 lines, 5 k-steps x 8 n-tiles."""
+    stage at n = 9: per element and pass one field per nonzero chain-rule row
+    entry plus pi, 5 tiles of 16 lines (the 81st line is FP64), 5 k-steps x
+    8 n-tiles."""
     fields = (nelem - ncurvi) * 6 + ncurvi * (3 + nnz_curvi)
-    return fields * 6 * 40
+    return fields * 5 * 40
 
 
 def fp64_variant_line(kinfo, nelem, ncurvi, n, fp64_peak):
