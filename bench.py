@@ -772,7 +772,7 @@ def grhd_initial_prim(xyz, seed, rho0=1e-3, center=(8.0, 0.0, 0.0), width=2.0):
     return prim
 
 
-def grhd_flops_per_stage(ndg, nfv, n, nf, c2p_iterations_per_stage):
+def grhd_flops_per_stage(ndg, nfv, n, nf, c2p_iterations_per_stage, dg_tensor=False):
     """Model of the FP64 work of one GRHD stage (add, mul, FMA, division and
     square root counted as one flop each, FMA as two), from the kernels'
     source: per DG node 3 directional fluxes (45), Cowling sources (35),
@@ -783,9 +783,15 @@ def grhd_flops_per_stage(ndg, nfv, n, nf, c2p_iterations_per_stage):
     WENO5 smoothness indicators (450), per midpoint two prim2con (50) and
     the LLF (95), the divergence (60 for all three directions) and the
     update (20); con2prim 40 per point plus 30 per root-finder iteration
-    (counted on the device)."""
+    (counted on the device).  With dg_tensor (the tensor-core DG kernel at
+    n = 7, 8, 9) the line derivatives are integer digit products on the
+    tensor cores, and only the line left over per direction at odd n
+    (one of n^2) is FP64 work."""
     npd, npf = n ** 3, nf ** 3
-    dg = ndg * (npd * (45 + 35 + 90 * n + 90 + 20) + 6 * n * n * 170)
+    deriv = 90 * n
+    if dg_tensor:
+        deriv = 90 * n / (n * n) if (n * n) % 16 == 1 else 0
+    dg = ndg * (npd * (45 + 35 + deriv + 90 + 20) + 6 * n * n * 170)
     fv = nfv * npf * (35 + 3 * 595 + 60 + 20)
     c2p = (ndg * npd + nfv * npf) * 40 + 30 * c2p_iterations_per_stage
     return dg + fv + c2p
@@ -834,7 +840,8 @@ def grhd_bench(args):
     u_dg, u_fv, p_dg, _ = ev.get_state()
     finite = bool(np.isfinite(u_dg).all() and np.isfinite(u_fv).all())
     ev.close()
-    flops = grhd_flops_per_stage(ndg, nfv, n, nf, iters / (4.0 * K))
+    dg_tensor = 7 <= n <= 9 and os.environ.get("NMG_GRHD_DG") != "fp64"
+    flops = grhd_flops_per_stage(ndg, nfv, n, nf, iters / (4.0 * K), dg_tensor)
     peak = ng.fp64_peak_gflops()
     achieved = flops / (ms / 1e3 / (4 * K)) / 1e9
     out = {"workload": f"GRHD Cowling, isotropic Schwarzschild M=1, Gamma=2, cubed shell "
@@ -847,6 +854,7 @@ def grhd_bench(args):
            "con2prim_iterations_per_point": iters / (4.0 * K) / (ndg * n ** 3 + nfv * nf ** 3),
            "atmosphere_points_per_stage": natm / (4.0 * K),
            "kernel_ms_per_step": shares,
+           "dg_kernel": "tensor-core line derivatives" if dg_tensor else "FP64",
            "con2prim_share": shares["con2prim"] / tot if tot > 0 else None,
            "roofline_fp64": {"bound": "fp64", "achieved": achieved, "peak": peak,
                              "unit": "GFLOP/s", "frac": achieved / peak,

@@ -335,7 +335,10 @@ int nmg_grhd_sources(const nmg_grhd_params *g, int64_t npts, const double *alpha
  * Every stage runs con2prim (newton1d_brak, atmosphere floors) on its input.
  * Outer faces (r_in, r_out) copy the interior state.  Host layouts: DG
  * [nelem][5][n^3], finite volume [nfv][5][nf^3] for the finite-volume
- * elements in ascending order. */
+ * elements in ascending order.  At n = 7, 8, 9 the DG elements' line
+ * derivatives run on the tensor cores (exact digit products); the
+ * environment variable NMG_GRHD_DG=fp64, read at creation, keeps them in
+ * FP64. */
 typedef struct nmg_grhd_evolve_params {
   nmg_grhd_params eos;
   double mass;   /* background mass M (>= 0) */

@@ -16,7 +16,7 @@ SOURCES = ["nmg.cu", "stage_eo.cu", "stage_tc.cu", "stage_gather.cu", "stage_fv.
 # per-file extra flags: the finite-volume kernel rounds every product and sum
 # separately, in the reference's order (no FMA contraction)
 EXTRA_FLAGS = {"stage_fv.cu": ["-fmad=false"], "grhd.cu": ["-fmad=false"]}
-HEADERS = ["mesh.h", "stage.cuh", "ctx.h", "weno.cuh", "grhd.cuh", "tc_build.h",os.path.join("..", "..", "include", "nmg.h")]
+HEADERS = ["mesh.h", "stage.cuh", "ctx.h", "weno.cuh", "grhd.cuh", "tc_build.h", "tc_device.cuh",os.path.join("..", "..", "include", "nmg.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
                      "-Xcompiler", "-fPIC,-ffp-contract=off", "-Xptxas", "-v"]

@@ -27,6 +27,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <string>
@@ -34,6 +35,7 @@
 
 #include "../../include/nmg.h"
 #include "mesh.h"
+#include "tc_device.cuh"
 
 namespace {
 
@@ -418,6 +420,44 @@ __device__ bool exterior(const GrP &P, int e, int f, int a, int b, double ps, do
   return true;
 }
 
+// DG faces (LLF with the fluid's characteristic speeds, lifted with
+// |grad X^d| (2/dX^d) / w_end), one direction at a time (its two faces are
+// disjoint), then the stage update of the element's r (shared by the DG
+// kernels)
+__device__ __forceinline__ void dg_faces_epilogue(const GrP &P, int e, const double *sP,
+                                                  double *sR, const double *Ug,
+                                                  const double *M, const double *bg,
+                                                  const double *s, double w_end) {
+  const int n = P.n, np = P.np, nn = P.nn;
+  // faces, one direction at a time (its two faces are disjoint)
+  for (int d = 0; d < 3; d++) {
+    for (int task = threadIdx.x; task < 2 * nn; task += blockDim.x) {
+      const int side = task / nn, ab = task - side * nn, a = ab % n, b = ab / n;
+      const int f = 2 * d + side, q2 = face_ijk(n, f, a, b);
+      const double al = bg[q2], ps = bg[np + q2];
+      double Ui[NF], Pi[NF], Uo[NF], Po[NF], Fs[NF], Fi[NF], nr[3];
+      if (!exterior(P, e, f, a, b, ps, Uo, Po)) continue;
+      for (int q = 0; q < NF; q++) {
+        Ui[q] = Ug[q * np + q2];
+        Pi[q] = sP[q * np + q2];
+      }
+      const double m0 = M[(d * 3 + 0) * np + q2], m1 = M[(d * 3 + 1) * np + q2],
+                   m2 = M[(d * 3 + 2) * np + q2];
+      const double nm = sqrt(m0 * m0 + m1 * m1 + m2 * m2);
+      const double sg = side ? 1. : -1.;
+      nr[0] = sg * m0 / nm;
+      nr[1] = sg * m1 / nm;
+      nr[2] = sg * m2 / nm;
+      const double g = nm * s[d] / w_end;
+      llf(P.g, Ui, Pi, Uo, Po, nr, al, ps, Fs, Fi);
+      for (int q = 0; q < NF; q++) sR[q * np + q2] -= g * (Fs[q] - Fi[q]);
+    }
+    __syncthreads();
+  }
+  for (int i = threadIdx.x; i < NF * np; i += blockDim.x)
+    epilogue(P, sR[i], (size_t)e * NF * np + i, P.u0_d, P.acc_d, P.wout_d);
+}
+
 // DG elements: one CTA per element
 __global__ void __launch_bounds__(kNT) dg_kernel(GrP P) {
   extern __shared__ double sm[];
@@ -468,33 +508,125 @@ __global__ void __launch_bounds__(kNT) dg_kernel(GrP P) {
     sR[f * np + q] -= div;
   }
   __syncthreads();
-  // faces, one direction at a time (its two faces are disjoint)
-  for (int d = 0; d < 3; d++) {
-    for (int task = threadIdx.x; task < 2 * nn; task += blockDim.x) {
-      const int side = task / nn, ab = task - side * nn, a = ab % n, b = ab / n;
-      const int f = 2 * d + side, q2 = face_ijk(n, f, a, b);
-      const double al = bg[q2], ps = bg[np + q2];
-      double Ui[NF], Pi[NF], Uo[NF], Po[NF], Fs[NF], Fi[NF], nr[3];
-      if (!exterior(P, e, f, a, b, ps, Uo, Po)) continue;
-      for (int q = 0; q < NF; q++) {
-        Ui[q] = Ug[q * np + q2];
-        Pi[q] = sP[q * np + q2];
+  dg_faces_epilogue(P, e, sP, sR, Ug, M, bg, s, w_end);
+}
+
+// DG elements with the divergence's line derivatives on the tensor cores
+// (n = 7, 8, 9; the exact integer digit products of stage_tc.cu): the fluxes
+// F^i along x^i are formed one i at a time for the five fields, split into
+// digits, and D applied along every direction a by 16-line MMA tiles (the
+// line left over at odd n in FP64); the chain rule M[a][i] (2/dX^a) D_a F^i,
+// the sources, the faces and the update are dg_kernel's FP64 code.
+constexpr int kNTD = 160;  // five warps: the 5 fields x 3 tiles of a pass at n = 7
+template <int N>
+constexpr size_t dg_tc_smem() {
+  return sizeof(double) * 3 * NF * N * N * N + sizeof(uint4) * NF * N * N * N;
+}
+
+template <int N>
+__global__ void __launch_bounds__(kNTD, 3) dg_tc_kernel(GrP P) {
+  using S = nmgk::TcShape<N>;
+  constexpr int np = S::NP, nn = S::NN, TILES = S::TILES, NWARP = kNTD / 32;
+  extern __shared__ __align__(16) unsigned char gsm[];
+  // the digits first: ldmatrix rows and uint4 stores want 16-byte addresses,
+  // and 15 np doubles are not a multiple of 16 bytes at odd np
+  uint4 *sDig = reinterpret_cast<uint4 *>(gsm);                 // [5][np] digits of sF
+  double *sP = reinterpret_cast<double *>(sDig + NF * np);      // [5][np] primitives
+  double *sR = sP + NF * np;                                    // [5][np] r
+  double *sF = sR + NF * np;                                    // [5][np] fluxes along x^i
+  __shared__ int sEmax[3][NF];
+  const int e = P.dglist[blockIdx.x];
+  const double *Pg = P.prim_d + (size_t)e * NF * np, *Ug = P.win_d + (size_t)e * NF * np;
+  const double *M = P.dXdx + (size_t)e * 9 * np, *bg = P.bgd + (size_t)e * 8 * np;
+  const double *bb = P.bbox + 6 * (size_t)e;
+  const double s[3] = {2. / (bb[1] - bb[0]), 2. / (bb[3] - bb[2]), 2. / (bb[5] - bb[4])};
+  const double w_end = P.basis[N * N];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, tq = lane & 3;
+  if (tid < 3 * NF) sEmax[tid / NF][tid % NF] = 0;
+  for (int i = tid; i < NF * np; i += kNTD) sP[i] = Pg[i];
+  __syncthreads();
+  for (int q = tid; q < np; q += kNTD) {
+    double Pq[NF], Fq[NF];
+    for (int f = 0; f < NF; f++) Pq[f] = sP[f * np + q];
+    sources(P.g, Pq, bg + q, np, Fq);
+    for (int f = 0; f < NF; f++) sR[f * np + q] = Fq[f];
+  }
+  const uint32_t digbase = (uint32_t)__cvta_generic_to_shared(sDig);
+  const int fd0 = nmgk::cTcRowExp[N - 7][tq], fd1 = nmgk::cTcRowExp[N - 7][min(tq + 4, 8)];
+  const int fd8 = nmgk::cTcRowExp[N - 7][8];
+  const uint4 *gB = &nmgk::gTcB[N - 7][0][0][0];
+  const double *gD = nmgk::gTcD[N - 7];
+#pragma unroll 1
+  for (int i = 0; i < 3; i++) {
+    {
+      // the fluxes along x^i and each field's largest exponent
+      int em[NF] = {0, 0, 0, 0, 0};
+      for (int q = tid; q < np; q += kNTD) {
+        double Uq[NF], Pq[NF], Fq[NF], nr[3] = {0., 0., 0.};
+        nr[i] = 1.;
+        for (int f = 0; f < NF; f++) {
+          Uq[f] = Ug[f * np + q];
+          Pq[f] = sP[f * np + q];
+        }
+        flux_n(Uq, Pq, nr, bg[q], bg[np + q], Fq);
+        for (int f = 0; f < NF; f++) {
+          sF[f * np + q] = Fq[f];
+          em[f] = max(em[f], (int)((unsigned long long)__double_as_longlong(Fq[f]) >> 52) & 0x7FF);
+        }
       }
-      const double m0 = M[(d * 3 + 0) * np + q2], m1 = M[(d * 3 + 1) * np + q2],
-                   m2 = M[(d * 3 + 2) * np + q2];
-      const double nm = sqrt(m0 * m0 + m1 * m1 + m2 * m2);
-      const double sg = side ? 1. : -1.;
-      nr[0] = sg * m0 / nm;
-      nr[1] = sg * m1 / nm;
-      nr[2] = sg * m2 / nm;
-      const double g = nm * s[d] / w_end;
-      llf(P.g, Ui, Pi, Uo, Po, nr, al, ps, Fs, Fi);
-      for (int q = 0; q < NF; q++) sR[q * np + q2] -= g * (Fs[q] - Fi[q]);
+#pragma unroll
+      for (int f = 0; f < NF; f++) {
+        const unsigned m = __reduce_max_sync(0xffffffffu, (unsigned)em[f]);
+        if (lane == 0) atomicMax(&sEmax[i][f], (int)m);
+      }
     }
     __syncthreads();
+    for (int q = tid; q < NF * np; q += kNTD) sDig[q] = nmgk::tc_digits(sF[q], sEmax[i][q / np]);
+    __syncthreads();
+#pragma unroll 1
+    for (int a = 0; a < 3; a++) {
+      const double sa = s[a];
+      const double *Mai = M + (a * 3 + i) * np;
+#pragma unroll 1
+      for (int task = warp; task < NF * TILES; task += NWARP) {
+        const int f = task / TILES, tile = task - f * TILES;
+        const int Lr = min(tile * 16 + (lane & 15), nn - 1), chunk = lane >> 4;
+        const int ps = a == 0 ? 1 : (a == 1 ? N : nn);
+        const int nb = a == 0 ? N * Lr : (a == 1 ? (Lr % N) + nn * (Lr / N) : Lr);
+        // owned output slots as in stage_tc.cu's kernel, and M[a][i] (2/dX^a) there
+        int nodeS[5];
+        bool okS[5];
+        double mS[5];
+#pragma unroll
+        for (int sl = 0; sl < 5; sl++) {
+          const int L = tile * 16 + g + (sl < 4 ? (sl >> 1) * 8 : tq * 8);
+          const int io = sl < 4 ? tq + (sl & 1) * 4 : N - 1;
+          okS[sl] = L < nn && io < N && (sl < 4 ? true : (N == 9 && tq < 2));
+          nodeS[sl] = okS[sl] ? nmgk::tc_node<N>(a, L, io) : 0;
+          mS[sl] = okS[sl] ? Mai[nodeS[sl]] * sa : 0.;
+        }
+        double dv[5];
+        nmgk::tc_derivs<N>(gB, digbase + (uint32_t)(f * np + nb) * 16u, (uint32_t)ps * 16u,
+                           chunk, lane, tq, sEmax[i][f], fd0, fd1, fd8, dv);
+#pragma unroll
+        for (int sl = 0; sl < 5; sl++)
+          if (okS[sl]) sR[f * np + nodeS[sl]] -= mS[sl] * dv[sl];
+      }
+      if (S::LAST) {
+        // the line left over (l0 = l1 = n - 1) in FP64
+        for (int t = tid; t < NF * N; t += kNTD) {
+          const int f = t / N, io = t - f * N, L = nn - 1;
+          double d = 0.;
+          for (int p = 0; p < N; p++)
+            d = fma(__ldg(gD + io * N + p), sF[f * np + nmgk::tc_node<N>(a, L, p)], d);
+          const int node = nmgk::tc_node<N>(a, L, io);
+          sR[f * np + node] -= Mai[node] * sa * d;
+        }
+      }
+      __syncthreads();
+    }
   }
-  for (int i = threadIdx.x; i < NF * np; i += blockDim.x)
-    epilogue(P, sR[i], (size_t)e * NF * np + i, P.u0_d, P.acc_d, P.wout_d);
+  dg_faces_epilogue(P, e, sP, sR, Ug, M, bg, s, w_end);
 }
 
 // finite-volume elements: one CTA per slot.  Per direction and chunk of
@@ -843,6 +975,7 @@ struct nmg_grhd_ctx {
   int64_t launches = 0, graph_launches = 0;
   size_t smem_dg = 0, smem_fv = 0;
   int pencils = 0;
+  bool dg_tc = false;  // DG divergence on the tensor cores (n = 7, 8, 9)
 };
 
 namespace {
@@ -1009,7 +1142,14 @@ int enqueue_stage(nmg_grhd_ctx *c, GrP P, double *win_d, double *win_f,
   mark(3);
   mark(4);
   if (c->ndg > 0) {
-    dg_kernel<<<c->ndg, kNT, c->smem_dg, c->stream>>>(P);
+    if (!c->dg_tc)
+      dg_kernel<<<c->ndg, kNT, c->smem_dg, c->stream>>>(P);
+    else if (c->n == 7)
+      dg_tc_kernel<7><<<c->ndg, kNTD, dg_tc_smem<7>(), c->stream>>>(P);
+    else if (c->n == 8)
+      dg_tc_kernel<8><<<c->ndg, kNTD, dg_tc_smem<8>(), c->stream>>>(P);
+    else
+      dg_tc_kernel<9><<<c->ndg, kNTD, dg_tc_smem<9>(), c->stream>>>(P);
     GCK(cudaGetLastError());
     c->launches++;
   }
@@ -1153,6 +1293,23 @@ int nmg_grhd_create(const nmg_mesh *m, const nmg_grhd_evolve_params *p, nmg_grhd
                            (int)c->smem_dg));
   GCK(cudaFuncSetAttribute(fv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)c->smem_fv));
+  // the tensor-core DG kernel at n = 7, 8, 9 (NMG_GRHD_DG=fp64 keeps the FP64 one)
+  {
+    const char *ev = std::getenv("NMG_GRHD_DG");
+    c->dg_tc = c->n >= 7 && c->n <= 9 && !(ev && std::strcmp(ev, "fp64") == 0);
+  }
+  if (c->dg_tc) {
+    GCK(nmgk::tc_upload_tables(c->n, m->D.data(), false));
+    if (c->n == 7)
+      GCK(cudaFuncSetAttribute(dg_tc_kernel<7>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)dg_tc_smem<7>()));
+    else if (c->n == 8)
+      GCK(cudaFuncSetAttribute(dg_tc_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)dg_tc_smem<8>()));
+    else
+      GCK(cudaFuncSetAttribute(dg_tc_kernel<9>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)dg_tc_smem<9>()));
+  }
   // mesh tables
   const int64_t E = c->E;
   c->h_nb.assign(m->nb.begin(), m->nb.end());

@@ -53,7 +53,7 @@ def _compare(fv, got_dg, got_fv, want_dg, want_fv, tol):
 
 
 @pytest.mark.parametrize("n,nf,rec", [(5, 9, "WENOm5_2"), (5, 10, "WENOm3_2"), (7, 13, "WENOm5_2"),
-                                      (4, 8, "WENOmZ_2")])
+                                      (4, 8, "WENOmZ_2"), (8, 15, "WENOm5_2"), (9, 15, "WENOm5_2")])
 def test_rhs_matches_oracle(n, nf, rec):
     o, ev, fv, (ud, uf, pd, pf) = _case(n, nf, 2, [1, 3, 10, 11, 20, 33, 47], rec=rec)
     u_dg, u_fv, _, _ = ev.get_state()
@@ -61,6 +61,35 @@ def test_rhs_matches_oracle(n, nf, rec):
     r_dg, r_fv = ev.rhs()
     want_dg, want_fv = o.rhs(ud, uf, pd, pf)
     _compare(fv, r_dg, r_fv, want_dg, want_fv, RTOL)
+
+
+@pytest.mark.parametrize("n,nf", [(7, 13), (8, 15), (9, 15)])
+def test_tensor_core_dg_kernel_matches_the_fp64_one(n, nf, monkeypatch):
+    """At n = 7, 8, 9 the DG elements' divergence runs on the tensor cores
+    (exact digit products, one FP64 rounding per line derivative); the FP64
+    kernel (NMG_GRHD_DG=fp64) gives the same right-hand side and RK4 step
+    within the oracle tolerance, and a blob moving across both kinds of
+    element."""
+    res = []
+    for mode in ("fp64", None):
+        if mode:
+            monkeypatch.setenv("NMG_GRHD_DG", mode)
+        else:
+            monkeypatch.delenv("NMG_GRHD_DG", raising=False)
+        o, ev, fv, _ = _case(n, nf, 2, [2, 5, 17, 30], vel=(0.04, 0.02, -0.03))
+        r = ev.rhs()
+        ev.rk4_steps(0.01, 2)
+        res.append((fv, r, ev.get_state()))
+        ev.close()
+    (fv, ra, sa), (_, rb, sb) = res
+
+    def full(compact):  # finite-volume rows back at their elements' places
+        out = np.zeros((fv.size,) + compact.shape[1:])
+        out[fv == 1] = compact
+        return out
+
+    _compare(fv, rb[0], rb[1], ra[0], full(ra[1]), RTOL)
+    _compare(fv, sb[0], sb[1], sa[0], full(sa[1]), RTOL)
 
 
 @pytest.mark.parametrize("mass", [1.0, 0.0])
