@@ -250,3 +250,47 @@ def test_host_builder_matches_restatement(harness, dmat):
                             b = [0, 0, 0, 0]
                         want += [b[0] | (b[1] << 16), b[2] | (b[3] << 16)]
                     assert frags[(kk * 4 + q) * 32 + lane] == want, (kk, q, lane)
+
+
+def _tc_node(N, a, L, p):
+    """node of point p on line L along direction a (tc_node in tc_device.cuh)"""
+    nn = N * N
+    return p + N * L if a == 0 else ((L % N) + N * p + nn * (L // N) if a == 1 else L + nn * p)
+
+
+@pytest.mark.parametrize("N", ORDERS)
+def test_tile_slots_cover_every_node_once_and_rows_stay_aligned(N):
+    """The work split of the tensor-core kernels (stage_tc.cu, and the GRHD
+    DG kernel in grhd_evolve.cu), restated: per direction a, 16-line tiles
+    whose lanes own outputs (g, t), (g, t+4), (g+8, t), (g+8, t+4) and, at
+    n = 9, output 8 of row g or g+8, plus the line left over at odd n in
+    FP64, write every node exactly once; and every ldmatrix row (16 bytes of
+    digits, points clamped to n - 1) of the GRHD kernel's shared layout
+    (digits of 5 fields first, then 15 n^3 doubles) lies inside the digit
+    array on a 16-byte boundary."""
+    NP, nn = N ** 3, N * N
+    tiles, last = nn // 16, nn % 16 == 1
+    ks = (N + 1) // 2
+    for a in range(3):
+        seen = np.zeros(NP, np.int64)
+        for tile in range(tiles):
+            for lane in range(32):
+                g, tq = lane >> 2, lane & 3
+                for sl in range(5):
+                    L = tile * 16 + g + ((sl >> 1) * 8 if sl < 4 else tq * 8)
+                    io = tq + (sl & 1) * 4 if sl < 4 else N - 1
+                    ok = L < nn and io < N and (sl < 4 or (N == 9 and tq < 2))
+                    if ok:
+                        seen[_tc_node(N, a, L, io)] += 1
+                # ldmatrix rows of this lane in the GRHD layout, field 4
+                Lr, chunk = min(tile * 16 + (lane & 15), nn - 1), lane >> 4
+                ps = 1 if a == 0 else (N if a == 1 else nn)
+                nb = _tc_node(N, a, Lr, 0)
+                for kk in range(ks):
+                    p = min(2 * kk + chunk, N - 1)
+                    addr = (4 * NP + nb + p * ps) * 16
+                    assert addr % 16 == 0 and addr + 16 <= 5 * NP * 16
+        if last:
+            for io in range(N):
+                seen[_tc_node(N, a, nn - 1, io)] += 1
+        assert (seen == 1).all(), (a, np.nonzero(seen != 1)[0][:8])
